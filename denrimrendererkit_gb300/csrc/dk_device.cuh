@@ -1,0 +1,217 @@
+// Device-side scene model, BVH traversal and shading of the sm_103a wavefront
+// path tracer.  Each function restates the named function of the reference
+// shader (Sources/DenrimRendererKit/Resources/Shaders/PathTrace.metal); the
+// kernels in dk_kernels.cu split the reference's per-pixel loop
+// (pathTraceKernel, PathTrace.metal:5167-5586) into extend / shade / shadow
+// stages over SoA path queues.
+#pragma once
+#include <cstdint>
+
+#include "../../include/denrim_cuda.h"
+#include "dk_kernels.h"
+#include "dk_math.cuh"
+
+namespace dk {
+
+// ------------------------------------------------------------- scene ------
+// Leaf children are encoded as 0x80000000 | first << 3 | (count - 1).
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kStackSize = 64;
+constexpr uint32_t kNoHit = 0xffffffffu;
+
+struct Ray { float3 origin, direction; };
+
+// Hit (PathTrace.metal:229-253) for triangle hits.
+struct Hit {
+    float t;
+    float3 position;
+    float3 normal;
+    float2 uv;
+    float3 tangent;
+    float3 bitangent;
+    uint32_t materialID;
+    uint32_t objectID;
+    uint32_t primitiveID;
+    bool frontFacing;
+};
+
+struct HitRec { float t; uint32_t tri; float u, v; };
+
+// ------------------------------------------------------- traversal --------
+// intersectBounds (PathTrace.metal:1854-1863) on one child box, exact ops.
+__device__ __forceinline__ bool childBox(float bx0, float bx1, float by0, float by1, float bz0, float bz1,
+                                         float3 o, float3 inv, float closestT, float& tNear) {
+    float tx0 = ex::mul(ex::sub(bx0, o.x), inv.x), tx1 = ex::mul(ex::sub(bx1, o.x), inv.x);
+    float ty0 = ex::mul(ex::sub(by0, o.y), inv.y), ty1 = ex::mul(ex::sub(by1, o.y), inv.y);
+    float tz0 = ex::mul(ex::sub(bz0, o.z), inv.z), tz1 = ex::mul(ex::sub(bz1, o.z), inv.z);
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), closestT));
+    tNear = tn;
+    return tn <= tf;
+}
+
+// Möller-Trumbore as intersectTriangle (PathTrace.metal:1801-1852), exact ops.
+__device__ __forceinline__ bool mtTest(float3 o, float3 d, float3 v0, float3 e1, float3 e2, float& t, float& u,
+                                       float& v) {
+    float3 p = ex::cross(d, e2);
+    float det = ex::dot(e1, p);
+    if (fabsf(det) < 1e-7f) return false;
+    float inv = ex::rcp(det);
+    float3 s = ex::sub(o, v0);
+    u = ex::mul(inv, ex::dot(s, p));
+    if (u < 0.0f || u > 1.0f) return false;
+    float3 q = ex::cross(s, e1);
+    v = ex::mul(inv, ex::dot(d, q));
+    if (v < 0.0f || ex::add(u, v) > 1.0f) return false;
+    t = ex::mul(inv, ex::dot(e2, q));
+    return t > 0.0005f;
+}
+
+__device__ __forceinline__ float3 rcp3(float3 d) { return f3(ex::rcp(d.x), ex::rcp(d.y), ex::rcp(d.z)); }
+
+// Closest hit.  Returns argmin over (t, reference leaf slot): the reference's
+// strict `t < closest.t` under left-first DFS picks, among equal t, the
+// triangle that comes first in its primitiveIndices order, which is the slot.
+__device__ HitRec traceClosest(const DevScene& S, float3 o, float3 d) {
+    HitRec best;
+    best.t = INFINITY;
+    best.tri = kNoHit;
+    best.u = 0.0f;
+    best.v = 0.0f;
+    uint32_t bestSlot = 0xffffffffu;
+    if (S.node_count == 0) return best;
+    float3 inv = rcp3(d);
+    int stackNode[kStackSize];
+    float stackT[kStackSize];
+    int sp = 0;
+    uint32_t node = 0;
+    for (;;) {
+        if ((node & kLeafBit) == 0) {
+            const float4* n = S.nodes + 4 * (size_t)node;
+            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
+            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
+            float tl, tr;
+            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, o, inv, best.t, tl);
+            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, o, inv, best.t, tr);
+            if (hl && hr) {
+                bool rFirst = tr < tl;
+                uint32_t nearC = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+                uint32_t farC = rFirst ? (uint32_t)ch.x : (uint32_t)ch.y;
+                if (sp < kStackSize) {
+                    stackNode[sp] = (int)farC;
+                    stackT[sp] = rFirst ? tl : tr;
+                    ++sp;
+                }
+                node = nearC;
+                continue;
+            }
+            if (hl) { node = (uint32_t)ch.x; continue; }
+            if (hr) { node = (uint32_t)ch.y; continue; }
+        } else {
+            uint32_t first = (node & ~kLeafBit) >> 3;
+            uint32_t cnt = (node & 7u) + 1u;
+            for (uint32_t i = first; i < first + cnt; ++i) {
+                const float4* q = S.isect + 3 * (size_t)i;
+                float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+                float t, u, v;
+                if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v)) {
+                    uint32_t slot = __float_as_uint(a.w);
+                    if (t < best.t || (t == best.t && slot < bestSlot)) {
+                        best.t = t;
+                        best.u = u;
+                        best.v = v;
+                        best.tri = __float_as_uint(b.w);
+                        bestSlot = slot;
+                    }
+                }
+            }
+        }
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stackT[sp] <= best.t) {
+                node = (uint32_t)stackNode[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return best;
+}
+
+// Any-hit over shadow-opaque triangles with 0.0005 < t < tmax.  Sets
+// `sawNonOpaque` when a cut-out or transmissive triangle lies in range.
+__device__ bool traceAnyOpaque(const DevScene& S, float3 o, float3 d, float tmax, bool& sawNonOpaque) {
+    if (S.node_count == 0) return false;
+    float3 inv = rcp3(d);
+    int stackNode[kStackSize];
+    int sp = 0;
+    uint32_t node = 0;
+    for (;;) {
+        if ((node & kLeafBit) == 0) {
+            const float4* n = S.nodes + 4 * (size_t)node;
+            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
+            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
+            float tl, tr;
+            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, o, inv, tmax, tl);
+            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, o, inv, tmax, tr);
+            if (hl && hr) {
+                bool rFirst = tr < tl;
+                if (sp < kStackSize) stackNode[sp++] = rFirst ? ch.x : ch.y;
+                node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+                continue;
+            }
+            if (hl) { node = (uint32_t)ch.x; continue; }
+            if (hr) { node = (uint32_t)ch.y; continue; }
+        } else {
+            uint32_t first = (node & ~kLeafBit) >> 3;
+            uint32_t cnt = (node & 7u) + 1u;
+            for (uint32_t i = first; i < first + cnt; ++i) {
+                const float4* q = S.isect + 3 * (size_t)i;
+                float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+                float t, u, v;
+                if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) && t < tmax) {
+                    if (__float_as_uint(c.w) & 1u) return true;
+                    sawNonOpaque = true;
+                }
+            }
+        }
+        if (sp == 0) break;
+        node = (uint32_t)stackNode[--sp];
+    }
+    return false;
+}
+
+// Hit attributes of intersectTriangle / intersectScene (PathTrace.metal:
+// 1840-1851, 3366-3380) from the traversal's (t, u, v), exact ops.
+__device__ __forceinline__ Hit makeHit(const DevScene& S, const Ray& ray, const HitRec& r) {
+    const dk_triangle& tri = S.tris[r.tri];
+    Hit h;
+    h.t = r.t;
+    h.position = ex::add(ray.origin, ex::mul(r.t, ray.direction));
+    float w = ex::sub(ex::sub(1.0f, r.u), r.v);
+    float4 n0 = __ldg(reinterpret_cast<const float4*>(&tri.n0));
+    float4 n1 = __ldg(reinterpret_cast<const float4*>(&tri.n1));
+    float4 n2 = __ldg(reinterpret_cast<const float4*>(&tri.n2));
+    float3 nn = ex::add(ex::add(ex::mul(w, xyz(n0)), ex::mul(r.u, xyz(n1))), ex::mul(r.v, xyz(n2)));
+    float3 normal = ex::normalize(nn);
+    float nd = ex::dot(normal, ray.direction);
+    h.frontFacing = nd <= 0.0f;
+    if (nd > 0.0f) normal = -normal;
+    h.normal = normal;
+    float4 t0 = __ldg(reinterpret_cast<const float4*>(&tri.uv0));
+    float4 t1 = __ldg(reinterpret_cast<const float4*>(&tri.uv1));
+    float4 t2 = __ldg(reinterpret_cast<const float4*>(&tri.uv2));
+    h.uv = make_float2(ex::add(ex::add(ex::mul(w, t0.x), ex::mul(r.u, t1.x)), ex::mul(r.v, t2.x)),
+                       ex::add(ex::add(ex::mul(w, t0.y), ex::mul(r.u, t1.y)), ex::mul(r.v, t2.y)));
+    h.tangent = ex::normalize(xyz(__ldg(reinterpret_cast<const float4*>(&tri.tangent))));
+    h.bitangent = ex::normalize(xyz(__ldg(reinterpret_cast<const float4*>(&tri.bitangent))));
+    uint4 ids = __ldg(reinterpret_cast<const uint4*>(&tri.material_id));
+    h.materialID = ids.x;
+    h.objectID = ids.y;
+    h.primitiveID = r.tri;
+    return h;
+}
+
+}  // namespace dk

@@ -1,0 +1,878 @@
+// Host side of the C ABI declared in include/denrim_cuda.h: device and
+// session management, the scene upload with the traversal-BVH conversion, the
+// per-sample batch scheduler, readback, and the scene-compile helpers that
+// restate the reference's Swift host builders.
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "dk_kernels.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+#define DK_CUDA(call, what)                                                                         \
+    do {                                                                                            \
+        cudaError_t _e = (call);                                                                    \
+        if (_e != cudaSuccess) {                                                                    \
+            int _code = (_e == cudaErrorMemoryAllocation) ? DK_ERROR_OUT_OF_MEMORY : DK_ERROR_COMMAND_FAILED; \
+            return fail(_code, std::string(what) + ": " + cudaGetErrorString(_e));                 \
+        }                                                                                           \
+    } while (0)
+
+int g_device = -1;
+cudaDeviceProp g_prop;
+
+int ensureDevice() {
+    if (g_device >= 0) return DK_OK;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(DK_ERROR_NO_DEVICE, "No compatible CUDA device is available.");
+    }
+    if (cudaSetDevice(0) != cudaSuccess) return fail(DK_ERROR_NO_DEVICE, "cudaSetDevice(0) failed.");
+    cudaGetDeviceProperties(&g_prop, 0);
+    g_device = 0;
+    return DK_OK;
+}
+
+// ------------------------------------------------------ BVH builder -------
+// BVHBuilder.build (Acceleration/BVHBuilder.swift:7-135) + BVHFlattener
+// (FlatBVH.swift:13-32).  The median split makes every subtree's node count a
+// function of its primitive count alone, so pre-order node indices are known
+// before the subtrees are built and the top levels can be built in parallel.
+struct BBox {
+    float mn[3], mx[3];
+};
+inline BBox emptyBox() { return {{FLT_MAX, FLT_MAX, FLT_MAX}, {-FLT_MAX, -FLT_MAX, -FLT_MAX}}; }
+inline void grow(BBox& b, const float* p) {
+    for (int a = 0; a < 3; ++a) {
+        b.mn[a] = std::fmin(b.mn[a], p[a]);
+        b.mx[a] = std::fmax(b.mx[a], p[a]);
+    }
+}
+
+struct BvhBuild {
+    const std::vector<BBox>* prim;
+    std::vector<float> centroid;  // 3 per primitive
+    uint32_t* idx;
+    dk_bvh_node* out;
+    uint32_t maxLeaf;
+
+    uint64_t subtreeNodes(uint64_t n) const {
+        if (n <= std::max<uint64_t>(1, maxLeaf)) return 1;
+        return 1 + subtreeNodes(n / 2) + subtreeNodes(n - n / 2);
+    }
+
+    void build(uint32_t lo, uint32_t hi, uint32_t nodeIndex, int depth) {
+        BBox b = emptyBox();
+        for (uint32_t i = lo; i < hi; ++i) {
+            grow(b, (*prim)[idx[i]].mn);
+            grow(b, (*prim)[idx[i]].mx);
+        }
+        uint32_t count = hi - lo;
+        dk_bvh_node& n = out[nodeIndex];
+        n.bounds_min = {b.mn[0], b.mn[1], b.mn[2], 0.0f};
+        n.bounds_max = {b.mx[0], b.mx[1], b.mx[2], 0.0f};
+        if (count <= std::max<uint32_t>(1, maxLeaf)) {
+            n.metadata = {0u, 0u, lo, count};
+            return;
+        }
+        BBox cb = emptyBox();
+        for (uint32_t i = lo; i < hi; ++i) grow(cb, &centroid[3 * (size_t)idx[i]]);
+        float e[3] = {cb.mx[0] - cb.mn[0], cb.mx[1] - cb.mn[1], cb.mx[2] - cb.mn[2]};
+        int axis = (e[0] >= e[1] && e[0] >= e[2]) ? 0 : (e[1] >= e[2] ? 1 : 2);
+        const float* c = centroid.data();
+        std::stable_sort(idx + lo, idx + hi, [c, axis](uint32_t l, uint32_t r) {
+            return c[3 * (size_t)l + axis] < c[3 * (size_t)r + axis];
+        });
+        uint32_t mid = lo + count / 2;
+        uint32_t left = nodeIndex + 1;
+        uint32_t right = left + (uint32_t)subtreeNodes(mid - lo);
+        n.metadata = {left, right, 0u, 0u};
+        if (depth < 4 && count > 65536) {
+            std::thread t([=] { this->build(lo, mid, left, depth + 1); });
+            build(mid, hi, right, depth + 1);
+            t.join();
+        } else {
+            build(lo, mid, left, depth + 1);
+            build(mid, hi, right, depth + 1);
+        }
+    }
+};
+
+uint32_t buildReferenceBvh(const dk_triangle* tris, uint32_t n, uint32_t maxLeaf, dk_bvh_node* nodes,
+                           uint32_t* primIdx) {
+    if (n == 0) return 0;
+    std::vector<BBox> prim(n);
+    BvhBuild b;
+    b.centroid.resize(3 * (size_t)n);
+    for (uint32_t i = 0; i < n; ++i) {
+        BBox bb = emptyBox();
+        grow(bb, &tris[i].v0.x);
+        grow(bb, &tris[i].v1.x);
+        grow(bb, &tris[i].v2.x);
+        prim[i] = bb;
+        for (int a = 0; a < 3; ++a) b.centroid[3 * (size_t)i + a] = (bb.mn[a] + bb.mx[a]) * 0.5f;
+    }
+    for (uint32_t i = 0; i < n; ++i) primIdx[i] = i;
+    b.prim = &prim;
+    b.idx = primIdx;
+    b.out = nodes;
+    b.maxLeaf = maxLeaf;
+    uint32_t count = (uint32_t)b.subtreeNodes(n);
+    b.build(0, n, 0, 0);
+    return count;
+}
+
+// ----------------------------------------------------- scene on device ----
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Session {
+    dk_settings settings;
+    dk::DevScene scene;
+    dk::Wave wave;
+    dk::Accum accum;
+    std::vector<DeviceBuffer> buffers;
+    float4* staging = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaEvent_t> evPool;
+    uint32_t sampleCount = 0;
+    uint32_t lightCount = 0;
+    dk_stats stats;
+    int gridGen = 0, gridExtend = 0, gridShade = 0, gridShadow = 0, gridFinal = 0;
+    size_t deviceBytes = 0;
+};
+
+template <typename T>
+int deviceAlloc(Session* s, T** out, size_t count, const char* what) {
+    *out = nullptr;
+    if (count == 0) return DK_OK;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? DK_ERROR_OUT_OF_MEMORY : DK_ERROR_COMMAND_FAILED,
+                    std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
+    }
+    s->buffers.push_back({p, count * sizeof(T)});
+    s->deviceBytes += count * sizeof(T);
+    *out = static_cast<T*>(p);
+    return DK_OK;
+}
+
+template <typename T>
+int upload(Session* s, T** out, const T* host, size_t count, const char* what) {
+    int rc = deviceAlloc(s, out, count, what);
+    if (rc != DK_OK || count == 0) return rc;
+    DK_CUDA(cudaMemcpy(*out, host, count * sizeof(T), cudaMemcpyHostToDevice), what);
+    return DK_OK;
+}
+
+void freeSession(Session* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto& b : s->buffers) cudaFree(b.ptr);
+    for (auto& e : s->evPool) cudaEventDestroy(e);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+// Traversal layout built from the reference flat BVH: every interior node
+// stores both child boxes (one 64-byte record), leaves are referenced from
+// their parent, triangles are stored per leaf slot with precomputed edges.
+struct TraversalBvh {
+    std::vector<float4> nodes;  // 4 per node
+    std::vector<float4> isect;  // 3 per slot
+};
+
+const uint32_t kLeafBit = 0x80000000u;
+
+struct Converter {
+    const dk_scene* sc;
+    const std::vector<uint8_t>* opaque;
+    const std::vector<int32_t>* slotOf;  // reference slot -> compacted isect slot (-1: skipped)
+    TraversalBvh* out;
+    uint32_t dummySlot;
+    std::string err;
+
+    static void setBox(float4* n, int side, const float* mn, const float* mx) {
+        float4& xy = n[side];
+        xy = make_float4(mn[0], mx[0], mn[1], mx[1]);
+        if (side == 0) {
+            n[2].x = mn[2];
+            n[2].y = mx[2];
+        } else {
+            n[2].z = mn[2];
+            n[2].w = mx[2];
+        }
+    }
+
+    uint32_t leafCode(uint32_t first, uint32_t count) { return kLeafBit | (first << 3) | (count - 1u); }
+
+    // Reference leaf [first, first+count) -> child reference (splitting >8).
+    bool leafRef(uint32_t firstRef, uint32_t countRef, uint32_t& ref, float* mn, float* mx, int depth) {
+        std::vector<uint32_t> slots;
+        for (uint32_t i = firstRef; i < firstRef + countRef; ++i) {
+            int32_t s = (*slotOf)[i];
+            if (s >= 0) slots.push_back((uint32_t)s);
+        }
+        return slotsRef(slots, 0, (uint32_t)slots.size(), ref, mn, mx, depth);
+    }
+
+    // Bounds of one slot from the exact vertex positions of its triangle.
+    void slotBounds(uint32_t slot, float* mn, float* mx) {
+        uint32_t tri = __float_as_uint_host(out->isect[3 * (size_t)slot + 1].w);
+        const dk_triangle& t = sc->triangles[tri];
+        const float* p[3] = {&t.v0.x, &t.v1.x, &t.v2.x};
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) {
+                mn[a] = std::fmin(mn[a], p[k][a]);
+                mx[a] = std::fmax(mx[a], p[k][a]);
+            }
+    }
+
+    static uint32_t __float_as_uint_host(float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return u;
+    }
+
+    bool slotsRef(const std::vector<uint32_t>& slots, uint32_t lo, uint32_t hi, uint32_t& ref, float* mn, float* mx,
+                  int depth) {
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = FLT_MAX;
+            mx[a] = -FLT_MAX;
+        }
+        if (hi == lo) {  // empty child: a far-away point box around the dummy slot
+            ref = leafCode(dummySlot, 1);
+            for (int a = 0; a < 3; ++a) mn[a] = mx[a] = 1e30f;
+            return true;
+        }
+        bool contiguous = true;
+        for (uint32_t i = lo + 1; i < hi; ++i) contiguous &= slots[i] == slots[i - 1] + 1;
+        if (hi - lo <= 8 && contiguous) {
+            for (uint32_t i = lo; i < hi; ++i) slotBounds(slots[i], mn, mx);
+            ref = leafCode(slots[lo], hi - lo);
+            return true;
+        }
+        if (depth > 60) {
+            err = "BVH too deep";
+            return false;
+        }
+        // Split oversized or non-contiguous leaves into a small subtree.
+        uint32_t mid = lo + (hi - lo) / 2;
+        if (hi - lo <= 8) mid = lo + 1;  // non-contiguous: peel one slot at a time
+        uint32_t nodeIndex = (uint32_t)(out->nodes.size() / 4);
+        out->nodes.resize(out->nodes.size() + 4);
+        uint32_t l, r;
+        float lmn[3], lmx[3], rmn[3], rmx[3];
+        if (!slotsRef(slots, lo, mid, l, lmn, lmx, depth + 1)) return false;
+        if (!slotsRef(slots, mid, hi, r, rmn, rmx, depth + 1)) return false;
+        float4* n = &out->nodes[4 * (size_t)nodeIndex];
+        setBox(n, 0, lmn, lmx);
+        setBox(n, 1, rmn, rmx);
+        n[3] = make_float4(__uint_as_float_host(l), __uint_as_float_host(r), 0.0f, 0.0f);
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = std::fmin(lmn[a], rmn[a]);
+            mx[a] = std::fmax(lmx[a], rmx[a]);
+        }
+        ref = nodeIndex;
+        return true;
+    }
+
+    static float __uint_as_float_host(uint32_t u) {
+        float f;
+        std::memcpy(&f, &u, 4);
+        return f;
+    }
+
+    // Reference node -> child reference (interior nodes become records).
+    bool nodeRef(uint32_t refNode, uint32_t& ref, float* mn, float* mx, int depth) {
+        if (refNode >= sc->node_count) {
+            err = "BVH child index out of range";
+            return false;
+        }
+        if (depth > 60) {
+            err = "BVH deeper than the 64-entry traversal stack";
+            return false;
+        }
+        const dk_bvh_node& n = sc->nodes[refNode];
+        if (n.metadata.w > 0) {
+            if ((uint64_t)n.metadata.z + n.metadata.w > sc->primitive_index_count) {
+                err = "BVH leaf range out of range";
+                return false;
+            }
+            return leafRef(n.metadata.z, n.metadata.w, ref, mn, mx, depth);
+        }
+        uint32_t nodeIndex = (uint32_t)(out->nodes.size() / 4);
+        out->nodes.resize(out->nodes.size() + 4);
+        uint32_t l, r;
+        float lmn[3], lmx[3], rmn[3], rmx[3];
+        if (n.metadata.x <= refNode || n.metadata.y <= refNode) {
+            err = "BVH is not in pre-order (child index not after its parent)";
+            return false;
+        }
+        if (!nodeRef(n.metadata.x, l, lmn, lmx, depth + 1)) return false;
+        if (!nodeRef(n.metadata.y, r, rmn, rmx, depth + 1)) return false;
+        float4* rec = &out->nodes[4 * (size_t)nodeIndex];
+        setBox(rec, 0, lmn, lmx);
+        setBox(rec, 1, rmn, rmx);
+        rec[3] = make_float4(__uint_as_float_host(l), __uint_as_float_host(r), 0.0f, 0.0f);
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = std::fmin(lmn[a], rmn[a]);
+            mx[a] = std::fmax(lmx[a], rmx[a]);
+        }
+        ref = nodeIndex;
+        return true;
+    }
+};
+
+// Builds the traversal layout.  `primIdx` is the reference leaf order: the
+// slot (tie-break key) of a triangle is its position there.
+int buildTraversal(const dk_scene* sc, const dk_bvh_node* nodes, uint32_t nodeCount, const uint32_t* primIdx,
+                   uint32_t primCount, TraversalBvh& tb) {
+    std::vector<uint8_t> opaque(sc->triangle_count);
+    for (uint32_t i = 0; i < sc->triangle_count; ++i) {
+        const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
+        float transmission = std::fmin(std::fmax(m.emission.w, 0.0f), 1.0f);
+        opaque[i] = (m.base_color.w > 0.001f && transmission <= 0.001f) ? 1 : 0;
+    }
+    std::vector<int32_t> slotOf(primCount, -1);
+    tb.isect.clear();
+    tb.isect.reserve(3 * (size_t)primCount + 3);
+    uint32_t valid = 0;
+    for (uint32_t i = 0; i < primCount; ++i) {
+        uint32_t t = primIdx[i];
+        if (t >= sc->triangle_count) continue;  // the reference skips these (PathTrace.metal:3358-3360)
+        const dk_triangle& tr = sc->triangles[t];
+        float4 a = make_float4(tr.v0.x, tr.v0.y, tr.v0.z, Converter::__uint_as_float_host(i));
+        float4 b = make_float4(tr.v1.x - tr.v0.x, tr.v1.y - tr.v0.y, tr.v1.z - tr.v0.z, Converter::__uint_as_float_host(t));
+        float4 c = make_float4(tr.v2.x - tr.v0.x, tr.v2.y - tr.v0.y, tr.v2.z - tr.v0.z,
+                               Converter::__uint_as_float_host(opaque[t] ? 1u : 0u));
+        tb.isect.push_back(a);
+        tb.isect.push_back(b);
+        tb.isect.push_back(c);
+        slotOf[i] = (int32_t)valid++;
+    }
+    uint32_t dummy = valid;
+    tb.isect.push_back(make_float4(0, 0, 0, Converter::__uint_as_float_host(0xffffffffu)));
+    tb.isect.push_back(make_float4(0, 0, 0, Converter::__uint_as_float_host(0u)));
+    tb.isect.push_back(make_float4(0, 0, 0, 0));
+    Converter cv{sc, &opaque, &slotOf, &tb, dummy, ""};
+    dk_scene view = *sc;
+    view.nodes = nodes;
+    view.node_count = nodeCount;
+    view.primitive_indices = primIdx;
+    view.primitive_index_count = primCount;
+    cv.sc = &view;
+    tb.nodes.clear();
+    tb.nodes.resize(4);  // root record
+    float mn[3], mx[3];
+    uint32_t rootRef;
+    const dk_bvh_node& root = nodes[0];
+    if (root.metadata.w > 0) {
+        if (!cv.nodeRef(0, rootRef, mn, mx, 1)) return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + cv.err + ".");
+        float4* rec = &tb.nodes[0];
+        float far[3] = {1e30f, 1e30f, 1e30f};
+        Converter::setBox(rec, 0, mn, mx);
+        Converter::setBox(rec, 1, far, far);
+        rec[3] = make_float4(Converter::__uint_as_float_host(rootRef),
+                             Converter::__uint_as_float_host(kLeafBit | (dummy << 3)), 0, 0);
+        return DK_OK;
+    }
+    // Interior root: build children into record 0.
+    uint32_t l, r;
+    float lmn[3], lmx[3], rmn[3], rmx[3];
+    if (root.metadata.x == 0 || root.metadata.y == 0 || !cv.nodeRef(root.metadata.x, l, lmn, lmx, 1) ||
+        !cv.nodeRef(root.metadata.y, r, rmn, rmx, 1))
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + (cv.err.empty() ? std::string("malformed BVH root") : cv.err) + ".");
+    float4* rec = &tb.nodes[0];
+    Converter::setBox(rec, 0, lmn, lmx);
+    Converter::setBox(rec, 1, rmn, rmx);
+    rec[3] = make_float4(Converter::__uint_as_float_host(l), Converter::__uint_as_float_host(r), 0, 0);
+    return DK_OK;
+}
+
+}  // namespace
+
+// Kernel symbols for occupancy queries.
+namespace dk {
+int kernelGrid(int which, int smCount);
+}
+
+extern "C" {
+
+const char* dk_last_error_message(void) { return g_error.c_str(); }
+
+const char* dk_version(void) { return "denrim-gb300 0.1 (sm_103a wavefront path tracer)"; }
+
+int dk_device_count(int* out) {
+    if (!out) return fail(DK_ERROR_INVALID_ARGUMENT, "out_count is null");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *out = n;
+    return DK_OK;
+}
+
+int dk_device_open(int ordinal) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(DK_ERROR_NO_DEVICE, "No compatible CUDA device is available.");
+    }
+    if (ordinal < 0 || ordinal >= n) return fail(DK_ERROR_INVALID_ARGUMENT, "device ordinal out of range");
+    DK_CUDA(cudaSetDevice(ordinal), "cudaSetDevice");
+    DK_CUDA(cudaGetDeviceProperties(&g_prop, ordinal), "cudaGetDeviceProperties");
+    if (g_prop.major < 10) return fail(DK_ERROR_MISSING_KERNEL, "this library carries sm_103a kernels only");
+    g_device = ordinal;
+    return DK_OK;
+}
+
+int dk_build_bvh(const dk_triangle* tris, uint32_t n, uint32_t maxLeaf, dk_bvh_node* nodes, uint32_t* nodeCount,
+                 uint32_t* primIdx) {
+    if (!nodeCount || (n > 0 && (!tris || !nodes || !primIdx)))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "dk_build_bvh: null argument");
+    *nodeCount = buildReferenceBvh(tris, n, maxLeaf, nodes, primIdx);
+    return DK_OK;
+}
+
+int dk_build_lights(dk_triangle* tris, uint32_t n, const dk_material* mats, uint32_t matCount,
+                    dk_light_record* lights, uint32_t* lightCount) {
+    if (!lightCount || (n > 0 && (!tris || !lights)) || (matCount > 0 && !mats))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "dk_build_lights: null argument");
+    *lightCount = 0;
+    if (matCount == 0) return DK_OK;
+    // lightRecordsAndTaggedTriangles (LightingGPUEncoding.swift:5-64).
+    struct C { uint32_t tri, mat; float area, weight, nx, ny, nz; };
+    std::vector<C> cands;
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t mi = std::min(tris[i].material_id, matCount - 1);
+        const dk_float4& e = mats[mi].emission;
+        if (!(std::fmax(std::fmax(e.x, e.y), e.z) > 0.0f)) continue;
+        float ax = tris[i].v1.x - tris[i].v0.x, ay = tris[i].v1.y - tris[i].v0.y, az = tris[i].v1.z - tris[i].v0.z;
+        float bx = tris[i].v2.x - tris[i].v0.x, by = tris[i].v2.y - tris[i].v0.y, bz = tris[i].v2.z - tris[i].v0.z;
+        float cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+        float len = std::sqrt(cx * cx + cy * cy + cz * cz);
+        float area = len * 0.5f;
+        if (!(area > 0.0f)) continue;
+        float power = (e.x * 0.2126f + e.y * 0.7152f + e.z * 0.0722f) * area;
+        if (!(power > 0.0f)) continue;
+        float s = 1.0f / len;
+        cands.push_back({i, mi, area, power, cx * s, cy * s, cz * s});
+    }
+    float total = 0.0f;
+    for (auto& c : cands) total += c.weight;
+    if (!(total > 0.0f)) return DK_OK;
+    float cum = 0.0f;
+    for (size_t k = 0; k < cands.size(); ++k) {
+        cum += cands[k].weight;
+        tris[cands[k].tri].padding2 = (uint32_t)(k + 1);
+        lights[k].triangle_index = cands[k].tri;
+        lights[k].material_index = cands[k].mat;
+        lights[k].area = cands[k].area;
+        lights[k].selection_cdf = (k == cands.size() - 1) ? 1.0f : std::fmin(cum / total, 1.0f);
+        lights[k].normal = {cands[k].nx, cands[k].ny, cands[k].nz, 0.0f};
+    }
+    *lightCount = (uint32_t)cands.size();
+    return DK_OK;
+}
+
+int dk_build_environment_samples(const dk_float4* pixels, uint32_t w, uint32_t h, float intensity, float maxRadiance,
+                                 dk_environment_sample* out, uint32_t* outCount) {
+    if (!outCount || (w > 0 && h > 0 && (!pixels || !out)))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "dk_build_environment_samples: null argument");
+    *outCount = 0;
+    if (w == 0 || h == 0) return DK_OK;
+    int rc = ensureDevice();
+    if (rc != DK_OK) return rc;
+    size_t n = (size_t)w * h;
+    if (n > 0xffffffffull / 2) return fail(DK_ERROR_INVALID_ARGUMENT, "environment map too large");
+    uint32_t nb = (uint32_t)((n + 1023) / 1024);
+    float4* dPix = nullptr;
+    double *dW = nullptr, *dP = nullptr, *dB = nullptr;
+    float2* dOut = nullptr;
+    cudaError_t e = cudaMalloc(&dPix, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&dW, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dP, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dB, (nb + 1) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dOut, n * sizeof(float2));
+    double total = 0.0;
+    if (e == cudaSuccess) e = cudaMemcpy(dPix, pixels, n * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = dk::buildEnvironmentTable(dPix, w, h, std::fmax(intensity, 0.0f), std::fmax(maxRadiance, 0.0f), dW, dP, dB,
+                                      dOut, 4 * g_prop.multiProcessorCount, 0, &total);
+    if (e == cudaSuccess && total > 0.0) e = cudaMemcpy(out, dOut, n * sizeof(float2), cudaMemcpyDeviceToHost);
+    cudaFree(dPix);
+    cudaFree(dW);
+    cudaFree(dP);
+    cudaFree(dB);
+    cudaFree(dOut);
+    if (e != cudaSuccess) return fail(DK_ERROR_COMMAND_FAILED, std::string("environment table: ") + cudaGetErrorString(e));
+    *outCount = total > 0.0 ? (uint32_t)n : 0u;
+    return DK_OK;
+}
+
+int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** outSession) {
+    if (!sc || !st || !outSession) return fail(DK_ERROR_INVALID_ARGUMENT, "dk_session_create: null argument");
+    *outSession = nullptr;
+    // RenderSession.init validation (RenderSession.swift:304-327).
+    if (st->width == 0 || st->height == 0)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Render dimensions must be positive.");
+    if (st->quality != DK_QUALITY_FINAL)
+        return fail(DK_ERROR_INVALID_ARGUMENT, "only RenderQuality.final (the path tracer) is implemented");
+    if (sc->triangle_count == 0 && sc->volume_count == 0)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no renderable geometry.");
+    if (sc->material_count == 0 || !sc->materials)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no materials.");
+    if (sc->volume_count != 0)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: distance volumes are not supported by this backend.");
+    if (!sc->triangles) return fail(DK_ERROR_INVALID_ARGUMENT, "triangles is null");
+    if ((sc->light_count && !sc->lights) || (sc->environment_sample_count && !sc->environment_samples) ||
+        (sc->texture_descriptor_count && !sc->texture_descriptors) || (sc->texture_pixel_count && !sc->texture_pixels) ||
+        (sc->node_count && !sc->nodes) || (sc->primitive_index_count && !sc->primitive_indices))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "a scene array pointer is null while its count is not zero");
+    if (sc->environment_texture_index_plus_one > sc->texture_descriptor_count)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: environment texture index out of range.");
+    for (uint32_t i = 0; i < sc->texture_descriptor_count; ++i) {
+        const dk_uint4& md = sc->texture_descriptors[i].metadata;
+        if ((uint64_t)md.x + (uint64_t)md.y * md.z > sc->texture_pixel_count)
+            return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: texture descriptor exceeds the pixel array.");
+    }
+    for (uint32_t i = 0; i < sc->light_count; ++i)
+        if (sc->lights[i].triangle_index >= sc->triangle_count && sc->lights[i].selection_cdf > 0.0f) {
+            // Tolerated like the reference (the light is skipped at sampling time).
+        }
+    int rc = ensureDevice();
+    if (rc != DK_OK) return rc;
+
+    // Traversal BVH: the caller's reference BVH, or (when none is given) the
+    // reference builder run here with slots = triangle index, which is the tie
+    // order of the reference's linear fallback (PathTrace.metal:3264-3290).
+    TraversalBvh tb;
+    if (sc->node_count > 0) {
+        rc = buildTraversal(sc, sc->nodes, sc->node_count, sc->primitive_indices, sc->primitive_index_count, tb);
+    } else {
+        std::vector<dk_bvh_node> nodes(2 * (size_t)sc->triangle_count + 1);
+        std::vector<uint32_t> prim(sc->triangle_count);
+        uint32_t nc = buildReferenceBvh(sc->triangles, sc->triangle_count, 4, nodes.data(), prim.data());
+        // Leaf order of this private BVH is not the tie order: rewrite slots.
+        rc = buildTraversal(sc, nodes.data(), nc, prim.data(), sc->triangle_count, tb);
+        if (rc == DK_OK)
+            for (size_t s = 0; s + 1 < tb.isect.size() / 3; ++s) {
+                uint32_t tri;
+                std::memcpy(&tri, &tb.isect[3 * s + 1].w, 4);
+                std::memcpy(&tb.isect[3 * s].w, &tri, 4);
+            }
+    }
+    if (rc != DK_OK) return rc;
+
+    Session* s = new Session();
+    std::memset(&s->stats, 0, sizeof(s->stats));
+    s->settings = *st;
+    if (s->settings.max_bounces < 1) s->settings.max_bounces = 1;
+#define TRY(x)                 \
+    do {                       \
+        int _rc = (x);         \
+        if (_rc != DK_OK) {    \
+            freeSession(s);    \
+            return _rc;        \
+        }                      \
+    } while (0)
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        freeSession(s);
+        return fail(DK_ERROR_COMMAND_FAILED, "cudaStreamCreate failed");
+    }
+
+    dk::DevScene& D = s->scene;
+    std::memset(&D, 0, sizeof(D));
+    TRY(upload(s, const_cast<dk_triangle**>(&D.tris), sc->triangles, sc->triangle_count, "triangles"));
+    TRY(upload(s, const_cast<dk_material**>(&D.mats), sc->materials, sc->material_count, "materials"));
+    TRY(upload(s, const_cast<float4**>(&D.isect), tb.isect.data(), tb.isect.size(), "triangle slots"));
+    TRY(upload(s, const_cast<float4**>(&D.nodes), tb.nodes.data(), tb.nodes.size(), "BVH nodes"));
+    TRY(upload(s, const_cast<dk_texture_descriptor**>(&D.texdesc), sc->texture_descriptors, sc->texture_descriptor_count,
+               "texture descriptors"));
+    TRY(upload(s, const_cast<float4**>(&D.texpix), reinterpret_cast<const float4*>(sc->texture_pixels),
+               (size_t)sc->texture_pixel_count, "texture pixels"));
+    TRY(upload(s, const_cast<dk_light_record**>(&D.lights), sc->lights, sc->light_count, "lights"));
+    TRY(upload(s, const_cast<float2**>(&D.env), reinterpret_cast<const float2*>(sc->environment_samples),
+               sc->environment_sample_count, "environment samples"));
+    D.tri_count = sc->triangle_count;
+    D.mat_count = sc->material_count;
+    D.node_count = (uint32_t)(tb.nodes.size() / 4);
+    D.texdesc_count = sc->texture_descriptor_count;
+    D.light_count = sc->lights ? sc->light_count : 0;
+    D.env_count = sc->environment_samples ? sc->environment_sample_count : 0;
+    D.env_tex_plus1 = sc->environment_texture_index_plus_one;
+    D.env_intensity = sc->environment_intensity;
+    D.env_rot_y = sc->environment_rotation_y;
+    D.env_max_radiance = sc->environment_max_radiance;
+
+    // Wave capacity: whole frames of the tile, up to a fixed path budget.
+    const uint32_t pixels = st->width * st->height;
+    uint64_t capPaths = 1ull << 24;  // 16.8 M paths (~3.5 GB of path state)
+    if (st->max_samples_per_launch > 0) capPaths = std::min<uint64_t>(capPaths, (uint64_t)st->max_samples_per_launch * pixels);
+    capPaths = std::max<uint64_t>(capPaths, pixels);
+    capPaths = std::min<uint64_t>(capPaths, 0x7fffffffull);
+    dk::Wave& W = s->wave;
+    W.cap = (uint32_t)capPaths;
+    size_t cap = W.cap;
+    TRY(deviceAlloc(s, &W.ray_o, cap, "ray origins"));
+    TRY(deviceAlloc(s, &W.ray_d, cap, "ray directions"));
+    TRY(deviceAlloc(s, &W.tp, cap, "throughput"));
+    TRY(deviceAlloc(s, &W.rad, cap, "radiance"));
+    TRY(deviceAlloc(s, &W.rng, cap, "rng"));
+    TRY(deviceAlloc(s, &W.hit, cap, "hits"));
+    TRY(deviceAlloc(s, &W.nee_o, 3 * cap, "shadow origins"));
+    TRY(deviceAlloc(s, &W.nee_d, 3 * cap, "shadow directions"));
+    TRY(deviceAlloc(s, &W.nee_c, 3 * cap, "shadow contributions"));
+    TRY(deviceAlloc(s, &W.nee_tp, cap, "shadow throughput"));
+    TRY(deviceAlloc(s, &W.q[0], cap, "queue 0"));
+    TRY(deviceAlloc(s, &W.q[1], cap, "queue 1"));
+    TRY(deviceAlloc(s, &W.qs, cap, "shadow queue"));
+    TRY(deviceAlloc(s, &W.counts, 4, "queue counters"));
+    TRY(deviceAlloc(s, &W.aov, 4 * (size_t)pixels, "AOV records"));
+    dk::Accum& A = s->accum;
+    TRY(deviceAlloc(s, &A.sum, pixels, "accumulation sum"));
+    TRY(deviceAlloc(s, &A.comp, pixels, "accumulation compensation"));
+    TRY(deviceAlloc(s, &A.resolved, pixels, "accumulation resolve"));
+    TRY(deviceAlloc(s, &A.count, pixels, "sample counts"));
+    TRY(deviceAlloc(s, &A.aov, 6 * (size_t)pixels, "AOV planes"));
+    TRY(deviceAlloc(s, &s->staging, pixels, "readback staging"));
+    if (cudaMemsetAsync(A.sum, 0, pixels * sizeof(float4), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(A.comp, 0, pixels * sizeof(float4), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(A.resolved, 0, pixels * sizeof(dk::D4), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(A.count, 0, pixels * sizeof(uint32_t), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(A.aov, 0, 6 * pixels * sizeof(float4), s->stream) != cudaSuccess ||
+        cudaStreamSynchronize(s->stream) != cudaSuccess) {
+        freeSession(s);
+        return fail(DK_ERROR_COMMAND_FAILED, "clearing accumulation buffers failed");
+    }
+    int sm = g_prop.multiProcessorCount;
+    s->gridGen = dk::kernelGrid(0, sm);
+    s->gridExtend = dk::kernelGrid(1, sm);
+    s->gridShade = dk::kernelGrid(2, sm);
+    s->gridShadow = dk::kernelGrid(3, sm);
+    s->gridFinal = dk::kernelGrid(4, sm);
+    s->stats.device_bytes = s->deviceBytes;
+    *outSession = reinterpret_cast<dk_session*>(s);
+    return DK_OK;
+#undef TRY
+}
+
+static int eventAt(Session* s, size_t i, cudaEvent_t* out) {
+    while (s->evPool.size() <= i) {
+        cudaEvent_t e;
+        DK_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+        s->evPool.push_back(e);
+    }
+    *out = s->evPool[i];
+    return DK_OK;
+}
+
+// Renders `samples` sample indices starting at `sampleBegin` over a tile, in
+// batches of whole tile-frames that fit the wave.  Every stage is bracketed by
+// events on the session stream; they are read once, after the last batch.
+static int renderSamples(Session* s, uint32_t tx, uint32_t ty, uint32_t tw, uint32_t th, uint32_t samples,
+                         uint32_t sampleBegin) {
+    const dk_settings& st = s->settings;
+    dk::DevParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.width = st.width;
+    P.height = st.height;
+    P.max_bounces = std::max(1u, st.max_bounces);
+    P.transparent_background = st.transparent_background;
+    P.shows_env_bg = st.shows_environment_background;
+    P.frame_seed = st.frame_seed;
+    P.denoiser = st.denoiser_enabled;
+    P.bg[0] = st.background_color[0];
+    P.bg[1] = st.background_color[1];
+    P.bg[2] = st.background_color[2];
+    P.clamp = st.sample_radiance_clamp_set ? st.sample_radiance_clamp : 64.0f;  // RenderQuality.final default
+    P.tile_x = tx;
+    P.tile_y = ty;
+    P.tile_w = tw;
+    P.tile_h = th;
+    P.cam = st.camera;
+    P.prev_cam = st.previous_camera;
+    const uint32_t tileN = tw * th;
+    const uint32_t perBatch = std::max(1u, s->wave.cap / tileN);
+    cudaStream_t q = s->stream;
+    // Event marks: kind 0 = other, 1 = extend, 2 = shade, 3 = shadow; the
+    // interval between mark i and mark i+1 belongs to kind[i].
+    std::vector<int> kinds;
+    size_t ev = 0;
+    cudaEvent_t e;
+    auto mark = [&](int kind) -> int {
+        int rc = eventAt(s, ev++, &e);
+        if (rc != DK_OK) return rc;
+        DK_CUDA(cudaEventRecord(e, q), "cudaEventRecord");
+        kinds.push_back(kind);
+        return DK_OK;
+    };
+#define MARK(k)                       \
+    do {                              \
+        int _rc = mark(k);            \
+        if (_rc != DK_OK) return _rc; \
+    } while (0)
+    uint64_t launches = 0;
+    uint32_t done = 0;
+    while (done < samples) {
+        uint32_t nb = std::min(perBatch, samples - done);
+        P.sample_begin = sampleBegin + done;
+        P.samples_in_batch = nb;
+        P.path_count = nb * tileN;
+        MARK(0);
+        DK_CUDA(dk::launchGenerate(s->scene, P, s->wave, s->gridGen, q), "generate launch");
+        ++launches;
+        for (uint32_t b = 0; b < P.max_bounces; ++b) {
+            uint32_t sel = b & 1u;
+            MARK(1);
+            DK_CUDA(dk::launchExtend(s->scene, s->wave, sel, s->gridExtend, q), "extend launch");
+            MARK(2);
+            DK_CUDA(dk::launchShade(s->scene, P, s->wave, b, sel, s->gridShade, q), "shade launch");
+            MARK(3);
+            DK_CUDA(dk::launchShadow(s->scene, P, s->wave, s->gridShadow, q), "shadow launch");
+            launches += 3;
+        }
+        MARK(0);
+        if (st.denoiser_enabled) {
+            DK_CUDA(dk::launchAovPrimary(s->scene, P, s->wave, s->gridExtend, q), "AOV launch");
+            ++launches;
+        }
+        DK_CUDA(dk::launchFinalize(P, s->wave, s->accum, 1u, s->gridFinal, q), "finalize launch");
+        ++launches;
+        done += nb;
+    }
+    MARK(0);
+#undef MARK
+    DK_CUDA(cudaEventSynchronize(s->evPool[ev - 1]), "render");
+    float t[4] = {0, 0, 0, 0};
+    for (size_t i = 0; i + 1 < ev; ++i) {
+        float ms = 0;
+        DK_CUDA(cudaEventElapsedTime(&ms, s->evPool[i], s->evPool[i + 1]), "cudaEventElapsedTime");
+        t[kinds[i]] += ms;
+    }
+    float total = 0;
+    DK_CUDA(cudaEventElapsedTime(&total, s->evPool[0], s->evPool[ev - 1]), "cudaEventElapsedTime");
+    s->stats.last_render_ms = total;
+    s->stats.last_extend_ms = t[1];
+    s->stats.last_shade_ms = t[2];
+    s->stats.last_shadow_ms = t[3];
+    s->stats.last_other_ms = t[0];
+    s->stats.last_launches = launches;
+    s->stats.kernel_launches += launches;
+    s->stats.paths_traced += (uint64_t)tileN * samples;
+    return DK_OK;
+}
+
+int dk_session_render(dk_session* session, uint32_t samples) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s) return fail(DK_ERROR_INVALID_ARGUMENT, "session is null");
+    if (samples == 0) return DK_OK;
+    int rc = renderSamples(s, 0, 0, s->settings.width, s->settings.height, samples, s->sampleCount);
+    if (rc != DK_OK) {
+        cudaGetLastError();
+        return rc;  // sampleCount unchanged (RenderSession.swift:844-847)
+    }
+    s->sampleCount += samples;
+    return DK_OK;
+}
+
+int dk_session_render_tile(dk_session* session, uint32_t x, uint32_t y, uint32_t w, uint32_t h, int completes) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s) return fail(DK_ERROR_INVALID_ARGUMENT, "session is null");
+    // encodeNextSample tile clamping (RenderSession.swift:898-907).
+    uint32_t W = s->settings.width, H = s->settings.height;
+    uint32_t tx = std::min(x, W), ty = std::min(y, H);
+    uint32_t tw = std::min(w, W - tx), th = std::min(h, H - ty);
+    if (tw == 0 || th == 0) return DK_OK;
+    int rc = renderSamples(s, tx, ty, tw, th, 1, s->sampleCount);
+    if (rc != DK_OK) {
+        cudaGetLastError();
+        return rc;
+    }
+    if (completes) s->sampleCount += 1;
+    return DK_OK;
+}
+
+int dk_session_update_camera(dk_session* session, const dk_camera* camera, const dk_camera* previous) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s || !camera) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    dk_camera old = s->settings.camera;
+    s->settings.camera = *camera;
+    s->settings.previous_camera = previous ? *previous : old;
+    return dk_session_reset(session);
+}
+
+int dk_session_reset(dk_session* session) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s) return fail(DK_ERROR_INVALID_ARGUMENT, "session is null");
+    size_t pixels = (size_t)s->settings.width * s->settings.height;
+    DK_CUDA(cudaMemsetAsync(s->accum.sum, 0, pixels * sizeof(float4), s->stream), "reset");
+    DK_CUDA(cudaMemsetAsync(s->accum.comp, 0, pixels * sizeof(float4), s->stream), "reset");
+    DK_CUDA(cudaMemsetAsync(s->accum.resolved, 0, pixels * sizeof(dk::D4), s->stream), "reset");
+    DK_CUDA(cudaMemsetAsync(s->accum.count, 0, pixels * sizeof(uint32_t), s->stream), "reset");
+    DK_CUDA(cudaStreamSynchronize(s->stream), "reset");
+    s->sampleCount = 0;
+    return DK_OK;
+}
+
+int dk_session_read_output(dk_session* session, int output, float* rgba, size_t pixelCount) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s || !rgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    size_t pixels = (size_t)s->settings.width * s->settings.height;
+    if (pixelCount != pixels) return fail(DK_ERROR_INVALID_ARGUMENT, "pixel_count must equal width*height");
+    if (output < DK_OUTPUT_BEAUTY || output > DK_OUTPUT_MOTION_VECTOR)
+        return fail(DK_ERROR_INVALID_ARGUMENT, "unknown output kind");
+    const float4* src;
+    if (output == DK_OUTPUT_BEAUTY) {
+        DK_CUDA(dk::launchResolveBeauty(s->accum, (uint32_t)pixels, s->staging, s->gridFinal, s->stream), "resolve launch");
+        src = s->staging;
+    } else {
+        src = s->accum.aov + (size_t)(output - 1) * pixels;
+    }
+    DK_CUDA(cudaMemcpyAsync(rgba, src, pixels * sizeof(float4), cudaMemcpyDeviceToHost, s->stream), "readback");
+    DK_CUDA(cudaStreamSynchronize(s->stream), "readback");
+    return DK_OK;
+}
+
+int dk_session_sample_count(const dk_session* session, uint32_t* out) {
+    const Session* s = reinterpret_cast<const Session*>(session);
+    if (!s || !out) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    *out = s->sampleCount;
+    return DK_OK;
+}
+
+int dk_session_stats(const dk_session* session, dk_stats* out) {
+    const Session* s = reinterpret_cast<const Session*>(session);
+    if (!s || !out) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    *out = s->stats;
+    return DK_OK;
+}
+
+int dk_session_destroy(dk_session* session) {
+    freeSession(reinterpret_cast<Session*>(session));
+    return DK_OK;
+}
+
+}  // extern "C"

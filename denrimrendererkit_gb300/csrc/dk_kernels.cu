@@ -1,0 +1,850 @@
+// Wavefront kernels of the sm_103a progressive path tracer.
+//
+// The reference runs the whole path of a pixel-sample in one thread
+// (pathTraceKernel, Sources/DenrimRendererKit/Resources/Shaders/
+// PathTrace.metal:5167-5586).  Here one batch of paths (tile pixels x several
+// sample indices) advances bounce by bounce through four stages over SoA path
+// state in HBM:
+//   k_generate  camera rays + RNG seeds              (:5204-5225)
+//   k_extend    closest hit of every active ray      (intersectScene, :3294-3421)
+//   k_shade     the bounce body: misses, materials, random walks, emission,
+//               NEE ray generation, BSDF sampling, Russian roulette  (:5252-5518)
+//   k_shadow    the NEE shadow queries and the clamped direct-light sum
+//               (sampleDirectLighting, :4407-4585; shadowOccluded, :4196-4274)
+//   k_finalize  Kahan-compensated accumulation + last-sample AOVs (:5520-5585)
+// Surviving paths are compacted into the next queue with warp-ballot appends.
+#include <cstdio>
+
+#include "dk_kernels.h"
+#include "dk_shade.cuh"
+
+namespace dk {
+
+__device__ __forceinline__ uint32_t laneId() { return threadIdx.x & 31u; }
+
+// Warp-aggregated append: one atomic per warp, order-stable within the warp.
+__device__ __forceinline__ uint32_t warpAppend(uint32_t* counter, bool pred) {
+    unsigned active = __activemask();
+    unsigned ballot = __ballot_sync(active, pred);
+    if (ballot == 0u) return 0u;
+    int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if ((int)laneId() == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+    base = __shfl_sync(active, base, leader);
+    unsigned lower = ballot & ((1u << laneId()) - 1u);
+    return base + (uint32_t)__popc(lower);
+}
+
+// makeCameraRay (PathTrace.metal:4056-4091); pinhole arithmetic in exact ops.
+__device__ Ray makeCameraRay(const dk_camera& cam, uint32_t width, uint32_t height, uint32_t gx, uint32_t gy, float jx,
+                             float jy, float lx, float ly) {
+    float u = ex::div(ex::add((float)gx, jx), (float)width);
+    float v = ex::sub(1.0f, ex::div(ex::add((float)gy, jy), (float)height));
+    float3 ll = f3(cam.lower_left.x, cam.lower_left.y, cam.lower_left.z);
+    float3 hz = f3(cam.horizontal.x, cam.horizontal.y, cam.horizontal.z);
+    float3 vt = f3(cam.vertical.x, cam.vertical.y, cam.vertical.z);
+    float3 planePoint = ex::add(ex::add(ll, ex::mul(u, hz)), ex::mul(v, vt));
+    Ray ray;
+    if (cam.origin.w > 0.5f) {
+        ray.origin = planePoint;
+        ray.direction = ex::normalize(ex::cross(vt, hz));
+    } else {
+        ray.origin = f3(cam.origin.x, cam.origin.y, cam.origin.z);
+        ray.direction = ex::normalize(ex::sub(planePoint, ray.origin));
+    }
+    float aperture = fmaxf(cam.lens.x, 0.0f);
+    if (cam.origin.w <= 0.5f && aperture > 0.0f) {
+        float3 forward = normalize(cross(vt, hz));
+        float focus = fmaxf(cam.lens.y, 0.0001f);
+        float focalT = focus / fmaxf(dot(ray.direction, forward), 0.0001f);
+        float3 focal = ray.origin + ray.direction * focalT;
+        float2 disk = uniformDisk(lx, ly);
+        disk.x *= aperture;
+        disk.y *= aperture;
+        ray.origin += normalize(hz) * disk.x + normalize(vt) * disk.y;
+        ray.direction = normalize(focal - ray.origin);
+    }
+    return ray;
+}
+
+// applyNormalMap (PathTrace.metal:4021-4054).
+__device__ Hit applyNormalMap(const DevScene& S, Hit h, uint32_t idx, float3 rayDir) {
+    float3 mapped = xyz(sampleTexture(S, idx, h.uv, make_float4(0.5f, 0.5f, 1.0f, 1.0f)));
+    mapped = ex::normalize(ex::sub(ex::mul(mapped, 2.0f), f3(1.0f)));
+    float3 t = ex::sub(h.tangent, ex::mul(h.normal, ex::dot(h.tangent, h.normal)));
+    if (__fsqrt_rn(ex::dot(t, t)) <= 1e-5f) {
+        float3 helper = fabsf(h.normal.y) < 0.999f ? f3(0, 1, 0) : f3(1, 0, 0);
+        t = ex::cross(helper, h.normal);
+    }
+    t = ex::normalize(t);
+    float3 b = ex::sub(h.bitangent, ex::mul(h.normal, ex::dot(h.bitangent, h.normal)));
+    if (__fsqrt_rn(ex::dot(b, b)) <= 1e-5f) b = ex::cross(h.normal, t);
+    b = ex::normalize(b);
+    h.normal = ex::normalize(ex::add(ex::add(ex::mul(mapped.x, t), ex::mul(mapped.y, b)), ex::mul(mapped.z, h.normal)));
+    if (ex::dot(h.normal, rayDir) > 0.0f) h.normal = -h.normal;
+    return h;
+}
+
+__device__ __forceinline__ Material materialForHit(const DevScene& S, const Hit& h) {  // :1096-1121
+    return loadMaterial(S.mats, min(h.materialID, S.mat_count - 1u));
+}
+
+// shadowOccluded (PathTrace.metal:4196-4274).  Opaque blockers are found by an
+// any-hit query; the ordered closest-hit walk through cut-outs and transmissive
+// layers runs only when such a layer lies on the segment.
+__device__ bool shadowOccluded(const DevScene& S, float3 o, float3 d, float maxDistance, float3& transmittance) {
+    bool sawNonOpaque = false;
+    if (traceAnyOpaque(S, o, d, maxDistance, sawNonOpaque)) return true;
+    if (!sawNonOpaque) return false;
+    float traveled = 0.0f;
+    for (uint32_t step = 0; step < 8u; ++step) {
+        HitRec r = traceClosest(S, o, d);
+        if (r.tri == kNoHit || traveled + r.t >= maxDistance) return false;
+        Ray ray{o, d};
+        Hit h = makeHit(S, ray, r);
+        Material sm = materialForHit(S, h);
+        if (sm.baseColor.w <= 0.001f) {
+            traveled += r.t;
+            o = h.position + d * 0.001f;
+            continue;
+        }
+        float transmission = materialTransmission(sm);
+        if (transmission <= 0.001f) return true;
+        bool insideSolid = !h.frontFacing && !materialThinWalled(sm);
+        float3 medium = (materialHasVolumeScattering(sm) && insideSolid)
+                            ? exp3((-materialVolumeSigmaT(sm)) * r.t)
+                            : materialTransmissionAbsorption(sm, r.t, insideSolid);
+        transmittance *= materialTransmissionTint(sm, 0.35f) * medium * transmission;
+        if (maxComponent(transmittance) < 0.02f) return true;
+        traveled += r.t;
+        o = h.position + d * 0.001f;
+    }
+    return true;
+}
+
+// Subsurface walk helpers (PathTrace.metal:3490-3523).
+__device__ __forceinline__ float sampleSubsurfaceFreeFlight(float3 sigmaT, float ux, float uy) {
+    float sigma = sigmaT.z;
+    if (ux < 0.33333333333f) sigma = sigmaT.x;
+    else if (ux < 0.66666666667f) sigma = sigmaT.y;
+    return -logf(fmaxf(1.0f - uy, 1e-6f)) / fmaxf(sigma, 1e-4f);
+}
+__device__ __forceinline__ float subsurfaceCollisionPDF(float3 s, float d) {
+    float3 tr = exp3((-s) * d);
+    return fmaxf((s.x * tr.x + s.y * tr.y + s.z * tr.z) * 0.33333333333f, 1e-6f);
+}
+__device__ __forceinline__ float subsurfaceBoundaryPDF(float3 s, float d) {
+    float3 tr = exp3((-s) * d);
+    return fmaxf((tr.x + tr.y + tr.z) * 0.33333333333f, 1e-6f);
+}
+
+// continueSubsurfaceRandomWalk (PathTrace.metal:3525-3621).
+__device__ bool continueSubsurfaceRandomWalk(const DevScene& S, const Hit& entry, const Material& m, Ray& ray,
+                                             float3& tp, float& prevPdf, uint32_t& state) {
+    if (materialSubsurface(m) <= 0.0f || !entry.frontFacing) return false;
+    float e0 = randomFloat(state);
+    float e1 = randomFloat(state);
+    float3 entryDir = orientHemisphere(cosineHemisphere(e0, e1), -entry.normal);
+    Ray medium{entry.position + entryDir * 0.001f, entryDir};
+    float3 sigmaT = 1.0f / mx(xyz(m.subsurfaceRadius) * fmaxf(m.subsurfaceRadius.w, 0.0f), f3(1e-4f));
+    float3 albedo = clamp3(xyz(m.subsurfaceColor), f3(0.0f), f3(0.999f));
+    float anisotropy = clampf(m.subsurfaceParameters.x, -0.95f, 0.95f);
+    for (uint32_t step = 0u; step < 8u; ++step) {
+        HitRec r = traceClosest(S, medium.origin, medium.direction);
+        if (r.tri == kNoHit) return false;
+        float f0 = randomFloat(state);
+        float f1 = randomFloat(state);
+        float freeFlight = sampleSubsurfaceFreeFlight(sigmaT, f0, f1);
+        if (freeFlight < r.t) {
+            medium.origin += medium.direction * freeFlight;
+            float h0 = randomFloat(state);
+            float h1 = randomFloat(state);
+            medium.direction = sampleHenyeyGreenstein(h0, h1, medium.direction, anisotropy);
+            float3 tr = exp3((-sigmaT) * freeFlight);
+            tp *= albedo * sigmaT * tr / subsurfaceCollisionPDF(sigmaT, freeFlight);
+            if (maxComponent(tp) <= 1e-4f) return false;
+            continue;
+        }
+        Hit b = makeHit(S, medium, r);
+        float3 exitNormal = normalize(b.frontFacing ? b.normal : -b.normal);
+        float x0 = randomFloat(state);
+        float x1 = randomFloat(state);
+        ray.direction = orientHemisphere(cosineHemisphere(x0, x1), exitNormal);
+        ray.origin = b.position + exitNormal * 0.001f;
+        float3 tr = exp3((-sigmaT) * r.t);
+        tp *= tr / subsurfaceBoundaryPDF(sigmaT, r.t);
+        prevPdf = fmaxf(dot(exitNormal, ray.direction), 0.0f) * 0.31830988618f;
+        return true;
+    }
+    return false;
+}
+
+// continueTransmissionVolumeRandomWalk (PathTrace.metal:3685-3721).
+__device__ bool continueTransmissionVolumeRandomWalk(const Hit& b, const Material& m, Ray& ray, float3& tp,
+                                                     float& prevPdf, uint32_t& state) {
+    if (b.frontFacing || !materialHasVolumeScattering(m)) return false;
+    float3 sigmaT = materialVolumeSigmaT(m);
+    float3 sigmaS = materialVolumeSigmaS(m);
+    if (maxComponent(sigmaT) <= 1e-5f || maxComponent(sigmaS) <= 1e-5f) return false;
+    float f0 = randomFloat(state);
+    float f1 = randomFloat(state);
+    float freeFlight = sampleSubsurfaceFreeFlight(sigmaT, f0, f1);
+    if (freeFlight >= b.t) {
+        tp *= exp3((-sigmaT) * b.t) / subsurfaceBoundaryPDF(sigmaT, b.t);
+        return false;
+    }
+    float3 tr = exp3((-sigmaT) * freeFlight);
+    tp *= sigmaS * tr / subsurfaceCollisionPDF(sigmaT, freeFlight);
+    ray.origin += ray.direction * freeFlight;
+    float h0 = randomFloat(state);
+    float h1 = randomFloat(state);
+    ray.direction = sampleHenyeyGreenstein(h0, h1, ray.direction, clampf(m.volumeParameters.y, -0.95f, 0.95f));
+    ray.origin += ray.direction * 0.001f;
+    prevPdf = 0.0f;
+    return maxComponent(tp) > 1e-4f;
+}
+
+// continueTransmissiveSurface (PathTrace.metal:1723-1799).
+__device__ bool continueTransmissiveSurface(const Hit& h, const Material& m, Ray& ray, float3& tp, float& prevPdf,
+                                            uint32_t& state) {
+    float transmission = materialTransmission(m);
+    if (transmission <= 0.0f || randomFloat(state) > transmission) return false;
+    float3 incoming = ray.direction;
+    float3 view = -incoming;
+    float roughness = clampf(m.parameters3.y, 0.001f, 1.0f);
+    float ior = fmaxf(m.parameters3.z, 1.0001f);
+    float3 micro = h.normal;
+    if (roughness > 0.01f) {
+        float a = randomFloat(state);
+        float b = randomFloat(state);
+        micro = sampleGGXHalfVector(a, b, h.normal, roughness);
+        if (dot(micro, incoming) > 0.0f) micro = -micro;
+    }
+    float etaI = h.frontFacing ? 1.0f : ior;
+    float etaT = h.frontFacing ? ior : 1.0f;
+    float eta = etaI / etaT;
+    float cosI = fmaxf(dot(view, micro), 0.0f);
+    float fresnel = dielectricFresnel(cosI, etaI, etaT);
+    if (materialThinWalled(m)) {
+        fresnel = dielectricFresnel(cosI, 1.0f, ior);
+        float rp = clampf(fresnel, 0.02f, 0.98f);
+        if (randomFloat(state) < rp) {
+            ray.direction = normalize(reflect(incoming, micro));
+            ray.origin = h.position + micro * 0.001f;
+            tp *= fresnel / fmaxf(rp, 1e-5f);
+        } else {
+            ray.direction = incoming;
+            ray.origin = h.position + ray.direction * 0.001f;
+            float grazing = 1.0f - fabsf(dot(view, h.normal));
+            float tint = mixf(0.35f, 0.95f, grazing * grazing);
+            tp *= materialTransmissionTint(m, tint) * ((1.0f - fresnel) / fmaxf(1.0f - rp, 1e-5f));
+        }
+        prevPdf = 0.0f;
+        return true;
+    }
+    float3 refracted = refract(incoming, micro, eta);
+    bool tir = dot(refracted, refracted) <= 1e-7f;
+    float rp = tir ? 1.0f : clampf(fresnel, 0.02f, 0.98f);
+    if (randomFloat(state) < rp) {
+        ray.direction = normalize(reflect(incoming, micro));
+        ray.origin = h.position + micro * 0.001f;
+        tp *= tir ? 1.0f : fresnel / fmaxf(rp, 1e-5f);
+    } else {
+        ray.direction = normalize(refracted);
+        ray.origin = h.position + ray.direction * 0.001f;
+        float grazing = 1.0f - fabsf(dot(view, h.normal));
+        float tint = mixf(0.35f, 0.95f, grazing * grazing);
+        float w = (1.0f - fresnel) / fmaxf(1.0f - rp, 1e-5f);
+        float3 absorption = materialTransmissionAbsorption(m, h.t, !h.frontFacing && !materialHasVolumeScattering(m));
+        tp *= materialTransmissionTint(m, tint) * absorption * w;
+    }
+    prevPdf = 0.0f;
+    return true;
+}
+
+// ================================================================ kernels ==
+
+__device__ __forceinline__ uint32_t gridStride() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ uint32_t globalId() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+__device__ __forceinline__ void writeAovMiss(float4* aov, uint32_t local, uint32_t tileN) {
+    aov[0 * (size_t)tileN + local] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0u));  // t, -, -, hasHit
+    aov[1 * (size_t)tileN + local] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    aov[2 * (size_t)tileN + local] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    aov[3 * (size_t)tileN + local] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+__device__ __forceinline__ void writeAovHit(float4* aov, uint32_t local, uint32_t tileN, const Hit& h, float4 albedo) {
+    aov[0 * (size_t)tileN + local] = make_float4(h.t, __uint_as_float(h.materialID), __uint_as_float(h.objectID), __uint_as_float(1u));
+    aov[1 * (size_t)tileN + local] = make_float4(h.normal.x, h.normal.y, h.normal.z, 0.0f);
+    aov[2 * (size_t)tileN + local] = albedo;
+    aov[3 * (size_t)tileN + local] = make_float4(h.position.x, h.position.y, h.position.z, 0.0f);
+}
+
+__global__ void __launch_bounds__(256) k_generate(DevScene S, DevParams P, Wave W) {
+    const uint32_t tileN = P.tile_w * P.tile_h;
+    for (uint32_t p = globalId(); p < P.path_count; p += gridStride()) {
+        uint32_t slice = p / tileN, local = p - slice * tileN;
+        uint32_t px = P.tile_x + local % P.tile_w, py = P.tile_y + local / P.tile_w;
+        uint32_t sample = P.sample_begin + slice;
+        uint32_t state = P.frame_seed ^ hash_u32(px + py * P.width) ^ hash_u32(sample + 1u);
+        float j0 = randomFloat(state);
+        float j1 = randomFloat(state);
+        float j2 = randomFloat(state);
+        float j3 = randomFloat(state);
+        Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, j0, j1, j2, j3);
+        W.ray_o[p] = make_float4(ray.origin.x, ray.origin.y, ray.origin.z, 0.0f);
+        W.ray_d[p] = make_float4(ray.direction.x, ray.direction.y, ray.direction.z, 0.0f);
+        W.tp[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        W.rad[p] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        W.rng[p] = make_uint2(state, 0u);
+        W.q[0][p] = p;
+        if (slice == P.samples_in_batch - 1u) writeAovMiss(W.aov, local, tileN);
+    }
+    if (globalId() == 0) {
+        W.counts[0] = P.path_count;
+        W.counts[1] = 0u;
+        W.counts[2] = 0u;
+    }
+}
+
+// Closest hit for every ray of the input queue (intersectScene).
+__global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel) {
+    const uint32_t* q = W.q[sel];
+    const uint32_t n = W.counts[sel];
+    if (globalId() == 0) {
+        W.counts[sel ^ 1u] = 0u;
+        W.counts[2] = 0u;
+    }
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t p = q[i];
+        float4 o = W.ray_o[p], d = W.ray_d[p];
+        HitRec r = traceClosest(S, xyz(o), xyz(d));
+        W.hit[p] = make_float4(r.t, __uint_as_float(r.tri), r.u, r.v);
+    }
+}
+
+struct ShadeOut { bool survive; uint32_t neeMask; };
+
+// The body of the reference bounce loop (PathTrace.metal:5252-5518) for one
+// path whose closest hit is already in W.hit.
+__device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave& W, uint32_t p, uint32_t bounce) {
+    ShadeOut out{false, 0u};
+    const uint32_t tileN = P.tile_w * P.tile_h;
+    float4 ro = W.ray_o[p], rd = W.ray_d[p], tpw = W.tp[p], radw = W.rad[p], hr = W.hit[p];
+    uint2 rs = W.rng[p];
+    Ray ray{xyz(ro), xyz(rd)};
+    float3 tp = xyz(tpw);
+    float prevPdf = tpw.w;
+    float3 rad = xyz(radw);
+    float alpha = radw.w;
+    uint32_t state = rs.x, flags = rs.y;
+    bool primaryFound = (flags & 1u) != 0u;
+    uint32_t tri = __float_as_uint(hr.y);
+
+    if (tri == kNoHit) {  // :5279-5305
+        if (P.transparent_background != 0u && !primaryFound) {
+            alpha = 0.0f;
+        } else if (P.shows_env_bg == 0u && !primaryFound) {
+            alpha = 1.0f;
+            rad += mx(f3(P.bg[0], P.bg[1], P.bg[2]), f3(0.0f));
+        } else {
+            float envWeight = 1.0f;
+            if (bounce > 0u && prevPdf > 0.0f) envWeight = powerHeuristic(prevPdf, environmentPDF(S, ray.direction));
+            rad += clampSampleContribution(tp * sampleEnvironment(S, ray.direction) * envWeight, P.clamp);
+        }
+        W.rad[p] = make_float4(rad.x, rad.y, rad.z, alpha);
+        return out;
+    }
+    HitRec rec{hr.x, tri, hr.z, hr.w};
+    Hit h = makeHit(S, ray, rec);
+    Material m = materialForHit(S, h);
+    uint32_t nIdx = (uint32_t)m.parameters.w;
+    if (nIdx != 0u) h = applyNormalMap(S, h, nIdx, ray.direction);
+    uint32_t bIdx = (uint32_t)m.parameters.z;
+    if (bIdx != 0u) {
+        float4 texel = sampleTexture(S, bIdx, h.uv, make_float4(1.0f, 1.0f, 1.0f, 1.0f));
+        m.baseColor = make_float4(ex::mul(m.baseColor.x, texel.x), ex::mul(m.baseColor.y, texel.y),
+                                  ex::mul(m.baseColor.z, texel.z), ex::mul(m.baseColor.w, texel.w));
+    }
+    if (m.baseColor.w <= 0.001f) {  // cut-out: pass through (:5318-5321)
+        ray.origin = ex::add(h.position, ex::mul(ray.direction, 0.001f));
+        W.ray_o[p] = make_float4(ray.origin.x, ray.origin.y, ray.origin.z, 0.0f);
+        out.survive = true;
+        return out;
+    }
+    if (!primaryFound) {
+        flags |= 1u;
+        uint32_t slice = p / tileN;
+        if (slice == P.samples_in_batch - 1u && P.denoiser == 0u) writeAovHit(W.aov, p - slice * tileN, tileN, h, m.baseColor);
+    }
+
+    bool continued = false;
+    if (continueTransmissionVolumeRandomWalk(h, m, ray, tp, prevPdf, state)) {
+        continued = true;
+    } else {
+        float subsurface = materialSubsurface(m);
+        if (subsurface > 0.0f && randomFloat(state) < subsurface &&
+            continueSubsurfaceRandomWalk(S, h, m, ray, tp, prevPdf, state)) {
+            continued = true;
+        } else if (continueTransmissiveSurface(h, m, ray, tp, prevPdf, state)) {
+            continued = true;
+        }
+    }
+    if (continued) {
+        bool dead = terminatePathWithRussianRoulette(bounce, tp, state);
+        W.ray_o[p] = make_float4(ray.origin.x, ray.origin.y, ray.origin.z, 0.0f);
+        W.ray_d[p] = make_float4(ray.direction.x, ray.direction.y, ray.direction.z, 0.0f);
+        W.tp[p] = make_float4(tp.x, tp.y, tp.z, prevPdf);
+        W.rng[p] = make_uint2(state, flags);
+        out.survive = !dead;
+        return out;
+    }
+
+    float3 emission = xyz(m.emission);
+    if (maxComponent(emission) > 0.0f) {  // :5376-5392
+        float w = 1.0f;
+        if (bounce > 0u && prevPdf > 0.0f) w = powerHeuristic(prevPdf, lightPDFForHit(S, h, ray.direction));
+        rad += clampSampleContribution(tp * emission * w, P.clamp);
+        W.rad[p] = make_float4(rad.x, rad.y, rad.z, alpha);
+        return out;
+    }
+
+    // ------------------------------------ NEE (sampleDirectLighting) ------
+    float3 view = -ray.direction;
+    float3 shadowOrigin = h.position + h.normal * 0.001f;
+    const size_t cap = W.cap;
+    if (S.light_count > 0u) {
+        uint32_t index = selectLightIndex(S, randomFloat(state));
+        const dk_light_record& L = S.lights[index];
+        float selPdf = lightSelectionPDF(S, index);
+        uint32_t lti = __ldg(&L.triangle_index);
+        if (lti < S.tri_count && selPdf > 0.0f) {
+            uint32_t lmi = min(__ldg(&L.material_index), S.mat_count - 1u);
+            float3 le = xyz(__ldg(reinterpret_cast<const float4*>(S.mats + lmi) + 1));
+            float area = __ldg(&L.area);
+            if (area > 0.0f) {
+                float r0 = randomFloat(state);
+                float r1 = randomFloat(state);
+                float3 lp = sampleTriangle(S.tris[lti], r0, r1);
+                float3 toL = lp - h.position;
+                float d2 = dot(toL, toL);
+                float dist = sqrtf(d2);
+                float3 ld = toL / dist;
+                float cosS = fmaxf(0.0f, dot(h.normal, ld));
+                float cosL = fmaxf(0.0f, dot(xyz(__ldg(reinterpret_cast<const float4*>(&L.normal))), -ld));
+                if (cosS > 0.0f && cosL > 0.0f) {
+                    float lightPdf = selPdf * (d2 / fmaxf(cosL * area, 1e-6f));
+                    float bsdfPdf = materialBSDFPDF(m, h.normal, h.tangent, h.bitangent, view, ld);
+                    float mis = powerHeuristic(lightPdf, bsdfPdf);
+                    float G = cosS * cosL * area / fmaxf(d2, 1e-6f);
+                    float3 c = evaluateMaterialBRDF(m, h.normal, h.tangent, h.bitangent, view, ld) * le * G * mis;
+                    if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f)) {
+                        W.nee_o[p] = make_float4(shadowOrigin.x, shadowOrigin.y, shadowOrigin.z, dist - 0.002f);
+                        W.nee_d[p] = make_float4(ld.x, ld.y, ld.z, 0.0f);
+                        W.nee_c[p] = make_float4(c.x, c.y, c.z, selPdf);
+                        out.neeMask |= 1u;
+                    }
+                }
+            }
+        }
+    }
+    for (uint32_t e = 0u; e < 2u; ++e) {
+        float a = randomFloat(state);
+        float b = randomFloat(state);
+        float cdf = randomFloat(state);
+        float envPdf;
+        float3 dir = sampleEnvironmentDirection(S, a, b, cdf, envPdf);
+        float cosS = fmaxf(0.0f, dot(h.normal, dir));
+        if (envPdf > 0.0f && cosS > 0.0f) {
+            float bsdfPdf = materialBSDFPDF(m, h.normal, h.tangent, h.bitangent, view, dir);
+            float mis = powerHeuristic(envPdf, bsdfPdf);
+            float3 c = evaluateMaterialBRDF(m, h.normal, h.tangent, h.bitangent, view, dir) *
+                       sampleEnvironment(S, dir) * cosS * mis;
+            if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f)) {
+                size_t slot = (size_t)(1u + e) * cap + p;
+                W.nee_o[slot] = make_float4(shadowOrigin.x, shadowOrigin.y, shadowOrigin.z, 1.0e20f);
+                W.nee_d[slot] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                W.nee_c[slot] = make_float4(c.x, c.y, c.z, envPdf * 2.0f);
+                out.neeMask |= 2u << e;
+            }
+        }
+    }
+    if (out.neeMask) W.nee_tp[p] = make_float4(tp.x, tp.y, tp.z, __uint_as_float(out.neeMask));
+
+    // --------------------------------------------- BSDF sampling ----------
+    float roughness = clampf(m.parameters.x, 0.02f, 1.0f);
+    float anisotropy = materialSpecularAnisotropy(m);
+    float3 f0 = materialF0(m);
+    float clearcoat = materialClearcoat(m);
+    float ccR = materialClearcoatRoughness(m);
+    float dP, sP, cP;
+    materialLobeProbabilities(m, dP, sP, cP);
+    float c0 = randomFloat(state);
+    float c1 = randomFloat(state);
+    float3 diffuseDir = orientHemisphere(cosineHemisphere(c0, c1), h.normal);
+    float lobe = randomFloat(state);
+    float3 next;
+    if (lobe < cP) {
+        float a = randomFloat(state);
+        float b = randomFloat(state);
+        float3 hv = sampleGGXVisibleNormal(a, b, h.normal, h.tangent, h.bitangent, view, ccR, 0.0f);
+        next = normalize(reflect(ray.direction, hv));
+        if (dot(next, h.normal) <= 0.0f) {
+            next = diffuseDir;
+            tp *= materialDiffuseBounceWeight(m, h.normal, view, next) / fmaxf(dP, 1e-5f);
+        } else {
+            float nDotL = fmaxf(dot(h.normal, next), 1e-5f);
+            float vDotH = fmaxf(dot(view, hv), 1e-5f);
+            tp *= clearcoat * fresnelSchlickThinFilm(vDotH, materialClearcoatF0Color(m), m) *
+                  geometrySmithG1GGX(nDotL, ccR) / fmaxf(cP, 1e-5f);
+        }
+    } else if (lobe < cP + sP) {
+        float a = randomFloat(state);
+        float b = randomFloat(state);
+        float3 hv = sampleGGXVisibleNormal(a, b, h.normal, h.tangent, h.bitangent, view, roughness, anisotropy);
+        next = normalize(reflect(ray.direction, hv));
+        if (dot(next, h.normal) <= 0.0f) {
+            next = diffuseDir;
+            tp *= materialDiffuseBounceWeight(m, h.normal, view, next) / fmaxf(dP, 1e-5f);
+        } else {
+            float vDotH = fmaxf(dot(view, hv), 1e-5f);
+            float3 fres = fresnelSchlickThinFilm(vDotH, f0, m);
+            float3 cca = materialClearcoatAttenuationForDirection(m, h.normal, view, next);
+            tp *= cca * fres * geometrySmithG1GGXAnisotropic(next, h.normal, h.tangent, h.bitangent, roughness, anisotropy) /
+                  fmaxf(sP, 1e-5f);
+        }
+    } else {
+        next = diffuseDir;
+        tp *= materialDiffuseBounceWeight(m, h.normal, view, next) / fmaxf(dP, 1e-5f);
+    }
+    prevPdf = materialBSDFPDF(m, h.normal, h.tangent, h.bitangent, view, next);
+    ray.origin = shadowOrigin;
+    ray.direction = next;
+    bool dead = terminatePathWithRussianRoulette(bounce, tp, state);
+    W.ray_o[p] = make_float4(ray.origin.x, ray.origin.y, ray.origin.z, 0.0f);
+    W.ray_d[p] = make_float4(ray.direction.x, ray.direction.y, ray.direction.z, 0.0f);
+    W.tp[p] = make_float4(tp.x, tp.y, tp.z, prevPdf);
+    W.rng[p] = make_uint2(state, flags);
+    out.survive = !dead;
+    return out;
+}
+
+__global__ void __launch_bounds__(128) k_shade(DevScene S, DevParams P, Wave W, uint32_t bounce, uint32_t sel) {
+    const uint32_t* q = W.q[sel];
+    uint32_t* qNext = W.q[sel ^ 1u];
+    const uint32_t n = W.counts[sel];
+    const bool lastBounce = bounce + 1u >= P.max_bounces;
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t p = q[i];
+        ShadeOut o = shadePath(S, P, W, p, bounce);
+        bool keep = o.survive && !lastBounce;
+        uint32_t slot = warpAppend(&W.counts[sel ^ 1u], keep);
+        if (keep) qNext[slot] = p;
+        bool sh = o.neeMask != 0u;
+        uint32_t sslot = warpAppend(&W.counts[2], sh);
+        if (sh) W.qs[sslot] = p;
+    }
+}
+
+// NEE shadow queries of one path and the clamped direct-light sum
+// (sampleDirectLighting + `radiance += clampSampleContribution(throughput * direct)`).
+__global__ void __launch_bounds__(128) k_shadow(DevScene S, DevParams P, Wave W) {
+    const uint32_t n = W.counts[2];
+    const size_t cap = W.cap;
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t p = W.qs[i];
+        float4 tpw = W.nee_tp[p];
+        uint32_t mask = __float_as_uint(tpw.w);
+        float3 direct = f3(0.0f);
+        for (uint32_t k = 0; k < 3u; ++k) {
+            if (!(mask & (1u << k))) continue;
+            size_t slot = k * cap + p;
+            float4 o = W.nee_o[slot], d = W.nee_d[slot], c = W.nee_c[slot];
+            float3 T = f3(1.0f);
+            if (!shadowOccluded(S, xyz(o), xyz(d), o.w, T)) direct += xyz(c) * T / c.w;
+        }
+        float4 r = W.rad[p];
+        float3 add = clampSampleContribution(xyz(tpw) * direct, P.clamp);
+        W.rad[p] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
+    }
+}
+
+// tracePrimaryAOV (PathTrace.metal:4093-4159) for the denoiser's unjittered AOV ray.
+__global__ void __launch_bounds__(128) k_aov_primary(DevScene S, DevParams P, Wave W) {
+    const uint32_t tileN = P.tile_w * P.tile_h;
+    for (uint32_t local = globalId(); local < tileN; local += gridStride()) {
+        uint32_t px = P.tile_x + local % P.tile_w, py = P.tile_y + local / P.tile_w;
+        Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, 0.5f, 0.5f, 0.0f, 0.0f);
+        writeAovMiss(W.aov, local, tileN);
+        for (uint32_t pass = 0; pass < 32u; ++pass) {
+            HitRec r = traceClosest(S, ray.origin, ray.direction);
+            if (r.tri == kNoHit) break;
+            Hit h = makeHit(S, ray, r);
+            Material m = materialForHit(S, h);
+            uint32_t nIdx = (uint32_t)m.parameters.w;
+            if (nIdx != 0u) h = applyNormalMap(S, h, nIdx, ray.direction);
+            uint32_t bIdx = (uint32_t)m.parameters.z;
+            if (bIdx != 0u) {
+                float4 t = sampleTexture(S, bIdx, h.uv, make_float4(1.0f, 1.0f, 1.0f, 1.0f));
+                m.baseColor = make_float4(ex::mul(m.baseColor.x, t.x), ex::mul(m.baseColor.y, t.y),
+                                          ex::mul(m.baseColor.z, t.z), ex::mul(m.baseColor.w, t.w));
+            }
+            if (m.baseColor.w <= 0.001f) {
+                ray.origin = ex::add(h.position, ex::mul(ray.direction, 0.001f));
+                continue;
+            }
+            writeAovHit(W.aov, local, tileN, h, m.baseColor);
+            break;
+        }
+    }
+}
+
+// projectToScreen (PathTrace.metal:1662-1697), exact ops.
+__device__ bool projectToScreen(const dk_camera& cam, float3 w, uint32_t width, uint32_t height, float2& s) {
+    float3 hz = f3(cam.horizontal.x, cam.horizontal.y, cam.horizontal.z);
+    float3 vt = f3(cam.vertical.x, cam.vertical.y, cam.vertical.z);
+    float3 ll = f3(cam.lower_left.x, cam.lower_left.y, cam.lower_left.z);
+    float3 org = f3(cam.origin.x, cam.origin.y, cam.origin.z);
+    float3 forward = ex::normalize(ex::cross(vt, hz));
+    float3 center = ex::add(ex::add(ll, ex::mul(hz, 0.5f)), ex::mul(vt, 0.5f));
+    float3 planePoint;
+    if (cam.origin.w > 0.5f) {
+        planePoint = ex::sub(w, ex::mul(forward, ex::dot(ex::sub(w, center), forward)));
+    } else {
+        float3 toPoint = ex::sub(w, org);
+        float den = ex::dot(toPoint, forward);
+        if (fabsf(den) <= 1e-5f) return false;
+        float planeT = ex::div(ex::dot(ex::sub(center, org), forward), den);
+        if (planeT <= 0.0f) return false;
+        planePoint = ex::add(org, ex::mul(toPoint, planeT));
+    }
+    float3 rel = ex::sub(planePoint, ll);
+    float u = ex::div(ex::dot(rel, hz), fmaxf(ex::dot(hz, hz), 1e-5f));
+    float v = ex::div(ex::dot(rel, vt), fmaxf(ex::dot(vt, vt), 1e-5f));
+    s = make_float2(ex::mul(u, (float)width), ex::mul(ex::sub(1.0f, v), (float)height));
+    return true;
+}
+
+// Kahan-compensated accumulation of every path of the batch into its pixel,
+// in sample order, plus the AOV block (PathTrace.metal:5559-5585) from the
+// batch's last sample.  Past every 4096 samples the FP32 sum is folded into
+// an FP64 resolve buffer.
+__global__ void __launch_bounds__(256) k_finalize(DevParams P, Wave W, Accum A, uint32_t writeAov) {
+    const uint32_t tileN = P.tile_w * P.tile_h;
+    for (uint32_t local = globalId(); local < tileN; local += gridStride()) {
+        uint32_t px = P.tile_x + local % P.tile_w, py = P.tile_y + local / P.tile_w;
+        size_t pix = (size_t)py * P.width + px;
+        float4 s = A.sum[pix], c = A.comp[pix];
+        uint32_t count = A.count[pix];
+        for (uint32_t k = 0; k < P.samples_in_batch; ++k) {
+            float4 r = W.rad[(size_t)k * tileN + local];
+            float y, t;
+            y = r.x - c.x; t = s.x + y; c.x = (t - s.x) - y; s.x = t;
+            y = r.y - c.y; t = s.y + y; c.y = (t - s.y) - y; s.y = t;
+            y = r.z - c.z; t = s.z + y; c.z = (t - s.z) - y; s.z = t;
+            y = r.w - c.w; t = s.w + y; c.w = (t - s.w) - y; s.w = t;
+        }
+        uint32_t newCount = count + P.samples_in_batch;
+        if ((newCount >> 12) != (count >> 12)) {
+            D4 R = A.resolved[pix];
+            R.x += (double)s.x - (double)c.x;
+            R.y += (double)s.y - (double)c.y;
+            R.z += (double)s.z - (double)c.z;
+            R.w += (double)s.w - (double)c.w;
+            A.resolved[pix] = R;
+            s = make_float4(0, 0, 0, 0);
+            c = make_float4(0, 0, 0, 0);
+        }
+        A.sum[pix] = s;
+        A.comp[pix] = c;
+        A.count[pix] = newCount;
+        if (!writeAov) continue;
+        float4 a0 = W.aov[local], a1 = W.aov[(size_t)tileN + local], a2 = W.aov[2 * (size_t)tileN + local],
+               a3 = W.aov[3 * (size_t)tileN + local];
+        size_t plane = (size_t)P.width * P.height;
+        if (__float_as_uint(a0.w) != 0u) {
+            float t = a0.x;
+            float3 n = f3(a1.x, a1.y, a1.z);
+            float3 enc = ex::add(ex::mul(n, 0.5f), f3(0.5f));
+            float mid = (float)(__float_as_uint(a0.y) + 1u), oid = (float)(__float_as_uint(a0.z) + 1u);
+            A.aov[0 * plane + pix] = make_float4(t, t, t, 1.0f);
+            A.aov[1 * plane + pix] = make_float4(enc.x, enc.y, enc.z, 1.0f);
+            A.aov[2 * plane + pix] = a2;
+            A.aov[3 * plane + pix] = make_float4(mid, mid, mid, 1.0f);
+            A.aov[4 * plane + pix] = make_float4(oid, oid, oid, 1.0f);
+            float2 cur, prev;
+            float3 pos = f3(a3.x, a3.y, a3.z);
+            if (projectToScreen(P.cam, pos, P.width, P.height, cur) &&
+                projectToScreen(P.prev_cam, pos, P.width, P.height, prev)) {
+                A.aov[5 * plane + pix] = make_float4(ex::sub(prev.x, cur.x), ex::sub(prev.y, cur.y), 0.0f, 1.0f);
+            } else {
+                A.aov[5 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        } else {
+            A.aov[0 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            A.aov[1 * plane + pix] = make_float4(0.5f, 0.5f, 0.5f, 0.0f);
+            A.aov[2 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            A.aov[3 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            A.aov[4 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            A.aov[5 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
+// Beauty resolve for readback: (FP64 resolve + FP32 Kahan sum) / samples.
+__global__ void k_resolve_beauty(Accum A, uint32_t pixels, float4* out) {
+    for (uint32_t i = globalId(); i < pixels; i += gridStride()) {
+        uint32_t n = A.count[i];
+        if (n == 0u) {
+            out[i] = make_float4(0, 0, 0, 0);
+            continue;
+        }
+        D4 R = A.resolved[i];
+        float4 s = A.sum[i], c = A.comp[i];
+        double inv = 1.0 / (double)n;
+        out[i] = make_float4((float)((R.x + ((double)s.x - (double)c.x)) * inv), (float)((R.y + ((double)s.y - (double)c.y)) * inv),
+                             (float)((R.z + ((double)s.z - (double)c.z)) * inv), (float)((R.w + ((double)s.w - (double)c.w)) * inv));
+    }
+}
+
+// ------------------------------------------ environment importance table --
+// environmentSamples (Acceleration/LightingGPUEncoding.swift:66-119) with an
+// FP64 weight and prefix sum; stored as FP32 {cdf, pdfSolidAngle}.
+__global__ void k_env_weights(const float4* px, uint32_t w, uint32_t h, float intensity, float maxR, double* weights) {
+    uint32_t n = w * h;
+    double dTheta = 3.141592653589793 / (double)h, dPhi = 2.0 * 3.141592653589793 / (double)w;
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t y = i / w;
+        double theta = ((double)y + 0.5) * dTheta;
+        double solid = fmax(sin(theta) * dTheta * dPhi, 1e-8);
+        float4 t = px[i];
+        double r = (double)t.x * intensity, g = (double)t.y * intensity, b = (double)t.z * intensity;
+        if (maxR > 0.0f) {
+            r = fmin(r, (double)maxR);
+            g = fmin(g, (double)maxR);
+            b = fmin(b, (double)maxR);
+        }
+        double lum = r * 0.2126 + g * 0.7152 + b * 0.0722;
+        weights[i] = fmax(lum, 0.0) * solid;
+    }
+}
+
+// Block-local inclusive scan (FP64) of 1024 elements per block; block totals out.
+__global__ void __launch_bounds__(1024) k_scan_block(double* data, uint32_t n, double* blockSums) {
+    __shared__ double warpSums[32];
+    uint32_t i = blockIdx.x * 1024u + threadIdx.x;
+    double v = i < n ? data[i] : 0.0;
+    for (int o = 1; o < 32; o <<= 1) {
+        double u = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)laneId() >= o) v += u;
+    }
+    if (laneId() == 31u) warpSums[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32u) {
+        double ws = warpSums[threadIdx.x];
+        for (int o = 1; o < 32; o <<= 1) {
+            double u = __shfl_up_sync(0xffffffffu, ws, o);
+            if ((int)threadIdx.x >= o) ws += u;
+        }
+        warpSums[threadIdx.x] = ws;
+    }
+    __syncthreads();
+    if ((threadIdx.x >> 5) > 0u) v += warpSums[(threadIdx.x >> 5) - 1u];
+    if (i < n) data[i] = v;
+    if (threadIdx.x == 1023u) blockSums[blockIdx.x] = v;
+}
+
+// Sequential scan of the (few thousand) block totals, then the finished table.
+__global__ void k_scan_totals(double* blockSums, uint32_t nb) {
+    if (globalId() != 0) return;
+    double acc = 0.0;
+    for (uint32_t b = 0; b < nb; ++b) {
+        double t = blockSums[b];
+        blockSums[b] = acc;
+        acc += t;
+    }
+    blockSums[nb] = acc;
+}
+
+__global__ void k_env_finish(const double* prefix, const double* blockSums, const double* weights, uint32_t w,
+                             uint32_t h, uint32_t nb, float2* out) {
+    uint32_t n = w * h;
+    double total = blockSums[nb];
+    double dTheta = 3.141592653589793 / (double)h, dPhi = 2.0 * 3.141592653589793 / (double)w;
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        double cum = prefix[i] + blockSums[i >> 10];
+        uint32_t y = i / w;
+        double theta = ((double)y + 0.5) * dTheta;
+        double solid = fmax(sin(theta) * dTheta * dPhi, 1e-8);
+        double prob = weights[i] / total;
+        out[i] = make_float2((float)fmin(cum / total, 1.0), (float)(prob / solid));
+    }
+}
+
+}  // namespace dk
+
+// =========================================================== launchers =====
+namespace dk {
+
+int kernelGrid(int which, int smCount) {
+    int perSM = 1;
+    switch (which) {
+        case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_generate, 256, 0); break;
+        case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend, 128, 0); break;
+        case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 128, 0); break;
+        case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow, 128, 0); break;
+        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_finalize, 256, 0); break;
+    }
+    return (perSM < 1 ? 1 : perSM) * smCount;
+}
+
+cudaError_t launchGenerate(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
+    k_generate<<<grid, 256, 0, st>>>(S, P, W);
+    return cudaGetLastError();
+}
+cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st) {
+    k_extend<<<grid, 128, 0, st>>>(S, W, sel);
+    return cudaGetLastError();
+}
+cudaError_t launchShade(const DevScene& S, const DevParams& P, const Wave& W, uint32_t bounce, uint32_t sel, int grid,
+                        cudaStream_t st) {
+    k_shade<<<grid, 128, 0, st>>>(S, P, W, bounce, sel);
+    return cudaGetLastError();
+}
+cudaError_t launchShadow(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
+    k_shadow<<<grid, 128, 0, st>>>(S, P, W);
+    return cudaGetLastError();
+}
+cudaError_t launchAovPrimary(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
+    k_aov_primary<<<grid, 128, 0, st>>>(S, P, W);
+    return cudaGetLastError();
+}
+cudaError_t launchFinalize(const DevParams& P, const Wave& W, const Accum& A, uint32_t writeAov, int grid,
+                           cudaStream_t st) {
+    k_finalize<<<grid, 256, 0, st>>>(P, W, A, writeAov);
+    return cudaGetLastError();
+}
+cudaError_t launchResolveBeauty(const Accum& A, uint32_t pixels, float4* out, int grid, cudaStream_t st) {
+    k_resolve_beauty<<<grid, 256, 0, st>>>(A, pixels, out);
+    return cudaGetLastError();
+}
+cudaError_t buildEnvironmentTable(const float4* dPixels, uint32_t w, uint32_t h, float intensity, float maxR,
+                                  double* dWeights, double* dPrefix, double* dBlockSums, float2* dOut, int grid,
+                                  cudaStream_t st, double* hostTotal) {
+    uint32_t n = w * h;
+    uint32_t nb = (n + 1023u) / 1024u;
+    k_env_weights<<<grid, 256, 0, st>>>(dPixels, w, h, intensity, maxR, dWeights);
+    cudaError_t e = cudaMemcpyAsync(dPrefix, dWeights, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+    k_scan_block<<<nb, 1024, 0, st>>>(dPrefix, n, dBlockSums);
+    k_scan_totals<<<1, 32, 0, st>>>(dBlockSums, nb);
+    e = cudaMemcpyAsync(hostTotal, dBlockSums + nb, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    if (!(*hostTotal > 0.0)) return cudaSuccess;
+    k_env_finish<<<grid, 256, 0, st>>>(dPrefix, dBlockSums, dWeights, w, h, nb, dOut);
+    return cudaGetLastError();
+}
+
+}  // namespace dk

@@ -1,0 +1,125 @@
+"""ctypes binding of the in-tree sm_103a library (include/denrim_cuda.h).
+
+The library is the only compute path: there is no CPU fallback.  Loading fails
+loudly when the shared object is missing (run `__graft_entry__.build()` or
+`python -m denrimrendererkit_gb300.build`).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from typing import Tuple
+
+import numpy as np
+
+from . import abi
+
+_LIB = None
+_LOCK = threading.Lock()
+
+
+class DenrimError(RuntimeError):
+    """A non-zero dk_status.  `code` maps onto DenrimRendererError
+    (Sources/DenrimRendererKit/Renderer/DenrimRenderer.swift:5-26)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+def lib_path() -> str:
+    from .build import LIB_PATH
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Loads libdenrim_cuda.so and declares every exported signature."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = lib_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise RuntimeError(
+                    f"{path} is missing: the sm_103a library must be built first "
+                    "(python -m denrimrendererkit_gb300.build); there is no CPU fallback")
+            from .build import build
+            build()
+        lib = C.CDLL(path)
+        P = C.c_void_p
+        u32, i32, sz = C.c_uint32, C.c_int, C.c_size_t
+        sig = {
+            "dk_device_open": (i32, [i32]),
+            "dk_device_count": (i32, [C.POINTER(i32)]),
+            "dk_session_create": (i32, [C.POINTER(abi.Scene), C.POINTER(abi.Settings), C.POINTER(P)]),
+            "dk_session_render": (i32, [P, u32]),
+            "dk_session_render_tile": (i32, [P, u32, u32, u32, u32, i32]),
+            "dk_session_update_camera": (i32, [P, C.POINTER(abi.Camera), C.POINTER(abi.Camera)]),
+            "dk_session_reset": (i32, [P]),
+            "dk_session_read_output": (i32, [P, i32, P, sz]),
+            "dk_session_sample_count": (i32, [P, C.POINTER(u32)]),
+            "dk_session_stats": (i32, [P, C.POINTER(abi.Stats)]),
+            "dk_session_destroy": (i32, [P]),
+            "dk_last_error_message": (C.c_char_p, []),
+            "dk_build_bvh": (i32, [P, u32, u32, P, C.POINTER(u32), P]),
+            "dk_build_lights": (i32, [P, u32, P, u32, P, C.POINTER(u32)]),
+            "dk_build_environment_samples": (i32, [P, u32, u32, C.c_float, C.c_float, P, C.POINTER(u32)]),
+            "dk_version": (C.c_char_p, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+        return lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = load().dk_last_error_message()
+        raise DenrimError(rc, msg.decode() if msg else "")
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    check(load().dk_device_count(C.byref(n)))
+    return n.value
+
+
+def build_bvh(triangles: np.ndarray, max_leaf: int = 4) -> Tuple[np.ndarray, np.ndarray]:
+    """dk_build_bvh: BVHBuilder + BVHFlattener (BVHBuilder.swift, FlatBVH.swift)."""
+    n = len(triangles)
+    if n == 0:
+        return np.zeros(0, abi.NODE_DTYPE), np.zeros(0, np.uint32)
+    tris = np.ascontiguousarray(triangles)
+    nodes = np.zeros(2 * n, abi.NODE_DTYPE)
+    prim = np.zeros(n, np.uint32)
+    count = C.c_uint32(0)
+    check(load().dk_build_bvh(tris.ctypes.data, n, max_leaf, nodes.ctypes.data, C.byref(count), prim.ctypes.data))
+    return nodes[: count.value].copy(), prim
+
+
+def build_lights(triangles: np.ndarray, materials: np.ndarray) -> np.ndarray:
+    """dk_build_lights: emissive-triangle records; tags `triangles` in place."""
+    n = len(triangles)
+    lights = np.zeros(max(n, 1), abi.LIGHT_DTYPE)
+    count = C.c_uint32(0)
+    if n == 0 or len(materials) == 0:
+        return lights[:0].copy()
+    assert triangles.flags["C_CONTIGUOUS"] and materials.flags["C_CONTIGUOUS"]
+    check(load().dk_build_lights(triangles.ctypes.data, n, materials.ctypes.data, len(materials),
+                                 lights.ctypes.data, C.byref(count)))
+    return lights[: count.value].copy()
+
+
+def build_environment_samples(texture, intensity: float, max_radiance: float) -> np.ndarray:
+    """dk_build_environment_samples: the HDRI importance table (FP64 prefix sum on the GPU)."""
+    px = np.ascontiguousarray(np.asarray(texture.pixels, np.float32).reshape(-1, 4))
+    n = texture.width * texture.height
+    out = np.zeros(max(n, 1), abi.ENVIRONMENT_SAMPLE_DTYPE)
+    count = C.c_uint32(0)
+    check(load().dk_build_environment_samples(px.ctypes.data, texture.width, texture.height, float(intensity),
+                                              float(max_radiance), out.ctypes.data, C.byref(count)))
+    return out[: count.value].copy()

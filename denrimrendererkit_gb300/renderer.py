@@ -1,0 +1,177 @@
+"""Python mirror of the reference's render API over the C ABI.
+
+* `RenderQuality`, `RenderSettings` (Renderer/RenderSettings.swift:5-116)
+* `RenderOutput` (Renderer/RenderOutput.swift:4-25)
+* `DenrimRenderer.make_session` (Renderer/DenrimRenderer.swift:253-292)
+* `RenderSession.render / render_next_sample / render_next_tile /
+  update_camera / reset_accumulation / pixels` (Renderer/RenderSession.swift)
+
+Every call goes through libdenrim_cuda.so; errors raise `DenrimError` with the
+status code that maps onto `DenrimRendererError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import enum
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import abi, library
+from .scene import AccelerationBuild, Camera, RenderScene, compile_scene
+
+
+class RenderQuality(enum.IntEnum):
+    PREVIEW = 0
+    INTERACTIVE = 1
+    FINAL = 2
+
+    @property
+    def default_sample_radiance_clamp(self) -> float:  # RenderSettings.swift:16-25
+        return {0: 10.0, 1: 24.0, 2: 64.0}[int(self)]
+
+
+class RenderOutput(enum.IntEnum):
+    BEAUTY = 0
+    DEPTH = 1
+    NORMAL = 2
+    ALBEDO = 3
+    MATERIAL_ID = 4
+    OBJECT_ID = 5
+    MOTION_VECTOR = 6
+
+
+@dataclasses.dataclass
+class RenderSettings:
+    width: int = 512
+    height: int = 512
+    max_bounces: int = 4
+    quality: RenderQuality = RenderQuality.FINAL
+    previous_camera: Optional[Camera] = None
+    transparent_background: bool = False
+    shows_environment_background: bool = True
+    background_color: Sequence[float] = (0.0, 0.0, 0.0)
+    denoise: bool = False
+    sample_radiance_clamp: Optional[float] = None
+    collects_traversal_stats: bool = False
+    frame_seed: int = 0x1234ABCD  # RenderSession.swift:917
+    max_samples_per_launch: int = 0
+
+    @property
+    def resolved_sample_radiance_clamp(self) -> float:
+        if self.sample_radiance_clamp is not None:
+            return float(self.sample_radiance_clamp)
+        return RenderQuality(self.quality).default_sample_radiance_clamp
+
+
+def make_settings_struct(settings: RenderSettings, camera: Camera) -> abi.Settings:
+    s = abi.Settings()
+    s.width, s.height = settings.width, settings.height
+    s.max_bounces = max(1, settings.max_bounces)
+    s.quality = int(settings.quality)
+    s.transparent_background = int(settings.transparent_background)
+    s.shows_environment_background = int(settings.shows_environment_background)
+    for i in range(3):
+        s.background_color[i] = float(settings.background_color[i])
+    s.sample_radiance_clamp_set = 1
+    s.sample_radiance_clamp = settings.resolved_sample_radiance_clamp
+    s.frame_seed = settings.frame_seed & 0xFFFFFFFF
+    s.denoiser_enabled = int(settings.denoise)
+    s.collects_traversal_stats = int(settings.collects_traversal_stats)
+    s.camera = camera.gpu_camera(settings.width, settings.height)
+    prev = settings.previous_camera or camera
+    s.previous_camera = prev.gpu_camera(settings.width, settings.height)
+    s.max_samples_per_launch = settings.max_samples_per_launch
+    return s
+
+
+class RenderSession:
+    """A compiled scene resident on the GPU with its progressive accumulation."""
+
+    def __init__(self, build: AccelerationBuild, settings: RenderSettings, camera: Camera):
+        self._lib = library.load()
+        self.settings = settings
+        self.camera = camera
+        self._build = build
+        self._handle = C.c_void_p()
+        scene_struct = build.as_struct()
+        settings_struct = make_settings_struct(settings, camera)
+        library.check(self._lib.dk_session_create(C.byref(scene_struct), C.byref(settings_struct),
+                                                  C.byref(self._handle)))
+
+    # RenderSession.render(samples:) (RenderSession.swift:1010-1017)
+    def render(self, samples: int) -> None:
+        if samples < 0:
+            raise ValueError("Invalid render scene: Sample count must not be negative.")
+        library.check(self._lib.dk_session_render(self._handle, samples))
+
+    def render_next_sample(self) -> None:
+        self.render(1)
+
+    # RenderSession.renderNextTile(_:completesSample:) (RenderSession.swift:875-889)
+    def render_next_tile(self, x: int, y: int, width: int, height: int, completes_sample: bool) -> None:
+        library.check(self._lib.dk_session_render_tile(self._handle, x, y, width, height, int(completes_sample)))
+
+    # RenderSession.updateCamera(_:previousCamera:) (RenderSession.swift:595-608)
+    def update_camera(self, camera: Camera, previous_camera: Optional[Camera] = None) -> None:
+        cur = camera.gpu_camera(self.settings.width, self.settings.height)
+        prev = (previous_camera or self.camera).gpu_camera(self.settings.width, self.settings.height)
+        library.check(self._lib.dk_session_update_camera(self._handle, C.byref(cur), C.byref(prev)))
+        self.camera = camera
+
+    def reset_accumulation(self) -> None:
+        library.check(self._lib.dk_session_reset(self._handle))
+
+    @property
+    def sample_count(self) -> int:
+        n = C.c_uint32(0)
+        library.check(self._lib.dk_session_sample_count(self._handle, C.byref(n)))
+        return n.value
+
+    def stats(self) -> abi.Stats:
+        st = abi.Stats()
+        library.check(self._lib.dk_session_stats(self._handle, C.byref(st)))
+        return st
+
+    # RenderSession.pixels(for:) (RenderSession.swift:1037-1039): (H, W, 4) float32
+    def pixels(self, output: RenderOutput = RenderOutput.BEAUTY, out: Optional[np.ndarray] = None) -> np.ndarray:
+        w, h = self.settings.width, self.settings.height
+        if out is None:
+            out = np.empty((h, w, 4), np.float32)
+        assert out.dtype == np.float32 and out.flags["C_CONTIGUOUS"] and out.size == w * h * 4
+        library.check(self._lib.dk_session_read_output(self._handle, int(output), out.ctypes.data, w * h))
+        return out
+
+    def close(self) -> None:
+        if self._handle:
+            self._lib.dk_session_destroy(self._handle)
+            self._handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class DenrimRenderer:
+    """Entry point (Renderer/DenrimRenderer.swift:28-292) for CUDA sessions."""
+
+    def __init__(self, device: int = 0):
+        lib = library.load()
+        library.check(lib.dk_device_open(device))
+        self.device = device
+
+    def make_session(self, scene: RenderScene, settings: RenderSettings,
+                     build: Optional[AccelerationBuild] = None) -> RenderSession:
+        if settings.width <= 0 or settings.height <= 0:
+            raise library.DenrimError(3, "Invalid render scene: Render dimensions must be positive.")
+        build = build or compile_scene(scene)
+        return RenderSession(build, settings, scene.camera)

@@ -1,0 +1,181 @@
+"""Seeded synthetic scenes: the benchmark configurations and the reference's
+own test scenes.
+
+* `cornell_small()`  — the small plain-method configuration: a Cornell-style box
+  of 5 Lambert quads (albedo 0.73, red/green side walls), a 0.25 x 0.25
+  emissive ceiling quad (radiance 17, 12, 4) and a subdivision-3 icosphere
+  (1,280 triangles, r = 0.3) with the `matte.clay` preset
+  (Scene/BuiltInMaterialLibrary.swift:62-67); pinhole camera, fov 40 degrees,
+  320x180, 16 spp, 8 bounces, frame seed 1.
+* `spheres_large()`  — the large plain-method configuration: 64 seeded
+  noise-displaced subdivision-5 icospheres (20,480 triangles each), a 2-tri
+  ground plane, 16 emissive triangles, a 2048x1024 HDRI with log-normal texel
+  luminance (mu 0, sigma 1.5) and a 2-degree sun of 1e4x peak; materials drawn
+  uniformly from diffuse / GGX metal (roughness U[0.05, 0.8]) / dielectric
+  (IOR 1.5) / clearcoat; 1920x1080, 64 spp, 12 bounces, maxRadiance and the
+  sample clamp both off so the sun is not clipped.
+* `cornell_box_reference()`, `parity_quad_scene()`,
+  `reused_mesh_instance_scene()` — RenderScene.cornellBox
+  (Scene/RenderScene.swift:324-380) and the scenes of
+  Tests/DenrimRendererKitTests/HardwareTraversalParityTests.swift:168-224.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from .renderer import RenderQuality, RenderSettings
+from .scene import Camera, Environment, Material, Mesh, RenderScene, Texture2D, Transform, icosphere
+
+f32 = np.float32
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    scene: RenderScene
+    settings: RenderSettings
+    samples: int
+
+
+MATTE_CLAY = dict(base_color=(0.78, 0.62, 0.48), roughness=0.82, specular=0.25)
+
+
+def cornell_small(width: int = 320, height: int = 180, samples: int = 16) -> Workload:
+    scene = RenderScene(camera=Camera((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), vertical_field_of_view_degrees=40.0))
+    grey = scene.add_material(Material(base_color=(0.73, 0.73, 0.73), specular=0.0))
+    red = scene.add_material(Material(base_color=(0.65, 0.05, 0.05), specular=0.0))
+    green = scene.add_material(Material(base_color=(0.12, 0.45, 0.15), specular=0.0))
+    light = scene.add_material(Material(base_color=(1.0, 1.0, 1.0), emission=(17.0, 12.0, 4.0), emission_strength=1.0))
+    clay = scene.add_material(Material(**MATTE_CLAY))
+    scene.add(Mesh.quad((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)), grey)      # floor
+    scene.add(Mesh.quad((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)), grey)      # ceiling
+    scene.add(Mesh.quad((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)), grey)    # back
+    scene.add(Mesh.quad((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)), red)     # left
+    scene.add(Mesh.quad((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)), green)       # right
+    scene.add(Mesh.quad((-0.125, 1.99, -0.125), (0.125, 1.99, -0.125), (0.125, 1.99, 0.125),
+                        (-0.125, 1.99, 0.125)), light)
+    scene.add(icosphere(3, 0.3), clay, Transform.translation((0.0, 0.3, 0.0)))
+    settings = RenderSettings(width=width, height=height, max_bounces=8, quality=RenderQuality.FINAL,
+                              frame_seed=1)
+    return Workload("cornell-small-320x180-16spp", scene, settings, samples)
+
+
+def _displaced_icosphere(rng: np.random.Generator, subdivisions: int, radius: float, amplitude: float) -> Mesh:
+    base = icosphere(subdivisions, 1.0)
+    v = base.vertices.astype(np.float64)
+    dirs = rng.normal(size=(4, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    freq = rng.uniform(2.0, 7.0, size=4)
+    phase = rng.uniform(0.0, 2 * math.pi, size=4)
+    noise = np.sin((v @ dirs.T) * freq + phase).sum(axis=1) / 4.0
+    pos = v * (radius * (1.0 + amplitude * noise))[:, None]
+    tri = base.indices.reshape(-1, 3).astype(np.int64)
+    fn = np.cross(pos[tri[:, 1]] - pos[tri[:, 0]], pos[tri[:, 2]] - pos[tri[:, 0]])
+    vn = np.zeros_like(pos)
+    for k in range(3):
+        np.add.at(vn, tri[:, k], fn)
+    vn /= np.linalg.norm(vn, axis=1, keepdims=True)
+    return Mesh(pos.astype(f32), base.indices, normals=vn.astype(f32))
+
+
+def synthetic_hdri(width: int = 2048, height: int = 1024, seed: int = 2, sigma: float = 1.5,
+                   sun_peak: float = 1.0e4, sun_radius_deg: float = 1.0,
+                   sun_dir=(0.45, 0.55, -0.70)) -> Texture2D:
+    """Equirectangular HDRI with log-normal texel luminance and a sun disc of
+    `sun_peak` times the log-normal level, in the reference's mapping
+    (u = atan2(z, x) / 2pi + 0.5, v = acos(y) / pi; PathTrace.metal:3785-3787)."""
+    rng = np.random.default_rng(seed)
+    lum = np.exp(rng.normal(0.0, sigma, size=(height, width)))
+    tint = np.stack([np.full_like(lum, 1.0), np.full_like(lum, 0.95), np.full_like(lum, 1.1)], axis=-1)
+    y = (np.arange(height) + 0.5) / height
+    x = (np.arange(width) + 0.5) / width
+    theta = y[:, None] * math.pi
+    phi = (x[None, :] - 0.5) * 2 * math.pi
+    d = np.stack([np.cos(phi) * np.sin(theta), np.cos(theta) * np.ones_like(phi), np.sin(phi) * np.sin(theta)], -1)
+    s = np.asarray(sun_dir, np.float64)
+    s /= np.linalg.norm(s)
+    cosang = d @ s
+    sun = cosang >= math.cos(math.radians(sun_radius_deg))
+    lum = np.where(sun, lum * sun_peak, lum)
+    rgb = lum[..., None] * tint
+    px = np.concatenate([rgb, np.ones((height, width, 1))], axis=-1).astype(f32).reshape(-1, 4)
+    return Texture2D(width, height, px, sampling_mode=1)
+
+
+def spheres_large(width: int = 1920, height: int = 1080, samples: int = 64, seed: int = 7,
+                  subdivisions: int = 5, hdri_size=(2048, 1024)) -> Workload:
+    rng = np.random.default_rng(seed)
+    env = Environment(texture=synthetic_hdri(*hdri_size), intensity=1.0, rotation_y=0.0, max_radiance=0.0)
+    scene = RenderScene(camera=Camera((0.0, 5.5, 10.5), (0.0, 0.4, 0.0), vertical_field_of_view_degrees=40.0),
+                        environment=env)
+    ground = scene.add_material(Material(base_color=(0.55, 0.55, 0.52), roughness=0.9, specular=0.2))
+    scene.add(Mesh.quad((-12, 0, 12), (12, 0, 12), (12, 0, -12), (-12, 0, -12)), ground)
+    families = ("diffuse", "metal", "dielectric", "clearcoat")
+    for i in range(64):
+        fam = families[int(rng.integers(0, 4))]
+        col = tuple(float(c) for c in rng.uniform(0.2, 0.95, size=3))
+        if fam == "diffuse":
+            m = Material(base_color=col, roughness=0.8, specular=0.0)
+        elif fam == "metal":
+            m = Material(base_color=col, metallic=1.0, roughness=float(rng.uniform(0.05, 0.8)))
+        elif fam == "dielectric":
+            m = Material(base_color=(1.0, 1.0, 1.0), roughness=0.0, transmission=1.0, index_of_refraction=1.5)
+        else:
+            m = Material(base_color=col, roughness=0.5, clearcoat=1.0, clearcoat_roughness=0.05)
+        mi = scene.add_material(m)
+        gx, gz = i % 8, i // 8
+        center = (-4.2 + 1.2 * gx, 0.5, -4.2 + 1.2 * gz)
+        mesh = _displaced_icosphere(rng, subdivisions, 0.45, 0.08)
+        scene.add(mesh, mi, Transform.translation(center))
+    warm = scene.add_material(Material(base_color=(1, 1, 1), emission=(1.0, 0.8, 0.6), emission_strength=40.0))
+    cool = scene.add_material(Material(base_color=(1, 1, 1), emission=(0.6, 0.75, 1.0), emission_strength=40.0))
+    for k in range(8):
+        cx, cz = -3.5 + k, -2.0 + 1.5 * (k % 3)
+        h = 0.15
+        scene.add(Mesh.quad((cx - h, 3.5, cz - h), (cx + h, 3.5, cz - h), (cx + h, 3.5, cz + h), (cx - h, 3.5, cz + h)),
+                  warm if k % 2 == 0 else cool)
+    settings = RenderSettings(width=width, height=height, max_bounces=12, quality=RenderQuality.FINAL,
+                              sample_radiance_clamp=0.0, frame_seed=1)
+    return Workload(f"spheres-large-{width}x{height}-{samples}spp", scene, settings, samples)
+
+
+def cornell_box_reference(width: int = 24, height: int = 24) -> Workload:
+    """RenderScene.cornellBox() (Scene/RenderScene.swift:324-380)."""
+    scene = RenderScene(camera=Camera((0, 1, 3.4), (0, 1, 0), vertical_field_of_view_degrees=42.0))
+    white = scene.add_material(Material(base_color=(0.78, 0.78, 0.74)))
+    red = scene.add_material(Material(base_color=(0.65, 0.05, 0.04)))
+    green = scene.add_material(Material(base_color=(0.12, 0.45, 0.15)))
+    light = scene.add_material(Material(base_color=(1, 1, 1), emission=(1, 0.86, 0.62), emission_strength=14.0))
+    scene.add(Mesh.quad((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)), white)
+    scene.add(Mesh.quad((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)), white)
+    scene.add(Mesh.quad((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)), white)
+    scene.add(Mesh.quad((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)), red)
+    scene.add(Mesh.quad((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)), green)
+    scene.add(Mesh.quad((-0.28, 1.99, -0.25), (0.28, 1.99, -0.25), (0.28, 1.99, 0.25), (-0.28, 1.99, 0.25)), light)
+    return Workload("cornell-box-reference", scene, RenderSettings(width=width, height=height, max_bounces=1), 1)
+
+
+def parity_quad_scene(width: int = 16, height: int = 16) -> Workload:
+    """HardwareTraversalParityTests.parityScene (:168-183)."""
+    scene = RenderScene(camera=Camera((0, 0, 2), (0, 0, 0), vertical_field_of_view_degrees=34.0))
+    m = scene.add_material(Material(base_color=(0.25, 0.5, 0.75)))
+    scene.add(Mesh.quad((-1, -1, 0), (1, -1, 0), (1, 1, 0), (-1, 1, 0)), m)
+    return Workload("parity-quad", scene, RenderSettings(width=width, height=height, max_bounces=1), 1)
+
+
+def reused_mesh_instance_scene(width: int = 40, height: int = 40) -> Workload:
+    """HardwareTraversalParityTests.reusedMeshInstanceScene (:185-224)."""
+    scene = RenderScene(camera=Camera((0, 0.7, 3.8), (0, 0.35, 0), vertical_field_of_view_degrees=42.0))
+    floor = scene.add_material(Material(base_color=(0.45, 0.47, 0.48)))
+    red = scene.add_material(Material(base_color=(0.9, 0.2, 0.12)))
+    blue = scene.add_material(Material(base_color=(0.16, 0.38, 0.9)))
+    green = scene.add_material(Material(base_color=(0.2, 0.8, 0.32)))
+    subject = Mesh.box((-0.275, -0.35, -0.225), (0.275, 0.35, 0.225))
+    scene.add(Mesh.quad((-2.2, 0, 2.0), (2.2, 0, 2.0), (2.2, 0, -1.5), (-2.2, 0, -1.5)), floor)
+    scene.add(subject, red, Transform.translation((-0.8, 0.35, 0)) * Transform.rotation_y(-0.25))
+    scene.add(subject, blue, Transform.translation((0, 0.35, 0.02)) * Transform.rotation_y(0.12))
+    scene.add(subject, green, Transform.translation((0.8, 0.35, -0.04)) * Transform.rotation_y(0.32))
+    return Workload("reused-mesh-instances", scene, RenderSettings(width=width, height=height, max_bounces=1), 1)

@@ -1,0 +1,330 @@
+/*
+ * denrim_cuda.h — C ABI of the GB300 (sm_103a) progressive path-tracing backend.
+ *
+ * This header is the drop-in seam for DenrimRendererKit's `final`-quality path
+ * tracer.  The reference binds its GPU work in `RenderSession.init`
+ * (Sources/DenrimRendererKit/Renderer/RenderSession.swift:292-579), which turns a
+ * `RenderScene` into an `AccelerationBuild`
+ * (Sources/DenrimRendererKit/Acceleration/AccelerationBuild.swift:4-48) and then
+ * dispatches `pathTraceKernel`
+ * (Sources/DenrimRendererKit/Resources/Shaders/PathTrace.metal:5167-5586) once per
+ * sample from `RenderSession.encodeNextSample` (RenderSession.swift:891-1007).
+ *
+ * The functions below receive exactly the `AccelerationBuild` arrays as plain
+ * old data with the byte layouts of Sources/DenrimRendererKit/Metal/GPUTypes.swift,
+ * so a Swift `RenderSession` (or any other host) can hand its arrays over
+ * unchanged.  Every function returns an `int` status (dk_status); the message of
+ * the last failure on the calling thread is returned by dk_last_error_message().
+ *
+ * Threading: one session is single-threaded (the reference `RenderSession` is a
+ * non-Sendable class); different sessions may be used from different threads.
+ */
+#ifndef DENRIM_CUDA_H
+#define DENRIM_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------- */
+/* Status codes.  1..5 map one-to-one onto `DenrimRendererError`             */
+/* (Sources/DenrimRendererKit/Renderer/DenrimRenderer.swift:5-26).           */
+/* ------------------------------------------------------------------------- */
+typedef enum dk_status {
+    DK_OK = 0,
+    DK_ERROR_NO_DEVICE = 1,          /* noMetalDevice: no usable CUDA device          */
+    DK_ERROR_MISSING_KERNEL = 2,     /* missingShaderFunction: kernel image absent    */
+    DK_ERROR_INVALID_SCENE = 3,      /* invalidScene(reason)                          */
+    DK_ERROR_COMMAND_FAILED = 4,     /* commandBufferFailed: a launch or copy failed  */
+    DK_ERROR_EXPORT_FAILED = 5,      /* pngExportFailed                               */
+    DK_ERROR_INVALID_ARGUMENT = 6,   /* null pointer, bad size or bad enum value      */
+    DK_ERROR_OUT_OF_MEMORY = 7,      /* device allocation refused                     */
+    DK_ERROR_DEVICE_TIMEOUT = 8      /* a bounded device-side wait gave up            */
+} dk_status;
+
+/* ------------------------------------------------------------------------- */
+/* GPU struct ABI (GPUTypes.swift).  Sizes are checked by static asserts in  */
+/* the library and by the Python ctypes mirror.                              */
+/* ------------------------------------------------------------------------- */
+typedef struct dk_float4 { float x, y, z, w; } dk_float4;
+typedef struct dk_uint4 { uint32_t x, y, z, w; } dk_uint4;
+
+/* GPUCamera, 80 B (GPUTypes.swift:4-10): origin.w = 1 for orthographic;
+ * lens = {apertureRadius, focusDistance, 0, 0}. */
+typedef struct dk_camera {
+    dk_float4 origin;
+    dk_float4 lower_left;
+    dk_float4 horizontal;
+    dk_float4 vertical;
+    dk_float4 lens;
+} dk_camera;
+
+/* GPUTriangle, 192 B (GPUTypes.swift:12-28).  padding2 = light index + 1
+ * (LightingGPUEncoding.swift:52) or 0 for a non-emissive triangle. */
+typedef struct dk_triangle {
+    dk_float4 v0, v1, v2;
+    dk_float4 n0, n1, n2;
+    dk_float4 uv0, uv1, uv2;
+    dk_float4 tangent, bitangent;
+    uint32_t material_id;
+    uint32_t object_id;
+    uint32_t primitive_id;
+    uint32_t padding2;
+} dk_triangle;
+
+/* GPUMaterial, 17 x float4 = 272 B (GPUTypes.swift:30-48); the packing of the
+ * user-facing fields is `Material.gpuMaterial` (Scene/Material.swift:222-284). */
+typedef struct dk_material {
+    dk_float4 base_color;              /* xyz base colour, w opacity                     */
+    dk_float4 emission;                /* xyz emission*strength, w transmission          */
+    dk_float4 parameters;              /* roughness, metallic, baseTex+1, normalMap+1    */
+    dk_float4 parameters2;             /* specular, ior, clearcoat, clearcoatRoughness   */
+    dk_float4 specular_color;          /* xyz tint, w clearcoat ior                      */
+    dk_float4 sheen_color;             /* xyz tint, w sheen                              */
+    dk_float4 transmission_color;      /* xyz tint, w thinWalled (0/1)                   */
+    dk_float4 parameters3;             /* sheenRough, transRough, transIOR, anisotropy   */
+    dk_float4 clearcoat_color;
+    dk_float4 clearcoat_attenuation;   /* xyz colour, w thickness                        */
+    dk_float4 transmission_absorption; /* xyz colour, w distance                         */
+    dk_float4 thin_film;               /* strength, thickness nm, ior, 0                 */
+    dk_float4 subsurface_color;        /* xyz colour, w subsurface                       */
+    dk_float4 subsurface_radius;       /* xyz radius, w scale                            */
+    dk_float4 subsurface_parameters;   /* anisotropy, 0, 0, 0                            */
+    dk_float4 volume_scattering;       /* xyz colour, w scattering                       */
+    dk_float4 volume_parameters;       /* distance, anisotropy, 0, 0                     */
+} dk_material;
+
+/* GPUAccelerationNode, 48 B (GPUTypes.swift:137-141, FlatBVH.swift:21-32):
+ * metadata = {left, right, firstPrimitive, primitiveCount}; leaf iff count > 0. */
+typedef struct dk_bvh_node {
+    dk_float4 bounds_min;
+    dk_float4 bounds_max;
+    dk_uint4 metadata;
+} dk_bvh_node;
+
+/* GPUTextureDescriptor, 16 B: {pixelOffset, width, height, samplingMode}
+ * (MaterialGPUEncoding.swift:26-33); samplingMode 0 nearest, 1 linear. */
+typedef struct dk_texture_descriptor { dk_uint4 metadata; } dk_texture_descriptor;
+
+/* GPULightRecord, 32 B (GPUTypes.swift:54-60). */
+typedef struct dk_light_record {
+    uint32_t triangle_index;
+    uint32_t material_index;
+    float area;
+    float selection_cdf;
+    dk_float4 normal;
+} dk_light_record;
+
+/* GPUEnvironmentSample, 8 B (GPUTypes.swift:62-64): {cdf, pdfSolidAngle}. */
+typedef struct dk_environment_sample { float cdf; float pdf_solid_angle; } dk_environment_sample;
+
+/* GPUVolumeDescriptor, 240 B (GPUTypes.swift:66-82).  Only sparse-brick
+ * volumes (metadata.w == 1) are traced by this backend. */
+typedef struct dk_volume_descriptor {
+    dk_float4 world_bounds_min, world_bounds_max;
+    dk_float4 local_bounds_min, local_bounds_max;
+    dk_uint4 dimensions;
+    dk_uint4 metadata;
+    dk_uint4 material_program;
+    dk_float4 world_to_local[4];
+    dk_float4 normal_transform[4];
+} dk_volume_descriptor;
+
+/* GPUVolumeBrickSample, 16 B (GPUTypes.swift:95). */
+typedef struct dk_volume_brick_sample {
+    float distance;
+    uint32_t material_a;
+    uint32_t material_b;
+    float material_blend;
+} dk_volume_brick_sample;
+
+/* GPUVolumeBrickDescriptor, 128 B (GPUTypes.swift:119-128). */
+typedef struct dk_volume_brick_descriptor {
+    dk_float4 world_bounds_min, world_bounds_max;
+    dk_float4 local_bounds_min, local_bounds_max;
+    dk_float4 sample_bounds_min, sample_bounds_max;
+    dk_uint4 grid_origin_and_volume;
+    dk_uint4 dimensions_and_sample_offset;
+} dk_volume_brick_descriptor;
+
+/* GPUVolumeBrickGrid, 64 B (GPUTypes.swift:130-135). */
+typedef struct dk_volume_brick_grid {
+    dk_uint4 dimensions_and_index_offset;
+    dk_uint4 brick_size_and_volume;
+    dk_uint4 macro_dimensions_and_index_offset;
+    dk_uint4 macro_size_and_reserved;
+} dk_volume_brick_grid;
+
+/* ------------------------------------------------------------------------- */
+/* The scene: the POD arrays of `AccelerationBuild` (AccelerationBuild.swift) */
+/* plus the environment settings that `RenderSession` copies into            */
+/* GPURenderConstants (RenderSession.swift:908-947).  The library copies     */
+/* everything into device memory inside dk_session_create; the caller's      */
+/* arrays may be freed as soon as it returns.                                */
+/* ------------------------------------------------------------------------- */
+typedef struct dk_scene {
+    const dk_triangle* triangles;                 uint32_t triangle_count;
+    const dk_material* materials;                 uint32_t material_count;
+    const dk_bvh_node* nodes;                     uint32_t node_count;
+    const uint32_t* primitive_indices;            uint32_t primitive_index_count;
+    const dk_texture_descriptor* texture_descriptors; uint32_t texture_descriptor_count;
+    const dk_float4* texture_pixels;              uint64_t texture_pixel_count;
+    const dk_light_record* lights;                uint32_t light_count;
+    const dk_environment_sample* environment_samples; uint32_t environment_sample_count;
+    uint32_t environment_texture_index_plus_one;
+    float environment_intensity;                  /* Environment.intensity   */
+    float environment_rotation_y;                 /* Environment.rotationY   */
+    float environment_max_radiance;               /* Environment.maxRadiance */
+    /* Sparse distance-volume bricks (SparseVolumeGPUEncoding.swift:9-299). */
+    const dk_volume_descriptor* volumes;          uint32_t volume_count;
+    const dk_volume_brick_descriptor* volume_bricks; uint32_t volume_brick_count;
+    const dk_volume_brick_sample* volume_brick_samples; uint64_t volume_brick_sample_count;
+    const dk_volume_brick_grid* volume_brick_grids; uint32_t volume_brick_grid_count;
+    const uint32_t* volume_brick_grid_indices;    uint64_t volume_brick_grid_index_count;
+} dk_scene;
+
+/* RenderQuality (RenderSettings.swift:5-26).  Only DK_QUALITY_FINAL selects the
+ * path tracer; the other two are rejected with DK_ERROR_INVALID_ARGUMENT. */
+enum { DK_QUALITY_PREVIEW = 0, DK_QUALITY_INTERACTIVE = 1, DK_QUALITY_FINAL = 2 };
+
+/* RenderSettings (RenderSettings.swift:29-116) plus the two cameras. */
+typedef struct dk_settings {
+    uint32_t width;
+    uint32_t height;
+    uint32_t max_bounces;                 /* clamped to >= 1 like RenderSession.swift:915 */
+    uint32_t quality;                     /* DK_QUALITY_*                                  */
+    uint32_t transparent_background;
+    uint32_t shows_environment_background;
+    float background_color[3];
+    uint32_t sample_radiance_clamp_set;   /* 0: inherit RenderQuality default (64 final)  */
+    float sample_radiance_clamp;          /* used when _set != 0; 0 disables the clamp     */
+    uint32_t frame_seed;                  /* reference hard-wires 0x1234ABCD               */
+    uint32_t denoiser_enabled;            /* 1: trace the unjittered AOV ray (PathTrace.metal:5530-5557) */
+    uint32_t collects_traversal_stats;
+    dk_camera camera;
+    dk_camera previous_camera;
+    uint32_t max_samples_per_launch;      /* 0: the library picks; caps one wavefront batch */
+    uint32_t reserved;
+} dk_settings;
+
+/* RenderOutput (Renderer/RenderOutput.swift:4-25). */
+typedef enum dk_output {
+    DK_OUTPUT_BEAUTY = 0,
+    DK_OUTPUT_DEPTH = 1,
+    DK_OUTPUT_NORMAL = 2,
+    DK_OUTPUT_ALBEDO = 3,
+    DK_OUTPUT_MATERIAL_ID = 4,
+    DK_OUTPUT_OBJECT_ID = 5,
+    DK_OUTPUT_MOTION_VECTOR = 6
+} dk_output;
+
+/* Per-session counters.  The first 13 are the reference's SDF traversal
+ * counters in its slot order (PathTrace.metal:191-203); the rest time and
+ * count this backend's own work. */
+typedef struct dk_stats {
+    uint64_t sdf_counters[13];
+    uint64_t paths_traced;                /* pixel-samples completed since create       */
+    uint64_t rays_extended;               /* closest-hit queries issued                  */
+    uint64_t shadow_rays;                 /* shadow queries issued                       */
+    uint64_t kernel_launches;             /* kernels launched since create               */
+    double last_render_ms;                /* device time of the last dk_session_render  */
+    double last_extend_ms;                /* of which: closest-hit (extend) kernels      */
+    double last_shade_ms;                 /* of which: shading kernels                   */
+    double last_shadow_ms;                /* of which: shadow kernels                    */
+    double last_other_ms;                 /* of which: generate / accumulate / AOV       */
+    uint64_t last_launches;               /* kernels launched by the last render call    */
+    uint64_t device_bytes;                /* device memory held by the session           */
+} dk_stats;
+
+typedef struct dk_session dk_session;
+
+/* ------------------------------------------------------------------------- */
+/* Device and session API.                                                    */
+/* ------------------------------------------------------------------------- */
+
+/* Selects and initialises a CUDA device (DenrimRenderer.init,
+ * DenrimRenderer.swift:52-70).  Returns DK_ERROR_NO_DEVICE when none exists. */
+int dk_device_open(int device_ordinal);
+
+/* Number of CUDA devices visible to the process (0 without a GPU). */
+int dk_device_count(int* out_count);
+
+/* DenrimRenderer.makeSession(scene:settings:accelerationMode:)
+ * (DenrimRenderer.swift:253-292) + RenderSession.init (RenderSession.swift:292-579).
+ * Validation follows RenderSession.swift:304-327: non-positive size, no
+ * geometry or no materials fail with DK_ERROR_INVALID_SCENE. */
+int dk_session_create(const dk_scene* scene, const dk_settings* settings, dk_session** out_session);
+
+/* RenderSession.render(samples:) (RenderSession.swift:1010-1017): adds
+ * `samples` progressive samples over the full frame.  On failure the sample
+ * count is left unchanged (RenderSession.swift:844-847). */
+int dk_session_render(dk_session* session, uint32_t samples);
+
+/* RenderSession.renderNextTile(_:completesSample:) (RenderSession.swift:875-889):
+ * one sample over a tile; the sample index advances only when
+ * completes_sample != 0. */
+int dk_session_render_tile(dk_session* session, uint32_t x, uint32_t y, uint32_t width,
+                           uint32_t height, int completes_sample);
+
+/* RenderSession.updateCamera(_:previousCamera:) (RenderSession.swift:595-608).
+ * `previous` may be NULL: the camera active before the update is used.
+ * Restarts accumulation. */
+int dk_session_update_camera(dk_session* session, const dk_camera* camera, const dk_camera* previous);
+
+/* RenderSession.resetAccumulation() (RenderSession.swift:582-588). */
+int dk_session_reset(dk_session* session);
+
+/* RenderSession.pixels(for:) (RenderSession.swift:1037-1039): copies the
+ * output as RGBA32F into `rgba` (pixel_count = width*height pixels). */
+int dk_session_read_output(dk_session* session, int output, float* rgba, size_t pixel_count);
+
+/* RenderSession.sampleCount. */
+int dk_session_sample_count(const dk_session* session, uint32_t* out_count);
+
+/* RenderSession.sdfTraversalStats() (RenderSession.swift:808-831) plus timing. */
+int dk_session_stats(const dk_session* session, dk_stats* out_stats);
+
+/* Releases every device buffer of the session. */
+int dk_session_destroy(dk_session* session);
+
+/* Message of the last failure on this thread ("" when none). */
+const char* dk_last_error_message(void);
+
+/* ------------------------------------------------------------------------- */
+/* Scene-compile helpers: GB300 restatements of the Swift host builders a    */
+/* caller without them needs in order to fill dk_scene.                      */
+/* ------------------------------------------------------------------------- */
+
+/* BVHBuilder.build(triangles:) + BVHFlattener.flatten
+ * (Acceleration/BVHBuilder.swift:7-92, FlatBVH.swift:13-32): median split on
+ * the largest centroid axis, stable ordering, pre-order node numbering.
+ * `nodes_out` must hold 2*triangle_count nodes, `primitive_indices_out`
+ * triangle_count entries; *node_count receives the node count. */
+int dk_build_bvh(const dk_triangle* triangles, uint32_t triangle_count, uint32_t max_leaf_primitives,
+                 dk_bvh_node* nodes_out, uint32_t* node_count, uint32_t* primitive_indices_out);
+
+/* LinearTriangleAccelerationBackend.lightRecordsAndTaggedTriangles
+ * (Acceleration/LightingGPUEncoding.swift:5-64): writes padding2 = light+1
+ * into `triangles` in place and fills `lights_out` (capacity triangle_count).
+ * *light_count receives the number of emissive-triangle lights. */
+int dk_build_lights(dk_triangle* triangles, uint32_t triangle_count, const dk_material* materials,
+                    uint32_t material_count, dk_light_record* lights_out, uint32_t* light_count);
+
+/* LinearTriangleAccelerationBackend.environmentSamples
+ * (Acceleration/LightingGPUEncoding.swift:66-119), computed on the GPU with an
+ * FP64 prefix sum and stored as FP32.  `out` holds width*height entries;
+ * *out_count is 0 when the map carries no energy (the reference's empty case). */
+int dk_build_environment_samples(const dk_float4* pixels, uint32_t width, uint32_t height, float intensity,
+                                 float max_radiance, dk_environment_sample* out, uint32_t* out_count);
+
+/* Library version string. */
+const char* dk_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DENRIM_CUDA_H */
