@@ -1,0 +1,374 @@
+"""Benchmark: Mpaths/s of the progressive path tracer on one GB300.
+
+Workload (one step = one frame): the large plain-method scene — 64 seeded
+noise-displaced subdivision-5 icospheres (1,310,738 triangles with ground and
+16 emissive triangles), a 2048x1024 log-normal HDRI with a 1e4x sun, mixed
+diffuse / GGX metal / dielectric / clearcoat materials — rendered at 1920x1080,
+64 spp, 12 bounces: 132.7 M paths per step.  A path is one pixel-sample, the
+unit of the reference's pixel-samples/s (Sources/DenrimCLI/main.swift:277-279).
+
+Printed JSON fields:
+  value       device-timed Mpaths/s with the scene resident in HBM (CUDA events
+              on the library's stream around every stage), max over ranks.
+  e2e         the same metric through the C ABI from pinned host buffers: every
+              step creates a session from the host arrays (host->device copy of
+              the scene), renders the frame and reads the beauty image back.
+  roofline    the dominant kernel's algorithmic bytes (the reference algorithm's
+              BVH-node / triangle / material / light / environment bytes, counted
+              by the CPU oracle on a 1/64 pixel subsample and scaled) over its
+              event-timed duration, against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a restatement of the reference shader) on the
+              host cores, on the 1/64 pixel subsample of the same frame.
+`--impl reference` times that CPU implementation alone (the reference's own
+Metal path cannot run on this machine).  `--gpus N` runs N independent
+replicas (one process per GPU, weak scaling): the path has no exchange step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mpaths/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    from denrimrendererkit_gb300 import scenes
+    return scenes.spheres_large(width=args.width, height=args.height, samples=args.spp)
+
+
+def config(args, wl, extra=None):
+    cfg = {"workload": wl.name, "scene": "64 displaced subdiv-5 icospheres + ground + 16 emissive tris, "
+                                        "2048x1024 HDRI (log-normal, 1e4x sun)",
+           "triangles": sum(len(i.mesh.indices) // 3 for i in wl.scene.mesh_instances),
+           "resolution": [args.width, args.height],
+           "spp_per_step": args.spp, "max_bounces": 12, "paths_per_step": args.width * args.height * args.spp,
+           "frame_seed": 1, "sample_radiance_clamp": 0, "environment_max_radiance": 0,
+           "l2": "path state (~3.5 GB) exceeds L2; a 512 MB buffer is also written between steps",
+           "parallelism": "replicas"}
+    cfg.update(extra or {})
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """dram bytes per launch of `kernel` on the bench workload, from the
+    committed ncu summary (profiles/<kernel>_spheres_large.md), else None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_spheres_large.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic_bytes_per_frame:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+# Algorithmic bytes per unit of the reference algorithm (reference layouts):
+# 48 B per BVH node visited, 192 B per triangle tested, 272 B per material
+# fetch, 32+192 B per light sample, 21*8 + 4*16 B per environment sample,
+# 4*16 B per environment lookup.
+def algorithmic_bytes(counters: dict, env_texels: int):
+    search = max(1, int(np.ceil(np.log2(max(env_texels, 2)))))
+    ext = 48 * counters["nodes_ext"] + 192 * counters["tris_ext"]
+    shadow = 48 * counters["nodes_shadow"] + 192 * counters["tris_shadow"]
+    walks = 48 * (counters["nodes_sss"]) + 192 * counters["tris_sss"]
+    shade = (272 * counters["material_fetch"] + (32 + 192) * counters["light_samples"]
+             + (search * 8 + 4 * 16) * counters["env_samples"] + 4 * 16 * counters["env_lookups"] + walks)
+    accum = (16 + 16 + 6 * 16) * counters["paths"]
+    return {"k_extend": ext, "k_shadow": shadow, "k_shade": shade, "k_finalize": accum}
+
+
+def cpu_oracle_sample(wl, build, threads=0):
+    """The FP32 oracle on every 8th pixel in x and y, all spp of the step."""
+    from oracle import oracle as orc
+    orc.build()
+    w, h = wl.settings.width, wl.settings.height
+    ys, xs = np.meshgrid(np.arange(0, h, 8), np.arange(0, w, 8), indexing="ij")
+    pixels = (ys * w + xs).reshape(-1).astype(np.uint32)
+    r = orc.OracleRender(build, wl.settings, wl.scene.camera)
+    t0 = time.perf_counter()
+    r.render(wl.samples, pixel_list=pixels, threads=threads)
+    dt = time.perf_counter() - t0
+    paths = len(pixels) * wl.samples
+    return paths, dt, r.counter_dict(), len(pixels)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from denrimrendererkit_gb300 import compile_scene
+    from oracle import oracle as orc
+    wl = workload(args)
+    build = compile_scene(wl.scene)
+    orc.build()
+    threads = os.cpu_count() or 1
+    w, h = wl.settings.width, wl.settings.height
+    ys, xs = np.meshgrid(np.arange(0, h, 32), np.arange(0, w, 32), indexing="ij")
+    pixels = (ys * w + xs).reshape(-1).astype(np.uint32)
+    times = []
+    for i in range(args.warmup + args.steps):
+        r = orc.OracleRender(build, wl.settings, wl.scene.camera)
+        t0 = time.perf_counter()
+        r.render(wl.samples, pixel_list=pixels, threads=threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    paths = len(pixels) * wl.samples
+    value = paths * len(times) / sum(times) / 1e6
+    sample = f"every 32nd pixel in x and y ({len(pixels)} px) x {wl.samples} spp = {paths} paths per step"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args, wl, {"implementation": "CPU oracle port of the reference shader (the reference's "
+                                                          "Metal path is unavailable on this box)"}),
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def flush_l2(buf):
+    import torch
+    buf.add_(1.0)
+    torch.cuda.synchronize()
+
+
+def run_gb300(args, rank, world, local):
+    import torch
+
+    from denrimrendererkit_gb300 import DenrimRenderer, RenderOutput, compile_scene, library
+    from denrimrendererkit_gb300.renderer import make_settings_struct
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    renderer = DenrimRenderer(local)
+    wl = workload(args)
+    build = compile_scene(wl.scene)
+    paths_per_step = wl.settings.width * wl.settings.height * wl.samples
+    flush = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---------------------------------------------------------- value ----
+    session = renderer.make_session(wl.scene, wl.settings, build=build)
+    for _ in range(args.warmup):
+        session.render(wl.samples)
+        flush_l2(flush)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    dev_ms, stage = 0.0, {"k_extend": 0.0, "k_shade": 0.0, "k_shadow": 0.0, "other": 0.0}
+    launches = 0
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        session.render(wl.samples)
+        st = session.stats()
+        dev_ms += st.last_render_ms
+        stage["k_extend"] += st.last_extend_ms
+        stage["k_shade"] += st.last_shade_ms
+        stage["k_shadow"] += st.last_shadow_ms
+        stage["other"] += st.last_other_ms
+        launches += st.last_launches
+        flush_l2(flush)
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    ms_step = dev_ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms_step], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = paths_per_step * world / (ms_step * 1e3)
+    beauty = session.pixels(RenderOutput.BEAUTY)
+    session.close()
+
+    # ------------------------------------------------------------ e2e ----
+    e2e = None
+    if not args.no_e2e:
+        pinned = {}
+        for name in ("triangles", "texture_pixels", "environment_samples", "nodes", "primitive_indices", "materials",
+                     "lights", "texture_descriptors"):
+            a = getattr(build, name)
+            t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+            t.numpy()[:] = np.frombuffer(np.ascontiguousarray(a).tobytes(), np.uint8)
+            pinned[name] = (t, t.numpy().view(a.dtype).reshape(a.shape))
+        pb = type(build)(**{**build.__dict__, **{k: v[1] for k, v in pinned.items()}})
+        out = torch.empty(wl.settings.width * wl.settings.height * 4 * 4, dtype=torch.uint8, pin_memory=True)
+        out_np = out.numpy().view(np.float32).reshape(wl.settings.height, wl.settings.width, 4)
+        h2d = sum(getattr(build, k).nbytes for k in pinned)
+        d2h = out.numel()
+        lib = library.load()
+        e2e_times = []
+        for i in range(1 + args.steps):
+            barrier()
+            t0 = time.perf_counter()
+            from denrimrendererkit_gb300.renderer import RenderSession
+            s = RenderSession(pb, wl.settings, wl.scene.camera)
+            s.render(wl.samples)
+            s.pixels(RenderOutput.BEAUTY, out=out_np)
+            s.close()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            if i >= 1:
+                e2e_times.append(dt)
+            flush_l2(flush)
+        e2e_s = sum(e2e_times) / len(e2e_times)
+        if world > 1:
+            t = torch.tensor([e2e_s], device=f"cuda:{local}")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": paths_per_step * world / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h),
+               "note": "per step: dk_session_create from pinned host arrays + render 64 spp + beauty readback"}
+        del lib
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+        return
+
+    # ------------------------------------------- CPU baseline + roofline ----
+    cpu = None
+    roof = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        paths, dt, counters, npx = cpu_oracle_sample(wl, build, threads)
+        scale = paths_per_step / paths
+        alg = algorithmic_bytes(counters, build.environment_samples.shape[0])
+        per_frame = {k: v * scale for k, v in alg.items()}
+        cpu = {"value": paths / dt / 1e6, "unit": METRIC, "cores": threads, "kind": "port",
+               "sample": f"every 8th pixel in x and y ({npx} px) x {wl.samples} spp = {paths} paths "
+                         f"(1/64 of a step), FP32 oracle, {dt:.1f} s"}
+        kernel_ms = {k: stage[k] / args.steps for k in ("k_extend", "k_shade", "k_shadow")}
+        dom = max(kernel_ms, key=kernel_ms.get)
+        peak, kind = measured_peaks()
+        achieved = per_frame[dom] / (kernel_ms[dom] * 1e-3) / 1e9
+        traffic = profile_traffic(dom)
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured"
+                else "fallback 6.8 TB/s", "traffic": traffic,
+                "algorithmic_bytes_per_step": {k: float(v) for k, v in per_frame.items()},
+                "kernel_ms_per_step": kernel_ms,
+                "per_path": {k: float(v) / paths for k, v in counters.items() if k != "paths"}}
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args, wl), "clocks": clk, "gpu_launches": int(launches), "e2e": e2e,
+            "roofline": roof, "cpu_baseline": cpu, "wall_s_timed": wall,
+            "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+            "beauty_mean": float(beauty[..., :3].mean())}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gb300(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,197 @@
+"""GPU parity: the sm_103a path through the C ABI against the CPU oracle.
+
+Bar (stated per output):
+* depth, normal, albedo, material-ID, object-ID and motion-vector AOVs: bit-exact
+  (every float equal) -- they depend only on the RNG stream, the camera ray and
+  the hit selection, all computed with correctly rounded IEEE operations;
+* beauty: the same RNG streams drive both sides, so paths agree except where a
+  transcendental's last-bit difference flips a later branch.  Tolerances:
+  relative RMSE <= 1e-3 on the small scenes and <= 2e-2 on the large-scene
+  sample (reference backend-parity metric: HardwareTraversalParityTests.swift
+  average beauty difference <= 5e-4), plus the mean over the image within 1%.
+"""
+import numpy as np
+import pytest
+
+from denrimrendererkit_gb300 import DenrimRenderer, RenderOutput, compile_scene, scenes
+from denrimrendererkit_gb300.renderer import RenderSettings
+
+pytestmark = pytest.mark.gpu
+
+AOVS = (RenderOutput.DEPTH, RenderOutput.NORMAL, RenderOutput.ALBEDO, RenderOutput.MATERIAL_ID,
+        RenderOutput.OBJECT_ID, RenderOutput.MOTION_VECTOR)
+
+
+@pytest.fixture(scope="module")
+def renderer(dk_lib):
+    return DenrimRenderer(0)
+
+
+def run_pair(renderer, oracle_lib, wl, samples, pixel_list=None, render_calls=1):
+    b = compile_scene(wl.scene)
+    s = renderer.make_session(wl.scene, wl.settings, build=b)
+    per = samples // render_calls
+    for _ in range(render_calls):
+        s.render(per)
+    o = oracle_lib.OracleRender(b, wl.settings, wl.scene.camera)
+    o.render(samples, pixel_list=pixel_list)
+    return s, o, b
+
+
+def assert_aovs_bit_exact(s, o, pixel_list=None):
+    for kind in AOVS:
+        g = s.pixels(kind).reshape(-1, 4)
+        c = o.aov[int(kind) - 1].reshape(-1, 4)
+        if pixel_list is not None:
+            g, c = g[pixel_list], c[pixel_list]
+        bad = (g.view(np.uint32) != c.view(np.uint32)).any(axis=-1)
+        assert not bad.any(), f"{kind.name}: {int(bad.sum())} pixels differ"
+
+
+def beauty_stats(s, o, pixel_list=None):
+    g = s.pixels(RenderOutput.BEAUTY).reshape(-1, 4).astype(np.float64)
+    c = o.accum.reshape(-1, 4)
+    if pixel_list is not None:
+        g, c = g[pixel_list], c[pixel_list]
+    rel = np.sqrt(((g[:, :3] - c[:, :3]) ** 2).mean()) / max(c[:, :3].mean(), 1e-12)
+    return rel, g, c
+
+
+@pytest.mark.parametrize("maker", [scenes.parity_quad_scene, scenes.cornell_box_reference,
+                                   scenes.reused_mesh_instance_scene])
+def test_reference_parity_scenes(renderer, oracle_lib, maker):
+    # The scenes and 1-bounce AOV checks of HardwareTraversalParityTests.swift:7-125.
+    wl = maker()
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 1)
+    assert_aovs_bit_exact(s, o)
+    rel, g, c = beauty_stats(s, o)
+    assert rel <= 1e-3
+    assert np.array_equal(g[:, 3], c[:, 3])
+
+
+def test_cornell_small_full(renderer, oracle_lib):
+    wl = scenes.cornell_small()
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 16)
+    assert s.sample_count == 16
+    assert_aovs_bit_exact(s, o)
+    rel, g, c = beauty_stats(s, o)
+    assert rel <= 1e-3
+    assert abs(g[:, :3].mean() - c[:, :3].mean()) <= 0.01 * c[:, :3].mean()
+    assert np.isfinite(g).all()
+
+
+def test_cornell_small_batched_equals_single_calls(renderer, oracle_lib):
+    # 16 samples in one call (one wave of 16 sample slices) and in 4 calls of 4.
+    wl = scenes.cornell_small(width=96, height=54)
+    s1, o, b = run_pair(renderer, oracle_lib, wl, 16, render_calls=1)
+    s2 = renderer.make_session(wl.scene, wl.settings, build=b)
+    for _ in range(4):
+        s2.render(4)
+    for kind in AOVS:
+        assert np.array_equal(s1.pixels(kind), s2.pixels(kind))
+    assert np.allclose(s1.pixels(RenderOutput.BEAUTY), s2.pixels(RenderOutput.BEAUTY), rtol=1e-6, atol=1e-7)
+
+
+def test_spheres_large_pixel_sample(renderer, oracle_lib):
+    # Full-size large scene (1.31 M triangles, HDRI, all material families),
+    # compared on 4096 seeded pixels at 2 spp.
+    wl = scenes.spheres_large()
+    rng = np.random.default_rng(0)
+    pl = np.sort(rng.choice(1920 * 1080, 4096, replace=False)).astype(np.uint32)
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 2, pixel_list=pl)
+    assert_aovs_bit_exact(s, o, pl)
+    rel, g, c = beauty_stats(s, o, pl)
+    assert rel <= 2e-2
+    assert abs(g[:, :3].mean() - c[:, :3].mean()) <= 0.01 * c[:, :3].mean()
+
+
+def test_environment_table_vs_reference_fp32(dk_lib, oracle_lib):
+    # FP64 GPU prefix sum vs the reference's FP32 running sum
+    # (LightingGPUEncoding.swift:66-119): same shape, |cdf diff| small, last = 1.
+    from denrimrendererkit_gb300 import library
+    tex = scenes.synthetic_hdri(512, 256)
+    gpu = library.build_environment_samples(tex, 1.0, 0.0)
+    ref = oracle_lib.build_environment_samples(tex.pixels, 512, 256, 1.0, 0.0)
+    assert len(gpu) == len(ref) == 512 * 256
+    assert np.abs(gpu["cdf"] - ref["cdf"]).max() < 1e-4
+    assert gpu["cdf"][-1] == 1.0
+    assert np.allclose(gpu["pdf_solid_angle"], ref["pdf_solid_angle"], rtol=1e-3, atol=1e-6)
+    # Reference known answer: {1, 3} on a 2x1 map gives cdf {0.25, 1}.
+    from denrimrendererkit_gb300.scene import Texture2D
+    small = library.build_environment_samples(
+        Texture2D(2, 1, np.array([[1, 1, 1, 1], [3, 3, 3, 1]], np.float32), 1), 1.0, 0.0)
+    assert small["cdf"].tolist() == pytest.approx([0.25, 1.0], abs=1e-6)
+    zero = library.build_environment_samples(Texture2D(2, 1, np.zeros((2, 4), np.float32), 1), 1.0, 0.0)
+    assert len(zero) == 0
+
+
+def test_tiles_complete_a_sample(renderer, oracle_lib):
+    # encodeNextTile semantics (RenderSession.swift:862-889): 4 tiles of one
+    # sample equal one full-frame sample; the count advances on the last tile.
+    wl = scenes.cornell_small(width=64, height=36)
+    b = compile_scene(wl.scene)
+    full = renderer.make_session(wl.scene, wl.settings, build=b)
+    full.render(1)
+    tiled = renderer.make_session(wl.scene, wl.settings, build=b)
+    tiles = [(0, 0, 32, 18), (32, 0, 40, 18), (0, 18, 32, 30), (32, 18, 32, 18)]
+    for i, (x, y, w, h) in enumerate(tiles):
+        tiled.render_next_tile(x, y, w, h, completes_sample=(i == len(tiles) - 1))
+        assert tiled.sample_count == (1 if i == len(tiles) - 1 else 0)
+    for kind in (RenderOutput.BEAUTY,) + AOVS:
+        assert np.array_equal(full.pixels(kind), tiled.pixels(kind)), kind
+
+
+def test_reset_and_camera_update(renderer, oracle_lib):
+    wl = scenes.cornell_small(width=48, height=27)
+    b = compile_scene(wl.scene)
+    s = renderer.make_session(wl.scene, wl.settings, build=b)
+    s.render(2)
+    first = s.pixels(RenderOutput.BEAUTY).copy()
+    s.reset_accumulation()
+    assert s.sample_count == 0
+    s.render(2)
+    assert np.array_equal(first, s.pixels(RenderOutput.BEAUTY))
+    from denrimrendererkit_gb300.scene import Camera
+    moved = Camera((0.2, 1.0, 3.4), (0.0, 1.0, 0.0), vertical_field_of_view_degrees=40.0)
+    s.update_camera(moved)
+    assert s.sample_count == 0
+    s.render(1)
+    o_settings = RenderSettings(**{**wl.settings.__dict__, "previous_camera": wl.scene.camera})
+    o = oracle_lib.OracleRender(b, o_settings, moved)
+    o.render(1)
+    assert_aovs_bit_exact(s, o)  # includes motion vectors against the previous camera
+
+
+def test_transparent_background_and_background_color(renderer, oracle_lib):
+    wl = scenes.cornell_small(width=64, height=36)
+    wl.settings.transparent_background = True
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 2)
+    rel, g, c = beauty_stats(s, o)
+    assert np.array_equal(g[:, 3].astype(np.float32), c[:, 3].astype(np.float32))
+    assert (g[:, 3] == 0).any()
+    wl = scenes.cornell_small(width=64, height=36)
+    wl.settings.shows_environment_background = False
+    wl.settings.background_color = (0.3, 0.2, 0.1)
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 2)
+    rel, g, c = beauty_stats(s, o)
+    assert rel <= 1e-3
+
+
+def test_denoiser_aov_ray(renderer, oracle_lib):
+    # denoiserEnabled: the AOVs come from the unjittered primary ray
+    # (tracePrimaryAOV, PathTrace.metal:5530-5557).
+    wl = scenes.cornell_small(width=64, height=36)
+    wl.settings.denoise = True
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 2)
+    assert_aovs_bit_exact(s, o)
+
+
+def test_invalid_scene_leaves_no_session(renderer):
+    from denrimrendererkit_gb300 import DenrimError
+    wl = scenes.cornell_small(width=8, height=8)
+    b = compile_scene(wl.scene)
+    b.nodes = b.nodes.copy()
+    b.nodes["metadata"][0, 0] = 10 ** 6  # child index out of range
+    with pytest.raises(DenrimError) as e:
+        renderer.make_session(wl.scene, wl.settings, build=b)
+    assert e.value.code == 3
