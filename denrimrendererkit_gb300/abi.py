@@ -164,7 +164,7 @@ EXPORTED_SYMBOLS = (
     "dk_session_render_tile", "dk_session_update_camera", "dk_session_reset",
     "dk_session_read_output", "dk_session_sample_count", "dk_session_stats",
     "dk_session_destroy", "dk_last_error_message", "dk_build_bvh", "dk_build_lights",
-    "dk_build_environment_samples", "dk_version",
+    "dk_build_environment_samples", "dk_build_environment_samples_noalloc", "dk_version",
 )
 
 assert C.sizeof(Camera) == 80

@@ -415,6 +415,9 @@ int buildTraversal(const dk_scene* sc, const dk_bvh_node* nodes, uint32_t nodeCo
 // Kernel symbols for occupancy queries.
 namespace dk {
 int kernelGrid(int which, int smCount);
+
+// Lets other translation units of the library report through dk_last_error_message().
+void setLastError(const std::string& message) { g_error = message; }
 }
 
 extern "C" {

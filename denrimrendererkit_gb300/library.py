@@ -66,6 +66,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_build_bvh": (i32, [P, u32, u32, P, C.POINTER(u32), P]),
             "dk_build_lights": (i32, [P, u32, P, u32, P, C.POINTER(u32)]),
             "dk_build_environment_samples": (i32, [P, u32, u32, C.c_float, C.c_float, P, C.POINTER(u32)]),
+            "dk_build_environment_samples_noalloc": (i32, [P, u32, u32, C.c_float, C.c_float, P,
+                                                             C.POINTER(u32), P]),
             "dk_version": (C.c_char_p, []),
         }
         for name, (res, args) in sig.items():

@@ -320,6 +320,26 @@ int dk_build_lights(dk_triangle* triangles, uint32_t triangle_count, const dk_ma
 int dk_build_environment_samples(const dk_float4* pixels, uint32_t width, uint32_t height, float intensity,
                                  float max_radiance, dk_environment_sample* out, uint32_t* out_count);
 
+/* Allocation-free variant of dk_build_environment_samples.  It has no
+ * counterpart in the reference.  It serves callers that cannot let the library
+ * call cudaMalloc: applications that give the renderer only device memory from
+ * their own arena or pool, and real-time frame loops that must not allocate.
+ * The caller passes DEVICE pointers: `device_pixels` (width*height float4
+ * texels) and `device_out` (width*height entries).  The FP64 prefix-sum scratch
+ * is one static __device__ array sized for DK_ENV_NOALLOC_MAX_TEXELS texels
+ * (2048 x 1024, 16 MiB), held by every GPU that loads this library until the
+ * process exits; larger maps fail with DK_ERROR_INVALID_ARGUMENT.  The first
+ * call on a device looks up the array's device address (make that first call
+ * before any stream capture).  All calls share the one array: calls that
+ * overlap on the GPU (other threads, other streams) race.  Works on `stream`
+ * (NULL: the default stream) and returns after the table is complete;
+ * *out_count is width*height, or 0 for a map without energy.  Allocates
+ * nothing: no cudaMalloc, no cudaFree, no allocating library routine. */
+#define DK_ENV_NOALLOC_MAX_TEXELS (2048u * 1024u)
+int dk_build_environment_samples_noalloc(const dk_float4* device_pixels, uint32_t width, uint32_t height,
+                                         float intensity, float max_radiance, dk_environment_sample* device_out,
+                                         uint32_t* out_count, void* stream);
+
 /* Library version string. */
 const char* dk_version(void);
 
