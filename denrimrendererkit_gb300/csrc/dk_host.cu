@@ -194,222 +194,6 @@ void freeSession(Session* s) {
     delete s;
 }
 
-// Traversal layout built from the reference flat BVH: every interior node
-// stores both child boxes (one 64-byte record), leaves are referenced from
-// their parent, triangles are stored per leaf slot with precomputed edges.
-struct TraversalBvh {
-    std::vector<float4> nodes;  // 4 per node
-    std::vector<float4> isect;  // 3 per slot
-};
-
-const uint32_t kLeafBit = 0x80000000u;
-
-struct Converter {
-    const dk_scene* sc;
-    const std::vector<uint8_t>* opaque;
-    const std::vector<int32_t>* slotOf;  // reference slot -> compacted isect slot (-1: skipped)
-    TraversalBvh* out;
-    uint32_t dummySlot;
-    std::string err;
-
-    static void setBox(float4* n, int side, const float* mn, const float* mx) {
-        float4& xy = n[side];
-        xy = make_float4(mn[0], mx[0], mn[1], mx[1]);
-        if (side == 0) {
-            n[2].x = mn[2];
-            n[2].y = mx[2];
-        } else {
-            n[2].z = mn[2];
-            n[2].w = mx[2];
-        }
-    }
-
-    uint32_t leafCode(uint32_t first, uint32_t count) { return kLeafBit | (first << 3) | (count - 1u); }
-
-    // Reference leaf [first, first+count) -> child reference (splitting >8).
-    bool leafRef(uint32_t firstRef, uint32_t countRef, uint32_t& ref, float* mn, float* mx, int depth) {
-        std::vector<uint32_t> slots;
-        for (uint32_t i = firstRef; i < firstRef + countRef; ++i) {
-            int32_t s = (*slotOf)[i];
-            if (s >= 0) slots.push_back((uint32_t)s);
-        }
-        return slotsRef(slots, 0, (uint32_t)slots.size(), ref, mn, mx, depth);
-    }
-
-    // Bounds of one slot from the exact vertex positions of its triangle.
-    void slotBounds(uint32_t slot, float* mn, float* mx) {
-        uint32_t tri = __float_as_uint_host(out->isect[3 * (size_t)slot + 1].w);
-        const dk_triangle& t = sc->triangles[tri];
-        const float* p[3] = {&t.v0.x, &t.v1.x, &t.v2.x};
-        for (int k = 0; k < 3; ++k)
-            for (int a = 0; a < 3; ++a) {
-                mn[a] = std::fmin(mn[a], p[k][a]);
-                mx[a] = std::fmax(mx[a], p[k][a]);
-            }
-    }
-
-    static uint32_t __float_as_uint_host(float f) {
-        uint32_t u;
-        std::memcpy(&u, &f, 4);
-        return u;
-    }
-
-    bool slotsRef(const std::vector<uint32_t>& slots, uint32_t lo, uint32_t hi, uint32_t& ref, float* mn, float* mx,
-                  int depth) {
-        for (int a = 0; a < 3; ++a) {
-            mn[a] = FLT_MAX;
-            mx[a] = -FLT_MAX;
-        }
-        if (hi == lo) {  // empty child: a far-away point box around the dummy slot
-            ref = leafCode(dummySlot, 1);
-            for (int a = 0; a < 3; ++a) mn[a] = mx[a] = 1e30f;
-            return true;
-        }
-        bool contiguous = true;
-        for (uint32_t i = lo + 1; i < hi; ++i) contiguous &= slots[i] == slots[i - 1] + 1;
-        if (hi - lo <= 8 && contiguous) {
-            for (uint32_t i = lo; i < hi; ++i) slotBounds(slots[i], mn, mx);
-            ref = leafCode(slots[lo], hi - lo);
-            return true;
-        }
-        if (depth > 60) {
-            err = "BVH too deep";
-            return false;
-        }
-        // Split oversized or non-contiguous leaves into a small subtree.
-        uint32_t mid = lo + (hi - lo) / 2;
-        if (hi - lo <= 8) mid = lo + 1;  // non-contiguous: peel one slot at a time
-        uint32_t nodeIndex = (uint32_t)(out->nodes.size() / 4);
-        out->nodes.resize(out->nodes.size() + 4);
-        uint32_t l, r;
-        float lmn[3], lmx[3], rmn[3], rmx[3];
-        if (!slotsRef(slots, lo, mid, l, lmn, lmx, depth + 1)) return false;
-        if (!slotsRef(slots, mid, hi, r, rmn, rmx, depth + 1)) return false;
-        float4* n = &out->nodes[4 * (size_t)nodeIndex];
-        setBox(n, 0, lmn, lmx);
-        setBox(n, 1, rmn, rmx);
-        n[3] = make_float4(__uint_as_float_host(l), __uint_as_float_host(r), 0.0f, 0.0f);
-        for (int a = 0; a < 3; ++a) {
-            mn[a] = std::fmin(lmn[a], rmn[a]);
-            mx[a] = std::fmax(lmx[a], rmx[a]);
-        }
-        ref = nodeIndex;
-        return true;
-    }
-
-    static float __uint_as_float_host(uint32_t u) {
-        float f;
-        std::memcpy(&f, &u, 4);
-        return f;
-    }
-
-    // Reference node -> child reference (interior nodes become records).
-    bool nodeRef(uint32_t refNode, uint32_t& ref, float* mn, float* mx, int depth) {
-        if (refNode >= sc->node_count) {
-            err = "BVH child index out of range";
-            return false;
-        }
-        if (depth > 60) {
-            err = "BVH deeper than the 64-entry traversal stack";
-            return false;
-        }
-        const dk_bvh_node& n = sc->nodes[refNode];
-        if (n.metadata.w > 0) {
-            if ((uint64_t)n.metadata.z + n.metadata.w > sc->primitive_index_count) {
-                err = "BVH leaf range out of range";
-                return false;
-            }
-            return leafRef(n.metadata.z, n.metadata.w, ref, mn, mx, depth);
-        }
-        uint32_t nodeIndex = (uint32_t)(out->nodes.size() / 4);
-        out->nodes.resize(out->nodes.size() + 4);
-        uint32_t l, r;
-        float lmn[3], lmx[3], rmn[3], rmx[3];
-        if (n.metadata.x <= refNode || n.metadata.y <= refNode) {
-            err = "BVH is not in pre-order (child index not after its parent)";
-            return false;
-        }
-        if (!nodeRef(n.metadata.x, l, lmn, lmx, depth + 1)) return false;
-        if (!nodeRef(n.metadata.y, r, rmn, rmx, depth + 1)) return false;
-        float4* rec = &out->nodes[4 * (size_t)nodeIndex];
-        setBox(rec, 0, lmn, lmx);
-        setBox(rec, 1, rmn, rmx);
-        rec[3] = make_float4(__uint_as_float_host(l), __uint_as_float_host(r), 0.0f, 0.0f);
-        for (int a = 0; a < 3; ++a) {
-            mn[a] = std::fmin(lmn[a], rmn[a]);
-            mx[a] = std::fmax(lmx[a], rmx[a]);
-        }
-        ref = nodeIndex;
-        return true;
-    }
-};
-
-// Builds the traversal layout.  `primIdx` is the reference leaf order: the
-// slot (tie-break key) of a triangle is its position there.
-int buildTraversal(const dk_scene* sc, const dk_bvh_node* nodes, uint32_t nodeCount, const uint32_t* primIdx,
-                   uint32_t primCount, TraversalBvh& tb) {
-    std::vector<uint8_t> opaque(sc->triangle_count);
-    for (uint32_t i = 0; i < sc->triangle_count; ++i) {
-        const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
-        float transmission = std::fmin(std::fmax(m.emission.w, 0.0f), 1.0f);
-        opaque[i] = (m.base_color.w > 0.001f && transmission <= 0.001f) ? 1 : 0;
-    }
-    std::vector<int32_t> slotOf(primCount, -1);
-    tb.isect.clear();
-    tb.isect.reserve(3 * (size_t)primCount + 3);
-    uint32_t valid = 0;
-    for (uint32_t i = 0; i < primCount; ++i) {
-        uint32_t t = primIdx[i];
-        if (t >= sc->triangle_count) continue;  // the reference skips these (PathTrace.metal:3358-3360)
-        const dk_triangle& tr = sc->triangles[t];
-        float4 a = make_float4(tr.v0.x, tr.v0.y, tr.v0.z, Converter::__uint_as_float_host(i));
-        float4 b = make_float4(tr.v1.x - tr.v0.x, tr.v1.y - tr.v0.y, tr.v1.z - tr.v0.z, Converter::__uint_as_float_host(t));
-        float4 c = make_float4(tr.v2.x - tr.v0.x, tr.v2.y - tr.v0.y, tr.v2.z - tr.v0.z,
-                               Converter::__uint_as_float_host(opaque[t] ? 1u : 0u));
-        tb.isect.push_back(a);
-        tb.isect.push_back(b);
-        tb.isect.push_back(c);
-        slotOf[i] = (int32_t)valid++;
-    }
-    uint32_t dummy = valid;
-    tb.isect.push_back(make_float4(0, 0, 0, Converter::__uint_as_float_host(0xffffffffu)));
-    tb.isect.push_back(make_float4(0, 0, 0, Converter::__uint_as_float_host(0u)));
-    tb.isect.push_back(make_float4(0, 0, 0, 0));
-    Converter cv{sc, &opaque, &slotOf, &tb, dummy, ""};
-    dk_scene view = *sc;
-    view.nodes = nodes;
-    view.node_count = nodeCount;
-    view.primitive_indices = primIdx;
-    view.primitive_index_count = primCount;
-    cv.sc = &view;
-    tb.nodes.clear();
-    tb.nodes.resize(4);  // root record
-    float mn[3], mx[3];
-    uint32_t rootRef;
-    const dk_bvh_node& root = nodes[0];
-    if (root.metadata.w > 0) {
-        if (!cv.nodeRef(0, rootRef, mn, mx, 1)) return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + cv.err + ".");
-        float4* rec = &tb.nodes[0];
-        float far[3] = {1e30f, 1e30f, 1e30f};
-        Converter::setBox(rec, 0, mn, mx);
-        Converter::setBox(rec, 1, far, far);
-        rec[3] = make_float4(Converter::__uint_as_float_host(rootRef),
-                             Converter::__uint_as_float_host(kLeafBit | (dummy << 3)), 0, 0);
-        return DK_OK;
-    }
-    // Interior root: build children into record 0.
-    uint32_t l, r;
-    float lmn[3], lmx[3], rmn[3], rmx[3];
-    if (root.metadata.x == 0 || root.metadata.y == 0 || !cv.nodeRef(root.metadata.x, l, lmn, lmx, 1) ||
-        !cv.nodeRef(root.metadata.y, r, rmn, rmx, 1))
-        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + (cv.err.empty() ? std::string("malformed BVH root") : cv.err) + ".");
-    float4* rec = &tb.nodes[0];
-    Converter::setBox(rec, 0, lmn, lmx);
-    Converter::setBox(rec, 1, rmn, rmx);
-    rec[3] = make_float4(Converter::__uint_as_float_host(l), Converter::__uint_as_float_host(r), 0, 0);
-    return DK_OK;
-}
-
 }  // namespace
 
 // Kernel symbols for occupancy queries.
@@ -568,26 +352,25 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     int rc = ensureDevice();
     if (rc != DK_OK) return rc;
 
-    // Traversal BVH: the caller's reference BVH, or (when none is given) the
-    // reference builder run here with slots = triangle index, which is the tie
-    // order of the reference's linear fallback (PathTrace.metal:3264-3290).
-    TraversalBvh tb;
-    if (sc->node_count > 0) {
-        rc = buildTraversal(sc, sc->nodes, sc->node_count, sc->primitive_indices, sc->primitive_index_count, tb);
-    } else {
-        std::vector<dk_bvh_node> nodes(2 * (size_t)sc->triangle_count + 1);
-        std::vector<uint32_t> prim(sc->triangle_count);
-        uint32_t nc = buildReferenceBvh(sc->triangles, sc->triangle_count, 4, nodes.data(), prim.data());
-        // Leaf order of this private BVH is not the tie order: rewrite slots.
-        rc = buildTraversal(sc, nodes.data(), nc, prim.data(), sc->triangle_count, tb);
-        if (rc == DK_OK)
-            for (size_t s = 0; s + 1 < tb.isect.size() / 3; ++s) {
-                uint32_t tri;
-                std::memcpy(&tri, &tb.isect[3 * s + 1].w, 4);
-                std::memcpy(&tb.isect[3 * s].w, &tri, 4);
-            }
+    // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
+    // reaches, each carrying its reference DFS slot as the tie-break key.
+    std::vector<float4> tNodes, tIsect;
+    bool allOpaque = true;
+    {
+        std::vector<uint32_t> slotOf;
+        std::string err;
+        if (!dk::referenceSlots(sc, slotOf, err)) return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + err + ".");
+        std::vector<uint8_t> opaque(sc->triangle_count);
+        for (uint32_t i = 0; i < sc->triangle_count; ++i) {
+            const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
+            float transmission = std::fmin(std::fmax(m.emission.w, 0.0f), 1.0f);
+            // shadowOccluded (PathTrace.metal:4230-4241): cut-outs pass, transmissive layers tint.
+            opaque[i] = (m.base_color.w > 0.001f && transmission <= 0.001f) ? 1 : 0;
+            if (!opaque[i] && slotOf[i] != dk::kNoSlot) allOpaque = false;
+        }
+        int brc = dk::buildSahTraversal(sc, slotOf, opaque, tNodes, tIsect, err);
+        if (brc != DK_OK) return fail(brc, "Invalid render scene: " + err + ".");
     }
-    if (rc != DK_OK) return rc;
 
     Session* s = new Session();
     std::memset(&s->stats, 0, sizeof(s->stats));
@@ -610,8 +393,8 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     std::memset(&D, 0, sizeof(D));
     TRY(upload(s, const_cast<dk_triangle**>(&D.tris), sc->triangles, sc->triangle_count, "triangles"));
     TRY(upload(s, const_cast<dk_material**>(&D.mats), sc->materials, sc->material_count, "materials"));
-    TRY(upload(s, const_cast<float4**>(&D.isect), tb.isect.data(), tb.isect.size(), "triangle slots"));
-    TRY(upload(s, const_cast<float4**>(&D.nodes), tb.nodes.data(), tb.nodes.size(), "BVH nodes"));
+    TRY(upload(s, const_cast<float4**>(&D.isect), tIsect.data(), tIsect.size(), "triangle slots"));
+    TRY(upload(s, const_cast<float4**>(&D.nodes), tNodes.data(), tNodes.size(), "BVH nodes"));
     TRY(upload(s, const_cast<dk_texture_descriptor**>(&D.texdesc), sc->texture_descriptors, sc->texture_descriptor_count,
                "texture descriptors"));
     TRY(upload(s, const_cast<float4**>(&D.texpix), reinterpret_cast<const float4*>(sc->texture_pixels),
@@ -621,7 +404,8 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
                sc->environment_sample_count, "environment samples"));
     D.tri_count = sc->triangle_count;
     D.mat_count = sc->material_count;
-    D.node_count = (uint32_t)(tb.nodes.size() / 4);
+    D.node_count = (uint32_t)(tNodes.size() / 4);
+    D.all_shadow_opaque = allOpaque ? 1u : 0u;
     D.texdesc_count = sc->texture_descriptor_count;
     D.light_count = sc->lights ? sc->light_count : 0;
     D.env_count = sc->environment_samples ? sc->environment_sample_count : 0;
@@ -652,6 +436,7 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     TRY(deviceAlloc(s, &W.q[0], cap, "queue 0"));
     TRY(deviceAlloc(s, &W.q[1], cap, "queue 1"));
     TRY(deviceAlloc(s, &W.qs, cap, "shadow queue"));
+    TRY(deviceAlloc(s, &W.qr, 3 * cap, "shadow ray queue"));
     TRY(deviceAlloc(s, &W.counts, 4, "queue counters"));
     TRY(deviceAlloc(s, &W.aov, 4 * (size_t)pixels, "AOV records"));
     dk::Accum& A = s->accum;
@@ -755,7 +540,8 @@ static int renderSamples(Session* s, uint32_t tx, uint32_t ty, uint32_t tw, uint
             DK_CUDA(dk::launchShade(s->scene, P, s->wave, b, sel, s->gridShade, q), "shade launch");
             MARK(3);
             DK_CUDA(dk::launchShadow(s->scene, P, s->wave, s->gridShadow, q), "shadow launch");
-            launches += 3;
+            DK_CUDA(dk::launchResolve(P, s->wave, s->gridFinal, q), "resolve launch");
+            launches += 4;
         }
         MARK(0);
         if (st.denoiser_enabled) {

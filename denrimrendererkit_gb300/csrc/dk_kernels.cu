@@ -89,39 +89,6 @@ __device__ __forceinline__ Material materialForHit(const DevScene& S, const Hit&
     return loadMaterial(S.mats, min(h.materialID, S.mat_count - 1u));
 }
 
-// shadowOccluded (PathTrace.metal:4196-4274).  Opaque blockers are found by an
-// any-hit query; the ordered closest-hit walk through cut-outs and transmissive
-// layers runs only when such a layer lies on the segment.
-__device__ bool shadowOccluded(const DevScene& S, float3 o, float3 d, float maxDistance, float3& transmittance) {
-    bool sawNonOpaque = false;
-    if (traceAnyOpaque(S, o, d, maxDistance, sawNonOpaque)) return true;
-    if (!sawNonOpaque) return false;
-    float traveled = 0.0f;
-    for (uint32_t step = 0; step < 8u; ++step) {
-        HitRec r = traceClosest(S, o, d);
-        if (r.tri == kNoHit || traveled + r.t >= maxDistance) return false;
-        Ray ray{o, d};
-        Hit h = makeHit(S, ray, r);
-        Material sm = materialForHit(S, h);
-        if (sm.baseColor.w <= 0.001f) {
-            traveled += r.t;
-            o = h.position + d * 0.001f;
-            continue;
-        }
-        float transmission = materialTransmission(sm);
-        if (transmission <= 0.001f) return true;
-        bool insideSolid = !h.frontFacing && !materialThinWalled(sm);
-        float3 medium = (materialHasVolumeScattering(sm) && insideSolid)
-                            ? exp3((-materialVolumeSigmaT(sm)) * r.t)
-                            : materialTransmissionAbsorption(sm, r.t, insideSolid);
-        transmittance *= materialTransmissionTint(sm, 0.35f) * medium * transmission;
-        if (maxComponent(transmittance) < 0.02f) return true;
-        traveled += r.t;
-        o = h.position + d * 0.001f;
-    }
-    return true;
-}
-
 // Subsurface walk helpers (PathTrace.metal:3490-3523).
 __device__ __forceinline__ float sampleSubsurfaceFreeFlight(float3 sigmaT, float ux, float uy) {
     float sigma = sigmaT.z;
@@ -304,6 +271,7 @@ __global__ void __launch_bounds__(256) k_generate(DevScene S, DevParams P, Wave 
         W.counts[0] = P.path_count;
         W.counts[1] = 0u;
         W.counts[2] = 0u;
+        W.counts[3] = 0u;
     }
 }
 
@@ -314,6 +282,7 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
     if (globalId() == 0) {
         W.counts[sel ^ 1u] = 0u;
         W.counts[2] = 0u;
+        W.counts[3] = 0u;
     }
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
         uint32_t p = q[i];
@@ -543,12 +512,124 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, DevParams P, Wave W, 
         bool sh = o.neeMask != 0u;
         uint32_t sslot = warpAppend(&W.counts[2], sh);
         if (sh) W.qs[sslot] = p;
+        for (uint32_t k = 0; k < 3u; ++k) {
+            bool has = (o.neeMask >> k) & 1u;
+            uint32_t r = warpAppend(&W.counts[3], has);
+            if (has) W.qr[r] = (p << 2) | k;
+        }
     }
 }
 
-// NEE shadow queries of one path and the clamped direct-light sum
-// (sampleDirectLighting + `radiance += clampSampleContribution(throughput * direct)`).
-__global__ void __launch_bounds__(128) k_shadow(DevScene S, DevParams P, Wave W) {
+// shadowOccluded (PathTrace.metal:4196-4274) for scenes with cut-out or
+// transmissive triangles, in one traversal: an opaque blocker anywhere in
+// (0.0005, maxDistance) occludes; otherwise the non-opaque layers are collected
+// in distance order and walked as the reference walks them (re-starting 0.001
+// past each layer, at most 8 steps, transmittance below 0.02 occludes).
+__device__ bool shadowLayers(const DevScene& S, float3 o, float3 d, float tmax, float3& T) {
+    constexpr int kMaxLayers = 8;
+    float lt[kMaxLayers];
+    uint32_t ltri[kMaxLayers];
+    float lu[kMaxLayers], lv[kMaxLayers];
+    int count = 0;
+    float3 inv = rcp3(d);
+    int stackNode[kStackSize];
+    int sp = 0;
+    uint32_t node = 0;
+    if (S.node_count == 0) return false;
+    for (;;) {
+        if ((node & kLeafBit) == 0) {
+            const float4* n = S.nodes + 4 * (size_t)node;
+            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
+            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
+            float tl, tr;
+            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, o, inv, tmax, tl);
+            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, o, inv, tmax, tr);
+            if (hl && hr) {
+                bool rFirst = tr < tl;
+                if (sp < kStackSize) stackNode[sp++] = rFirst ? ch.x : ch.y;
+                node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+                continue;
+            }
+            if (hl) { node = (uint32_t)ch.x; continue; }
+            if (hr) { node = (uint32_t)ch.y; continue; }
+        } else {
+            uint32_t first = (node & ~kLeafBit) >> 3;
+            uint32_t cnt = (node & 7u) + 1u;
+            for (uint32_t i = first; i < first + cnt; ++i) {
+                const float4* q = S.isect + 3 * (size_t)i;
+                float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+                float t, u, v;
+                if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) || !(t < tmax)) continue;
+                if (__float_as_uint(c.w) & 1u) return true;  // opaque blocker
+                if (count == kMaxLayers - 1) return true;    // an 8th layer: the walk ends occluded
+                int j = count++;
+                while (j > 0 && lt[j - 1] > t) {
+                    lt[j] = lt[j - 1];
+                    ltri[j] = ltri[j - 1];
+                    lu[j] = lu[j - 1];
+                    lv[j] = lv[j - 1];
+                    --j;
+                }
+                lt[j] = t;
+                ltri[j] = __float_as_uint(b.w);
+                lu[j] = u;
+                lv[j] = v;
+            }
+        }
+        if (sp == 0) break;
+        node = (uint32_t)stackNode[--sp];
+    }
+    float prev = 0.0f;
+    bool started = false;
+    Ray ray{o, d};
+    for (int i = 0; i < count; ++i) {
+        float a = lt[i];
+        if (started && a <= prev + 0.0015f) continue;  // inside the 0.001 restart gap + 0.0005 epsilon
+        float trel = started ? a - (prev + 0.001f) : a;
+        HitRec r{a, ltri[i], lu[i], lv[i]};
+        Hit h = makeHit(S, ray, r);
+        Material sm = materialForHit(S, h);
+        prev = a;
+        started = true;
+        if (sm.baseColor.w <= 0.001f) continue;
+        float transmission = materialTransmission(sm);
+        bool insideSolid = !h.frontFacing && !materialThinWalled(sm);
+        float3 medium = (materialHasVolumeScattering(sm) && insideSolid)
+                            ? exp3((-materialVolumeSigmaT(sm)) * trel)
+                            : materialTransmissionAbsorption(sm, trel, insideSolid);
+        T *= materialTransmissionTint(sm, 0.35f) * medium * transmission;
+        if (maxComponent(T) < 0.02f) return true;
+    }
+    return false;
+}
+
+// One thread per shadow ray: replaces the slot's unshadowed contribution by
+// its shadowed value (contribution * transmittance / pdf divisor, or 0).
+template <bool kLayered>
+__global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
+    const uint32_t n = W.counts[3];
+    const size_t cap = W.cap;
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t e = W.qr[i];
+        size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
+        float4 o = W.nee_o[slot], d = W.nee_d[slot], c = W.nee_c[slot];
+        float3 T = f3(1.0f);
+        bool occluded;
+        if (kLayered) {
+            occluded = shadowLayers(S, xyz(o), xyz(d), o.w, T);
+        } else {
+            bool unused = false;
+            occluded = traceAnyOpaque(S, xyz(o), xyz(d), o.w, unused);
+        }
+        float3 v = occluded ? f3(0.0f) : xyz(c) * T / c.w;
+        W.nee_c[slot] = make_float4(v.x, v.y, v.z, 0.0f);
+    }
+}
+
+// `radiance += clampSampleContribution(throughput * direct)` with direct the
+// sum of the path's shadowed NEE terms in the reference's order (light, env 0,
+// env 1; PathTrace.metal:4437-4584, 5396-5421).
+__global__ void __launch_bounds__(256) k_resolve(DevParams P, Wave W) {
     const uint32_t n = W.counts[2];
     const size_t cap = W.cap;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
@@ -556,13 +637,8 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, DevParams P, Wave W)
         float4 tpw = W.nee_tp[p];
         uint32_t mask = __float_as_uint(tpw.w);
         float3 direct = f3(0.0f);
-        for (uint32_t k = 0; k < 3u; ++k) {
-            if (!(mask & (1u << k))) continue;
-            size_t slot = k * cap + p;
-            float4 o = W.nee_o[slot], d = W.nee_d[slot], c = W.nee_c[slot];
-            float3 T = f3(1.0f);
-            if (!shadowOccluded(S, xyz(o), xyz(d), o.w, T)) direct += xyz(c) * T / c.w;
-        }
+        for (uint32_t k = 0; k < 3u; ++k)
+            if (mask & (1u << k)) direct += xyz(W.nee_c[k * cap + p]);
         float4 r = W.rad[p];
         float3 add = clampSampleContribution(xyz(tpw) * direct, P.clamp);
         W.rad[p] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
@@ -792,7 +868,7 @@ int kernelGrid(int which, int smCount) {
         case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_generate, 256, 0); break;
         case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend, 128, 0); break;
         case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 128, 0); break;
-        case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow, 128, 0); break;
+        case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<true>, 128, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_finalize, 256, 0); break;
     }
     return (perSM < 1 ? 1 : perSM) * smCount;
@@ -812,7 +888,15 @@ cudaError_t launchShade(const DevScene& S, const DevParams& P, const Wave& W, ui
     return cudaGetLastError();
 }
 cudaError_t launchShadow(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
-    k_shadow<<<grid, 128, 0, st>>>(S, P, W);
+    (void)P;
+    if (S.all_shadow_opaque)
+        k_shadow_rays<false><<<grid, 128, 0, st>>>(S, W);
+    else
+        k_shadow_rays<true><<<grid, 128, 0, st>>>(S, W);
+    return cudaGetLastError();
+}
+cudaError_t launchResolve(const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
+    k_resolve<<<grid, 256, 0, st>>>(P, W);
     return cudaGetLastError();
 }
 cudaError_t launchAovPrimary(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {

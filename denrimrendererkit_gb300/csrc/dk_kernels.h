@@ -2,11 +2,16 @@
 // (dk_kernels.cu) of the sm_103a path tracer, plus the kernel launchers.
 #pragma once
 #include <cstdint>
+#include <string>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "../../include/denrim_cuda.h"
 
 namespace dk {
+
+constexpr uint32_t kNoSlot = 0xffffffffu;
 
 // Device copy of the scene.  `isect` holds 3 x float4 per BVH leaf slot:
 // (v0.xyz, reference slot), (v1 - v0, triangle index), (v2 - v0, flags with
@@ -51,7 +56,8 @@ struct Wave {
     float4* nee_tp;    // throughput at NEE, w = slot mask
     uint32_t* q[2];    // active path queues (ping-pong)
     uint32_t* qs;      // paths with shadow queries
-    uint32_t* counts;  // [0], [1] queue lengths, [2] shadow queue length
+    uint32_t* qr;      // shadow rays: path << 2 | slot (3 x cap entries)
+    uint32_t* counts;  // [0], [1] queue lengths, [2] shadow-path count, [3] shadow-ray count
     float4* aov;       // 4 x tile pixels: primary-hit record of the batch's last sample
     uint32_t cap;
     uint32_t pad;
@@ -68,11 +74,17 @@ struct Accum {
     float4* aov;       // 6 planes: depth, normal, albedo, materialID, objectID, motion
 };
 
+// Host-side traversal BVH (dk_bvh.cu).
+bool referenceSlots(const dk_scene* sc, std::vector<uint32_t>& slotOfTri, std::string& err);
+int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri, const std::vector<uint8_t>& opaque,
+                      std::vector<float4>& nodes, std::vector<float4>& isect, std::string& err);
+
 cudaError_t launchGenerate(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st);
 cudaError_t launchShade(const DevScene& S, const DevParams& P, const Wave& W, uint32_t bounce, uint32_t sel, int grid,
                         cudaStream_t st);
 cudaError_t launchShadow(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st);
+cudaError_t launchResolve(const DevParams& P, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchAovPrimary(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchFinalize(const DevParams& P, const Wave& W, const Accum& A, uint32_t writeAov, int grid,
                            cudaStream_t st);

@@ -248,7 +248,7 @@ __device__ float3 materialClearcoatAttenuationForDirection(const Material& m, fl
     float3 att = mx(f3(0.0f), f3(1.0f) - ccF * clearcoat);
     return att * materialClearcoatDepthAttenuation(m, n, v, l);
 }
-__device__ float3 evaluateMaterialBRDF(const Material& m, float3 n, float3 tg, float3 bt, float3 v, float3 l) {  // :1323-1384
+__device__ __noinline__ float3 evaluateMaterialBRDF(const Material& m, float3 n, float3 tg, float3 bt, float3 v, float3 l) {  // :1323-1384
     const float inversePi = 0.31830988618f;
     float roughness = clampf(m.parameters.x, 0.02f, 1.0f);
     float metallic = clampf(m.parameters.y, 0.0f, 1.0f);
@@ -304,7 +304,7 @@ __device__ float ggxReflectionPDF(float3 n, float3 tg, float3 bt, float3 v, floa
     return distributionGGXAnisotropic(h, n, f.tangent, f.bitangent, r, an) *
            geometrySmithG1GGXAnisotropic(v, n, f.tangent, f.bitangent, r, an) / fmaxf(4.0f * nDotV, 1e-5f);
 }
-__device__ float materialBSDFPDF(const Material& m, float3 n, float3 tg, float3 bt, float3 v, float3 l) {  // :1445-1490
+__device__ __noinline__ float materialBSDFPDF(const Material& m, float3 n, float3 tg, float3 bt, float3 v, float3 l) {  // :1445-1490
     float nDotL = fmaxf(dot(n, l), 0.0f), nDotV = fmaxf(dot(n, v), 0.0f);
     if (nDotL <= 0.0f || nDotV <= 0.0f) return 0.0f;
     float dP, sP, cP;
@@ -315,7 +315,7 @@ __device__ float materialBSDFPDF(const Material& m, float3 n, float3 tg, float3 
     float ccPDF = ggxReflectionPDF(n, tg, bt, v, l, materialClearcoatRoughness(m), 0.0f);
     return dP * (nDotL * 0.31830988618f) + sP * specPDF + cP * ccPDF;
 }
-__device__ float3 materialDiffuseBounceWeight(const Material& m, float3 n, float3 v, float3 l) {  // :1492-1518
+__device__ __noinline__ float3 materialDiffuseBounceWeight(const Material& m, float3 n, float3 v, float3 l) {  // :1492-1518
     float metallic = clampf(m.parameters.y, 0.0f, 1.0f);
     float3 hd = v + l;
     if (dot(hd, hd) <= 1e-8f) return f3(0.0f);
@@ -377,7 +377,7 @@ __device__ float3 sampleGGXHalfVector(float ux, float uy, float3 n, float roughn
     float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
     return orientHemisphere(f3(c * sinT, s * sinT, cosT), n);
 }
-__device__ float3 sampleGGXVisibleNormal(float ux, float uy, float3 n, float3 tg, float3 bt, float3 v, float r,
+__device__ __noinline__ float3 sampleGGXVisibleNormal(float ux, float uy, float3 n, float3 tg, float3 bt, float3 v, float r,
                                          float an) {  // :1620-1660
     TangentFrame fr = makeTangentFrame(n, tg, bt);
     float2 a = anisotropicGGXAlpha(r, an);
@@ -440,7 +440,7 @@ __device__ __forceinline__ float3 rotateEnv(const DevScene& S, float3 d, float& 
     sincosf(S.env_rot_y, &sn, &cs);
     return normalize(f3(cs * d.x - sn * d.z, d.y, sn * d.x + cs * d.z));
 }
-__device__ float3 sampleEnvironment(const DevScene& S, float3 d) {  // :3770-3802
+__device__ __noinline__ float3 sampleEnvironment(const DevScene& S, float3 d) {  // :3770-3802
     float intensity = fmaxf(S.env_intensity, 0.0f);
     if (S.env_tex_plus1 == 0u) return fallbackSky(d) * intensity;
     float sn, cs;
@@ -453,7 +453,7 @@ __device__ float3 sampleEnvironment(const DevScene& S, float3 d) {  // :3770-380
     if (maxR > 0.0f) color = mn(color, f3(maxR));
     return color;
 }
-__device__ float environmentPDF(const DevScene& S, float3 d) {  // :3870-3914
+__device__ __noinline__ float environmentPDF(const DevScene& S, float3 d) {  // :3870-3914
     if (S.env == nullptr || S.env_count == 0u || S.env_tex_plus1 == 0u) return 0.0f;
     uint4 md = __ldg(reinterpret_cast<const uint4*>(&S.texdesc[S.env_tex_plus1 - 1u]));
     uint32_t w = md.y, hgt = md.z;
@@ -471,7 +471,7 @@ __device__ float environmentPDF(const DevScene& S, float3 d) {  // :3870-3914
     return fmaxf(__ldg(&S.env[index].y), 0.0f);
 }
 // sampleEnvironmentDirection (:3937-3987) with selectEnvironmentSampleIndex (:3916-3935).
-__device__ float3 sampleEnvironmentDirection(const DevScene& S, float px, float py, float cdfSample, float& pdf) {
+__device__ __noinline__ float3 sampleEnvironmentDirection(const DevScene& S, float px, float py, float cdfSample, float& pdf) {
     pdf = 0.0f;
     if (S.env_tex_plus1 == 0u || S.env_count == 0u || S.env == nullptr) return f3(0, 1, 0);
     uint4 md = __ldg(reinterpret_cast<const uint4*>(&S.texdesc[S.env_tex_plus1 - 1u]));
