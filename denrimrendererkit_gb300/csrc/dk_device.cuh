@@ -183,6 +183,142 @@ __device__ bool traceAnyOpaque(const DevScene& S, float3 o, float3 d, float tmax
     return false;
 }
 
+// ---------------------------------------------- resumable traversal ------
+// The persistent kernels advance each lane's ray a bounded number of node or
+// leaf visits at a time and refill finished lanes with new rays, so a warp's
+// lanes stay busy instead of waiting for the warp's longest traversal.
+struct ClosestState {
+    float3 o, d, inv;
+    float bestT, bu, bv;
+    uint32_t bestTri, bestSlot, node;
+    int sp;
+};
+
+__device__ __forceinline__ void closestInit(ClosestState& st, float3 o, float3 d) {
+    st.o = o;
+    st.d = d;
+    st.inv = rcp3(d);
+    st.bestT = INFINITY;
+    st.bu = st.bv = 0.0f;
+    st.bestTri = kNoHit;
+    st.bestSlot = 0xffffffffu;
+    st.node = 0;
+    st.sp = 0;
+}
+
+// Up to `budget` visits of the closest-hit traversal of traceClosest; returns
+// true when the ray is finished.
+__device__ __forceinline__ bool closestSteps(const DevScene& S, ClosestState& st, int* stackNode, float* stackT,
+                                             int budget) {
+    for (int it = 0; it < budget; ++it) {
+        if ((st.node & kLeafBit) == 0) {
+            const float4* n = S.nodes + 4 * (size_t)st.node;
+            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
+            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
+            float tl, tr;
+            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, st.o, st.inv, st.bestT, tl);
+            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, st.o, st.inv, st.bestT, tr);
+            if (hl && hr) {
+                bool rFirst = tr < tl;
+                if (st.sp < kStackSize) {
+                    stackNode[st.sp] = rFirst ? ch.x : ch.y;
+                    stackT[st.sp] = rFirst ? tl : tr;
+                    ++st.sp;
+                }
+                st.node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+                continue;
+            }
+            if (hl) { st.node = (uint32_t)ch.x; continue; }
+            if (hr) { st.node = (uint32_t)ch.y; continue; }
+        } else {
+            uint32_t first = (st.node & ~kLeafBit) >> 3;
+            uint32_t cnt = (st.node & 7u) + 1u;
+            for (uint32_t i = first; i < first + cnt; ++i) {
+                const float4* q = S.isect + 3 * (size_t)i;
+                float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+                float t, u, v;
+                if (mtTest(st.o, st.d, xyz(a), xyz(b), xyz(c), t, u, v)) {
+                    uint32_t slot = __float_as_uint(a.w);
+                    if (t < st.bestT || (t == st.bestT && slot < st.bestSlot)) {
+                        st.bestT = t;
+                        st.bu = u;
+                        st.bv = v;
+                        st.bestTri = __float_as_uint(b.w);
+                        st.bestSlot = slot;
+                    }
+                }
+            }
+        }
+        bool found = false;
+        while (st.sp > 0) {
+            --st.sp;
+            if (stackT[st.sp] <= st.bestT) {
+                st.node = (uint32_t)stackNode[st.sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) return true;
+    }
+    return false;
+}
+
+struct AnyState {
+    float3 o, d, inv;
+    float tmax;
+    uint32_t node;
+    int sp;
+    bool sawNonOpaque;
+};
+
+__device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float tmax) {
+    st.o = o;
+    st.d = d;
+    st.inv = rcp3(d);
+    st.tmax = tmax;
+    st.node = 0;
+    st.sp = 0;
+    st.sawNonOpaque = false;
+}
+
+// Up to `budget` visits of traceAnyOpaque: 0 running, 1 finished without an
+// opaque blocker, 2 occluded.
+__device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* stackNode, int budget) {
+    for (int it = 0; it < budget; ++it) {
+        if ((st.node & kLeafBit) == 0) {
+            const float4* n = S.nodes + 4 * (size_t)st.node;
+            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
+            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
+            float tl, tr;
+            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, st.o, st.inv, st.tmax, tl);
+            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, st.o, st.inv, st.tmax, tr);
+            if (hl && hr) {
+                bool rFirst = tr < tl;
+                if (st.sp < kStackSize) stackNode[st.sp++] = rFirst ? ch.x : ch.y;
+                st.node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+                continue;
+            }
+            if (hl) { st.node = (uint32_t)ch.x; continue; }
+            if (hr) { st.node = (uint32_t)ch.y; continue; }
+        } else {
+            uint32_t first = (st.node & ~kLeafBit) >> 3;
+            uint32_t cnt = (st.node & 7u) + 1u;
+            for (uint32_t i = first; i < first + cnt; ++i) {
+                const float4* q = S.isect + 3 * (size_t)i;
+                float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+                float t, u, v;
+                if (mtTest(st.o, st.d, xyz(a), xyz(b), xyz(c), t, u, v) && t < st.tmax) {
+                    if (__float_as_uint(c.w) & 1u) return 2;
+                    st.sawNonOpaque = true;
+                }
+            }
+        }
+        if (st.sp == 0) return 1;
+        st.node = (uint32_t)stackNode[--st.sp];
+    }
+    return 0;
+}
+
 // Hit attributes of intersectTriangle / intersectScene (PathTrace.metal:
 // 1840-1851, 3366-3380) from the traversal's (t, u, v), exact ops.
 __device__ __forceinline__ Hit makeHit(const DevScene& S, const Ray& ray, const HitRec& r) {

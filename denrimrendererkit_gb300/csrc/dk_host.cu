@@ -437,7 +437,8 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     TRY(deviceAlloc(s, &W.q[1], cap, "queue 1"));
     TRY(deviceAlloc(s, &W.qs, cap, "shadow queue"));
     TRY(deviceAlloc(s, &W.qr, 3 * cap, "shadow ray queue"));
-    TRY(deviceAlloc(s, &W.counts, 4, "queue counters"));
+    TRY(deviceAlloc(s, &W.qr2, 3 * cap, "layer-walk queue"));
+    TRY(deviceAlloc(s, &W.counts, 8, "queue counters"));
     TRY(deviceAlloc(s, &W.aov, 4 * (size_t)pixels, "AOV records"));
     dk::Accum& A = s->accum;
     TRY(deviceAlloc(s, &A.sum, pixels, "accumulation sum"));

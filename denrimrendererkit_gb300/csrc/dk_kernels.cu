@@ -269,13 +269,34 @@ __global__ void __launch_bounds__(256) k_generate(DevScene S, DevParams P, Wave 
     }
     if (globalId() == 0) {
         W.counts[0] = P.path_count;
-        W.counts[1] = 0u;
-        W.counts[2] = 0u;
-        W.counts[3] = 0u;
+        for (int k = 1; k < 8; ++k) W.counts[k] = 0u;
     }
 }
 
-// Closest hit for every ray of the input queue (intersectScene).
+constexpr uint32_t kNoWork = 0xffffffffu;
+constexpr int kStepBudget = 16;
+
+// Refills the lanes that asked for work with consecutive items of a queue of
+// length `n` through one atomic per warp; returns this lane's item or kNoWork.
+__device__ __forceinline__ uint32_t warpFetch(uint32_t* counter, uint32_t n, bool need, bool& exhausted) {
+    unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m == 0u) return kNoWork;
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if ((int)laneId() == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!need) return kNoWork;
+    uint32_t idx = base + (uint32_t)__popc(m & ((1u << laneId()) - 1u));
+    if (idx >= n) {
+        exhausted = true;
+        return kNoWork;
+    }
+    return idx;
+}
+
+// Closest hit for every ray of the input queue (intersectScene), persistent
+// threads with per-lane refill.  W.counts[4] is the work cursor (zeroed by the
+// kernel that runs before).
 __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel) {
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
@@ -283,12 +304,31 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
         W.counts[sel ^ 1u] = 0u;
         W.counts[2] = 0u;
         W.counts[3] = 0u;
+        W.counts[5] = 0u;
+        W.counts[6] = 0u;
+        W.counts[7] = 0u;
     }
-    for (uint32_t i = globalId(); i < n; i += gridStride()) {
-        uint32_t p = q[i];
-        float4 o = W.ray_o[p], d = W.ray_d[p];
-        HitRec r = traceClosest(S, xyz(o), xyz(d));
-        W.hit[p] = make_float4(r.t, __uint_as_float(r.tri), r.u, r.v);
+    int stackNode[kStackSize];
+    float stackT[kStackSize];
+    ClosestState st;
+    uint32_t p = kNoWork;
+    bool exhausted = false;
+    for (;;) {
+        uint32_t idx = warpFetch(&W.counts[4], n, p == kNoWork && !exhausted, exhausted);
+        if (idx != kNoWork) {
+            p = q[idx];
+            float4 o = W.ray_o[p], d = W.ray_d[p];
+            closestInit(st, xyz(o), xyz(d));
+            if (S.node_count == 0) {
+                W.hit[p] = make_float4(INFINITY, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                p = kNoWork;
+            }
+        }
+        if (__all_sync(0xffffffffu, p == kNoWork && exhausted)) break;
+        if (p != kNoWork && closestSteps(S, st, stackNode, stackT, kStepBudget)) {
+            W.hit[p] = make_float4(st.bestT, __uint_as_float(st.bestTri), st.bu, st.bv);
+            p = kNoWork;
+        }
     }
 }
 
@@ -502,6 +542,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, DevParams P, Wave W, 
     const uint32_t* q = W.q[sel];
     uint32_t* qNext = W.q[sel ^ 1u];
     const uint32_t n = W.counts[sel];
+    if (globalId() == 0) W.counts[4] = 0u;  // extend cursor of the next bounce
     const bool lastBounce = bounce + 1u >= P.max_bounces;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
         uint32_t p = q[i];
@@ -603,24 +644,53 @@ __device__ bool shadowLayers(const DevScene& S, float3 o, float3 d, float tmax, 
     return false;
 }
 
-// One thread per shadow ray: replaces the slot's unshadowed contribution by
-// its shadowed value (contribution * transmittance / pdf divisor, or 0).
-template <bool kLayered>
+// Shadow rays, persistent threads with per-lane refill: an any-hit query for
+// an opaque blocker replaces the slot's unshadowed contribution by its
+// shadowed value (contribution / pdf divisor, or 0).  Rays that crossed a
+// cut-out or transmissive triangle without meeting an opaque one go to a
+// second queue for the layer walk (W.counts[6]).  W.counts[5] is the cursor.
 __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
     const uint32_t n = W.counts[3];
     const size_t cap = W.cap;
+    int stackNode[kStackSize];
+    AnyState st;
+    uint32_t e = kNoWork;
+    bool exhausted = false;
+    for (;;) {
+        uint32_t idx = warpFetch(&W.counts[5], n, e == kNoWork && !exhausted, exhausted);
+        if (idx != kNoWork) {
+            e = W.qr[idx];
+            size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
+            float4 o = W.nee_o[slot], d = W.nee_d[slot];
+            anyInit(st, xyz(o), xyz(d), o.w);
+        }
+        if (__all_sync(0xffffffffu, e == kNoWork && exhausted)) break;
+        if (e == kNoWork) continue;
+        int r = S.node_count == 0 ? 1 : anySteps(S, st, stackNode, kStepBudget);
+        if (r == 0) continue;
+        size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
+        if (r == 2) {
+            W.nee_c[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else if (st.sawNonOpaque) {
+            W.qr2[atomicAdd(&W.counts[6], 1u)] = e;
+        } else {
+            float4 c = W.nee_c[slot];
+            W.nee_c[slot] = make_float4(c.x / c.w, c.y / c.w, c.z / c.w, 0.0f);
+        }
+        e = kNoWork;
+    }
+}
+
+// The layer walk for the rays the any-hit pass could not settle.
+__global__ void __launch_bounds__(128) k_shadow_layers(DevScene S, Wave W) {
+    const uint32_t n = W.counts[6];
+    const size_t cap = W.cap;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
-        uint32_t e = W.qr[i];
+        uint32_t e = W.qr2[i];
         size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
         float4 o = W.nee_o[slot], d = W.nee_d[slot], c = W.nee_c[slot];
         float3 T = f3(1.0f);
-        bool occluded;
-        if (kLayered) {
-            occluded = shadowLayers(S, xyz(o), xyz(d), o.w, T);
-        } else {
-            bool unused = false;
-            occluded = traceAnyOpaque(S, xyz(o), xyz(d), o.w, unused);
-        }
+        bool occluded = shadowLayers(S, xyz(o), xyz(d), o.w, T);
         float3 v = occluded ? f3(0.0f) : xyz(c) * T / c.w;
         W.nee_c[slot] = make_float4(v.x, v.y, v.z, 0.0f);
     }
@@ -868,7 +938,7 @@ int kernelGrid(int which, int smCount) {
         case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_generate, 256, 0); break;
         case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend, 128, 0); break;
         case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 128, 0); break;
-        case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<true>, 128, 0); break;
+        case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays, 128, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_finalize, 256, 0); break;
     }
     return (perSM < 1 ? 1 : perSM) * smCount;
@@ -889,10 +959,8 @@ cudaError_t launchShade(const DevScene& S, const DevParams& P, const Wave& W, ui
 }
 cudaError_t launchShadow(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
     (void)P;
-    if (S.all_shadow_opaque)
-        k_shadow_rays<false><<<grid, 128, 0, st>>>(S, W);
-    else
-        k_shadow_rays<true><<<grid, 128, 0, st>>>(S, W);
+    k_shadow_rays<<<grid, 128, 0, st>>>(S, W);
+    if (!S.all_shadow_opaque) k_shadow_layers<<<grid, 128, 0, st>>>(S, W);
     return cudaGetLastError();
 }
 cudaError_t launchResolve(const DevParams& P, const Wave& W, int grid, cudaStream_t st) {

@@ -57,7 +57,9 @@ struct Wave {
     uint32_t* q[2];    // active path queues (ping-pong)
     uint32_t* qs;      // paths with shadow queries
     uint32_t* qr;      // shadow rays: path << 2 | slot (3 x cap entries)
-    uint32_t* counts;  // [0], [1] queue lengths, [2] shadow-path count, [3] shadow-ray count
+    uint32_t* qr2;     // shadow rays that need the layer walk (3 x cap entries)
+    uint32_t* counts;  // [0], [1] queue lengths, [2] shadow paths, [3] shadow rays, [4] extend cursor,
+                       // [5] shadow cursor, [6] layer-walk rays, [7] spare
     float4* aov;       // 4 x tile pixels: primary-hit record of the batch's last sample
     uint32_t cap;
     uint32_t pad;
