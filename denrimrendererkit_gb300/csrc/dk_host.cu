@@ -402,6 +402,28 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     TRY(upload(s, const_cast<dk_light_record**>(&D.lights), sc->lights, sc->light_count, "lights"));
     TRY(upload(s, const_cast<float2**>(&D.env), reinterpret_cast<const float2*>(sc->environment_samples),
                sc->environment_sample_count, "environment samples"));
+    // Guide table over the environment CDF (only when the CDF is monotone).
+    if (sc->environment_sample_count > 1 && sc->environment_samples) {
+        const uint32_t n = sc->environment_sample_count;
+        bool monotone = true;
+        for (uint32_t i = 1; i < n && monotone; ++i)
+            monotone = sc->environment_samples[i].cdf >= sc->environment_samples[i - 1].cdf;
+        if (monotone) {
+            const uint32_t G = 8192;
+            std::vector<uint32_t> guide(G + 1);
+            for (uint32_t b = 0; b <= G; ++b) {
+                float target = (float)b / (float)G;  // exact: b * 2^-13
+                uint32_t lo = 0, hi = n;
+                while (lo < hi) {
+                    uint32_t mid = (lo + hi) >> 1;
+                    if (target <= sc->environment_samples[mid].cdf) hi = mid; else lo = mid + 1;
+                }
+                guide[b] = lo;
+            }
+            TRY(upload(s, const_cast<uint32_t**>(&D.env_guide), guide.data(), guide.size(), "environment guide"));
+            D.env_guide_size = G;
+        }
+    }
     D.tri_count = sc->triangle_count;
     D.mat_count = sc->material_count;
     D.node_count = (uint32_t)(tNodes.size() / 4);

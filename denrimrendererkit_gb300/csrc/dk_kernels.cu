@@ -420,6 +420,8 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
 
     // ------------------------------------ NEE (sampleDirectLighting) ------
     float3 view = -ray.direction;
+    ShadePoint sp;
+    makeShadePoint(sp, m, h.normal, h.tangent, h.bitangent, view);
     float3 shadowOrigin = h.position + h.normal * 0.001f;
     const size_t cap = W.cap;
     if (S.light_count > 0u) {
@@ -443,10 +445,10 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
                 float cosL = fmaxf(0.0f, dot(xyz(__ldg(reinterpret_cast<const float4*>(&L.normal))), -ld));
                 if (cosS > 0.0f && cosL > 0.0f) {
                     float lightPdf = selPdf * (d2 / fmaxf(cosL * area, 1e-6f));
-                    float bsdfPdf = materialBSDFPDF(m, h.normal, h.tangent, h.bitangent, view, ld);
+                    float bsdfPdf = bsdfPDF(sp, ld);
                     float mis = powerHeuristic(lightPdf, bsdfPdf);
                     float G = cosS * cosL * area / fmaxf(d2, 1e-6f);
-                    float3 c = evaluateMaterialBRDF(m, h.normal, h.tangent, h.bitangent, view, ld) * le * G * mis;
+                    float3 c = evalBRDF(m, sp, ld) * le * G * mis;
                     if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f)) {
                         W.nee_o[p] = make_float4(shadowOrigin.x, shadowOrigin.y, shadowOrigin.z, dist - 0.002f);
                         W.nee_d[p] = make_float4(ld.x, ld.y, ld.z, 0.0f);
@@ -457,6 +459,7 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
             }
         }
     }
+#pragma unroll 1
     for (uint32_t e = 0u; e < 2u; ++e) {
         float a = randomFloat(state);
         float b = randomFloat(state);
@@ -465,10 +468,9 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
         float3 dir = sampleEnvironmentDirection(S, a, b, cdf, envPdf);
         float cosS = fmaxf(0.0f, dot(h.normal, dir));
         if (envPdf > 0.0f && cosS > 0.0f) {
-            float bsdfPdf = materialBSDFPDF(m, h.normal, h.tangent, h.bitangent, view, dir);
+            float bsdfPdf = bsdfPDF(sp, dir);
             float mis = powerHeuristic(envPdf, bsdfPdf);
-            float3 c = evaluateMaterialBRDF(m, h.normal, h.tangent, h.bitangent, view, dir) *
-                       sampleEnvironment(S, dir) * cosS * mis;
+            float3 c = evalBRDF(m, sp, dir) * sampleEnvironment(S, dir) * cosS * mis;
             if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f)) {
                 size_t slot = (size_t)(1u + e) * cap + p;
                 W.nee_o[slot] = make_float4(shadowOrigin.x, shadowOrigin.y, shadowOrigin.z, 1.0e20f);
@@ -481,52 +483,47 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
     if (out.neeMask) W.nee_tp[p] = make_float4(tp.x, tp.y, tp.z, __uint_as_float(out.neeMask));
 
     // --------------------------------------------- BSDF sampling ----------
-    float roughness = clampf(m.parameters.x, 0.02f, 1.0f);
-    float anisotropy = materialSpecularAnisotropy(m);
-    float3 f0 = materialF0(m);
-    float clearcoat = materialClearcoat(m);
-    float ccR = materialClearcoatRoughness(m);
-    float dP, sP, cP;
-    materialLobeProbabilities(m, dP, sP, cP);
     float c0 = randomFloat(state);
     float c1 = randomFloat(state);
     float3 diffuseDir = orientHemisphere(cosineHemisphere(c0, c1), h.normal);
     float lobe = randomFloat(state);
     float3 next;
-    if (lobe < cP) {
+    if (lobe < sp.cP) {
         float a = randomFloat(state);
         float b = randomFloat(state);
-        float3 hv = sampleGGXVisibleNormal(a, b, h.normal, h.tangent, h.bitangent, view, ccR, 0.0f);
+        float3 hv = sampleVNDF(sp, a, b, sp.ccAlpha);
         next = normalize(reflect(ray.direction, hv));
         if (dot(next, h.normal) <= 0.0f) {
             next = diffuseDir;
-            tp *= materialDiffuseBounceWeight(m, h.normal, view, next) / fmaxf(dP, 1e-5f);
+            tp *= diffuseBounceWeight(m, sp, next) / fmaxf(sp.dP, 1e-5f);
         } else {
             float nDotL = fmaxf(dot(h.normal, next), 1e-5f);
             float vDotH = fmaxf(dot(view, hv), 1e-5f);
-            tp *= clearcoat * fresnelSchlickThinFilm(vDotH, materialClearcoatF0Color(m), m) *
-                  geometrySmithG1GGX(nDotL, ccR) / fmaxf(cP, 1e-5f);
+            tp *= sp.clearcoat * fresnelSchlickThinFilm(vDotH, sp.ccF0, m) * geometrySmithG1GGX(nDotL, sp.ccR) /
+                  fmaxf(sp.cP, 1e-5f);
         }
-    } else if (lobe < cP + sP) {
+    } else if (lobe < sp.cP + sp.sP) {
         float a = randomFloat(state);
         float b = randomFloat(state);
-        float3 hv = sampleGGXVisibleNormal(a, b, h.normal, h.tangent, h.bitangent, view, roughness, anisotropy);
+        float3 hv = sampleVNDF(sp, a, b, sp.specAlpha);
         next = normalize(reflect(ray.direction, hv));
         if (dot(next, h.normal) <= 0.0f) {
             next = diffuseDir;
-            tp *= materialDiffuseBounceWeight(m, h.normal, view, next) / fmaxf(dP, 1e-5f);
+            tp *= diffuseBounceWeight(m, sp, next) / fmaxf(sp.dP, 1e-5f);
         } else {
             float vDotH = fmaxf(dot(view, hv), 1e-5f);
-            float3 fres = fresnelSchlickThinFilm(vDotH, f0, m);
+            float3 fres = fresnelSchlickThinFilm(vDotH, sp.f0, m);
             float3 cca = materialClearcoatAttenuationForDirection(m, h.normal, view, next);
-            tp *= cca * fres * geometrySmithG1GGXAnisotropic(next, h.normal, h.tangent, h.bitangent, roughness, anisotropy) /
-                  fmaxf(sP, 1e-5f);
+            // The reference passes the raw tangent / bitangent here (PathTrace.metal:5486-5493).
+            tp *= cca * fres *
+                  geometrySmithG1GGXAnisotropic(next, h.normal, h.tangent, h.bitangent, sp.roughness, sp.anisotropy) /
+                  fmaxf(sp.sP, 1e-5f);
         }
     } else {
         next = diffuseDir;
-        tp *= materialDiffuseBounceWeight(m, h.normal, view, next) / fmaxf(dP, 1e-5f);
+        tp *= diffuseBounceWeight(m, sp, next) / fmaxf(sp.dP, 1e-5f);
     }
-    prevPdf = materialBSDFPDF(m, h.normal, h.tangent, h.bitangent, view, next);
+    prevPdf = bsdfPDF(sp, next);
     ray.origin = shadowOrigin;
     ray.direction = next;
     bool dead = terminatePathWithRussianRoulette(bounce, tp, state);
@@ -538,7 +535,11 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
     return out;
 }
 
-__global__ void __launch_bounds__(128) k_shade(DevScene S, DevParams P, Wave W, uint32_t bounce, uint32_t sel) {
+#ifndef DK_SHADE_MIN_BLOCKS
+#define DK_SHADE_MIN_BLOCKS 5
+#endif
+__global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, DevParams P, Wave W, uint32_t bounce,
+                                                                  uint32_t sel) {
     const uint32_t* q = W.q[sel];
     uint32_t* qNext = W.q[sel ^ 1u];
     const uint32_t n = W.counts[sel];

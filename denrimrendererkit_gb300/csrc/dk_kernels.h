@@ -26,9 +26,11 @@ struct DevScene {
     const float4* texpix;
     const dk_light_record* lights;
     const float2* env;
+    const uint32_t* env_guide;  // G + 1 entries: first index with cdf >= b / G (G a power of two)
     uint32_t tri_count, mat_count, node_count, texdesc_count;
     uint32_t light_count, env_count, env_tex_plus1, all_shadow_opaque;
-    float env_intensity, env_rot_y, env_max_radiance, pad0;
+    float env_intensity, env_rot_y, env_max_radiance;
+    uint32_t env_guide_size;
 };
 
 // GPURenderConstants (PathTrace.metal:143-182) for one batch of samples.

@@ -206,14 +206,6 @@ __device__ __forceinline__ float geometrySmithG1GGX(float nDotV, float roughness
     float den = nDotV + sqrtf(fmaxf(a2 + (1.0f - a2) * nDotV * nDotV, 0.0f));
     return (2.0f * nDotV) / fmaxf(den, 1e-5f);
 }
-__device__ float distributionGGXAnisotropic(float3 h, float3 n, float3 t, float3 b, float r, float an) {  // :1207-1227
-    float nDotH = fmaxf(dot(n, h), 0.0f);
-    if (nDotH <= 0.0f) return 0.0f;
-    float2 a = anisotropicGGXAlpha(r, an);
-    float tDotH = dot(t, h), bDotH = dot(b, h);
-    float den = (tDotH * tDotH) / fmaxf(a.x * a.x, 1e-6f) + (bDotH * bDotH) / fmaxf(a.y * a.y, 1e-6f) + nDotH * nDotH;
-    return 1.0f / fmaxf(3.14159265359f * a.x * a.y * den * den, 1e-6f);
-}
 __device__ float geometrySmithG1GGXAnisotropic(float3 d, float3 n, float3 t, float3 b, float r, float an) {  // :1229-1250
     float nDotD = fmaxf(dot(n, d), 0.0f);
     if (nDotD <= 0.0f) return 0.0f;
@@ -248,34 +240,6 @@ __device__ float3 materialClearcoatAttenuationForDirection(const Material& m, fl
     float3 att = mx(f3(0.0f), f3(1.0f) - ccF * clearcoat);
     return att * materialClearcoatDepthAttenuation(m, n, v, l);
 }
-__device__ __noinline__ float3 evaluateMaterialBRDF(const Material& m, float3 n, float3 tg, float3 bt, float3 v, float3 l) {  // :1323-1384
-    const float inversePi = 0.31830988618f;
-    float roughness = clampf(m.parameters.x, 0.02f, 1.0f);
-    float metallic = clampf(m.parameters.y, 0.0f, 1.0f);
-    float3 h = normalize(v + l);
-    float nDotL = fmaxf(dot(n, l), 0.0f), nDotV = fmaxf(dot(n, v), 0.0f);
-    float nDotH = fmaxf(dot(n, h), 0.0f), vDotH = fmaxf(dot(v, h), 0.0f);
-    if (nDotL <= 0.0f || nDotV <= 0.0f) return f3(0.0f);
-    float3 f0 = materialF0(m);
-    float3 tint = thinFilmTint(m, vDotH);
-    float3 fresnel = fresnelSchlick(vDotH, f0) * tint;
-    TangentFrame fr = makeTangentFrame(n, tg, bt);
-    float an = materialSpecularAnisotropy(m);
-    float D = distributionGGXAnisotropic(h, n, fr.tangent, fr.bitangent, roughness, an);
-    float G = geometrySmithG1GGXAnisotropic(v, n, fr.tangent, fr.bitangent, roughness, an) *
-              geometrySmithG1GGXAnisotropic(l, n, fr.tangent, fr.bitangent, roughness, an);
-    float3 specular = D * G * fresnel / fmaxf(4.0f * nDotV * nDotL, 1e-5f);
-    float clearcoat = materialClearcoat(m);
-    float ccR = materialClearcoatRoughness(m);
-    float3 ccFresnel = fresnelSchlick(vDotH, materialClearcoatF0Color(m)) * tint;
-    float ccD = distributionGGX(nDotH, ccR);
-    float ccG = geometrySmithG1GGX(nDotV, ccR) * geometrySmithG1GGX(nDotL, ccR);
-    float3 ccSpecular = ccD * ccG * ccFresnel / fmaxf(4.0f * nDotV * nDotL, 1e-5f);
-    float3 ccAtt = materialClearcoatAttenuationForDirection(m, n, v, l);
-    float3 diffuse = ccAtt * (f3(1.0f) - fresnel) * (1.0f - metallic) * xyz(m.baseColor) * inversePi;
-    float3 sheen = evaluateMaterialSheenBRDF(m, n, v, l);
-    return diffuse + ccAtt * (specular + sheen) + ccSpecular * clearcoat;
-}
 __device__ __forceinline__ float powerHeuristic(float a, float b) {  // :1386-1390
     float a2 = a * a, b2 = b * b;
     return a2 / fmaxf(a2 + b2, 1e-8f);
@@ -296,37 +260,6 @@ __device__ void materialLobeProbabilities(const Material& m, float& dP, float& s
     else sP = clampf(specularW / total, 0.08f, remaining);
     dP = fmaxf(0.0f, 1.0f - sP - cP);
 }
-__device__ float ggxReflectionPDF(float3 n, float3 tg, float3 bt, float3 v, float3 l, float r, float an) {  // :1424-1443
-    float3 h = normalize(v + l);
-    float nDotH = fmaxf(dot(n, h), 0.0f), nDotV = fmaxf(dot(n, v), 0.0f), vDotH = fmaxf(dot(v, h), 0.0f);
-    if (nDotH <= 0.0f || nDotV <= 0.0f || vDotH <= 0.0f) return 0.0f;
-    TangentFrame f = makeTangentFrame(n, tg, bt);
-    return distributionGGXAnisotropic(h, n, f.tangent, f.bitangent, r, an) *
-           geometrySmithG1GGXAnisotropic(v, n, f.tangent, f.bitangent, r, an) / fmaxf(4.0f * nDotV, 1e-5f);
-}
-__device__ __noinline__ float materialBSDFPDF(const Material& m, float3 n, float3 tg, float3 bt, float3 v, float3 l) {  // :1445-1490
-    float nDotL = fmaxf(dot(n, l), 0.0f), nDotV = fmaxf(dot(n, v), 0.0f);
-    if (nDotL <= 0.0f || nDotV <= 0.0f) return 0.0f;
-    float dP, sP, cP;
-    materialLobeProbabilities(m, dP, sP, cP);
-    float roughness = clampf(m.parameters.x, 0.02f, 1.0f);
-    float an = materialSpecularAnisotropy(m);
-    float specPDF = ggxReflectionPDF(n, tg, bt, v, l, roughness, an);
-    float ccPDF = ggxReflectionPDF(n, tg, bt, v, l, materialClearcoatRoughness(m), 0.0f);
-    return dP * (nDotL * 0.31830988618f) + sP * specPDF + cP * ccPDF;
-}
-__device__ __noinline__ float3 materialDiffuseBounceWeight(const Material& m, float3 n, float3 v, float3 l) {  // :1492-1518
-    float metallic = clampf(m.parameters.y, 0.0f, 1.0f);
-    float3 hd = v + l;
-    if (dot(hd, hd) <= 1e-8f) return f3(0.0f);
-    float3 h = normalize(hd);
-    float vDotH = fmaxf(dot(v, h), 0.0f);
-    float3 fresnel = fresnelSchlickThinFilm(vDotH, materialF0(m), m);
-    float3 ccAtt = materialClearcoatAttenuationForDirection(m, n, v, l);
-    float3 diffuse = (f3(1.0f) - fresnel) * (1.0f - metallic) * xyz(m.baseColor);
-    float3 sheen = evaluateMaterialSheenBRDF(m, n, v, l) * 3.14159265359f;
-    return ccAtt * (diffuse + sheen);
-}
 __device__ __forceinline__ bool terminatePathWithRussianRoulette(uint32_t bounce, float3& tp, uint32_t& state) {  // :1520-1540
     float w = maxComponent(tp);
     if (w <= 0.0f) return true;
@@ -335,6 +268,142 @@ __device__ __forceinline__ bool terminatePathWithRussianRoulette(uint32_t bounce
     if (randomFloat(state) > survival) return true;
     tp /= survival;
     return false;
+}
+
+// ------------------------------------------------ per-shading-point cache --
+// The reference re-derives the tangent frame, GGX alphas, lobe probabilities
+// and the view-side Smith terms inside every BRDF / PDF evaluation (three NEE
+// directions, the sampled direction and its PDF).  They depend only on the
+// shading point, so they are computed once here; each evaluation below then
+// performs the remaining operations of evaluateMaterialBRDF (:1323-1384),
+// materialBSDFPDF (:1445-1490) and materialDiffuseBounceWeight (:1492-1518)
+// in the reference's order.
+struct ShadePoint {
+    float3 n, t, b, v;      // normal, raw tangent/bitangent, view direction
+    TangentFrame fr;        // makeTangentFrame(n, t, b)
+    float nDotV;            // max(dot(n, v), 0)
+    float roughness, metallic, clearcoat, ccR, anisotropy;
+    float3 baseColor, f0, ccF0;
+    float2 specAlpha, ccAlpha;
+    float g1vSpecAniso, g1vCCAniso, g1vCCIso;
+    float dP, sP, cP;
+};
+
+__device__ __forceinline__ float distributionGGXAnisotropicA(float3 h, float3 n, float3 t, float3 b, float2 a) {
+    float nDotH = fmaxf(dot(n, h), 0.0f);
+    if (nDotH <= 0.0f) return 0.0f;
+    float tDotH = dot(t, h), bDotH = dot(b, h);
+    float den = (tDotH * tDotH) / fmaxf(a.x * a.x, 1e-6f) + (bDotH * bDotH) / fmaxf(a.y * a.y, 1e-6f) + nDotH * nDotH;
+    return 1.0f / fmaxf(3.14159265359f * a.x * a.y * den * den, 1e-6f);
+}
+__device__ __forceinline__ float g1AnisoA(float3 d, float3 n, float3 t, float3 b, float2 a) {
+    float nDotD = fmaxf(dot(n, d), 0.0f);
+    if (nDotD <= 0.0f) return 0.0f;
+    float tD = dot(t, d), bD = dot(b, d);
+    float root = sqrtf(fmaxf(a.x * a.x * tD * tD + a.y * a.y * bD * bD + nDotD * nDotD, 0.0f));
+    return (2.0f * nDotD) / fmaxf(nDotD + root, 1e-5f);
+}
+
+__device__ void makeShadePoint(ShadePoint& sp, const Material& m, float3 n, float3 t, float3 b, float3 v) {
+    sp.n = n;
+    sp.t = t;
+    sp.b = b;
+    sp.v = v;
+    sp.fr = makeTangentFrame(n, t, b);
+    sp.nDotV = fmaxf(dot(n, v), 0.0f);
+    sp.roughness = clampf(m.parameters.x, 0.02f, 1.0f);
+    sp.metallic = clampf(m.parameters.y, 0.0f, 1.0f);
+    sp.clearcoat = materialClearcoat(m);
+    sp.ccR = materialClearcoatRoughness(m);
+    sp.anisotropy = materialSpecularAnisotropy(m);
+    sp.baseColor = xyz(m.baseColor);
+    sp.f0 = materialF0(m);
+    sp.ccF0 = materialClearcoatF0Color(m);
+    sp.specAlpha = anisotropicGGXAlpha(sp.roughness, sp.anisotropy);
+    sp.ccAlpha = anisotropicGGXAlpha(sp.ccR, 0.0f);
+    sp.g1vSpecAniso = g1AnisoA(v, n, sp.fr.tangent, sp.fr.bitangent, sp.specAlpha);
+    sp.g1vCCAniso = g1AnisoA(v, n, sp.fr.tangent, sp.fr.bitangent, sp.ccAlpha);
+    sp.g1vCCIso = geometrySmithG1GGX(sp.nDotV, sp.ccR);
+    materialLobeProbabilities(m, sp.dP, sp.sP, sp.cP);
+}
+
+// materialClearcoatAttenuationForDirection with the clearcoat Fresnel at the
+// already-known half vector.
+__device__ __forceinline__ float3 clearcoatAttenuationAt(const Material& m, const ShadePoint& sp, float3 l,
+                                                         float3 ccFresnel, bool halfOk) {
+    if (sp.clearcoat <= 0.0f || !halfOk) return f3(1.0f);
+    float3 att = mx(f3(0.0f), f3(1.0f) - ccFresnel * sp.clearcoat);
+    return att * materialClearcoatDepthAttenuation(m, sp.n, sp.v, l);
+}
+
+__device__ __noinline__ float3 evalBRDF(const Material& m, const ShadePoint& sp, float3 l) {  // :1323-1384
+    const float inversePi = 0.31830988618f;
+    float3 hd = sp.v + l;
+    float3 h = normalize(hd);
+    float nDotL = fmaxf(dot(sp.n, l), 0.0f);
+    float nDotH = fmaxf(dot(sp.n, h), 0.0f), vDotH = fmaxf(dot(sp.v, h), 0.0f);
+    if (nDotL <= 0.0f || sp.nDotV <= 0.0f) return f3(0.0f);
+    float3 tint = thinFilmTint(m, vDotH);
+    float3 fresnel = fresnelSchlick(vDotH, sp.f0) * tint;
+    float D = distributionGGXAnisotropicA(h, sp.n, sp.fr.tangent, sp.fr.bitangent, sp.specAlpha);
+    float G = sp.g1vSpecAniso * g1AnisoA(l, sp.n, sp.fr.tangent, sp.fr.bitangent, sp.specAlpha);
+    float3 specular = D * G * fresnel / fmaxf(4.0f * sp.nDotV * nDotL, 1e-5f);
+    float3 ccFresnel = fresnelSchlick(vDotH, sp.ccF0) * tint;
+    float ccD = distributionGGX(nDotH, sp.ccR);
+    float ccG = sp.g1vCCIso * geometrySmithG1GGX(nDotL, sp.ccR);
+    float3 ccSpecular = ccD * ccG * ccFresnel / fmaxf(4.0f * sp.nDotV * nDotL, 1e-5f);
+    float3 ccAtt = clearcoatAttenuationAt(m, sp, l, ccFresnel, dot(hd, hd) > 1e-8f);
+    float3 diffuse = ccAtt * (f3(1.0f) - fresnel) * (1.0f - sp.metallic) * sp.baseColor * inversePi;
+    float3 sheen = evaluateMaterialSheenBRDF(m, sp.n, sp.v, l);
+    return diffuse + ccAtt * (specular + sheen) + ccSpecular * sp.clearcoat;
+}
+
+__device__ __forceinline__ float ggxPDFAt(const ShadePoint& sp, float3 h, float nDotH, float vDotH, float2 a,
+                                          float g1v) {  // ggxReflectionPDF (:1424-1443)
+    if (nDotH <= 0.0f || sp.nDotV <= 0.0f || vDotH <= 0.0f) return 0.0f;
+    return distributionGGXAnisotropicA(h, sp.n, sp.fr.tangent, sp.fr.bitangent, a) * g1v / fmaxf(4.0f * sp.nDotV, 1e-5f);
+}
+
+__device__ __noinline__ float bsdfPDF(const ShadePoint& sp, float3 l) {  // :1445-1490
+    float nDotL = fmaxf(dot(sp.n, l), 0.0f);
+    if (nDotL <= 0.0f || sp.nDotV <= 0.0f) return 0.0f;
+    float3 h = normalize(sp.v + l);
+    float nDotH = fmaxf(dot(sp.n, h), 0.0f), vDotH = fmaxf(dot(sp.v, h), 0.0f);
+    float specPDF = ggxPDFAt(sp, h, nDotH, vDotH, sp.specAlpha, sp.g1vSpecAniso);
+    float ccPDF = ggxPDFAt(sp, h, nDotH, vDotH, sp.ccAlpha, sp.g1vCCAniso);
+    return sp.dP * (nDotL * 0.31830988618f) + sp.sP * specPDF + sp.cP * ccPDF;
+}
+
+__device__ __noinline__ float3 diffuseBounceWeight(const Material& m, const ShadePoint& sp, float3 l) {  // :1492-1518
+    float3 hd = sp.v + l;
+    if (dot(hd, hd) <= 1e-8f) return f3(0.0f);
+    float3 h = normalize(hd);
+    float vDotH = fmaxf(dot(sp.v, h), 0.0f);
+    float3 tint = thinFilmTint(m, vDotH);
+    float3 fresnel = fresnelSchlick(vDotH, sp.f0) * tint;
+    float3 ccAtt = clearcoatAttenuationAt(m, sp, l, fresnelSchlick(vDotH, sp.ccF0) * tint, true);
+    float3 diffuse = (f3(1.0f) - fresnel) * (1.0f - sp.metallic) * sp.baseColor;
+    float3 sheen = evaluateMaterialSheenBRDF(m, sp.n, sp.v, l) * 3.14159265359f;
+    return ccAtt * (diffuse + sheen);
+}
+
+// sampleGGXVisibleNormal (:1620-1660) with the shading point's frame.
+__device__ __noinline__ float3 sampleVNDF(const ShadePoint& sp, float ux, float uy, float2 a) {
+    float3 lv = normalize(f3(dot(sp.v, sp.fr.tangent), dot(sp.v, sp.fr.bitangent), fmaxf(dot(sp.v, sp.n), 1e-5f)));
+    float3 sv = normalize(f3(a.x * lv.x, a.y * lv.y, lv.z));
+    float lensq = sv.x * sv.x + sv.y * sv.y;
+    float3 t1 = lensq > 1e-7f ? f3(-sv.y, sv.x, 0.0f) * (1.0f / sqrtf(lensq)) : f3(1, 0, 0);
+    float3 t2 = cross(sv, t1);
+    float radius = sqrtf(ux);
+    float s, c;
+    sincosf(6.28318530718f * uy, &s, &c);
+    float p1 = radius * c;
+    float p2 = radius * s;
+    float blend = 0.5f * (1.0f + sv.z);
+    p2 = mixf(sqrtf(fmaxf(0.0f, 1.0f - p1 * p1)), p2, blend);
+    float3 vn = p1 * t1 + p2 * t2 + sqrtf(fmaxf(0.0f, 1.0f - p1 * p1 - p2 * p2)) * sv;
+    float3 lh = normalize(f3(a.x * vn.x, a.y * vn.y, fmaxf(vn.z, 0.0f)));
+    return normalize(lh.x * sp.fr.tangent + lh.y * sp.fr.bitangent + lh.z * sp.n);
 }
 
 // --------------------------------------------------------------- lights ----
@@ -376,26 +445,6 @@ __device__ float3 sampleGGXHalfVector(float ux, float uy, float3 n, float roughn
     float cosT = sqrtf((1.0f - uy) / fmaxf(1.0f + (a2 - 1.0f) * uy, 1e-5f));
     float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
     return orientHemisphere(f3(c * sinT, s * sinT, cosT), n);
-}
-__device__ __noinline__ float3 sampleGGXVisibleNormal(float ux, float uy, float3 n, float3 tg, float3 bt, float3 v, float r,
-                                         float an) {  // :1620-1660
-    TangentFrame fr = makeTangentFrame(n, tg, bt);
-    float2 a = anisotropicGGXAlpha(r, an);
-    float3 lv = normalize(f3(dot(v, fr.tangent), dot(v, fr.bitangent), fmaxf(dot(v, n), 1e-5f)));
-    float3 sv = normalize(f3(a.x * lv.x, a.y * lv.y, lv.z));
-    float lensq = sv.x * sv.x + sv.y * sv.y;
-    float3 t1 = lensq > 1e-7f ? f3(-sv.y, sv.x, 0.0f) * (1.0f / sqrtf(lensq)) : f3(1, 0, 0);
-    float3 t2 = cross(sv, t1);
-    float radius = sqrtf(ux);
-    float s, c;
-    sincosf(6.28318530718f * uy, &s, &c);
-    float p1 = radius * c;
-    float p2 = radius * s;
-    float blend = 0.5f * (1.0f + sv.z);
-    p2 = mixf(sqrtf(fmaxf(0.0f, 1.0f - p1 * p1)), p2, blend);
-    float3 vn = p1 * t1 + p2 * t2 + sqrtf(fmaxf(0.0f, 1.0f - p1 * p1 - p2 * p2)) * sv;
-    float3 lh = normalize(f3(a.x * vn.x, a.y * vn.y, fmaxf(vn.z, 0.0f)));
-    return normalize(lh.x * fr.tangent + lh.y * fr.bitangent + lh.z * n);
 }
 __device__ __forceinline__ float3 sampleTriangle(const dk_triangle& tri, float rx, float ry) {  // :1711-1717
     float su0 = sqrtf(rx);
@@ -477,10 +526,19 @@ __device__ __noinline__ float3 sampleEnvironmentDirection(const DevScene& S, flo
     uint4 md = __ldg(reinterpret_cast<const uint4*>(&S.texdesc[S.env_tex_plus1 - 1u]));
     uint32_t w = md.y, hgt = md.z;
     if (w == 0u || hgt == 0u) return f3(0, 1, 0);
+    // selectEnvironmentSampleIndex: the first index with target <= cdf[i]
+    // (clamped to the last).  The guide table bounds that index for the
+    // target's 1/G bucket, so the search covers only the bucket's range and
+    // returns the same index as the full binary search over a monotone CDF.
     uint32_t index = 0u;
     if (S.env_count > 1u) {
         float target = clampf(cdfSample, 0.0f, 0.99999994f);
         uint32_t lo = 0u, hi = S.env_count - 1u;
+        if (S.env_guide_size) {
+            uint32_t bucket = min((uint32_t)(target * (float)S.env_guide_size), S.env_guide_size - 1u);
+            lo = min(__ldg(S.env_guide + bucket), S.env_count - 1u);
+            hi = min(__ldg(S.env_guide + bucket + 1u), S.env_count - 1u);
+        }
         while (lo < hi) {
             uint32_t mid = (lo + hi) >> 1u;
             if (target <= __ldg(&S.env[mid].x)) hi = mid; else lo = mid + 1u;
