@@ -164,7 +164,21 @@ EXPORTED_SYMBOLS = (
     "dk_session_render_tile", "dk_session_update_camera", "dk_session_reset",
     "dk_session_read_output", "dk_session_sample_count", "dk_session_stats",
     "dk_session_destroy", "dk_last_error_message", "dk_build_bvh", "dk_build_lights",
-    "dk_build_environment_samples", "dk_build_environment_samples_noalloc", "dk_version",
+    "dk_build_environment_samples", "dk_build_environment_samples_noalloc", "dk_build_sparse_sphere_volume",
+    "dk_sparse_volume_view", "dk_sparse_volume_destroy", "dk_version",
 )
+
+
+class SdfSphere(C.Structure):
+    """dk_sdf_sphere."""
+    _fields_ = [("center", C.c_float * 3), ("radius", C.c_float), ("material", C.c_uint32),
+                ("smooth_union_radius", C.c_float)]
+
+
+class SparseVolumeSettings(C.Structure):
+    """dk_sparse_volume_settings."""
+    _fields_ = [("resolution", C.c_uint32 * 3), ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+                ("brick_size", C.c_uint32 * 3), ("narrow_band", C.c_float), ("volume_material", C.c_uint32),
+                ("object_id", C.c_uint32), ("primitive_id", C.c_uint32)]
 
 assert C.sizeof(Camera) == 80

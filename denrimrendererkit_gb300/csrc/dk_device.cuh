@@ -30,6 +30,8 @@ struct Hit {
     float3 tangent;
     float3 bitangent;
     uint32_t materialID;
+    uint32_t materialID2;
+    float materialBlend;
     uint32_t objectID;
     uint32_t primitiveID;
     bool frontFacing;
@@ -345,6 +347,8 @@ __device__ __forceinline__ Hit makeHit(const DevScene& S, const Ray& ray, const 
     h.bitangent = ex::normalize(xyz(__ldg(reinterpret_cast<const float4*>(&tri.bitangent))));
     uint4 ids = __ldg(reinterpret_cast<const uint4*>(&tri.material_id));
     h.materialID = ids.x;
+    h.materialID2 = ids.x;
+    h.materialBlend = 0.0f;
     h.objectID = ids.y;
     h.primitiveID = r.tri;
     return h;

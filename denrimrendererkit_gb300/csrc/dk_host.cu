@@ -331,9 +331,20 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
         return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no renderable geometry.");
     if (sc->material_count == 0 || !sc->materials)
         return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no materials.");
-    if (sc->volume_count != 0)
-        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: distance volumes are not supported by this backend.");
-    if (!sc->triangles) return fail(DK_ERROR_INVALID_ARGUMENT, "triangles is null");
+    if (sc->volume_count != 0) {
+        if (!sc->volumes) return fail(DK_ERROR_INVALID_ARGUMENT, "volumes is null while volume_count is not zero");
+        for (uint32_t i = 0; i < sc->volume_count; ++i)
+            if (sc->volumes[i].metadata.w != 1u)
+                return fail(DK_ERROR_INVALID_SCENE,
+                            "Invalid render scene: only sparse-brick distance volumes are supported by this backend.");
+        if ((sc->volume_brick_count && !sc->volume_bricks) || (sc->volume_brick_sample_count && !sc->volume_brick_samples) ||
+            (sc->volume_brick_grid_count && !sc->volume_brick_grids) ||
+            (sc->volume_brick_grid_index_count && !sc->volume_brick_grid_indices))
+            return fail(DK_ERROR_INVALID_ARGUMENT, "a volume array pointer is null while its count is not zero");
+        if (sc->volume_brick_sample_count >= (1ull << 32) || sc->volume_brick_grid_index_count >= (1ull << 32))
+            return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: volume arrays exceed 2^32 entries.");
+    }
+    if (sc->triangle_count && !sc->triangles) return fail(DK_ERROR_INVALID_ARGUMENT, "triangles is null");
     if ((sc->light_count && !sc->lights) || (sc->environment_sample_count && !sc->environment_samples) ||
         (sc->texture_descriptor_count && !sc->texture_descriptors) || (sc->texture_pixel_count && !sc->texture_pixels) ||
         (sc->node_count && !sc->nodes) || (sc->primitive_index_count && !sc->primitive_indices))
@@ -423,6 +434,34 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
             TRY(upload(s, const_cast<uint32_t**>(&D.env_guide), guide.data(), guide.size(), "environment guide"));
             D.env_guide_size = G;
         }
+    }
+    // Sparse distance volumes: the reference arrays plus a distance-only copy
+    // of the packed samples for the march.
+    if (sc->volume_count) {
+        TRY(upload(s, const_cast<dk_volume_descriptor**>(&D.volumes), sc->volumes, sc->volume_count, "volumes"));
+        TRY(upload(s, const_cast<dk_volume_brick_descriptor**>(&D.bricks), sc->volume_bricks, sc->volume_brick_count,
+                   "volume bricks"));
+        TRY(upload(s, const_cast<dk_volume_brick_sample**>(&D.brick_samples), sc->volume_brick_samples,
+                   (size_t)sc->volume_brick_sample_count, "volume brick samples"));
+        std::vector<float> dist((size_t)sc->volume_brick_sample_count);
+        for (size_t i = 0; i < dist.size(); ++i) dist[i] = sc->volume_brick_samples[i].distance;
+        TRY(upload(s, const_cast<float**>(&D.brick_dist), dist.data(), dist.size(), "volume brick distances"));
+        TRY(upload(s, const_cast<dk_volume_brick_grid**>(&D.brick_grids), sc->volume_brick_grids,
+                   sc->volume_brick_grid_count, "volume brick grids"));
+        TRY(upload(s, const_cast<uint32_t**>(&D.brick_grid_indices), sc->volume_brick_grid_indices,
+                   (size_t)sc->volume_brick_grid_index_count, "volume brick grid indices"));
+        D.volume_count = sc->volume_count;
+        D.brick_count = sc->volume_brick_count;
+        D.brick_sample_count = sc->volume_brick_sample_count;
+        D.brick_grid_count = sc->volume_brick_grid_count;
+        D.brick_grid_index_count = sc->volume_brick_grid_index_count;
+        bool volOpaque = true;
+        for (uint32_t i = 0; i < sc->material_count; ++i) {
+            const dk_material& m = sc->materials[i];
+            float transmission = std::fmin(std::fmax(m.emission.w, 0.0f), 1.0f);
+            if (!(m.base_color.w > 0.001f && transmission <= 0.001f)) volOpaque = false;
+        }
+        D.volume_all_opaque = volOpaque ? 1u : 0u;
     }
     D.tri_count = sc->triangle_count;
     D.mat_count = sc->material_count;

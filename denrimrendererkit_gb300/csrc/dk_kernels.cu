@@ -16,6 +16,7 @@
 #include <cstdio>
 
 #include "dk_kernels.h"
+#include "dk_sdf.cuh"
 #include "dk_shade.cuh"
 
 namespace dk {
@@ -85,8 +86,98 @@ __device__ Hit applyNormalMap(const DevScene& S, Hit h, uint32_t idx, float3 ray
     return h;
 }
 
-__device__ __forceinline__ Material materialForHit(const DevScene& S, const Hit& h) {  // :1096-1121
-    return loadMaterial(S.mats, min(h.materialID, S.mat_count - 1u));
+__device__ __forceinline__ float4 exMix4(float4 a, float4 b, float t) {
+    return make_float4(exMix(a.x, b.x, t), exMix(a.y, b.y, t), exMix(a.z, b.z, t), exMix(a.w, b.w, t));
+}
+
+// blendMaterials (:527-547): m = mix(m, materials[b], t) field by field.
+__device__ __noinline__ void blendMaterialInto(Material& m, const dk_material* mats, uint32_t b, float t) {
+    const float4* p = reinterpret_cast<const float4*>(mats + b);
+    float4* f = reinterpret_cast<float4*>(&m);
+#pragma unroll 1
+    for (int k = 0; k < 17; ++k) f[k] = exMix4(f[k], __ldg(p + k), t);
+}
+
+// materialForHit (:1096-1121); the material-program VM and the field
+// overrides are no-ops here (no programs, no material-field samples).
+__device__ __forceinline__ Material materialForHit(const DevScene& S, const Hit& h) {
+    Material m = loadMaterial(S.mats, min(h.materialID, S.mat_count - 1u));
+    if (h.materialBlend > 0.0f)
+        blendMaterialInto(m, S.mats, min(h.materialID2, S.mat_count - 1u), clampf(h.materialBlend, 0.0f, 1.0f));
+    return m;
+}
+
+__device__ __forceinline__ VolumeScene volumeScene(const DevScene& S) {
+    VolumeScene V;
+    V.volumes = S.volumes;
+    V.bricks = S.bricks;
+    V.samples = S.brick_samples;
+    V.dist = S.brick_dist;
+    V.grids = S.brick_grids;
+    V.gridIndices = S.brick_grid_indices;
+    V.sampleCount = S.brick_sample_count;
+    V.gridIndexCount = S.brick_grid_index_count;
+    V.volumeCount = S.volume_count;
+    V.brickCount = S.brick_count;
+    V.gridCount = S.brick_grid_count;
+    return V;
+}
+
+// Hit attributes of a distance-field hit at (t, brick): the tail of
+// intersectVolumeBrickPrepared (PathTrace.metal:2741-2802).
+__device__ __noinline__ Hit makeVolumeHit(const DevScene& S, const Ray& ray, float t, uint32_t brickIndex) {
+    VolumeScene V = volumeScene(S);
+    const dk_volume_brick_descriptor& brick = V.bricks[brickIndex];
+    uint32_t vi = __ldg(&brick.grid_origin_and_volume.w);
+    if (vi >= V.volumeCount) vi = 0;
+    const dk_volume_descriptor& vol = V.volumes[vi];
+    VolumeRay vr = volumeRay(vol, ray.origin, ray.direction);
+    BrickCtx c = makeBrickCtx(brick, V.sampleCount);
+    float3 rp = ex::add(vr.lo, ex::mul(vr.ld, t));
+    bool cubic = vr.cellSize <= 0.03f;
+    Hit h;
+    h.t = t;
+    h.position = ex::add(ray.origin, ex::mul(ray.direction, t));
+    float3 n = brickNormal(V, vol, c, rp, cubic, !cubic);
+    h.frontFacing = ex::dot(n, ray.direction) <= 0.0f;
+    if (!h.frontFacing) n = -n;
+    h.normal = n;
+    h.uv = make_float2(0.0f, 0.0f);
+    h.tangent = ex::normalize(ex::cross(fabsf(n.y) < 0.999f ? f3(0, 1, 0) : f3(1, 0, 0), n));
+    h.bitangent = ex::normalize(ex::cross(n, h.tangent));
+    // sampleVolumeBrickMaterial: nearest stored sample (:2319-2372)
+    float3 uvw = clamp3(exDiv(ex::sub(rp, c.sampleMin), c.sampleExtent), f3(0.0f), f3(1.0f));
+    uint32_t nx = min((uint32_t)roundf(ex::mul(uvw.x, (float)(c.dims[0] - 1u))), c.dims[0] - 1u);
+    uint32_t ny = min((uint32_t)roundf(ex::mul(uvw.y, (float)(c.dims[1] - 1u))), c.dims[1] - 1u);
+    uint32_t nz = min((uint32_t)roundf(ex::mul(uvw.z, (float)(c.dims[2] - 1u))), c.dims[2] - 1u);
+    uint4 ms = __ldg(reinterpret_cast<const uint4*>(V.samples + c.sampleOffset + nx + ny * c.strideY + nz * c.strideZ));
+    h.materialID = ms.y;
+    h.materialID2 = ms.z;
+    h.materialBlend = clampf(__uint_as_float(ms.w), 0.0f, 1.0f);
+    h.objectID = __ldg(&vol.metadata.y);
+    h.primitiveID = __ldg(&vol.metadata.z);
+    return h;
+}
+
+__device__ __forceinline__ Hit makeHitAny(const DevScene& S, const Ray& ray, const HitRec& r) {
+    if (r.tri == kVolumeHit) return makeVolumeHit(S, ray, r.t, __float_as_uint(r.u));
+    return makeHit(S, ray, r);
+}
+
+// intersectScene (:3294-3421): triangles, then the sparse volumes with the
+// triangle distance as the bound.
+__device__ __noinline__ HitRec traceScene(const DevScene& S, float3 o, float3 d) {
+    HitRec r = traceClosest(S, o, d);
+    if (S.volume_count) {
+        VolumeHitRec vh;
+        if (closestVolumeHit(volumeScene(S), o, d, r.t, vh)) {
+            r.t = vh.t;
+            r.tri = kVolumeHit;
+            r.u = __uint_as_float(vh.brick);
+            r.v = 0.0f;
+        }
+    }
+    return r;
 }
 
 // Subsurface walk helpers (PathTrace.metal:3490-3523).
@@ -106,6 +197,7 @@ __device__ __forceinline__ float subsurfaceBoundaryPDF(float3 s, float d) {
 }
 
 // continueSubsurfaceRandomWalk (PathTrace.metal:3525-3621).
+template <bool kVolumes>
 __device__ bool continueSubsurfaceRandomWalk(const DevScene& S, const Hit& entry, const Material& m, Ray& ray,
                                              float3& tp, float& prevPdf, uint32_t& state) {
     if (materialSubsurface(m) <= 0.0f || !entry.frontFacing) return false;
@@ -117,7 +209,7 @@ __device__ bool continueSubsurfaceRandomWalk(const DevScene& S, const Hit& entry
     float3 albedo = clamp3(xyz(m.subsurfaceColor), f3(0.0f), f3(0.999f));
     float anisotropy = clampf(m.subsurfaceParameters.x, -0.95f, 0.95f);
     for (uint32_t step = 0u; step < 8u; ++step) {
-        HitRec r = traceClosest(S, medium.origin, medium.direction);
+        HitRec r = kVolumes ? traceScene(S, medium.origin, medium.direction) : traceClosest(S, medium.origin, medium.direction);
         if (r.tri == kNoHit) return false;
         float f0 = randomFloat(state);
         float f1 = randomFloat(state);
@@ -132,7 +224,7 @@ __device__ bool continueSubsurfaceRandomWalk(const DevScene& S, const Hit& entry
             if (maxComponent(tp) <= 1e-4f) return false;
             continue;
         }
-        Hit b = makeHit(S, medium, r);
+        Hit b = kVolumes ? makeHitAny(S, medium, r) : makeHit(S, medium, r);
         float3 exitNormal = normalize(b.frontFacing ? b.normal : -b.normal);
         float x0 = randomFloat(state);
         float x1 = randomFloat(state);
@@ -336,6 +428,7 @@ struct ShadeOut { bool survive; uint32_t neeMask; };
 
 // The body of the reference bounce loop (PathTrace.metal:5252-5518) for one
 // path whose closest hit is already in W.hit.
+template <bool kVolumes>
 __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave& W, uint32_t p, uint32_t bounce) {
     ShadeOut out{false, 0u};
     const uint32_t tileN = P.tile_w * P.tile_h;
@@ -365,8 +458,8 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
         return out;
     }
     HitRec rec{hr.x, tri, hr.z, hr.w};
-    Hit h = makeHit(S, ray, rec);
-    Material m = materialForHit(S, h);
+    Hit h = kVolumes ? makeHitAny(S, ray, rec) : makeHit(S, ray, rec);
+    Material m = kVolumes ? materialForHit(S, h) : loadMaterial(S.mats, min(h.materialID, S.mat_count - 1u));
     uint32_t nIdx = (uint32_t)m.parameters.w;
     if (nIdx != 0u) h = applyNormalMap(S, h, nIdx, ray.direction);
     uint32_t bIdx = (uint32_t)m.parameters.z;
@@ -393,7 +486,7 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
     } else {
         float subsurface = materialSubsurface(m);
         if (subsurface > 0.0f && randomFloat(state) < subsurface &&
-            continueSubsurfaceRandomWalk(S, h, m, ray, tp, prevPdf, state)) {
+            continueSubsurfaceRandomWalk<kVolumes>(S, h, m, ray, tp, prevPdf, state)) {
             continued = true;
         } else if (continueTransmissiveSurface(h, m, ray, tp, prevPdf, state)) {
             continued = true;
@@ -538,6 +631,7 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
 #ifndef DK_SHADE_MIN_BLOCKS
 #define DK_SHADE_MIN_BLOCKS 5
 #endif
+template <bool kVolumes>
 __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, DevParams P, Wave W, uint32_t bounce,
                                                                   uint32_t sel) {
     const uint32_t* q = W.q[sel];
@@ -547,7 +641,7 @@ __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
     const bool lastBounce = bounce + 1u >= P.max_bounces;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
         uint32_t p = q[i];
-        ShadeOut o = shadePath(S, P, W, p, bounce);
+        ShadeOut o = shadePath<kVolumes>(S, P, W, p, bounce);
         bool keep = o.survive && !lastBounce;
         uint32_t slot = warpAppend(&W.counts[sel ^ 1u], keep);
         if (keep) qNext[slot] = p;
@@ -645,6 +739,52 @@ __device__ bool shadowLayers(const DevScene& S, float3 o, float3 d, float tmax, 
     return false;
 }
 
+// shadowOccluded (PathTrace.metal:4196-4274) exactly as the reference walks
+// it — closest hit per layer, including distance-field hits — for scenes with
+// sparse volumes whose layers the single-pass collection does not model.
+__device__ bool shadowWalk(const DevScene& S, float3 o, float3 d, float maxDistance, float3& T) {
+    float traveled = 0.0f;
+    for (uint32_t step = 0; step < 8u; ++step) {
+        HitRec r = traceScene(S, o, d);
+        if (r.tri == kNoHit || traveled + r.t >= maxDistance) return false;
+        Ray ray{o, d};
+        Hit h = makeHitAny(S, ray, r);
+        Material sm = materialForHit(S, h);
+        if (sm.baseColor.w <= 0.001f) {
+            traveled += r.t;
+            o = h.position + d * 0.001f;
+            continue;
+        }
+        float transmission = materialTransmission(sm);
+        if (transmission <= 0.001f) return true;
+        bool insideSolid = !h.frontFacing && !materialThinWalled(sm);
+        float3 medium = (materialHasVolumeScattering(sm) && insideSolid)
+                            ? exp3((-materialVolumeSigmaT(sm)) * r.t)
+                            : materialTransmissionAbsorption(sm, r.t, insideSolid);
+        T *= materialTransmissionTint(sm, 0.35f) * medium * transmission;
+        if (maxComponent(T) < 0.02f) return true;
+        traveled += r.t;
+        o = h.position + d * 0.001f;
+    }
+    return true;
+}
+
+// Distance-volume closest hit for every ray of the queue, bounded by the
+// triangle hit k_extend found (the volume half of intersectScene).
+__global__ void __launch_bounds__(128) k_extend_volume(DevScene S, Wave W, uint32_t sel) {
+    const uint32_t* q = W.q[sel];
+    const uint32_t n = W.counts[sel];
+    VolumeScene V = volumeScene(S);
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t p = q[i];
+        float4 o = W.ray_o[p], d = W.ray_d[p];
+        float4 h = W.hit[p];
+        VolumeHitRec vh;
+        if (closestVolumeHit(V, xyz(o), xyz(d), h.x, vh))
+            W.hit[p] = make_float4(vh.t, __uint_as_float(kVolumeHit), __uint_as_float(vh.brick), 0.0f);
+    }
+}
+
 // Shadow rays, persistent threads with per-lane refill: an any-hit query for
 // an opaque blocker replaces the slot's unshadowed contribution by its
 // shadowed value (contribution / pdf divisor, or 0).  Rays that crossed a
@@ -670,6 +810,7 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
         int r = S.node_count == 0 ? 1 : anySteps(S, st, stackNode, kStepBudget);
         if (r == 0) continue;
         size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
+        if (r == 1 && S.volume_count) st.sawNonOpaque = true;  // distance volumes: the walk decides
         if (r == 2) {
             W.nee_c[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         } else if (st.sawNonOpaque) {
@@ -691,7 +832,7 @@ __global__ void __launch_bounds__(128) k_shadow_layers(DevScene S, Wave W) {
         size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
         float4 o = W.nee_o[slot], d = W.nee_d[slot], c = W.nee_c[slot];
         float3 T = f3(1.0f);
-        bool occluded = shadowLayers(S, xyz(o), xyz(d), o.w, T);
+        bool occluded = S.volume_count ? shadowWalk(S, xyz(o), xyz(d), o.w, T) : shadowLayers(S, xyz(o), xyz(d), o.w, T);
         float3 v = occluded ? f3(0.0f) : xyz(c) * T / c.w;
         W.nee_c[slot] = make_float4(v.x, v.y, v.z, 0.0f);
     }
@@ -724,9 +865,9 @@ __global__ void __launch_bounds__(128) k_aov_primary(DevScene S, DevParams P, Wa
         Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, 0.5f, 0.5f, 0.0f, 0.0f);
         writeAovMiss(W.aov, local, tileN);
         for (uint32_t pass = 0; pass < 32u; ++pass) {
-            HitRec r = traceClosest(S, ray.origin, ray.direction);
+            HitRec r = traceScene(S, ray.origin, ray.direction);
             if (r.tri == kNoHit) break;
-            Hit h = makeHit(S, ray, r);
+            Hit h = makeHitAny(S, ray, r);
             Material m = materialForHit(S, h);
             uint32_t nIdx = (uint32_t)m.parameters.w;
             if (nIdx != 0u) h = applyNormalMap(S, h, nIdx, ray.direction);
@@ -938,7 +1079,7 @@ int kernelGrid(int which, int smCount) {
     switch (which) {
         case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_generate, 256, 0); break;
         case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend, 128, 0); break;
-        case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade, 128, 0); break;
+        case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade<false>, 128, 0); break;
         case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays, 128, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_finalize, 256, 0); break;
     }
@@ -951,17 +1092,21 @@ cudaError_t launchGenerate(const DevScene& S, const DevParams& P, const Wave& W,
 }
 cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st) {
     k_extend<<<grid, 128, 0, st>>>(S, W, sel);
+    if (S.volume_count) k_extend_volume<<<grid, 128, 0, st>>>(S, W, sel);
     return cudaGetLastError();
 }
 cudaError_t launchShade(const DevScene& S, const DevParams& P, const Wave& W, uint32_t bounce, uint32_t sel, int grid,
                         cudaStream_t st) {
-    k_shade<<<grid, 128, 0, st>>>(S, P, W, bounce, sel);
+    if (S.volume_count)
+        k_shade<true><<<grid, 128, 0, st>>>(S, P, W, bounce, sel);
+    else
+        k_shade<false><<<grid, 128, 0, st>>>(S, P, W, bounce, sel);
     return cudaGetLastError();
 }
 cudaError_t launchShadow(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
     (void)P;
     k_shadow_rays<<<grid, 128, 0, st>>>(S, W);
-    if (!S.all_shadow_opaque) k_shadow_layers<<<grid, 128, 0, st>>>(S, W);
+    if (!S.all_shadow_opaque || S.volume_count) k_shadow_layers<<<grid, 128, 0, st>>>(S, W);
     return cudaGetLastError();
 }
 cudaError_t launchResolve(const DevParams& P, const Wave& W, int grid, cudaStream_t st) {

@@ -31,6 +31,15 @@ struct DevScene {
     uint32_t light_count, env_count, env_tex_plus1, all_shadow_opaque;
     float env_intensity, env_rot_y, env_max_radiance;
     uint32_t env_guide_size;
+    // Sparse distance volumes (GPUVolumeDescriptor with metadata.w == 1).
+    const dk_volume_descriptor* volumes;
+    const dk_volume_brick_descriptor* bricks;
+    const dk_volume_brick_sample* brick_samples;
+    const float* brick_dist;  // distance-only copy of brick_samples
+    const dk_volume_brick_grid* brick_grids;
+    const uint32_t* brick_grid_indices;
+    uint64_t brick_sample_count, brick_grid_index_count;
+    uint32_t volume_count, brick_count, brick_grid_count, volume_all_opaque;
 };
 
 // GPURenderConstants (PathTrace.metal:143-182) for one batch of samples.

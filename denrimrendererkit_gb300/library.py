@@ -68,6 +68,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_build_environment_samples": (i32, [P, u32, u32, C.c_float, C.c_float, P, C.POINTER(u32)]),
             "dk_build_environment_samples_noalloc": (i32, [P, u32, u32, C.c_float, C.c_float, P,
                                                              C.POINTER(u32), P]),
+            "dk_build_sparse_sphere_volume": (i32, [P, u32, C.POINTER(abi.SparseVolumeSettings), C.POINTER(P)]),
+            "dk_sparse_volume_view": (i32, [P, C.POINTER(abi.Scene)]),
+            "dk_sparse_volume_destroy": (i32, [P]),
             "dk_version": (C.c_char_p, []),
         }
         for name, (res, args) in sig.items():
@@ -125,3 +128,50 @@ def build_environment_samples(texture, intensity: float, max_radiance: float) ->
     check(load().dk_build_environment_samples(px.ctypes.data, texture.width, texture.height, float(intensity),
                                               float(max_radiance), out.ctypes.data, C.byref(count)))
     return out[: count.value].copy()
+
+
+class SparseVolume:
+    """A sparse distance volume built by dk_build_sparse_sphere_volume; the
+    arrays are numpy views of the library-owned buffers (valid while this
+    object lives)."""
+
+    def __init__(self, spheres, resolution, bounds_min, bounds_max, brick_size, narrow_band, volume_material=0,
+                 object_id=0, primitive_id=0):
+        lib = load()
+        arr = (abi.SdfSphere * len(spheres))()
+        for i, s in enumerate(spheres):
+            arr[i].center[:] = [float(x) for x in s["center"]]
+            arr[i].radius = float(s["radius"])
+            arr[i].material = int(s["material"])
+            arr[i].smooth_union_radius = float(s.get("smooth_union_radius", 0.0))
+        st = abi.SparseVolumeSettings()
+        st.resolution[:] = list(resolution)
+        st.bounds_min[:] = list(bounds_min)
+        st.bounds_max[:] = list(bounds_max)
+        st.brick_size[:] = list(brick_size)
+        st.narrow_band = narrow_band
+        st.volume_material = volume_material
+        st.object_id, st.primitive_id = object_id, primitive_id
+        self._h = C.c_void_p()
+        check(lib.dk_build_sparse_sphere_volume(arr, len(spheres), C.byref(st), C.byref(self._h)))
+        view = abi.Scene()
+        check(lib.dk_sparse_volume_view(self._h, C.byref(view)))
+
+        def arr_of(ptr, count, dtype):
+            if not count:
+                return np.zeros(0, dtype)
+            buf = (C.c_uint8 * (count * dtype.itemsize)).from_address(ptr)
+            return np.frombuffer(buf, dtype=dtype, count=count)
+
+        self.volumes = arr_of(view.volumes, view.volume_count, abi.VOLUME_DTYPE)
+        self.bricks = arr_of(view.volume_bricks, view.volume_brick_count, abi.BRICK_DTYPE)
+        self.samples = arr_of(view.volume_brick_samples, view.volume_brick_sample_count, abi.BRICK_SAMPLE_DTYPE)
+        self.grids = arr_of(view.volume_brick_grids, view.volume_brick_grid_count, abi.BRICK_GRID_DTYPE)
+        self.grid_indices = arr_of(view.volume_brick_grid_indices, view.volume_brick_grid_index_count, np.dtype(np.uint32))
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().dk_sparse_volume_destroy(self._h)
+        except Exception:
+            pass

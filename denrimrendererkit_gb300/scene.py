@@ -365,6 +365,8 @@ class RenderScene:
     # Pre-built triangle arrays appended after the instances (a bulk path for
     # large generated scenes; same layout as materialised instances).
     extra_triangles: List[np.ndarray] = dataclasses.field(default_factory=list)
+    # Sparse distance volumes (library.SparseVolume), bound after the meshes.
+    sparse_volumes: List[object] = dataclasses.field(default_factory=list)
 
     def add_material(self, m: Material) -> int:
         self.materials.append(m)
@@ -496,7 +498,15 @@ def compile_scene(scene: RenderScene, build_bvh: bool = True) -> AccelerationBui
         env_samples = library.build_environment_samples(env.texture, env.intensity, env.max_radiance)
     else:
         env_samples = np.zeros(0, abi.ENVIRONMENT_SAMPLE_DTYPE)
+    vols = {}
+    if scene.sparse_volumes:
+        if len(scene.sparse_volumes) > 1:
+            raise ValueError("Invalid render scene: one sparse distance volume per scene is supported.")
+        sv = scene.sparse_volumes[0]
+        vols = dict(volumes=sv.volumes, volume_bricks=sv.bricks, volume_brick_samples=sv.samples,
+                    volume_brick_grids=sv.grids, volume_brick_grid_indices=sv.grid_indices)
     return AccelerationBuild(
+        **vols,
         triangles=triangles, materials=materials, nodes=nodes, primitive_indices=prim,
         texture_descriptors=texture_descriptors, texture_pixels=np.ascontiguousarray(texture_pixels, f32),
         lights=lights, environment_samples=env_samples, environment_texture_index_plus_one=env_plus_one,

@@ -320,6 +320,42 @@ int dk_build_lights(dk_triangle* triangles, uint32_t triangle_count, const dk_ma
 int dk_build_environment_samples(const dk_float4* pixels, uint32_t width, uint32_t height, float intensity,
                                  float max_radiance, dk_environment_sample* out, uint32_t* out_count);
 
+/* Sparse distance volume for models of sphere primitives, the input of the
+ * sparse-brick path (GPUVolumeDescriptor metadata.w == 1).  Restates
+ * DistanceVolumeBuilder.buildSparse (Scene/SDFModel.swift:255-355, 2-voxel
+ * stored overlap, narrow-band brick selection), gpuVolumeBricks
+ * (Acceleration/SparseVolumeGPUEncoding.swift:9-299, brick grid + 4^3 macro
+ * occupancy) and appendSparseVolumeDescriptor (VolumeGPUEncoding.swift:184-243)
+ * for an identity instance transform.  The primitives are combined in order by
+ * union with the polynomial smooth minimum of `smooth_union_radius`. */
+typedef struct dk_sdf_sphere {
+    float center[3];
+    float radius;
+    uint32_t material;
+    float smooth_union_radius;
+} dk_sdf_sphere;
+
+typedef struct dk_sparse_volume_settings {
+    uint32_t resolution[3];   /* samples per axis of the virtual grid        */
+    float bounds_min[3];
+    float bounds_max[3];
+    uint32_t brick_size[3];   /* core brick size in samples                   */
+    float narrow_band;        /* keep bricks with min <= band && max >= -band */
+    uint32_t volume_material; /* the volume's fallback material               */
+    uint32_t object_id;
+    uint32_t primitive_id;
+} dk_sparse_volume_settings;
+
+typedef struct dk_sparse_volume dk_sparse_volume;
+
+int dk_build_sparse_sphere_volume(const dk_sdf_sphere* spheres, uint32_t sphere_count,
+                                  const dk_sparse_volume_settings* settings, dk_sparse_volume** out_volume);
+
+/* Points the volume fields of `scene` at the built arrays (owned by the volume). */
+int dk_sparse_volume_view(const dk_sparse_volume* volume, dk_scene* scene);
+
+int dk_sparse_volume_destroy(dk_sparse_volume* volume);
+
 /* Allocation-free variant of dk_build_environment_samples.  It has no
  * counterpart in the reference.  It serves callers that cannot let the library
  * call cudaMalloc: applications that give the renderer only device memory from

@@ -20,7 +20,8 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 COUNTERS = ("paths", "material_fetch", "light_samples", "env_samples", "env_search_steps", "miss_env",
             "shadow_queries", "bounces", "env_lookups", "queries_ext", "queries_shadow", "queries_sss",
             "queries_aov", "nodes_ext", "nodes_shadow", "nodes_sss", "nodes_aov", "tris_ext", "tris_shadow",
-            "tris_sss", "tris_aov")
+            "tris_sss", "tris_aov", "grid_cells", "macro_skips", "brick_tests", "brick_marches", "march_steps",
+            "brick_hits", "brick_samples", "range_culls")
 
 _lib = None
 

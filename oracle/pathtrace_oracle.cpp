@@ -49,6 +49,8 @@ enum {
     C_QUERIES_K0, C_QUERIES_K1, C_QUERIES_K2, C_QUERIES_K3,
     C_NODES_K0, C_NODES_K1, C_NODES_K2, C_NODES_K3,
     C_TRIS_K0, C_TRIS_K1, C_TRIS_K2, C_TRIS_K3,
+    C_GRID_CELLS, C_MACRO_SKIPS, C_BRICK_TESTS, C_BRICK_MARCHES, C_MARCH_STEPS, C_BRICK_HITS, C_BRICK_SAMPLES,
+    C_RANGE_CULLS,
     C_COUNT
 };
 struct Counters { uint64_t c[C_COUNT]; };
@@ -716,6 +718,8 @@ static void recordHit(Hit& closest, const Ray& ray, const dk_triangle& tri, uint
     closest.primitiveID = triangleIndex;
     closest.frontFacing = frontFacing;
 }
+#include "sparse_oracle.inc"
+
 // intersectSceneLinear / intersectScene: PathTrace.metal:3264-3421 (binary BVH,
 // 64-entry stack, left child first, strict `t < closest.t`).
 static Hit intersectScene(const Ctx& c, const Ray& ray, int kind) {
@@ -729,7 +733,8 @@ static Hit intersectScene(const Ctx& c, const Ray& ray, int kind) {
             if (intersectTriangle(ray, s->triangles[i], t, n, uv, tg, bt, ff) && t < closest.t)
                 recordHit(closest, ray, s->triangles[i], i, t, n, uv, tg, bt, ff);
         }
-        return closest;
+        Hit vh = closestVolumeHit(c, ray, closest.t);
+        return vh.hit ? vh : closest;
     }
     uint32_t stack[64];
     uint32_t stackCount = 0;
@@ -755,6 +760,8 @@ static Hit intersectScene(const Ctx& c, const Ray& ray, int kind) {
             stack[stackCount++] = node.metadata.x;
         }
     }
+    Hit vh = closestVolumeHit(c, ray, closest.t);
+    if (vh.hit) closest = vh;
     return closest;
 }
 
@@ -1406,7 +1413,6 @@ int ORACLE_EXPORT(render)(const dk_scene* scene, const oracle_params* params, ui
                           double* accum, float* aov, uint64_t* counters) {
     if (!scene || !params || !accum) return 1;
     if (scene->material_count == 0) return 3;
-    if (scene->volume_count != 0) return 4;  // triangle scenes only
     std::vector<uint32_t> pixels;
     if (pixel_list) {
         pixels.assign(pixel_list, pixel_list + pixel_list_count);

@@ -195,3 +195,42 @@ def test_invalid_scene_leaves_no_session(renderer):
     with pytest.raises(DenrimError) as e:
         renderer.make_session(wl.scene, wl.settings, build=b)
     assert e.value.code == 3
+
+
+# ------------------------------------------------------------ sparse bricks --
+def test_sdf_spheres_small(renderer, oracle_lib):
+    # The sparse-SDF configuration on a 192^3 virtual grid, 128x128, 4 spp.
+    wl = scenes.sdf_spheres(width=128, height=128, samples=4, resolution=192)
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 4)
+    assert_aovs_bit_exact(s, o)
+    rel, g, c = beauty_stats(s, o)
+    assert rel <= 1e-3
+    assert (o.aov[4, ..., 0] > 0).mean() > 0.05  # the field is actually hit
+
+
+def test_sdf_spheres_full_size_pixel_sample(renderer, oracle_lib):
+    # The full configuration (768^3 grid, 8^3 bricks, ~3.2% occupied,
+    # 1024x1024), compared on 4096 seeded pixels at 2 spp.
+    wl = scenes.sdf_spheres()
+    rng = np.random.default_rng(1)
+    pl = np.sort(rng.choice(1024 * 1024, 4096, replace=False)).astype(np.uint32)
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 2, pixel_list=pl)
+    assert_aovs_bit_exact(s, o, pl)
+    rel, g, c = beauty_stats(s, o, pl)
+    assert rel <= 2e-2
+
+
+def test_sparse_volume_only_scene_gpu(renderer, oracle_lib, dk_lib):
+    # RenderSessionTests.swift:806-860 on the GPU path.
+    from denrimrendererkit_gb300 import library
+    from denrimrendererkit_gb300.scene import Camera, Material, RenderScene
+    cam = Camera((0, 0, 3), (0, 0, 0), orthographic_scale=2.4)
+    scene = RenderScene(camera=cam)
+    scene.add_material(Material(base_color=(0.2, 0.65, 0.9), roughness=0.55))
+    scene.sparse_volumes.append(library.SparseVolume([dict(center=(0, 0, 0), radius=0.55, material=0)], (20,) * 3,
+                                                     (-1, -1, -1), (1, 1, 1), (5,) * 3, 0.3))
+    wl = scenes.Workload("sparse-sphere", scene, RenderSettings(width=20, height=20, max_bounces=1), 1)
+    s, o, _ = run_pair(renderer, oracle_lib, wl, 1)
+    assert_aovs_bit_exact(s, o)
+    albedo = s.pixels(RenderOutput.ALBEDO).reshape(-1, 4)
+    assert ((albedo[:, 0] < 0.35) & (albedo[:, 1] > 0.45) & (albedo[:, 2] > 0.65) & (albedo[:, 3] > 0.9)).any()

@@ -196,3 +196,87 @@ def test_oracle_fp32_vs_fp64_small(oracle_lib):
     assert np.array_equal(r32.aov[3], r64.aov[3]) and np.array_equal(r32.aov[4], r64.aov[4])
     m32, m64 = r32.accum[..., :3].mean(), r64.accum[..., :3].mean()
     assert abs(m32 - m64) / m64 < 0.05
+
+
+# ------------------------------------------------------------ sparse bricks --
+def _sdf_build(spheres, resolution, brick, band, camera, settings=None):
+    from denrimrendererkit_gb300 import library
+    from denrimrendererkit_gb300.scene import compile_scene
+    scene = RenderScene(camera=camera)
+    scene.add_material(Material(base_color=(0.2, 0.65, 0.9), roughness=0.55))
+    scene.sparse_volumes.append(library.SparseVolume(spheres, (resolution,) * 3, (-1, -1, -1), (1, 1, 1),
+                                                     (brick,) * 3, band, volume_material=0))
+    return scene, compile_scene(scene)
+
+
+def test_sparse_sphere_known_hit(oracle_lib, dk_lib):
+    # The geometry of CPUIntersectorTests.testRayHitsDistanceVolumeSphere
+    # (CPUIntersectorTests.swift:73-89): r = 0.5 sphere on a 24^3 grid over
+    # [-1, 1]^3, ray from z = 2 towards -z hits at t = 1.5 +- 0.08, normal +z.
+    from denrimrendererkit_gb300.scene import Camera
+    _, b = _sdf_build([dict(center=(0, 0, 0), radius=0.5, material=0)], 24, 8, 0.3, Camera((0, 0, 3), (0, 0, 0)))
+    h = oracle_lib.intersect(b, (0, 0, 2), (0, 0, -1))
+    assert h["hit"] == 1
+    assert h["t"] == pytest.approx(1.5, abs=0.08)
+    assert h["pz"] == pytest.approx(0.5, abs=0.08)
+    assert h["nz"] == pytest.approx(1.0, abs=0.08)
+    assert oracle_lib.intersect(b, (2, 2, 2), (0, 0, -1))["hit"] == 0
+
+
+def test_sparse_volume_only_scene_uses_brick_path(oracle_lib, dk_lib):
+    # RenderSessionTests.testSparseVolumeOnlySceneRendersThroughBrickPathOnFlatPath
+    # (RenderSessionTests.swift:806-860): sphere r = 0.55, resolution 20, brick 5,
+    # band 0.3, orthographic camera (scale 2.4), 20x20, 1 bounce.
+    from denrimrendererkit_gb300.renderer import RenderSettings
+    from denrimrendererkit_gb300.scene import Camera
+    cam = Camera((0, 0, 3), (0, 0, 0), orthographic_scale=2.4)
+    scene, b = _sdf_build([dict(center=(0, 0, 0), radius=0.55, material=0)], 20, 5, 0.3, cam)
+    settings = RenderSettings(width=20, height=20, max_bounces=1)
+    r = oracle_lib.OracleRender(b, settings, cam)
+    r.render(1)
+    c = r.counter_dict()
+    assert c["grid_cells"] > 0 and c["brick_tests"] > 0 and c["brick_marches"] > 0
+    assert c["march_steps"] > 0 and c["brick_hits"] > 0
+    albedo = r.aov[2].reshape(-1, 4)
+    assert ((albedo[:, 0] < 0.35) & (albedo[:, 1] > 0.45) & (albedo[:, 2] > 0.65) & (albedo[:, 3] > 0.9)).any()
+
+
+def test_sparse_brick_without_zero_crossing_is_culled(oracle_lib):
+    # RenderSessionTests.testSparseBrickWithoutZeroCrossingIsCulledBeforeMarch
+    # (RenderSessionTests.swift:862-919): one 3^3 brick, all distances 0.05.
+    from denrimrendererkit_gb300.renderer import RenderSettings
+    from denrimrendererkit_gb300.scene import AccelerationBuild, Camera
+    cam = Camera((0, 0, 3), (0, 0, 0), orthographic_scale=2.0)
+    mats = _materials(Material(base_color=(0.8, 0.2, 0.2)))
+    vol = np.zeros(1, abi.VOLUME_DTYPE)
+    vol["world_bounds_min"][0] = vol["local_bounds_min"][0] = (-1, -1, -1, 0)
+    vol["world_bounds_max"][0] = vol["local_bounds_max"][0] = (1, 1, 1, 0)
+    vol["dimensions"][0] = (3, 3, 3, 0)
+    vol["metadata"][0] = (0, 0, 0, 1)
+    vol["material_program"][0] = (0xFFFFFFFF, 0, 0, 0)
+    vol["world_to_local"][0] = np.eye(4)
+    vol["normal_transform"][0] = np.eye(4)
+    brick = np.zeros(1, abi.BRICK_DTYPE)
+    brick["world_bounds_min"][0] = brick["local_bounds_min"][0] = (-1, -1, -1, 0)
+    brick["world_bounds_max"][0] = brick["local_bounds_max"][0] = (1, 1, 1, 0)
+    brick["sample_bounds_min"][0] = (-1, -1, -1, 0.05)
+    brick["sample_bounds_max"][0] = (1, 1, 1, 0.05)
+    brick["dimensions_and_sample_offset"][0] = (3, 3, 3, 0)
+    samples = np.zeros(27, abi.BRICK_SAMPLE_DTYPE)
+    samples["distance"] = 0.05
+    grid = np.zeros(1, abi.BRICK_GRID_DTYPE)
+    grid["dimensions_and_index_offset"][0] = (1, 1, 1, 0)
+    grid["brick_size_and_volume"][0] = (3, 3, 3, 0)
+    grid["macro_dimensions_and_index_offset"][0] = (1, 1, 1, 1)
+    grid["macro_size_and_reserved"][0] = (4, 4, 4, 0)
+    gidx = np.array([0, 1], np.uint32)
+    z = lambda dt: np.zeros(0, dt)  # noqa: E731
+    b = AccelerationBuild(z(abi.TRIANGLE_DTYPE), mats, z(abi.NODE_DTYPE), z(np.uint32), z(abi.TEXTURE_DESCRIPTOR_DTYPE),
+                          np.zeros((0, 4), np.float32), z(abi.LIGHT_DTYPE), z(abi.ENVIRONMENT_SAMPLE_DTYPE), 0, 1.0, 0.0,
+                          16.0, volumes=vol, volume_bricks=brick, volume_brick_samples=samples,
+                          volume_brick_grids=grid, volume_brick_grid_indices=gidx)
+    r = oracle_lib.OracleRender(b, RenderSettings(width=8, height=8, max_bounces=1), cam)
+    r.render(1)
+    c = r.counter_dict()
+    assert c["grid_cells"] > 0 and c["brick_tests"] > 0 and c["range_culls"] > 0
+    assert c["brick_marches"] == 0 and c["march_steps"] == 0 and c["brick_hits"] == 0
