@@ -17,10 +17,11 @@ Printed JSON fields:
               BVH-node / triangle / material / light / environment bytes, counted
               by the CPU oracle on a 1/64 pixel subsample and scaled) over its
               event-timed duration, against the measured HBM copy bandwidth.
-  cpu_baseline  the CPU oracle (a restatement of the reference shader) on the
-              host cores, on the 1/64 pixel subsample of the same frame.
-`--impl reference` times that CPU implementation alone (the reference's own
-Metal path cannot run on this machine).  `--gpus N` runs N independent
+  cpu_baseline  the reference's own kernel (PathTrace.metal compiled for the
+              host from oracle/_ref; the FP32 oracle port where that is not
+              built) on all host cores, on a 1/64 pixel subsample of the frame.
+`--impl reference` times that CPU implementation alone on a 1/256 subsample
+(the reference's Metal dispatch cannot run on this machine).  `--gpus N` runs N independent
 replicas (one process per GPU, weak scaling): the path has no exchange step.
 """
 from __future__ import annotations
@@ -172,7 +173,8 @@ def algorithmic_bytes(counters: dict, env_texels: int):
 
 
 def cpu_oracle_sample(wl, build, threads=0):
-    """The FP32 oracle on every 8th pixel in x and y, all spp of the step."""
+    """The FP32 oracle on every 8th pixel in x and y, all spp of the step: the
+    work counters behind the roofline's algorithmic bytes."""
     from oracle import oracle as orc
     orc.build()
     w, h = wl.settings.width, wl.settings.height
@@ -186,35 +188,57 @@ def cpu_oracle_sample(wl, build, threads=0):
     return paths, dt, r.counter_dict(), len(pixels)
 
 
+def cpu_reference_sample(wl, build, stride, threads):
+    """Times the reference's own kernel (PathTrace.metal pathTraceKernel compiled
+    for the host, kind "reference") on every `stride`-th pixel in x and y, all
+    spp of the step; the FP32 oracle port (kind "port") where it is not built.
+    Returns (paths, seconds, kind, description)."""
+    from oracle import oracle as orc
+    w, h = wl.settings.width, wl.settings.height
+    ys, xs = np.meshgrid(np.arange(0, h, stride), np.arange(0, w, stride), indexing="ij")
+    pixels = (ys * w + xs).reshape(-1).astype(np.uint32)
+    kind, what = "port", "FP32 oracle port of the reference shader"
+    try:
+        if orc.reference_available():
+            orc.load_reference()
+            kind, what = "reference", "the reference's pathTraceKernel (PathTrace.metal) compiled for the host"
+    except Exception as exc:  # the generated source failed to build: fall back to the port, say so
+        what = f"FP32 oracle port (reference kernel build failed: {str(exc).splitlines()[0][:120]})"
+    if kind == "reference":
+        r = orc.ReferenceRender(build, wl.settings, wl.scene.camera)
+    else:
+        orc.build()
+        r = orc.OracleRender(build, wl.settings, wl.scene.camera)
+    t0 = time.perf_counter()
+    r.render(wl.samples, pixel_list=pixels, threads=threads)
+    dt = time.perf_counter() - t0
+    paths = len(pixels) * wl.samples
+    desc = (f"every {stride}th pixel in x and y ({len(pixels)} px) x {wl.samples} spp = {paths} paths, {what}, "
+            f"{threads} threads, {dt:.1f} s")
+    return paths, dt, kind, desc
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     from denrimrendererkit_gb300 import compile_scene
     from oracle import oracle as orc
     wl = workload(args)
-    build = compile_scene(wl.scene)
-    orc.build()
+    build = compile_scene(wl.scene, host_builders=orc.HostBuilders)
     threads = os.cpu_count() or 1
-    w, h = wl.settings.width, wl.settings.height
-    ys, xs = np.meshgrid(np.arange(0, h, 32), np.arange(0, w, 32), indexing="ij")
-    pixels = (ys * w + xs).reshape(-1).astype(np.uint32)
-    times = []
+    times, kind, desc, paths = [], "port", "", 0
     for i in range(args.warmup + args.steps):
-        r = orc.OracleRender(build, wl.settings, wl.scene.camera)
-        t0 = time.perf_counter()
-        r.render(wl.samples, pixel_list=pixels, threads=threads)
-        dt = time.perf_counter() - t0
+        paths, dt, kind, desc = cpu_reference_sample(wl, build, 16, threads)
         if i >= args.warmup:
             times.append(dt)
-    paths = len(pixels) * wl.samples
     value = paths * len(times) / sum(times) / 1e6
-    sample = f"every 32nd pixel in x and y ({len(pixels)} px) x {wl.samples} spp = {paths} paths per step"
+    impl = ("the reference's pathTraceKernel (PathTrace.metal) compiled for the host CPU; its Metal dispatch is "
+            "unavailable on this box" if kind == "reference" else "CPU oracle port of the reference shader")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(args, wl, {"implementation": "CPU oracle port of the reference shader (the reference's "
-                                                          "Metal path is unavailable on this box)"}),
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
+            "config": config(args, wl, {"implementation": impl}),
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": kind, "sample": desc},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -334,9 +358,9 @@ def run_gb300(args, rank, world, local):
         scale = paths_per_step / paths
         alg = algorithmic_bytes(counters, build.environment_samples.shape[0])
         per_frame = {k: v * scale for k, v in alg.items()}
-        cpu = {"value": paths / dt / 1e6, "unit": METRIC, "cores": threads, "kind": "port",
-               "sample": f"every 8th pixel in x and y ({npx} px) x {wl.samples} spp = {paths} paths "
-                         f"(1/64 of a step), FP32 oracle, {dt:.1f} s"}
+        rpaths, rdt, rkind, rdesc = cpu_reference_sample(wl, build, 8, threads)
+        cpu = {"value": rpaths / rdt / 1e6, "unit": METRIC, "cores": threads, "kind": rkind, "sample": rdesc,
+               "oracle_port_mpaths_s": paths / dt / 1e6}
         kernel_ms = {k: stage[k] / args.steps for k in ("k_extend", "k_shade", "k_shadow")}
         dom = max(kernel_ms, key=kernel_ms.get)
         peak, kind = measured_peaks()

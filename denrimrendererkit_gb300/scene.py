@@ -427,9 +427,15 @@ class AccelerationBuild:
         return s
 
 
-def compile_scene(scene: RenderScene, build_bvh: bool = True) -> AccelerationBuild:
-    """LinearTriangleAccelerationBackend.build (AccelerationBackend.swift:7-68)."""
+def compile_scene(scene: RenderScene, build_bvh: bool = True, host_builders=None) -> AccelerationBuild:
+    """LinearTriangleAccelerationBackend.build (AccelerationBackend.swift:7-68).
+
+    The BVH, light list and environment table come from the GB300 library
+    (`dk_build_bvh`, `dk_build_lights`, `dk_build_environment_samples`);
+    `host_builders` — any object with the same three functions — replaces
+    them (the test oracle passes its restatement of the Swift builders)."""
     from . import library  # the scene-compile helpers live in the GB300 library
+    builders = host_builders or library
 
     # InstanceAccelerationBuilder.build + materializedTriangles
     # (InstanceAcceleration.swift:23-128): local triangles with identity
@@ -488,14 +494,14 @@ def compile_scene(scene: RenderScene, build_bvh: bool = True) -> AccelerationBui
                            else np.zeros(0, abi.TEXTURE_DESCRIPTOR_DTYPE))
     texture_pixels = np.concatenate(pixels) if pixels else np.zeros((0, 4), f32)
 
-    lights = library.build_lights(triangles, materials)
+    lights = builders.build_lights(triangles, materials)
     if build_bvh:
-        nodes, prim = library.build_bvh(triangles, 4)
+        nodes, prim = builders.build_bvh(triangles, 4)
     else:
         nodes, prim = np.zeros(0, abi.NODE_DTYPE), np.zeros(0, np.uint32)
     env = scene.environment
     if env.texture is not None:
-        env_samples = library.build_environment_samples(env.texture, env.intensity, env.max_radiance)
+        env_samples = builders.build_environment_samples(env.texture, env.intensity, env.max_radiance)
     else:
         env_samples = np.zeros(0, abi.ENVIRONMENT_SAMPLE_DTYPE)
     vols = {}

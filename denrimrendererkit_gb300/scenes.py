@@ -164,6 +164,77 @@ def sdf_spheres(width: int = 1024, height: int = 1024, samples: int = 16, resolu
     return Workload(f"sdf-spheres-{resolution}^3-{width}x{height}-{samples}spp", scene, settings, samples)
 
 
+def _checker(width: int, height: int, a, b, cells: int = 8) -> Texture2D:
+    y, x = np.mgrid[0:height, 0:width]
+    mask = ((x * cells // width + y * cells // height) % 2).astype(bool)
+    rgb = np.where(mask[..., None], np.asarray(a, np.float64), np.asarray(b, np.float64))
+    px = np.concatenate([rgb, np.ones((height, width, 1))], axis=-1).astype(f32).reshape(-1, 4)
+    return Texture2D(width, height, px, sampling_mode=1)
+
+
+def _bump_normal_map(width: int, height: int, seed: int) -> Texture2D:
+    rng = np.random.default_rng(seed)
+    n = rng.normal(0.0, 0.25, size=(height, width, 2))
+    xyz = np.concatenate([n, np.ones((height, width, 1))], axis=-1)
+    xyz /= np.linalg.norm(xyz, axis=-1, keepdims=True)
+    enc = xyz * 0.5 + 0.5
+    px = np.concatenate([enc, np.ones((height, width, 1))], axis=-1).astype(f32).reshape(-1, 4)
+    return Texture2D(width, height, px, sampling_mode=0)
+
+
+def material_zoo(width: int = 96, height: int = 64, samples: int = 8, seed: int = 11) -> Workload:
+    """Feature-coverage scene: one subdivision-2 icosphere per material feature
+    of the layered BSDF (Scene/Material.swift:16-219) — thin film, sheen,
+    anisotropic GGX metal, clearcoat with thickness and attenuation, random-walk
+    subsurface, rough and thin-walled transmission with Beer absorption, a
+    scattering interior medium, a cut-out (opacity 0.5), a checker base-colour
+    texture and a normal map — on a textured ground under a rotated HDRI with
+    maxRadiance clipping, two emissive quads, and the per-sample radiance clamp
+    at its `final` default."""
+    rng = np.random.default_rng(seed)
+    env = Environment(texture=synthetic_hdri(256, 128, seed=seed, sun_peak=200.0, sun_radius_deg=4.0),
+                      intensity=0.8, rotation_y=0.7, max_radiance=24.0)
+    scene = RenderScene(camera=Camera((0.0, 2.4, 6.2), (0.0, 0.45, 0.0), vertical_field_of_view_degrees=38.0),
+                        environment=env)
+    ground = scene.add_material(Material(base_color=(0.7, 0.7, 0.7), roughness=0.7, specular=0.5,
+                                         base_color_texture=_checker(64, 64, (0.8, 0.78, 0.7), (0.25, 0.27, 0.3))))
+    scene.add(Mesh.quad((-6, 0, 6), (6, 0, 6), (6, 0, -6), (-6, 0, -6)), ground)
+    presets = [
+        Material(base_color=(0.3, 0.35, 0.4), metallic=1.0, roughness=0.25, thin_film=1.0,
+                 thin_film_thickness_nanometers=380.0),
+        Material(base_color=(0.35, 0.08, 0.12), roughness=0.9, specular=0.3, sheen=1.0, sheen_color=(1.0, 0.9, 0.9),
+                 sheen_roughness=0.4),
+        Material(base_color=(0.95, 0.7, 0.35), metallic=1.0, roughness=0.35, specular_anisotropy=0.8),
+        Material(base_color=(0.6, 0.05, 0.05), roughness=0.45, clearcoat=1.0, clearcoat_roughness=0.08,
+                 clearcoat_thickness=0.6, clearcoat_attenuation_color=(0.9, 0.7, 0.3)),
+        Material(base_color=(0.9, 0.75, 0.65), roughness=0.5, subsurface=0.9, subsurface_color=(0.95, 0.6, 0.45),
+                 subsurface_radius=(0.5, 0.25, 0.12), subsurface_scale=0.3, subsurface_anisotropy=0.2),
+        Material(base_color=(1.0, 1.0, 1.0), roughness=0.15, transmission=1.0, index_of_refraction=1.45,
+                 transmission_roughness=0.2, transmission_absorption_color=(0.4, 0.8, 0.6),
+                 transmission_absorption_distance=0.5),
+        Material(base_color=(1.0, 1.0, 1.0), roughness=0.0, transmission=1.0, thin_walled=True,
+                 transmission_color=(0.8, 0.9, 1.0)),
+        Material(base_color=(0.95, 0.95, 0.92), roughness=0.2, transmission=1.0, index_of_refraction=1.35,
+                 volume_scattering=1.0, volume_scattering_color=(0.9, 0.9, 0.85), volume_scattering_distance=0.2,
+                 volume_anisotropy=0.3),
+        Material(base_color=(0.2, 0.6, 0.3), roughness=0.6, opacity=0.5),
+        Material(base_color=(1.0, 1.0, 1.0), roughness=0.4, specular=0.6,
+                 base_color_texture=_checker(32, 32, (0.9, 0.3, 0.1), (0.1, 0.3, 0.9), cells=4)),
+        Material(base_color=(0.75, 0.75, 0.8), metallic=0.5, roughness=0.3, normal_map=_bump_normal_map(32, 32, seed)),
+        Material(base_color=(0.5, 0.5, 0.5), roughness=0.3, specular=1.0, metallic=0.0),
+    ]
+    for i, m in enumerate(presets):
+        mi = scene.add_material(m)
+        gx, gz = i % 4, i // 4
+        center = (-2.1 + 1.4 * gx + float(rng.uniform(-0.05, 0.05)), 0.5, -1.4 + 1.4 * gz)
+        scene.add(icosphere(2, 0.5), mi, Transform.translation(center) * Transform.rotation_y(0.3 * i))
+    warm = scene.add_material(Material(base_color=(1, 1, 1), emission=(1.0, 0.85, 0.6), emission_strength=12.0))
+    scene.add(Mesh.quad((-0.5, 3.2, -0.3), (0.5, 3.2, -0.3), (0.5, 3.2, 0.3), (-0.5, 3.2, 0.3)), warm)
+    scene.add(Mesh.quad((2.8, 0.2, 1.5), (2.8, 0.2, 0.5), (2.8, 1.4, 0.5), (2.8, 1.4, 1.5)), warm)
+    settings = RenderSettings(width=width, height=height, max_bounces=8, quality=RenderQuality.FINAL, frame_seed=1)
+    return Workload(f"material-zoo-{width}x{height}-{samples}spp", scene, settings, samples)
+
+
 def cornell_box_reference(width: int = 24, height: int = 24) -> Workload:
     """RenderScene.cornellBox() (Scene/RenderScene.swift:324-380)."""
     scene = RenderScene(camera=Camera((0, 1, 3.4), (0, 1, 0), vertical_field_of_view_degrees=42.0))

@@ -88,6 +88,26 @@ def build_environment_samples(pixels: np.ndarray, width: int, height: int, inten
     return out[:n].copy()
 
 
+class HostBuilders:
+    """compile_scene(host_builders=...) hook: the restatements of the Swift
+    builders (BVHBuilder + BVHFlattener, lightRecordsAndTaggedTriangles,
+    environmentSamples) in place of the GB300 library's."""
+
+    @staticmethod
+    def build_bvh(triangles, max_leaf=4):
+        return build_bvh(triangles, max_leaf)
+
+    @staticmethod
+    def build_lights(triangles, materials):
+        tagged, lights = build_lights(triangles, materials)
+        triangles["padding2"] = tagged["padding2"]
+        return lights
+
+    @staticmethod
+    def build_environment_samples(texture, intensity, max_radiance):
+        return build_environment_samples(texture.pixels, texture.width, texture.height, intensity, max_radiance)
+
+
 def make_params(settings, camera, tile=None):
     """oracle_params from RenderSettings + Camera (GPURenderConstants fields)."""
     from denrimrendererkit_gb300 import abi
@@ -158,3 +178,66 @@ def random_sequence(state: int, n: int, fp64: bool = False):
 
 def hash_u32(v: int) -> int:
     return load().oracle32_hash(v)
+
+
+# ------------------------------------------------ reference-shader oracle ---
+# oracle/_ref/libref_pathtrace.so: the reference's own PathTrace.metal compiled
+# as C++ (oracle/ref/build_ref.py).  Present only where it could be built.
+REF_LIB = os.path.join(HERE, "_ref", "libref_pathtrace.so")
+REF_SDF_COUNTERS = ("dense_volume_tests", "dense_march_steps", "grid_cells", "macro_skips", "brick_tests",
+                    "brick_invalid", "range_culls", "brick_marches", "march_steps", "brick_hits",
+                    "primary_queries", "bounce_queries", "shadow_queries")
+_ref_lib = None
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_LIB) or os.path.exists(os.path.join(HERE, "_ref", "pathtrace_ref.cpp"))
+
+
+def load_reference() -> C.CDLL:
+    global _ref_lib
+    if _ref_lib is None:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("build_ref", os.path.join(HERE, "ref", "build_ref.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+        lib = C.CDLL(REF_LIB)
+        P, u32 = C.c_void_p, C.c_uint32
+        lib.ref_render.argtypes = [P, P, u32, u32, P, u32, C.c_int, P, P, P]
+        lib.ref_render.restype = C.c_int
+        lib.ref_sdf_counter_count.restype = u32
+        assert lib.ref_sdf_counter_count() == len(REF_SDF_COUNTERS)
+        _ref_lib = lib
+    return _ref_lib
+
+
+class ReferenceRender:
+    """The reference kernel run on the host: RGBA32F accumulation texture and
+    last-sample AOV planes, exactly as the kernel writes them."""
+
+    def __init__(self, build, settings, camera, tile=None, collect_sdf_counters: bool = False):
+        self.build = build
+        self.settings = settings
+        self.params = make_params(settings, camera, tile)
+        self.scene_struct = build.as_struct()
+        w, h = settings.width, settings.height
+        self.accum = np.zeros((h, w, 4), np.float32)
+        self.aov = np.zeros((6, h, w, 4), np.float32)
+        self.aov[1, ..., :3] = 0.5
+        self.sdf_counters = np.zeros(len(REF_SDF_COUNTERS), np.uint32) if collect_sdf_counters else None
+        self.sample_count = 0
+
+    def render(self, samples: int, pixel_list=None, threads: int = 0) -> None:
+        pl = None if pixel_list is None else np.ascontiguousarray(pixel_list, np.uint32)
+        rc = load_reference().ref_render(
+            C.byref(self.scene_struct), C.byref(self.params), self.sample_count, samples,
+            None if pl is None else pl.ctypes.data, 0 if pl is None else len(pl), threads,
+            self.accum.ctypes.data, self.aov.ctypes.data,
+            None if self.sdf_counters is None else self.sdf_counters.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"reference render failed with {rc}")
+        self.sample_count += samples
+
+    def sdf_counter_dict(self):
+        return {k: int(v) for k, v in zip(REF_SDF_COUNTERS, self.sdf_counters)}

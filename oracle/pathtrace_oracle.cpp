@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "oracle_math.hpp"
+#include "oracle_params.h"
 
 using namespace om;
 
@@ -107,21 +108,6 @@ static Material loadMaterial(const dk_material& m) {
 
 }  // namespace
 
-extern "C" {
-// Parameters the reference packs into GPURenderConstants
-// (RenderSession.swift:908-947) plus the two cameras.
-typedef struct oracle_params {
-    uint32_t width, height, max_bounces;
-    uint32_t transparent_background, shows_environment_background;
-    float background_color[3];
-    float sample_radiance_clamp;  // resolved (RenderSettings.resolvedSampleRadianceClamp)
-    uint32_t frame_seed;
-    uint32_t denoiser_enabled;
-    uint32_t tile_x, tile_y, tile_w, tile_h;
-    dk_camera camera;
-    dk_camera previous_camera;
-} oracle_params;
-}
 
 namespace {
 
