@@ -166,7 +166,46 @@ EXPORTED_SYMBOLS = (
     "dk_session_destroy", "dk_last_error_message", "dk_build_bvh", "dk_build_lights",
     "dk_build_environment_samples", "dk_build_environment_samples_noalloc", "dk_build_sparse_sphere_volume",
     "dk_sparse_volume_view", "dk_sparse_volume_destroy", "dk_version",
+    "dk_server_create", "dk_server_submit", "dk_server_step", "dk_server_start", "dk_server_stop",
+    "dk_server_wait", "dk_server_job_status", "dk_server_read_output", "dk_server_release",
+    "dk_server_get_stats", "dk_server_destroy", "dk_denoise_spatial",
 )
+
+
+class SpatialDenoiseSettings(C.Structure):
+    """dk_spatial_denoise_settings (DenoiseSettings defaults, Denoiser.swift:44-60)."""
+    _fields_ = [("radius", C.c_uint32), ("normal_sigma", C.c_float), ("depth_sigma", C.c_float),
+                ("albedo_sigma", C.c_float), ("color_sigma", C.c_float), ("iterations", C.c_uint32)]
+
+
+class ServerConfig(C.Structure):
+    """dk_server_config."""
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("wave_paths", C.c_uint32), ("max_jobs_per_wave", C.c_uint32),
+                ("max_resident_jobs", C.c_uint32), ("samples_per_wave", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+
+
+class JobDesc(C.Structure):
+    """dk_job_desc."""
+    _fields_ = [("settings", Settings), ("samples", C.c_uint32), ("material_count", C.c_uint32),
+                ("materials", C.c_void_p)]
+
+
+class JobStatus(C.Structure):
+    """dk_job_status."""
+    _fields_ = [("job_id", C.c_uint64), ("state", C.c_uint32), ("samples_done", C.c_uint32),
+                ("samples", C.c_uint32), ("waves", C.c_uint32), ("submit_ms", C.c_double),
+                ("admit_ms", C.c_double), ("finish_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    """dk_server_stats."""
+    _fields_ = [(k, C.c_uint64) for k in ("jobs_submitted", "jobs_done", "jobs_queued", "jobs_running", "waves",
+                                          "paths_traced", "kernel_launches", "budget_used_bytes",
+                                          "budget_peak_bytes", "device_bytes")] + \
+               [("busy_ms", C.c_double), ("max_jobs_in_wave", C.c_double), ("mean_jobs_in_wave", C.c_double)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_RELEASED = 0, 1, 2, 3
 
 
 class SdfSphere(C.Structure):

@@ -248,8 +248,9 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
         const dk_triangle& t = sc->triangles[prims[s].tri];
         isect[3 * (size_t)s + 0] = make_float4(t.v0.x, t.v0.y, t.v0.z, asFloat(slotOfTri[prims[s].tri]));
         isect[3 * (size_t)s + 1] = make_float4(t.v1.x - t.v0.x, t.v1.y - t.v0.y, t.v1.z - t.v0.z, asFloat(prims[s].tri));
-        isect[3 * (size_t)s + 2] =
-            make_float4(t.v2.x - t.v0.x, t.v2.y - t.v0.y, t.v2.z - t.v0.z, asFloat(opaque[prims[s].tri] ? 1u : 0u));
+        uint32_t mid = std::min(std::min(t.material_id, sc->material_count - 1u), 255u);
+        uint32_t flags = (opaque[prims[s].tri] ? 1u : 0u) | (mid << 8);
+        isect[3 * (size_t)s + 2] = make_float4(t.v2.x - t.v0.x, t.v2.y - t.v0.y, t.v2.z - t.v0.z, asFloat(flags));
     }
     isect[3 * (size_t)n + 0] = make_float4(0, 0, 0, asFloat(0xffffffffu));  // dummy slot (degenerate)
     isect[3 * (size_t)n + 1] = make_float4(0, 0, 0, asFloat(0u));

@@ -142,49 +142,6 @@ __device__ HitRec traceClosest(const DevScene& S, float3 o, float3 d) {
     return best;
 }
 
-// Any-hit over shadow-opaque triangles with 0.0005 < t < tmax.  Sets
-// `sawNonOpaque` when a cut-out or transmissive triangle lies in range.
-__device__ bool traceAnyOpaque(const DevScene& S, float3 o, float3 d, float tmax, bool& sawNonOpaque) {
-    if (S.node_count == 0) return false;
-    float3 inv = rcp3(d);
-    int stackNode[kStackSize];
-    int sp = 0;
-    uint32_t node = 0;
-    for (;;) {
-        if ((node & kLeafBit) == 0) {
-            const float4* n = S.nodes + 4 * (size_t)node;
-            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
-            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
-            float tl, tr;
-            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, o, inv, tmax, tl);
-            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, o, inv, tmax, tr);
-            if (hl && hr) {
-                bool rFirst = tr < tl;
-                if (sp < kStackSize) stackNode[sp++] = rFirst ? ch.x : ch.y;
-                node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
-                continue;
-            }
-            if (hl) { node = (uint32_t)ch.x; continue; }
-            if (hr) { node = (uint32_t)ch.y; continue; }
-        } else {
-            uint32_t first = (node & ~kLeafBit) >> 3;
-            uint32_t cnt = (node & 7u) + 1u;
-            for (uint32_t i = first; i < first + cnt; ++i) {
-                const float4* q = S.isect + 3 * (size_t)i;
-                float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
-                float t, u, v;
-                if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) && t < tmax) {
-                    if (__float_as_uint(c.w) & 1u) return true;
-                    sawNonOpaque = true;
-                }
-            }
-        }
-        if (sp == 0) break;
-        node = (uint32_t)stackNode[--sp];
-    }
-    return false;
-}
-
 // ---------------------------------------------- resumable traversal ------
 // The persistent kernels advance each lane's ray a bounded number of node or
 // leaf visits at a time and refill finished lanes with new rays, so a warp's
@@ -265,25 +222,35 @@ __device__ __forceinline__ bool closestSteps(const DevScene& S, ClosestState& st
     return false;
 }
 
+// Whether a triangle slot's flags block a shadow ray for a render whose
+// material table has opacity bits `mask` (material IDs below 32).
+__device__ __forceinline__ bool blocksShadow(uint32_t flags, uint32_t mask) {
+    uint32_t mid = flags >> 8;
+    return mid < 32u ? ((mask >> mid) & 1u) != 0u : (flags & 1u) != 0u;
+}
+
 struct AnyState {
     float3 o, d, inv;
     float tmax;
     uint32_t node;
+    uint32_t opaqueMask;
     int sp;
     bool sawNonOpaque;
 };
 
-__device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float tmax) {
+__device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float tmax, uint32_t opaqueMask) {
     st.o = o;
     st.d = d;
     st.inv = rcp3(d);
     st.tmax = tmax;
     st.node = 0;
+    st.opaqueMask = opaqueMask;
     st.sp = 0;
     st.sawNonOpaque = false;
 }
 
-// Up to `budget` visits of traceAnyOpaque: 0 running, 1 finished without an
+// Up to `budget` node visits of the any-hit query over shadow-blocking
+// triangles with 0.0005 < t < tmax: 0 running, 1 finished without an
 // opaque blocker, 2 occluded.
 __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* stackNode, int budget) {
     for (int it = 0; it < budget; ++it) {
@@ -310,7 +277,7 @@ __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* st
                 float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
                 float t, u, v;
                 if (mtTest(st.o, st.d, xyz(a), xyz(b), xyz(c), t, u, v) && t < st.tmax) {
-                    if (__float_as_uint(c.w) & 1u) return 2;
+                    if (blocksShadow(__float_as_uint(c.w), st.opaqueMask)) return 2;
                     st.sawNonOpaque = true;
                 }
             }

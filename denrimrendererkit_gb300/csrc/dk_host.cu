@@ -13,28 +13,23 @@
 #include <thread>
 #include <vector>
 
-#include "dk_kernels.h"
+#include "dk_host.h"
+
+namespace dk {
 
 namespace {
-
 thread_local std::string g_error;
+int g_device = -1;
+cudaDeviceProp g_prop;
+}  // namespace
 
 int fail(int code, const std::string& msg) {
     g_error = msg;
     return code;
 }
 
-#define DK_CUDA(call, what)                                                                         \
-    do {                                                                                            \
-        cudaError_t _e = (call);                                                                    \
-        if (_e != cudaSuccess) {                                                                    \
-            int _code = (_e == cudaErrorMemoryAllocation) ? DK_ERROR_OUT_OF_MEMORY : DK_ERROR_COMMAND_FAILED; \
-            return fail(_code, std::string(what) + ": " + cudaGetErrorString(_e));                 \
-        }                                                                                           \
-    } while (0)
-
-int g_device = -1;
-cudaDeviceProp g_prop;
+// Lets other translation units of the library report through dk_last_error_message().
+void setLastError(const std::string& message) { g_error = message; }
 
 int ensureDevice() {
     if (g_device >= 0) return DK_OK;
@@ -48,6 +43,30 @@ int ensureDevice() {
     g_device = 0;
     return DK_OK;
 }
+
+const cudaDeviceProp& deviceProp() { return g_prop; }
+
+int openDevice(int ordinal) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(DK_ERROR_NO_DEVICE, "No compatible CUDA device is available.");
+    }
+    if (ordinal < 0 || ordinal >= n) return fail(DK_ERROR_INVALID_ARGUMENT, "device ordinal out of range");
+    DK_CUDA(cudaSetDevice(ordinal), "cudaSetDevice");
+    DK_CUDA(cudaGetDeviceProperties(&g_prop, ordinal), "cudaGetDeviceProperties");
+    if (g_prop.major < 10) return fail(DK_ERROR_MISSING_KERNEL, "this library carries sm_103a kernels only");
+    g_device = ordinal;
+    return DK_OK;
+}
+
+const char* lastError() { return g_error.c_str(); }
+
+}  // namespace dk
+
+namespace {
+
+using dk::fail;
 
 // ------------------------------------------------------ BVH builder -------
 // BVHBuilder.build (Acceleration/BVHBuilder.swift:7-135) + BVHFlattener
@@ -138,57 +157,27 @@ uint32_t buildReferenceBvh(const dk_triangle* tris, uint32_t n, uint32_t maxLeaf
     return count;
 }
 
-// ----------------------------------------------------- scene on device ----
-struct DeviceBuffer {
-    void* ptr = nullptr;
-    size_t bytes = 0;
-};
-
+// ----------------------------------------------------------- session ----
 struct Session {
     dk_settings settings;
     dk::DevScene scene;
     dk::Wave wave;
     dk::Accum accum;
-    std::vector<DeviceBuffer> buffers;
+    dk::DevJob* jobs = nullptr;  // device copy of the wave's job table (one job)
+    dk::Arena arena;
     float4* staging = nullptr;
     cudaStream_t stream = nullptr;
     std::vector<cudaEvent_t> evPool;
     uint32_t sampleCount = 0;
-    uint32_t lightCount = 0;
     dk_stats stats;
-    int gridGen = 0, gridExtend = 0, gridShade = 0, gridShadow = 0, gridFinal = 0;
-    size_t deviceBytes = 0;
+    dk::Grids grids;
+    uint32_t opaqueMask = 0;
 };
-
-template <typename T>
-int deviceAlloc(Session* s, T** out, size_t count, const char* what) {
-    *out = nullptr;
-    if (count == 0) return DK_OK;
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(e == cudaErrorMemoryAllocation ? DK_ERROR_OUT_OF_MEMORY : DK_ERROR_COMMAND_FAILED,
-                    std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
-    }
-    s->buffers.push_back({p, count * sizeof(T)});
-    s->deviceBytes += count * sizeof(T);
-    *out = static_cast<T*>(p);
-    return DK_OK;
-}
-
-template <typename T>
-int upload(Session* s, T** out, const T* host, size_t count, const char* what) {
-    int rc = deviceAlloc(s, out, count, what);
-    if (rc != DK_OK || count == 0) return rc;
-    DK_CUDA(cudaMemcpy(*out, host, count * sizeof(T), cudaMemcpyHostToDevice), what);
-    return DK_OK;
-}
 
 void freeSession(Session* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    for (auto& b : s->buffers) cudaFree(b.ptr);
+    s->arena.release();
     for (auto& e : s->evPool) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -196,17 +185,299 @@ void freeSession(Session* s) {
 
 }  // namespace
 
-// Kernel symbols for occupancy queries.
 namespace dk {
+
+int Arena::allocBytes(void** out, size_t n, const char* what) {
+    *out = nullptr;
+    if (n == 0) return DK_OK;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? DK_ERROR_OUT_OF_MEMORY : DK_ERROR_COMMAND_FAILED,
+                    std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
+    }
+    buffers.push_back({p, n});
+    bytes += n;
+    *out = p;
+    return DK_OK;
+}
+
+void Arena::release() {
+    for (auto& b : buffers) cudaFree(b.ptr);
+    buffers.clear();
+    bytes = 0;
+}
+
 int kernelGrid(int which, int smCount);
 
-// Lets other translation units of the library report through dk_last_error_message().
-void setLastError(const std::string& message) { g_error = message; }
+Grids kernelGrids() {
+    int sm = g_prop.multiProcessorCount;
+    return Grids{kernelGrid(0, sm), kernelGrid(1, sm), kernelGrid(2, sm), kernelGrid(3, sm), kernelGrid(4, sm)};
 }
+
+bool materialBlocksShadow(const dk_material& m) {
+    float transmission = std::fmin(std::fmax(m.emission.w, 0.0f), 1.0f);
+    return m.base_color.w > 0.001f && transmission <= 0.001f;
+}
+
+uint32_t opaqueMask(const dk_material* mats, uint32_t count) {
+    uint32_t mask = 0;
+    for (uint32_t i = 0; i < count && i < 32u; ++i)
+        if (materialBlocksShadow(mats[i])) mask |= 1u << i;
+    return mask;
+}
+
+int validateScene(const dk_scene* sc) {
+    if (sc->triangle_count == 0 && sc->volume_count == 0)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no renderable geometry.");
+    if (sc->material_count == 0 || !sc->materials)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no materials.");
+    if (sc->volume_count != 0) {
+        if (!sc->volumes) return fail(DK_ERROR_INVALID_ARGUMENT, "volumes is null while volume_count is not zero");
+        for (uint32_t i = 0; i < sc->volume_count; ++i)
+            if (sc->volumes[i].metadata.w != 1u)
+                return fail(DK_ERROR_INVALID_SCENE,
+                            "Invalid render scene: only sparse-brick distance volumes are supported by this backend.");
+        if ((sc->volume_brick_count && !sc->volume_bricks) || (sc->volume_brick_sample_count && !sc->volume_brick_samples) ||
+            (sc->volume_brick_grid_count && !sc->volume_brick_grids) ||
+            (sc->volume_brick_grid_index_count && !sc->volume_brick_grid_indices))
+            return fail(DK_ERROR_INVALID_ARGUMENT, "a volume array pointer is null while its count is not zero");
+        if (sc->volume_brick_sample_count >= (1ull << 32) || sc->volume_brick_grid_index_count >= (1ull << 32))
+            return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: volume arrays exceed 2^32 entries.");
+    }
+    if (sc->triangle_count && !sc->triangles) return fail(DK_ERROR_INVALID_ARGUMENT, "triangles is null");
+    if ((sc->light_count && !sc->lights) || (sc->environment_sample_count && !sc->environment_samples) ||
+        (sc->texture_descriptor_count && !sc->texture_descriptors) || (sc->texture_pixel_count && !sc->texture_pixels) ||
+        (sc->node_count && !sc->nodes) || (sc->primitive_index_count && !sc->primitive_indices))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "a scene array pointer is null while its count is not zero");
+    if (sc->environment_texture_index_plus_one > sc->texture_descriptor_count)
+        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: environment texture index out of range.");
+    for (uint32_t i = 0; i < sc->texture_descriptor_count; ++i) {
+        const dk_uint4& md = sc->texture_descriptors[i].metadata;
+        if ((uint64_t)md.x + (uint64_t)md.y * md.z > sc->texture_pixel_count)
+            return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: texture descriptor exceeds the pixel array.");
+    }
+    // Light records whose triangle is out of range are tolerated like the
+    // reference: sampleDirectLighting skips them.
+    return DK_OK;
+}
+
+int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity) {
+    // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
+    // reaches, each carrying its reference DFS slot as the tie-break key.
+    std::vector<float4> tNodes, tIsect;
+    bool allOpaque = true;
+    {
+        std::vector<uint32_t> slotOf;
+        std::string err;
+        if (!referenceSlots(sc, slotOf, err)) return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + err + ".");
+        std::vector<uint8_t> opaque(sc->triangle_count);
+        for (uint32_t i = 0; i < sc->triangle_count; ++i) {
+            const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
+            // shadowOccluded (PathTrace.metal:4230-4241): cut-outs pass, transmissive layers tint.
+            opaque[i] = materialBlocksShadow(m) ? 1 : 0;
+            if (!opaque[i] && slotOf[i] != kNoSlot) allOpaque = false;
+        }
+        int brc = buildSahTraversal(sc, slotOf, opaque, tNodes, tIsect, err);
+        if (brc != DK_OK) return fail(brc, "Invalid render scene: " + err + ".");
+    }
+    std::memset(&D, 0, sizeof(D));
+#define TRY(x)                         \
+    do {                               \
+        int _rc = (x);                 \
+        if (_rc != DK_OK) return _rc;  \
+    } while (0)
+    TRY(arena.upload(const_cast<dk_triangle**>(&D.tris), sc->triangles, sc->triangle_count, "triangles"));
+    {
+        dk_material* mats = nullptr;
+        TRY(arena.alloc(&mats, std::max(materialCapacity, sc->material_count), "materials"));
+        DK_CUDA(cudaMemcpy(mats, sc->materials, sc->material_count * sizeof(dk_material), cudaMemcpyHostToDevice),
+                "materials");
+        D.mats = mats;
+    }
+    TRY(arena.upload(const_cast<float4**>(&D.isect), tIsect.data(), tIsect.size(), "triangle slots"));
+    TRY(arena.upload(const_cast<float4**>(&D.nodes), tNodes.data(), tNodes.size(), "BVH nodes"));
+    TRY(arena.upload(const_cast<dk_texture_descriptor**>(&D.texdesc), sc->texture_descriptors,
+                     sc->texture_descriptor_count, "texture descriptors"));
+    TRY(arena.upload(const_cast<float4**>(&D.texpix), reinterpret_cast<const float4*>(sc->texture_pixels),
+                     (size_t)sc->texture_pixel_count, "texture pixels"));
+    TRY(arena.upload(const_cast<dk_light_record**>(&D.lights), sc->lights, sc->light_count, "lights"));
+    TRY(arena.upload(const_cast<float2**>(&D.env), reinterpret_cast<const float2*>(sc->environment_samples),
+                     sc->environment_sample_count, "environment samples"));
+    // Guide table over the environment CDF (only when the CDF is monotone).
+    if (sc->environment_sample_count > 1 && sc->environment_samples) {
+        const uint32_t n = sc->environment_sample_count;
+        bool monotone = true;
+        for (uint32_t i = 1; i < n && monotone; ++i)
+            monotone = sc->environment_samples[i].cdf >= sc->environment_samples[i - 1].cdf;
+        if (monotone) {
+            const uint32_t G = 8192;
+            std::vector<uint32_t> guide(G + 1);
+            for (uint32_t b = 0; b <= G; ++b) {
+                float target = (float)b / (float)G;  // exact: b * 2^-13
+                uint32_t lo = 0, hi = n;
+                while (lo < hi) {
+                    uint32_t mid = (lo + hi) >> 1;
+                    if (target <= sc->environment_samples[mid].cdf) hi = mid; else lo = mid + 1;
+                }
+                guide[b] = lo;
+            }
+            TRY(arena.upload(const_cast<uint32_t**>(&D.env_guide), guide.data(), guide.size(), "environment guide"));
+            D.env_guide_size = G;
+        }
+    }
+    // Sparse distance volumes: the reference arrays plus a distance-only copy
+    // of the packed samples for the march.
+    if (sc->volume_count) {
+        TRY(arena.upload(const_cast<dk_volume_descriptor**>(&D.volumes), sc->volumes, sc->volume_count, "volumes"));
+        TRY(arena.upload(const_cast<dk_volume_brick_descriptor**>(&D.bricks), sc->volume_bricks,
+                         sc->volume_brick_count, "volume bricks"));
+        TRY(arena.upload(const_cast<dk_volume_brick_sample**>(&D.brick_samples), sc->volume_brick_samples,
+                         (size_t)sc->volume_brick_sample_count, "volume brick samples"));
+        std::vector<float> dist((size_t)sc->volume_brick_sample_count);
+        for (size_t i = 0; i < dist.size(); ++i) dist[i] = sc->volume_brick_samples[i].distance;
+        TRY(arena.upload(const_cast<float**>(&D.brick_dist), dist.data(), dist.size(), "volume brick distances"));
+        TRY(arena.upload(const_cast<dk_volume_brick_grid**>(&D.brick_grids), sc->volume_brick_grids,
+                         sc->volume_brick_grid_count, "volume brick grids"));
+        TRY(arena.upload(const_cast<uint32_t**>(&D.brick_grid_indices), sc->volume_brick_grid_indices,
+                         (size_t)sc->volume_brick_grid_index_count, "volume brick grid indices"));
+        D.volume_count = sc->volume_count;
+        D.brick_count = sc->volume_brick_count;
+        D.brick_sample_count = sc->volume_brick_sample_count;
+        D.brick_grid_count = sc->volume_brick_grid_count;
+        D.brick_grid_index_count = sc->volume_brick_grid_index_count;
+        bool volOpaque = true;
+        for (uint32_t i = 0; i < sc->material_count; ++i)
+            if (!materialBlocksShadow(sc->materials[i])) volOpaque = false;
+        D.volume_all_opaque = volOpaque ? 1u : 0u;
+    }
+#undef TRY
+    D.tri_count = sc->triangle_count;
+    D.mat_count = sc->material_count;
+    D.node_count = (uint32_t)(tNodes.size() / 4);
+    D.all_shadow_opaque = allOpaque ? 1u : 0u;
+    D.texdesc_count = sc->texture_descriptor_count;
+    D.light_count = sc->lights ? sc->light_count : 0;
+    D.env_count = sc->environment_samples ? sc->environment_sample_count : 0;
+    D.env_tex_plus1 = sc->environment_texture_index_plus_one;
+    D.env_intensity = sc->environment_intensity;
+    D.env_rot_y = sc->environment_rotation_y;
+    D.env_max_radiance = sc->environment_max_radiance;
+    return DK_OK;
+}
+
+int allocWave(Arena& arena, Wave& W, uint64_t capPaths, uint32_t pixelCap, uint32_t jobCap) {
+    std::memset(&W, 0, sizeof(W));
+    W.cap = (uint32_t)capPaths;
+    W.aov_stride = pixelCap;
+    const size_t cap = W.cap;
+#define TRY(x)                         \
+    do {                               \
+        int _rc = (x);                 \
+        if (_rc != DK_OK) return _rc;  \
+    } while (0)
+    TRY(arena.alloc(&W.ray_o, cap, "ray origins"));
+    TRY(arena.alloc(&W.ray_d, cap, "ray directions"));
+    TRY(arena.alloc(&W.tp, cap, "throughput"));
+    TRY(arena.alloc(&W.rad, cap, "radiance"));
+    TRY(arena.alloc(&W.rng, cap, "rng"));
+    TRY(arena.alloc(&W.hit, cap, "hits"));
+    TRY(arena.alloc(&W.nee_o, 3 * cap, "shadow origins"));
+    TRY(arena.alloc(&W.nee_d, 3 * cap, "shadow directions"));
+    TRY(arena.alloc(&W.nee_c, 3 * cap, "shadow contributions"));
+    TRY(arena.alloc(&W.nee_tp, cap, "shadow throughput"));
+    TRY(arena.alloc(&W.q[0], cap, "queue 0"));
+    TRY(arena.alloc(&W.q[1], cap, "queue 1"));
+    TRY(arena.alloc(&W.qs, cap, "shadow queue"));
+    TRY(arena.alloc(&W.qr, 3 * cap, "shadow ray queue"));
+    TRY(arena.alloc(&W.qr2, 3 * cap, "layer-walk queue"));
+    TRY(arena.alloc(&W.counts, 8, "queue counters"));
+    TRY(arena.alloc(&W.aov, 4 * (size_t)pixelCap, "AOV records"));
+    DevJob* jobs = nullptr;
+    TRY(arena.alloc(&jobs, std::max(jobCap, 1u), "job table"));
+    W.jobs = jobs;
+#undef TRY
+    return DK_OK;
+}
+
+int allocAccum(Arena& arena, Accum& A, size_t pixels) {
+    std::memset(&A, 0, sizeof(A));
+    int rc;
+    if ((rc = arena.alloc(&A.sum, pixels, "accumulation sum")) != DK_OK) return rc;
+    if ((rc = arena.alloc(&A.comp, pixels, "accumulation compensation")) != DK_OK) return rc;
+    if ((rc = arena.alloc(&A.resolved, pixels, "accumulation resolve")) != DK_OK) return rc;
+    if ((rc = arena.alloc(&A.count, pixels, "sample counts")) != DK_OK) return rc;
+    return arena.alloc(&A.aov, 6 * pixels, "AOV planes");
+}
+
+int clearAccum(const Accum& A, size_t pixels, cudaStream_t st) {
+    DK_CUDA(cudaMemsetAsync(A.sum, 0, pixels * sizeof(float4), st), "clear accumulation");
+    DK_CUDA(cudaMemsetAsync(A.comp, 0, pixels * sizeof(float4), st), "clear accumulation");
+    DK_CUDA(cudaMemsetAsync(A.resolved, 0, pixels * sizeof(D4), st), "clear accumulation");
+    DK_CUDA(cudaMemsetAsync(A.count, 0, pixels * sizeof(uint32_t), st), "clear accumulation");
+    return DK_OK;
+}
+
+void fillParams(DevParams& P, const dk_settings& st) {
+    std::memset(&P, 0, sizeof(P));
+    P.width = st.width;
+    P.height = st.height;
+    P.max_bounces = std::max(1u, st.max_bounces);
+    P.transparent_background = st.transparent_background;
+    P.shows_env_bg = st.shows_environment_background;
+    P.frame_seed = st.frame_seed;
+    P.denoiser = st.denoiser_enabled;
+    P.bg[0] = st.background_color[0];
+    P.bg[1] = st.background_color[1];
+    P.bg[2] = st.background_color[2];
+    P.clamp = st.sample_radiance_clamp_set ? st.sample_radiance_clamp : 64.0f;  // RenderQuality.final default
+    P.tile_x = 0;
+    P.tile_y = 0;
+    P.tile_w = st.width;
+    P.tile_h = st.height;
+    P.cam = st.camera;
+    P.prev_cam = st.previous_camera;
+}
+
+int launchWave(const DevScene& S, const Wave& W, uint32_t maxBounces, bool anyDenoiser, const Grids& g,
+               cudaStream_t q, const std::function<int(int)>& mark, uint64_t& launches) {
+#define MARK(k)                       \
+    do {                              \
+        int _rc = mark(k);            \
+        if (_rc != DK_OK) return _rc; \
+    } while (0)
+    MARK(0);
+    DK_CUDA(launchGenerate(S, W, g.gen, q), "generate launch");
+    ++launches;
+    for (uint32_t b = 0; b < maxBounces; ++b) {
+        uint32_t sel = b & 1u;
+        MARK(1);
+        DK_CUDA(launchExtend(S, W, sel, g.extend, q), "extend launch");
+        MARK(2);
+        DK_CUDA(launchShade(S, W, b, sel, g.shade, q), "shade launch");
+        MARK(3);
+        DK_CUDA(launchShadow(S, W, g.shadow, q), "shadow launch");
+        DK_CUDA(launchResolve(W, g.final, q), "resolve launch");
+        launches += 4;
+    }
+    MARK(0);
+    if (anyDenoiser) {
+        DK_CUDA(launchAovPrimary(S, W, g.extend, q), "AOV launch");
+        ++launches;
+    }
+    DK_CUDA(launchFinalize(W, g.final, q), "finalize launch");
+    ++launches;
+    MARK(0);
+#undef MARK
+    return DK_OK;
+}
+
+}  // namespace dk
 
 extern "C" {
 
-const char* dk_last_error_message(void) { return g_error.c_str(); }
+const char* dk_last_error_message(void) { return dk::lastError(); }
 
 const char* dk_version(void) { return "denrim-gb300 0.1 (sm_103a wavefront path tracer)"; }
 
@@ -221,19 +492,7 @@ int dk_device_count(int* out) {
     return DK_OK;
 }
 
-int dk_device_open(int ordinal) {
-    int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
-        cudaGetLastError();
-        return fail(DK_ERROR_NO_DEVICE, "No compatible CUDA device is available.");
-    }
-    if (ordinal < 0 || ordinal >= n) return fail(DK_ERROR_INVALID_ARGUMENT, "device ordinal out of range");
-    DK_CUDA(cudaSetDevice(ordinal), "cudaSetDevice");
-    DK_CUDA(cudaGetDeviceProperties(&g_prop, ordinal), "cudaGetDeviceProperties");
-    if (g_prop.major < 10) return fail(DK_ERROR_MISSING_KERNEL, "this library carries sm_103a kernels only");
-    g_device = ordinal;
-    return DK_OK;
-}
+int dk_device_open(int ordinal) { return dk::openDevice(ordinal); }
 
 int dk_build_bvh(const dk_triangle* tris, uint32_t n, uint32_t maxLeaf, dk_bvh_node* nodes, uint32_t* nodeCount,
                  uint32_t* primIdx) {
@@ -290,7 +549,7 @@ int dk_build_environment_samples(const dk_float4* pixels, uint32_t w, uint32_t h
         return fail(DK_ERROR_INVALID_ARGUMENT, "dk_build_environment_samples: null argument");
     *outCount = 0;
     if (w == 0 || h == 0) return DK_OK;
-    int rc = ensureDevice();
+    int rc = dk::ensureDevice();
     if (rc != DK_OK) return rc;
     size_t n = (size_t)w * h;
     if (n > 0xffffffffull / 2) return fail(DK_ERROR_INVALID_ARGUMENT, "environment map too large");
@@ -307,7 +566,7 @@ int dk_build_environment_samples(const dk_float4* pixels, uint32_t w, uint32_t h
     if (e == cudaSuccess) e = cudaMemcpy(dPix, pixels, n * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = dk::buildEnvironmentTable(dPix, w, h, std::fmax(intensity, 0.0f), std::fmax(maxRadiance, 0.0f), dW, dP, dB,
-                                      dOut, 4 * g_prop.multiProcessorCount, 0, &total);
+                                      dOut, 4 * dk::deviceProp().multiProcessorCount, 0, &total);
     if (e == cudaSuccess && total > 0.0) e = cudaMemcpy(out, dOut, n * sizeof(float2), cudaMemcpyDeviceToHost);
     cudaFree(dPix);
     cudaFree(dW);
@@ -327,61 +586,10 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
         return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Render dimensions must be positive.");
     if (st->quality != DK_QUALITY_FINAL)
         return fail(DK_ERROR_INVALID_ARGUMENT, "only RenderQuality.final (the path tracer) is implemented");
-    if (sc->triangle_count == 0 && sc->volume_count == 0)
-        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no renderable geometry.");
-    if (sc->material_count == 0 || !sc->materials)
-        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Scene contains no materials.");
-    if (sc->volume_count != 0) {
-        if (!sc->volumes) return fail(DK_ERROR_INVALID_ARGUMENT, "volumes is null while volume_count is not zero");
-        for (uint32_t i = 0; i < sc->volume_count; ++i)
-            if (sc->volumes[i].metadata.w != 1u)
-                return fail(DK_ERROR_INVALID_SCENE,
-                            "Invalid render scene: only sparse-brick distance volumes are supported by this backend.");
-        if ((sc->volume_brick_count && !sc->volume_bricks) || (sc->volume_brick_sample_count && !sc->volume_brick_samples) ||
-            (sc->volume_brick_grid_count && !sc->volume_brick_grids) ||
-            (sc->volume_brick_grid_index_count && !sc->volume_brick_grid_indices))
-            return fail(DK_ERROR_INVALID_ARGUMENT, "a volume array pointer is null while its count is not zero");
-        if (sc->volume_brick_sample_count >= (1ull << 32) || sc->volume_brick_grid_index_count >= (1ull << 32))
-            return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: volume arrays exceed 2^32 entries.");
-    }
-    if (sc->triangle_count && !sc->triangles) return fail(DK_ERROR_INVALID_ARGUMENT, "triangles is null");
-    if ((sc->light_count && !sc->lights) || (sc->environment_sample_count && !sc->environment_samples) ||
-        (sc->texture_descriptor_count && !sc->texture_descriptors) || (sc->texture_pixel_count && !sc->texture_pixels) ||
-        (sc->node_count && !sc->nodes) || (sc->primitive_index_count && !sc->primitive_indices))
-        return fail(DK_ERROR_INVALID_ARGUMENT, "a scene array pointer is null while its count is not zero");
-    if (sc->environment_texture_index_plus_one > sc->texture_descriptor_count)
-        return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: environment texture index out of range.");
-    for (uint32_t i = 0; i < sc->texture_descriptor_count; ++i) {
-        const dk_uint4& md = sc->texture_descriptors[i].metadata;
-        if ((uint64_t)md.x + (uint64_t)md.y * md.z > sc->texture_pixel_count)
-            return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: texture descriptor exceeds the pixel array.");
-    }
-    for (uint32_t i = 0; i < sc->light_count; ++i)
-        if (sc->lights[i].triangle_index >= sc->triangle_count && sc->lights[i].selection_cdf > 0.0f) {
-            // Tolerated like the reference (the light is skipped at sampling time).
-        }
-    int rc = ensureDevice();
+    int rc = dk::validateScene(sc);
     if (rc != DK_OK) return rc;
-
-    // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
-    // reaches, each carrying its reference DFS slot as the tie-break key.
-    std::vector<float4> tNodes, tIsect;
-    bool allOpaque = true;
-    {
-        std::vector<uint32_t> slotOf;
-        std::string err;
-        if (!dk::referenceSlots(sc, slotOf, err)) return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + err + ".");
-        std::vector<uint8_t> opaque(sc->triangle_count);
-        for (uint32_t i = 0; i < sc->triangle_count; ++i) {
-            const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
-            float transmission = std::fmin(std::fmax(m.emission.w, 0.0f), 1.0f);
-            // shadowOccluded (PathTrace.metal:4230-4241): cut-outs pass, transmissive layers tint.
-            opaque[i] = (m.base_color.w > 0.001f && transmission <= 0.001f) ? 1 : 0;
-            if (!opaque[i] && slotOf[i] != dk::kNoSlot) allOpaque = false;
-        }
-        int brc = dk::buildSahTraversal(sc, slotOf, opaque, tNodes, tIsect, err);
-        if (brc != DK_OK) return fail(brc, "Invalid render scene: " + err + ".");
-    }
+    rc = dk::ensureDevice();
+    if (rc != DK_OK) return rc;
 
     Session* s = new Session();
     std::memset(&s->stats, 0, sizeof(s->stats));
@@ -399,81 +607,8 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
         freeSession(s);
         return fail(DK_ERROR_COMMAND_FAILED, "cudaStreamCreate failed");
     }
-
-    dk::DevScene& D = s->scene;
-    std::memset(&D, 0, sizeof(D));
-    TRY(upload(s, const_cast<dk_triangle**>(&D.tris), sc->triangles, sc->triangle_count, "triangles"));
-    TRY(upload(s, const_cast<dk_material**>(&D.mats), sc->materials, sc->material_count, "materials"));
-    TRY(upload(s, const_cast<float4**>(&D.isect), tIsect.data(), tIsect.size(), "triangle slots"));
-    TRY(upload(s, const_cast<float4**>(&D.nodes), tNodes.data(), tNodes.size(), "BVH nodes"));
-    TRY(upload(s, const_cast<dk_texture_descriptor**>(&D.texdesc), sc->texture_descriptors, sc->texture_descriptor_count,
-               "texture descriptors"));
-    TRY(upload(s, const_cast<float4**>(&D.texpix), reinterpret_cast<const float4*>(sc->texture_pixels),
-               (size_t)sc->texture_pixel_count, "texture pixels"));
-    TRY(upload(s, const_cast<dk_light_record**>(&D.lights), sc->lights, sc->light_count, "lights"));
-    TRY(upload(s, const_cast<float2**>(&D.env), reinterpret_cast<const float2*>(sc->environment_samples),
-               sc->environment_sample_count, "environment samples"));
-    // Guide table over the environment CDF (only when the CDF is monotone).
-    if (sc->environment_sample_count > 1 && sc->environment_samples) {
-        const uint32_t n = sc->environment_sample_count;
-        bool monotone = true;
-        for (uint32_t i = 1; i < n && monotone; ++i)
-            monotone = sc->environment_samples[i].cdf >= sc->environment_samples[i - 1].cdf;
-        if (monotone) {
-            const uint32_t G = 8192;
-            std::vector<uint32_t> guide(G + 1);
-            for (uint32_t b = 0; b <= G; ++b) {
-                float target = (float)b / (float)G;  // exact: b * 2^-13
-                uint32_t lo = 0, hi = n;
-                while (lo < hi) {
-                    uint32_t mid = (lo + hi) >> 1;
-                    if (target <= sc->environment_samples[mid].cdf) hi = mid; else lo = mid + 1;
-                }
-                guide[b] = lo;
-            }
-            TRY(upload(s, const_cast<uint32_t**>(&D.env_guide), guide.data(), guide.size(), "environment guide"));
-            D.env_guide_size = G;
-        }
-    }
-    // Sparse distance volumes: the reference arrays plus a distance-only copy
-    // of the packed samples for the march.
-    if (sc->volume_count) {
-        TRY(upload(s, const_cast<dk_volume_descriptor**>(&D.volumes), sc->volumes, sc->volume_count, "volumes"));
-        TRY(upload(s, const_cast<dk_volume_brick_descriptor**>(&D.bricks), sc->volume_bricks, sc->volume_brick_count,
-                   "volume bricks"));
-        TRY(upload(s, const_cast<dk_volume_brick_sample**>(&D.brick_samples), sc->volume_brick_samples,
-                   (size_t)sc->volume_brick_sample_count, "volume brick samples"));
-        std::vector<float> dist((size_t)sc->volume_brick_sample_count);
-        for (size_t i = 0; i < dist.size(); ++i) dist[i] = sc->volume_brick_samples[i].distance;
-        TRY(upload(s, const_cast<float**>(&D.brick_dist), dist.data(), dist.size(), "volume brick distances"));
-        TRY(upload(s, const_cast<dk_volume_brick_grid**>(&D.brick_grids), sc->volume_brick_grids,
-                   sc->volume_brick_grid_count, "volume brick grids"));
-        TRY(upload(s, const_cast<uint32_t**>(&D.brick_grid_indices), sc->volume_brick_grid_indices,
-                   (size_t)sc->volume_brick_grid_index_count, "volume brick grid indices"));
-        D.volume_count = sc->volume_count;
-        D.brick_count = sc->volume_brick_count;
-        D.brick_sample_count = sc->volume_brick_sample_count;
-        D.brick_grid_count = sc->volume_brick_grid_count;
-        D.brick_grid_index_count = sc->volume_brick_grid_index_count;
-        bool volOpaque = true;
-        for (uint32_t i = 0; i < sc->material_count; ++i) {
-            const dk_material& m = sc->materials[i];
-            float transmission = std::fmin(std::fmax(m.emission.w, 0.0f), 1.0f);
-            if (!(m.base_color.w > 0.001f && transmission <= 0.001f)) volOpaque = false;
-        }
-        D.volume_all_opaque = volOpaque ? 1u : 0u;
-    }
-    D.tri_count = sc->triangle_count;
-    D.mat_count = sc->material_count;
-    D.node_count = (uint32_t)(tNodes.size() / 4);
-    D.all_shadow_opaque = allOpaque ? 1u : 0u;
-    D.texdesc_count = sc->texture_descriptor_count;
-    D.light_count = sc->lights ? sc->light_count : 0;
-    D.env_count = sc->environment_samples ? sc->environment_sample_count : 0;
-    D.env_tex_plus1 = sc->environment_texture_index_plus_one;
-    D.env_intensity = sc->environment_intensity;
-    D.env_rot_y = sc->environment_rotation_y;
-    D.env_max_radiance = sc->environment_max_radiance;
+    TRY(dk::uploadScene(s->arena, sc, s->scene, sc->material_count));
+    s->opaqueMask = dk::opaqueMask(sc->materials, sc->material_count);
 
     // Wave capacity: whole frames of the tile, up to a fixed path budget.
     const uint32_t pixels = st->width * st->height;
@@ -481,49 +616,18 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     if (st->max_samples_per_launch > 0) capPaths = std::min<uint64_t>(capPaths, (uint64_t)st->max_samples_per_launch * pixels);
     capPaths = std::max<uint64_t>(capPaths, pixels);
     capPaths = std::min<uint64_t>(capPaths, 0x7fffffffull);
-    dk::Wave& W = s->wave;
-    W.cap = (uint32_t)capPaths;
-    size_t cap = W.cap;
-    TRY(deviceAlloc(s, &W.ray_o, cap, "ray origins"));
-    TRY(deviceAlloc(s, &W.ray_d, cap, "ray directions"));
-    TRY(deviceAlloc(s, &W.tp, cap, "throughput"));
-    TRY(deviceAlloc(s, &W.rad, cap, "radiance"));
-    TRY(deviceAlloc(s, &W.rng, cap, "rng"));
-    TRY(deviceAlloc(s, &W.hit, cap, "hits"));
-    TRY(deviceAlloc(s, &W.nee_o, 3 * cap, "shadow origins"));
-    TRY(deviceAlloc(s, &W.nee_d, 3 * cap, "shadow directions"));
-    TRY(deviceAlloc(s, &W.nee_c, 3 * cap, "shadow contributions"));
-    TRY(deviceAlloc(s, &W.nee_tp, cap, "shadow throughput"));
-    TRY(deviceAlloc(s, &W.q[0], cap, "queue 0"));
-    TRY(deviceAlloc(s, &W.q[1], cap, "queue 1"));
-    TRY(deviceAlloc(s, &W.qs, cap, "shadow queue"));
-    TRY(deviceAlloc(s, &W.qr, 3 * cap, "shadow ray queue"));
-    TRY(deviceAlloc(s, &W.qr2, 3 * cap, "layer-walk queue"));
-    TRY(deviceAlloc(s, &W.counts, 8, "queue counters"));
-    TRY(deviceAlloc(s, &W.aov, 4 * (size_t)pixels, "AOV records"));
-    dk::Accum& A = s->accum;
-    TRY(deviceAlloc(s, &A.sum, pixels, "accumulation sum"));
-    TRY(deviceAlloc(s, &A.comp, pixels, "accumulation compensation"));
-    TRY(deviceAlloc(s, &A.resolved, pixels, "accumulation resolve"));
-    TRY(deviceAlloc(s, &A.count, pixels, "sample counts"));
-    TRY(deviceAlloc(s, &A.aov, 6 * (size_t)pixels, "AOV planes"));
-    TRY(deviceAlloc(s, &s->staging, pixels, "readback staging"));
-    if (cudaMemsetAsync(A.sum, 0, pixels * sizeof(float4), s->stream) != cudaSuccess ||
-        cudaMemsetAsync(A.comp, 0, pixels * sizeof(float4), s->stream) != cudaSuccess ||
-        cudaMemsetAsync(A.resolved, 0, pixels * sizeof(dk::D4), s->stream) != cudaSuccess ||
-        cudaMemsetAsync(A.count, 0, pixels * sizeof(uint32_t), s->stream) != cudaSuccess ||
-        cudaMemsetAsync(A.aov, 0, 6 * pixels * sizeof(float4), s->stream) != cudaSuccess ||
+    TRY(dk::allocWave(s->arena, s->wave, capPaths, pixels, 1));
+    s->jobs = const_cast<dk::DevJob*>(s->wave.jobs);
+    TRY(dk::allocAccum(s->arena, s->accum, pixels));
+    TRY(s->arena.alloc(&s->staging, pixels, "readback staging"));
+    TRY(dk::clearAccum(s->accum, pixels, s->stream));
+    if (cudaMemsetAsync(s->accum.aov, 0, 6 * (size_t)pixels * sizeof(float4), s->stream) != cudaSuccess ||
         cudaStreamSynchronize(s->stream) != cudaSuccess) {
         freeSession(s);
         return fail(DK_ERROR_COMMAND_FAILED, "clearing accumulation buffers failed");
     }
-    int sm = g_prop.multiProcessorCount;
-    s->gridGen = dk::kernelGrid(0, sm);
-    s->gridExtend = dk::kernelGrid(1, sm);
-    s->gridShade = dk::kernelGrid(2, sm);
-    s->gridShadow = dk::kernelGrid(3, sm);
-    s->gridFinal = dk::kernelGrid(4, sm);
-    s->stats.device_bytes = s->deviceBytes;
+    s->grids = dk::kernelGrids();
+    s->stats.device_bytes = s->arena.bytes;
     *outSession = reinterpret_cast<dk_session*>(s);
     return DK_OK;
 #undef TRY
@@ -540,30 +644,23 @@ static int eventAt(Session* s, size_t i, cudaEvent_t* out) {
 }
 
 // Renders `samples` sample indices starting at `sampleBegin` over a tile, in
-// batches of whole tile-frames that fit the wave.  Every stage is bracketed by
-// events on the session stream; they are read once, after the last batch.
+// batches of whole tile-frames that fit the wave (a one-job wave each).  Every
+// stage is bracketed by events on the session stream; they are read once,
+// after the last batch.
 static int renderSamples(Session* s, uint32_t tx, uint32_t ty, uint32_t tw, uint32_t th, uint32_t samples,
                          uint32_t sampleBegin) {
     const dk_settings& st = s->settings;
-    dk::DevParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.width = st.width;
-    P.height = st.height;
-    P.max_bounces = std::max(1u, st.max_bounces);
-    P.transparent_background = st.transparent_background;
-    P.shows_env_bg = st.shows_environment_background;
-    P.frame_seed = st.frame_seed;
-    P.denoiser = st.denoiser_enabled;
-    P.bg[0] = st.background_color[0];
-    P.bg[1] = st.background_color[1];
-    P.bg[2] = st.background_color[2];
-    P.clamp = st.sample_radiance_clamp_set ? st.sample_radiance_clamp : 64.0f;  // RenderQuality.final default
-    P.tile_x = tx;
-    P.tile_y = ty;
-    P.tile_w = tw;
-    P.tile_h = th;
-    P.cam = st.camera;
-    P.prev_cam = st.previous_camera;
+    dk::DevJob job;
+    std::memset(&job, 0, sizeof(job));
+    dk::fillParams(job.P, st);
+    job.P.tile_x = tx;
+    job.P.tile_y = ty;
+    job.P.tile_w = tw;
+    job.P.tile_h = th;
+    job.A = s->accum;
+    job.mat_base = 0;
+    job.mat_count = s->scene.mat_count;
+    job.opaque_mask = s->opaqueMask;
     const uint32_t tileN = tw * th;
     const uint32_t perBatch = std::max(1u, s->wave.cap / tileN);
     cudaStream_t q = s->stream;
@@ -571,51 +668,32 @@ static int renderSamples(Session* s, uint32_t tx, uint32_t ty, uint32_t tw, uint
     // interval between mark i and mark i+1 belongs to kind[i].
     std::vector<int> kinds;
     size_t ev = 0;
-    cudaEvent_t e;
     auto mark = [&](int kind) -> int {
+        cudaEvent_t e;
         int rc = eventAt(s, ev++, &e);
         if (rc != DK_OK) return rc;
         DK_CUDA(cudaEventRecord(e, q), "cudaEventRecord");
         kinds.push_back(kind);
         return DK_OK;
     };
-#define MARK(k)                       \
-    do {                              \
-        int _rc = mark(k);            \
-        if (_rc != DK_OK) return _rc; \
-    } while (0)
     uint64_t launches = 0;
     uint32_t done = 0;
     while (done < samples) {
         uint32_t nb = std::min(perBatch, samples - done);
-        P.sample_begin = sampleBegin + done;
-        P.samples_in_batch = nb;
-        P.path_count = nb * tileN;
-        MARK(0);
-        DK_CUDA(dk::launchGenerate(s->scene, P, s->wave, s->gridGen, q), "generate launch");
-        ++launches;
-        for (uint32_t b = 0; b < P.max_bounces; ++b) {
-            uint32_t sel = b & 1u;
-            MARK(1);
-            DK_CUDA(dk::launchExtend(s->scene, s->wave, sel, s->gridExtend, q), "extend launch");
-            MARK(2);
-            DK_CUDA(dk::launchShade(s->scene, P, s->wave, b, sel, s->gridShade, q), "shade launch");
-            MARK(3);
-            DK_CUDA(dk::launchShadow(s->scene, P, s->wave, s->gridShadow, q), "shadow launch");
-            DK_CUDA(dk::launchResolve(P, s->wave, s->gridFinal, q), "resolve launch");
-            launches += 4;
-        }
-        MARK(0);
-        if (st.denoiser_enabled) {
-            DK_CUDA(dk::launchAovPrimary(s->scene, P, s->wave, s->gridExtend, q), "AOV launch");
-            ++launches;
-        }
-        DK_CUDA(dk::launchFinalize(P, s->wave, s->accum, 1u, s->gridFinal, q), "finalize launch");
-        ++launches;
+        job.P.sample_begin = sampleBegin + done;
+        job.P.samples_in_batch = nb;
+        job.P.path_count = nb * tileN;
+        // Pageable source: the copy is staged before the call returns, so
+        // `job` may change for the next batch at once.
+        DK_CUDA(cudaMemcpyAsync(s->jobs, &job, sizeof(job), cudaMemcpyHostToDevice, q), "job table upload");
+        dk::Wave W = s->wave;
+        W.job_count = 1;
+        W.path_count = job.P.path_count;
+        W.pixel_count = tileN;
+        int rc = dk::launchWave(s->scene, W, job.P.max_bounces, st.denoiser_enabled != 0, s->grids, q, mark, launches);
+        if (rc != DK_OK) return rc;
         done += nb;
     }
-    MARK(0);
-#undef MARK
     DK_CUDA(cudaEventSynchronize(s->evPool[ev - 1]), "render");
     float t[4] = {0, 0, 0, 0};
     for (size_t i = 0; i + 1 < ev; ++i) {
@@ -679,10 +757,8 @@ int dk_session_reset(dk_session* session) {
     Session* s = reinterpret_cast<Session*>(session);
     if (!s) return fail(DK_ERROR_INVALID_ARGUMENT, "session is null");
     size_t pixels = (size_t)s->settings.width * s->settings.height;
-    DK_CUDA(cudaMemsetAsync(s->accum.sum, 0, pixels * sizeof(float4), s->stream), "reset");
-    DK_CUDA(cudaMemsetAsync(s->accum.comp, 0, pixels * sizeof(float4), s->stream), "reset");
-    DK_CUDA(cudaMemsetAsync(s->accum.resolved, 0, pixels * sizeof(dk::D4), s->stream), "reset");
-    DK_CUDA(cudaMemsetAsync(s->accum.count, 0, pixels * sizeof(uint32_t), s->stream), "reset");
+    int rc = dk::clearAccum(s->accum, pixels, s->stream);
+    if (rc != DK_OK) return rc;
     DK_CUDA(cudaStreamSynchronize(s->stream), "reset");
     s->sampleCount = 0;
     return DK_OK;
@@ -697,7 +773,7 @@ int dk_session_read_output(dk_session* session, int output, float* rgba, size_t 
         return fail(DK_ERROR_INVALID_ARGUMENT, "unknown output kind");
     const float4* src;
     if (output == DK_OUTPUT_BEAUTY) {
-        DK_CUDA(dk::launchResolveBeauty(s->accum, (uint32_t)pixels, s->staging, s->gridFinal, s->stream), "resolve launch");
+        DK_CUDA(dk::launchResolveBeauty(s->accum, (uint32_t)pixels, s->staging, s->grids.final, s->stream), "resolve launch");
         src = s->staging;
     } else {
         src = s->accum.aov + (size_t)(output - 1) * pixels;

@@ -98,12 +98,21 @@ __device__ __noinline__ void blendMaterialInto(Material& m, const dk_material* m
     for (int k = 0; k < 17; ++k) f[k] = exMix4(f[k], __ldg(p + k), t);
 }
 
+// A render's material table: S.mats[base, base + count).
+struct MatTable {
+    uint32_t base, count;
+};
+
+__device__ __forceinline__ MatTable matTable(const DevJob& J) {
+    return MatTable{__ldg(&J.mat_base), __ldg(&J.mat_count)};
+}
+
 // materialForHit (:1096-1121); the material-program VM and the field
 // overrides are no-ops here (no programs, no material-field samples).
-__device__ __forceinline__ Material materialForHit(const DevScene& S, const Hit& h) {
-    Material m = loadMaterial(S.mats, min(h.materialID, S.mat_count - 1u));
+__device__ __forceinline__ Material materialForHit(const DevScene& S, MatTable mt, const Hit& h) {
+    Material m = loadMaterial(S.mats, mt.base + min(h.materialID, mt.count - 1u));
     if (h.materialBlend > 0.0f)
-        blendMaterialInto(m, S.mats, min(h.materialID2, S.mat_count - 1u), clampf(h.materialBlend, 0.0f, 1.0f));
+        blendMaterialInto(m, S.mats, mt.base + min(h.materialID2, mt.count - 1u), clampf(h.materialBlend, 0.0f, 1.0f));
     return m;
 }
 
@@ -326,6 +335,26 @@ __device__ bool continueTransmissiveSurface(const Hit& h, const Material& m, Ray
 __device__ __forceinline__ uint32_t gridStride() { return gridDim.x * blockDim.x; }
 __device__ __forceinline__ uint32_t globalId() { return blockIdx.x * blockDim.x + threadIdx.x; }
 
+// The job whose [begin, next begin) range holds `i` (the last job whose
+// begin <= i), by binary search over the wave's ascending job table.
+__device__ __forceinline__ uint32_t jobOfPath(const Wave& W, uint32_t i) {
+    uint32_t lo = 0, hi = W.job_count - 1u;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1u) >> 1;
+        if (__ldg(&W.jobs[mid].path_begin) <= i) lo = mid; else hi = mid - 1u;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint32_t jobOfPixel(const Wave& W, uint32_t i) {
+    uint32_t lo = 0, hi = W.job_count - 1u;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1u) >> 1;
+        if (__ldg(&W.jobs[mid].pixel_begin) <= i) lo = mid; else hi = mid - 1u;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint32_t jobOf(const Wave& W, uint32_t p) { return W.rng[p].y >> 8; }
+
 __device__ __forceinline__ void writeAovMiss(float4* aov, uint32_t local, uint32_t tileN) {
     aov[0 * (size_t)tileN + local] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0u));  // t, -, -, hasHit
     aov[1 * (size_t)tileN + local] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -339,10 +368,14 @@ __device__ __forceinline__ void writeAovHit(float4* aov, uint32_t local, uint32_
     aov[3 * (size_t)tileN + local] = make_float4(h.position.x, h.position.y, h.position.z, 0.0f);
 }
 
-__global__ void __launch_bounds__(256) k_generate(DevScene S, DevParams P, Wave W) {
-    const uint32_t tileN = P.tile_w * P.tile_h;
-    for (uint32_t p = globalId(); p < P.path_count; p += gridStride()) {
-        uint32_t slice = p / tileN, local = p - slice * tileN;
+__global__ void __launch_bounds__(256) k_generate(DevScene S, Wave W) {
+    for (uint32_t p = globalId(); p < W.path_count; p += gridStride()) {
+        uint32_t j = jobOfPath(W, p);
+        const DevJob& J = W.jobs[j];
+        const DevParams& P = J.P;
+        const uint32_t tileN = P.tile_w * P.tile_h;
+        uint32_t rel = p - J.path_begin;
+        uint32_t slice = rel / tileN, local = rel - slice * tileN;
         uint32_t px = P.tile_x + local % P.tile_w, py = P.tile_y + local / P.tile_w;
         uint32_t sample = P.sample_begin + slice;
         uint32_t state = P.frame_seed ^ hash_u32(px + py * P.width) ^ hash_u32(sample + 1u);
@@ -355,12 +388,12 @@ __global__ void __launch_bounds__(256) k_generate(DevScene S, DevParams P, Wave 
         W.ray_d[p] = make_float4(ray.direction.x, ray.direction.y, ray.direction.z, 0.0f);
         W.tp[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         W.rad[p] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-        W.rng[p] = make_uint2(state, 0u);
+        W.rng[p] = make_uint2(state, j << 8);
         W.q[0][p] = p;
-        if (slice == P.samples_in_batch - 1u) writeAovMiss(W.aov, local, tileN);
+        if (slice == P.samples_in_batch - 1u) writeAovMiss(W.aov, J.pixel_begin + local, W.aov_stride);
     }
     if (globalId() == 0) {
-        W.counts[0] = P.path_count;
+        W.counts[0] = W.path_count;
         for (int k = 1; k < 8; ++k) W.counts[k] = 0u;
     }
 }
@@ -424,16 +457,17 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
     }
 }
 
-struct ShadeOut { bool survive; uint32_t neeMask; };
+struct ShadeOut { bool survive; uint32_t neeMask; uint32_t maxBounces; };
 
 // The body of the reference bounce loop (PathTrace.metal:5252-5518) for one
 // path whose closest hit is already in W.hit.
 template <bool kVolumes>
-__device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave& W, uint32_t p, uint32_t bounce) {
-    ShadeOut out{false, 0u};
-    const uint32_t tileN = P.tile_w * P.tile_h;
+__device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint32_t bounce) {
     float4 ro = W.ray_o[p], rd = W.ray_d[p], tpw = W.tp[p], radw = W.rad[p], hr = W.hit[p];
     uint2 rs = W.rng[p];
+    const DevJob& J = W.jobs[rs.y >> 8];
+    const DevParams& P = J.P;
+    ShadeOut out{false, 0u, P.max_bounces};
     Ray ray{xyz(ro), xyz(rd)};
     float3 tp = xyz(tpw);
     float prevPdf = tpw.w;
@@ -459,7 +493,8 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
     }
     HitRec rec{hr.x, tri, hr.z, hr.w};
     Hit h = kVolumes ? makeHitAny(S, ray, rec) : makeHit(S, ray, rec);
-    Material m = kVolumes ? materialForHit(S, h) : loadMaterial(S.mats, min(h.materialID, S.mat_count - 1u));
+    const MatTable mt = matTable(J);
+    Material m = kVolumes ? materialForHit(S, mt, h) : loadMaterial(S.mats, mt.base + min(h.materialID, mt.count - 1u));
     uint32_t nIdx = (uint32_t)m.parameters.w;
     if (nIdx != 0u) h = applyNormalMap(S, h, nIdx, ray.direction);
     uint32_t bIdx = (uint32_t)m.parameters.z;
@@ -476,8 +511,11 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
     }
     if (!primaryFound) {
         flags |= 1u;
-        uint32_t slice = p / tileN;
-        if (slice == P.samples_in_batch - 1u && P.denoiser == 0u) writeAovHit(W.aov, p - slice * tileN, tileN, h, m.baseColor);
+        const uint32_t tileN = P.tile_w * P.tile_h;
+        uint32_t rel = p - J.path_begin;
+        uint32_t slice = rel / tileN;
+        if (slice == P.samples_in_batch - 1u && P.denoiser == 0u)
+            writeAovHit(W.aov, J.pixel_begin + (rel - slice * tileN), W.aov_stride, h, m.baseColor);
     }
 
     bool continued = false;
@@ -632,17 +670,15 @@ __device__ ShadeOut shadePath(const DevScene& S, const DevParams& P, const Wave&
 #define DK_SHADE_MIN_BLOCKS 5
 #endif
 template <bool kVolumes>
-__global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, DevParams P, Wave W, uint32_t bounce,
-                                                                  uint32_t sel) {
+__global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, Wave W, uint32_t bounce, uint32_t sel) {
     const uint32_t* q = W.q[sel];
     uint32_t* qNext = W.q[sel ^ 1u];
     const uint32_t n = W.counts[sel];
     if (globalId() == 0) W.counts[4] = 0u;  // extend cursor of the next bounce
-    const bool lastBounce = bounce + 1u >= P.max_bounces;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
         uint32_t p = q[i];
-        ShadeOut o = shadePath<kVolumes>(S, P, W, p, bounce);
-        bool keep = o.survive && !lastBounce;
+        ShadeOut o = shadePath<kVolumes>(S, W, p, bounce);
+        bool keep = o.survive && bounce + 1u < o.maxBounces;
         uint32_t slot = warpAppend(&W.counts[sel ^ 1u], keep);
         if (keep) qNext[slot] = p;
         bool sh = o.neeMask != 0u;
@@ -661,7 +697,8 @@ __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
 // (0.0005, maxDistance) occludes; otherwise the non-opaque layers are collected
 // in distance order and walked as the reference walks them (re-starting 0.001
 // past each layer, at most 8 steps, transmittance below 0.02 occludes).
-__device__ bool shadowLayers(const DevScene& S, float3 o, float3 d, float tmax, float3& T) {
+__device__ bool shadowLayers(const DevScene& S, MatTable mt, uint32_t opaqueMask, float3 o, float3 d, float tmax,
+                             float3& T) {
     constexpr int kMaxLayers = 8;
     float lt[kMaxLayers];
     uint32_t ltri[kMaxLayers];
@@ -696,7 +733,7 @@ __device__ bool shadowLayers(const DevScene& S, float3 o, float3 d, float tmax, 
                 float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
                 float t, u, v;
                 if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) || !(t < tmax)) continue;
-                if (__float_as_uint(c.w) & 1u) return true;  // opaque blocker
+                if (blocksShadow(__float_as_uint(c.w), opaqueMask)) return true;  // opaque blocker
                 if (count == kMaxLayers - 1) return true;    // an 8th layer: the walk ends occluded
                 int j = count++;
                 while (j > 0 && lt[j - 1] > t) {
@@ -724,7 +761,7 @@ __device__ bool shadowLayers(const DevScene& S, float3 o, float3 d, float tmax, 
         float trel = started ? a - (prev + 0.001f) : a;
         HitRec r{a, ltri[i], lu[i], lv[i]};
         Hit h = makeHit(S, ray, r);
-        Material sm = materialForHit(S, h);
+        Material sm = materialForHit(S, mt, h);
         prev = a;
         started = true;
         if (sm.baseColor.w <= 0.001f) continue;
@@ -742,14 +779,14 @@ __device__ bool shadowLayers(const DevScene& S, float3 o, float3 d, float tmax, 
 // shadowOccluded (PathTrace.metal:4196-4274) exactly as the reference walks
 // it — closest hit per layer, including distance-field hits — for scenes with
 // sparse volumes whose layers the single-pass collection does not model.
-__device__ bool shadowWalk(const DevScene& S, float3 o, float3 d, float maxDistance, float3& T) {
+__device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, float maxDistance, float3& T) {
     float traveled = 0.0f;
     for (uint32_t step = 0; step < 8u; ++step) {
         HitRec r = traceScene(S, o, d);
         if (r.tri == kNoHit || traveled + r.t >= maxDistance) return false;
         Ray ray{o, d};
         Hit h = makeHitAny(S, ray, r);
-        Material sm = materialForHit(S, h);
+        Material sm = materialForHit(S, mt, h);
         if (sm.baseColor.w <= 0.001f) {
             traveled += r.t;
             o = h.position + d * 0.001f;
@@ -803,7 +840,7 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
             e = W.qr[idx];
             size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
             float4 o = W.nee_o[slot], d = W.nee_d[slot];
-            anyInit(st, xyz(o), xyz(d), o.w);
+            anyInit(st, xyz(o), xyz(d), o.w, __ldg(&W.jobs[jobOf(W, e >> 2)].opaque_mask));
         }
         if (__all_sync(0xffffffffu, e == kNoWork && exhausted)) break;
         if (e == kNoWork) continue;
@@ -832,7 +869,10 @@ __global__ void __launch_bounds__(128) k_shadow_layers(DevScene S, Wave W) {
         size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
         float4 o = W.nee_o[slot], d = W.nee_d[slot], c = W.nee_c[slot];
         float3 T = f3(1.0f);
-        bool occluded = S.volume_count ? shadowWalk(S, xyz(o), xyz(d), o.w, T) : shadowLayers(S, xyz(o), xyz(d), o.w, T);
+        const DevJob& J = W.jobs[jobOf(W, e >> 2)];
+        const MatTable mt = matTable(J);
+        bool occluded = S.volume_count ? shadowWalk(S, mt, xyz(o), xyz(d), o.w, T)
+                                       : shadowLayers(S, mt, __ldg(&J.opaque_mask), xyz(o), xyz(d), o.w, T);
         float3 v = occluded ? f3(0.0f) : xyz(c) * T / c.w;
         W.nee_c[slot] = make_float4(v.x, v.y, v.z, 0.0f);
     }
@@ -841,7 +881,7 @@ __global__ void __launch_bounds__(128) k_shadow_layers(DevScene S, Wave W) {
 // `radiance += clampSampleContribution(throughput * direct)` with direct the
 // sum of the path's shadowed NEE terms in the reference's order (light, env 0,
 // env 1; PathTrace.metal:4437-4584, 5396-5421).
-__global__ void __launch_bounds__(256) k_resolve(DevParams P, Wave W) {
+__global__ void __launch_bounds__(256) k_resolve(Wave W) {
     const uint32_t n = W.counts[2];
     const size_t cap = W.cap;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
@@ -852,23 +892,27 @@ __global__ void __launch_bounds__(256) k_resolve(DevParams P, Wave W) {
         for (uint32_t k = 0; k < 3u; ++k)
             if (mask & (1u << k)) direct += xyz(W.nee_c[k * cap + p]);
         float4 r = W.rad[p];
-        float3 add = clampSampleContribution(xyz(tpw) * direct, P.clamp);
+        float3 add = clampSampleContribution(xyz(tpw) * direct, __ldg(&W.jobs[jobOf(W, p)].P.clamp));
         W.rad[p] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
     }
 }
 
 // tracePrimaryAOV (PathTrace.metal:4093-4159) for the denoiser's unjittered AOV ray.
-__global__ void __launch_bounds__(128) k_aov_primary(DevScene S, DevParams P, Wave W) {
-    const uint32_t tileN = P.tile_w * P.tile_h;
-    for (uint32_t local = globalId(); local < tileN; local += gridStride()) {
+__global__ void __launch_bounds__(128) k_aov_primary(DevScene S, Wave W) {
+    for (uint32_t i = globalId(); i < W.pixel_count; i += gridStride()) {
+        const DevJob& J = W.jobs[jobOfPixel(W, i)];
+        const DevParams& P = J.P;
+        if (P.denoiser == 0u) continue;
+        const MatTable mt = matTable(J);
+        uint32_t local = i - J.pixel_begin;
         uint32_t px = P.tile_x + local % P.tile_w, py = P.tile_y + local / P.tile_w;
         Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, 0.5f, 0.5f, 0.0f, 0.0f);
-        writeAovMiss(W.aov, local, tileN);
+        writeAovMiss(W.aov, i, W.aov_stride);
         for (uint32_t pass = 0; pass < 32u; ++pass) {
             HitRec r = traceScene(S, ray.origin, ray.direction);
             if (r.tri == kNoHit) break;
             Hit h = makeHitAny(S, ray, r);
-            Material m = materialForHit(S, h);
+            Material m = materialForHit(S, mt, h);
             uint32_t nIdx = (uint32_t)m.parameters.w;
             if (nIdx != 0u) h = applyNormalMap(S, h, nIdx, ray.direction);
             uint32_t bIdx = (uint32_t)m.parameters.z;
@@ -881,7 +925,7 @@ __global__ void __launch_bounds__(128) k_aov_primary(DevScene S, DevParams P, Wa
                 ray.origin = ex::add(h.position, ex::mul(ray.direction, 0.001f));
                 continue;
             }
-            writeAovHit(W.aov, local, tileN, h, m.baseColor);
+            writeAovHit(W.aov, i, W.aov_stride, h, m.baseColor);
             break;
         }
     }
@@ -915,40 +959,45 @@ __device__ bool projectToScreen(const dk_camera& cam, float3 w, uint32_t width, 
 
 // Kahan-compensated accumulation of every path of the batch into its pixel,
 // in sample order, plus the AOV block (PathTrace.metal:5559-5585) from the
-// batch's last sample.  Past every 4096 samples the FP32 sum is folded into
-// an FP64 resolve buffer.
-__global__ void __launch_bounds__(256) k_finalize(DevParams P, Wave W, Accum A, uint32_t writeAov) {
-    const uint32_t tileN = P.tile_w * P.tile_h;
-    for (uint32_t local = globalId(); local < tileN; local += gridStride()) {
+// batch's last sample.  After every 4096th sample of a pixel the FP32 sum is
+// folded into an FP64 resolve buffer, so the result does not depend on how the
+// samples were split into batches.
+__global__ void __launch_bounds__(256) k_finalize(Wave W) {
+    for (uint32_t i = globalId(); i < W.pixel_count; i += gridStride()) {
+        const DevJob& J = W.jobs[jobOfPixel(W, i)];
+        const DevParams& P = J.P;
+        const Accum A = J.A;
+        const uint32_t tileN = P.tile_w * P.tile_h;
+        uint32_t local = i - J.pixel_begin;
+        const float4* rad = W.rad + J.path_begin;
         uint32_t px = P.tile_x + local % P.tile_w, py = P.tile_y + local / P.tile_w;
         size_t pix = (size_t)py * P.width + px;
         float4 s = A.sum[pix], c = A.comp[pix];
         uint32_t count = A.count[pix];
         for (uint32_t k = 0; k < P.samples_in_batch; ++k) {
-            float4 r = W.rad[(size_t)k * tileN + local];
+            float4 r = rad[(size_t)k * tileN + local];
             float y, t;
             y = r.x - c.x; t = s.x + y; c.x = (t - s.x) - y; s.x = t;
             y = r.y - c.y; t = s.y + y; c.y = (t - s.y) - y; s.y = t;
             y = r.z - c.z; t = s.z + y; c.z = (t - s.z) - y; s.z = t;
             y = r.w - c.w; t = s.w + y; c.w = (t - s.w) - y; s.w = t;
+            if (((count + k + 1u) & 4095u) == 0u) {  // a 4096-sample block is complete: fold it in FP64
+                D4 R = A.resolved[pix];
+                R.x += (double)s.x - (double)c.x;
+                R.y += (double)s.y - (double)c.y;
+                R.z += (double)s.z - (double)c.z;
+                R.w += (double)s.w - (double)c.w;
+                A.resolved[pix] = R;
+                s = make_float4(0, 0, 0, 0);
+                c = make_float4(0, 0, 0, 0);
+            }
         }
         uint32_t newCount = count + P.samples_in_batch;
-        if ((newCount >> 12) != (count >> 12)) {
-            D4 R = A.resolved[pix];
-            R.x += (double)s.x - (double)c.x;
-            R.y += (double)s.y - (double)c.y;
-            R.z += (double)s.z - (double)c.z;
-            R.w += (double)s.w - (double)c.w;
-            A.resolved[pix] = R;
-            s = make_float4(0, 0, 0, 0);
-            c = make_float4(0, 0, 0, 0);
-        }
         A.sum[pix] = s;
         A.comp[pix] = c;
         A.count[pix] = newCount;
-        if (!writeAov) continue;
-        float4 a0 = W.aov[local], a1 = W.aov[(size_t)tileN + local], a2 = W.aov[2 * (size_t)tileN + local],
-               a3 = W.aov[3 * (size_t)tileN + local];
+        const size_t st = W.aov_stride;
+        float4 a0 = W.aov[i], a1 = W.aov[st + i], a2 = W.aov[2 * st + i], a3 = W.aov[3 * st + i];
         size_t plane = (size_t)P.width * P.height;
         if (__float_as_uint(a0.w) != 0u) {
             float t = a0.x;
@@ -1086,8 +1135,8 @@ int kernelGrid(int which, int smCount) {
     return (perSM < 1 ? 1 : perSM) * smCount;
 }
 
-cudaError_t launchGenerate(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
-    k_generate<<<grid, 256, 0, st>>>(S, P, W);
+cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStream_t st) {
+    k_generate<<<grid, 256, 0, st>>>(S, W);
     return cudaGetLastError();
 }
 cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st) {
@@ -1095,31 +1144,28 @@ cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int gri
     if (S.volume_count) k_extend_volume<<<grid, 128, 0, st>>>(S, W, sel);
     return cudaGetLastError();
 }
-cudaError_t launchShade(const DevScene& S, const DevParams& P, const Wave& W, uint32_t bounce, uint32_t sel, int grid,
-                        cudaStream_t st) {
+cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint32_t sel, int grid, cudaStream_t st) {
     if (S.volume_count)
-        k_shade<true><<<grid, 128, 0, st>>>(S, P, W, bounce, sel);
+        k_shade<true><<<grid, 128, 0, st>>>(S, W, bounce, sel);
     else
-        k_shade<false><<<grid, 128, 0, st>>>(S, P, W, bounce, sel);
+        k_shade<false><<<grid, 128, 0, st>>>(S, W, bounce, sel);
     return cudaGetLastError();
 }
-cudaError_t launchShadow(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
-    (void)P;
+cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st) {
     k_shadow_rays<<<grid, 128, 0, st>>>(S, W);
     if (!S.all_shadow_opaque || S.volume_count) k_shadow_layers<<<grid, 128, 0, st>>>(S, W);
     return cudaGetLastError();
 }
-cudaError_t launchResolve(const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
-    k_resolve<<<grid, 256, 0, st>>>(P, W);
+cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st) {
+    k_resolve<<<grid, 256, 0, st>>>(W);
     return cudaGetLastError();
 }
-cudaError_t launchAovPrimary(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st) {
-    k_aov_primary<<<grid, 128, 0, st>>>(S, P, W);
+cudaError_t launchAovPrimary(const DevScene& S, const Wave& W, int grid, cudaStream_t st) {
+    k_aov_primary<<<grid, 128, 0, st>>>(S, W);
     return cudaGetLastError();
 }
-cudaError_t launchFinalize(const DevParams& P, const Wave& W, const Accum& A, uint32_t writeAov, int grid,
-                           cudaStream_t st) {
-    k_finalize<<<grid, 256, 0, st>>>(P, W, A, writeAov);
+cudaError_t launchFinalize(const Wave& W, int grid, cudaStream_t st) {
+    k_finalize<<<grid, 256, 0, st>>>(W);
     return cudaGetLastError();
 }
 cudaError_t launchResolveBeauty(const Accum& A, uint32_t pixels, float4* out, int grid, cudaStream_t st) {

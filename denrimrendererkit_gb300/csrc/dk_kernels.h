@@ -15,8 +15,9 @@ constexpr uint32_t kNoSlot = 0xffffffffu;
 
 // Device copy of the scene.  `isect` holds 3 x float4 per BVH leaf slot:
 // (v0.xyz, reference slot), (v1 - v0, triangle index), (v2 - v0, flags with
-// bit 0 = blocks shadow rays); `nodes` holds 4 x float4 per node: the x, y and
-// z slabs of both child boxes and the two child references.
+// bit 0 = blocks shadow rays under the scene's own materials and bits 8..15 =
+// min(material ID, 255)); `nodes` holds 4 x float4 per node: the x, y and z
+// slabs of both child boxes and the two child references.
 struct DevScene {
     const dk_triangle* tris;
     const dk_material* mats;
@@ -42,7 +43,8 @@ struct DevScene {
     uint32_t volume_count, brick_count, brick_grid_count, volume_all_opaque;
 };
 
-// GPURenderConstants (PathTrace.metal:143-182) for one batch of samples.
+// GPURenderConstants (PathTrace.metal:143-182) for one batch of samples of
+// one render.
 struct DevParams {
     uint32_t width, height, max_bounces, transparent_background;
     uint32_t shows_env_bg, frame_seed, denoiser, pad0;
@@ -53,13 +55,47 @@ struct DevParams {
     dk_camera cam, prev_cam;
 };
 
-// SoA path state of one batch ("wave") of `cap` paths.
+struct alignas(32) D4 { double x, y, z, w; };
+
+// Per-pixel accumulation of one render (a session or a serving job).
+struct Accum {
+    float4* sum;       // Kahan sum
+    float4* comp;      // Kahan compensation
+    D4* resolved;      // FP64 resolve of every completed 4096-sample block
+    uint32_t* count;   // samples accumulated per pixel
+    float4* aov;       // 6 planes: depth, normal, albedo, materialID, objectID, motion
+};
+
+// One render in a wave: a session's batch of samples over a tile, or one
+// serving job's share of the wave.  Its paths are [path_begin, path_begin +
+// P.path_count) of the wave (sample slice major, tile pixel minor) and its
+// tile pixels [pixel_begin, pixel_begin + tile_w * tile_h) of the wave's AOV
+// record.  Its materials are S.mats[mat_base, mat_base + mat_count): the
+// shared geometry's material IDs index the job's own table.  After generation
+// a path carries its job index in bits 8..31 of its flags.
+// `opaque_mask` bit i: material i of the job's table blocks shadow rays
+// (shadowOccluded, PathTrace.metal:4230-4241: not a cut-out, no
+// transmission); material IDs from 32 up use the flag baked into the
+// triangle slot.
+struct DevJob {
+    DevParams P;
+    Accum A;
+    uint32_t path_begin;
+    uint32_t pixel_begin;
+    uint32_t mat_base;
+    uint32_t mat_count;
+    uint32_t opaque_mask;
+    uint32_t pad[3];
+};
+
+// SoA path state of one batch ("wave") of at most `cap` paths, shared by the
+// `job_count` renders of `jobs` (ascending path_begin and pixel_begin).
 struct Wave {
     float4* ray_o;     // origin
     float4* ray_d;     // direction
     float4* tp;        // throughput, w = previous BSDF pdf
     float4* rad;       // radiance, w = alpha
-    uint2* rng;        // RNG state, flags (bit 0: primary hit found)
+    uint2* rng;        // RNG state, flags (bit 0: primary hit found; bits 8..31: job index)
     float4* hit;       // t, triangle, u, v
     float4* nee_o;     // 3 slots x cap: shadow origin, w = max distance
     float4* nee_d;     // 3 slots x cap: shadow direction
@@ -71,20 +107,14 @@ struct Wave {
     uint32_t* qr2;     // shadow rays that need the layer walk (3 x cap entries)
     uint32_t* counts;  // [0], [1] queue lengths, [2] shadow paths, [3] shadow rays, [4] extend cursor,
                        // [5] shadow cursor, [6] layer-walk rays, [7] spare
-    float4* aov;       // 4 x tile pixels: primary-hit record of the batch's last sample
+    float4* aov;       // 4 planes of aov_stride tile pixels: primary-hit record of each job's last sample
+    const DevJob* jobs;
     uint32_t cap;
+    uint32_t aov_stride;
+    uint32_t job_count;
+    uint32_t path_count;   // sum of the jobs' path counts
+    uint32_t pixel_count;  // sum of the jobs' tile pixels
     uint32_t pad;
-};
-
-struct alignas(32) D4 { double x, y, z, w; };
-
-// Per-pixel accumulation of a session.
-struct Accum {
-    float4* sum;       // Kahan sum
-    float4* comp;      // Kahan compensation
-    D4* resolved;   // FP64 resolve of every completed 4096-sample block
-    uint32_t* count;   // samples accumulated per pixel
-    float4* aov;       // 6 planes: depth, normal, albedo, materialID, objectID, motion
 };
 
 // Host-side traversal BVH (dk_bvh.cu).
@@ -92,15 +122,13 @@ bool referenceSlots(const dk_scene* sc, std::vector<uint32_t>& slotOfTri, std::s
 int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri, const std::vector<uint8_t>& opaque,
                       std::vector<float4>& nodes, std::vector<float4>& isect, std::string& err);
 
-cudaError_t launchGenerate(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st);
+cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st);
-cudaError_t launchShade(const DevScene& S, const DevParams& P, const Wave& W, uint32_t bounce, uint32_t sel, int grid,
-                        cudaStream_t st);
-cudaError_t launchShadow(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st);
-cudaError_t launchResolve(const DevParams& P, const Wave& W, int grid, cudaStream_t st);
-cudaError_t launchAovPrimary(const DevScene& S, const DevParams& P, const Wave& W, int grid, cudaStream_t st);
-cudaError_t launchFinalize(const DevParams& P, const Wave& W, const Accum& A, uint32_t writeAov, int grid,
-                           cudaStream_t st);
+cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint32_t sel, int grid, cudaStream_t st);
+cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
+cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st);
+cudaError_t launchAovPrimary(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
+cudaError_t launchFinalize(const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchResolveBeauty(const Accum& A, uint32_t pixels, float4* out, int grid, cudaStream_t st);
 cudaError_t buildEnvironmentTable(const float4* dPixels, uint32_t w, uint32_t h, float intensity, float maxR,
                                   double* dWeights, double* dPrefix, double* dBlockSums, float2* dOut, int grid,

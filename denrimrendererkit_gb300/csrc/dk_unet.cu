@@ -1,0 +1,733 @@
+// Kernels of the learned denoiser (dk_unet_* in include/denrim_cuda.h): a
+// 5-level U-Net over the tracer's beauty + albedo + normal + depth AOVs.
+//
+// Tensors are NHWC bf16 with channel counts that are multiples of 16; a
+// tensor may be a channel slice of a wider buffer (leading dimension `ld`,
+// channel offset), so the decoder's concat(upsampled, skip) inputs are written
+// in place.  3x3 convolutions (stride 1, zero padding 1) are implicit GEMMs
+// on the tensor cores with FP32 accumulation:
+//   forward   out[p][co] = act(b[co] + sum_{tap, ci} in[p + tap][ci] w[co][tap][ci])
+//             M = pixels, N = Cout, K = 9 Cin; also the input gradient, as a
+//             forward convolution of the output gradient with the
+//             tap-flipped, transposed weights;
+//   wgrad     dW[co][tap][ci] += sum_p dOut[p][co] in[p + tap][ci]
+//             M = Cout, N = Cin, K = pixels, split over pixel chunks.
+// Shared-memory tiles are filled with cp.async (zero fill for the padding)
+// through an XOR swizzle that keeps ldmatrix conflict-free.
+#include <cstdint>
+
+#include <cuda_bf16.h>
+
+#include "dk_host.h"
+
+namespace dk {
+namespace {
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// 16-byte async copy; `bytes` 0 fills the destination with zeros.
+__device__ __forceinline__ void cpAsync16(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smemAddr(dst)), "l"(src), "r"(bytes));
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cpAsyncWait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+__device__ __forceinline__ void ldmatrixX4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(smemAddr(p)));
+}
+__device__ __forceinline__ void ldmatrixX4T(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(smemAddr(p)));
+}
+
+// D = A (16x16 bf16, row) * B (16x8 bf16, col) + D (fp32).
+__device__ __forceinline__ void mmaBf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ------------------------------------------------------------ forward ----
+struct ConvArgs {
+    const __nv_bfloat16* in;
+    const __nv_bfloat16* w;  // [cout][9][cin]
+    const float* bias;       // [cout] or null
+    __nv_bfloat16* out;
+    uint32_t n, h, w_, cin, ldi, cout, ldo, coOff;
+    uint32_t M;  // n * h * w
+    int act;     // 0 identity, 1 ReLU
+    int accumulate;
+};
+
+constexpr int kBM = 128;  // pixels per block
+constexpr int kBK = 32;   // channels per k step (4 chunks of 16 bytes)
+constexpr int kStages = 3;
+
+// Byte offset of 16-byte chunk `seg` (0..3) of row `r` in a 64-byte-row tile.
+__device__ __forceinline__ uint32_t swz64(uint32_t r, uint32_t seg) { return r * 64u + ((seg ^ ((r >> 1) & 3u)) << 4); }
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_conv3x3_fwd(ConvArgs a) {
+    __shared__ __align__(128) unsigned char sA[kStages][kBM * 64];
+    __shared__ __align__(128) unsigned char sB[kStages][BN * 64];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+    const uint32_t HW = a.h * a.w_;
+    // This thread loads A row `tid` (one output pixel).
+    const uint32_t m = m0 + tid;
+    const bool rowValid = m < a.M;
+    const uint32_t img = rowValid ? m / HW : 0u, rem = rowValid ? m - img * HW : 0u;
+    const int py = (int)(rem / a.w_), px = (int)(rem - (rem / a.w_) * a.w_);
+    const uint32_t chunks = (a.cin + kBK - 1) / kBK;
+    const uint32_t kIters = 9u * chunks;
+
+    auto loadStage = [&](uint32_t it, int stage) {
+        uint32_t tap = it / chunks, c0 = (it - tap * chunks) * kBK;
+        int dy = (int)(tap / 3u) - 1, dx = (int)(tap % 3u) - 1;
+        int yy = py + dy, xx = px + dx;
+        bool inb = rowValid && yy >= 0 && yy < (int)a.h && xx >= 0 && xx < (int)a.w_;
+        const __nv_bfloat16* src =
+            inb ? a.in + ((size_t)(img * a.h + (uint32_t)yy) * a.w_ + (uint32_t)xx) * a.ldi + c0 : a.in;
+#pragma unroll
+        for (uint32_t seg = 0; seg < 4; ++seg) {
+            bool v = inb && c0 + seg * 8u < a.cin;
+            cpAsync16(&sA[stage][swz64(tid, seg)], v ? src + seg * 8u : a.in, v ? 16u : 0u);
+        }
+#pragma unroll
+        for (uint32_t i = tid; i < (uint32_t)BN * 4u; i += 128u) {
+            uint32_t row = i >> 2, seg = i & 3u;
+            bool v = c0 + seg * 8u < a.cin;
+            const __nv_bfloat16* wsrc = a.w + ((size_t)(n0 + row) * 9u + tap) * a.cin + c0 + seg * 8u;
+            cpAsync16(&sB[stage][swz64(row, seg)], v ? wsrc : a.w, v ? 16u : 0u);
+        }
+    };
+
+    float acc[2][BN / 8][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < BN / 8; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.0f;
+
+#pragma unroll
+    for (int s = 0; s < kStages - 1; ++s) {
+        if ((uint32_t)s < kIters) loadStage(s, s);
+        cpAsyncCommit();
+    }
+    for (uint32_t it = 0; it < kIters; ++it) {
+        cpAsyncWait<kStages - 2>();
+        __syncthreads();
+        uint32_t nxt = it + kStages - 1;
+        if (nxt < kIters) loadStage(nxt, (int)(nxt % kStages));
+        cpAsyncCommit();
+        const int st = (int)(it % kStages);
+#pragma unroll
+        for (uint32_t kk = 0; kk < 2; ++kk) {
+            uint32_t af[2][4];
+#pragma unroll
+            for (uint32_t mt = 0; mt < 2; ++mt) {
+                uint32_t r = warp * 32u + mt * 16u + (lane & 15u);
+                uint32_t seg = kk * 2u + (lane >> 4);
+                ldmatrixX4(af[mt][0], af[mt][1], af[mt][2], af[mt][3], &sA[st][swz64(r, seg)]);
+            }
+#pragma unroll
+            for (uint32_t np = 0; np < (uint32_t)BN / 16u; ++np) {
+                uint32_t r = np * 16u + (lane & 7u) + ((lane >> 4) << 3);
+                uint32_t seg = kk * 2u + ((lane >> 3) & 1u);
+                uint32_t b0, b1, b2, b3;
+                ldmatrixX4(b0, b1, b2, b3, &sB[st][swz64(r, seg)]);
+#pragma unroll
+                for (uint32_t mt = 0; mt < 2; ++mt) {
+                    mmaBf16(acc[mt][2 * np], af[mt], b0, b1);
+                    mmaBf16(acc[mt][2 * np + 1], af[mt], b2, b3);
+                }
+            }
+        }
+    }
+    cpAsyncWait<0>();
+    // Epilogue: bias, activation, optional accumulate, bf16 store.
+#pragma unroll
+    for (uint32_t mt = 0; mt < 2; ++mt) {
+#pragma unroll
+        for (uint32_t half = 0; half < 2; ++half) {
+            uint32_t row = m0 + warp * 32u + mt * 16u + (lane >> 2) + half * 8u;
+            if (row >= a.M) continue;
+            __nv_bfloat16* orow = a.out + (size_t)row * a.ldo + a.coOff;
+#pragma unroll
+            for (uint32_t nt = 0; nt < (uint32_t)BN / 8u; ++nt) {
+                uint32_t col = n0 + nt * 8u + (lane & 3u) * 2u;
+                float v0 = acc[mt][nt][half * 2 + 0], v1 = acc[mt][nt][half * 2 + 1];
+                if (a.bias) {
+                    v0 += a.bias[col];
+                    v1 += a.bias[col + 1];
+                }
+                if (a.act == 1) {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                }
+                __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(orow + col);
+                if (a.accumulate) {
+                    float2 o = __bfloat1622float2(*dst);
+                    v0 += o.x;
+                    v1 += o.y;
+                }
+                *dst = __floats2bfloat162_rn(v0, v1);
+            }
+        }
+    }
+}
+
+// -------------------------------------------------------------- wgrad ----
+struct WgradArgs {
+    const __nv_bfloat16* in;    // [M][ldi], channels [0, cin)
+    const __nv_bfloat16* dout;  // [M][ldd], channels [0, cout)
+    float* dw;                  // [cout][9][cin], accumulated
+    uint32_t n, h, w_, cin, ldi, cout, ldd, M;
+    uint32_t chunk;             // pixels per block (multiple of 32)
+};
+
+constexpr int kWB = 64;  // co and ci per block
+
+// Byte offset of 16-byte chunk `seg` (0..7) of row `r` in a 128-byte-row tile.
+__device__ __forceinline__ uint32_t swz128(uint32_t r, uint32_t seg) { return r * 128u + ((seg ^ (r & 7u)) << 4); }
+
+__global__ void __launch_bounds__(128) k_conv3x3_wgrad(WgradArgs a) {
+    __shared__ __align__(128) unsigned char sA[2][32 * 128];  // [pixel][64 co]
+    __shared__ __align__(128) unsigned char sB[2][32 * 128];  // [pixel][64 ci]
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t tap = blockIdx.z;
+    const uint32_t ciTiles = (a.cin + kWB - 1) / kWB;
+    const uint32_t co0 = (blockIdx.y / ciTiles) * kWB, ci0 = (blockIdx.y % ciTiles) * kWB;
+    const uint32_t p0 = blockIdx.x * a.chunk, p1 = min(p0 + a.chunk, a.M);
+    const int dy = (int)(tap / 3u) - 1, dx = (int)(tap % 3u) - 1;
+    const uint32_t HW = a.h * a.w_;
+    const uint32_t wm = warp >> 1, wn = warp & 1u;  // 2 x 2 warps of 32 co x 32 ci
+
+    auto loadStage = [&](uint32_t pb, int stage) {
+        // 32 pixels x 8 chunks for each operand: 2 + 2 chunks per thread.
+#pragma unroll
+        for (uint32_t k = 0; k < 2; ++k) {
+            uint32_t i = tid + k * 128u, row = i >> 3, seg = i & 7u;
+            uint32_t p = pb + row;
+            bool pv = p < p1;
+            bool v = pv && co0 + seg * 8u < a.cout;
+            const __nv_bfloat16* src = a.dout + (size_t)p * a.ldd + co0 + seg * 8u;
+            cpAsync16(&sA[stage][swz128(row, seg)], v ? src : a.dout, v ? 16u : 0u);
+            bool vb = false;
+            const __nv_bfloat16* bsrc = a.in;
+            if (pv && ci0 + seg * 8u < a.cin) {
+                uint32_t img = p / HW, rem = p - img * HW;
+                int yy = (int)(rem / a.w_) + dy, xx = (int)(rem % a.w_) + dx;
+                if (yy >= 0 && yy < (int)a.h && xx >= 0 && xx < (int)a.w_) {
+                    vb = true;
+                    bsrc = a.in + ((size_t)(img * a.h + (uint32_t)yy) * a.w_ + (uint32_t)xx) * a.ldi + ci0 + seg * 8u;
+                }
+            }
+            cpAsync16(&sB[stage][swz128(row, seg)], bsrc, vb ? 16u : 0u);
+        }
+    };
+
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.0f;
+
+    const uint32_t steps = (p1 > p0) ? (p1 - p0 + 31u) / 32u : 0u;
+    if (steps > 0) loadStage(p0, 0);
+    cpAsyncCommit();
+    for (uint32_t s = 0; s < steps; ++s) {
+        if (s + 1 < steps) loadStage(p0 + (s + 1) * 32u, (int)((s + 1) & 1u));
+        cpAsyncCommit();
+        cpAsyncWait<1>();
+        __syncthreads();
+        const int st = (int)(s & 1u);
+#pragma unroll
+        for (uint32_t kk = 0; kk < 2; ++kk) {  // 16 pixels each
+            uint32_t af[2][4];
+#pragma unroll
+            for (uint32_t mt = 0; mt < 2; ++mt) {
+                // A (co x p) from sA[p][co] through transposed 8x8 loads:
+                // matrices (co 0-7, p 0-7), (co 8-15, p 0-7), (co 0-7, p 8-15), (co 8-15, p 8-15).
+                uint32_t id = lane >> 3;
+                uint32_t prow = kk * 16u + ((id >> 1) << 3) + (lane & 7u);
+                uint32_t seg = (wm * 32u + mt * 16u) / 8u + (id & 1u);
+                ldmatrixX4T(af[mt][0], af[mt][1], af[mt][2], af[mt][3], &sA[st][swz128(prow, seg)]);
+            }
+#pragma unroll
+            for (uint32_t np = 0; np < 2; ++np) {
+                // B (p x ci): matrices (p 0-7, ci 0-7), (p 8-15, ci 0-7), (p 0-7, ci 8-15), (p 8-15, ci 8-15).
+                uint32_t id = lane >> 3;
+                uint32_t prow = kk * 16u + ((id & 1u) << 3) + (lane & 7u);
+                uint32_t seg = (wn * 32u + np * 16u) / 8u + (id >> 1);
+                uint32_t b0, b1, b2, b3;
+                ldmatrixX4T(b0, b1, b2, b3, &sB[st][swz128(prow, seg)]);
+#pragma unroll
+                for (uint32_t mt = 0; mt < 2; ++mt) {
+                    mmaBf16(acc[mt][2 * np], af[mt], b0, b1);
+                    mmaBf16(acc[mt][2 * np + 1], af[mt], b2, b3);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    cpAsyncWait<0>();
+#pragma unroll
+    for (uint32_t mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (uint32_t half = 0; half < 2; ++half) {
+            uint32_t co = co0 + wm * 32u + mt * 16u + (lane >> 2) + half * 8u;
+            if (co >= a.cout) continue;
+#pragma unroll
+            for (uint32_t nt = 0; nt < 4; ++nt) {
+                uint32_t ci = ci0 + wn * 32u + nt * 8u + (lane & 3u) * 2u;
+                if (ci >= a.cin) continue;
+                float* dst = a.dw + ((size_t)co * 9u + tap) * a.cin + ci;
+                atomicAdd(dst, acc[mt][nt][half * 2 + 0]);
+                atomicAdd(dst + 1, acc[mt][nt][half * 2 + 1]);
+            }
+        }
+}
+
+// ------------------------------------------------------- elementwise ----
+__device__ __forceinline__ uint32_t gid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
+
+// dPre = dOut where out > 0 (ReLU), over `c` channels of every pixel.
+__global__ void k_relu_backward(const __nv_bfloat16* out, uint32_t ldo, const __nv_bfloat16* dout, uint32_t ldd,
+                                __nv_bfloat16* dpre, uint32_t ldp, uint32_t c, uint32_t M) {
+    const uint32_t pairs = c / 2u;
+    for (uint64_t i = gid(); i < (uint64_t)M * pairs; i += gstride()) {
+        uint32_t p = (uint32_t)(i / pairs), k = (uint32_t)(i % pairs) * 2u;
+        __nv_bfloat162 o = *reinterpret_cast<const __nv_bfloat162*>(out + (size_t)p * ldo + k);
+        __nv_bfloat162 d = *reinterpret_cast<const __nv_bfloat162*>(dout + (size_t)p * ldd + k);
+        float2 of = __bfloat1622float2(o), df = __bfloat1622float2(d);
+        *reinterpret_cast<__nv_bfloat162*>(dpre + (size_t)p * ldp + k) =
+            __floats2bfloat162_rn(of.x > 0.0f ? df.x : 0.0f, of.y > 0.0f ? df.y : 0.0f);
+    }
+}
+
+// Per-channel sums of dPre (the bias gradient), accumulated into db.
+__global__ void k_bias_grad(const __nv_bfloat16* dpre, uint32_t ld, uint32_t c, uint32_t M, float* db) {
+    // blockDim.x = 256: thread handles channel (tid % c) over a pixel stripe.
+    __shared__ float partial[256];
+    uint32_t ch = threadIdx.x % c, lanes = 256u / c;
+    uint32_t lanePix = threadIdx.x / c;
+    float s = 0.0f;
+    if (lanePix < lanes)
+        for (uint32_t p = blockIdx.x * lanes + lanePix; p < M; p += gridDim.x * lanes)
+            s += __bfloat162float(dpre[(size_t)p * ld + ch]);
+    partial[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < c) {
+        float t = 0.0f;
+        for (uint32_t k = 0; k < lanes; ++k) t += partial[k * c + threadIdx.x];
+        atomicAdd(&db[threadIdx.x], t);
+    }
+}
+
+// 2x2 average pooling: out (h/2, w/2).
+__global__ void k_avgpool2(const __nv_bfloat16* in, uint32_t ldi, __nv_bfloat16* out, uint32_t ldo, uint32_t coOff,
+                           uint32_t c, uint32_t n, uint32_t h, uint32_t w) {
+    const uint32_t ho = h / 2u, wo = w / 2u, pairs = c / 2u;
+    for (uint64_t i = gid(); i < (uint64_t)n * ho * wo * pairs; i += gstride()) {
+        uint32_t k = (uint32_t)(i % pairs) * 2u;
+        uint64_t q = i / pairs;
+        uint32_t x = (uint32_t)(q % wo), y = (uint32_t)((q / wo) % ho), b = (uint32_t)(q / ((uint64_t)wo * ho));
+        size_t base = ((size_t)(b * h + 2u * y) * w + 2u * x) * ldi + k;
+        float2 s = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(in + base));
+        float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(in + base + ldi));
+        float2 u = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(in + base + (size_t)w * ldi));
+        float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(in + base + (size_t)w * ldi + ldi));
+        *reinterpret_cast<__nv_bfloat162*>(out + q * ldo + coOff + k) =
+            __floats2bfloat162_rn(0.25f * (s.x + t.x + u.x + v.x), 0.25f * (s.y + t.y + u.y + v.y));
+    }
+}
+
+// Gradient of the 2x2 average pool: din (+)= dout / 4 on each of the 4 inputs.
+__global__ void k_avgpool2_backward(const __nv_bfloat16* dout, uint32_t ldd, __nv_bfloat16* din, uint32_t ldi,
+                                    uint32_t c, uint32_t n, uint32_t h, uint32_t w, int accumulate) {
+    const uint32_t wo = w / 2u, pairs = c / 2u;
+    for (uint64_t i = gid(); i < (uint64_t)n * h * w * pairs; i += gstride()) {
+        uint32_t k = (uint32_t)(i % pairs) * 2u;
+        uint64_t q = i / pairs;
+        uint32_t x = (uint32_t)(q % w), y = (uint32_t)((q / w) % h), b = (uint32_t)(q / ((uint64_t)w * h));
+        float2 d = __bfloat1622float2(
+            *reinterpret_cast<const __nv_bfloat162*>(dout + ((size_t)(b * (h / 2u) + y / 2u) * wo + x / 2u) * ldd + k));
+        __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(din + q * ldi + k);
+        float2 v = make_float2(0.25f * d.x, 0.25f * d.y);
+        if (accumulate) {
+            float2 o = __bfloat1622float2(*dst);
+            v.x += o.x;
+            v.y += o.y;
+        }
+        *dst = __floats2bfloat162_rn(v.x, v.y);
+    }
+}
+
+// Nearest 2x upsampling: out (2h, 2w).
+__global__ void k_upsample2(const __nv_bfloat16* in, uint32_t ldi, __nv_bfloat16* out, uint32_t ldo, uint32_t coOff,
+                            uint32_t c, uint32_t n, uint32_t h, uint32_t w) {
+    const uint32_t H = 2u * h, W = 2u * w, pairs = c / 2u;
+    for (uint64_t i = gid(); i < (uint64_t)n * H * W * pairs; i += gstride()) {
+        uint32_t k = (uint32_t)(i % pairs) * 2u;
+        uint64_t q = i / pairs;
+        uint32_t x = (uint32_t)(q % W), y = (uint32_t)((q / W) % H), b = (uint32_t)(q / ((uint64_t)W * H));
+        *reinterpret_cast<__nv_bfloat162*>(out + q * ldo + coOff + k) =
+            *reinterpret_cast<const __nv_bfloat162*>(in + ((size_t)(b * h + y / 2u) * w + x / 2u) * ldi + k);
+    }
+}
+
+// Gradient of the nearest upsampling: din = sum of the 4 output gradients.
+__global__ void k_upsample2_backward(const __nv_bfloat16* dout, uint32_t ldd, uint32_t ciOff, __nv_bfloat16* din,
+                                     uint32_t ldi, uint32_t c, uint32_t n, uint32_t h, uint32_t w) {
+    const uint32_t W = 2u * w, pairs = c / 2u;
+    for (uint64_t i = gid(); i < (uint64_t)n * h * w * pairs; i += gstride()) {
+        uint32_t k = (uint32_t)(i % pairs) * 2u;
+        uint64_t q = i / pairs;
+        uint32_t x = (uint32_t)(q % w), y = (uint32_t)((q / w) % h), b = (uint32_t)(q / ((uint64_t)w * h));
+        size_t base = ((size_t)(b * 2u * h + 2u * y) * W + 2u * x) * ldd + ciOff + k;
+        float2 s = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(dout + base));
+        float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(dout + base + ldd));
+        float2 u = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(dout + base + (size_t)W * ldd));
+        float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(dout + base + (size_t)W * ldd + ldd));
+        *reinterpret_cast<__nv_bfloat162*>(din + q * ldi + k) =
+            __floats2bfloat162_rn(s.x + t.x + u.x + v.x, s.y + t.y + u.y + v.y);
+    }
+}
+
+// Channel-slice copy (skip connections into concat buffers, gradient routing).
+__global__ void k_copy_channels(const __nv_bfloat16* src, uint32_t lds, uint32_t sOff, __nv_bfloat16* dst,
+                                uint32_t ldd, uint32_t dOff, uint32_t c, uint32_t M, int accumulate) {
+    const uint32_t pairs = c / 2u;
+    for (uint64_t i = gid(); i < (uint64_t)M * pairs; i += gstride()) {
+        uint32_t p = (uint32_t)(i / pairs), k = (uint32_t)(i % pairs) * 2u;
+        float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(src + (size_t)p * lds + sOff + k));
+        __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(dst + (size_t)p * ldd + dOff + k);
+        if (accumulate) {
+            float2 o = __bfloat1622float2(*d);
+            v.x += o.x;
+            v.y += o.y;
+        }
+        *d = __floats2bfloat162_rn(v.x, v.y);
+    }
+}
+
+// Network input: 16 channels per pixel from the AOV planes (RGBA32F, image
+// rows y0.., columns x0.. of a W_img-wide image; pixels outside the image are
+// zero): log(1 + beauty) (3), albedo (3), normal in [-1, 1] (3), depth / (1 +
+// depth) (1), zeros (6).
+__global__ void k_pack_input(const float4* beauty, const float4* albedo, const float4* normal, const float4* depth,
+                             uint32_t imgW, uint32_t imgH, uint32_t x0, uint32_t y0, __nv_bfloat16* out, uint32_t h,
+                             uint32_t w, uint32_t batchIndex) {
+    for (uint32_t i = gid(); i < h * w; i += gstride()) {
+        uint32_t x = i % w, y = i / w;
+        uint32_t ix = x0 + x, iy = y0 + y;
+        float v[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = 0.0f;
+        if (ix < imgW && iy < imgH) {
+            size_t s = (size_t)iy * imgW + ix;
+            float4 b = beauty[s], a = albedo[s], nm = normal[s], d = depth[s];
+            v[0] = log1pf(fmaxf(b.x, 0.0f));
+            v[1] = log1pf(fmaxf(b.y, 0.0f));
+            v[2] = log1pf(fmaxf(b.z, 0.0f));
+            v[3] = a.x;
+            v[4] = a.y;
+            v[5] = a.z;
+            v[6] = nm.x * 2.0f - 1.0f;
+            v[7] = nm.y * 2.0f - 1.0f;
+            v[8] = nm.z * 2.0f - 1.0f;
+            float dd = fmaxf(d.x, 0.0f);
+            v[9] = dd / (1.0f + dd);
+        }
+        __nv_bfloat16* o = out + ((size_t)batchIndex * h * w + i) * 16u;
+#pragma unroll
+        for (int k = 0; k < 16; k += 2)
+            *reinterpret_cast<__nv_bfloat162*>(o + k) = __floats2bfloat162_rn(v[k], v[k + 1]);
+    }
+}
+
+// L1 loss in log space against a target image (RGBA32F) and its gradient
+// (scaled by 1 / (3 * pixels)) into the prediction's first 3 channels.
+__global__ void k_l1_loss(const __nv_bfloat16* pred, uint32_t ldp, const float4* target, uint32_t M,
+                          __nv_bfloat16* grad, uint32_t ldg, float* loss) {
+    __shared__ float red[256];
+    float s = 0.0f;
+    const float scale = 1.0f / (3.0f * (float)M);
+    for (uint32_t p = gid(); p < M; p += gstride()) {
+        float4 t = target[p];
+        float tl[3] = {log1pf(fmaxf(t.x, 0.0f)), log1pf(fmaxf(t.y, 0.0f)), log1pf(fmaxf(t.z, 0.0f))};
+        float g[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float d = __bfloat162float(pred[(size_t)p * ldp + k]) - tl[k];
+            s += fabsf(d);
+            g[k] = (d > 0.0f ? scale : (d < 0.0f ? -scale : 0.0f));
+        }
+        __nv_bfloat16* gp = grad + (size_t)p * ldg;
+        gp[0] = __float2bfloat16_rn(g[0]);
+        gp[1] = __float2bfloat16_rn(g[1]);
+        gp[2] = __float2bfloat16_rn(g[2]);
+        for (uint32_t k = 3; k < ldg; ++k) gp[k] = __float2bfloat16_rn(0.0f);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (uint32_t o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, red[0] * scale);
+}
+
+// Network output (log space, first 3 channels) to an RGBA32F image; alpha from `alphaSrc`.
+__global__ void k_unpack_output(const __nv_bfloat16* pred, uint32_t ldp, uint32_t h, uint32_t w, const float4* alphaSrc,
+                                uint32_t imgW, uint32_t imgH, uint32_t x0, uint32_t y0, float4* out) {
+    for (uint32_t i = gid(); i < h * w; i += gstride()) {
+        uint32_t ix = x0 + i % w, iy = y0 + i / w;
+        if (ix >= imgW || iy >= imgH) continue;
+        size_t s = (size_t)iy * imgW + ix;
+        const __nv_bfloat16* p = pred + (size_t)i * ldp;
+        out[s] = make_float4(fmaxf(expm1f(__bfloat162float(p[0])), 0.0f), fmaxf(expm1f(__bfloat162float(p[1])), 0.0f),
+                             fmaxf(expm1f(__bfloat162float(p[2])), 0.0f), alphaSrc[s].w);
+    }
+}
+
+// Adam on FP32 master weights; writes the bf16 forward weights and, for 3x3
+// layers, the tap-flipped transposed copy the input gradient uses.
+__global__ void k_adam(float* wts, const float* grad, float* m, float* v, uint32_t count, float lr, float b1, float b2,
+                       float eps, float c1, float c2, __nv_bfloat16* wbf, __nv_bfloat16* wflip, uint32_t cout,
+                       uint32_t cin) {
+    for (uint32_t i = gid(); i < count; i += gstride()) {
+        float g = grad[i];
+        float mi = b1 * m[i] + (1.0f - b1) * g;
+        float vi = b2 * v[i] + (1.0f - b2) * g * g;
+        m[i] = mi;
+        v[i] = vi;
+        float wv = wts[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        wts[i] = wv;
+        if (wbf) wbf[i] = __float2bfloat16_rn(wv);
+        if (wflip) {
+            uint32_t ci = i % cin, tap = (i / cin) % 9u, co = i / (9u * cin);
+            wflip[((size_t)ci * 9u + (8u - tap)) * cout + co] = __float2bfloat16_rn(wv);
+        }
+    }
+}
+
+__global__ void k_weights_to_bf16(const float* wts, uint32_t count, __nv_bfloat16* wbf, __nv_bfloat16* wflip,
+                                  uint32_t cout, uint32_t cin) {
+    for (uint32_t i = gid(); i < count; i += gstride()) {
+        float wv = wts[i];
+        wbf[i] = __float2bfloat16_rn(wv);
+        if (wflip) {
+            uint32_t ci = i % cin, tap = (i / cin) % 9u, co = i / (9u * cin);
+            wflip[((size_t)ci * 9u + (8u - tap)) * cout + co] = __float2bfloat16_rn(wv);
+        }
+    }
+}
+
+inline int gridFor(uint64_t work, int block = 256) {
+    if (deviceProp().multiProcessorCount == 0) ensureDevice();
+    uint64_t g = (work + block - 1) / block;
+    uint64_t cap = (uint64_t)deviceProp().multiProcessorCount * 16u;
+    return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+inline bool aligned16(uint32_t v) { return v % 16u == 0u; }
+
+}  // namespace
+}  // namespace dk
+
+using bf16 = __nv_bfloat16;
+
+extern "C" {
+
+int dk_unet_conv3x3(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, uint32_t ldi,
+                    const void* weight, const float* bias, uint32_t cout, void* out, uint32_t ldo, uint32_t coOff,
+                    int act, int accumulate, void* stream) {
+    if (!in || !weight || !out) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_conv3x3: null argument");
+    if (!dk::aligned16(cin) || !dk::aligned16(cout) || ldi < cin || ldo < coOff + cout || ldi % 8u || ldo % 2u ||
+        coOff % 2u)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT,
+                        "dk_unet_conv3x3: channel counts must be multiples of 16 within their leading dimensions");
+    uint64_t M = (uint64_t)n * h * w;
+    if (M == 0) return DK_OK;
+    if (M >= (1ull << 31)) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_conv3x3: tensor too large");
+    dk::ConvArgs a{static_cast<const bf16*>(in), static_cast<const bf16*>(weight), bias, static_cast<bf16*>(out),
+                   n, h, w, cin, ldi, cout, ldo, coOff, (uint32_t)M, act, accumulate};
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    dim3 grid((uint32_t)((M + dk::kBM - 1) / dk::kBM), 1);
+    if (cout % 64u == 0) {
+        grid.y = cout / 64u;
+        dk::k_conv3x3_fwd<64><<<grid, 128, 0, st>>>(a);
+    } else if (cout % 32u == 0) {
+        grid.y = cout / 32u;
+        dk::k_conv3x3_fwd<32><<<grid, 128, 0, st>>>(a);
+    } else {
+        grid.y = cout / 16u;
+        dk::k_conv3x3_fwd<16><<<grid, 128, 0, st>>>(a);
+    }
+    DK_CUDA(cudaGetLastError(), "conv3x3 launch");
+    return DK_OK;
+}
+
+int dk_unet_conv3x3_wgrad(const void* in, uint32_t ldi, const void* dout, uint32_t ldd, uint32_t n, uint32_t h,
+                          uint32_t w, uint32_t cin, uint32_t cout, float* dweight, void* stream) {
+    if (!in || !dout || !dweight) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_conv3x3_wgrad: null argument");
+    if (!dk::aligned16(cin) || !dk::aligned16(cout) || ldi < cin || ldd < cout || ldi % 8u || ldd % 8u)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_conv3x3_wgrad: channel counts must be multiples of 16");
+    uint64_t M = (uint64_t)n * h * w;
+    if (M == 0) return DK_OK;
+    if (M >= (1ull << 31)) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_conv3x3_wgrad: tensor too large");
+    uint32_t tiles = ((cout + 63u) / 64u) * ((cin + 63u) / 64u);
+    // Enough pixel chunks to fill the GPU several times over, 32-pixel aligned.
+    if (dk::deviceProp().multiProcessorCount == 0) dk::ensureDevice();
+    uint64_t target = (uint64_t)dk::deviceProp().multiProcessorCount * 8u;
+    uint64_t perTile = (target + 9u * tiles - 1) / (9u * tiles);
+    uint64_t chunk = (M + perTile - 1) / perTile;
+    chunk = ((chunk + 31u) / 32u) * 32u;
+    if (chunk < 256u) chunk = 256u;
+    dk::WgradArgs a{static_cast<const bf16*>(in), static_cast<const bf16*>(dout), dweight, n, h, w, cin, ldi, cout,
+                    ldd, (uint32_t)M, (uint32_t)chunk};
+    dim3 grid((uint32_t)((M + chunk - 1) / chunk), tiles, 9);
+    dk::k_conv3x3_wgrad<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    DK_CUDA(cudaGetLastError(), "conv3x3 wgrad launch");
+    return DK_OK;
+}
+
+int dk_unet_relu_backward(const void* out, uint32_t ldo, const void* dout, uint32_t ldd, void* dpre, uint32_t ldp,
+                          uint32_t c, uint32_t pixels, void* stream) {
+    if (!out || !dout || !dpre || c % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_relu_backward");
+    dk::k_relu_backward<<<dk::gridFor((uint64_t)pixels * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(out), ldo, static_cast<const bf16*>(dout), ldd, static_cast<bf16*>(dpre), ldp, c,
+        pixels);
+    DK_CUDA(cudaGetLastError(), "relu backward launch");
+    return DK_OK;
+}
+
+int dk_unet_bias_grad(const void* dpre, uint32_t ld, uint32_t c, uint32_t pixels, float* dbias, void* stream) {
+    if (!dpre || !dbias || c == 0 || c > 256u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_bias_grad");
+    uint32_t lanes = 256u / c;
+    uint64_t blocks = ((uint64_t)pixels + lanes * 64u - 1) / (lanes * 64u);
+    int grid = (int)(blocks < 1 ? 1 : (blocks > 1024 ? 1024 : blocks));
+    dk::k_bias_grad<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(dpre), ld, c, pixels,
+                                                                          dbias);
+    DK_CUDA(cudaGetLastError(), "bias grad launch");
+    return DK_OK;
+}
+
+int dk_unet_avgpool2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint32_t coOff, uint32_t c, uint32_t n,
+                     uint32_t h, uint32_t w, void* stream) {
+    if (!in || !out || c % 2u || h % 2u || w % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_avgpool2");
+    dk::k_avgpool2<<<dk::gridFor((uint64_t)n * h * w / 4 * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c, n, h, w);
+    DK_CUDA(cudaGetLastError(), "avgpool launch");
+    return DK_OK;
+}
+
+int dk_unet_avgpool2_backward(const void* dout, uint32_t ldd, void* din, uint32_t ldi, uint32_t c, uint32_t n,
+                              uint32_t h, uint32_t w, int accumulate, void* stream) {
+    if (!dout || !din || c % 2u || h % 2u || w % 2u)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_avgpool2_backward");
+    dk::k_avgpool2_backward<<<dk::gridFor((uint64_t)n * h * w * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(dout), ldd, static_cast<bf16*>(din), ldi, c, n, h, w, accumulate);
+    DK_CUDA(cudaGetLastError(), "avgpool backward launch");
+    return DK_OK;
+}
+
+int dk_unet_upsample2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint32_t coOff, uint32_t c, uint32_t n,
+                      uint32_t h, uint32_t w, void* stream) {
+    if (!in || !out || c % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_upsample2");
+    dk::k_upsample2<<<dk::gridFor((uint64_t)n * h * w * 4 * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c, n, h, w);
+    DK_CUDA(cudaGetLastError(), "upsample launch");
+    return DK_OK;
+}
+
+int dk_unet_upsample2_backward(const void* dout, uint32_t ldd, uint32_t ciOff, void* din, uint32_t ldi, uint32_t c,
+                               uint32_t n, uint32_t h, uint32_t w, void* stream) {
+    if (!dout || !din || c % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_upsample2_backward");
+    dk::k_upsample2_backward<<<dk::gridFor((uint64_t)n * h * w * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(dout), ldd, ciOff, static_cast<bf16*>(din), ldi, c, n, h, w);
+    DK_CUDA(cudaGetLastError(), "upsample backward launch");
+    return DK_OK;
+}
+
+int dk_unet_copy_channels(const void* src, uint32_t lds, uint32_t sOff, void* dst, uint32_t ldd, uint32_t dOff,
+                          uint32_t c, uint32_t pixels, int accumulate, void* stream) {
+    if (!src || !dst || c % 2u || sOff % 2u || dOff % 2u)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_copy_channels");
+    dk::k_copy_channels<<<dk::gridFor((uint64_t)pixels * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(src), lds, sOff, static_cast<bf16*>(dst), ldd, dOff, c, pixels, accumulate);
+    DK_CUDA(cudaGetLastError(), "copy channels launch");
+    return DK_OK;
+}
+
+int dk_unet_pack_input(const float* beauty, const float* albedo, const float* normal, const float* depth,
+                       uint32_t imgW, uint32_t imgH, uint32_t x0, uint32_t y0, void* out, uint32_t h, uint32_t w,
+                       uint32_t batchIndex, void* stream) {
+    if (!beauty || !albedo || !normal || !depth || !out) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_pack_input");
+    dk::k_pack_input<<<dk::gridFor((uint64_t)h * w), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<const float4*>(beauty), reinterpret_cast<const float4*>(albedo),
+        reinterpret_cast<const float4*>(normal), reinterpret_cast<const float4*>(depth), imgW, imgH, x0, y0,
+        static_cast<bf16*>(out), h, w, batchIndex);
+    DK_CUDA(cudaGetLastError(), "pack input launch");
+    return DK_OK;
+}
+
+int dk_unet_l1_loss(const void* pred, uint32_t ldp, const float* target, uint32_t pixels, void* grad, uint32_t ldg,
+                    float* loss, void* stream) {
+    if (!pred || !target || !grad || !loss || ldp < 3u || ldg < 3u)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_l1_loss");
+    dk::k_l1_loss<<<dk::gridFor(pixels), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(pred), ldp, reinterpret_cast<const float4*>(target), pixels, static_cast<bf16*>(grad),
+        ldg, loss);
+    DK_CUDA(cudaGetLastError(), "loss launch");
+    return DK_OK;
+}
+
+int dk_unet_unpack_output(const void* pred, uint32_t ldp, uint32_t h, uint32_t w, const float* alphaSrc, uint32_t imgW,
+                          uint32_t imgH, uint32_t x0, uint32_t y0, float* out, void* stream) {
+    if (!pred || !alphaSrc || !out) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_unpack_output");
+    dk::k_unpack_output<<<dk::gridFor((uint64_t)h * w), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(pred), ldp, h, w, reinterpret_cast<const float4*>(alphaSrc), imgW, imgH, x0, y0,
+        reinterpret_cast<float4*>(out));
+    DK_CUDA(cudaGetLastError(), "unpack output launch");
+    return DK_OK;
+}
+
+int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t count, float lr, float beta1,
+                 float beta2, float eps, uint32_t step, void* wbf16, void* wflip, uint32_t cout, uint32_t cin,
+                 void* stream) {
+    if (!weights || !grad || !m || !v || step == 0) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_adam");
+    float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+    dk::k_adam<<<dk::gridFor(count), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        weights, grad, m, v, count, lr, beta1, beta2, eps, c1, c2, static_cast<bf16*>(wbf16), static_cast<bf16*>(wflip),
+        cout, cin);
+    DK_CUDA(cudaGetLastError(), "adam launch");
+    return DK_OK;
+}
+
+int dk_unet_weights_to_bf16(const float* weights, uint32_t count, void* wbf16, void* wflip, uint32_t cout, uint32_t cin,
+                            void* stream) {
+    if (!weights || !wbf16) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_weights_to_bf16");
+    dk::k_weights_to_bf16<<<dk::gridFor(count), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        weights, count, static_cast<bf16*>(wbf16), static_cast<bf16*>(wflip), cout, cin);
+    DK_CUDA(cudaGetLastError(), "weights launch");
+    return DK_OK;
+}
+
+}  // extern "C"

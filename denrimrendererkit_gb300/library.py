@@ -72,6 +72,18 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_sparse_volume_view": (i32, [P, C.POINTER(abi.Scene)]),
             "dk_sparse_volume_destroy": (i32, [P]),
             "dk_version": (C.c_char_p, []),
+            "dk_server_create": (i32, [C.POINTER(abi.Scene), C.POINTER(abi.ServerConfig), C.POINTER(P)]),
+            "dk_server_submit": (i32, [P, C.POINTER(abi.JobDesc), C.POINTER(C.c_uint64)]),
+            "dk_server_step": (i32, [P, C.POINTER(u32)]),
+            "dk_server_start": (i32, [P]),
+            "dk_server_stop": (i32, [P]),
+            "dk_server_wait": (i32, [P, C.c_uint64, u32]),
+            "dk_server_job_status": (i32, [P, C.c_uint64, C.POINTER(abi.JobStatus)]),
+            "dk_server_read_output": (i32, [P, C.c_uint64, i32, P, sz]),
+            "dk_server_release": (i32, [P, C.c_uint64]),
+            "dk_server_get_stats": (i32, [P, C.POINTER(abi.ServerStats)]),
+            "dk_server_destroy": (i32, [P]),
+            "dk_denoise_spatial": (i32, [P, P, P, P, P, P, u32, u32, C.POINTER(abi.SpatialDenoiseSettings), P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

@@ -235,6 +235,53 @@ def material_zoo(width: int = 96, height: int = 64, samples: int = 8, seed: int 
     return Workload(f"material-zoo-{width}x{height}-{samples}spp", scene, settings, samples)
 
 
+def material_preview(hdri=None, subdivisions: int = 4) -> RenderScene:
+    """The material-preview scene of the serving workload: a subdivision-4
+    icosphere (5,120 triangles, r = 0.5) resting on a 2-triangle ground plane
+    under the large configuration's HDRI.  Material 0 is the ground, material 1
+    the sphere (the one a job replaces)."""
+    env = Environment(texture=hdri if hdri is not None else synthetic_hdri(), intensity=1.0, rotation_y=0.0,
+                      max_radiance=0.0)
+    scene = RenderScene(camera=Camera((0.0, 0.75, 2.6), (0.0, 0.45, 0.0), vertical_field_of_view_degrees=35.0),
+                        environment=env)
+    ground = scene.add_material(Material(base_color=(0.5, 0.5, 0.48), roughness=0.85, specular=0.2))
+    sphere = scene.add_material(Material(**MATTE_CLAY))
+    scene.add(Mesh.quad((-4, 0, 4), (4, 0, 4), (4, 0, -4), (-4, 0, -4)), ground)
+    scene.add(icosphere(subdivisions, 0.5), sphere, Transform.translation((0.0, 0.5, 0.0)))
+    return scene
+
+
+@dataclasses.dataclass
+class PreviewJob:
+    arrival_s: float
+    width: int
+    height: int
+    samples: int
+    family: str
+    preset: str
+
+
+def serving_jobs(count: int = 4096, rate_per_s: float = 200.0, seed: int = 3):
+    """The serving workload: `count` material-preview jobs with Poisson
+    arrivals (rate 200/s), square resolutions {96: 50%, 256: 30%, 512: 15%,
+    1024: 5%}, samples uniform over {16, 64, 256}, a preset family uniform over
+    diffuse / plastic / sheen / subsurface / metal / clearcoat / thin-film and a
+    preset uniform within the family."""
+    from .presets import FAMILIES
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=count))
+    sizes = rng.choice([96, 256, 512, 1024], size=count, p=[0.5, 0.3, 0.15, 0.05])
+    spp = rng.choice([16, 64, 256], size=count)
+    fams = list(FAMILIES)
+    jobs = []
+    for i in range(count):
+        fam = fams[int(rng.integers(0, len(fams)))]
+        names = FAMILIES[fam]
+        preset = names[int(rng.integers(0, len(names)))]
+        jobs.append(PreviewJob(float(arrivals[i]), int(sizes[i]), int(sizes[i]), int(spp[i]), fam, preset))
+    return jobs
+
+
 def cornell_box_reference(width: int = 24, height: int = 24) -> Workload:
     """RenderScene.cornellBox() (Scene/RenderScene.swift:324-380)."""
     scene = RenderScene(camera=Camera((0, 1, 3.4), (0, 1, 0), vertical_field_of_view_degrees=42.0))

@@ -379,6 +379,107 @@ int dk_build_environment_samples_noalloc(const dk_float4* device_pixels, uint32_
 /* Library version string. */
 const char* dk_version(void);
 
+/* ------------------------------------------------------------------------- */
+/* Denoising.                                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* DenoiseSettings for the simple spatial denoiser
+ * (Sources/DenrimRendererKit/Denoising/Denoiser.swift:20-77). */
+typedef struct dk_spatial_denoise_settings {
+    uint32_t radius;        /* clamped to 1..2 */
+    float normal_sigma;
+    float depth_sigma;
+    float albedo_sigma;
+    float color_sigma;
+    uint32_t iterations;    /* a-trous passes, clamped to 1..5; step width 1 << pass */
+} dk_spatial_denoise_settings;
+
+/* Replaces SimpleSpatialDenoiser.encode (Denoiser.swift:103-160) running
+ * simpleSpatialDenoiseKernel (Denoise.metal:39-115).  All image pointers are
+ * DEVICE RGBA32F planes of width*height texels (beauty, depth, encoded normal,
+ * albedo AOVs as dk_session_read_output lays them out); `scratch` holds two
+ * planes (may be null for one pass); `stream` is a cudaStream_t or null.
+ * Asynchronous on `stream`. */
+int dk_denoise_spatial(const float* beauty, const float* depth, const float* normal, const float* albedo,
+                       float* out, float* scratch, uint32_t width, uint32_t height,
+                       const dk_spatial_denoise_settings* settings, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Serving: a persistent request loop over one resident scene.                */
+/* No counterpart in the reference: its RenderSession (RenderSession.swift)  */
+/* renders one scene per session, one dispatch per sample.  A server keeps   */
+/* the scene (triangles, BVH, textures, HDRI table) resident and renders     */
+/* jobs -- each with its own settings, camera, sample count and material     */
+/* table over the shared geometry -- by packing the paths of every admitted  */
+/* job into one shared wavefront per wave.  Jobs are admitted first-in       */
+/* first-out while their accumulation buffers fit the HBM budget; a job      */
+/* admitted while others run joins the next wave.  A job's result equals the */
+/* result of a session over the same scene with the job's materials and     */
+/* settings, bit for bit.                                                    */
+/* ------------------------------------------------------------------------- */
+typedef struct dk_server dk_server;
+
+typedef struct dk_server_config {
+    uint64_t hbm_budget_bytes;     /* admission budget for per-job buffers; 0: 64 GiB            */
+    uint32_t wave_paths;           /* path capacity of the shared wave; 0: 2^24                  */
+    uint32_t max_jobs_per_wave;    /* 0: 512                                                     */
+    uint32_t max_resident_jobs;    /* admitted and not yet released; 0: 4096                     */
+    uint32_t samples_per_wave;     /* samples one job advances per wave at most; 0: 64           */
+    uint32_t reserved[2];
+} dk_server_config;
+
+/* One render request.  `materials` replaces the scene's material table for
+ * this job (same count); it may change any material's parameters except
+ * emission (the light list is the scene's) and, for material IDs from 32 up,
+ * whether the material blocks shadow rays. */
+typedef struct dk_job_desc {
+    dk_settings settings;
+    uint32_t samples;
+    uint32_t material_count;
+    const dk_material* materials;
+} dk_job_desc;
+
+enum { DK_JOB_QUEUED = 0, DK_JOB_RUNNING = 1, DK_JOB_DONE = 2, DK_JOB_RELEASED = 3 };
+
+typedef struct dk_job_status {
+    uint64_t job_id;
+    uint32_t state;                /* DK_JOB_*                                                   */
+    uint32_t samples_done;
+    uint32_t samples;
+    uint32_t waves;                /* waves the job took part in                                 */
+    double submit_ms;              /* server clock (ms since dk_server_create)                   */
+    double admit_ms;
+    double finish_ms;
+} dk_job_status;
+
+typedef struct dk_server_stats {
+    uint64_t jobs_submitted, jobs_done, jobs_queued, jobs_running;
+    uint64_t waves, paths_traced, kernel_launches;
+    uint64_t budget_used_bytes, budget_peak_bytes, device_bytes;
+    double busy_ms;                /* device time of all waves                                   */
+    double max_jobs_in_wave, mean_jobs_in_wave;
+} dk_server_stats;
+
+/* Uploads `scene` once and prepares the shared wave. */
+int dk_server_create(const dk_scene* scene, const dk_server_config* config, dk_server** out_server);
+/* Queues a job; validation errors are returned here (DK_ERROR_INVALID_*). */
+int dk_server_submit(dk_server* server, const dk_job_desc* job, uint64_t* out_job_id);
+/* Admits queued jobs and runs one wave on the calling thread; `out_jobs` (may
+ * be null) receives the number of jobs in the wave (0: nothing to do). */
+int dk_server_step(dk_server* server, uint32_t* out_jobs);
+/* Runs waves on a background thread until dk_server_stop / destroy. */
+int dk_server_start(dk_server* server);
+int dk_server_stop(dk_server* server);
+/* Blocks until the job is done (or `timeout_ms` passes: DK_ERROR_DEVICE_TIMEOUT). */
+int dk_server_wait(dk_server* server, uint64_t job_id, uint32_t timeout_ms);
+int dk_server_job_status(dk_server* server, uint64_t job_id, dk_job_status* out_status);
+/* Reads a finished job's output (as dk_session_read_output). */
+int dk_server_read_output(dk_server* server, uint64_t job_id, int output, float* rgba, size_t pixel_count);
+/* Frees a finished job's buffers (its budget returns to admission). */
+int dk_server_release(dk_server* server, uint64_t job_id);
+int dk_server_get_stats(dk_server* server, dk_server_stats* out_stats);
+int dk_server_destroy(dk_server* server);
+
 #ifdef __cplusplus
 }
 #endif

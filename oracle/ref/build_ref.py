@@ -1,8 +1,8 @@
 """Test infrastructure: builds the reference-shader oracle.
 
 Where the reference sources are present, rewrites the reference's own
-PathTrace.metal into C++ (metal2cpp.py) under oracle/_ref/; then, wherever that
-generated file exists (it travels with the repository copy to machines without
+PathTrace.metal and Denoise.metal into C++ (metal2cpp.py) under oracle/_ref/;
+then, wherever those generated files exist (it travels with the repository copy to machines without
 the reference), compiles it with the host driver into
 oracle/_ref/libref_pathtrace.so.  Outputs go to oracle/_ref/ only.
 
@@ -16,30 +16,37 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
-REFERENCE_SHADER = os.path.join("/root/reference", "Sources", "DenrimRendererKit", "Resources", "Shaders",
-                                "PathTrace.metal")
+SHADERS = os.path.join("/root/reference", "Sources", "DenrimRendererKit", "Resources", "Shaders")
+# (reference shader, kernels kept, generated file)
+UNITS = (("PathTrace.metal", ("pathTraceKernel",), "pathtrace_ref.cpp"),
+         ("Denoise.metal", ("simpleSpatialDenoiseKernel",), "denoise_ref.cpp"))
 GENERATED = os.path.join(OUT, "pathtrace_ref.cpp")
 LIB = os.path.join(OUT, "libref_pathtrace.so")
 
 
 def build(force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    if os.path.exists(REFERENCE_SHADER):
-        sys.path.insert(0, HERE)
-        import metal2cpp
-        text = metal2cpp.convert(REFERENCE_SHADER)
-        old = open(GENERATED).read() if os.path.exists(GENERATED) else None
-        if old != text:
-            with open(GENERATED, "w") as f:
-                f.write(text)
-    if not os.path.exists(GENERATED):
-        raise FileNotFoundError("reference shader not available and no generated copy in oracle/_ref")
-    deps = [GENERATED, os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "metal_shim.hpp"),
-            os.path.join(ORACLE, "oracle_params.h")]
+    for shader, kernels, name in UNITS:
+        path = os.path.join(SHADERS, shader)
+        out = os.path.join(OUT, name)
+        if os.path.exists(path):
+            sys.path.insert(0, HERE)
+            import metal2cpp
+            text = metal2cpp.convert(path, kernels)
+            old = open(out).read() if os.path.exists(out) else None
+            if old != text:
+                with open(out, "w") as f:
+                    f.write(text)
+        if not os.path.exists(out):
+            raise FileNotFoundError(f"reference shader {shader} not available and no generated copy in oracle/_ref")
+    deps = [os.path.join(OUT, name) for _, _, name in UNITS] + [
+        os.path.join(HERE, f) for f in ("ref_driver.cpp", "ref_denoise.cpp", "metal_shim.hpp")] + [
+        os.path.join(ORACLE, "oracle_params.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     cmd = ["g++", "-O2", "-std=c++20", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-fno-fast-math",
-           "-Wno-attributes", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_driver.cpp"), "-o", LIB + ".tmp"]
+           "-Wno-attributes", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_driver.cpp"),
+           os.path.join(HERE, "ref_denoise.cpp"), "-o", LIB + ".tmp"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("reference-shader oracle build failed:\n" + res.stderr[-4000:])

@@ -1,12 +1,13 @@
-"""Test infrastructure: mechanical rewrite of the reference path tracer's Metal
-source (Sources/DenrimRendererKit/Resources/Shaders/PathTrace.metal) into C++
-that compiles against metal_shim.hpp.  The output is a build artefact written
+"""Test infrastructure: mechanical rewrite of the reference's Metal shaders
+(Sources/DenrimRendererKit/Resources/Shaders/PathTrace.metal, Denoise.metal)
+into C++ that compiles against metal_shim.hpp.  The output is a build artefact written
 only under oracle/_ref/; it is never committed and never hand-edited.
 
 The rewrite changes no arithmetic.  It:
   1. drops the Metal headers and `using namespace` lines and every function
      that needs the hardware ray-tracing API (names containing `Hardware`),
-     plus the compute kernels other than `pathTraceKernel`;
+     plus the compute kernels other than the requested ones (`pathTraceKernel`,
+     `simpleSpatialDenoiseKernel`);
   2. strips `[[...]]` attributes;
   3. turns swizzle reads `.xyz/.xy/.xz` into calls and swizzle writes
      `v.xyz = e;` into `v.set_xyz(e);`;
@@ -17,6 +18,7 @@ The rewrite changes no arithmetic.  It:
      clang-based Metal compiler evaluates left to right.  A statement whose
      draws sit behind `&&`, `||` or `?:` is refused rather than reordered.
 """
+import os
 import re
 import sys
 
@@ -68,11 +70,11 @@ def top_level_items(src: str):
     yield start, len(src), src[start:]
 
 
-def keep_item(text: str) -> bool:
+def keep_item(text: str, kernels) -> bool:
     if HARDWARE.search(text):
         return False
     m = re.search(r"\bkernel\s+void\s+(\w+)", text)
-    if m and m.group(1) != "pathTraceKernel":
+    if m and m.group(1) not in kernels:
         return False
     return True
 
@@ -176,17 +178,17 @@ def rewrite_swizzles(src: str) -> str:
     return re.sub(r"\.(xyz|xy|xz)\b(?!\s*\()", r".\1()", src)
 
 
-def convert(metal_path: str) -> str:
+def convert(metal_path: str, kernels=("pathTraceKernel",)) -> str:
     raw = open(metal_path).read()
     src = blank_comments(raw)
     src = re.sub(r"#include\s*<metal_\w+>", "", src)
     src = re.sub(r"using\s+namespace\s+(metal|raytracing)\s*;", "", src)
-    items = [t for _, _, t in top_level_items(src) if keep_item(t)]
+    items = [t for _, _, t in top_level_items(src) if keep_item(t, kernels)]
     src = "".join(items)
     src = re.sub(r"\[\[[^\]]*\]\]", "", src)
     src, hoisted = hoist_draws(src)
     src = rewrite_swizzles(src)
-    header = ("// Generated by oracle/ref/metal2cpp.py from the reference's PathTrace.metal.\n"
+    header = (f"// Generated by oracle/ref/metal2cpp.py from the reference's {os.path.basename(metal_path)}.\n"
               "// Build artefact: do not edit, do not commit.\n"
               "#include \"metal_shim.hpp\"\nnamespace mref {\n")
     notes = "".join(f"// hoisted draws: {h}\n" for h in hoisted)
@@ -195,8 +197,8 @@ def convert(metal_path: str) -> str:
 
 
 if __name__ == "__main__":
-    if len(sys.argv) != 3:
-        raise SystemExit("usage: metal2cpp.py PathTrace.metal out.cpp")
-    text = convert(sys.argv[1])
+    if len(sys.argv) < 3:
+        raise SystemExit("usage: metal2cpp.py SHADER.metal out.cpp [kernel ...]")
+    text = convert(sys.argv[1], tuple(sys.argv[3:]) or ("pathTraceKernel",))
     with open(sys.argv[2], "w") as f:
         f.write(text)
