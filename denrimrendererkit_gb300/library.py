@@ -84,6 +84,21 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_server_get_stats": (i32, [P, C.POINTER(abi.ServerStats)]),
             "dk_server_destroy": (i32, [P]),
             "dk_denoise_spatial": (i32, [P, P, P, P, P, P, u32, u32, C.POINTER(abi.SpatialDenoiseSettings), P]),
+            "dk_unet_conv3x3": (i32, [P, u32, u32, u32, u32, u32, P, P, u32, P, u32, u32, i32, i32, P]),
+            "dk_unet_conv3x3_wgrad": (i32, [P, u32, P, u32, u32, u32, u32, u32, u32, P, P]),
+            "dk_unet_relu_backward": (i32, [P, u32, P, u32, P, u32, u32, u32, P]),
+            "dk_unet_bias_grad": (i32, [P, u32, u32, u32, P, P]),
+            "dk_unet_avgpool2": (i32, [P, u32, P, u32, u32, u32, u32, u32, u32, P]),
+            "dk_unet_avgpool2_backward": (i32, [P, u32, P, u32, u32, u32, u32, u32, i32, P]),
+            "dk_unet_upsample2": (i32, [P, u32, P, u32, u32, u32, u32, u32, u32, P]),
+            "dk_unet_upsample2_backward": (i32, [P, u32, u32, P, u32, u32, u32, u32, u32, P]),
+            "dk_unet_copy_channels": (i32, [P, u32, u32, P, u32, u32, u32, u32, i32, P]),
+            "dk_unet_pack_input": (i32, [P, P, P, P, u32, u32, u32, u32, P, u32, u32, u32, P]),
+            "dk_unet_l1_loss": (i32, [P, u32, P, u32, P, u32, P, P]),
+            "dk_unet_unpack_output": (i32, [P, u32, u32, u32, P, u32, u32, u32, u32, P, P]),
+            "dk_unet_adam": (i32, [P, P, P, P, u32, C.c_float, C.c_float, C.c_float, C.c_float, u32, P, P, u32, u32,
+                                   P]),
+            "dk_unet_weights_to_bf16": (i32, [P, u32, P, P, u32, u32, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

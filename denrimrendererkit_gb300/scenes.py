@@ -63,6 +63,50 @@ def cornell_small(width: int = 320, height: int = 180, samples: int = 16) -> Wor
     return Workload("cornell-small-320x180-16spp", scene, settings, samples)
 
 
+def cornell_variant(seed: int, width: int = 256, height: int = 256, samples: int = 4) -> Workload:
+    """A reseeded variant of the small configuration, for denoiser training
+    pairs: wall colours, the ceiling light's size and power, a sphere with a
+    material drawn from the preset library (position, radius) and a box with a
+    random diffuse colour, size and rotation are drawn from `seed`."""
+    from .presets import PRESETS
+    rng = np.random.default_rng(seed)
+    cam = Camera((float(rng.uniform(-0.15, 0.15)), float(rng.uniform(0.9, 1.1)), float(rng.uniform(3.2, 3.6))),
+                 (0.0, 1.0, 0.0), vertical_field_of_view_degrees=float(rng.uniform(36.0, 44.0)))
+    scene = RenderScene(camera=cam)
+
+    def col(lo, hi):
+        return tuple(float(v) for v in rng.uniform(lo, hi, 3))
+
+    grey = scene.add_material(Material(base_color=col(0.55, 0.8), specular=0.0))
+    left = scene.add_material(Material(base_color=col(0.05, 0.8), specular=0.0))
+    right = scene.add_material(Material(base_color=col(0.05, 0.8), specular=0.0))
+    power = float(rng.uniform(0.6, 1.4))
+    light = scene.add_material(Material(base_color=(1.0, 1.0, 1.0), emission=(17.0 * power, 12.0 * power, 4.0 * power),
+                                         emission_strength=1.0))
+    names = sorted(PRESETS)
+    sphere = scene.add_material(PRESETS[names[int(rng.integers(0, len(names)))]])
+    box = scene.add_material(Material(base_color=col(0.1, 0.9), roughness=float(rng.uniform(0.3, 0.9)),
+                                      specular=float(rng.uniform(0.0, 0.5))))
+    scene.add(Mesh.quad((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)), grey)
+    scene.add(Mesh.quad((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)), grey)
+    scene.add(Mesh.quad((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)), grey)
+    scene.add(Mesh.quad((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)), left)
+    scene.add(Mesh.quad((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)), right)
+    hl = float(rng.uniform(0.1, 0.3))
+    scene.add(Mesh.quad((-hl, 1.99, -hl), (hl, 1.99, -hl), (hl, 1.99, hl), (-hl, 1.99, hl)), light)
+    r = float(rng.uniform(0.2, 0.4))
+    scene.add(icosphere(3, r), sphere, Transform.translation((float(rng.uniform(-0.5, 0.1)), r,
+                                                             float(rng.uniform(-0.4, 0.4)))))
+    bh = float(rng.uniform(0.3, 1.1))
+    bw = float(rng.uniform(0.2, 0.35))
+    scene.add(Mesh.box((-bw, 0.0, -bw), (bw, bh, bw)), box,
+              Transform.translation((float(rng.uniform(0.3, 0.6)), 0.0, float(rng.uniform(-0.5, 0.2))))
+              * Transform.rotation_y(float(rng.uniform(0.0, 1.5))))
+    settings = RenderSettings(width=width, height=height, max_bounces=8, quality=RenderQuality.FINAL,
+                              frame_seed=int(rng.integers(1, 2 ** 31)))
+    return Workload(f"cornell-variant-{seed}-{width}x{height}-{samples}spp", scene, settings, samples)
+
+
 def _displaced_icosphere(rng: np.random.Generator, subdivisions: int, radius: float, amplitude: float) -> Mesh:
     base = icosphere(subdivisions, 1.0)
     v = base.vertices.astype(np.float64)

@@ -404,6 +404,63 @@ int dk_denoise_spatial(const float* beauty, const float* depth, const float* nor
                        float* out, float* scratch, uint32_t width, uint32_t height,
                        const dk_spatial_denoise_settings* settings, void* stream);
 
+/* Learned denoiser building blocks (no counterpart in the reference, whose
+ * denoisers are the spatial filter above and Apple's SVGF).  Tensors are
+ * DEVICE NHWC bf16 (raw 16-bit storage) with channel counts that are
+ * multiples of 16; `ld*` is the channel stride of a pixel (a tensor may be a
+ * channel slice of a wider buffer) and `*_off` a channel offset.  All calls
+ * are asynchronous on `stream` (a cudaStream_t or null). */
+
+/* 3x3 convolution, stride 1, zero padding 1, FP32 accumulation on the tensor
+ * cores: out[p][co_off + co] (+)= act(bias[co] + sum in[p + tap][ci] *
+ * weight[co][tap][ci]); act 0 = identity, 1 = ReLU; bias may be null.  With
+ * the tap-flipped transposed weights (dk_unet_adam / dk_unet_weights_to_bf16
+ * `wflip`) it computes the input gradient. */
+int dk_unet_conv3x3(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, uint32_t ldi,
+                    const void* weight, const float* bias, uint32_t cout, void* out, uint32_t ldo, uint32_t co_off,
+                    int act, int accumulate, void* stream);
+/* Weight gradient: dweight[co][tap][ci] += sum_p dout[p][co] * in[p + tap][ci] (FP32). */
+int dk_unet_conv3x3_wgrad(const void* in, uint32_t ldi, const void* dout, uint32_t ldd, uint32_t n, uint32_t h,
+                          uint32_t w, uint32_t cin, uint32_t cout, float* dweight, void* stream);
+/* dpre = dout where out > 0. */
+int dk_unet_relu_backward(const void* out, uint32_t ldo, const void* dout, uint32_t ldd, void* dpre, uint32_t ldp,
+                          uint32_t c, uint32_t pixels, void* stream);
+/* dbias[c] += sum_p dpre[p][c] (c <= 256). */
+int dk_unet_bias_grad(const void* dpre, uint32_t ld, uint32_t c, uint32_t pixels, float* dbias, void* stream);
+/* 2x2 average pooling of an (h, w) tensor, and its gradient. */
+int dk_unet_avgpool2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint32_t co_off, uint32_t c, uint32_t n,
+                     uint32_t h, uint32_t w, void* stream);
+int dk_unet_avgpool2_backward(const void* dout, uint32_t ldd, void* din, uint32_t ldi, uint32_t c, uint32_t n,
+                              uint32_t h, uint32_t w, int accumulate, void* stream);
+/* Nearest 2x upsampling of an (h, w) tensor, and its gradient. */
+int dk_unet_upsample2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint32_t co_off, uint32_t c, uint32_t n,
+                      uint32_t h, uint32_t w, void* stream);
+int dk_unet_upsample2_backward(const void* dout, uint32_t ldd, uint32_t ci_off, void* din, uint32_t ldi, uint32_t c,
+                               uint32_t n, uint32_t h, uint32_t w, void* stream);
+int dk_unet_copy_channels(const void* src, uint32_t lds, uint32_t s_off, void* dst, uint32_t ldd, uint32_t d_off,
+                          uint32_t c, uint32_t pixels, int accumulate, void* stream);
+/* 16-channel network input of batch item `batch_index` from an (h, w) window at
+ * (x0, y0) of the RGBA32F AOV planes: log(1 + beauty), albedo, normal in
+ * [-1, 1], depth / (1 + depth), zeros. */
+int dk_unet_pack_input(const float* beauty, const float* albedo, const float* normal, const float* depth,
+                       uint32_t image_width, uint32_t image_height, uint32_t x0, uint32_t y0, void* out, uint32_t h,
+                       uint32_t w, uint32_t batch_index, void* stream);
+/* L1 loss between the prediction's first 3 channels (log space) and
+ * log(1 + target) (RGBA32F); loss (+)= mean, grad = its gradient. */
+int dk_unet_l1_loss(const void* pred, uint32_t ldp, const float* target, uint32_t pixels, void* grad, uint32_t ldg,
+                    float* loss, void* stream);
+/* Prediction (log space) to an RGBA32F image window; alpha from alpha_src. */
+int dk_unet_unpack_output(const void* pred, uint32_t ldp, uint32_t h, uint32_t w, const float* alpha_src,
+                          uint32_t image_width, uint32_t image_height, uint32_t x0, uint32_t y0, float* out,
+                          void* stream);
+/* Adam step on FP32 master weights; refreshes the bf16 copy and (3x3 layers,
+ * wflip non-null) the tap-flipped transposed copy [cin][9][cout]. */
+int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t count, float lr, float beta1,
+                 float beta2, float eps, uint32_t step, void* wbf16, void* wflip, uint32_t cout, uint32_t cin,
+                 void* stream);
+int dk_unet_weights_to_bf16(const float* weights, uint32_t count, void* wbf16, void* wflip, uint32_t cout,
+                            uint32_t cin, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Serving: a persistent request loop over one resident scene.                */
 /* No counterpart in the reference: its RenderSession (RenderSession.swift)  */

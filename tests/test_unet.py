@@ -1,0 +1,162 @@
+"""The learned denoiser's kernels against a plain PyTorch FP32 reference on the
+CPU: convolution forward (with bias, ReLU, channel slices, accumulation), its
+input gradient (tap-flipped transposed weights) and weight gradient, and the
+full network's loss gradient w.r.t. every weight and bias.
+
+Tolerances follow from bf16 operands and activations with FP32 accumulation:
+a single convolution is compared at relative RMS error <= 1e-2 (bf16 rounding
+of the output, 2^-8), whole-network gradients at <= 6e-2."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from denrimrendererkit_gb300 import library  # noqa: E402
+from denrimrendererkit_gb300.denoiser import IN_CH, LEVELS, OUT_CH, UNet, _ptr  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_rms(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(((a - b) ** 2).mean()) / max(np.sqrt((b ** 2).mean()), 1e-30))
+
+
+def to_torch_weight(w):  # [co][9][ci] -> [co][ci][3][3]
+    co, _, ci = w.shape
+    return w.reshape(co, 3, 3, ci).permute(0, 3, 1, 2).contiguous()
+
+
+@pytest.fixture(scope="module")
+def lib(dk_lib):
+    from denrimrendererkit_gb300 import DenrimRenderer
+    DenrimRenderer(0)
+    return library.load()
+
+
+@pytest.mark.parametrize("cin,cout,act,ldi_extra,ldo_extra,co_off", [
+    (16, 32, 1, 0, 0, 0), (32, 16, 0, 16, 32, 32), (96, 96, 1, 0, 0, 0), (160, 64, 1, 32, 0, 0),
+    (288, 128, 1, 0, 64, 32)])
+def test_conv3x3_forward(lib, cin, cout, act, ldi_extra, ldo_extra, co_off):
+    g = torch.Generator().manual_seed(cin * 7 + cout)
+    n, h, w = 2, 13, 37  # not multiples of the tiles: ragged edges
+    ldi, ldo = cin + ldi_extra, cout + ldo_extra + co_off
+    x = torch.randn(n, h, w, ldi, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) / (3 * cin ** 0.5)).to(torch.bfloat16)
+    b = torch.randn(cout, generator=g) * 0.1
+    prior = torch.randn(n, h, w, ldo, generator=g).to(torch.bfloat16)
+    for accumulate in (0, 1):
+        xd, wd, bd = x.cuda(), wt.cuda(), b.cuda()
+        out = prior.clone().cuda()
+        library.check(lib.dk_unet_conv3x3(_ptr(xd), n, h, w, cin, ldi, _ptr(wd), _ptr(bd), cout, _ptr(out), ldo,
+                                          co_off, act, accumulate, None))
+        torch.cuda.synchronize()
+        got = out.cpu().float()
+        ref = torch.nn.functional.conv2d(x[..., :cin].float().permute(0, 3, 1, 2), to_torch_weight(wt.float()),
+                                         b, padding=1).permute(0, 2, 3, 1)
+        if act:
+            ref = torch.relu(ref)
+        if accumulate:
+            ref = ref + prior[..., co_off:co_off + cout].float()
+        assert rel_rms(got[..., co_off:co_off + cout], ref) <= 1e-2
+        untouched = torch.cat([got[..., :co_off], got[..., co_off + cout:]], -1)
+        expect = torch.cat([prior[..., :co_off], prior[..., co_off + cout:]], -1).float()
+        assert torch.equal(untouched, expect)
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 32), (64, 96), (160, 128), (96, 16)])
+def test_conv3x3_input_and_weight_gradients(lib, cin, cout):
+    g = torch.Generator().manual_seed(cin + 3 * cout)
+    n, h, w = 2, 16, 24
+    x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) / (3 * cin ** 0.5))
+    dy = torch.randn(n, h, w, cout, generator=g).to(torch.bfloat16)
+    # reference gradients in FP32 from bf16-rounded operands
+    xr = x.float().permute(0, 3, 1, 2).requires_grad_(True)
+    wr = to_torch_weight(wt.to(torch.bfloat16).float()).requires_grad_(True)
+    y = torch.nn.functional.conv2d(xr, wr, padding=1)
+    y.backward(dy.float().permute(0, 3, 1, 2))
+    gx_ref = xr.grad.permute(0, 2, 3, 1)
+    gw_ref = wr.grad.permute(0, 2, 3, 1).reshape(cout, 9, cin)
+    # device: flipped weights via the bf16 conversion kernel, dgrad as a forward conv
+    wd = wt.cuda().contiguous()
+    wbf = torch.empty(cout, 9, cin, dtype=torch.bfloat16, device="cuda")
+    wflip = torch.empty(cin, 9, cout, dtype=torch.bfloat16, device="cuda")
+    library.check(lib.dk_unet_weights_to_bf16(_ptr(wd), wd.numel(), _ptr(wbf), _ptr(wflip), cout, cin, None))
+    dyd, xd = dy.cuda(), x.cuda()
+    gx = torch.zeros(n, h, w, cin, dtype=torch.bfloat16, device="cuda")
+    library.check(lib.dk_unet_conv3x3(_ptr(dyd), n, h, w, cout, cout, _ptr(wflip), None, cin, _ptr(gx), cin, 0, 0, 0,
+                                      None))
+    gw = torch.zeros(cout, 9, cin, dtype=torch.float32, device="cuda")
+    library.check(lib.dk_unet_conv3x3_wgrad(_ptr(xd), cin, _ptr(dyd), cout, n, h, w, cin, cout, _ptr(gw), None))
+    gb = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    library.check(lib.dk_unet_bias_grad(_ptr(dyd), cout, cout, n * h * w, _ptr(gb), None))
+    torch.cuda.synchronize()
+    assert rel_rms(gx.cpu().float(), gx_ref) <= 1e-2
+    assert rel_rms(gw.cpu(), gw_ref) <= 1e-3  # FP32 accumulation of exact bf16 products
+    assert rel_rms(gb.cpu(), dy.float().sum(dim=(0, 1, 2))) <= 1e-4
+
+
+def torch_unet(x, weights):
+    """The same network in plain PyTorch FP32 (NCHW)."""
+    F = torch.nn.functional
+
+    def conv(name, t, act=True):
+        w, b = weights[name]
+        y = F.conv2d(t, to_torch_weight(w), b, padding=1)
+        return torch.relu(y) if act else y
+
+    skips = []
+    t = x
+    for k in range(4):
+        t = conv(f"enc{k}b", conv(f"enc{k}a", t))
+        skips.append(t)
+        t = F.avg_pool2d(t, 2)
+    t = conv("botb", conv("bota", t))
+    for k in (3, 2, 1, 0):
+        t = F.interpolate(t, scale_factor=2, mode="nearest")
+        t = torch.cat([t, skips[k]], 1)
+        t = conv(f"dec{k}b", conv(f"dec{k}a", t))
+    return conv("out", t, act=False)
+
+
+def test_network_gradients_match_fp32_reference(lib):
+    n, h, w = 2, 32, 48
+    net = UNet(seed=3)
+    g = torch.Generator().manual_seed(11)
+    # biases non-zero so their gradients and the ReLU masks are exercised
+    state = {}
+    for l in net.layers:
+        wv, _ = net.state()[l.name]
+        state[l.name] = (wv, (torch.randn(l.cout, generator=g) * 0.05).numpy())
+    net.load_state(state)
+    x = torch.randn(n, h, w, IN_CH, generator=g).to(torch.bfloat16)
+    target = torch.rand(n * h * w, 4, generator=g) * 2.0
+    B = net.grad_buffers(n, h, w)
+    B["x"].copy_(x.cuda())
+    net.zero_grad()
+    B["loss"].zero_()
+    net.forward(n, h, w)
+    net.loss(target.cuda().contiguous(), n, h, w)
+    net.backward(n, h, w)
+    torch.cuda.synchronize()
+    # FP32 reference on the CPU, same (bf16-rounded) weights
+    wts = {}
+    for l in net.layers:
+        wr = l.wbf.cpu().float().requires_grad_(True)
+        br = l.b.cpu().clone().requires_grad_(True)
+        wts[l.name] = (wr, br)
+    pred = torch_unet(x.float().permute(0, 3, 1, 2), wts)
+    tl = torch.log1p(target[:, :3].reshape(n, h, w, 3).permute(0, 3, 1, 2))
+    loss = (pred[:, :3] - tl).abs().mean()
+    loss.backward()
+    assert abs(B["loss"].item() - loss.item()) <= 2e-2 * loss.item()
+    got_pred = B["pred"].cpu().float()[..., :3].permute(0, 3, 1, 2)
+    assert rel_rms(got_pred, pred[:, :3].detach()) <= 3e-2
+    for l in net.layers:
+        wr, br = wts[l.name]
+        ew = rel_rms(l.gw.cpu(), wr.grad)
+        eb = rel_rms(l.gb.cpu(), br.grad)
+        assert ew <= 6e-2, (l.name, ew)
+        assert eb <= 6e-2, (l.name, eb)
