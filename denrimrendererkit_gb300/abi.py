@@ -172,6 +172,7 @@ EXPORTED_SYMBOLS = (
     "dk_unet_conv3x3", "dk_unet_conv3x3_wgrad", "dk_unet_relu_backward", "dk_unet_bias_grad", "dk_unet_avgpool2",
     "dk_unet_avgpool2_backward", "dk_unet_upsample2", "dk_unet_upsample2_backward", "dk_unet_copy_channels",
     "dk_unet_pack_input", "dk_unet_l1_loss", "dk_unet_unpack_output", "dk_unet_adam", "dk_unet_weights_to_bf16",
+    "dk_unet_set_conv_path", "dk_unet_error",
 )
 
 

@@ -188,6 +188,193 @@ __global__ void __launch_bounds__(128) k_conv3x3_fwd(ConvArgs a) {
     }
 }
 
+// ------------------------------------------------- tcgen05 forward ----
+// The same convolution on the 5th-generation tensor cores: one CTA computes
+// 128 output pixels x all Cout (one tcgen05.mma of M = 128, N = Cout, K = 16
+// per 16 input channels of a tap), accumulating in tensor memory.  Operand
+// tiles are K-major with the 128-byte swizzle: 64 channels (128 bytes) per
+// row, 8-row atoms of 1024 bytes; cp.async fills them (zero fill for the
+// padding), one thread issues the MMAs and commits each stage to an
+// mbarrier that the copies of the stage's next use wait on.  Every wait is
+// bounded: on timeout the kernel records an error, waits (bounded) for its
+// MMAs, frees its tensor memory and returns.
+constexpr int kTcStages = 4;
+constexpr uint32_t kTcRows = 128;
+
+__device__ int g_unetError;
+
+__device__ __forceinline__ uint64_t umaDesc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4)  // start address
+           | ((uint64_t)1 << 16)                // leading byte offset (unused for swizzled K-major)
+           | ((uint64_t)(1024u >> 4) << 32)     // stride byte offset: 8 rows x 128 B
+           | ((uint64_t)1 << 46)                // descriptor version
+           | ((uint64_t)2 << 61);               // 128-byte swizzle
+}
+
+__device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
+    const long long start = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - start > 4000000000ll) return false;  // about 2 s
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) k_conv3x3_tc(ConvArgs a, uint32_t tmemCols) {
+    extern __shared__ unsigned char dsm[];
+    const uint32_t raw = smemAddr(dsm);
+    unsigned char* sm = dsm + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t N = a.cout;
+    const uint32_t aBytes = kTcRows * 128u, bBytes = N * 128u;
+    unsigned char* sA = sm;
+    unsigned char* sB = sm + kTcStages * aBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kTcStages * bBytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kTcStages);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(tslot)),
+                     "r"(tmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kTcStages; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smemAddr(&bars[s])));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *tslot;
+
+    const uint32_t m0 = blockIdx.x * kTcRows;
+    const uint32_t HW = a.h * a.w_;
+    const uint32_t m = m0 + tid;
+    const bool rowValid = m < a.M;
+    const uint32_t img = rowValid ? m / HW : 0u, rem = rowValid ? m - img * HW : 0u;
+    const int py = (int)(rem / a.w_), px = (int)(rem - (rem / a.w_) * a.w_);
+    const uint32_t chunks = (a.cin + 63u) / 64u;
+    const uint32_t kIters = 9u * chunks;
+    // kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, N, M = 128.
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((kTcRows >> 4) << 24);
+
+    auto loadStage = [&](uint32_t it, uint32_t stage) {
+        uint32_t tap = it / chunks, c0 = (it - tap * chunks) * 64u;
+        int yy = py + (int)(tap / 3u) - 1, xx = px + (int)(tap % 3u) - 1;
+        bool inb = rowValid && yy >= 0 && yy < (int)a.h && xx >= 0 && xx < (int)a.w_;
+        const __nv_bfloat16* src =
+            inb ? a.in + ((size_t)(img * a.h + (uint32_t)yy) * a.w_ + (uint32_t)xx) * a.ldi + c0 : a.in;
+        unsigned char* rowA = sA + stage * aBytes + tid * 128u;
+#pragma unroll
+        for (uint32_t j = 0; j < 8; ++j) {
+            bool v = inb && c0 + j * 8u < a.cin;
+            cpAsync16(rowA + ((j ^ (tid & 7u)) << 4), v ? src + j * 8u : a.in, v ? 16u : 0u);
+        }
+        unsigned char* tileB = sB + stage * bBytes;
+        for (uint32_t i = tid; i < N * 8u; i += 128u) {
+            uint32_t row = i >> 3, j = i & 7u;
+            bool v = c0 + j * 8u < a.cin;
+            const __nv_bfloat16* wsrc = a.w + ((size_t)row * 9u + tap) * a.cin + c0 + j * 8u;
+            cpAsync16(tileB + row * 128u + ((j ^ (row & 7u)) << 4), v ? wsrc : a.w, v ? 16u : 0u);
+        }
+    };
+
+    bool failed = false;
+    uint32_t lastCommitted = 0xffffffffu;
+#pragma unroll
+    for (int s = 0; s < kTcStages - 1; ++s) {
+        if ((uint32_t)s < kIters) loadStage((uint32_t)s, (uint32_t)s);
+        cpAsyncCommit();
+    }
+    for (uint32_t it = 0; it < kIters && !failed; ++it) {
+        const uint32_t stage = it % kTcStages;
+        cpAsyncWait<kTcStages - 2>();
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t c0 = (it % chunks) * 64u;
+            const uint32_t aBase = smemAddr(sA + stage * aBytes), bBase = smemAddr(sB + stage * bBytes);
+#pragma unroll
+            for (uint32_t ks = 0; ks < 4; ++ks) {
+                if (c0 + ks * 16u >= a.cin) break;
+                uint64_t ad = umaDesc(aBase + ks * 32u), bd = umaDesc(bBase + ks * 32u);
+                uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smemAddr(&bars[stage]))
+                         : "memory");
+        }
+        lastCommitted = it;
+        const uint32_t nxt = it + kTcStages - 1;
+        if (nxt < kIters) {
+            const uint32_t ps = nxt % kTcStages;
+            if (nxt >= (uint32_t)kTcStages) {  // the buffer's previous MMAs (iteration nxt - stages) must be done
+                uint32_t use = (nxt - kTcStages) / kTcStages;
+                if (!mbarWait(smemAddr(&bars[ps]), use & 1u)) failed = true;
+            }
+            if (!failed) loadStage(nxt, ps);
+        }
+        cpAsyncCommit();
+    }
+    cpAsyncWait<0>();
+    bool done = false;
+    if (lastCommitted != 0xffffffffu)
+        done = mbarWait(smemAddr(&bars[lastCommitted % kTcStages]), (lastCommitted / kTcStages) & 1u);
+    if (!done || failed) {
+        if (tid == 0) atomicExch(&g_unetError, 1);
+    } else {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t row = warp * 32u + lane;
+        const uint32_t pix = m0 + row;
+        __nv_bfloat16* orow = a.out + (size_t)pix * a.ldo + a.coOff;
+        for (uint32_t c0 = 0; c0 < N; c0 += 16u) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(taddr + ((warp * 32u) << 16) + c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (pix >= a.M) continue;
+#pragma unroll
+            for (uint32_t k = 0; k < 16; k += 2) {
+                float v0 = __uint_as_float(r[k]), v1 = __uint_as_float(r[k + 1]);
+                uint32_t col = c0 + k;
+                if (a.bias) {
+                    v0 += a.bias[col];
+                    v1 += a.bias[col + 1];
+                }
+                if (a.act == 1) {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                }
+                __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(orow + col);
+                if (a.accumulate) {
+                    float2 o = __bfloat1622float2(*dst);
+                    v0 += o.x;
+                    v1 += o.y;
+                }
+                *dst = __floats2bfloat162_rn(v0, v1);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(tmemCols));
+}
+
+size_t tcSmemBytes(uint32_t cout) { return (size_t)kTcStages * (kTcRows * 128u + cout * 128u) + 1024u + 64u; }
+
 // -------------------------------------------------------------- wgrad ----
 struct WgradArgs {
     const __nv_bfloat16* in;    // [M][ldi], channels [0, cin)
@@ -548,6 +735,9 @@ inline int gridFor(uint64_t work, int block = 256) {
 
 inline bool aligned16(uint32_t v) { return v % 16u == 0u; }
 
+// 1: tcgen05 forward convolution (default), 0: the mma.sync kernel.
+int g_convPath = 1;
+
 }  // namespace
 }  // namespace dk
 
@@ -569,6 +759,20 @@ int dk_unet_conv3x3(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t
     dk::ConvArgs a{static_cast<const bf16*>(in), static_cast<const bf16*>(weight), bias, static_cast<bf16*>(out),
                    n, h, w, cin, ldi, cout, ldo, coOff, (uint32_t)M, act, accumulate};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dk::g_convPath == 1 && cout <= 256u) {
+        uint32_t cols = 32u;
+        while (cols < cout) cols <<= 1;
+        size_t smem = dk::tcSmemBytes(cout);
+        static size_t configured = 0;
+        if (smem > configured) {
+            DK_CUDA(cudaFuncSetAttribute(dk::k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "conv3x3 shared memory");
+            configured = smem;
+        }
+        dk::k_conv3x3_tc<<<(uint32_t)((M + dk::kTcRows - 1) / dk::kTcRows), 128, smem, st>>>(a, cols);
+        DK_CUDA(cudaGetLastError(), "conv3x3 (tcgen05) launch");
+        return DK_OK;
+    }
     dim3 grid((uint32_t)((M + dk::kBM - 1) / dk::kBM), 1);
     if (cout % 64u == 0) {
         grid.y = cout / 64u;
@@ -718,6 +922,20 @@ int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t
         weights, grad, m, v, count, lr, beta1, beta2, eps, c1, c2, static_cast<bf16*>(wbf16), static_cast<bf16*>(wflip),
         cout, cin);
     DK_CUDA(cudaGetLastError(), "adam launch");
+    return DK_OK;
+}
+
+int dk_unet_set_conv_path(int path) {
+    if (path != 0 && path != 1) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_set_conv_path: 0 or 1");
+    dk::g_convPath = path;
+    return DK_OK;
+}
+
+int dk_unet_error(int* out) {
+    if (!out) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_error: null argument");
+    int zero = 0;
+    DK_CUDA(cudaMemcpyFromSymbol(out, dk::g_unetError, sizeof(int)), "read denoiser error flag");
+    DK_CUDA(cudaMemcpyToSymbol(dk::g_unetError, &zero, sizeof(int)), "clear denoiser error flag");
     return DK_OK;
 }
 

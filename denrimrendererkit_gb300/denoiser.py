@@ -418,8 +418,28 @@ def train(net: UNet, data: TrainingSet, steps: int, batch: int = 16, lr: float =
 
 
 def relative_rmse(image, reference) -> float:
-    """sqrt(mean((image - reference)^2)) / mean(reference) over RGB."""
+    """sqrt(mean((image - reference)^2)) / mean(reference) over linear RGB."""
     torch = _torch()
     a = image[..., :3].double()
     b = reference[..., :3].double()
+    return float(torch.sqrt(((a - b) ** 2).mean()) / b.mean())
+
+
+def display(image):
+    """The reference's PNG tone curve before 8-bit quantisation
+    (PNGWriter.tonemap, Sources/DenrimRendererKit/Image/PNGWriter.swift:182-188):
+    exposure 0.8, the ACES fit x (2.51 x + 0.03) / (x (2.43 x + 0.59) + 0.14),
+    clamp to [0, 1], gamma 1 / 2.2."""
+    torch = _torch()
+    x = image[..., :3].double().clamp(min=0.0) * 0.8
+    mapped = (x * (2.51 * x + 0.03)) / (x * (2.43 * x + 0.59) + 0.14)
+    return torch.pow(mapped.clamp(0.0, 1.0), 1.0 / 2.2)
+
+
+def display_relative_rmse(image, reference) -> float:
+    """Relative RMSE of the displayed images: sqrt(mean((d(x) - d(t))^2)) /
+    mean(d(t)) with d the reference's PNG tone curve.  The error measure of
+    the denoisers: in the linear domain it is dominated by a few fireflies."""
+    torch = _torch()
+    a, b = display(image), display(reference)
     return float(torch.sqrt(((a - b) ** 2).mean()) / b.mean())

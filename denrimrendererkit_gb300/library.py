@@ -99,6 +99,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_unet_adam": (i32, [P, P, P, P, u32, C.c_float, C.c_float, C.c_float, C.c_float, u32, P, P, u32, u32,
                                    P]),
             "dk_unet_weights_to_bf16": (i32, [P, u32, P, P, u32, u32, P]),
+            "dk_unet_set_conv_path": (i32, [i32]),
+            "dk_unet_error": (i32, [C.POINTER(i32)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

@@ -460,6 +460,12 @@ int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t
                  void* stream);
 int dk_unet_weights_to_bf16(const float* weights, uint32_t count, void* wbf16, void* wflip, uint32_t cout,
                             uint32_t cin, void* stream);
+/* Selects the convolution kernel: 1 (default) the tcgen05 kernel (tensor
+ * memory accumulators, Cout <= 256), 0 the mma.sync kernel; for comparison. */
+int dk_unet_set_conv_path(int path);
+/* Reads and clears the denoiser kernels' error flag (1: a bounded wait for the
+ * tensor cores timed out and the affected tiles were not written). */
+int dk_unet_error(int* out_error);
 
 /* ------------------------------------------------------------------------- */
 /* Serving: a persistent request loop over one resident scene.                */

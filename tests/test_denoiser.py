@@ -1,0 +1,80 @@
+"""The denoisers on rendered images.
+
+* The spatial filter (dk_denoise_spatial) against the reference's own
+  simpleSpatialDenoiseKernel (Denoise.metal:39-115) compiled for the host
+  (oracle/_ref): the same arithmetic up to the last bits of `exp`, so a
+  relative tolerance of 1e-5 per texel.
+* The U-Net trained on the GPU by the library's kernels on pairs the tracer
+  renders (4 spp + AOVs -> 512 spp): on held-out scene variants it must beat
+  both the 4-spp input (by half) and the spatial filter in relative RMSE of
+  the displayed image (the reference's PNG tone curve) against the converged
+  render -- what the network gains over the method without it.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from denrimrendererkit_gb300 import DenrimRenderer, RenderOutput, compile_scene, scenes  # noqa: E402
+from denrimrendererkit_gb300.denoiser import (UNet, display_relative_rmse, relative_rmse, render_pairs,  # noqa: E402
+                                              spatial_denoise, train)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def renderer(dk_lib):
+    return DenrimRenderer(0)
+
+
+def test_spatial_filter_matches_reference_kernel(renderer, oracle_lib):
+    from oracle import oracle as orc
+    if not orc.reference_available():
+        pytest.skip("reference shaders not built")
+    lib = orc.load_reference()
+    wl = scenes.cornell_variant(5, 96, 64)
+    b = compile_scene(wl.scene)
+    with renderer.make_session(wl.scene, wl.settings, build=b) as s:
+        s.render(4)
+        planes = {k: s.pixels(k) for k in (RenderOutput.BEAUTY, RenderOutput.DEPTH, RenderOutput.NORMAL,
+                                           RenderOutput.ALBEDO)}
+    dev = {k: torch.from_numpy(v).cuda() for k, v in planes.items()}
+    for iterations, sigmas in ((1, (0.18, 0.03, 0.25, 1.0)), (3, (0.18, 0.03, 0.25, 1.0)), (5, (0.18, 0.08, 0.25, 4.0))):
+        out = torch.empty_like(dev[RenderOutput.BEAUTY])
+        spatial_denoise(dev[RenderOutput.BEAUTY], dev[RenderOutput.DEPTH], dev[RenderOutput.NORMAL],
+                        dev[RenderOutput.ALBEDO], out, 96, 64, 2, *sigmas, iterations)
+        torch.cuda.synchronize()
+        ref = np.zeros_like(planes[RenderOutput.BEAUTY])
+        import ctypes as C
+        lib.ref_denoise_spatial.argtypes = [C.c_void_p] * 5 + [C.c_uint32] * 3 + [C.c_float] * 4 + [C.c_uint32]
+        rc = lib.ref_denoise_spatial(planes[RenderOutput.BEAUTY].ctypes.data, planes[RenderOutput.DEPTH].ctypes.data,
+                                     planes[RenderOutput.NORMAL].ctypes.data, planes[RenderOutput.ALBEDO].ctypes.data,
+                                     ref.ctypes.data, 96, 64, 2, *sigmas, iterations)
+        assert rc == 0
+        got = out.cpu().numpy()
+        assert np.allclose(got, ref, rtol=1e-5, atol=1e-6), float(np.abs(got - ref).max())
+        assert not np.array_equal(got, planes[RenderOutput.BEAUTY])
+
+
+def test_unet_trained_on_rendered_pairs_beats_input_and_spatial_filter(renderer):
+    train_set = render_pairs(range(24), size=128, noisy_spp=4, target_spp=512)
+    held_out = render_pairs(range(1000, 1004), size=128, noisy_spp=4, target_spp=512)
+    net = UNet(seed=1)
+    losses = train(net, train_set, steps=500, batch=8, lr=2e-3, log_every=50)
+    assert losses[-1] < 0.7 * losses[0], losses
+    noisy, spatial, learned, lin = [], [], [], []
+    for k in range(held_out.count):
+        out = torch.empty_like(held_out.beauty[k])
+        net.denoise(held_out.beauty[k], held_out.albedo[k], held_out.normal[k], held_out.depth[k], 128, 128, out)
+        sp = torch.empty_like(out)
+        spatial_denoise(held_out.beauty[k], held_out.depth[k], held_out.normal[k], held_out.albedo[k], sp, 128, 128)
+        torch.cuda.synchronize()
+        t = held_out.target[k]
+        noisy.append(display_relative_rmse(held_out.beauty[k], t))
+        spatial.append(display_relative_rmse(sp, t))
+        learned.append(display_relative_rmse(out, t))
+        lin.append((relative_rmse(held_out.beauty[k], t), relative_rmse(sp, t), relative_rmse(out, t)))
+    n, s, l = np.mean(noisy), np.mean(spatial), np.mean(learned)
+    print(f"display relative RMSE on held-out variants: 4 spp {n:.4f}, spatial filter {s:.4f}, U-Net {l:.4f}; "
+          f"linear: {np.mean(lin, axis=0)}; losses {losses}")
+    assert l < 0.5 * n and l < s

@@ -28,11 +28,19 @@ def to_torch_weight(w):  # [co][9][ci] -> [co][ci][3][3]
     return w.reshape(co, 3, 3, ci).permute(0, 3, 1, 2).contiguous()
 
 
-@pytest.fixture(scope="module")
-def lib(dk_lib):
+@pytest.fixture(scope="module", params=[1, 0], ids=["tcgen05", "mma_sync"])
+def lib(dk_lib, request):
+    """Runs every test with the tcgen05 convolution and with the mma.sync one."""
+    import ctypes as C
     from denrimrendererkit_gb300 import DenrimRenderer
     DenrimRenderer(0)
-    return library.load()
+    lib = library.load()
+    library.check(lib.dk_unet_set_conv_path(request.param))
+    yield lib
+    err = C.c_int(0)
+    library.check(lib.dk_unet_error(C.byref(err)))
+    library.check(lib.dk_unet_set_conv_path(1))
+    assert err.value == 0, "a tensor-core wait timed out"
 
 
 @pytest.mark.parametrize("cin,cout,act,ldi_extra,ldo_extra,co_off", [
