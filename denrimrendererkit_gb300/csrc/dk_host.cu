@@ -394,6 +394,9 @@ int allocWave(Arena& arena, Wave& W, uint64_t capPaths, uint32_t pixelCap, uint3
     TRY(arena.alloc(&W.qr2, 3 * cap, "layer-walk queue"));
     TRY(arena.alloc(&W.counts, 8, "queue counters"));
     TRY(arena.alloc(&W.aov, 4 * (size_t)pixelCap, "AOV records"));
+    TRY(arena.alloc(&W.qsorted, cap, "material-ordered queue"));
+    TRY(arena.alloc(&W.keys, cap, "material keys"));
+    TRY(arena.alloc(&W.bins, kSortBins + 1, "material bins"));
     DevJob* jobs = nullptr;
     TRY(arena.alloc(&jobs, std::max(jobCap, 1u), "job table"));
     W.jobs = jobs;
@@ -459,7 +462,7 @@ int launchWave(const DevScene& S, const Wave& W, uint32_t maxBounces, bool anyDe
         MARK(3);
         DK_CUDA(launchShadow(S, W, g.shadow, q), "shadow launch");
         DK_CUDA(launchResolve(W, g.final, q), "resolve launch");
-        launches += 4;
+        launches += bounceLaunches(S);
     }
     MARK(0);
     if (anyDenoiser) {

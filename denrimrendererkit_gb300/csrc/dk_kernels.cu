@@ -14,6 +14,7 @@
 //   k_finalize  Kahan-compensated accumulation + last-sample AOVs (:5520-5585)
 // Surviving paths are compacted into the next queue with warp-ballot appends.
 #include <cstdio>
+#include <cstdlib>
 
 #include "dk_kernels.h"
 #include "dk_sdf.cuh"
@@ -425,6 +426,8 @@ __device__ __forceinline__ uint32_t warpFetch(uint32_t* counter, uint32_t n, boo
 __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel) {
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
+    if (blockIdx.x == 0)
+        for (uint32_t b = threadIdx.x; b <= kSortBins; b += blockDim.x) W.bins[b] = 0u;
     if (globalId() == 0) {
         W.counts[sel ^ 1u] = 0u;
         W.counts[2] = 0u;
@@ -454,6 +457,67 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
             W.hit[p] = make_float4(st.bestT, __uint_as_float(st.bestTri), st.bu, st.bv);
             p = kNoWork;
         }
+    }
+}
+
+// ------------------------------------------------ material ordering ----
+// The active queue is reordered by material before shading (a counting sort
+// on the hit's material ID), so the paths of a warp take the same BSDF
+// branches and read the same material record.  The order of paths does not
+// change any result: every path carries its own RNG state and pixel samples
+// are accumulated in sample order.
+__device__ __forceinline__ uint32_t shadeKey(const DevScene& S, const Wave& W, uint32_t p) {
+    uint32_t tri = __float_as_uint(W.hit[p].y);
+    if (tri == kNoHit) return 0u;
+    if (tri >= S.tri_count) return kSortBins - 1u;  // distance-volume hits
+    return 1u + min(__ldg(&S.tris[tri].material_id), kSortBins - 3u);
+}
+
+__global__ void __launch_bounds__(256) k_sort_count(DevScene S, Wave W, uint32_t sel) {
+    __shared__ uint32_t hist[kSortBins];
+    for (uint32_t b = threadIdx.x; b < kSortBins; b += blockDim.x) hist[b] = 0u;
+    __syncthreads();
+    const uint32_t* q = W.q[sel];
+    const uint32_t n = W.counts[sel];
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t k = shadeKey(S, W, q[i]);
+        W.keys[i] = k;
+        atomicAdd(&hist[k], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < kSortBins; b += blockDim.x)
+        if (hist[b]) atomicAdd(&W.bins[b], hist[b]);
+}
+
+// Exclusive scan of the histogram into bucket cursors (one block of kSortBins threads).
+__global__ void __launch_bounds__(kSortBins) k_sort_scan(Wave W) {
+    __shared__ uint32_t v[kSortBins];
+    uint32_t t = threadIdx.x;
+    uint32_t x = W.bins[t];
+    v[t] = x;
+    __syncthreads();
+    for (uint32_t o = 1; o < kSortBins; o <<= 1) {
+        uint32_t y = t >= o ? v[t - o] : 0u;
+        __syncthreads();
+        v[t] += y;
+        __syncthreads();
+    }
+    W.bins[t] = v[t] - x;
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(Wave W, uint32_t sel) {
+    const uint32_t* q = W.q[sel];
+    const uint32_t n = W.counts[sel];
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t k = W.keys[i];
+        unsigned active = __activemask();
+        unsigned peers = __match_any_sync(active, k);
+        int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)laneId() == leader) base = atomicAdd(&W.bins[k], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        uint32_t rank = (uint32_t)__popc(peers & ((1u << laneId()) - 1u));
+        W.qsorted[base + rank] = q[i];
     }
 }
 
@@ -670,8 +734,9 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
 #define DK_SHADE_MIN_BLOCKS 5
 #endif
 template <bool kVolumes>
-__global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, Wave W, uint32_t bounce, uint32_t sel) {
-    const uint32_t* q = W.q[sel];
+__global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, Wave W, uint32_t bounce, uint32_t sel,
+                                                                  uint32_t sorted) {
+    const uint32_t* q = sorted ? W.qsorted : W.q[sel];
     uint32_t* qNext = W.q[sel ^ 1u];
     const uint32_t n = W.counts[sel];
     if (globalId() == 0) W.counts[4] = 0u;  // extend cursor of the next bounce
@@ -1144,11 +1209,35 @@ cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int gri
     if (S.volume_count) k_extend_volume<<<grid, 128, 0, st>>>(S, W, sel);
     return cudaGetLastError();
 }
+int g_sortMaterials = -1;  // -1: from DK_SORT_MATERIALS (default on)
+
+// Kernels one bounce launches (extend, shade, shadow, resolve stages).
+uint32_t bounceLaunches(const DevScene& S) {
+    if (g_sortMaterials < 0) {
+        const char* e = getenv("DK_SORT_MATERIALS");
+        g_sortMaterials = (e && e[0] == '0') ? 0 : 1;
+    }
+    uint32_t n = 1u + (S.volume_count ? 1u : 0u);                  // extend
+    n += 1u + (g_sortMaterials ? 3u : 0u);                           // shade
+    n += 1u + ((!S.all_shadow_opaque || S.volume_count) ? 1u : 0u);  // shadow
+    return n + 1u;                                                   // resolve
+}
+
 cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint32_t sel, int grid, cudaStream_t st) {
+    if (g_sortMaterials < 0) {
+        const char* e = getenv("DK_SORT_MATERIALS");
+        g_sortMaterials = (e && e[0] == '0') ? 0 : 1;
+    }
+    uint32_t sorted = (uint32_t)g_sortMaterials;
+    if (sorted) {
+        k_sort_count<<<grid, 256, 0, st>>>(S, W, sel);
+        k_sort_scan<<<1, kSortBins, 0, st>>>(W);
+        k_sort_scatter<<<grid, 256, 0, st>>>(W, sel);
+    }
     if (S.volume_count)
-        k_shade<true><<<grid, 128, 0, st>>>(S, W, bounce, sel);
+        k_shade<true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
     else
-        k_shade<false><<<grid, 128, 0, st>>>(S, W, bounce, sel);
+        k_shade<false><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
     return cudaGetLastError();
 }
 cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st) {

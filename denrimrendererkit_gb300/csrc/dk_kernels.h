@@ -12,6 +12,7 @@
 namespace dk {
 
 constexpr uint32_t kNoSlot = 0xffffffffu;
+constexpr uint32_t kSortBins = 256;  // shading-order keys: 0 miss, 1 + material ID (< 254), 255 other
 
 // Device copy of the scene.  `isect` holds 3 x float4 per BVH leaf slot:
 // (v0.xyz, reference slot), (v1 - v0, triangle index), (v2 - v0, flags with
@@ -108,6 +109,9 @@ struct Wave {
     uint32_t* counts;  // [0], [1] queue lengths, [2] shadow paths, [3] shadow rays, [4] extend cursor,
                        // [5] shadow cursor, [6] layer-walk rays, [7] spare
     float4* aov;       // 4 planes of aov_stride tile pixels: primary-hit record of each job's last sample
+    uint32_t* qsorted; // the active queue reordered by material (the shading order)
+    uint32_t* keys;    // material key of each active-queue entry
+    uint32_t* bins;    // kSortBins + 1 counters: key histogram, then bucket cursors
     const DevJob* jobs;
     uint32_t cap;
     uint32_t aov_stride;
@@ -129,6 +133,7 @@ cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_
 cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchAovPrimary(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchFinalize(const Wave& W, int grid, cudaStream_t st);
+uint32_t bounceLaunches(const DevScene& S);
 cudaError_t launchResolveBeauty(const Accum& A, uint32_t pixels, float4* out, int grid, cudaStream_t st);
 cudaError_t buildEnvironmentTable(const float4* dPixels, uint32_t w, uint32_t h, float intensity, float maxR,
                                   double* dWeights, double* dPrefix, double* dBlockSums, float2* dOut, int grid,

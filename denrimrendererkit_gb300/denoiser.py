@@ -389,12 +389,17 @@ def render_pairs(seeds, size: int = 256, noisy_spp: int = 4, target_spp: int = 1
     return TrainingSet(**planes)
 
 
-def train(net: UNet, data: TrainingSet, steps: int, batch: int = 16, lr: float = 1e-3, seed: int = 0,
-          log_every: int = 0) -> List[float]:
-    """Adam on random batches of whole training images (L1 in log space).
-    Returns the per-step losses."""
+def train(net: UNet, data: TrainingSet, steps: int, batch: int = 16, crop: Optional[int] = None, lr: float = 1e-3,
+          seed: int = 0, log_every: int = 0) -> List[float]:
+    """Adam on random batches of random `crop` x `crop` windows of the
+    training images (whole images when `crop` is None); L1 in log space with
+    a cosine learning-rate decay to 10 %.  Returns the logged losses."""
     torch = _torch()
-    n, h, w = batch, data.beauty.shape[1], data.beauty.shape[2]
+    H, W = data.beauty.shape[1], data.beauty.shape[2]
+    h = w = crop if crop else None
+    if h is None:
+        h, w = H, W
+    n = batch
     B = net.grad_buffers(n, h, w)
     target = torch.empty(n, h, w, 4, dtype=torch.float32, device="cuda")
     rng = np.random.default_rng(seed)
@@ -402,14 +407,15 @@ def train(net: UNet, data: TrainingSet, steps: int, batch: int = 16, lr: float =
     for step in range(steps):
         idx = rng.integers(0, data.count, size=n)
         for j, k in enumerate(idx):
-            net.pack(data.beauty[k], data.albedo[k], data.normal[k], data.depth[k], w, h, 0, 0, n, h, w, j)
-            target[j].copy_(data.target[k])
+            x0 = int(rng.integers(0, W - w + 1))
+            y0 = int(rng.integers(0, H - h + 1))
+            net.pack(data.beauty[k], data.albedo[k], data.normal[k], data.depth[k], W, H, x0, y0, n, h, w, j)
+            target[j].copy_(data.target[k][y0:y0 + h, x0:x0 + w])
         net.zero_grad()
         B["loss"].zero_()
         net.forward(n, h, w)
         net.loss(target, n, h, w)
         net.backward(n, h, w)
-        # cosine decay to 10 % of the initial rate
         cur = lr * (0.1 + 0.9 * 0.5 * (1.0 + math.cos(math.pi * step / max(steps, 1))))
         net.adam(cur)
         if log_every and (step % log_every == 0 or step == steps - 1):

@@ -57,17 +57,18 @@ def test_spatial_filter_matches_reference_kernel(renderer, oracle_lib):
 
 
 def test_unet_trained_on_rendered_pairs_beats_input_and_spatial_filter(renderer):
-    train_set = render_pairs(range(24), size=128, noisy_spp=4, target_spp=512)
-    held_out = render_pairs(range(1000, 1004), size=128, noisy_spp=4, target_spp=512)
+    size = 256
+    train_set = render_pairs(range(48), size=size, noisy_spp=4, target_spp=512)
+    held_out = render_pairs(range(1000, 1004), size=size, noisy_spp=4, target_spp=512)
     net = UNet(seed=1)
-    losses = train(net, train_set, steps=500, batch=8, lr=2e-3, log_every=50)
+    losses = train(net, train_set, steps=1500, batch=16, crop=128, lr=1e-3, log_every=100)
     assert losses[-1] < 0.7 * losses[0], losses
     noisy, spatial, learned, lin = [], [], [], []
     for k in range(held_out.count):
         out = torch.empty_like(held_out.beauty[k])
-        net.denoise(held_out.beauty[k], held_out.albedo[k], held_out.normal[k], held_out.depth[k], 128, 128, out)
+        net.denoise(held_out.beauty[k], held_out.albedo[k], held_out.normal[k], held_out.depth[k], size, size, out)
         sp = torch.empty_like(out)
-        spatial_denoise(held_out.beauty[k], held_out.depth[k], held_out.normal[k], held_out.albedo[k], sp, 128, 128)
+        spatial_denoise(held_out.beauty[k], held_out.depth[k], held_out.normal[k], held_out.albedo[k], sp, size, size)
         torch.cuda.synchronize()
         t = held_out.target[k]
         noisy.append(display_relative_rmse(held_out.beauty[k], t))
