@@ -16,6 +16,7 @@
 // through an XOR swizzle that keeps ldmatrix conflict-free.
 #include <cstdint>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "dk_host.h"
@@ -374,6 +375,229 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_tc(ConvArgs a, uint32_t tmem
 }
 
 size_t tcSmemBytes(uint32_t cout) { return (size_t)kTcStages * (kTcRows * 128u + cout * 128u) + 1024u + 64u; }
+
+// ------------------------------------------- tcgen05 + TMA, persistent ----
+// The production convolution.  Persistent CTAs (one per SM) walk output
+// tiles of 128 pixels (th image rows x tw columns, tw a power of two <= 128)
+// with three warp roles:
+//   warp 0     TMA producer: per (tap, 64-channel chunk) one 4-D box of the
+//              activation tensor {64 ch, tw, th, 1} at the tap-shifted
+//              coordinate (out-of-range pixels and channels are zero filled
+//              by the copy engine) and one 3-D box of the weights
+//              {64 ch, 1 tap, Cout}, both into 128-byte-swizzled K-major tiles;
+//   warp 1     MMA issuer: tcgen05.mma M = 128, N = Cout, K = 16 into one of
+//              two tensor-memory accumulators, stage release and
+//              accumulator hand-off through tcgen05.commit;
+//   warps 2-5  epilogue: tcgen05.ld of their TMEM lane quarter, bias, ReLU,
+//              optional accumulate, bf16 stores; the next tile's MMAs run
+//              into the other accumulator meanwhile.
+// Every mbarrier wait is bounded (about 2 s); a role that times out records
+// the error and stops, the others then time out in turn, and the CTA frees
+// its tensor memory before returning.
+constexpr int kTmaStages = 4;
+
+struct TmaConvArgs {
+    const float* bias;
+    __nv_bfloat16* out;
+    uint32_t n, h, w, cin, cout, ldo, coOff, tw, th, tilesX, tilesY, numTiles, chunks, cols;
+    int act, accumulate;
+};
+
+__device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbarArrive(uint32_t bar) {
+    asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbarExpectTx(uint32_t bar, uint32_t bytes) {
+    asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(bar),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tmaLoad4(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tmaLoad3(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void umaCommit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1)
+    k_conv3x3_tma(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW, TmaConvArgs a) {
+    extern __shared__ unsigned char dsm[];
+    const uint32_t raw = smemAddr(dsm);
+    unsigned char* sm = dsm + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t N = a.cout;
+    const uint32_t aBytes = 128u * 128u, bBytes = N * 128u;
+    unsigned char* sA = sm;
+    unsigned char* sB = sm + kTmaStages * aBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kTmaStages * bBytes);
+    // bars: full[S], empty[S], accFull[2], accEmpty[2]
+    const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kTmaStages;
+    const uint32_t accFullBar = emptyBar + 8u * kTmaStages, accEmptyBar = accFullBar + 16u;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kTmaStages + 4);
+    int* abortFlag = reinterpret_cast<int*>(tslot + 1);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(tslot)),
+                     "r"(2u * a.cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kTmaStages; ++s) {
+            mbarInit(fullBar + 8u * s, 1);
+            mbarInit(emptyBar + 8u * s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbarInit(accFullBar + 8u * b, 1);
+            mbarInit(accEmptyBar + 8u * b, 128);
+        }
+        *abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(&mapIn) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(&mapW) : "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *tslot;
+    const uint32_t kIters = 9u * a.chunks;
+    const uint32_t txBytes = aBytes + bBytes;
+    volatile int* abortV = abortFlag;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t g = 0;
+            for (uint32_t tile = blockIdx.x; tile < a.numTiles && !*abortV; tile += gridDim.x) {
+                uint32_t tx = tile % a.tilesX, rest = tile / a.tilesX;
+                uint32_t ty = rest % a.tilesY, img = rest / a.tilesY;
+                int x0 = (int)(tx * a.tw), y0 = (int)(ty * a.th);
+                for (uint32_t it = 0; it < kIters; ++it, ++g) {
+                    uint32_t s = g % kTmaStages, u = g / kTmaStages;
+                    if (u > 0 && !mbarWait(emptyBar + 8u * s, (u - 1u) & 1u)) {
+                        *abortV = 1;
+                        break;
+                    }
+                    uint32_t tap = it / a.chunks, c0 = (it - tap * a.chunks) * 64u;
+                    mbarExpectTx(fullBar + 8u * s, txBytes);
+                    tmaLoad4(smemAddr(sA + s * aBytes), &mapIn, (int)c0, x0 + (int)(tap % 3u) - 1,
+                             y0 + (int)(tap / 3u) - 1, (int)img, fullBar + 8u * s);
+                    tmaLoad3(smemAddr(sB + s * bBytes), &mapW, (int)c0, (int)tap, 0, fullBar + 8u * s);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
+            uint32_t g = 0, t = 0;
+            for (uint32_t tile = blockIdx.x; tile < a.numTiles && !*abortV; tile += gridDim.x, ++t) {
+                uint32_t b = t & 1u, v = t >> 1;
+                if (v > 0 && !mbarWait(accEmptyBar + 8u * b, (v - 1u) & 1u)) {
+                    *abortV = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t dAddr = taddr + b * a.cols;
+                bool ok = true;
+                for (uint32_t it = 0; it < kIters; ++it, ++g) {
+                    uint32_t s = g % kTmaStages, u = g / kTmaStages;
+                    if (!mbarWait(fullBar + 8u * s, u & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t c0 = (it % a.chunks) * 64u;
+                    const uint32_t aBase = smemAddr(sA + s * aBytes), bBase = smemAddr(sB + s * bBytes);
+                    for (uint32_t ks = 0; ks < 4; ++ks) {
+                        if (c0 + ks * 16u >= a.cin) break;
+                        uint64_t ad = umaDesc(aBase + ks * 32u), bd = umaDesc(bBase + ks * 32u);
+                        uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dAddr),
+                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                    }
+                    umaCommit(emptyBar + 8u * s);  // the stage is free once these MMAs are done
+                }
+                if (!ok) {
+                    *abortV = 1;
+                    break;
+                }
+                umaCommit(accFullBar + 8u * b);  // the accumulator is complete
+            }
+        }
+    } else {
+        // Epilogue warps 2..5: TMEM lane quarter (warp % 4).
+        const uint32_t q = warp & 3u;
+        const uint32_t r = q * 32u + lane;
+        uint32_t t = 0;
+        for (uint32_t tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++t) {
+            uint32_t b = t & 1u, v = t >> 1;
+            if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
+                *abortV = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            uint32_t tx = tile % a.tilesX, rest = tile / a.tilesX;
+            uint32_t ty = rest % a.tilesY, img = rest / a.tilesY;
+            uint32_t px = tx * a.tw + r % a.tw, py = ty * a.th + r / a.tw;
+            bool valid = px < a.w && py < a.h;
+            __nv_bfloat16* orow = a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff;
+            const uint32_t src = taddr + ((q * 32u) << 16) + b * a.cols;
+            for (uint32_t c0 = 0; c0 < N; c0 += 16u) {
+                uint32_t rr[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];\n"
+                    : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]),
+                      "=r"(rr[7]), "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]),
+                      "=r"(rr[14]), "=r"(rr[15])
+                    : "r"(src + c0));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (!valid) continue;
+                float v2[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    float x = __uint_as_float(rr[k]);
+                    if (a.bias) x += a.bias[c0 + k];
+                    if (a.act == 1) x = fmaxf(x, 0.0f);
+                    v2[k] = x;
+                }
+                __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(orow + c0);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    float x0v = v2[2 * k], x1v = v2[2 * k + 1];
+                    if (a.accumulate) {
+                        float2 o = __bfloat1622float2(dst[k]);
+                        x0v += o.x;
+                        x1v += o.y;
+                    }
+                    dst[k] = __floats2bfloat162_rn(x0v, x1v);
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            mbarArrive(accEmptyBar + 8u * b);
+        }
+    }
+    __syncthreads();
+    if (*abortV && tid == 0) atomicExch(&g_unetError, 2);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(2u * a.cols));
+}
+
+size_t tmaSmemBytes(uint32_t cout) { return (size_t)kTmaStages * (128u * 128u + cout * 128u) + 1024u + 128u; }
 
 // -------------------------------------------------------------- wgrad ----
 struct WgradArgs {
@@ -735,8 +959,83 @@ inline int gridFor(uint64_t work, int block = 256) {
 
 inline bool aligned16(uint32_t v) { return v % 16u == 0u; }
 
-// 1: tcgen05 forward convolution (default), 0: the mma.sync kernel.
-int g_convPath = 1;
+// 2: persistent TMA + tcgen05 convolution (default), 1: the cp.async +
+// tcgen05 one, 0: the mma.sync one.
+int g_convPath = 2;
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encodeTiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+int launchConvTma(const ConvArgs& c, cudaStream_t st) {
+    EncodeTiledFn enc = encodeTiled();
+    if (!enc) return fail(DK_ERROR_COMMAND_FAILED, "cuTensorMapEncodeTiled is not available");
+    TmaConvArgs a;
+    a.bias = c.bias;
+    a.out = c.out;
+    a.n = c.n;
+    a.h = c.h;
+    a.w = c.w_;
+    a.cin = c.cin;
+    a.cout = c.cout;
+    a.ldo = c.ldo;
+    a.coOff = c.coOff;
+    a.act = c.act;
+    a.accumulate = c.accumulate;
+    uint32_t tw = 1;
+    while (tw * 2u <= c.w_ && tw < 128u) tw *= 2u;
+    a.tw = tw;
+    a.th = 128u / tw;
+    a.tilesX = (c.w_ + a.tw - 1) / a.tw;
+    a.tilesY = (c.h + a.th - 1) / a.th;
+    a.numTiles = a.tilesX * a.tilesY * c.n;
+    a.chunks = (c.cin + 63u) / 64u;
+    a.cols = 32u;
+    while (a.cols < c.cout) a.cols <<= 1;
+    alignas(64) CUtensorMap mapIn, mapW;
+    cuuint64_t dimIn[4] = {c.cin, c.w_, c.h, c.n};
+    cuuint64_t strideIn[3] = {(cuuint64_t)c.ldi * 2u, (cuuint64_t)c.w_ * c.ldi * 2u, (cuuint64_t)c.h * c.w_ * c.ldi * 2u};
+    cuuint32_t boxIn[4] = {64u, a.tw, a.th, 1u};
+    cuuint32_t unit[4] = {1u, 1u, 1u, 1u};
+    CUresult r = enc(&mapIn, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(c.in), dimIn, strideIn,
+                     boxIn, unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "activation tensor map rejected");
+    cuuint64_t dimW[3] = {c.cin, 9u, c.cout};
+    cuuint64_t strideW[2] = {(cuuint64_t)c.cin * 2u, (cuuint64_t)9u * c.cin * 2u};
+    cuuint32_t boxW[3] = {64u, 1u, c.cout};
+    r = enc(&mapW, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(c.w), dimW, strideW, boxW, unit,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "weight tensor map rejected");
+    size_t smem = tmaSmemBytes(c.cout);
+    static size_t configured = 0;
+    if (smem > configured) {
+        DK_CUDA(cudaFuncSetAttribute(k_conv3x3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                "conv3x3 shared memory");
+        configured = smem;
+    }
+    uint32_t grid = (uint32_t)deviceProp().multiProcessorCount;
+    if (grid > a.numTiles) grid = a.numTiles;
+    k_conv3x3_tma<<<grid, 192, smem, st>>>(mapIn, mapW, a);
+    DK_CUDA(cudaGetLastError(), "conv3x3 (TMA + tcgen05) launch");
+    return DK_OK;
+}
 
 }  // namespace
 }  // namespace dk
@@ -759,6 +1058,11 @@ int dk_unet_conv3x3(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t
     dk::ConvArgs a{static_cast<const bf16*>(in), static_cast<const bf16*>(weight), bias, static_cast<bf16*>(out),
                    n, h, w, cin, ldi, cout, ldo, coOff, (uint32_t)M, act, accumulate};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dk::g_convPath == 2 && cout <= 256u) {
+        int rc = dk::launchConvTma(a, st);
+        if (rc != DK_OK) return rc;
+        return DK_OK;
+    }
     if (dk::g_convPath == 1 && cout <= 256u) {
         uint32_t cols = 32u;
         while (cols < cout) cols <<= 1;
@@ -926,7 +1230,7 @@ int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t
 }
 
 int dk_unet_set_conv_path(int path) {
-    if (path != 0 && path != 1) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_set_conv_path: 0 or 1");
+    if (path < 0 || path > 2) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_set_conv_path: 0, 1 or 2");
     dk::g_convPath = path;
     return DK_OK;
 }

@@ -460,8 +460,9 @@ int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t
                  void* stream);
 int dk_unet_weights_to_bf16(const float* weights, uint32_t count, void* wbf16, void* wflip, uint32_t cout,
                             uint32_t cin, void* stream);
-/* Selects the convolution kernel: 1 (default) the tcgen05 kernel (tensor
- * memory accumulators, Cout <= 256), 0 the mma.sync kernel; for comparison. */
+/* Selects the convolution kernel (Cout <= 256 for the tcgen05 ones): 2
+ * (default) persistent TMA + tcgen05 with warp roles, 1 cp.async + tcgen05,
+ * 0 mma.sync; the alternatives are kept for comparison. */
 int dk_unet_set_conv_path(int path);
 /* Reads and clears the denoiser kernels' error flag (1: a bounded wait for the
  * tensor cores timed out and the affected tiles were not written). */

@@ -28,9 +28,10 @@ def to_torch_weight(w):  # [co][9][ci] -> [co][ci][3][3]
     return w.reshape(co, 3, 3, ci).permute(0, 3, 1, 2).contiguous()
 
 
-@pytest.fixture(scope="module", params=[1, 0], ids=["tcgen05", "mma_sync"])
+@pytest.fixture(scope="module", params=[2, 1, 0], ids=["tma_tcgen05", "cpasync_tcgen05", "mma_sync"])
 def lib(dk_lib, request):
-    """Runs every test with the tcgen05 convolution and with the mma.sync one."""
+    """Runs every test with each convolution kernel: persistent TMA + tcgen05
+    (the default), cp.async + tcgen05, and mma.sync."""
     import ctypes as C
     from denrimrendererkit_gb300 import DenrimRenderer
     DenrimRenderer(0)
@@ -39,7 +40,7 @@ def lib(dk_lib, request):
     yield lib
     err = C.c_int(0)
     library.check(lib.dk_unet_error(C.byref(err)))
-    library.check(lib.dk_unet_set_conv_path(1))
+    library.check(lib.dk_unet_set_conv_path(2))
     assert err.value == 0, "a tensor-core wait timed out"
 
 
