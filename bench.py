@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--spp", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="large", choices=["large", "serving", "denoise"],
+                    help="large: the headline path-tracing step (default); serving: the material-preview job "
+                         "stream through the serving loop; denoise: U-Net training and 1080p inference")
+    ap.add_argument("--jobs", type=int, default=1024, help="serving: jobs taken from the 4096-job stream")
     return ap.parse_args()
 
 
@@ -138,13 +142,16 @@ class ClockSampler:
                 "samples": len(sm), "power_w_max": max(power)}
 
 
-def measured_peaks():
+def measured_peaks(key: str = "hbm_gbs"):
+    """The measured peak `key` of MEASURED_PEAKS.json (HBM copy GB/s or dense
+    bf16 TFLOP/s), else the fallback figure."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         with open(path) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        if key in d:
+            return float(d[key]), "measured"
+    return (6800.0 if key == "hbm_gbs" else 1900.0), "fallback"
 
 
 def profile_traffic(kernel: str):
@@ -369,6 +376,8 @@ def run_gb300(args, rank, world, local):
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured"
                 else "fallback 6.8 TB/s", "traffic": traffic,
+                "units": "achieved and traffic are per step (one frame, all launches of the stage); traffic = "
+                         "DRAM read+write bytes scaled from a small-case ncu capture (profiles/<stage>_spheres_large.md)",
                 "algorithmic_bytes_per_step": {k: float(v) for k, v in per_frame.items()},
                 "kernel_ms_per_step": kernel_ms,
                 "per_path": {k: float(v) / paths for k, v in counters.items() if k != "paths"}}
@@ -385,9 +394,168 @@ def run_gb300(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+def percentile(values, q):
+    v = sorted(values)
+    if not v:
+        return None
+    k = min(len(v) - 1, max(0, int(round(q / 100.0 * (len(v) - 1)))))
+    return v[k]
+
+
+def run_serving(args, rank):
+    """Material-preview jobs arriving as a Poisson stream (200/s) through the
+    serving loop; once with waves packing all admitted jobs, once with one job
+    per wave (per-job plain launches over the same resident scene)."""
+    if rank != 0:
+        return
+    from denrimrendererkit_gb300 import DenrimRenderer, abi, compile_scene, scenes
+    from denrimrendererkit_gb300.presets import PRESETS
+    from denrimrendererkit_gb300.renderer import RenderQuality, RenderSettings
+    from denrimrendererkit_gb300.serving import RenderServer, ServerConfig
+    DenrimRenderer(0)
+    scene = scenes.material_preview()
+    build = compile_scene(scene)
+    jobs = scenes.serving_jobs()[:args.jobs]
+    tables = {}
+    for j in jobs:
+        if j.preset not in tables:
+            t = build.materials.copy()
+            t[1] = PRESETS[j.preset].gpu_material()
+            tables[j.preset] = t
+    paths = sum(j.width * j.height * j.samples for j in jobs)
+    results = {}
+    for mode, per_wave in (("packed", 512), ("one_job_per_wave", 1)):
+        with RenderServer(build, ServerConfig(max_jobs_per_wave=per_wave)) as srv:
+            srv.start()
+            ids = []
+            done = {}
+            stop = threading.Event()
+
+            def collect():
+                k = 0
+                while k < len(jobs):
+                    while k >= len(ids):
+                        if stop.is_set():
+                            return
+                        time.sleep(0.0005)
+                    st = srv.status(ids[k])
+                    if st.state == abi.JOB_DONE:
+                        done[k] = st
+                        srv.release(ids[k])
+                        k += 1
+                    else:
+                        time.sleep(0.0005)
+
+            th = threading.Thread(target=collect)
+            th.start()
+            t0 = time.perf_counter()
+            backlog = 0
+            for j in jobs:
+                delay = j.arrival_s - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                st = RenderSettings(width=j.width, height=j.height, max_bounces=8, quality=RenderQuality.FINAL,
+                                    frame_seed=1)
+                ids.append(srv.submit(st, scene.camera, j.samples, tables[j.preset]))
+                backlog = max(backlog, len(ids) - len(done))
+            th.join()
+            wall = time.perf_counter() - t0
+            stats = srv.stats()
+            srv.stop()
+        lat = [done[k].latency_ms for k in range(len(jobs))]
+        small = [done[k].latency_ms for k in range(len(jobs)) if jobs[k].width <= 96]
+        results[mode] = {"wall_s": wall, "images_per_s": len(jobs) / wall, "mpaths_s": paths / wall / 1e6,
+                         "p50_ms": percentile(lat, 50), "p99_ms": percentile(lat, 99),
+                         "p50_ms_96px_jobs": percentile(small, 50), "p99_ms_96px_jobs": percentile(small, 99),
+                         "max_backlog_jobs": backlog, "waves": stats["waves"],
+                         "mean_jobs_per_wave": stats["mean_jobs_in_wave"], "busy_s": stats["busy_ms"] / 1e3,
+                         "gpu_launches": stats["kernel_launches"], "budget_peak_gb": stats["budget_peak_bytes"] / 1e9}
+    line = {"metric": "serving images/s", "value": results["packed"]["images_per_s"], "unit": "images/s",
+            "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"material-preview stream: first {len(jobs)} of 4096 seeded jobs, Poisson 200/s, "
+                                   "res {96,256,512,1024}^2 (50/30/15/5 %), spp {16,64,256}, 7 preset families, "
+                                   "icosphere on a plane under the 2048x1024 HDRI",
+                       "paths": paths, "offered_load_gpaths_s": paths / max(jobs[-1].arrival_s, 1e-9) / 1e9},
+            "serving": results,
+            "images_per_s_vs_one_job_per_wave": results["packed"]["images_per_s"]
+            / results["one_job_per_wave"]["images_per_s"]}
+    print(json.dumps(line), flush=True)
+
+
+def run_denoise(args, rank):
+    """U-Net: training throughput on 16 x 256^2 crops, 1920x1088 inference
+    time (tcgen05 convolution) against the bf16 tensor peak, and the
+    equal-error sample count on held-out scene variants."""
+    if rank != 0:
+        return
+    import torch
+    from denrimrendererkit_gb300 import DenrimRenderer
+    from denrimrendererkit_gb300.denoiser import (UNet, display_relative_rmse, flops_per_pixel, render_pairs,
+                                                  spatial_denoise, train)
+    DenrimRenderer(0)
+    t0 = time.perf_counter()
+    data = render_pairs(range(64), size=256, noisy_spp=4, target_spp=1024)
+    held = render_pairs(range(2000, 2008), size=256, noisy_spp=4, target_spp=1024)
+    render_s = time.perf_counter() - t0
+    net = UNet(seed=1)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    steps = 2000
+    losses = train(net, data, steps=steps, batch=16, crop=128, lr=1e-3, log_every=500)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    errs = {"noisy_4spp": [], "spatial_filter": [], "unet": []}
+    for k in range(held.count):
+        out = torch.empty_like(held.beauty[k])
+        net.denoise(held.beauty[k], held.albedo[k], held.normal[k], held.depth[k], 256, 256, out)
+        sp = torch.empty_like(out)
+        spatial_denoise(held.beauty[k], held.depth[k], held.normal[k], held.albedo[k], sp, 256, 256)
+        torch.cuda.synchronize()
+        errs["noisy_4spp"].append(display_relative_rmse(held.beauty[k], held.target[k]))
+        errs["spatial_filter"].append(display_relative_rmse(sp, held.target[k]))
+        errs["unet"].append(display_relative_rmse(out, held.target[k]))
+    mean = {k: float(np.mean(v)) for k, v in errs.items()}
+    # plain sample count with the U-Net's error (noise error falls as 1/sqrt(spp))
+    equal_spp = 4.0 * (mean["noisy_4spp"] / mean["unet"]) ** 2
+    # 1080p inference timing
+    B = net.buffers(1, 1088, 1920)
+    for _ in range(3):
+        net.forward(1, 1088, 1920)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        net.forward(1, 1088, 1920)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    flops = flops_per_pixel() * 1088 * 1920
+    peak, kind = measured_peaks("bf16_tflops")
+    achieved = flops / (ms * 1e-3) / 1e12
+    line = {"metric": "denoiser 1080p inference ms", "value": ms, "unit": "ms", "n_gpus": 1,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "5-level U-Net 32-64-96-128-160 over beauty+albedo+normal+depth, "
+                                   "1920x1088 inference; training 16 x 128^2 crops of 64 rendered 256^2 "
+                                   "small-scene variants (4 spp -> 1024 spp)", "train_steps": steps},
+            "roofline": {"kernel": "k_conv3x3_tma (whole forward pass)", "bound": "tensor", "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                         "peak_source": kind, "traffic": None, "gflop_per_inference": flops / 1e9},
+            "train_step_ms": train_s / steps * 1e3, "render_pairs_s": render_s,
+            "display_relative_rmse_held_out": mean, "plain_spp_with_unet_error": equal_spp,
+            "losses": losses}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "serving" and args.impl != "reference":
+        run_serving(args, rank)
+        return
+    if args.workload == "denoise" and args.impl != "reference":
+        run_denoise(args, rank)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:
