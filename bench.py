@@ -404,8 +404,9 @@ def percentile(values, q):
 
 def run_serving(args, rank):
     """Material-preview jobs arriving as a Poisson stream (200/s) through the
-    serving loop; once with waves packing all admitted jobs, once with one job
-    per wave (per-job plain launches over the same resident scene)."""
+    serving loop: waves packing all admitted jobs (oldest first, then fewest
+    remaining paths; and in admission order), and one job per wave (per-job
+    plain launches over the same resident scene)."""
     if rank != 0:
         return
     from denrimrendererkit_gb300 import DenrimRenderer, abi, compile_scene, scenes
@@ -424,8 +425,8 @@ def run_serving(args, rank):
             tables[j.preset] = t
     paths = sum(j.width * j.height * j.samples for j in jobs)
     results = {}
-    for mode, per_wave in (("packed", 512), ("one_job_per_wave", 1)):
-        with RenderServer(build, ServerConfig(max_jobs_per_wave=per_wave)) as srv:
+    for mode, per_wave, policy in (("packed", 512, 1), ("packed_fifo", 512, 0), ("one_job_per_wave", 1, 0)):
+        with RenderServer(build, ServerConfig(max_jobs_per_wave=per_wave, policy=policy)) as srv:
             srv.start()
             ids = []
             done = {}

@@ -185,7 +185,8 @@ class SpatialDenoiseSettings(C.Structure):
 class ServerConfig(C.Structure):
     """dk_server_config."""
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("wave_paths", C.c_uint32), ("max_jobs_per_wave", C.c_uint32),
-                ("max_resident_jobs", C.c_uint32), ("samples_per_wave", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("max_resident_jobs", C.c_uint32), ("samples_per_wave", C.c_uint32), ("policy", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class JobDesc(C.Structure):

@@ -9,11 +9,12 @@
 // binned-SAH binary tree built here (`buildSahTraversal`); the kernels return
 // the argmin over (t, slot), which is the reference's answer.
 //
-// Output layout (see dk_kernels.h): 4 x float4 per interior node holding the
-// x, y, z slabs of both children and the two child references (interior index,
-// or 0x80000000 | first << 3 | (count - 1) for a leaf of <= 8 slots); 3 x
-// float4 per leaf slot: (v0, reference slot), (v1 - v0, triangle index),
-// (v2 - v0, flags: bit 0 = blocks shadow rays); one dummy slot at the end.
+// Output layout (see dk_kernels.h): the binary SAH tree collapsed into 4-wide
+// nodes of 8 x float4 (the x, y, z slabs of four children, one lane each, and
+// the four child references: interior index, or 0x80000000 | first << 3 |
+// (count - 1) for a leaf of <= 8 slots); 3 x float4 per leaf slot: (v0,
+// reference slot), (v1 - v0, triangle index), (v2 - v0, flags: bit 0 = blocks
+// shadow rays, bits 8..15 material ID); one dummy slot at the end.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -146,28 +147,53 @@ std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth) {
     return node;
 }
 
-void setChild(float4* rec, int side, const Box& b) {
-    rec[side] = make_float4(b.mn[0], b.mx[0], b.mn[1], b.mx[1]);
-    if (side == 0) {
-        rec[2].x = b.mn[2];
-        rec[2].y = b.mx[2];
-    } else {
-        rec[2].z = b.mn[2];
-        rec[2].w = b.mx[2];
+// 4-wide node record (8 x float4): child boxes as x-min, x-max, y-min, y-max,
+// z-min, z-max rows (one lane per child), the four child references, a spare
+// row.  Unused child lanes reference the dummy slot behind a box at 1e30.
+void setChild4(float4* rec, int lane, const Box& b, uint32_t ref) {
+    float* f = reinterpret_cast<float*>(rec);
+    for (int a = 0; a < 3; ++a) {
+        f[(2 * a) * 4 + lane] = b.mn[a];
+        f[(2 * a + 1) * 4 + lane] = b.mx[a];
     }
+    reinterpret_cast<uint32_t*>(rec + 6)[lane] = ref;
 }
 
-uint32_t flatten(const TNode* t, std::vector<float4>& nodes, int depth, int& maxDepth) {
+// Collapses the binary tree under `t` (an interior node) into 4-wide nodes:
+// a node's children are the binary subtrees reached by repeatedly opening the
+// interior child of largest surface area until there are four.
+uint32_t flatten4(const TNode* t, std::vector<float4>& nodes, uint32_t dummyLeaf, int depth, int& maxDepth) {
     maxDepth = std::max(maxDepth, depth);
-    if (!t->l) return kLeaf | (t->first << 3) | (t->count - 1u);
-    uint32_t idx = (uint32_t)(nodes.size() / 4);
-    nodes.resize(nodes.size() + 4);
-    uint32_t l = flatten(t->l.get(), nodes, depth + 1, maxDepth);
-    uint32_t r = flatten(t->r.get(), nodes, depth + 1, maxDepth);
-    float4* rec = &nodes[4 * (size_t)idx];
-    setChild(rec, 0, t->l->box);
-    setChild(rec, 1, t->r->box);
-    rec[3] = make_float4(asFloat(l), asFloat(r), 0.0f, 0.0f);
+    std::vector<const TNode*> kids = {t->l.get(), t->r.get()};
+    while (kids.size() < 4) {
+        int best = -1;
+        float area = -1.0f;
+        for (int i = 0; i < (int)kids.size(); ++i)
+            if (kids[i]->l && kids[i]->box.halfArea() > area) {
+                area = kids[i]->box.halfArea();
+                best = i;
+            }
+        if (best < 0) break;
+        const TNode* open = kids[best];
+        kids[best] = open->l.get();
+        kids.insert(kids.begin() + best + 1, open->r.get());
+    }
+    uint32_t idx = (uint32_t)(nodes.size() / 8);
+    nodes.resize(nodes.size() + 8);
+    uint32_t refs[4];
+    for (size_t k = 0; k < kids.size(); ++k)
+        refs[k] = kids[k]->l ? flatten4(kids[k], nodes, dummyLeaf, depth + 1, maxDepth)
+                             : (kLeaf | (kids[k]->first << 3) | (kids[k]->count - 1u));
+    float4* rec = &nodes[8 * (size_t)idx];
+    Box far;
+    for (int a = 0; a < 3; ++a) far.mn[a] = far.mx[a] = 1e30f;
+    for (int k = 0; k < 4; ++k) {
+        if (k < (int)kids.size())
+            setChild4(rec, k, kids[k]->box, refs[k]);
+        else
+            setChild4(rec, k, far, dummyLeaf);
+    }
+    rec[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     return idx;
 }
 
@@ -256,17 +282,19 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
     isect[3 * (size_t)n + 1] = make_float4(0, 0, 0, asFloat(0u));
     isect[3 * (size_t)n + 2] = make_float4(0, 0, 0, 0);
     int maxDepth = 0;
-    if (!root->l) {  // single leaf: root record with the leaf and a far-away dummy child
-        nodes.resize(4);
-        setChild(&nodes[0], 0, root->box);
+    const uint32_t dummyLeaf = kLeaf | (n << 3);
+    if (!root->l) {  // single leaf: a root with the leaf and three dummy children
+        nodes.resize(8);
         Box far;
         for (int a = 0; a < 3; ++a) far.mn[a] = far.mx[a] = 1e30f;
-        setChild(&nodes[0], 1, far);
-        nodes[3] = make_float4(asFloat(kLeaf | (0u << 3) | (root->count - 1u)), asFloat(kLeaf | (n << 3)), 0, 0);
+        setChild4(&nodes[0], 0, root->box, kLeaf | (0u << 3) | (root->count - 1u));
+        for (int k = 1; k < 4; ++k) setChild4(&nodes[0], k, far, dummyLeaf);
+        nodes[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return DK_OK;
     }
-    flatten(root.get(), nodes, 0, maxDepth);
-    if (maxDepth >= 60) {
+    flatten4(root.get(), nodes, dummyLeaf, 0, maxDepth);
+    // Each level pushes at most three siblings on the 64-entry traversal stack.
+    if (3 * (maxDepth + 1) + 1 > 64) {
         err = "traversal BVH deeper than the 64-entry stack";
         return DK_ERROR_INVALID_SCENE;
     }

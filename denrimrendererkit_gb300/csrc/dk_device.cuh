@@ -71,6 +71,54 @@ __device__ __forceinline__ bool mtTest(float3 o, float3 d, float3 v0, float3 e1,
 
 __device__ __forceinline__ float3 rcp3(float3 d) { return f3(ex::rcp(d.x), ex::rcp(d.y), ex::rcp(d.z)); }
 
+// The children of a 4-wide node (8 x float4: x/y/z slab rows with one lane per
+// child, then the child references) whose boxes the ray enters no later than
+// `tmax`, nearest first.  Misses sort behind the hits with t = +inf.
+struct Wide {
+    uint32_t c0, c1, c2, c3;
+    float t0, t1, t2, t3;
+};
+
+__device__ __forceinline__ void wideSwap(uint32_t& ca, float& ta, uint32_t& cb, float& tb) {
+    if (tb < ta) {
+        float t = ta;
+        ta = tb;
+        tb = t;
+        uint32_t c = ca;
+        ca = cb;
+        cb = c;
+    }
+}
+
+__device__ __forceinline__ int wideVisit(const DevScene& S, uint32_t node, float3 o, float3 inv, float tmax, Wide& w) {
+    const float4* n = S.nodes + 8 * (size_t)node;
+    float4 lx = __ldg(n + 0), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3), lz = __ldg(n + 4),
+           hz = __ldg(n + 5);
+    uint4 ch = __ldg(reinterpret_cast<const uint4*>(n + 6));
+    float t;
+    w.c0 = ch.x;
+    w.t0 = childBox(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, o, inv, tmax, t) ? t : INFINITY;
+    w.c1 = ch.y;
+    w.t1 = childBox(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, o, inv, tmax, t) ? t : INFINITY;
+    w.c2 = ch.z;
+    w.t2 = childBox(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, o, inv, tmax, t) ? t : INFINITY;
+    w.c3 = ch.w;
+    w.t3 = childBox(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, o, inv, tmax, t) ? t : INFINITY;
+    int k = (w.t0 != INFINITY) + (w.t1 != INFINITY) + (w.t2 != INFINITY) + (w.t3 != INFINITY);
+    if (k > 1) {
+        wideSwap(w.c0, w.t0, w.c1, w.t1);
+        wideSwap(w.c2, w.t2, w.c3, w.t3);
+        wideSwap(w.c0, w.t0, w.c2, w.t2);
+        wideSwap(w.c1, w.t1, w.c3, w.t3);
+        wideSwap(w.c1, w.t1, w.c2, w.t2);
+    } else if (k == 1) {  // move the single hit to lane 0
+        if (w.t1 != INFINITY) { w.c0 = w.c1; w.t0 = w.t1; }
+        if (w.t2 != INFINITY) { w.c0 = w.c2; w.t0 = w.t2; }
+        if (w.t3 != INFINITY) { w.c0 = w.c3; w.t0 = w.t3; }
+    }
+    return k;
+}
+
 // Closest hit.  Returns argmin over (t, reference leaf slot): the reference's
 // strict `t < closest.t` under left-first DFS picks, among equal t, the
 // triangle that comes first in its primitiveIndices order, which is the slot.
@@ -89,26 +137,15 @@ __device__ HitRec traceClosest(const DevScene& S, float3 o, float3 d) {
     uint32_t node = 0;
     for (;;) {
         if ((node & kLeafBit) == 0) {
-            const float4* n = S.nodes + 4 * (size_t)node;
-            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
-            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
-            float tl, tr;
-            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, o, inv, best.t, tl);
-            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, o, inv, best.t, tr);
-            if (hl && hr) {
-                bool rFirst = tr < tl;
-                uint32_t nearC = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
-                uint32_t farC = rFirst ? (uint32_t)ch.x : (uint32_t)ch.y;
-                if (sp < kStackSize) {
-                    stackNode[sp] = (int)farC;
-                    stackT[sp] = rFirst ? tl : tr;
-                    ++sp;
-                }
-                node = nearC;
+            Wide w;
+            int k = wideVisit(S, node, o, inv, best.t, w);
+            if (k > 0) {
+                if (k > 3) { stackNode[sp] = (int)w.c3; stackT[sp] = w.t3; ++sp; }
+                if (k > 2) { stackNode[sp] = (int)w.c2; stackT[sp] = w.t2; ++sp; }
+                if (k > 1) { stackNode[sp] = (int)w.c1; stackT[sp] = w.t1; ++sp; }
+                node = w.c0;
                 continue;
             }
-            if (hl) { node = (uint32_t)ch.x; continue; }
-            if (hr) { node = (uint32_t)ch.y; continue; }
         } else {
             uint32_t first = (node & ~kLeafBit) >> 3;
             uint32_t cnt = (node & 7u) + 1u;
@@ -171,24 +208,15 @@ __device__ __forceinline__ bool closestSteps(const DevScene& S, ClosestState& st
                                              int budget) {
     for (int it = 0; it < budget; ++it) {
         if ((st.node & kLeafBit) == 0) {
-            const float4* n = S.nodes + 4 * (size_t)st.node;
-            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
-            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
-            float tl, tr;
-            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, st.o, st.inv, st.bestT, tl);
-            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, st.o, st.inv, st.bestT, tr);
-            if (hl && hr) {
-                bool rFirst = tr < tl;
-                if (st.sp < kStackSize) {
-                    stackNode[st.sp] = rFirst ? ch.x : ch.y;
-                    stackT[st.sp] = rFirst ? tl : tr;
-                    ++st.sp;
-                }
-                st.node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+            Wide w;
+            int k = wideVisit(S, st.node, st.o, st.inv, st.bestT, w);
+            if (k > 0) {
+                if (k > 3) { stackNode[st.sp] = (int)w.c3; stackT[st.sp] = w.t3; ++st.sp; }
+                if (k > 2) { stackNode[st.sp] = (int)w.c2; stackT[st.sp] = w.t2; ++st.sp; }
+                if (k > 1) { stackNode[st.sp] = (int)w.c1; stackT[st.sp] = w.t1; ++st.sp; }
+                st.node = w.c0;
                 continue;
             }
-            if (hl) { st.node = (uint32_t)ch.x; continue; }
-            if (hr) { st.node = (uint32_t)ch.y; continue; }
         } else {
             uint32_t first = (st.node & ~kLeafBit) >> 3;
             uint32_t cnt = (st.node & 7u) + 1u;
@@ -255,20 +283,15 @@ __device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float 
 __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* stackNode, int budget) {
     for (int it = 0; it < budget; ++it) {
         if ((st.node & kLeafBit) == 0) {
-            const float4* n = S.nodes + 4 * (size_t)st.node;
-            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
-            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
-            float tl, tr;
-            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, st.o, st.inv, st.tmax, tl);
-            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, st.o, st.inv, st.tmax, tr);
-            if (hl && hr) {
-                bool rFirst = tr < tl;
-                if (st.sp < kStackSize) stackNode[st.sp++] = rFirst ? ch.x : ch.y;
-                st.node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+            Wide w;
+            int k = wideVisit(S, st.node, st.o, st.inv, st.tmax, w);
+            if (k > 0) {
+                if (k > 3) stackNode[st.sp++] = (int)w.c3;
+                if (k > 2) stackNode[st.sp++] = (int)w.c2;
+                if (k > 1) stackNode[st.sp++] = (int)w.c1;
+                st.node = w.c0;
                 continue;
             }
-            if (hl) { st.node = (uint32_t)ch.x; continue; }
-            if (hr) { st.node = (uint32_t)ch.y; continue; }
         } else {
             uint32_t first = (st.node & ~kLeafBit) >> 3;
             uint32_t cnt = (st.node & 7u) + 1u;

@@ -355,7 +355,7 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
 #undef TRY
     D.tri_count = sc->triangle_count;
     D.mat_count = sc->material_count;
-    D.node_count = (uint32_t)(tNodes.size() / 4);
+    D.node_count = (uint32_t)(tNodes.size() / 8);
     D.all_shadow_opaque = allOpaque ? 1u : 0u;
     D.texdesc_count = sc->texture_descriptor_count;
     D.light_count = sc->lights ? sc->light_count : 0;

@@ -776,20 +776,15 @@ __device__ bool shadowLayers(const DevScene& S, MatTable mt, uint32_t opaqueMask
     if (S.node_count == 0) return false;
     for (;;) {
         if ((node & kLeafBit) == 0) {
-            const float4* n = S.nodes + 4 * (size_t)node;
-            float4 a = __ldg(n + 0), b = __ldg(n + 1), c = __ldg(n + 2);
-            int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
-            float tl, tr;
-            bool hl = childBox(a.x, a.y, a.z, a.w, c.x, c.y, o, inv, tmax, tl);
-            bool hr = childBox(b.x, b.y, b.z, b.w, c.z, c.w, o, inv, tmax, tr);
-            if (hl && hr) {
-                bool rFirst = tr < tl;
-                if (sp < kStackSize) stackNode[sp++] = rFirst ? ch.x : ch.y;
-                node = rFirst ? (uint32_t)ch.y : (uint32_t)ch.x;
+            Wide w;
+            int k = wideVisit(S, node, o, inv, tmax, w);
+            if (k > 0) {
+                if (k > 3) stackNode[sp++] = (int)w.c3;
+                if (k > 2) stackNode[sp++] = (int)w.c2;
+                if (k > 1) stackNode[sp++] = (int)w.c1;
+                node = w.c0;
                 continue;
             }
-            if (hl) { node = (uint32_t)ch.x; continue; }
-            if (hr) { node = (uint32_t)ch.y; continue; }
         } else {
             uint32_t first = (node & ~kLeafBit) >> 3;
             uint32_t cnt = (node & 7u) + 1u;

@@ -17,8 +17,9 @@ constexpr uint32_t kSortBins = 256;  // shading-order keys: 0 miss, 1 + material
 // Device copy of the scene.  `isect` holds 3 x float4 per BVH leaf slot:
 // (v0.xyz, reference slot), (v1 - v0, triangle index), (v2 - v0, flags with
 // bit 0 = blocks shadow rays under the scene's own materials and bits 8..15 =
-// min(material ID, 255)); `nodes` holds 4 x float4 per node: the x, y and z
-// slabs of both child boxes and the two child references.
+// min(material ID, 255)); `nodes` holds 8 x float4 per 4-wide node: x-min,
+// x-max, y-min, y-max, z-min, z-max rows with one lane per child, the four
+// child references, a spare row.
 struct DevScene {
     const dk_triangle* tris;
     const dk_material* mats;

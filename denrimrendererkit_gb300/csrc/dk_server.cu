@@ -177,9 +177,22 @@ int stepServer(Server* s, uint32_t* outJobs) {
         if (rc != DK_OK) return rc;
         uint64_t used = 0, pix = 0;
         const uint64_t cap = s->wave.cap;
-        for (uint64_t id : s->running) {
+        // Wave order: the oldest running job first (it always progresses), then
+        // the others by remaining paths, fewest first (policy 1), or in
+        // admission order (policy 0).
+        std::vector<uint64_t> order;
+        for (uint64_t id : s->running)
+            if (s->jobs[id]->state == DK_JOB_RUNNING) order.push_back(id);
+        if (s->cfg.policy == 1 && order.size() > 2) {
+            auto remaining = [&](uint64_t id) {
+                const Job& j = *s->jobs[id];
+                return (uint64_t)(j.samples - j.samplesDone) * j.settings.width * j.settings.height;
+            };
+            std::stable_sort(order.begin() + 1, order.end(),
+                             [&](uint64_t x, uint64_t y) { return remaining(x) < remaining(y); });
+        }
+        for (uint64_t id : order) {
             Job& j = *s->jobs[id];
-            if (j.state != DK_JOB_RUNNING) continue;
             if (table.size() >= s->cfg.max_jobs_per_wave) break;
             uint64_t pixels = (uint64_t)j.settings.width * j.settings.height;
             uint64_t room = (cap - used) / pixels;
@@ -316,6 +329,10 @@ int dk_server_create(const dk_scene* sc, const dk_server_config* config, dk_serv
     if (s->cfg.max_jobs_per_wave == 0) s->cfg.max_jobs_per_wave = 512;
     if (s->cfg.max_resident_jobs == 0) s->cfg.max_resident_jobs = 4096;
     if (s->cfg.samples_per_wave == 0) s->cfg.samples_per_wave = 64;
+    if (s->cfg.policy > 1) {
+        destroyServer(s);
+        return fail(DK_ERROR_INVALID_ARGUMENT, "dk_server_config.policy must be 0 or 1");
+    }
     s->cfg.wave_paths = std::min<uint32_t>(s->cfg.wave_paths, 0x7fffffffu);
 #define TRY(x)                  \
     do {                        \

@@ -30,6 +30,7 @@ class ServerConfig:
     max_jobs_per_wave: int = 512
     max_resident_jobs: int = 4096
     samples_per_wave: int = 64
+    policy: int = 1  # after the oldest running job: 0 admission order, 1 fewest remaining paths first
 
     def as_struct(self) -> abi.ServerConfig:
         c = abi.ServerConfig()
@@ -38,6 +39,7 @@ class ServerConfig:
         c.max_jobs_per_wave = int(self.max_jobs_per_wave)
         c.max_resident_jobs = int(self.max_resident_jobs)
         c.samples_per_wave = int(self.samples_per_wave)
+        c.policy = int(self.policy)
         return c
 
 

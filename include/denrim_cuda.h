@@ -489,7 +489,9 @@ typedef struct dk_server_config {
     uint32_t max_jobs_per_wave;    /* 0: 512                                                     */
     uint32_t max_resident_jobs;    /* admitted and not yet released; 0: 4096                     */
     uint32_t samples_per_wave;     /* samples one job advances per wave at most; 0: 64           */
-    uint32_t reserved[2];
+    uint32_t policy;               /* wave packing after the oldest running job: 0 admission      */
+                                   /* order, 1 fewest remaining paths first                       */
+    uint32_t reserved;
 } dk_server_config;
 
 /* One render request.  `materials` replaces the scene's material table for
