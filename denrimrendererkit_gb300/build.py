@@ -40,6 +40,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
     flags = [*ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread",
              "--expt-relaxed-constexpr"]
+    # Tuning knobs, e.g. DK_NVCC_DEFINES="DK_SHADE_MIN_BLOCKS=6 DK_LAYERS_MIN_BLOCKS=4".
+    flags += [f"-D{d}" for d in os.environ.get("DK_NVCC_DEFINES", "").split()]
 
     def compile_one(src: str) -> str:
         obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")

@@ -921,7 +921,10 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
 }
 
 // The layer walk for the rays the any-hit pass could not settle.
-__global__ void __launch_bounds__(128) k_shadow_layers(DevScene S, Wave W) {
+#ifndef DK_LAYERS_MIN_BLOCKS
+#define DK_LAYERS_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(128, DK_LAYERS_MIN_BLOCKS) k_shadow_layers(DevScene S, Wave W) {
     const uint32_t n = W.counts[6];
     const size_t cap = W.cap;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {

@@ -348,13 +348,17 @@ __device__ __noinline__ float3 evalBRDF(const Material& m, const ShadePoint& sp,
     float D = distributionGGXAnisotropicA(h, sp.n, sp.fr.tangent, sp.fr.bitangent, sp.specAlpha);
     float G = sp.g1vSpecAniso * g1AnisoA(l, sp.n, sp.fr.tangent, sp.fr.bitangent, sp.specAlpha);
     float3 specular = D * G * fresnel / fmaxf(4.0f * sp.nDotV * nDotL, 1e-5f);
+    // The clearcoat lobe is finite, so with clearcoat 0 its weighted term is
+    // exactly 0 and is skipped (a warp of one material takes one branch).
+    float3 diffuseBase = (f3(1.0f) - fresnel) * (1.0f - sp.metallic) * sp.baseColor * inversePi;
+    float3 sheen = evaluateMaterialSheenBRDF(m, sp.n, sp.v, l);
+    if (sp.clearcoat <= 0.0f) return diffuseBase + (specular + sheen);
     float3 ccFresnel = fresnelSchlick(vDotH, sp.ccF0) * tint;
     float ccD = distributionGGX(nDotH, sp.ccR);
     float ccG = sp.g1vCCIso * geometrySmithG1GGX(nDotL, sp.ccR);
     float3 ccSpecular = ccD * ccG * ccFresnel / fmaxf(4.0f * sp.nDotV * nDotL, 1e-5f);
     float3 ccAtt = clearcoatAttenuationAt(m, sp, l, ccFresnel, dot(hd, hd) > 1e-8f);
     float3 diffuse = ccAtt * (f3(1.0f) - fresnel) * (1.0f - sp.metallic) * sp.baseColor * inversePi;
-    float3 sheen = evaluateMaterialSheenBRDF(m, sp.n, sp.v, l);
     return diffuse + ccAtt * (specular + sheen) + ccSpecular * sp.clearcoat;
 }
 
@@ -370,7 +374,7 @@ __device__ __noinline__ float bsdfPDF(const ShadePoint& sp, float3 l) {  // :144
     float3 h = normalize(sp.v + l);
     float nDotH = fmaxf(dot(sp.n, h), 0.0f), vDotH = fmaxf(dot(sp.v, h), 0.0f);
     float specPDF = ggxPDFAt(sp, h, nDotH, vDotH, sp.specAlpha, sp.g1vSpecAniso);
-    float ccPDF = ggxPDFAt(sp, h, nDotH, vDotH, sp.ccAlpha, sp.g1vCCAniso);
+    float ccPDF = sp.cP > 0.0f ? ggxPDFAt(sp, h, nDotH, vDotH, sp.ccAlpha, sp.g1vCCAniso) : 0.0f;
     return sp.dP * (nDotL * 0.31830988618f) + sp.sP * specPDF + sp.cP * ccPDF;
 }
 
