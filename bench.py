@@ -63,6 +63,24 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(value: float, device: str) -> float:
+    """The maximum of a per-rank value over all ranks (identity when the
+    process group is not initialised): the step time the job is charged."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mpaths(paths_per_rank_step: float, world: int, slowest_ms: float) -> float:
+    """Replicas: every rank renders its own step; the job's throughput is all
+    ranks' paths over the slowest rank's step time."""
+    return paths_per_rank_step * world / (slowest_ms * 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -301,12 +319,8 @@ def run_gb300(args, rank, world, local):
     barrier()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
-    ms_step = dev_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms_step], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = paths_per_step * world / (ms_step * 1e3)
+    ms_step = max_over_ranks(dev_ms / args.steps, f"cuda:{local}")
+    value = whole_job_mpaths(paths_per_step, world, ms_step)
     beauty = session.pixels(RenderOutput.BEAUTY)
     session.close()
 
@@ -340,11 +354,7 @@ def run_gb300(args, rank, world, local):
             if i >= 1:
                 e2e_times.append(dt)
             flush_l2(flush)
-        e2e_s = sum(e2e_times) / len(e2e_times)
-        if world > 1:
-            t = torch.tensor([e2e_s], device=f"cuda:{local}")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times), f"cuda:{local}")
         e2e = {"value": paths_per_step * world / e2e_s / 1e6, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h),
                "note": "per step: dk_session_create from pinned host arrays + render 64 spp + beauty readback"}

@@ -868,7 +868,10 @@ __device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, f
 
 // Distance-volume closest hit for every ray of the queue, bounded by the
 // triangle hit k_extend found (the volume half of intersectScene).
-__global__ void __launch_bounds__(128) k_extend_volume(DevScene S, Wave W, uint32_t sel) {
+#ifndef DK_VOLUME_MIN_BLOCKS
+#define DK_VOLUME_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(DevScene S, Wave W, uint32_t sel) {
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
     VolumeScene V = volumeScene(S);
