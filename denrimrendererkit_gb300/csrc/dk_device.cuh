@@ -257,6 +257,9 @@ __device__ __forceinline__ bool blocksShadow(uint32_t flags, uint32_t mask) {
     return mid < 32u ? ((mask >> mid) & 1u) != 0u : (flags & 1u) != 0u;
 }
 
+// `rec` (may be null) receives the first kRecLayers non-opaque triangles the
+// query crosses as (t bits, slot); `recCount` counts them, `recOverflow` marks
+// more.
 struct AnyState {
     float3 o, d, inv;
     float tmax;
@@ -264,9 +267,13 @@ struct AnyState {
     uint32_t opaqueMask;
     int sp;
     bool sawNonOpaque;
+    bool recOverflow;
+    uint32_t recCount;
+    uint2* rec;
 };
 
-__device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float tmax, uint32_t opaqueMask) {
+__device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float tmax, uint32_t opaqueMask,
+                                        uint2* rec) {
     st.o = o;
     st.d = d;
     st.inv = rcp3(d);
@@ -275,6 +282,9 @@ __device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float 
     st.opaqueMask = opaqueMask;
     st.sp = 0;
     st.sawNonOpaque = false;
+    st.recOverflow = false;
+    st.recCount = 0;
+    st.rec = rec;
 }
 
 // Up to `budget` node visits of the any-hit query over shadow-blocking
@@ -302,6 +312,12 @@ __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* st
                 if (mtTest(st.o, st.d, xyz(a), xyz(b), xyz(c), t, u, v) && t < st.tmax) {
                     if (blocksShadow(__float_as_uint(c.w), st.opaqueMask)) return 2;
                     st.sawNonOpaque = true;
+                    if (st.rec) {
+                        if (st.recCount < kRecLayers)
+                            st.rec[st.recCount++] = make_uint2(__float_as_uint(t), i);
+                        else
+                            st.recOverflow = true;
+                    }
                 }
             }
         }

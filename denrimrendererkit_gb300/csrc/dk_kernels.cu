@@ -505,19 +505,33 @@ __global__ void __launch_bounds__(kSortBins) k_sort_scan(Wave W) {
     W.bins[t] = v[t] - x;
 }
 
+// Block b places queue entries [b * 2048, b * 2048 + 2048): ranks within the
+// block from shared-memory counters, one global reservation per (block, key).
+constexpr uint32_t kSortItems = 8;
 __global__ void __launch_bounds__(256) k_sort_scatter(Wave W, uint32_t sel) {
+    __shared__ uint32_t cnt[kSortBins];
+    __shared__ uint32_t base[kSortBins];
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
-    for (uint32_t i = globalId(); i < n; i += gridStride()) {
-        uint32_t k = W.keys[i];
-        unsigned active = __activemask();
-        unsigned peers = __match_any_sync(active, k);
-        int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if ((int)laneId() == leader) base = atomicAdd(&W.bins[k], (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        uint32_t rank = (uint32_t)__popc(peers & ((1u << laneId()) - 1u));
-        W.qsorted[base + rank] = q[i];
+    const uint32_t start = blockIdx.x * 256u * kSortItems;
+    if (start >= n) return;  // uniform over the block
+    for (uint32_t b = threadIdx.x; b < kSortBins; b += blockDim.x) cnt[b] = 0u;
+    __syncthreads();
+    uint32_t key[kSortItems], rank[kSortItems];
+#pragma unroll
+    for (uint32_t k = 0; k < kSortItems; ++k) {
+        uint32_t i = start + k * 256u + threadIdx.x;
+        key[k] = i < n ? W.keys[i] : 0u;
+        rank[k] = i < n ? atomicAdd(&cnt[key[k]], 1u) : 0u;
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < kSortBins; b += blockDim.x)
+        if (cnt[b]) base[b] = atomicAdd(&W.bins[b], cnt[b]);
+    __syncthreads();
+#pragma unroll
+    for (uint32_t k = 0; k < kSortItems; ++k) {
+        uint32_t i = start + k * 256u + threadIdx.x;
+        if (i < n) W.qsorted[base[key[k]] + rank[k]] = q[i];
     }
 }
 
@@ -757,16 +771,63 @@ __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
     }
 }
 
-// shadowOccluded (PathTrace.metal:4196-4274) for scenes with cut-out or
-// transmissive triangles, in one traversal: an opaque blocker anywhere in
-// (0.0005, maxDistance) occludes; otherwise the non-opaque layers are collected
-// in distance order and walked as the reference walks them (re-starting 0.001
-// past each layer, at most 8 steps, transmittance below 0.02 occludes).
+// The ordered walk of shadowOccluded (PathTrace.metal:4196-4274) over layers
+// collected in (distance, reference slot) order -- the order the reference's
+// repeated closest-hit queries meet them: restart 0.001 past each layer,
+// transmittance below 0.02 occludes.
+__device__ __noinline__ bool walkLayers(const DevScene& S, MatTable mt, float3 o, float3 d, const float* lt,
+                                        const uint32_t* ltri, const float* lu, const float* lv, int count, float3& T) {
+    float prev = 0.0f;
+    bool started = false;
+    Ray ray{o, d};
+    for (int i = 0; i < count; ++i) {
+        float a = lt[i];
+        if (started && a <= prev + 0.0015f) continue;  // inside the 0.001 restart gap + 0.0005 epsilon
+        float trel = started ? a - (prev + 0.001f) : a;
+        HitRec r{a, ltri[i], lu[i], lv[i]};
+        Hit h = makeHit(S, ray, r);
+        Material sm = materialForHit(S, mt, h);
+        prev = a;
+        started = true;
+        if (sm.baseColor.w <= 0.001f) continue;
+        float transmission = materialTransmission(sm);
+        bool insideSolid = !h.frontFacing && !materialThinWalled(sm);
+        float3 medium = (materialHasVolumeScattering(sm) && insideSolid)
+                            ? exp3((-materialVolumeSigmaT(sm)) * trel)
+                            : materialTransmissionAbsorption(sm, trel, insideSolid);
+        T *= materialTransmissionTint(sm, 0.35f) * medium * transmission;
+        if (maxComponent(T) < 0.02f) return true;
+    }
+    return false;
+}
+
+// Inserts a layer into (t, slot) order.
+__device__ __forceinline__ void insertLayer(float* lt, uint32_t* ltri, uint32_t* lslot, float* lu, float* lv,
+                                            int& count, float t, uint32_t tri, uint32_t slot, float u, float v) {
+    int j = count++;
+    while (j > 0 && (lt[j - 1] > t || (lt[j - 1] == t && lslot[j - 1] > slot))) {
+        lt[j] = lt[j - 1];
+        ltri[j] = ltri[j - 1];
+        lslot[j] = lslot[j - 1];
+        lu[j] = lu[j - 1];
+        lv[j] = lv[j - 1];
+        --j;
+    }
+    lt[j] = t;
+    ltri[j] = tri;
+    lslot[j] = slot;
+    lu[j] = u;
+    lv[j] = v;
+}
+
+// shadowOccluded for scenes with cut-out or transmissive triangles, in one
+// traversal: an opaque blocker anywhere in (0.0005, maxDistance) occludes;
+// otherwise the non-opaque layers are collected and walked.
 __device__ bool shadowLayers(const DevScene& S, MatTable mt, uint32_t opaqueMask, float3 o, float3 d, float tmax,
                              float3& T) {
     constexpr int kMaxLayers = 8;
     float lt[kMaxLayers];
-    uint32_t ltri[kMaxLayers];
+    uint32_t ltri[kMaxLayers], lslot[kMaxLayers];
     float lu[kMaxLayers], lv[kMaxLayers];
     int count = 0;
     float3 inv = rcp3(d);
@@ -795,45 +856,32 @@ __device__ bool shadowLayers(const DevScene& S, MatTable mt, uint32_t opaqueMask
                 if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) || !(t < tmax)) continue;
                 if (blocksShadow(__float_as_uint(c.w), opaqueMask)) return true;  // opaque blocker
                 if (count == kMaxLayers - 1) return true;    // an 8th layer: the walk ends occluded
-                int j = count++;
-                while (j > 0 && lt[j - 1] > t) {
-                    lt[j] = lt[j - 1];
-                    ltri[j] = ltri[j - 1];
-                    lu[j] = lu[j - 1];
-                    lv[j] = lv[j - 1];
-                    --j;
-                }
-                lt[j] = t;
-                ltri[j] = __float_as_uint(b.w);
-                lu[j] = u;
-                lv[j] = v;
+                insertLayer(lt, ltri, lslot, lu, lv, count, t, __float_as_uint(b.w), __float_as_uint(a.w), u, v);
             }
         }
         if (sp == 0) break;
         node = (uint32_t)stackNode[--sp];
     }
-    float prev = 0.0f;
-    bool started = false;
-    Ray ray{o, d};
-    for (int i = 0; i < count; ++i) {
-        float a = lt[i];
-        if (started && a <= prev + 0.0015f) continue;  // inside the 0.001 restart gap + 0.0005 epsilon
-        float trel = started ? a - (prev + 0.001f) : a;
-        HitRec r{a, ltri[i], lu[i], lv[i]};
-        Hit h = makeHit(S, ray, r);
-        Material sm = materialForHit(S, mt, h);
-        prev = a;
-        started = true;
-        if (sm.baseColor.w <= 0.001f) continue;
-        float transmission = materialTransmission(sm);
-        bool insideSolid = !h.frontFacing && !materialThinWalled(sm);
-        float3 medium = (materialHasVolumeScattering(sm) && insideSolid)
-                            ? exp3((-materialVolumeSigmaT(sm)) * trel)
-                            : materialTransmissionAbsorption(sm, trel, insideSolid);
-        T *= materialTransmissionTint(sm, 0.35f) * medium * transmission;
-        if (maxComponent(T) < 0.02f) return true;
+    return walkLayers(S, mt, o, d, lt, ltri, lu, lv, count, T);
+}
+
+// The same walk over the (at most kRecLayers) layers the any-hit pass
+// recorded: each recorded triangle slot is intersected again with the same
+// arithmetic, which reproduces its (t, u, v).
+__device__ bool recordedLayers(const DevScene& S, MatTable mt, float3 o, float3 d, const uint2* rec, uint32_t n,
+                               float3& T) {
+    float lt[kRecLayers];
+    uint32_t ltri[kRecLayers], lslot[kRecLayers];
+    float lu[kRecLayers], lv[kRecLayers];
+    int count = 0;
+    for (uint32_t k = 0; k < n && k < kRecLayers; ++k) {
+        const float4* q = S.isect + 3 * (size_t)rec[k].y;
+        float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+        float t, u, v;
+        if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v)) continue;
+        insertLayer(lt, ltri, lslot, lu, lv, count, t, __float_as_uint(b.w), __float_as_uint(a.w), u, v);
     }
-    return false;
+    return walkLayers(S, mt, o, d, lt, ltri, lu, lv, count, T);
 }
 
 // shadowOccluded (PathTrace.metal:4196-4274) exactly as the reference walks
@@ -869,7 +917,7 @@ __device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, f
 // Distance-volume closest hit for every ray of the queue, bounded by the
 // triangle hit k_extend found (the volume half of intersectScene).
 #ifndef DK_VOLUME_MIN_BLOCKS
-#define DK_VOLUME_MIN_BLOCKS 1
+#define DK_VOLUME_MIN_BLOCKS 3
 #endif
 __global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(DevScene S, Wave W, uint32_t sel) {
     const uint32_t* q = W.q[sel];
@@ -903,7 +951,8 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
             e = W.qr[idx];
             size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
             float4 o = W.nee_o[slot], d = W.nee_d[slot];
-            anyInit(st, xyz(o), xyz(d), o.w, __ldg(&W.jobs[jobOf(W, e >> 2)].opaque_mask));
+            anyInit(st, xyz(o), xyz(d), o.w, __ldg(&W.jobs[jobOf(W, e >> 2)].opaque_mask),
+                    S.volume_count ? nullptr : W.layer_hits + slot * kRecLayers);
         }
         if (__all_sync(0xffffffffu, e == kNoWork && exhausted)) break;
         if (e == kNoWork) continue;
@@ -914,6 +963,7 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
         if (r == 2) {
             W.nee_c[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         } else if (st.sawNonOpaque) {
+            W.layer_count[slot] = st.recCount | (st.recOverflow ? 0x80000000u : 0u);
             W.qr2[atomicAdd(&W.counts[6], 1u)] = e;
         } else {
             float4 c = W.nee_c[slot];
@@ -923,7 +973,8 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
     }
 }
 
-// The layer walk for the rays the any-hit pass could not settle.
+// The layer walk for the rays the any-hit pass could not settle: from the
+// layers it recorded, or by a collecting traversal when it crossed more.
 #ifndef DK_LAYERS_MIN_BLOCKS
 #define DK_LAYERS_MIN_BLOCKS 4
 #endif
@@ -937,8 +988,15 @@ __global__ void __launch_bounds__(128, DK_LAYERS_MIN_BLOCKS) k_shadow_layers(Dev
         float3 T = f3(1.0f);
         const DevJob& J = W.jobs[jobOf(W, e >> 2)];
         const MatTable mt = matTable(J);
-        bool occluded = S.volume_count ? shadowWalk(S, mt, xyz(o), xyz(d), o.w, T)
-                                       : shadowLayers(S, mt, __ldg(&J.opaque_mask), xyz(o), xyz(d), o.w, T);
+        bool occluded;
+        if (S.volume_count) {
+            occluded = shadowWalk(S, mt, xyz(o), xyz(d), o.w, T);
+        } else {
+            uint32_t lc = W.layer_count[slot];
+            occluded = (lc & 0x80000000u)
+                           ? shadowLayers(S, mt, __ldg(&J.opaque_mask), xyz(o), xyz(d), o.w, T)
+                           : recordedLayers(S, mt, xyz(o), xyz(d), W.layer_hits + slot * kRecLayers, lc, T);
+        }
         float3 v = occluded ? f3(0.0f) : xyz(c) * T / c.w;
         W.nee_c[slot] = make_float4(v.x, v.y, v.z, 0.0f);
     }
@@ -1233,7 +1291,7 @@ cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint3
     if (sorted) {
         k_sort_count<<<grid, 256, 0, st>>>(S, W, sel);
         k_sort_scan<<<1, kSortBins, 0, st>>>(W);
-        k_sort_scatter<<<grid, 256, 0, st>>>(W, sel);
+        k_sort_scatter<<<(W.cap + 256u * kSortItems - 1u) / (256u * kSortItems), 256, 0, st>>>(W, sel);
     }
     if (S.volume_count)
         k_shade<true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);

@@ -12,7 +12,8 @@
 namespace dk {
 
 constexpr uint32_t kNoSlot = 0xffffffffu;
-constexpr uint32_t kSortBins = 256;  // shading-order keys: 0 miss, 1 + material ID (< 254), 255 other
+constexpr uint32_t kSortBins = 256;
+constexpr uint32_t kRecLayers = 4;   // non-opaque layers the any-hit pass records per shadow ray  // shading-order keys: 0 miss, 1 + material ID (< 254), 255 other
 
 // Device copy of the scene.  `isect` holds 3 x float4 per BVH leaf slot:
 // (v0.xyz, reference slot), (v1 - v0, triangle index), (v2 - v0, flags with
@@ -110,6 +111,8 @@ struct Wave {
     uint32_t* counts;  // [0], [1] queue lengths, [2] shadow paths, [3] shadow rays, [4] extend cursor,
                        // [5] shadow cursor, [6] layer-walk rays, [7] spare
     float4* aov;       // 4 planes of aov_stride tile pixels: primary-hit record of each job's last sample
+    uint2* layer_hits;      // kRecLayers per shadow-ray slot: (t bits, triangle slot) of crossed non-opaque triangles
+    uint32_t* layer_count;  // per shadow-ray slot: recorded layers, bit 31 = more than kRecLayers
     uint32_t* qsorted; // the active queue reordered by material (the shading order)
     uint32_t* keys;    // material key of each active-queue entry
     uint32_t* bins;    // kSortBins + 1 counters: key histogram, then bucket cursors
