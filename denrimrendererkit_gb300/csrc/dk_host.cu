@@ -363,6 +363,16 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
     D.env_tex_plus1 = sc->environment_texture_index_plus_one;
     D.env_intensity = sc->environment_intensity;
     D.env_rot_y = sc->environment_rotation_y;
+    {
+        float* dsc = nullptr;
+        int rc = arena.alloc(&dsc, 2, "environment rotation");
+        if (rc != DK_OK) return rc;
+        DK_CUDA(envRotation(D.env_rot_y, dsc, 0), "environment rotation");
+        float hsc[2];
+        DK_CUDA(cudaMemcpy(hsc, dsc, sizeof(hsc), cudaMemcpyDeviceToHost), "environment rotation");
+        D.env_rot_sin = hsc[0];
+        D.env_rot_cos = hsc[1];
+    }
     D.env_max_radiance = sc->environment_max_radiance;
     return DK_OK;
 }
@@ -620,7 +630,7 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     uint64_t capPaths = 1ull << 24;  // 16.8 M paths (~3.5 GB of path state)
     if (st->max_samples_per_launch > 0) capPaths = std::min<uint64_t>(capPaths, (uint64_t)st->max_samples_per_launch * pixels);
     capPaths = std::max<uint64_t>(capPaths, pixels);
-    capPaths = std::min<uint64_t>(capPaths, 0x7fffffffull);
+    capPaths = std::min<uint64_t>(capPaths, 1ull << 29);  // path indices fit 29 bits of the NEE record
     TRY(dk::allocWave(s->arena, s->wave, capPaths, pixels, 1));
     s->jobs = const_cast<dk::DevJob*>(s->wave.jobs);
     TRY(dk::allocAccum(s->arena, s->accum, pixels));

@@ -540,7 +540,7 @@ struct ShadeOut { bool survive; uint32_t neeMask; uint32_t maxBounces; };
 // The body of the reference bounce loop (PathTrace.metal:5252-5518) for one
 // path whose closest hit is already in W.hit.
 template <bool kVolumes>
-__device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint32_t bounce) {
+__device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint32_t i, uint32_t bounce) {
     float4 ro = W.ray_o[p], rd = W.ray_d[p], tpw = W.tp[p], radw = W.rad[p], hr = W.hit[p];
     uint2 rs = W.rng[p];
     const DevJob& J = W.jobs[rs.y >> 8];
@@ -633,6 +633,9 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
     makeShadePoint(sp, m, h.normal, h.tangent, h.bitangent, view);
     float3 shadowOrigin = h.position + h.normal * 0.001f;
     const size_t cap = W.cap;
+    // NEE slots are indexed by shading order `i` (coalesced); the slot's
+    // direction.w carries the path's job, nee_tp.w the slot mask | path << 3.
+    const float jobBits = __uint_as_float(rs.y >> 8);
     if (S.light_count > 0u) {
         uint32_t index = selectLightIndex(S, randomFloat(state));
         const dk_light_record& L = S.lights[index];
@@ -659,9 +662,9 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
                     float G = cosS * cosL * area / fmaxf(d2, 1e-6f);
                     float3 c = evalBRDF(m, sp, ld) * le * G * mis;
                     if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f)) {
-                        W.nee_o[p] = make_float4(shadowOrigin.x, shadowOrigin.y, shadowOrigin.z, dist - 0.002f);
-                        W.nee_d[p] = make_float4(ld.x, ld.y, ld.z, 0.0f);
-                        W.nee_c[p] = make_float4(c.x, c.y, c.z, selPdf);
+                        W.nee_o[i] = make_float4(shadowOrigin.x, shadowOrigin.y, shadowOrigin.z, dist - 0.002f);
+                        W.nee_d[i] = make_float4(ld.x, ld.y, ld.z, jobBits);
+                        W.nee_c[i] = make_float4(c.x, c.y, c.z, selPdf);
                         out.neeMask |= 1u;
                     }
                 }
@@ -681,15 +684,15 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
             float mis = powerHeuristic(envPdf, bsdfPdf);
             float3 c = evalBRDF(m, sp, dir) * sampleEnvironment(S, dir) * cosS * mis;
             if (!(c.x == 0.0f && c.y == 0.0f && c.z == 0.0f)) {
-                size_t slot = (size_t)(1u + e) * cap + p;
+                size_t slot = (size_t)(1u + e) * cap + i;
                 W.nee_o[slot] = make_float4(shadowOrigin.x, shadowOrigin.y, shadowOrigin.z, 1.0e20f);
-                W.nee_d[slot] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                W.nee_d[slot] = make_float4(dir.x, dir.y, dir.z, jobBits);
                 W.nee_c[slot] = make_float4(c.x, c.y, c.z, envPdf * 2.0f);
                 out.neeMask |= 2u << e;
             }
         }
     }
-    if (out.neeMask) W.nee_tp[p] = make_float4(tp.x, tp.y, tp.z, __uint_as_float(out.neeMask));
+    if (out.neeMask) W.nee_tp[i] = make_float4(tp.x, tp.y, tp.z, __uint_as_float(out.neeMask | (p << 3)));
 
     // --------------------------------------------- BSDF sampling ----------
     float c0 = randomFloat(state);
@@ -756,17 +759,17 @@ __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
     if (globalId() == 0) W.counts[4] = 0u;  // extend cursor of the next bounce
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
         uint32_t p = q[i];
-        ShadeOut o = shadePath<kVolumes>(S, W, p, bounce);
+        ShadeOut o = shadePath<kVolumes>(S, W, p, i, bounce);
         bool keep = o.survive && bounce + 1u < o.maxBounces;
         uint32_t slot = warpAppend(&W.counts[sel ^ 1u], keep);
         if (keep) qNext[slot] = p;
         bool sh = o.neeMask != 0u;
         uint32_t sslot = warpAppend(&W.counts[2], sh);
-        if (sh) W.qs[sslot] = p;
+        if (sh) W.qs[sslot] = i;
         for (uint32_t k = 0; k < 3u; ++k) {
             bool has = (o.neeMask >> k) & 1u;
             uint32_t r = warpAppend(&W.counts[3], has);
-            if (has) W.qr[r] = (p << 2) | k;
+            if (has) W.qr[r] = (i << 2) | k;
         }
     }
 }
@@ -951,7 +954,7 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
             e = W.qr[idx];
             size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
             float4 o = W.nee_o[slot], d = W.nee_d[slot];
-            anyInit(st, xyz(o), xyz(d), o.w, __ldg(&W.jobs[jobOf(W, e >> 2)].opaque_mask),
+            anyInit(st, xyz(o), xyz(d), o.w, __ldg(&W.jobs[__float_as_uint(d.w)].opaque_mask),
                     S.volume_count ? nullptr : W.layer_hits + slot * kRecLayers);
         }
         if (__all_sync(0xffffffffu, e == kNoWork && exhausted)) break;
@@ -986,7 +989,7 @@ __global__ void __launch_bounds__(128, DK_LAYERS_MIN_BLOCKS) k_shadow_layers(Dev
         size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
         float4 o = W.nee_o[slot], d = W.nee_d[slot], c = W.nee_c[slot];
         float3 T = f3(1.0f);
-        const DevJob& J = W.jobs[jobOf(W, e >> 2)];
+        const DevJob& J = W.jobs[__float_as_uint(d.w)];
         const MatTable mt = matTable(J);
         bool occluded;
         if (S.volume_count) {
@@ -1009,12 +1012,13 @@ __global__ void __launch_bounds__(256) k_resolve(Wave W) {
     const uint32_t n = W.counts[2];
     const size_t cap = W.cap;
     for (uint32_t i = globalId(); i < n; i += gridStride()) {
-        uint32_t p = W.qs[i];
-        float4 tpw = W.nee_tp[p];
-        uint32_t mask = __float_as_uint(tpw.w);
+        uint32_t si = W.qs[i];
+        float4 tpw = W.nee_tp[si];
+        uint32_t bits = __float_as_uint(tpw.w);
+        uint32_t mask = bits & 7u, p = bits >> 3;
         float3 direct = f3(0.0f);
         for (uint32_t k = 0; k < 3u; ++k)
-            if (mask & (1u << k)) direct += xyz(W.nee_c[k * cap + p]);
+            if (mask & (1u << k)) direct += xyz(W.nee_c[k * cap + si]);
         float4 r = W.rad[p];
         float3 add = clampSampleContribution(xyz(tpw) * direct, __ldg(&W.jobs[jobOf(W, p)].P.clamp));
         W.rad[p] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
@@ -1268,6 +1272,20 @@ cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int gri
     if (S.volume_count) k_extend_volume<<<grid, 128, 0, st>>>(S, W, sel);
     return cudaGetLastError();
 }
+// The environment rotation's sine and cosine with the device's sincosf, the
+// values every environment lookup of the reference computes per call.
+__global__ void k_env_rotation(float radians, float* out) {
+    float sn, cs;
+    sincosf(radians, &sn, &cs);
+    out[0] = sn;
+    out[1] = cs;
+}
+
+cudaError_t envRotation(float radians, float* sinCos, cudaStream_t st) {
+    k_env_rotation<<<1, 1, 0, st>>>(radians, sinCos);
+    return cudaGetLastError();
+}
+
 int g_sortMaterials = -1;  // -1: from DK_SORT_MATERIALS (default on)
 
 // Kernels one bounce launches (extend, shade, shadow, resolve stages).

@@ -35,6 +35,7 @@ struct DevScene {
     uint32_t light_count, env_count, env_tex_plus1, all_shadow_opaque;
     float env_intensity, env_rot_y, env_max_radiance;
     uint32_t env_guide_size;
+    float env_rot_sin, env_rot_cos;  // sincosf(env_rot_y), evaluated once on the device
     // Sparse distance volumes (GPUVolumeDescriptor with metadata.w == 1).
     const dk_volume_descriptor* volumes;
     const dk_volume_brick_descriptor* bricks;
@@ -100,13 +101,14 @@ struct Wave {
     float4* rad;       // radiance, w = alpha
     uint2* rng;        // RNG state, flags (bit 0: primary hit found; bits 8..31: job index)
     float4* hit;       // t, triangle, u, v
+    // NEE slots are indexed by the path's position in the shading order.
     float4* nee_o;     // 3 slots x cap: shadow origin, w = max distance
-    float4* nee_d;     // 3 slots x cap: shadow direction
+    float4* nee_d;     // 3 slots x cap: shadow direction, w = job index (bits)
     float4* nee_c;     // 3 slots x cap: unshadowed contribution, w = pdf divisor
-    float4* nee_tp;    // throughput at NEE, w = slot mask
+    float4* nee_tp;    // throughput at NEE, w = slot mask | path index << 3 (bits)
     uint32_t* q[2];    // active path queues (ping-pong)
-    uint32_t* qs;      // paths with shadow queries
-    uint32_t* qr;      // shadow rays: path << 2 | slot (3 x cap entries)
+    uint32_t* qs;      // shading-order indices of paths with shadow queries
+    uint32_t* qr;      // shadow rays: shading-order index << 2 | slot (3 x cap entries)
     uint32_t* qr2;     // shadow rays that need the layer walk (3 x cap entries)
     uint32_t* counts;  // [0], [1] queue lengths, [2] shadow paths, [3] shadow rays, [4] extend cursor,
                        // [5] shadow cursor, [6] layer-walk rays, [7] spare
@@ -138,6 +140,7 @@ cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchAovPrimary(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchFinalize(const Wave& W, int grid, cudaStream_t st);
 uint32_t bounceLaunches(const DevScene& S);
+cudaError_t envRotation(float radians, float* sinCos /* device, 2 floats */, cudaStream_t st);
 cudaError_t launchResolveBeauty(const Accum& A, uint32_t pixels, float4* out, int grid, cudaStream_t st);
 cudaError_t buildEnvironmentTable(const float4* dPixels, uint32_t w, uint32_t h, float intensity, float maxR,
                                   double* dWeights, double* dPrefix, double* dBlockSums, float2* dOut, int grid,

@@ -333,7 +333,7 @@ int dk_server_create(const dk_scene* sc, const dk_server_config* config, dk_serv
         destroyServer(s);
         return fail(DK_ERROR_INVALID_ARGUMENT, "dk_server_config.policy must be 0 or 1");
     }
-    s->cfg.wave_paths = std::min<uint32_t>(s->cfg.wave_paths, 0x7fffffffu);
+    s->cfg.wave_paths = std::min<uint32_t>(s->cfg.wave_paths, 1u << 29);  // path indices fit 29 bits
 #define TRY(x)                  \
     do {                        \
         int _rc = (x);          \

@@ -490,7 +490,8 @@ __device__ __forceinline__ float3 fallbackSky(float3 d) {  // :3765-3768
     return mix3(f3(0.02f, 0.025f, 0.035f), f3(0.25f, 0.32f, 0.45f), sky);
 }
 __device__ __forceinline__ float3 rotateEnv(const DevScene& S, float3 d, float& sn, float& cs) {
-    sincosf(S.env_rot_y, &sn, &cs);
+    sn = S.env_rot_sin;
+    cs = S.env_rot_cos;
     return normalize(f3(cs * d.x - sn * d.z, d.y, sn * d.x + cs * d.z));
 }
 __device__ __noinline__ float3 sampleEnvironment(const DevScene& S, float3 d) {  // :3770-3802
@@ -559,8 +560,7 @@ __device__ __noinline__ float3 sampleEnvironmentDirection(const DevScene& S, flo
     sincosf(phi, &sp, &cp);
     sincosf(theta, &st, &ct);
     float3 local = normalize(f3(cp * st, ct, sp * st));
-    float sn, cs;
-    sincosf(S.env_rot_y, &sn, &cs);
+    float sn = S.env_rot_sin, cs = S.env_rot_cos;
     pdf = fmaxf(__ldg(&S.env[index].y), 0.0f);
     return normalize(f3(cs * local.x + sn * local.z, local.y, -sn * local.x + cs * local.z));
 }
