@@ -9,12 +9,20 @@
 // binned-SAH binary tree built here (`buildSahTraversal`); the kernels return
 // the argmin over (t, slot), which is the reference's answer.
 //
-// Output layout (see dk_kernels.h): the binary SAH tree collapsed into 4-wide
-// nodes of 8 x float4 (the x, y, z slabs of four children, one lane each, and
-// the four child references: interior index, or 0x80000000 | first << 3 |
-// (count - 1) for a leaf of <= 8 slots); 3 x float4 per leaf slot: (v0,
-// reference slot), (v1 - v0, triangle index), (v2 - v0, flags: bit 0 = blocks
-// shadow rays, bits 8..15 material ID); one dummy slot at the end.
+// Output layouts (`width`):
+// * 4 (the default): the binary SAH tree (leaves of <= 8 triangles) collapsed
+//   into 4-wide nodes of 8 x float4 (the x, y, z slabs of four children, one
+//   lane each, and the four child references: interior index, or 0x80000000 |
+//   first << 3 | (count - 1) for a leaf); one dummy slot at the end;
+// * 8: the binary SAH tree (leaves of <= 4 triangles) collapsed into 8-wide
+//   nodes of 5 x 16 bytes with child boxes quantised to 8 bits per bound
+//   (record layout at `Quantizer` below; the compressed wide BVH of Ylitie,
+//   Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+//   Compressed Wide BVHs", HPG 2017, with an encoding of this file's own), the
+//   slots of a node's leaves consecutive.
+// Both: 3 x float4 per leaf slot: (v0, reference slot), (v1 - v0, triangle
+// index), (v2 - v0, flags: bit 0 = blocks shadow rays, bits 8..15 material
+// ID).
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -31,7 +39,6 @@ namespace dk {
 namespace {
 
 constexpr uint32_t kLeaf = 0x80000000u;
-constexpr uint32_t kMaxLeaf = 8;
 constexpr int kBins = 32;
 
 inline float asFloat(uint32_t u) {
@@ -65,21 +72,19 @@ struct Box {
 struct TNode {
     Box box;
     std::unique_ptr<TNode> l, r;
-    uint32_t first = 0, count = 0;
+    uint32_t first = 0, count = 0;  // triangle range of the subtree (in SAH order)
 };
 
-std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth) {
+std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth, uint32_t maxLeaf) {
     auto node = std::make_unique<TNode>();
+    node->first = first;
+    node->count = n;
     Box cb;
     for (uint32_t i = first; i < first + n; ++i) {
         node->box.grow(p[i].mn, p[i].mx);
         cb.grow(p[i].c, p[i].c);
     }
-    auto makeLeaf = [&]() {
-        node->first = first;
-        node->count = n;
-        return std::move(node);
-    };
+    auto makeLeaf = [&]() { return std::move(node); };
     if (n == 1) return makeLeaf();
     // Binned SAH over the three axes (traversal cost 1, intersection cost 1).
     float bestCost = FLT_MAX;
@@ -121,7 +126,7 @@ std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth) {
     }
     float nodeArea = node->box.halfArea();
     float splitCost = 1.0f + (nodeArea > 0.0f ? bestCost / nodeArea : 0.0f);
-    if (n <= kMaxLeaf && (bestAxis < 0 || (float)n <= splitCost)) return makeLeaf();
+    if (n <= maxLeaf && (bestAxis < 0 || (float)n <= splitCost)) return makeLeaf();
     uint32_t mid;
     if (bestAxis < 0) {  // coincident centroids: split the range in half
         mid = first + n / 2;
@@ -137,12 +142,12 @@ std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth) {
         if (mid == first || mid == first + n) mid = first + n / 2;
     }
     if (n > 65536 && depth < 6) {
-        auto fut = std::async(std::launch::async, [=] { return build(p, first, mid - first, depth + 1); });
-        node->r = build(p, mid, first + n - mid, depth + 1);
+        auto fut = std::async(std::launch::async, [=] { return build(p, first, mid - first, depth + 1, maxLeaf); });
+        node->r = build(p, mid, first + n - mid, depth + 1, maxLeaf);
         node->l = fut.get();
     } else {
-        node->l = build(p, first, mid - first, depth + 1);
-        node->r = build(p, mid, first + n - mid, depth + 1);
+        node->l = build(p, first, mid - first, depth + 1, maxLeaf);
+        node->r = build(p, mid, first + n - mid, depth + 1, maxLeaf);
     }
     return node;
 }
@@ -197,6 +202,181 @@ uint32_t flatten4(const TNode* t, std::vector<float4>& nodes, uint32_t dummyLeaf
     return idx;
 }
 
+// 8-wide node record (5 x 16 bytes):
+//   word 0: origin p (3 x f32: the node box minimum), then one byte each of
+//           the biased exponents of the x, y, z quantisation steps and the
+//           mask of interior children (bit = slot);
+//   word 1: index of the first interior child node, index of the first leaf
+//           slot, and one byte per child slot: (count << 5) | offset of the
+//           leaf's triangles from the first leaf slot (0 for interior and
+//           empty slots);
+//   words 2-4: per child slot, 8-bit box bounds lo.x, lo.y, lo.z, hi.x, hi.y,
+//           hi.z (8 bytes each, slot s in byte s), i.e. the box
+//           p + q * 2^(E - 127) per axis, rounded outwards.
+// Interior children are stored consecutively from the first child index in
+// slot order, and so are the leaves' triangles from the first leaf slot.
+// The child in slot s is the one lying furthest towards the box corner s (bit
+// a of s set = high side on axis a), so a ray whose direction signs form s
+// meets slot s first; the traversal visits slots in the order (slot ^ s).
+struct Quantizer {
+    float p[3];
+    double e[3];
+    uint32_t E[3];
+    explicit Quantizer(const Box& b) {
+        for (int a = 0; a < 3; ++a) {
+            p[a] = b.mn[a];
+            double ext = (double)b.mx[a] - (double)b.mn[a];
+            int k = -126;
+            if (ext > 0.0) {
+                k = (int)std::ceil(std::log2(ext / 255.0));
+                while (std::ldexp(1.0, k) * 255.0 <= ext) ++k;  // strictly above: the top plane keeps a margin
+                while (k > -126 && std::ldexp(1.0, k - 1) * 255.0 > ext) --k;
+            }
+            k = std::max(-126, std::min(127, k));
+            E[a] = (uint32_t)(k + 127);
+            e[a] = std::ldexp(1.0, k);
+        }
+    }
+    // Outward-rounded bounds of `b`; a bound that falls exactly on a grid
+    // plane is moved one step out (except the node's own minimum plane, which
+    // the traversal evaluates exactly), so child boxes keep a margin.
+    void quantize(const Box& b, int a, uint32_t& lo, uint32_t& hi) const {
+        double rl = ((double)b.mn[a] - (double)p[a]) / e[a];
+        double rh = ((double)b.mx[a] - (double)p[a]) / e[a];
+        double ql = std::floor(rl), qh = std::ceil(rh);
+        if (ql == rl && ql > 0.0) ql -= 1.0;
+        if (qh == rh && qh < 255.0) qh += 1.0;
+        lo = (uint32_t)std::max(0.0, std::min(255.0, ql));
+        hi = (uint32_t)std::max(0.0, std::min(255.0, qh));
+    }
+};
+
+// A leaf of the 8-wide tree: a binary leaf, or a subtree of at most
+// DK_WIDE_LEAF_MERGE triangles (consecutive in SAH order; at most 4).
+// Merging fills the nodes but tests more triangles per ray; the default
+// keeps the SAH leaves.
+#ifndef DK_WIDE_LEAF_MERGE
+#define DK_WIDE_LEAF_MERGE 1
+#endif
+inline bool wideLeaf(const TNode* t) { return !t->l || t->count <= DK_WIDE_LEAF_MERGE; }
+
+struct Wide8Builder {
+    const std::vector<Prim>& prims;   // SAH order: leaf ranges index it
+    const dk_scene* sc;
+    const std::vector<uint32_t>& slotOfTri;
+    const std::vector<uint8_t>& opaque;
+    std::vector<float4>& nodes;       // 5 x float4 per node
+    std::vector<float4>& isect;       // 3 x float4 per leaf slot
+    int maxDepth = 0;
+
+    uint32_t appendTriangles(const TNode* leaf) {
+        uint32_t first = (uint32_t)(isect.size() / 3);
+        for (uint32_t k = leaf->first; k < leaf->first + leaf->count; ++k) {
+            uint32_t tri = prims[k].tri;
+            const dk_triangle& t = sc->triangles[tri];
+            uint32_t mid = std::min(std::min(t.material_id, sc->material_count - 1u), 255u);
+            uint32_t flags = (opaque[tri] ? 1u : 0u) | (mid << 8);
+            isect.push_back(make_float4(t.v0.x, t.v0.y, t.v0.z, asFloat(slotOfTri[tri])));
+            isect.push_back(make_float4(t.v1.x - t.v0.x, t.v1.y - t.v0.y, t.v1.z - t.v0.z, asFloat(tri)));
+            isect.push_back(make_float4(t.v2.x - t.v0.x, t.v2.y - t.v0.y, t.v2.z - t.v0.z, asFloat(flags)));
+        }
+        return first;
+    }
+
+    // Children of interior node `t`: binary subtrees reached by repeatedly
+    // opening the interior child of largest surface area, up to eight.
+    static std::vector<const TNode*> collapse(const TNode* t) {
+        if (wideLeaf(t)) return {t};  // a single-leaf tree: the root holds the leaf
+        std::vector<const TNode*> kids = {t->l.get(), t->r.get()};
+        while (kids.size() < 8) {
+            int best = -1;
+            float area = -1.0f;
+            for (int i = 0; i < (int)kids.size(); ++i)
+                if (!wideLeaf(kids[i]) && kids[i]->box.halfArea() > area) {
+                    area = kids[i]->box.halfArea();
+                    best = i;
+                }
+            if (best < 0) break;
+            const TNode* open = kids[best];
+            kids[best] = open->l.get();
+            kids.push_back(open->r.get());
+        }
+        return kids;
+    }
+
+    // Slot of every child: greedy assignment of (corner, child) pairs in
+    // decreasing order of how far the child's centre lies towards the corner.
+    static void assignSlots(const Box& nb, const std::vector<const TNode*>& kids, const TNode* slot[8]) {
+        for (int s = 0; s < 8; ++s) slot[s] = nullptr;
+        struct Cand { float score; int s, k; };
+        std::vector<Cand> cand;
+        float cn[3];
+        for (int a = 0; a < 3; ++a) cn[a] = 0.5f * (nb.mn[a] + nb.mx[a]);
+        for (int k = 0; k < (int)kids.size(); ++k) {
+            float c[3];
+            for (int a = 0; a < 3; ++a) c[a] = 0.5f * (kids[k]->box.mn[a] + kids[k]->box.mx[a]) - cn[a];
+            for (int s = 0; s < 8; ++s) {
+                float sc = 0.0f;
+                for (int a = 0; a < 3; ++a) sc += ((s >> a) & 1) ? c[a] : -c[a];
+                cand.push_back({sc, s, k});
+            }
+        }
+        std::stable_sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) { return x.score > y.score; });
+        bool used[8] = {};
+        for (const Cand& c : cand) {
+            if (slot[c.s] || used[c.k]) continue;
+            slot[c.s] = kids[c.k];
+            used[c.k] = true;
+        }
+    }
+
+    // Writes the record of interior node `t` at index `idx`, then its subtree.
+    void emit(const TNode* t, uint32_t idx, int depth) {
+        maxDepth = std::max(maxDepth, depth);
+        std::vector<const TNode*> kids = collapse(t);
+        const TNode* slot[8];
+        assignSlots(t->box, kids, slot);
+        Quantizer qz(t->box);
+        uint32_t imask = 0, nInterior = 0;
+        for (int s = 0; s < 8; ++s)
+            if (slot[s] && !wideLeaf(slot[s])) {
+                imask |= 1u << s;
+                ++nInterior;
+            }
+        const uint32_t childBase = (uint32_t)(nodes.size() / 5);
+        nodes.resize(nodes.size() + 5 * (size_t)nInterior);
+        const uint32_t triBase = (uint32_t)(isect.size() / 3);
+        uint8_t meta[8] = {}, q[6][8] = {};
+        for (int s = 0; s < 8; ++s) {
+            const TNode* c = slot[s];
+            if (!c) continue;
+            for (int a = 0; a < 3; ++a) {
+                uint32_t lo, hi;
+                qz.quantize(c->box, a, lo, hi);
+                q[a][s] = (uint8_t)lo;
+                q[3 + a][s] = (uint8_t)hi;
+            }
+            if (wideLeaf(c)) {
+                uint32_t first = appendTriangles(c);
+                meta[s] = (uint8_t)((c->count << 5) | (first - triBase));
+            }
+        }
+        uint32_t w[20];
+        std::memcpy(&w[0], &qz.p[0], 4);
+        std::memcpy(&w[1], &qz.p[1], 4);
+        std::memcpy(&w[2], &qz.p[2], 4);
+        w[3] = qz.E[0] | (qz.E[1] << 8) | (qz.E[2] << 16) | (imask << 24);
+        w[4] = childBase;
+        w[5] = triBase;
+        std::memcpy(&w[6], meta, 8);
+        std::memcpy(&w[8], q, 48);
+        std::memcpy(&nodes[5 * (size_t)idx], w, 80);
+        uint32_t j = 0;
+        for (int s = 0; s < 8; ++s)
+            if (slot[s] && !wideLeaf(slot[s])) emit(slot[s], childBase + j++, depth + 1);
+    }
+};
+
 }  // namespace
 
 // DFS leaf order of the caller's flat BVH (left child first), the tie order of
@@ -243,8 +423,8 @@ bool referenceSlots(const dk_scene* sc, std::vector<uint32_t>& slotOfTri, std::s
 
 // Binned-SAH traversal tree over every triangle that has a slot.
 int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri,
-                      const std::vector<uint8_t>& opaque, std::vector<float4>& nodes, std::vector<float4>& isect,
-                      std::string& err) {
+                      const std::vector<uint8_t>& opaque, int width, std::vector<float4>& nodes,
+                      std::vector<float4>& isect, std::string& err) {
     std::vector<Prim> prims;
     prims.reserve(sc->triangle_count);
     for (uint32_t i = 0; i < sc->triangle_count; ++i) {
@@ -268,7 +448,21 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
         return DK_ERROR_INVALID_SCENE;
     }
     if (n == 0) return DK_OK;
-    std::unique_ptr<TNode> root = build(prims.data(), 0, n, 0);
+    if (width == 8) {
+        // Leaves of <= 4 triangles: eight of them fill a node's 32-bit slot mask.
+        std::unique_ptr<TNode> root = build(prims.data(), 0, n, 0, 4);
+        isect.reserve(3 * (size_t)n);
+        nodes.resize(5);
+        Wide8Builder wb{prims, sc, slotOfTri, opaque, nodes, isect};
+        wb.emit(root.get(), 0, 0);
+        // Each node visit pushes at most one group of siblings.
+        if (wb.maxDepth + 1 > (int)kTraversalStack) {
+            err = "traversal BVH deeper than the traversal stack";
+            return DK_ERROR_INVALID_SCENE;
+        }
+        return DK_OK;
+    }
+    std::unique_ptr<TNode> root = build(prims.data(), 0, n, 0, 8);
     isect.resize(3 * (size_t)(n + 1));
     for (uint32_t s = 0; s < n; ++s) {
         const dk_triangle& t = sc->triangles[prims[s].tri];

@@ -327,6 +327,200 @@ __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* st
     return 0;
 }
 
+// ------------------------------------- 8-wide quantised traversal ------
+// The alternative layout (DevScene::wide8; node layout in dk_bvh.cu): child
+// boxes quantised to 8 bits per bound against a per-node origin and
+// power-of-two steps, rounded outwards, so a box test never rejects a child
+// whose exact box the ray enters.  The traversal state holds two groups:
+// interior children still to visit (first child index; interior mask << 8 |
+// visit mask, bit slot ^ oct) and leaf slots still to test (first slot;
+// 32-bit mask).  The builder puts the child lying furthest towards box corner
+// c in slot c, so a ray whose direction signs form oct meets slot oct first
+// and visiting by increasing slot ^ oct is roughly front to back.  A node
+// visit pushes at most one group, so the stack depth is bounded by the tree
+// depth (checked when the tree is built).
+struct Trav {
+    float3 o, d, inv;
+    uint32_t oct;   // sign bits of the direction: x, y, z
+    uint2 group;
+    uint2 tris;
+    int sp;
+};
+
+// Reciprocal direction for the box tests: a zero component is taken as
+// +-1e-20 so that every slab distance stays finite.
+__device__ __forceinline__ float3 boxInv(float3 d) {
+    auto r = [](float v) { return 1.0f / (fabsf(v) < 1e-20f ? copysignf(1e-20f, v) : v); };
+    return f3(r(d.x), r(d.y), r(d.z));
+}
+
+__device__ __forceinline__ void travInit(Trav& t, float3 o, float3 d) {
+    t.o = o;
+    t.d = d;
+    t.inv = boxInv(d);
+    t.oct = (t.inv.x < 0.0f ? 1u : 0u) | (t.inv.y < 0.0f ? 2u : 0u) | (t.inv.z < 0.0f ? 4u : 0u);
+    t.group = make_uint2(0u, (1u << 8) | (1u << t.oct));  // the root: slot 0 of a one-child group
+    t.tris = make_uint2(0u, 0u);
+    t.sp = 0;
+}
+
+// Byte j of `w` as a float: 2^23 + b assembled by a byte permute, minus 2^23.
+__device__ __forceinline__ float qByte(uint32_t w, uint32_t j) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | j)) - 8388608.0f;
+}
+
+// Tests the eight child boxes of `node` against (0, tmax]; the hit interior
+// children become the current group, the hit leaves' slots the triangle set.
+__device__ __forceinline__ void visit8(const DevScene& S, Trav& t, uint32_t node, float tmax) {
+    const uint4* n = reinterpret_cast<const uint4*>(S.nodes) + 5 * (size_t)node;
+    const uint4 w0 = __ldg(n + 0), w1 = __ldg(n + 1), w2 = __ldg(n + 2), w3 = __ldg(n + 3), w4 = __ldg(n + 4);
+    const float ax = __uint_as_float((w0.w & 0xffu) << 23) * t.inv.x;
+    const float ay = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * t.inv.y;
+    const float az = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * t.inv.z;
+    const float bx = (__uint_as_float(w0.x) - t.o.x) * t.inv.x;
+    const float by = (__uint_as_float(w0.y) - t.o.y) * t.inv.y;
+    const float bz = (__uint_as_float(w0.z) - t.o.z) * t.inv.z;
+    const uint32_t imask = w0.w >> 24;
+    // Near and far planes per axis by the sign of the direction.
+    const bool sx = t.oct & 1u, sy = t.oct & 2u, sz = t.oct & 4u;
+    const uint32_t nx[2] = {sx ? w3.z : w2.x, sx ? w3.w : w2.y}, fx[2] = {sx ? w2.x : w3.z, sx ? w2.y : w3.w};
+    const uint32_t ny[2] = {sy ? w4.x : w2.z, sy ? w4.y : w2.w}, fy[2] = {sy ? w2.z : w4.x, sy ? w2.w : w4.y};
+    const uint32_t nz[2] = {sz ? w4.z : w3.x, sz ? w4.w : w3.y}, fz[2] = {sz ? w3.x : w4.z, sz ? w3.y : w4.w};
+    const uint32_t meta[2] = {w1.z, w1.w};
+    uint32_t order = 0u, triMask = 0u;
+#pragma unroll
+    for (uint32_t h = 0; h < 2; ++h) {
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j) {
+            const uint32_t s = 4u * h + j;
+            float tn = fmaxf(fmaxf(fmaf(qByte(nx[h], j), ax, bx), fmaf(qByte(ny[h], j), ay, by)),
+                             fmaxf(fmaf(qByte(nz[h], j), az, bz), 0.0f));
+            float tf = fminf(fminf(fmaf(qByte(fx[h], j), ax, bx), fmaf(qByte(fy[h], j), ay, by)),
+                             fminf(fmaf(qByte(fz[h], j), az, bz), tmax));
+            if (tn <= tf) {
+                const uint32_t m = (meta[h] >> (8u * j)) & 0xffu;
+                triMask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+                order |= ((imask >> s) & 1u) << (s ^ t.oct);
+            }
+        }
+    }
+    t.group = make_uint2(w1.x, (imask << 8) | order);
+    t.tris = make_uint2(w1.y, triMask);
+}
+
+// Up to `budget` node visits, each followed by the triangles of the leaves
+// it hit; `leaf(slot, tmax)` tests one leaf slot (it may lower tmax) and
+// returns true to stop the query.  Returns 0 running, 1 finished, 2 stopped.
+template <class LeafFn>
+__device__ __forceinline__ int travSteps(const DevScene& S, Trav& t, uint2* stack, float& tmax, int budget,
+                                         LeafFn&& leaf) {
+    for (int it = 0;; ++it) {
+        while (t.tris.y) {
+            const uint32_t j = __ffs(t.tris.y) - 1;
+            t.tris.y &= t.tris.y - 1u;
+            if (leaf(t.tris.x + j, tmax)) return 2;
+        }
+        if ((t.group.y & 0xffu) == 0u) {
+            if (t.sp == 0) return 1;
+            t.group = stack[--t.sp];
+        }
+        if (it == budget) return 0;
+        const uint32_t k = __ffs(t.group.y & 0xffu) - 1;
+        t.group.y &= ~(1u << k);
+        const uint32_t s = k ^ t.oct;
+        const uint32_t node = t.group.x + __popc((t.group.y >> 8) & ((1u << s) - 1u));
+        if (t.group.y & 0xffu) stack[t.sp++] = t.group;
+        visit8(S, t, node, tmax);
+    }
+}
+
+// Closest hit over the 8-wide tree, the same (t, slot) argmin as above.
+struct Closest8 {
+    Trav tr;
+    float bestT, bu, bv;
+    uint32_t bestTri, bestSlot;
+};
+
+__device__ __forceinline__ void closestInit(Closest8& st, float3 o, float3 d) {
+    travInit(st.tr, o, d);
+    st.bestT = INFINITY;
+    st.bu = st.bv = 0.0f;
+    st.bestTri = kNoHit;
+    st.bestSlot = 0xffffffffu;
+}
+
+__device__ __forceinline__ bool closestSteps(const DevScene& S, Closest8& st, uint2* stack, int budget) {
+    if (S.node_count == 0) return true;
+    const float3 o = st.tr.o, d = st.tr.d;
+    return travSteps(S, st.tr, stack, st.bestT, budget, [&](uint32_t i, float& tmax) {
+        const float4* q = S.isect + 3 * (size_t)i;
+        const float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+        float t, u, v;
+        if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v)) {
+            const uint32_t slot = __float_as_uint(a.w);
+            if (t < tmax || (t == tmax && slot < st.bestSlot)) {
+                tmax = t;
+                st.bu = u;
+                st.bv = v;
+                st.bestTri = __float_as_uint(b.w);
+                st.bestSlot = slot;
+            }
+        }
+        return false;
+    }) != 0;
+}
+
+__device__ __noinline__ HitRec traceClosest8(const DevScene& S, float3 o, float3 d) {
+    Closest8 st;
+    uint2 stack[kTraversalStack];
+    closestInit(st, o, d);
+    closestSteps(S, st, stack, 1 << 30);
+    return HitRec{st.bestT, st.bestTri, st.bu, st.bv};
+}
+
+// Any hit over the 8-wide tree (the AnyState query above).
+struct Any8 {
+    Trav tr;
+    float tmax;
+    uint32_t opaqueMask;
+    bool sawNonOpaque;
+    bool recOverflow;
+    uint32_t recCount;
+    uint2* rec;
+};
+
+__device__ __forceinline__ void anyInit(Any8& st, float3 o, float3 d, float tmax, uint32_t opaqueMask, uint2* rec) {
+    travInit(st.tr, o, d);
+    st.tmax = tmax;
+    st.opaqueMask = opaqueMask;
+    st.sawNonOpaque = false;
+    st.recOverflow = false;
+    st.recCount = 0;
+    st.rec = rec;
+}
+
+__device__ __forceinline__ int anySteps(const DevScene& S, Any8& st, uint2* stack, int budget) {
+    if (S.node_count == 0) return 1;
+    const float3 o = st.tr.o, d = st.tr.d;
+    float tmax = st.tmax;
+    return travSteps(S, st.tr, stack, tmax, budget, [&](uint32_t i, float&) {
+        const float4* q = S.isect + 3 * (size_t)i;
+        const float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+        float t, u, v;
+        if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) && t < st.tmax) {
+            if (blocksShadow(__float_as_uint(c.w), st.opaqueMask)) return true;
+            st.sawNonOpaque = true;
+            if (st.rec) {
+                if (st.recCount < kRecLayers)
+                    st.rec[st.recCount++] = make_uint2(__float_as_uint(t), i);
+                else
+                    st.recOverflow = true;
+            }
+        }
+        return false;
+    });
+}
+
 // Hit attributes of intersectTriangle / intersectScene (PathTrace.metal:
 // 1840-1851, 3366-3380) from the traversal's (t, u, v), exact ops.
 __device__ __forceinline__ Hit makeHit(const DevScene& S, const Ray& ray, const HitRec& r) {

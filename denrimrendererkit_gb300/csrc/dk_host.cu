@@ -213,7 +213,8 @@ int kernelGrid(int which, int smCount);
 
 Grids kernelGrids() {
     int sm = g_prop.multiProcessorCount;
-    return Grids{kernelGrid(0, sm), kernelGrid(1, sm), kernelGrid(2, sm), kernelGrid(3, sm), kernelGrid(4, sm)};
+    return Grids{kernelGrid(0, sm), kernelGrid(1, sm), kernelGrid(2, sm), kernelGrid(3, sm), kernelGrid(4, sm),
+                 kernelGrid(5, sm), kernelGrid(6, sm)};
 }
 
 bool materialBlocksShadow(const dk_material& m) {
@@ -263,11 +264,21 @@ int validateScene(const dk_scene* sc) {
     return DK_OK;
 }
 
+// Traversal tree layout of the scenes uploaded from now on: DK_BVH_WIDTH=8
+// selects the 8-wide quantised nodes, anything else the 4-wide FP32 nodes
+// (the faster of the two on GB300, where the tree stays in L2 and traversal
+// is bound by instruction issue).
+static int traversalWidth() {
+    const char* e = getenv("DK_BVH_WIDTH");
+    return (e && e[0] == '8' && e[1] == 0) ? 8 : 4;
+}
+
 int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity) {
     // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
     // reaches, each carrying its reference DFS slot as the tie-break key.
     std::vector<float4> tNodes, tIsect;
     bool allOpaque = true;
+    const int width = traversalWidth();
     {
         std::vector<uint32_t> slotOf;
         std::string err;
@@ -279,7 +290,7 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
             opaque[i] = materialBlocksShadow(m) ? 1 : 0;
             if (!opaque[i] && slotOf[i] != kNoSlot) allOpaque = false;
         }
-        int brc = buildSahTraversal(sc, slotOf, opaque, tNodes, tIsect, err);
+        int brc = buildSahTraversal(sc, slotOf, opaque, width, tNodes, tIsect, err);
         if (brc != DK_OK) return fail(brc, "Invalid render scene: " + err + ".");
     }
     std::memset(&D, 0, sizeof(D));
@@ -355,7 +366,8 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
 #undef TRY
     D.tri_count = sc->triangle_count;
     D.mat_count = sc->material_count;
-    D.node_count = (uint32_t)(tNodes.size() / 8);
+    D.node_count = (uint32_t)(tNodes.size() / (width == 8 ? 5 : 8));
+    D.wide8 = width == 8 ? 1u : 0u;
     D.all_shadow_opaque = allOpaque ? 1u : 0u;
     D.texdesc_count = sc->texture_descriptor_count;
     D.light_count = sc->lights ? sc->light_count : 0;
@@ -468,11 +480,11 @@ int launchWave(const DevScene& S, const Wave& W, uint32_t maxBounces, bool anyDe
     for (uint32_t b = 0; b < maxBounces; ++b) {
         uint32_t sel = b & 1u;
         MARK(1);
-        DK_CUDA(launchExtend(S, W, sel, g.extend, q), "extend launch");
+        DK_CUDA(launchExtend(S, W, sel, S.wide8 ? g.extend8 : g.extend, q), "extend launch");
         MARK(2);
         DK_CUDA(launchShade(S, W, b, sel, g.shade, q), "shade launch");
         MARK(3);
-        DK_CUDA(launchShadow(S, W, g.shadow, q), "shadow launch");
+        DK_CUDA(launchShadow(S, W, S.wide8 ? g.shadow8 : g.shadow, q), "shadow launch");
         DK_CUDA(launchResolve(W, g.final, q), "resolve launch");
         launches += bounceLaunches(S);
     }

@@ -76,6 +76,7 @@ void fillParams(DevParams& P, const dk_settings& st);
 
 struct Grids {
     int gen, extend, shade, shadow, final;
+    int extend8, shadow8;  // the traversal kernels over the 8-wide tree
 };
 Grids kernelGrids();
 

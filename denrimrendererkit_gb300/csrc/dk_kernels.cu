@@ -15,6 +15,7 @@
 // Surviving paths are compacted into the next queue with warp-ballot appends.
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 
 #include "dk_kernels.h"
 #include "dk_sdf.cuh"
@@ -177,7 +178,7 @@ __device__ __forceinline__ Hit makeHitAny(const DevScene& S, const Ray& ray, con
 // intersectScene (:3294-3421): triangles, then the sparse volumes with the
 // triangle distance as the bound.
 __device__ __noinline__ HitRec traceScene(const DevScene& S, float3 o, float3 d) {
-    HitRec r = traceClosest(S, o, d);
+    HitRec r = S.wide8 ? traceClosest8(S, o, d) : traceClosest(S, o, d);
     if (S.volume_count) {
         VolumeHitRec vh;
         if (closestVolumeHit(volumeScene(S), o, d, r.t, vh)) {
@@ -423,6 +424,7 @@ __device__ __forceinline__ uint32_t warpFetch(uint32_t* counter, uint32_t n, boo
 // Closest hit for every ray of the input queue (intersectScene), persistent
 // threads with per-lane refill.  W.counts[4] is the work cursor (zeroed by the
 // kernel that runs before).
+template <bool kWide8>
 __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel) {
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
@@ -436,9 +438,12 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
         W.counts[6] = 0u;
         W.counts[7] = 0u;
     }
-    int stackNode[kStackSize];
-    float stackT[kStackSize];
-    ClosestState st;
+    // The stacks stay separate objects from the scalar state, so that only
+    // they live in local memory.
+    int stackNode[kWide8 ? 1 : kStackSize];
+    float stackT[kWide8 ? 1 : kStackSize];
+    uint2 stack8[kWide8 ? kTraversalStack : 1];
+    std::conditional_t<kWide8, Closest8, ClosestState> st;
     uint32_t p = kNoWork;
     bool exhausted = false;
     for (;;) {
@@ -453,7 +458,14 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
             }
         }
         if (__all_sync(0xffffffffu, p == kNoWork && exhausted)) break;
-        if (p != kNoWork && closestSteps(S, st, stackNode, stackT, kStepBudget)) {
+        bool done = false;
+        if (p != kNoWork) {
+            if constexpr (kWide8)
+                done = closestSteps(S, st, stack8, kStepBudget);
+            else
+                done = closestSteps(S, st, stackNode, stackT, kStepBudget);
+        }
+        if (done) {
             W.hit[p] = make_float4(st.bestT, __uint_as_float(st.bestTri), st.bu, st.bv);
             p = kNoWork;
         }
@@ -826,8 +838,36 @@ __device__ __forceinline__ void insertLayer(float* lt, uint32_t* ltri, uint32_t*
 // shadowOccluded for scenes with cut-out or transmissive triangles, in one
 // traversal: an opaque blocker anywhere in (0.0005, maxDistance) occludes;
 // otherwise the non-opaque layers are collected and walked.
+// The same collecting traversal over the 8-wide tree.
+__device__ __noinline__ bool shadowLayers8(const DevScene& S, MatTable mt, uint32_t opaqueMask, float3 o, float3 d,
+                                           float tmax, float3& T) {
+    constexpr int kMaxLayers = 8;
+    float lt[kMaxLayers];
+    uint32_t ltri[kMaxLayers], lslot[kMaxLayers];
+    float lu[kMaxLayers], lv[kMaxLayers];
+    int count = 0;
+    if (S.node_count == 0) return false;
+    Trav tr;
+    uint2 stack[kTraversalStack];
+    travInit(tr, o, d);
+    float tm = tmax;
+    int r = travSteps(S, tr, stack, tm, 1 << 30, [&](uint32_t i, float&) {
+        const float4* q = S.isect + 3 * (size_t)i;
+        const float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
+        float t, u, v;
+        if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) || !(t < tmax)) return false;
+        if (blocksShadow(__float_as_uint(c.w), opaqueMask)) return true;  // opaque blocker
+        if (count == kMaxLayers - 1) return true;                        // an 8th layer: the walk ends occluded
+        insertLayer(lt, ltri, lslot, lu, lv, count, t, __float_as_uint(b.w), __float_as_uint(a.w), u, v);
+        return false;
+    });
+    if (r == 2) return true;
+    return walkLayers(S, mt, o, d, lt, ltri, lu, lv, count, T);
+}
+
 __device__ bool shadowLayers(const DevScene& S, MatTable mt, uint32_t opaqueMask, float3 o, float3 d, float tmax,
                              float3& T) {
+    if (S.wide8) return shadowLayers8(S, mt, opaqueMask, o, d, tmax, T);
     constexpr int kMaxLayers = 8;
     float lt[kMaxLayers];
     uint32_t ltri[kMaxLayers], lslot[kMaxLayers];
@@ -941,11 +981,13 @@ __global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(Dev
 // shadowed value (contribution / pdf divisor, or 0).  Rays that crossed a
 // cut-out or transmissive triangle without meeting an opaque one go to a
 // second queue for the layer walk (W.counts[6]).  W.counts[5] is the cursor.
+template <bool kWide8>
 __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
     const uint32_t n = W.counts[3];
     const size_t cap = W.cap;
-    int stackNode[kStackSize];
-    AnyState st;
+    int stackNode[kWide8 ? 1 : kStackSize];
+    uint2 stack8[kWide8 ? kTraversalStack : 1];
+    std::conditional_t<kWide8, Any8, AnyState> st;
     uint32_t e = kNoWork;
     bool exhausted = false;
     for (;;) {
@@ -959,7 +1001,13 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
         }
         if (__all_sync(0xffffffffu, e == kNoWork && exhausted)) break;
         if (e == kNoWork) continue;
-        int r = S.node_count == 0 ? 1 : anySteps(S, st, stackNode, kStepBudget);
+        int r = 1;
+        if (S.node_count) {
+            if constexpr (kWide8)
+                r = anySteps(S, st, stack8, kStepBudget);
+            else
+                r = anySteps(S, st, stackNode, kStepBudget);
+        }
         if (r == 0) continue;
         size_t slot = (size_t)(e & 3u) * cap + (e >> 2);
         if (r == 1 && S.volume_count) st.sawNonOpaque = true;  // distance volumes: the walk decides
@@ -1255,9 +1303,11 @@ int kernelGrid(int which, int smCount) {
     int perSM = 1;
     switch (which) {
         case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_generate, 256, 0); break;
-        case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend, 128, 0); break;
+        case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend<false>, 128, 0); break;
         case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade<false>, 128, 0); break;
-        case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays, 128, 0); break;
+        case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<false>, 128, 0); break;
+        case 5: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend<true>, 128, 0); break;
+        case 6: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<true>, 128, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_finalize, 256, 0); break;
     }
     return (perSM < 1 ? 1 : perSM) * smCount;
@@ -1268,7 +1318,10 @@ cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStrea
     return cudaGetLastError();
 }
 cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st) {
-    k_extend<<<grid, 128, 0, st>>>(S, W, sel);
+    if (S.wide8)
+        k_extend<true><<<grid, 128, 0, st>>>(S, W, sel);
+    else
+        k_extend<false><<<grid, 128, 0, st>>>(S, W, sel);
     if (S.volume_count) k_extend_volume<<<grid, 128, 0, st>>>(S, W, sel);
     return cudaGetLastError();
 }
@@ -1311,14 +1364,20 @@ cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint3
         k_sort_scan<<<1, kSortBins, 0, st>>>(W);
         k_sort_scatter<<<(W.cap + 256u * kSortItems - 1u) / (256u * kSortItems), 256, 0, st>>>(W, sel);
     }
-    if (S.volume_count)
+    // The general shading kernel (volume hits, random walks through
+    // traceScene) also serves the 8-wide tree, keeping the layout switch out
+    // of the triangle-only kernel.
+    if (S.volume_count || S.wide8)
         k_shade<true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
     else
         k_shade<false><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
     return cudaGetLastError();
 }
 cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st) {
-    k_shadow_rays<<<grid, 128, 0, st>>>(S, W);
+    if (S.wide8)
+        k_shadow_rays<true><<<grid, 128, 0, st>>>(S, W);
+    else
+        k_shadow_rays<false><<<grid, 128, 0, st>>>(S, W);
     if (!S.all_shadow_opaque || S.volume_count) k_shadow_layers<<<grid, 128, 0, st>>>(S, W);
     return cudaGetLastError();
 }

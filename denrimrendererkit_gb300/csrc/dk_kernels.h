@@ -12,15 +12,18 @@
 namespace dk {
 
 constexpr uint32_t kNoSlot = 0xffffffffu;
-constexpr uint32_t kSortBins = 256;
-constexpr uint32_t kRecLayers = 4;   // non-opaque layers the any-hit pass records per shadow ray  // shading-order keys: 0 miss, 1 + material ID (< 254), 255 other
+constexpr uint32_t kSortBins = 256;      // shading-order keys: 0 miss, 1 + material ID (< 254), 255 other
+constexpr uint32_t kRecLayers = 4;       // non-opaque layers the any-hit pass records per shadow ray
+constexpr uint32_t kTraversalStack = 32; // groups on the 8-wide traversal stack (bounds the tree depth)
 
 // Device copy of the scene.  `isect` holds 3 x float4 per BVH leaf slot:
 // (v0.xyz, reference slot), (v1 - v0, triangle index), (v2 - v0, flags with
 // bit 0 = blocks shadow rays under the scene's own materials and bits 8..15 =
-// min(material ID, 255)); `nodes` holds 8 x float4 per 4-wide node: x-min,
+// min(material ID, 255)); `nodes` holds the traversal tree in one of two
+// layouts (dk_bvh.cu): 8 x float4 per 4-wide node with FP32 child boxes (x-min,
 // x-max, y-min, y-max, z-min, z-max rows with one lane per child, the four
-// child references, a spare row.
+// child references, a spare row), or, with `wide8`, 5 x 16 bytes per 8-wide
+// node with 8-bit quantised child boxes.
 struct DevScene {
     const dk_triangle* tris;
     const dk_material* mats;
@@ -36,6 +39,7 @@ struct DevScene {
     float env_intensity, env_rot_y, env_max_radiance;
     uint32_t env_guide_size;
     float env_rot_sin, env_rot_cos;  // sincosf(env_rot_y), evaluated once on the device
+    uint32_t wide8;                  // traversal tree layout: 0 = 4-wide FP32, 1 = 8-wide quantised
     // Sparse distance volumes (GPUVolumeDescriptor with metadata.w == 1).
     const dk_volume_descriptor* volumes;
     const dk_volume_brick_descriptor* bricks;
@@ -129,8 +133,9 @@ struct Wave {
 
 // Host-side traversal BVH (dk_bvh.cu).
 bool referenceSlots(const dk_scene* sc, std::vector<uint32_t>& slotOfTri, std::string& err);
+// `width` 4 or 8 selects the node layout.
 int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri, const std::vector<uint8_t>& opaque,
-                      std::vector<float4>& nodes, std::vector<float4>& isect, std::string& err);
+                      int width, std::vector<float4>& nodes, std::vector<float4>& isect, std::string& err);
 
 cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st);

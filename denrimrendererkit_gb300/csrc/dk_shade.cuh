@@ -336,7 +336,7 @@ __device__ __forceinline__ float3 clearcoatAttenuationAt(const Material& m, cons
     return att * materialClearcoatDepthAttenuation(m, sp.n, sp.v, l);
 }
 
-__device__ __noinline__ float3 evalBRDF(const Material& m, const ShadePoint& sp, float3 l) {  // :1323-1384
+__device__ __forceinline__ float3 evalBRDF(const Material& m, const ShadePoint& sp, float3 l) {  // :1323-1384
     const float inversePi = 0.31830988618f;
     float3 hd = sp.v + l;
     float3 h = normalize(hd);
@@ -368,7 +368,7 @@ __device__ __forceinline__ float ggxPDFAt(const ShadePoint& sp, float3 h, float 
     return distributionGGXAnisotropicA(h, sp.n, sp.fr.tangent, sp.fr.bitangent, a) * g1v / fmaxf(4.0f * sp.nDotV, 1e-5f);
 }
 
-__device__ __noinline__ float bsdfPDF(const ShadePoint& sp, float3 l) {  // :1445-1490
+__device__ __forceinline__ float bsdfPDF(const ShadePoint& sp, float3 l) {  // :1445-1490
     float nDotL = fmaxf(dot(sp.n, l), 0.0f);
     if (nDotL <= 0.0f || sp.nDotV <= 0.0f) return 0.0f;
     float3 h = normalize(sp.v + l);
