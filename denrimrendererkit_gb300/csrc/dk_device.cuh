@@ -90,6 +90,7 @@ __device__ __forceinline__ void wideSwap(uint32_t& ca, float& ta, uint32_t& cb, 
     }
 }
 
+template <bool kSort = true>
 __device__ __forceinline__ int wideVisit(const DevScene& S, uint32_t node, float3 o, float3 inv, float tmax, Wide& w) {
     const float4* n = S.nodes + 8 * (size_t)node;
     float4 lx = __ldg(n + 0), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3), lz = __ldg(n + 4),
@@ -105,6 +106,7 @@ __device__ __forceinline__ int wideVisit(const DevScene& S, uint32_t node, float
     w.c3 = ch.w;
     w.t3 = childBox(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, o, inv, tmax, t) ? t : INFINITY;
     int k = (w.t0 != INFINITY) + (w.t1 != INFINITY) + (w.t2 != INFINITY) + (w.t3 != INFINITY);
+    if (!kSort) return k;  // lanes in child order, misses at t = +inf
     if (k > 1) {
         wideSwap(w.c0, w.t0, w.c1, w.t1);
         wideSwap(w.c2, w.t2, w.c3, w.t3);
@@ -287,6 +289,11 @@ __device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float 
     st.rec = rec;
 }
 
+// Children of an any-hit query are visited nearest first (DK_ANY_SORTED=1) or
+// in child order (0).
+#ifndef DK_ANY_SORTED
+#define DK_ANY_SORTED 0
+#endif
 // Up to `budget` node visits of the any-hit query over shadow-blocking
 // triangles with 0.0005 < t < tmax: 0 running, 1 finished without an
 // opaque blocker, 2 occluded.
@@ -294,7 +301,17 @@ __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* st
     for (int it = 0; it < budget; ++it) {
         if ((st.node & kLeafBit) == 0) {
             Wide w;
-            int k = wideVisit(S, st.node, st.o, st.inv, st.tmax, w);
+            int k = wideVisit<DK_ANY_SORTED != 0>(S, st.node, st.o, st.inv, st.tmax, w);
+            if (k > 0 && !DK_ANY_SORTED) {  // first hit child next, the others pushed
+                uint32_t next = 0u;
+                bool have = false;
+                if (w.t3 != INFINITY) { next = w.c3; have = true; }
+                if (w.t2 != INFINITY) { if (have) stackNode[st.sp++] = (int)next; next = w.c2; have = true; }
+                if (w.t1 != INFINITY) { if (have) stackNode[st.sp++] = (int)next; next = w.c1; have = true; }
+                if (w.t0 != INFINITY) { if (have) stackNode[st.sp++] = (int)next; next = w.c0; }
+                st.node = next;
+                continue;
+            }
             if (k > 0) {
                 if (k > 3) stackNode[st.sp++] = (int)w.c3;
                 if (k > 2) stackNode[st.sp++] = (int)w.c2;

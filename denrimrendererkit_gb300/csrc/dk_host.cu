@@ -323,16 +323,16 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
         for (uint32_t i = 1; i < n && monotone; ++i)
             monotone = sc->environment_samples[i].cdf >= sc->environment_samples[i - 1].cdf;
         if (monotone) {
-            const uint32_t G = 8192;
+            // One bucket per texel or finer (a power of two >= n, 2^13..2^22),
+            // so the search after the guide lookup takes one or two steps.
+            uint32_t G = 8192;
+            while (G < n && G < (1u << 22)) G <<= 1;
             std::vector<uint32_t> guide(G + 1);
+            uint32_t i = 0;
             for (uint32_t b = 0; b <= G; ++b) {
-                float target = (float)b / (float)G;  // exact: b * 2^-13
-                uint32_t lo = 0, hi = n;
-                while (lo < hi) {
-                    uint32_t mid = (lo + hi) >> 1;
-                    if (target <= sc->environment_samples[mid].cdf) hi = mid; else lo = mid + 1;
-                }
-                guide[b] = lo;
+                float target = (float)b / (float)G;  // exact: b * 2^-log2(G)
+                while (i < n && !(target <= sc->environment_samples[i].cdf)) ++i;
+                guide[b] = i;  // first index with target <= cdf (n if none)
             }
             TRY(arena.upload(const_cast<uint32_t**>(&D.env_guide), guide.data(), guide.size(), "environment guide"));
             D.env_guide_size = G;

@@ -401,7 +401,10 @@ __global__ void __launch_bounds__(256) k_generate(DevScene S, Wave W) {
 }
 
 constexpr uint32_t kNoWork = 0xffffffffu;
-constexpr int kStepBudget = 16;
+#ifndef DK_STEP_BUDGET
+#define DK_STEP_BUDGET 16
+#endif
+constexpr int kStepBudget = DK_STEP_BUDGET;
 
 // Refills the lanes that asked for work with consecutive items of a queue of
 // length `n` through one atomic per warp; returns this lane's item or kNoWork.
@@ -760,7 +763,7 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
 }
 
 #ifndef DK_SHADE_MIN_BLOCKS
-#define DK_SHADE_MIN_BLOCKS 5
+#define DK_SHADE_MIN_BLOCKS 4
 #endif
 template <bool kVolumes>
 __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, Wave W, uint32_t bounce, uint32_t sel,

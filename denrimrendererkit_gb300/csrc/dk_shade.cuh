@@ -494,7 +494,7 @@ __device__ __forceinline__ float3 rotateEnv(const DevScene& S, float3 d, float& 
     cs = S.env_rot_cos;
     return normalize(f3(cs * d.x - sn * d.z, d.y, sn * d.x + cs * d.z));
 }
-__device__ __noinline__ float3 sampleEnvironment(const DevScene& S, float3 d) {  // :3770-3802
+__device__ __forceinline__ float3 sampleEnvironment(const DevScene& S, float3 d) {  // :3770-3802
     float intensity = fmaxf(S.env_intensity, 0.0f);
     if (S.env_tex_plus1 == 0u) return fallbackSky(d) * intensity;
     float sn, cs;
@@ -507,7 +507,7 @@ __device__ __noinline__ float3 sampleEnvironment(const DevScene& S, float3 d) { 
     if (maxR > 0.0f) color = mn(color, f3(maxR));
     return color;
 }
-__device__ __noinline__ float environmentPDF(const DevScene& S, float3 d) {  // :3870-3914
+__device__ __forceinline__ float environmentPDF(const DevScene& S, float3 d) {  // :3870-3914
     if (S.env == nullptr || S.env_count == 0u || S.env_tex_plus1 == 0u) return 0.0f;
     uint4 md = __ldg(reinterpret_cast<const uint4*>(&S.texdesc[S.env_tex_plus1 - 1u]));
     uint32_t w = md.y, hgt = md.z;
