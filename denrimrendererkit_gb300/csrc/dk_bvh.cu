@@ -39,7 +39,14 @@ namespace dk {
 namespace {
 
 constexpr uint32_t kLeaf = 0x80000000u;
-constexpr int kBins = 32;
+#ifndef DK_SAH_BINS
+#define DK_SAH_BINS 32
+#endif
+#ifndef DK_SAH_NODE_COST
+#define DK_SAH_NODE_COST 1.0f
+#endif
+constexpr int kBins = DK_SAH_BINS;
+constexpr float kNodeCost = DK_SAH_NODE_COST;  // traversal step cost in triangle tests
 
 inline float asFloat(uint32_t u) {
     float f;
@@ -86,7 +93,7 @@ std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth, uin
     }
     auto makeLeaf = [&]() { return std::move(node); };
     if (n == 1) return makeLeaf();
-    // Binned SAH over the three axes (traversal cost 1, intersection cost 1).
+    // Binned SAH over the three axes (traversal cost kNodeCost, intersection cost 1).
     float bestCost = FLT_MAX;
     int bestAxis = -1, bestSplit = -1;
     for (int a = 0; a < 3; ++a) {
@@ -125,7 +132,7 @@ std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth, uin
         }
     }
     float nodeArea = node->box.halfArea();
-    float splitCost = 1.0f + (nodeArea > 0.0f ? bestCost / nodeArea : 0.0f);
+    float splitCost = kNodeCost + (nodeArea > 0.0f ? bestCost / nodeArea : 0.0f);
     if (n <= maxLeaf && (bestAxis < 0 || (float)n <= splitCost)) return makeLeaf();
     uint32_t mid;
     if (bestAxis < 0) {  // coincident centroids: split the range in half

@@ -289,8 +289,9 @@ __device__ __forceinline__ void anyInit(AnyState& st, float3 o, float3 d, float 
     st.rec = rec;
 }
 
-// Children of an any-hit query are visited nearest first (DK_ANY_SORTED=1) or
-// in child order (0).
+// Children of an any-hit query are visited in the SAH tree's left-right order
+// (DK_ANY_SORTED=0, the default) or nearest first (1): an any-hit query needs
+// no order for its answer, and skipping the sort is the faster of the two.
 #ifndef DK_ANY_SORTED
 #define DK_ANY_SORTED 0
 #endif
@@ -303,12 +304,14 @@ __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* st
             Wide w;
             int k = wideVisit<DK_ANY_SORTED != 0>(S, st.node, st.o, st.inv, st.tmax, w);
             if (k > 0 && !DK_ANY_SORTED) {  // first hit child next, the others pushed
+                const uint32_t cA = w.c0, cB = w.c1, cC = w.c2, cD = w.c3;
+                const bool hA = w.t0 != INFINITY, hB = w.t1 != INFINITY, hC = w.t2 != INFINITY, hD = w.t3 != INFINITY;
                 uint32_t next = 0u;
                 bool have = false;
-                if (w.t3 != INFINITY) { next = w.c3; have = true; }
-                if (w.t2 != INFINITY) { if (have) stackNode[st.sp++] = (int)next; next = w.c2; have = true; }
-                if (w.t1 != INFINITY) { if (have) stackNode[st.sp++] = (int)next; next = w.c1; have = true; }
-                if (w.t0 != INFINITY) { if (have) stackNode[st.sp++] = (int)next; next = w.c0; }
+                if (hD) { next = cD; have = true; }
+                if (hC) { if (have) stackNode[st.sp++] = (int)next; next = cC; have = true; }
+                if (hB) { if (have) stackNode[st.sp++] = (int)next; next = cB; have = true; }
+                if (hA) { if (have) stackNode[st.sp++] = (int)next; next = cA; }
                 st.node = next;
                 continue;
             }
