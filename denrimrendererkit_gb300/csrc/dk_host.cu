@@ -166,6 +166,8 @@ struct Session {
     dk::DevJob* jobs = nullptr;  // device copy of the wave's job table (one job)
     dk::Arena arena;
     float4* staging = nullptr;
+    uint32_t* rgba8 = nullptr;     // display bytes (allocated on first use)
+    uint32_t* encodeWs = nullptr;  // display-encoding workspace
     cudaStream_t stream = nullptr;
     std::vector<cudaEvent_t> evPool;
     uint32_t sampleCount = 0;
@@ -808,6 +810,50 @@ int dk_session_read_output(dk_session* session, int output, float* rgba, size_t 
     DK_CUDA(cudaMemcpyAsync(rgba, src, pixels * sizeof(float4), cudaMemcpyDeviceToHost, s->stream), "readback");
     DK_CUDA(cudaStreamSynchronize(s->stream), "readback");
     return DK_OK;
+}
+
+// The output plane `output` of the session on the device (the resolved
+// beauty in the staging buffer, or an AOV plane).
+static int outputPlane(Session* s, int output, const float4** src) {
+    const size_t pixels = (size_t)s->settings.width * s->settings.height;
+    if (output < DK_OUTPUT_BEAUTY || output > DK_OUTPUT_MOTION_VECTOR)
+        return fail(DK_ERROR_INVALID_ARGUMENT, "unknown output kind");
+    if (output == DK_OUTPUT_BEAUTY) {
+        DK_CUDA(dk::launchResolveBeauty(s->accum, (uint32_t)pixels, s->staging, s->grids.final, s->stream), "resolve launch");
+        *src = s->staging;
+    } else {
+        *src = s->accum.aov + (size_t)(output - 1) * pixels;
+    }
+    return DK_OK;
+}
+
+int dk_session_read_rgba8(dk_session* session, int output, uint8_t* rgba, size_t bytes) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s || !rgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    const size_t pixels = (size_t)s->settings.width * s->settings.height;
+    if (bytes != pixels * 4) return fail(DK_ERROR_INVALID_ARGUMENT, "bytes must equal width*height*4");
+    const float4* src = nullptr;
+    int rc = outputPlane(s, output, &src);
+    if (rc != DK_OK) return rc;
+    if (!s->rgba8) {
+        int arc = s->arena.alloc(&s->rgba8, pixels, "display bytes");
+        if (arc != DK_OK) return arc;
+        arc = s->arena.alloc(&s->encodeWs, DK_ENCODE_WORKSPACE_BYTES / sizeof(uint32_t), "display workspace");
+        if (arc != DK_OK) return arc;
+    }
+    DK_CUDA(dk::encodeRgba8(src, (uint32_t)pixels, output, s->encodeWs, s->rgba8, s->stream), "encode launch");
+    DK_CUDA(cudaMemcpyAsync(rgba, s->rgba8, bytes, cudaMemcpyDeviceToHost, s->stream), "readback");
+    DK_CUDA(cudaStreamSynchronize(s->stream), "readback");
+    return DK_OK;
+}
+
+int dk_session_write_png(dk_session* session, int output, const char* path) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s || !path) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    std::vector<uint8_t> bytes((size_t)s->settings.width * s->settings.height * 4);
+    int rc = dk_session_read_rgba8(session, output, bytes.data(), bytes.size());
+    if (rc != DK_OK) return rc;
+    return dk::writePng(path, bytes.data(), s->settings.width, s->settings.height);
 }
 
 int dk_session_sample_count(const dk_session* session, uint32_t* out) {

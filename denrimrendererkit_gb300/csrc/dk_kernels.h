@@ -131,6 +131,10 @@ struct Wave {
     uint32_t pad;
 };
 
+// Display encoding and PNG export (dk_image.cu).
+cudaError_t encodeRgba8(const float4* px, uint32_t n, int kind, uint32_t* ws, uint32_t* out, cudaStream_t st);
+int writePng(const char* path, const uint8_t* rgba, uint32_t w, uint32_t h);
+
 // Host-side traversal BVH (dk_bvh.cu).
 bool referenceSlots(const dk_scene* sc, std::vector<uint32_t>& slotOfTri, std::string& err);
 // `width` 4 or 8 selects the node layout.

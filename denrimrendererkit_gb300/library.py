@@ -59,6 +59,10 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_session_update_camera": (i32, [P, C.POINTER(abi.Camera), C.POINTER(abi.Camera)]),
             "dk_session_reset": (i32, [P]),
             "dk_session_read_output": (i32, [P, i32, P, sz]),
+            "dk_session_read_rgba8": (i32, [P, i32, P, sz]),
+            "dk_session_write_png": (i32, [P, i32, C.c_char_p]),
+            "dk_encode_rgba8": (i32, [P, u32, u32, i32, P, P, P]),
+            "dk_write_png": (i32, [C.c_char_p, P, u32, u32]),
             "dk_session_sample_count": (i32, [P, C.POINTER(u32)]),
             "dk_session_stats": (i32, [P, C.POINTER(abi.Stats)]),
             "dk_session_destroy": (i32, [P]),

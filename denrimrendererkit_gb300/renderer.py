@@ -14,6 +14,7 @@ from __future__ import annotations
 import ctypes as C
 import dataclasses
 import enum
+import os
 from typing import Optional, Sequence
 
 import numpy as np
@@ -101,10 +102,28 @@ class RenderSession:
                                                   C.byref(self._handle)))
 
     # RenderSession.render(samples:) (RenderSession.swift:1010-1017)
-    def render(self, samples: int) -> None:
+    def render(self, samples: int, to: Optional[str] = None) -> None:
+        """RenderSession.render(samples:) and render(samples:to:) (RenderSession.swift:1010-1023):
+        with `to`, the beauty output is then written as a PNG file there."""
         if samples < 0:
             raise ValueError("Invalid render scene: Sample count must not be negative.")
         library.check(self._lib.dk_session_render(self._handle, samples))
+        if to is not None:
+            self.write_png(to)
+
+    # RenderSession.writePNG(output:to:) (RenderSession.swift:1026-1034)
+    def write_png(self, path: str, output: "RenderOutput" = None) -> None:
+        output = RenderOutput.BEAUTY if output is None else output
+        library.check(self._lib.dk_session_write_png(self._handle, int(output), os.fsencode(path)))
+
+    def rgba8(self, output: "RenderOutput" = None) -> np.ndarray:
+        """The output as the reference's PNG export shows it (PNGWriter.visualizedRGBA8Pixels,
+        Image/PNGWriter.swift:35-53), encoded on the device: uint8 (height, width, 4)."""
+        output = RenderOutput.BEAUTY if output is None else output
+        w, h = self.settings.width, self.settings.height
+        out = np.empty((h, w, 4), np.uint8)
+        library.check(self._lib.dk_session_read_rgba8(self._handle, int(output), out.ctypes.data, out.size))
+        return out
 
     def render_next_sample(self) -> None:
         self.render(1)

@@ -342,6 +342,44 @@ def cornell_box_reference(width: int = 24, height: int = 24) -> Workload:
     return Workload("cornell-box-reference", scene, RenderSettings(width=width, height=height, max_bounces=1), 1)
 
 
+def material_reference(width: int = 56, height: int = 56) -> Workload:
+    """RenderScene.materialReference() (Scene/RenderScene.swift:383-455) with the settings of
+    MaterialReferenceRenderTests.swift:11-19 (56x56, 2 bounces, final quality, 4 samples)."""
+    scene = RenderScene(camera=Camera((0, 1.65, 5.2), (0, 0.75, 0), vertical_field_of_view_degrees=38.0))
+    floor = scene.add_material(Material(base_color=(0.62, 0.62, 0.58)))
+    back = scene.add_material(Material(base_color=(0.38, 0.42, 0.48)))
+    warm = scene.add_material(Material(base_color=(0.95, 0.42, 0.24), roughness=0.8))
+    cool = scene.add_material(Material(base_color=(0.18, 0.44, 0.9), roughness=0.18, metallic=1.0))
+    green = scene.add_material(Material(base_color=(0.18, 0.72, 0.35), roughness=0.58, sheen=0.65,
+                                         sheen_color=(0.72, 1.0, 0.82), sheen_roughness=0.72))
+    violet = scene.add_material(Material(base_color=(0.62, 0.36, 0.95), roughness=0.35, metallic=0.55,
+                                          specular_color=(0.85, 0.72, 1.0), index_of_refraction=1.65, clearcoat=0.35,
+                                          clearcoat_roughness=0.06, clearcoat_index_of_refraction=1.55))
+    bright = scene.add_material(Material(base_color=(0.95, 0.86, 0.42), roughness=0.08, metallic=1.0))
+    light = scene.add_material(Material(base_color=(1, 1, 1), emission=(1, 0.9, 0.72), emission_strength=10.0))
+    scene.add(Mesh.quad((-3, 0, 2.2), (3, 0, 2.2), (3, 0, -2.2), (-3, 0, -2.2)), floor)
+    scene.add(Mesh.quad((-3, 0, -2.2), (3, 0, -2.2), (3, 2.8, -2.2), (-3, 2.8, -2.2)), back)
+    scene.add(Mesh.quad((-0.8, 2.75, -0.6), (0.8, 2.75, -0.6), (0.8, 2.75, 0.4), (-0.8, 2.75, 0.4)), light)
+    box = Mesh.box((-0.29, -0.29, -0.29), (0.29, 0.29, 0.29))  # Mesh.box(size: 0.58)
+    placements = [(warm, (-1.6, 0.29, 0.15)), (cool, (-0.8, 0.29, -0.1)), (green, (0, 0.29, 0.1)),
+                  (violet, (0.8, 0.29, -0.05)), (bright, (1.6, 0.29, 0.12))]
+    for index, (material, position) in enumerate(placements):
+        angle = float(np.float32(index) * np.float32(0.28) - np.float32(0.45))
+        scene.add(box, material, Transform.translation(position) * Transform.rotation_y(angle))
+    settings = RenderSettings(width=width, height=height, max_bounces=2, quality=RenderQuality.FINAL)
+    return Workload("material-reference", scene, settings, 4)
+
+
+def transparent_export_scene(width: int = 32, height: int = 32) -> Workload:
+    """TransparentExportRenderTests.floatingQuadScene() with the test's settings (32x32, 1 bounce,
+    transparent background, 1 sample)."""
+    scene = RenderScene(camera=Camera((0, 0, 3), (0, 0, 0), vertical_field_of_view_degrees=34.0))
+    m = scene.add_material(Material(base_color=(0.9, 0.2, 0.1), emission=(0.9, 0.2, 0.1), emission_strength=1.0))
+    scene.add(Mesh.quad((-0.45, -0.45, 0), (0.45, -0.45, 0), (0.45, 0.45, 0), (-0.45, 0.45, 0)), m)
+    settings = RenderSettings(width=width, height=height, max_bounces=1, transparent_background=True)
+    return Workload("transparent-export", scene, settings, 1)
+
+
 def parity_quad_scene(width: int = 16, height: int = 16) -> Workload:
     """HardwareTraversalParityTests.parityScene (:168-183)."""
     scene = RenderScene(camera=Camera((0, 0, 2), (0, 0, 0), vertical_field_of_view_degrees=34.0))

@@ -281,6 +281,28 @@ int dk_session_reset(dk_session* session);
  * output as RGBA32F into `rgba` (pixel_count = width*height pixels). */
 int dk_session_read_output(dk_session* session, int output, float* rgba, size_t pixel_count);
 
+/* PNGWriter.visualizedRGBA8Pixels (Image/PNGWriter.swift:35-53) on the device:
+ * the output as the reference's PNG export shows it (beauty tonemapped, depth
+ * normalised to its range, IDs hashed to colours, ...), 8-bit RGBA, row major,
+ * width*height*4 bytes into host `rgba`. */
+int dk_session_read_rgba8(dk_session* session, int output, uint8_t* rgba, size_t bytes);
+
+/* RenderSession.writePNG(output:to:) (RenderSession.swift:1026-1034): the
+ * output encoded as above, written as an 8-bit RGBA PNG file at `path`.
+ * DK_ERROR_EXPORT_FAILED when the file cannot be written. */
+int dk_session_write_png(dk_session* session, int output, const char* path);
+
+/* The same encoding of caller-owned device pixels: `pixels` RGBA32F (16-byte
+ * aligned, width*height), `rgba` device bytes (width*height*4, 4-byte
+ * aligned), `workspace` DK_ENCODE_WORKSPACE_BYTES of device memory; launched
+ * on `stream` (a cudaStream_t, may be null), not synchronised. */
+#define DK_ENCODE_WORKSPACE_BYTES 16
+int dk_encode_rgba8(const float* pixels, uint32_t width, uint32_t height, int output, uint8_t* rgba,
+                    void* workspace, void* stream);
+
+/* PNGWriter.write (PNGWriter.swift:55-70): host 8-bit RGBA bytes as a PNG file. */
+int dk_write_png(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height);
+
 /* RenderSession.sampleCount. */
 int dk_session_sample_count(const dk_session* session, uint32_t* out_count);
 
