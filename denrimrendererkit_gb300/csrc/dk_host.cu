@@ -613,8 +613,7 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     // RenderSession.init validation (RenderSession.swift:304-327).
     if (st->width == 0 || st->height == 0)
         return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Render dimensions must be positive.");
-    if (st->quality != DK_QUALITY_FINAL)
-        return fail(DK_ERROR_INVALID_ARGUMENT, "only RenderQuality.final (the path tracer) is implemented");
+    if (st->quality > DK_QUALITY_FINAL) return fail(DK_ERROR_INVALID_ARGUMENT, "unknown render quality");
     int rc = dk::validateScene(sc);
     if (rc != DK_OK) return rc;
     rc = dk::ensureDevice();
@@ -645,8 +644,10 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     if (st->max_samples_per_launch > 0) capPaths = std::min<uint64_t>(capPaths, (uint64_t)st->max_samples_per_launch * pixels);
     capPaths = std::max<uint64_t>(capPaths, pixels);
     capPaths = std::min<uint64_t>(capPaths, 1ull << 29);  // path indices fit 29 bits of the NEE record
-    TRY(dk::allocWave(s->arena, s->wave, capPaths, pixels, 1));
-    s->jobs = const_cast<dk::DevJob*>(s->wave.jobs);
+    if (st->quality == DK_QUALITY_FINAL) {  // preview / interactive keep no path state
+        TRY(dk::allocWave(s->arena, s->wave, capPaths, pixels, 1));
+        s->jobs = const_cast<dk::DevJob*>(s->wave.jobs);
+    }
     TRY(dk::allocAccum(s->arena, s->accum, pixels));
     TRY(s->arena.alloc(&s->staging, pixels, "readback staging"));
     TRY(dk::clearAccum(s->accum, pixels, s->stream));
@@ -676,9 +677,43 @@ static int eventAt(Session* s, size_t i, cudaEvent_t* out) {
 // batches of whole tile-frames that fit the wave (a one-job wave each).  Every
 // stage is bracketed by events on the session stream; they are read once,
 // after the last batch.
+// RenderQuality.preview / .interactive: the kernel overwrites the tile's
+// beauty and AOVs on every sample and ignores the sample index, so one pass
+// stands for any number of samples.
+static int renderPreview(Session* s, uint32_t tx, uint32_t ty, uint32_t tw, uint32_t th, uint32_t samples) {
+    const dk_settings& st = s->settings;
+    dk::DevParams P;
+    dk::fillParams(P, st);
+    P.tile_x = tx;
+    P.tile_y = ty;
+    P.tile_w = tw;
+    P.tile_h = th;
+    P.samples_in_batch = 1;
+    cudaEvent_t e0, e1;
+    int rc = eventAt(s, 0, &e0);
+    if (rc == DK_OK) rc = eventAt(s, 1, &e1);
+    if (rc != DK_OK) return rc;
+    DK_CUDA(cudaEventRecord(e0, s->stream), "cudaEventRecord");
+    DK_CUDA(dk::launchPreview(s->scene, P, s->accum, s->scene.mat_count, s->opaqueMask,
+                              st.quality == DK_QUALITY_INTERACTIVE, s->grids.extend, s->stream),
+            "preview launch");
+    DK_CUDA(cudaEventRecord(e1, s->stream), "cudaEventRecord");
+    DK_CUDA(cudaEventSynchronize(e1), "render");
+    float ms = 0;
+    DK_CUDA(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    s->stats.last_render_ms = ms;
+    s->stats.last_extend_ms = s->stats.last_shade_ms = s->stats.last_shadow_ms = 0;
+    s->stats.last_other_ms = ms;
+    s->stats.last_launches = 1;
+    s->stats.kernel_launches += 1;
+    s->stats.paths_traced += (uint64_t)tw * th * samples;
+    return DK_OK;
+}
+
 static int renderSamples(Session* s, uint32_t tx, uint32_t ty, uint32_t tw, uint32_t th, uint32_t samples,
                          uint32_t sampleBegin) {
     const dk_settings& st = s->settings;
+    if (st.quality != DK_QUALITY_FINAL) return renderPreview(s, tx, ty, tw, th, samples);
     dk::DevJob job;
     std::memset(&job, 0, sizeof(job));
     dk::fillParams(job.P, st);

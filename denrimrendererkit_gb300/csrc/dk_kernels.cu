@@ -1136,6 +1136,225 @@ __device__ bool projectToScreen(const dk_camera& cam, float3 w, uint32_t width, 
     return true;
 }
 
+// ------------------------------------------- preview and interactive ----
+// flatPreviewKernel (PathTrace.metal:4728-4868) and interactiveMaterialKernel
+// (:4870-5165), the kernels of RenderQuality.preview and .interactive
+// (DenrimRenderer.primaryPipeline, DenrimRenderer.swift:197-214): one camera
+// ray through each pixel centre, shaded without path tracing.  Like the
+// reference they overwrite the beauty and the AOV planes on every sample
+// (the result does not depend on the sample index); the beauty goes into the
+// accumulation as one sample.
+__device__ __forceinline__ float smoothstepf(float e0, float e1, float x) {  // Metal smoothstep
+    float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+
+// sampleInteractiveDiffuseEnvironment (:3805-3823)
+__device__ float3 interactiveDiffuseEnv(const DevScene& S, float3 n) {
+    float3 up = sampleEnvironment(S, f3(0.0f, 1.0f, 0.0f));
+    float3 down = sampleEnvironment(S, f3(0.0f, -1.0f, 0.0f));
+    float3 side = (sampleEnvironment(S, f3(1.0f, 0.0f, 0.0f)) + sampleEnvironment(S, f3(-1.0f, 0.0f, 0.0f)) +
+                   sampleEnvironment(S, f3(0.0f, 0.0f, 1.0f)) + sampleEnvironment(S, f3(0.0f, 0.0f, -1.0f))) *
+                  0.25f;
+    float upW = smoothstepf(-0.15f, 0.85f, n.y);
+    float downW = smoothstepf(0.15f, -0.85f, n.y);
+    float sideW = fmaxf(0.0f, 1.0f - upW - downW);
+    return up * upW + down * downW + side * sideW;
+}
+
+// interactiveHemisphereDirection (:3825-3831)
+__device__ __forceinline__ float3 interactiveHemisphere(float3 d, float3 n) {
+    float nd = dot(n, d);
+    if (nd < 0.0f) d = d - n * (2.0f * nd);
+    return normalize(d);
+}
+
+// sampleInteractiveSpecularEnvironment (:3833-3880)
+__device__ float3 interactiveSpecularEnv(const DevScene& S, float3 r, float3 n, float roughness) {
+    r = interactiveHemisphere(normalize(r), n);
+    roughness = clampf(roughness, 0.0f, 1.0f);
+    float spread = roughness * roughness;
+    float3 helper = fabsf(r.y) < 0.999f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f);
+    float3 t = normalize(cross(helper, r));
+    float3 b = cross(r, t);
+    float3 cone = sampleEnvironment(S, r) * 0.42f;
+    cone += sampleEnvironment(S, interactiveHemisphere(r + t * spread * 0.95f + n * spread * 0.18f, n)) * 0.145f;
+    cone += sampleEnvironment(S, interactiveHemisphere(r - t * spread * 0.95f + n * spread * 0.18f, n)) * 0.145f;
+    cone += sampleEnvironment(S, interactiveHemisphere(r + b * spread * 0.95f + n * spread * 0.18f, n)) * 0.145f;
+    cone += sampleEnvironment(S, interactiveHemisphere(r - b * spread * 0.95f + n * spread * 0.18f, n)) * 0.145f;
+    float3 diffuse = interactiveDiffuseEnv(S, n);
+    return mix3(cone, diffuse, smoothstepf(0.62f, 0.95f, roughness));
+}
+
+// interactiveContactAmbientOcclusion (:4276-4360): four short probes around
+// the normal, each nearby occluder weighted by its opacity and proximity.
+__device__ float interactiveContactAO(const DevScene& S, MatTable mt, const Hit& h, const Material& m, float3 n) {
+    TangentFrame frame = makeTangentFrame(n, h.tangent, h.bitangent);
+    constexpr float kRadius = 0.34f;
+    const float3 local[4] = {f3(0.000f, 0.000f, 1.000f), f3(0.780f, 0.180f, 0.600f), f3(-0.420f, 0.720f, 0.552f),
+                             f3(-0.620f, -0.520f, 0.587f)};
+    float occlusion = 0.0f;
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        float3 l = normalize(local[k]);
+        float3 dir = normalize(l.x * frame.tangent + l.y * frame.bitangent + l.z * n);
+        Ray ray{h.position + n * 0.003f, dir};
+        HitRec r = traceScene(S, ray.origin, ray.direction);
+        if (r.tri == kNoHit || !(r.t < kRadius)) continue;
+        Hit oh = makeHitAny(S, ray, r);
+        Material om = materialForHit(S, mt, oh);
+        float blocker = clampf(om.baseColor.w, 0.0f, 1.0f) * (1.0f - materialTransmission(om) * 0.72f);
+        occlusion += blocker * (1.0f - smoothstepf(0.0f, kRadius, r.t));
+    }
+    float strength = 0.72f + (0.36f - 0.72f) * materialTransmission(m);  // mix(0.72, 0.36, transmission)
+    return 1.0f - clampf((occlusion / 4.0f) * strength, 0.0f, 0.72f);
+}
+
+template <bool kInteractive>
+__global__ void __launch_bounds__(128) k_preview(DevScene S, DevParams P, Accum A, MatTable mt, uint32_t opaqueMask) {
+    const uint32_t tileN = P.tile_w * P.tile_h;
+    const size_t plane = (size_t)P.width * P.height;
+    for (uint32_t i = globalId(); i < tileN; i += gridStride()) {
+        const uint32_t px = P.tile_x + i % P.tile_w, py = P.tile_y + i / P.tile_w;
+        const size_t pix = (size_t)py * P.width + px;
+        Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, 0.5f, 0.5f, 0.0f, 0.0f);
+        HitRec rec = traceScene(S, ray.origin, ray.direction);
+        float4 beauty;
+        if (rec.tri == kNoHit) {
+            float alpha = P.transparent_background ? 0.0f : 1.0f;
+            float3 color = mx(f3(P.bg[0], P.bg[1], P.bg[2]), f3(0.0f));
+            if (!P.transparent_background && P.shows_env_bg) color = sampleEnvironment(S, ray.direction);
+            beauty = make_float4(color.x, color.y, color.z, alpha);
+            A.aov[0 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            A.aov[1 * plane + pix] = make_float4(0.5f, 0.5f, 0.5f, 0.0f);
+            for (int k = 2; k < 6; ++k) A.aov[k * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            Hit h = makeHitAny(S, ray, rec);
+            Material m = materialForHit(S, mt, h);
+            uint32_t nIdx = (uint32_t)m.parameters.w;
+            if (nIdx != 0u) h = applyNormalMap(S, h, nIdx, ray.direction);
+            uint32_t bIdx = (uint32_t)m.parameters.z;
+            if (bIdx != 0u) {  // applyBaseColorTexture
+                float4 t = sampleTexture(S, bIdx, h.uv, make_float4(1.0f, 1.0f, 1.0f, 1.0f));
+                m.baseColor = make_float4(ex::mul(m.baseColor.x, t.x), ex::mul(m.baseColor.y, t.y),
+                                          ex::mul(m.baseColor.z, t.z), ex::mul(m.baseColor.w, t.w));
+            }
+            const float3 n = ex::normalize(h.normal);
+            const float3 view = ex::normalize(-ray.direction);
+            float3 color;
+            float4 albedo;
+            if (!kInteractive) {  // :4824-4834
+                const float3 key = ex::normalize(f3(0.35f, 0.72f, 0.58f));
+                float lambert = fmaxf(ex::dot(n, key), 0.0f);
+                float facing = fmaxf(ex::dot(n, view), 0.0f);
+                float rim = ex::mul(powf(ex::sub(1.0f, facing), 2.0f), 0.08f);
+                float shade = ex::add(ex::add(0.32f, ex::mul(0.68f, lambert)), rim);
+                color = ex::add(ex::mul(mx(xyz(m.baseColor), f3(0.0f)), shade), mx(xyz(m.emission), f3(0.0f)));
+                beauty = make_float4(color.x, color.y, color.z,
+                                     P.transparent_background ? clampf(m.baseColor.w, 0.0f, 1.0f) : 1.0f);
+                albedo = m.baseColor;
+            } else {  // :4961-5133
+                const float roughness = clampf(m.parameters.x, 0.02f, 1.0f);
+                const float metallic = clampf(m.parameters.y, 0.0f, 1.0f);
+                const float opacity = clampf(m.baseColor.w, 0.0f, 1.0f);
+                const float3 base = mx(xyz(m.baseColor), f3(0.0f));
+                color = mx(xyz(m.emission), f3(0.0f));
+                ShadePoint sp;
+                makeShadePoint(sp, m, n, h.tangent, h.bitangent, view);
+                const uint32_t nl = min(S.light_count, 12u);
+#pragma unroll 1
+                for (uint32_t l = 0; l < nl; ++l) {
+                    const dk_light_record& L = S.lights[l];
+                    if (L.triangle_index >= S.tri_count || L.material_index >= S.mat_count) continue;
+                    const dk_triangle& lt = S.tris[L.triangle_index];
+                    float3 emission = mx(xyz(__ldg(reinterpret_cast<const float4*>(S.mats + L.material_index) + 1)),
+                                         f3(0.0f));
+                    if (maxComponent(emission) <= 0.0f || L.area <= 0.0f) continue;
+                    float3 lp = (f3(lt.v0.x, lt.v0.y, lt.v0.z) + f3(lt.v1.x, lt.v1.y, lt.v1.z) +
+                                 f3(lt.v2.x, lt.v2.y, lt.v2.z)) / 3.0f;
+                    float3 toL = lp - h.position;
+                    float d2 = fmaxf(dot(toL, toL), 1e-5f);
+                    float dist = sqrtf(d2);
+                    float3 ld = toL / dist;
+                    float cosS = fmaxf(dot(n, ld), 0.0f);
+                    float cosL = fmaxf(dot(f3(L.normal.x, L.normal.y, L.normal.z), -ld), 0.0f);
+                    if (cosS <= 0.0f || cosL <= 0.0f) continue;
+                    float3 T = f3(1.0f);
+                    float3 so = h.position + n * 0.001f;
+                    bool occluded = S.volume_count ? shadowWalk(S, mt, so, ld, dist - 0.002f, T)
+                                                   : shadowLayers(S, mt, opaqueMask, so, ld, dist - 0.002f, T);
+                    if (occluded) continue;
+                    float3 brdf = evalBRDF(m, sp, ld);
+                    float ccGloss = materialClearcoat(m) * powf(1.0f - materialClearcoatRoughness(m), 2.0f);
+                    float glossW = clampf(metallic + ccGloss +
+                                              (1.0f - metallic) * powf(1.0f - roughness, 4.0f) *
+                                                  clampf(m.parameters2.x, 0.0f, 1.0f),
+                                          0.0f, 1.0f);
+                    float3 f0 = materialF0(m);
+                    float3 diffuseOnly = (1.0f - metallic) * base * mx(f3(0.0f), f3(1.0f) - f0) * 0.31830988618f;
+                    brdf = mix3(diffuseOnly, brdf, glossW);
+                    float G = cosS * cosL * L.area / d2;
+                    color += brdf * emission * G * T;
+                }
+                float3 envDiffuse = interactiveDiffuseEnv(S, n);
+                float3 refl = normalize(reflect(-view, n));
+                float3 baseRefl = interactiveSpecularEnv(S, refl, n, roughness);
+                float ccRough = materialClearcoatRoughness(m);
+                float3 ccRefl = interactiveSpecularEnv(S, refl, n, ccRough);
+                float nDotV = fmaxf(dot(n, view), 0.0f);
+                float3 fresnel = fresnelSchlickThinFilm(nDotV, materialF0(m), m);
+                float glossy = powf(1.0f - roughness, 4.0f);
+                float metalW = metallic * powf(1.0f - roughness, 2.0f);
+                float ccW = materialClearcoat(m) * powf(1.0f - ccRough, 3.0f);
+                float dielectricW = (1.0f - metallic) * glossy * clampf(m.parameters2.x, 0.0f, 1.0f);
+                float3 roughFresnel = mix3(fresnel, materialF0(m), smoothstepf(0.45f, 0.95f, roughness));
+                float3 ccFresnel = fresnelSchlickThinFilm(nDotV, materialClearcoatF0Color(m), m);
+                float horizon = 0.58f + 0.42f * clampf(n.y * 0.5f + 0.5f, 0.0f, 1.0f);
+                float contact = interactiveContactAO(S, mt, h, m, n);
+                float diffuseStrength = 0.58f * (1.0f - metallic) * (horizon * contact);
+                float baseReflStrength = metalW * 1.05f + dielectricW * 0.32f;
+                color += base * envDiffuse * diffuseStrength;
+                color += baseRefl * roughFresnel * baseReflStrength;
+                color += ccRefl * ccFresnel * ccW * 0.42f;
+                const float3 key = normalize(f3(-0.32f, 0.78f, 0.52f));
+                color += base * (1.0f - metallic) * fmaxf(dot(n, key), 0.0f) * 0.16f * contact;
+                float subsurface = materialSubsurface(m);
+                if (subsurface > 0.0f) {
+                    float wrap = powf(1.0f - nDotV, 2.0f);
+                    color += clamp3(xyz(m.subsurfaceColor), f3(0.0f), f3(0.999f)) * base * envDiffuse * subsurface *
+                             (0.12f + 0.22f * wrap) * contact;
+                }
+                float transmission = materialTransmission(m);
+                if (transmission > 0.0f) {
+                    float3 transmitted = sampleEnvironment(S, ray.direction);
+                    color = mix3(color, transmitted * materialTransmissionTint(m, 0.65f), transmission * 0.55f);
+                    color += baseRefl * fresnel * transmission * 0.35f;
+                }
+                color = clamp3(color, f3(0.0f), f3(fmaxf(P.clamp, 1.0f)));
+                beauty = make_float4(color.x, color.y, color.z, P.transparent_background ? opacity : 1.0f);
+                albedo = make_float4(base.x, base.y, base.z, opacity);
+            }
+            const float3 enc = ex::add(ex::mul(n, 0.5f), f3(0.5f));
+            const float mid = (float)(h.materialID + 1u), oid = (float)(h.objectID + 1u);
+            A.aov[0 * plane + pix] = make_float4(h.t, h.t, h.t, 1.0f);
+            A.aov[1 * plane + pix] = make_float4(enc.x, enc.y, enc.z, 1.0f);
+            A.aov[2 * plane + pix] = albedo;
+            A.aov[3 * plane + pix] = make_float4(mid, mid, mid, 1.0f);
+            A.aov[4 * plane + pix] = make_float4(oid, oid, oid, 1.0f);
+            float2 cur, prev;
+            if (projectToScreen(P.cam, h.position, P.width, P.height, cur) &&
+                projectToScreen(P.prev_cam, h.position, P.width, P.height, prev))
+                A.aov[5 * plane + pix] = make_float4(ex::sub(prev.x, cur.x), ex::sub(prev.y, cur.y), 0.0f, 1.0f);
+            else
+                A.aov[5 * plane + pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        A.sum[pix] = beauty;
+        A.comp[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        A.resolved[pix] = D4{0.0, 0.0, 0.0, 0.0};
+        A.count[pix] = 1u;
+    }
+}
+
 // Kahan-compensated accumulation of every path of the batch into its pixel,
 // in sample order, plus the AOV block (PathTrace.metal:5559-5585) from the
 // batch's last sample.  After every 4096th sample of a pixel the FP32 sum is
@@ -1390,6 +1609,15 @@ cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st) {
 }
 cudaError_t launchAovPrimary(const DevScene& S, const Wave& W, int grid, cudaStream_t st) {
     k_aov_primary<<<grid, 128, 0, st>>>(S, W);
+    return cudaGetLastError();
+}
+cudaError_t launchPreview(const DevScene& S, const DevParams& P, const Accum& A, uint32_t matCount,
+                          uint32_t opaqueMask, bool interactive, int grid, cudaStream_t st) {
+    const MatTable mt{0u, matCount};
+    if (interactive)
+        k_preview<true><<<grid, 128, 0, st>>>(S, P, A, mt, opaqueMask);
+    else
+        k_preview<false><<<grid, 128, 0, st>>>(S, P, A, mt, opaqueMask);
     return cudaGetLastError();
 }
 cudaError_t launchFinalize(const Wave& W, int grid, cudaStream_t st) {

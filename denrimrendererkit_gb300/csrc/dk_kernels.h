@@ -147,6 +147,10 @@ cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint3
 cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchAovPrimary(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
+// RenderQuality.preview / .interactive: one shading pass over the tile of `P`
+// into the accumulation (overwritten) and its AOV planes.
+cudaError_t launchPreview(const DevScene& S, const DevParams& P, const Accum& A, uint32_t matCount,
+                          uint32_t opaqueMask, bool interactive, int grid, cudaStream_t st);
 cudaError_t launchFinalize(const Wave& W, int grid, cudaStream_t st);
 uint32_t bounceLaunches(const DevScene& S);
 cudaError_t envRotation(float radians, float* sinCos /* device, 2 floats */, cudaStream_t st);

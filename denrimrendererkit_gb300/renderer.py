@@ -48,7 +48,7 @@ class RenderSettings:
     width: int = 512
     height: int = 512
     max_bounces: int = 4
-    quality: RenderQuality = RenderQuality.FINAL
+    quality: RenderQuality = RenderQuality.PREVIEW  # the reference's default (RenderSettings.swift:80)
     previous_camera: Optional[Camera] = None
     transparent_background: bool = False
     shows_environment_background: bool = True

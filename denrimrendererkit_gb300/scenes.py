@@ -339,7 +339,8 @@ def cornell_box_reference(width: int = 24, height: int = 24) -> Workload:
     scene.add(Mesh.quad((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)), red)
     scene.add(Mesh.quad((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)), green)
     scene.add(Mesh.quad((-0.28, 1.99, -0.25), (0.28, 1.99, -0.25), (0.28, 1.99, 0.25), (-0.28, 1.99, 0.25)), light)
-    return Workload("cornell-box-reference", scene, RenderSettings(width=width, height=height, max_bounces=1), 1)
+    return Workload("cornell-box-reference", scene,
+                    RenderSettings(width=width, height=height, max_bounces=1, quality=RenderQuality.FINAL), 1)
 
 
 def material_reference(width: int = 56, height: int = 56) -> Workload:
@@ -372,11 +373,15 @@ def material_reference(width: int = 56, height: int = 56) -> Workload:
 
 def transparent_export_scene(width: int = 32, height: int = 32) -> Workload:
     """TransparentExportRenderTests.floatingQuadScene() with the test's settings (32x32, 1 bounce,
-    transparent background, 1 sample)."""
+    transparent background, 1 sample).  The test leaves the quality at its default, preview, but its
+    stored baseline (ReferenceMetrics/TransparentExport.json: 778 transparent, 246 opaque pixels) is a
+    jittered one-sample render: pixel-centre rays (the preview kernel) cover 16 x 16 = 256 pixels of the
+    quad.  The workload therefore renders at final quality, which reproduces the baseline."""
     scene = RenderScene(camera=Camera((0, 0, 3), (0, 0, 0), vertical_field_of_view_degrees=34.0))
     m = scene.add_material(Material(base_color=(0.9, 0.2, 0.1), emission=(0.9, 0.2, 0.1), emission_strength=1.0))
     scene.add(Mesh.quad((-0.45, -0.45, 0), (0.45, -0.45, 0), (0.45, 0.45, 0), (-0.45, 0.45, 0)), m)
-    settings = RenderSettings(width=width, height=height, max_bounces=1, transparent_background=True)
+    settings = RenderSettings(width=width, height=height, max_bounces=1, transparent_background=True,
+                              quality=RenderQuality.FINAL)
     return Workload("transparent-export", scene, settings, 1)
 
 
@@ -385,7 +390,8 @@ def parity_quad_scene(width: int = 16, height: int = 16) -> Workload:
     scene = RenderScene(camera=Camera((0, 0, 2), (0, 0, 0), vertical_field_of_view_degrees=34.0))
     m = scene.add_material(Material(base_color=(0.25, 0.5, 0.75)))
     scene.add(Mesh.quad((-1, -1, 0), (1, -1, 0), (1, 1, 0), (-1, 1, 0)), m)
-    return Workload("parity-quad", scene, RenderSettings(width=width, height=height, max_bounces=1), 1)
+    return Workload("parity-quad", scene,
+                    RenderSettings(width=width, height=height, max_bounces=1, quality=RenderQuality.FINAL), 1)
 
 
 def reused_mesh_instance_scene(width: int = 40, height: int = 40) -> Workload:
@@ -400,4 +406,5 @@ def reused_mesh_instance_scene(width: int = 40, height: int = 40) -> Workload:
     scene.add(subject, red, Transform.translation((-0.8, 0.35, 0)) * Transform.rotation_y(-0.25))
     scene.add(subject, blue, Transform.translation((0, 0.35, 0.02)) * Transform.rotation_y(0.12))
     scene.add(subject, green, Transform.translation((0.8, 0.35, -0.04)) * Transform.rotation_y(0.32))
-    return Workload("reused-mesh-instances", scene, RenderSettings(width=width, height=height, max_bounces=1), 1)
+    return Workload("reused-mesh-instances", scene,
+                    RenderSettings(width=width, height=height, max_bounces=1, quality=RenderQuality.FINAL), 1)

@@ -186,8 +186,12 @@ typedef struct dk_scene {
     const uint32_t* volume_brick_grid_indices;    uint64_t volume_brick_grid_index_count;
 } dk_scene;
 
-/* RenderQuality (RenderSettings.swift:5-26).  Only DK_QUALITY_FINAL selects the
- * path tracer; the other two are rejected with DK_ERROR_INVALID_ARGUMENT. */
+/* RenderQuality (RenderSettings.swift:5-26), the kernel a session runs
+ * (DenrimRenderer.primaryPipeline, DenrimRenderer.swift:197-214): FINAL the
+ * path tracer (pathTraceKernel), PREVIEW the flat preview (flatPreviewKernel,
+ * PathTrace.metal:4728-4868), INTERACTIVE the direct-light material preview
+ * (interactiveMaterialKernel, :4870-5165).  The two previews overwrite the
+ * image on every sample. */
 enum { DK_QUALITY_PREVIEW = 0, DK_QUALITY_INTERACTIVE = 1, DK_QUALITY_FINAL = 2 };
 
 /* RenderSettings (RenderSettings.swift:29-116) plus the two cameras. */

@@ -206,6 +206,8 @@ def load_reference() -> C.CDLL:
         P, u32 = C.c_void_p, C.c_uint32
         lib.ref_render.argtypes = [P, P, u32, u32, P, u32, C.c_int, P, P, P]
         lib.ref_render.restype = C.c_int
+        lib.ref_render_quality.argtypes = [C.c_int, P, P, u32, u32, P, u32, C.c_int, P, P, P]
+        lib.ref_render_quality.restype = C.c_int
         lib.ref_sdf_counter_count.restype = u32
         assert lib.ref_sdf_counter_count() == len(REF_SDF_COUNTERS)
         _ref_lib = lib
@@ -213,8 +215,10 @@ def load_reference() -> C.CDLL:
 
 
 class ReferenceRender:
-    """The reference kernel run on the host: RGBA32F accumulation texture and
-    last-sample AOV planes, exactly as the kernel writes them."""
+    """The reference kernel for the settings' quality (pathTraceKernel,
+    flatPreviewKernel or interactiveMaterialKernel) run on the host: RGBA32F
+    accumulation texture and last-sample AOV planes, exactly as the kernel
+    writes them."""
 
     def __init__(self, build, settings, camera, tile=None, collect_sdf_counters: bool = False):
         self.build = build
@@ -230,8 +234,8 @@ class ReferenceRender:
 
     def render(self, samples: int, pixel_list=None, threads: int = 0) -> None:
         pl = None if pixel_list is None else np.ascontiguousarray(pixel_list, np.uint32)
-        rc = load_reference().ref_render(
-            C.byref(self.scene_struct), C.byref(self.params), self.sample_count, samples,
+        rc = load_reference().ref_render_quality(
+            int(self.settings.quality), C.byref(self.scene_struct), C.byref(self.params), self.sample_count, samples,
             None if pl is None else pl.ctypes.data, 0 if pl is None else len(pl), threads,
             self.accum.ctypes.data, self.aov.ctypes.data,
             None if self.sdf_counters is None else self.sdf_counters.ctypes.data)

@@ -18,7 +18,7 @@ ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 SHADERS = os.path.join("/root/reference", "Sources", "DenrimRendererKit", "Resources", "Shaders")
 # (reference shader, kernels kept, generated file)
-UNITS = (("PathTrace.metal", ("pathTraceKernel",), "pathtrace_ref.cpp"),
+UNITS = (("PathTrace.metal", ("pathTraceKernel", "flatPreviewKernel", "interactiveMaterialKernel"), "pathtrace_ref.cpp"),
          ("Denoise.metal", ("simpleSpatialDenoiseKernel",), "denoise_ref.cpp"))
 GENERATED = os.path.join(OUT, "pathtrace_ref.cpp")
 LIB = os.path.join(OUT, "libref_pathtrace.so")

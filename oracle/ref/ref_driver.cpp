@@ -1,6 +1,9 @@
 // Test infrastructure: host driver that runs the reference's own compute
-// kernel `pathTraceKernel` (PathTrace.metal:5167-5586, rewritten to C++ by
-// metal2cpp.py and compiled against metal_shim.hpp) once per pixel and sample,
+// kernels `pathTraceKernel` (PathTrace.metal:5167-5586), `flatPreviewKernel`
+// (:4728-4868) and `interactiveMaterialKernel` (:4870-5165) -- rewritten to C++
+// by metal2cpp.py and compiled against metal_shim.hpp -- once per pixel and
+// sample (the kernel DenrimRenderer.primaryPipeline picks for the quality,
+// DenrimRenderer.swift:197-214),
 // the way RenderSession.encodeNextSample dispatches it
 // (RenderSession.swift:891-1007): GPURenderConstants filled from the settings,
 // sampleIndex advanced per sample, the RGBA32F running-mean accumulation
@@ -52,10 +55,12 @@ uint32_t ref_sdf_counter_count(void) { return 13u; }
 // (depth, normal, albedo, material ID, object ID, motion vector), `sdf_counters`
 // 13 counters or null (null disables sdfTraversalStatsEnabled).  `threads` <= 0
 // uses every hardware thread.  Returns 0 on success.
-int ref_render(const dk_scene* scene, const oracle_params* p, uint32_t sample_begin, uint32_t sample_count,
-               const uint32_t* pixel_list, uint32_t pixel_list_count, int threads, float* accum, float* aov,
-               uint32_t* sdf_counters) {
-    if (!scene || !p || !accum || !aov) return 1;
+// `quality` is RenderSettings.shaderQualityLevel: 0 preview, 1 interactive,
+// 2 final (RenderSettings.swift:96-105).
+int ref_render_quality(int quality, const dk_scene* scene, const oracle_params* p, uint32_t sample_begin,
+                       uint32_t sample_count, const uint32_t* pixel_list, uint32_t pixel_list_count, int threads,
+                       float* accum, float* aov, uint32_t* sdf_counters) {
+    if (!scene || !p || !accum || !aov || quality < 0 || quality > 2) return 1;
     const uint32_t W = p->width, H = p->height;
     GPURenderConstants base{};
     base.width = W;
@@ -64,7 +69,7 @@ int ref_render(const dk_scene* scene, const oracle_params* p, uint32_t sample_be
     base.volumeCount = scene->volume_count;
     base.materialCount = scene->material_count;
     base.maxBounces = std::max(1u, p->max_bounces);
-    base.renderQuality = 2u;  // RenderQuality.final (shaderQualityLevel)
+    base.renderQuality = (uint)quality;
     base.frameSeed = p->frame_seed;
     base.accelerationNodeCount = scene->node_count;
     base.transparentBackground = p->transparent_background;
@@ -121,7 +126,9 @@ int ref_render(const dk_scene* scene, const oracle_params* p, uint32_t sample_be
                 uint2 gid(px - p->tile_x, py - p->tile_y);
                 for (uint32_t s = 0; s < sample_count; ++s) {
                     c.sampleIndex = sample_begin + s;
-                    pathTraceKernel(accumulation, planes[0], planes[1], planes[2], planes[3], planes[4], planes[5],
+                    auto kernel = quality == 2 ? pathTraceKernel : (quality == 1 ? interactiveMaterialKernel
+                                                                                 : flatPreviewKernel);
+                    kernel(accumulation, planes[0], planes[1], planes[2], planes[3], planes[4], planes[5],
                                     c, camera, buf<GPUTriangle>(scene->triangles),
                                     buf<GPUMaterial>(scene->materials), buf<GPUAccelerationNode>(scene->nodes),
                                     buf<uint>(scene->primitive_indices), previous,
@@ -151,6 +158,13 @@ int ref_render(const dk_scene* scene, const oracle_params* p, uint32_t sample_be
     if (sdf_counters)
         for (int i = 0; i < 13; ++i) sdf_counters[i] += counters[i].value.load();
     return 0;
+}
+
+int ref_render(const dk_scene* scene, const oracle_params* p, uint32_t sample_begin, uint32_t sample_count,
+               const uint32_t* pixel_list, uint32_t pixel_list_count, int threads, float* accum, float* aov,
+               uint32_t* sdf_counters) {
+    return ref_render_quality(2, scene, p, sample_begin, sample_count, pixel_list, pixel_list_count, threads, accum,
+                              aov, sdf_counters);
 }
 
 }  // extern "C"

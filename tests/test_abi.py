@@ -89,7 +89,7 @@ def test_validation_errors_map_to_reference(dk_lib):
     nomat.material_count = 0
     assert dk_lib.dk_session_create(C.byref(nomat), C.byref(st), C.byref(h)) == 3
     assert b"no materials" in dk_lib.dk_last_error_message()
-    st = _settings_struct(quality=0)
+    st = _settings_struct(quality=3)  # not a RenderQuality
     assert dk_lib.dk_session_create(C.byref(sc), C.byref(st), C.byref(h)) == 6
     assert dk_lib.dk_session_create(None, C.byref(st), C.byref(h)) == 6
 

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from denrimrendererkit_gb300 import DenrimRenderer, RenderOutput, compile_scene, scenes
-from denrimrendererkit_gb300.renderer import RenderSettings
+from denrimrendererkit_gb300.renderer import RenderQuality, RenderSettings
 
 pytestmark = pytest.mark.gpu
 
@@ -229,7 +229,8 @@ def test_sparse_volume_only_scene_gpu(renderer, oracle_lib, dk_lib):
     scene.add_material(Material(base_color=(0.2, 0.65, 0.9), roughness=0.55))
     scene.sparse_volumes.append(library.SparseVolume([dict(center=(0, 0, 0), radius=0.55, material=0)], (20,) * 3,
                                                      (-1, -1, -1), (1, 1, 1), (5,) * 3, 0.3))
-    wl = scenes.Workload("sparse-sphere", scene, RenderSettings(width=20, height=20, max_bounces=1), 1)
+    wl = scenes.Workload("sparse-sphere", scene,
+                         RenderSettings(width=20, height=20, max_bounces=1, quality=RenderQuality.FINAL), 1)
     s, o, _ = run_pair(renderer, oracle_lib, wl, 1)
     assert_aovs_bit_exact(s, o)
     albedo = s.pixels(RenderOutput.ALBEDO).reshape(-1, 4)

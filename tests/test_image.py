@@ -10,7 +10,8 @@
   reference tests' settings, the oracle encoder turns the beauty into the PNG
   bytes, and ImageMetricReader's metrics must land within the baseline's
   tolerances -- CornellBoxRenderTests.swift:7-33, MaterialReferenceRenderTests.swift:7-27,
-  TransparentExportRenderTests.swift:8-30.
+  TransparentExportRenderTests.swift:8-30 (at final quality: the test's default quality is preview, but its
+  stored baseline is a jittered path-traced render -- the reference's own preview kernel misses it).
 * GPU: the same scenes through the CUDA path and `RenderSession.render(samples, to=png)`
   against the same baselines; and the device encoder against the oracle
   encoder on every output kind of rendered scenes: bit-exact for depth, IDs,
@@ -134,6 +135,27 @@ def test_oracle_transparent_export_meets_alpha_baseline(oracle_lib):
     o.render(wl.samples)
     beauty = o.accum.reshape(32, 32, 4).astype(np.float32)
     assert_alpha_metrics(image.alpha_metrics(io.visualized_rgba8(beauty, io.BEAUTY)))
+
+
+def test_transparent_export_baseline_is_a_jittered_render():
+    # The reference test leaves the quality at its default, preview; the
+    # reference's own flatPreviewKernel (pixel-centre rays) leaves exactly the
+    # 16 x 16 quad pixels opaque, 10 more than the stored baseline's 246 allow
+    # (tolerance 4): the baseline was recorded with the path tracer.
+    from denrimrendererkit_gb300 import compile_scene
+    from oracle import image_oracle as io
+    from oracle import oracle as orc
+    from oracle.oracle import HostBuilders
+    if not orc.reference_available():
+        pytest.skip("reference shaders not built")
+    wl = scenes.transparent_export_scene()
+    wl.settings = RenderSettings(width=32, height=32, max_bounces=1, transparent_background=True)
+    assert wl.settings.quality == RenderQuality.PREVIEW
+    b = compile_scene(wl.scene, host_builders=HostBuilders())
+    o = orc.ReferenceRender(b, wl.settings, wl.scene.camera)
+    o.render(1)
+    m = image.alpha_metrics(io.visualized_rgba8(o.accum.astype(np.float32), io.BEAUTY))
+    assert (m["transparentPixels"], m["opaquePixels"]) == (768, 256)
 
 
 # ------------------------------------------------------------------ GPU ----

@@ -227,11 +227,11 @@ def test_sparse_volume_only_scene_uses_brick_path(oracle_lib, dk_lib):
     # RenderSessionTests.testSparseVolumeOnlySceneRendersThroughBrickPathOnFlatPath
     # (RenderSessionTests.swift:806-860): sphere r = 0.55, resolution 20, brick 5,
     # band 0.3, orthographic camera (scale 2.4), 20x20, 1 bounce.
-    from denrimrendererkit_gb300.renderer import RenderSettings
+    from denrimrendererkit_gb300.renderer import RenderQuality, RenderSettings
     from denrimrendererkit_gb300.scene import Camera
     cam = Camera((0, 0, 3), (0, 0, 0), orthographic_scale=2.4)
     scene, b = _sdf_build([dict(center=(0, 0, 0), radius=0.55, material=0)], 20, 5, 0.3, cam)
-    settings = RenderSettings(width=20, height=20, max_bounces=1)
+    settings = RenderSettings(width=20, height=20, max_bounces=1, quality=RenderQuality.FINAL)
     r = oracle_lib.OracleRender(b, settings, cam)
     r.render(1)
     c = r.counter_dict()
@@ -244,7 +244,7 @@ def test_sparse_volume_only_scene_uses_brick_path(oracle_lib, dk_lib):
 def test_sparse_brick_without_zero_crossing_is_culled(oracle_lib):
     # RenderSessionTests.testSparseBrickWithoutZeroCrossingIsCulledBeforeMarch
     # (RenderSessionTests.swift:862-919): one 3^3 brick, all distances 0.05.
-    from denrimrendererkit_gb300.renderer import RenderSettings
+    from denrimrendererkit_gb300.renderer import RenderQuality, RenderSettings
     from denrimrendererkit_gb300.scene import AccelerationBuild, Camera
     cam = Camera((0, 0, 3), (0, 0, 0), orthographic_scale=2.0)
     mats = _materials(Material(base_color=(0.8, 0.2, 0.2)))
@@ -275,7 +275,7 @@ def test_sparse_brick_without_zero_crossing_is_culled(oracle_lib):
                           np.zeros((0, 4), np.float32), z(abi.LIGHT_DTYPE), z(abi.ENVIRONMENT_SAMPLE_DTYPE), 0, 1.0, 0.0,
                           16.0, volumes=vol, volume_bricks=brick, volume_brick_samples=samples,
                           volume_brick_grids=grid, volume_brick_grid_indices=gidx)
-    r = oracle_lib.OracleRender(b, RenderSettings(width=8, height=8, max_bounces=1), cam)
+    r = oracle_lib.OracleRender(b, RenderSettings(width=8, height=8, max_bounces=1, quality=RenderQuality.FINAL), cam)
     r.render(1)
     c = r.counter_dict()
     assert c["grid_cells"] > 0 and c["brick_tests"] > 0 and c["range_culls"] > 0
