@@ -2,7 +2,8 @@
  * denrim_cuda.h — C ABI of the GB300 (sm_103a) progressive path-tracing backend.
  *
  * This header is the drop-in seam for DenrimRendererKit's `final`-quality path
- * tracer (and the preview / interactive kernels of the same dispatch point).  The reference binds its GPU work in `RenderSession.init`
+ * tracer (and the preview / interactive kernels of the same dispatch point).
+ * The reference binds its GPU work in `RenderSession.init`
  * (Sources/DenrimRendererKit/Renderer/RenderSession.swift:292-579), which turns a
  * `RenderScene` into an `AccelerationBuild`
  * (Sources/DenrimRendererKit/Acceleration/AccelerationBuild.swift:4-48) and then
