@@ -166,6 +166,7 @@ EXPORTED_SYMBOLS = (
     "dk_session_sample_count", "dk_session_stats",
     "dk_session_destroy", "dk_last_error_message", "dk_build_bvh", "dk_build_lights",
     "dk_build_environment_samples", "dk_build_environment_samples_noalloc", "dk_build_sparse_sphere_volume",
+    "dk_bake_sparse_sphere_volume",
     "dk_sparse_volume_view", "dk_sparse_volume_destroy", "dk_version",
     "dk_server_create", "dk_server_submit", "dk_server_step", "dk_server_start", "dk_server_stop",
     "dk_server_wait", "dk_server_job_status", "dk_server_read_output", "dk_server_release",

@@ -73,6 +73,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_build_environment_samples_noalloc": (i32, [P, u32, u32, C.c_float, C.c_float, P,
                                                              C.POINTER(u32), P]),
             "dk_build_sparse_sphere_volume": (i32, [P, u32, C.POINTER(abi.SparseVolumeSettings), C.POINTER(P)]),
+            "dk_bake_sparse_sphere_volume": (i32, [P, u32, C.POINTER(abi.SparseVolumeSettings), C.POINTER(P)]),
             "dk_sparse_volume_view": (i32, [P, C.POINTER(abi.Scene)]),
             "dk_sparse_volume_destroy": (i32, [P]),
             "dk_version": (C.c_char_p, []),
@@ -164,13 +165,17 @@ def build_environment_samples(texture, intensity: float, max_radiance: float) ->
 
 
 class SparseVolume:
-    """A sparse distance volume built by dk_build_sparse_sphere_volume; the
-    arrays are numpy views of the library-owned buffers (valid while this
-    object lives)."""
+    """A sparse distance volume built by dk_bake_sparse_sphere_volume on the GPU
+    (`on_device` None: when a CUDA device is present) or by the host build
+    dk_build_sparse_sphere_volume (the two are bit-identical); the arrays are
+    numpy views of the library-owned buffers (valid while this object lives)."""
 
     def __init__(self, spheres, resolution, bounds_min, bounds_max, brick_size, narrow_band, volume_material=0,
-                 object_id=0, primitive_id=0):
+                 object_id=0, primitive_id=0, on_device=None):
         lib = load()
+        if on_device is None:
+            n = C.c_int(0)
+            on_device = lib.dk_device_count(C.byref(n)) == 0 and n.value > 0
         arr = (abi.SdfSphere * len(spheres))()
         for i, s in enumerate(spheres):
             arr[i].center[:] = [float(x) for x in s["center"]]
@@ -186,7 +191,8 @@ class SparseVolume:
         st.volume_material = volume_material
         st.object_id, st.primitive_id = object_id, primitive_id
         self._h = C.c_void_p()
-        check(lib.dk_build_sparse_sphere_volume(arr, len(spheres), C.byref(st), C.byref(self._h)))
+        build = lib.dk_bake_sparse_sphere_volume if on_device else lib.dk_build_sparse_sphere_volume
+        check(build(arr, len(spheres), C.byref(st), C.byref(self._h)))
         view = abi.Scene()
         check(lib.dk_sparse_volume_view(self._h, C.byref(view)))
 

@@ -378,6 +378,13 @@ typedef struct dk_sparse_volume dk_sparse_volume;
 int dk_build_sparse_sphere_volume(const dk_sdf_sphere* spheres, uint32_t sphere_count,
                                   const dk_sparse_volume_settings* settings, dk_sparse_volume** out_volume);
 
+/* The same volume baked on the current CUDA device (DistanceFieldBaker's
+ * sparse GPU path, Scene/DistanceFieldBaker.swift:700-966 with
+ * SDFBake.metal:1056-1200: classify bricks, sample the kept ones), bit-identical
+ * to dk_build_sparse_sphere_volume; the arrays are returned in host memory. */
+int dk_bake_sparse_sphere_volume(const dk_sdf_sphere* spheres, uint32_t sphere_count,
+                                 const dk_sparse_volume_settings* settings, dk_sparse_volume** out_volume);
+
 /* Points the volume fields of `scene` at the built arrays (owned by the volume). */
 int dk_sparse_volume_view(const dk_sparse_volume* volume, dk_scene* scene);
 
