@@ -24,6 +24,8 @@
 // index), (v2 - v0, flags: bit 0 = blocks shadow rays, bits 8..15 material
 // ID).
 #include <algorithm>
+#include <deque>
+#include <mutex>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -78,85 +80,231 @@ struct Box {
 
 struct TNode {
     Box box;
-    std::unique_ptr<TNode> l, r;
+    TNode* l = nullptr;
+    TNode* r = nullptr;
     uint32_t first = 0, count = 0;  // triangle range of the subtree (in SAH order)
 };
 
-std::unique_ptr<TNode> build(Prim* p, uint32_t first, uint32_t n, int depth, uint32_t maxLeaf) {
-    auto node = std::make_unique<TNode>();
+// Nodes come from per-task chunked arenas (one heap allocation per 16K nodes,
+// not per node); the arenas live until the wide tree has been emitted.
+class NodeArena {
+  public:
+    TNode* alloc() {
+        if (chunks_.empty() || used_ == kChunk) {
+            chunks_.emplace_back(new TNode[kChunk]);
+            used_ = 0;
+        }
+        return &chunks_.back()[used_++];
+    }
+
+  private:
+    static constexpr size_t kChunk = 16384;
+    std::vector<std::unique_ptr<TNode[]>> chunks_;
+    size_t used_ = 0;
+};
+
+struct Arenas {
+    std::mutex m;
+    std::deque<NodeArena> list;
+    NodeArena& make() {
+        std::lock_guard<std::mutex> g(m);
+        list.emplace_back();
+        return list.back();
+    }
+};
+
+// Per-axis bins of one node: the union of the primitive boxes, the union of
+// their centroids, and the count, for each of kBins centroid bins.  Only the
+// counts are initialised: a bin's boxes are set by its first primitive and
+// read only while its count is non-zero (an empty bin is the identity of the
+// union), so a small node does not pay for the whole table.
+struct AxisBins {
+    Box box[kBins], cen[kBins];
+    uint32_t cnt[kBins];
+};
+
+struct NodeBins {
+    AxisBins axis[3];
+    NodeBins() {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < kBins; ++b) axis[a].cnt[b] = 0;
+    }
+    void add(int a, int b, const Prim& q) {
+        AxisBins& ab = axis[a];
+        if (ab.cnt[b]++ == 0) {
+            for (int k = 0; k < 3; ++k) {
+                ab.box[b].mn[k] = q.mn[k];
+                ab.box[b].mx[k] = q.mx[k];
+                ab.cen[b].mn[k] = ab.cen[b].mx[k] = q.c[k];
+            }
+        } else {
+            ab.box[b].grow(q.mn, q.mx);
+            ab.cen[b].grow(q.c, q.c);
+        }
+    }
+    void merge(const NodeBins& o) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < kBins; ++b) {
+                if (o.axis[a].cnt[b] == 0) continue;
+                if (axis[a].cnt[b] == 0) {
+                    axis[a].box[b] = o.axis[a].box[b];
+                    axis[a].cen[b] = o.axis[a].cen[b];
+                } else {
+                    axis[a].box[b].grow(o.axis[a].box[b]);
+                    axis[a].cen[b].grow(o.axis[a].cen[b]);
+                }
+                axis[a].cnt[b] += o.axis[a].cnt[b];
+            }
+    }
+};
+
+inline int binOf(float c, float lo, float scale) { return std::min(kBins - 1, (int)((c - lo) * scale)); }
+
+void binRange(const Prim* p, uint32_t begin, uint32_t end, const Box& cb, const float* scale, const bool* live,
+              NodeBins& nb) {
+    for (uint32_t i = begin; i < end; ++i)
+        for (int a = 0; a < 3; ++a)
+            if (live[a]) nb.add(a, binOf(p[i].c[a], cb.mn[a], scale[a]), p[i]);
+}
+
+// Binned SAH (traversal cost kNodeCost, intersection cost 1) over the node's
+// primitives [first, first + n), whose box and centroid box are given.
+// Children inherit their boxes from the chosen split's bins (unions, exact).
+TNode* build(Prim* p, uint32_t first, uint32_t n, int depth, uint32_t maxLeaf, const Box& box, const Box& cb,
+             Arenas& arenas, NodeArena& arena) {
+    TNode* node = arena.alloc();
+    node->box = box;
     node->first = first;
     node->count = n;
-    Box cb;
-    for (uint32_t i = first; i < first + n; ++i) {
-        node->box.grow(p[i].mn, p[i].mx);
-        cb.grow(p[i].c, p[i].c);
+    if (n == 1) return node;
+    float scale[3];
+    bool live[3];
+    for (int a = 0; a < 3; ++a) {
+        float ext = cb.mx[a] - cb.mn[a];
+        live[a] = ext > 0.0f;
+        scale[a] = live[a] ? (float)kBins / ext : 0.0f;
     }
-    auto makeLeaf = [&]() { return std::move(node); };
-    if (n == 1) return makeLeaf();
-    // Binned SAH over the three axes (traversal cost kNodeCost, intersection cost 1).
+    NodeBins nb;
+    const uint32_t kParallelBins = 1u << 18;
+    if (n >= kParallelBins) {  // large node: bin slices on several threads, merge the unions
+        const uint32_t parts = std::min<uint32_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+        std::vector<NodeBins> partial(parts);
+        std::vector<std::thread> pool;
+        for (uint32_t t = 0; t < parts; ++t)
+            pool.emplace_back([&, t] {
+                uint32_t b0 = first + (uint32_t)((uint64_t)n * t / parts), b1 = first + (uint32_t)((uint64_t)n * (t + 1) / parts);
+                binRange(p, b0, b1, cb, scale, live, partial[t]);
+            });
+        for (auto& th : pool) th.join();
+        for (uint32_t t = 0; t < parts; ++t) nb.merge(partial[t]);
+    } else {
+        binRange(p, first, first + n, cb, scale, live, nb);
+    }
+    // The sweeps visit the non-empty bins only: the cost of a split after an
+    // empty bin equals the cost after the last non-empty bin before it, and
+    // the strict `<` keeps that earlier bin, which is the split the full
+    // 32-bin sweep selects.
     float bestCost = FLT_MAX;
     int bestAxis = -1, bestSplit = -1;
     for (int a = 0; a < 3; ++a) {
-        float ext = cb.mx[a] - cb.mn[a];
-        if (!(ext > 0.0f)) continue;
-        Box bins[kBins];
-        uint32_t counts[kBins] = {};
-        float scale = (float)kBins / ext;
-        for (uint32_t i = first; i < first + n; ++i) {
-            int b = std::min(kBins - 1, (int)((p[i].c[a] - cb.mn[a]) * scale));
-            bins[b].grow(p[i].mn, p[i].mx);
-            ++counts[b];
-        }
+        if (!live[a]) continue;
+        const AxisBins& ab = nb.axis[a];
+        int nz[kBins], m = 0;
+        for (int b = 0; b < kBins; ++b)
+            if (ab.cnt[b]) nz[m++] = b;
         float rightArea[kBins];
         uint32_t rightCount[kBins];
         Box acc;
         uint32_t cnt = 0;
-        for (int b = kBins - 1; b > 0; --b) {
-            acc.grow(bins[b]);
-            cnt += counts[b];
-            rightArea[b] = acc.halfArea();
-            rightCount[b] = cnt;
+        for (int k = m - 1; k > 0; --k) {  // right side from the k-th non-empty bin on
+            acc.grow(ab.box[nz[k]]);
+            cnt += ab.cnt[nz[k]];
+            rightArea[k] = acc.halfArea();
+            rightCount[k] = cnt;
         }
         acc = Box();
         cnt = 0;
-        for (int b = 0; b < kBins - 1; ++b) {
-            acc.grow(bins[b]);
-            cnt += counts[b];
-            if (cnt == 0 || rightCount[b + 1] == 0) continue;
-            float cost = acc.halfArea() * (float)cnt + rightArea[b + 1] * (float)rightCount[b + 1];
+        for (int k = 0; k + 1 < m; ++k) {
+            acc.grow(ab.box[nz[k]]);
+            cnt += ab.cnt[nz[k]];
+            float cost = acc.halfArea() * (float)cnt + rightArea[k + 1] * (float)rightCount[k + 1];
             if (cost < bestCost) {
                 bestCost = cost;
                 bestAxis = a;
-                bestSplit = b;
+                bestSplit = nz[k];
             }
         }
     }
-    float nodeArea = node->box.halfArea();
+    float nodeArea = box.halfArea();
     float splitCost = kNodeCost + (nodeArea > 0.0f ? bestCost / nodeArea : 0.0f);
-    if (n <= maxLeaf && (bestAxis < 0 || (float)n <= splitCost)) return makeLeaf();
+    if (n <= maxLeaf && (bestAxis < 0 || (float)n <= splitCost)) return node;
     uint32_t mid;
-    if (bestAxis < 0) {  // coincident centroids: split the range in half
-        mid = first + n / 2;
-    } else {
-        float ext = cb.mx[bestAxis] - cb.mn[bestAxis];
-        float scale = (float)kBins / ext;
-        float lo = cb.mn[bestAxis];
-        int a = bestAxis, s = bestSplit;
-        Prim* m = std::partition(p + first, p + first + n, [=](const Prim& q) {
-            return std::min(kBins - 1, (int)((q.c[a] - lo) * scale)) <= s;
-        });
+    Box lb, rb, lc, rc;
+    bool haveBoxes = false;
+    if (bestAxis >= 0) {
+        const int a = bestAxis, sp = bestSplit;
+        const float lo = cb.mn[a], sc = scale[a];
+        Prim* m = std::partition(p + first, p + first + n, [=](const Prim& q) { return binOf(q.c[a], lo, sc) <= sp; });
         mid = (uint32_t)(m - p);
-        if (mid == first || mid == first + n) mid = first + n / 2;
+        if (mid != first && mid != first + n) {
+            const AxisBins& ab = nb.axis[a];
+            for (int b = 0; b < kBins; ++b) {
+                if (!ab.cnt[b]) continue;
+                (b <= sp ? lb : rb).grow(ab.box[b]);
+                (b <= sp ? lc : rc).grow(ab.cen[b]);
+            }
+            haveBoxes = true;
+        } else {
+            mid = first + n / 2;
+        }
+    } else {  // coincident centroids: split the range in half
+        mid = first + n / 2;
     }
-    if (n > 65536 && depth < 6) {
-        auto fut = std::async(std::launch::async, [=] { return build(p, first, mid - first, depth + 1, maxLeaf); });
-        node->r = build(p, mid, first + n - mid, depth + 1, maxLeaf);
+    if (!haveBoxes) {  // a range split: boxes of the two halves
+        for (uint32_t i = first; i < mid; ++i) {
+            lb.grow(p[i].mn, p[i].mx);
+            lc.grow(p[i].c, p[i].c);
+        }
+        for (uint32_t i = mid; i < first + n; ++i) {
+            rb.grow(p[i].mn, p[i].mx);
+            rc.grow(p[i].c, p[i].c);
+        }
+    }
+    if (n > 16384 && depth < 9) {
+        NodeArena& other = arenas.make();
+        auto fut = std::async(std::launch::async, [&, first, mid, depth, maxLeaf] {
+            return build(p, first, mid - first, depth + 1, maxLeaf, lb, lc, arenas, other);
+        });
+        node->r = build(p, mid, first + n - mid, depth + 1, maxLeaf, rb, rc, arenas, arena);
         node->l = fut.get();
     } else {
-        node->l = build(p, first, mid - first, depth + 1, maxLeaf);
-        node->r = build(p, mid, first + n - mid, depth + 1, maxLeaf);
+        node->l = build(p, first, mid - first, depth + 1, maxLeaf, lb, lc, arenas, arena);
+        node->r = build(p, mid, first + n - mid, depth + 1, maxLeaf, rb, rc, arenas, arena);
     }
     return node;
+}
+
+// The tree over all primitives; the root's boxes from a parallel pass.
+TNode* buildTree(std::vector<Prim>& prims, uint32_t maxLeaf, Arenas& arenas) {
+    const uint32_t n = (uint32_t)prims.size();
+    const uint32_t parts = std::min<uint32_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<Box> pb(parts), pc(parts);
+    std::vector<std::thread> pool;
+    for (uint32_t t = 0; t < parts; ++t)
+        pool.emplace_back([&, t] {
+            uint32_t b0 = (uint32_t)((uint64_t)n * t / parts), b1 = (uint32_t)((uint64_t)n * (t + 1) / parts);
+            for (uint32_t i = b0; i < b1; ++i) {
+                pb[t].grow(prims[i].mn, prims[i].mx);
+                pc[t].grow(prims[i].c, prims[i].c);
+            }
+        });
+    for (auto& th : pool) th.join();
+    Box box, cb;
+    for (uint32_t t = 0; t < parts; ++t) {
+        box.grow(pb[t]);
+        cb.grow(pc[t]);
+    }
+    return build(prims.data(), 0, n, 0, maxLeaf, box, cb, arenas, arenas.make());
 }
 
 // 4-wide node record (8 x float4): child boxes as x-min, x-max, y-min, y-max,
@@ -176,7 +324,7 @@ void setChild4(float4* rec, int lane, const Box& b, uint32_t ref) {
 // interior child of largest surface area until there are four.
 uint32_t flatten4(const TNode* t, std::vector<float4>& nodes, uint32_t dummyLeaf, int depth, int& maxDepth) {
     maxDepth = std::max(maxDepth, depth);
-    std::vector<const TNode*> kids = {t->l.get(), t->r.get()};
+    std::vector<const TNode*> kids = {t->l, t->r};
     while (kids.size() < 4) {
         int best = -1;
         float area = -1.0f;
@@ -187,8 +335,8 @@ uint32_t flatten4(const TNode* t, std::vector<float4>& nodes, uint32_t dummyLeaf
             }
         if (best < 0) break;
         const TNode* open = kids[best];
-        kids[best] = open->l.get();
-        kids.insert(kids.begin() + best + 1, open->r.get());
+        kids[best] = open->l;
+        kids.insert(kids.begin() + best + 1, open->r);
     }
     uint32_t idx = (uint32_t)(nodes.size() / 8);
     nodes.resize(nodes.size() + 8);
@@ -294,7 +442,7 @@ struct Wide8Builder {
     // opening the interior child of largest surface area, up to eight.
     static std::vector<const TNode*> collapse(const TNode* t) {
         if (wideLeaf(t)) return {t};  // a single-leaf tree: the root holds the leaf
-        std::vector<const TNode*> kids = {t->l.get(), t->r.get()};
+        std::vector<const TNode*> kids = {t->l, t->r};
         while (kids.size() < 8) {
             int best = -1;
             float area = -1.0f;
@@ -305,8 +453,8 @@ struct Wide8Builder {
                 }
             if (best < 0) break;
             const TNode* open = kids[best];
-            kids[best] = open->l.get();
-            kids.push_back(open->r.get());
+            kids[best] = open->l;
+            kids.push_back(open->r);
         }
         return kids;
     }
@@ -457,11 +605,12 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
     if (n == 0) return DK_OK;
     if (width == 8) {
         // Leaves of <= 4 triangles: eight of them fill a node's 32-bit slot mask.
-        std::unique_ptr<TNode> root = build(prims.data(), 0, n, 0, 4);
+        Arenas arenas;
+        TNode* root = buildTree(prims, 4, arenas);
         isect.reserve(3 * (size_t)n);
         nodes.resize(5);
         Wide8Builder wb{prims, sc, slotOfTri, opaque, nodes, isect};
-        wb.emit(root.get(), 0, 0);
+        wb.emit(root, 0, 0);
         // Each node visit pushes at most one group of siblings.
         if (wb.maxDepth + 1 > (int)kTraversalStack) {
             err = "traversal BVH deeper than the traversal stack";
@@ -469,7 +618,8 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
         }
         return DK_OK;
     }
-    std::unique_ptr<TNode> root = build(prims.data(), 0, n, 0, 8);
+    Arenas arenas;
+    TNode* root = buildTree(prims, 8, arenas);
     isect.resize(3 * (size_t)(n + 1));
     for (uint32_t s = 0; s < n; ++s) {
         const dk_triangle& t = sc->triangles[prims[s].tri];
@@ -493,7 +643,7 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
         nodes[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return DK_OK;
     }
-    flatten4(root.get(), nodes, dummyLeaf, 0, maxDepth);
+    flatten4(root, nodes, dummyLeaf, 0, maxDepth);
     // Each level pushes at most three siblings on the 64-entry traversal stack.
     if (3 * (maxDepth + 1) + 1 > 64) {
         err = "traversal BVH deeper than the 64-entry stack";
