@@ -113,13 +113,13 @@ struct Arenas {
     }
 };
 
-// Per-axis bins of one node: the union of the primitive boxes, the union of
-// their centroids, and the count, for each of kBins centroid bins.  Only the
-// counts are initialised: a bin's boxes are set by its first primitive and
-// read only while its count is non-zero (an empty bin is the identity of the
-// union), so a small node does not pay for the whole table.
+// Per-axis bins of one node: the union of the primitive boxes and the count,
+// for each of kBins centroid bins.  Only the counts are initialised: a bin's
+// box is set by its first primitive and read only while its count is
+// non-zero (an empty bin is the identity of the union), so a small node does
+// not pay for the whole table.
 struct AxisBins {
-    Box box[kBins], cen[kBins];
+    Box box[kBins];
     uint32_t cnt[kBins];
 };
 
@@ -135,24 +135,19 @@ struct NodeBins {
             for (int k = 0; k < 3; ++k) {
                 ab.box[b].mn[k] = q.mn[k];
                 ab.box[b].mx[k] = q.mx[k];
-                ab.cen[b].mn[k] = ab.cen[b].mx[k] = q.c[k];
             }
         } else {
             ab.box[b].grow(q.mn, q.mx);
-            ab.cen[b].grow(q.c, q.c);
         }
     }
     void merge(const NodeBins& o) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < kBins; ++b) {
                 if (o.axis[a].cnt[b] == 0) continue;
-                if (axis[a].cnt[b] == 0) {
+                if (axis[a].cnt[b] == 0)
                     axis[a].box[b] = o.axis[a].box[b];
-                    axis[a].cen[b] = o.axis[a].cen[b];
-                } else {
+                else
                     axis[a].box[b].grow(o.axis[a].box[b]);
-                    axis[a].cen[b].grow(o.axis[a].cen[b]);
-                }
                 axis[a].cnt[b] += o.axis[a].cnt[b];
             }
     }
@@ -169,7 +164,8 @@ void binRange(const Prim* p, uint32_t begin, uint32_t end, const Box& cb, const 
 
 // Binned SAH (traversal cost kNodeCost, intersection cost 1) over the node's
 // primitives [first, first + n), whose box and centroid box are given.
-// Children inherit their boxes from the chosen split's bins (unions, exact).
+// Children inherit their boxes from the chosen split's bins (unions, exact);
+// their centroid boxes come from one pass over the partitioned primitives.
 TNode* build(Prim* p, uint32_t first, uint32_t n, int depth, uint32_t maxLeaf, const Box& box, const Box& cb,
              Arenas& arenas, NodeArena& arena) {
     TNode* node = arena.alloc();
@@ -251,8 +247,9 @@ TNode* build(Prim* p, uint32_t first, uint32_t n, int depth, uint32_t maxLeaf, c
             for (int b = 0; b < kBins; ++b) {
                 if (!ab.cnt[b]) continue;
                 (b <= sp ? lb : rb).grow(ab.box[b]);
-                (b <= sp ? lc : rc).grow(ab.cen[b]);
             }
+            for (uint32_t i = first; i < mid; ++i) lc.grow(p[i].c, p[i].c);
+            for (uint32_t i = mid; i < first + n; ++i) rc.grow(p[i].c, p[i].c);
             haveBoxes = true;
         } else {
             mid = first + n / 2;
