@@ -617,15 +617,30 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
     }
     Arenas arenas;
     TNode* root = buildTree(prims, 8, arenas);
+    // The leaf slots in SAH order, filled by several threads while this
+    // thread collapses the tree (the two are independent).
     isect.resize(3 * (size_t)(n + 1));
-    for (uint32_t s = 0; s < n; ++s) {
-        const dk_triangle& t = sc->triangles[prims[s].tri];
-        isect[3 * (size_t)s + 0] = make_float4(t.v0.x, t.v0.y, t.v0.z, asFloat(slotOfTri[prims[s].tri]));
-        isect[3 * (size_t)s + 1] = make_float4(t.v1.x - t.v0.x, t.v1.y - t.v0.y, t.v1.z - t.v0.z, asFloat(prims[s].tri));
-        uint32_t mid = std::min(std::min(t.material_id, sc->material_count - 1u), 255u);
-        uint32_t flags = (opaque[prims[s].tri] ? 1u : 0u) | (mid << 8);
-        isect[3 * (size_t)s + 2] = make_float4(t.v2.x - t.v0.x, t.v2.y - t.v0.y, t.v2.z - t.v0.z, asFloat(flags));
-    }
+    auto fillSlots = [&](uint32_t b0, uint32_t b1) {
+        for (uint32_t s = b0; s < b1; ++s) {
+            const dk_triangle& t = sc->triangles[prims[s].tri];
+            isect[3 * (size_t)s + 0] = make_float4(t.v0.x, t.v0.y, t.v0.z, asFloat(slotOfTri[prims[s].tri]));
+            isect[3 * (size_t)s + 1] =
+                make_float4(t.v1.x - t.v0.x, t.v1.y - t.v0.y, t.v1.z - t.v0.z, asFloat(prims[s].tri));
+            uint32_t mid = std::min(std::min(t.material_id, sc->material_count - 1u), 255u);
+            uint32_t flags = (opaque[prims[s].tri] ? 1u : 0u) | (mid << 8);
+            isect[3 * (size_t)s + 2] = make_float4(t.v2.x - t.v0.x, t.v2.y - t.v0.y, t.v2.z - t.v0.z, asFloat(flags));
+        }
+    };
+    std::vector<std::thread> fill;
+    const uint32_t parts = std::min<uint32_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+    for (uint32_t t = 0; t < parts; ++t)
+        fill.emplace_back(fillSlots, (uint32_t)((uint64_t)n * t / parts), (uint32_t)((uint64_t)n * (t + 1) / parts));
+    struct Join {
+        std::vector<std::thread>& v;
+        ~Join() {
+            for (auto& th : v) th.join();
+        }
+    } join{fill};
     isect[3 * (size_t)n + 0] = make_float4(0, 0, 0, asFloat(0xffffffffu));  // dummy slot (degenerate)
     isect[3 * (size_t)n + 1] = make_float4(0, 0, 0, asFloat(0u));
     isect[3 * (size_t)n + 2] = make_float4(0, 0, 0, 0);

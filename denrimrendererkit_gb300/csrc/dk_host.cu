@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <future>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -275,26 +276,46 @@ static int traversalWidth() {
     return (e && e[0] == '8' && e[1] == 0) ? 8 : 4;
 }
 
-int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity) {
+TraversalBuild buildTraversal(const dk_scene* sc) {
     // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
     // reaches, each carrying its reference DFS slot as the tie-break key.
-    std::vector<float4> tNodes, tIsect;
-    bool allOpaque = true;
-    const int width = traversalWidth();
-    {
-        std::vector<uint32_t> slotOf;
-        std::string err;
-        if (!referenceSlots(sc, slotOf, err)) return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: " + err + ".");
-        std::vector<uint8_t> opaque(sc->triangle_count);
-        for (uint32_t i = 0; i < sc->triangle_count; ++i) {
-            const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
-            // shadowOccluded (PathTrace.metal:4230-4241): cut-outs pass, transmissive layers tint.
-            opaque[i] = materialBlocksShadow(m) ? 1 : 0;
-            if (!opaque[i] && slotOf[i] != kNoSlot) allOpaque = false;
-        }
-        int brc = buildSahTraversal(sc, slotOf, opaque, width, tNodes, tIsect, err);
-        if (brc != DK_OK) return fail(brc, "Invalid render scene: " + err + ".");
+    TraversalBuild t;
+    t.width = traversalWidth();
+    std::vector<uint32_t> slotOf;
+    std::string err;
+    if (!referenceSlots(sc, slotOf, err)) {
+        t.rc = DK_ERROR_INVALID_SCENE;
+        t.err = "Invalid render scene: " + err + ".";
+        return t;
     }
+    std::vector<uint8_t> opaque(sc->triangle_count);
+    for (uint32_t i = 0; i < sc->triangle_count; ++i) {
+        const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
+        // shadowOccluded (PathTrace.metal:4230-4241): cut-outs pass, transmissive layers tint.
+        opaque[i] = materialBlocksShadow(m) ? 1 : 0;
+        if (!opaque[i] && slotOf[i] != kNoSlot) t.allOpaque = false;
+    }
+    t.rc = buildSahTraversal(sc, slotOf, opaque, t.width, t.nodes, t.isect, err);
+    if (t.rc != DK_OK) t.err = "Invalid render scene: " + err + ".";
+    return t;
+}
+
+int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity,
+                std::future<TraversalBuild>* pending) {
+    // The traversal tree is built on another thread (`pending`, started by
+    // the caller before its own allocations) or here; the other arrays are
+    // uploaded meanwhile.
+    std::future<TraversalBuild> local;
+    if (!pending) {
+        local = std::async(std::launch::async, [sc] { return buildTraversal(sc); });
+        pending = &local;
+    }
+    struct Wait {  // the build reads `sc`: it must end before this returns
+        std::future<TraversalBuild>* f;
+        ~Wait() {
+            if (f->valid()) f->wait();
+        }
+    } wait{pending};
     std::memset(&D, 0, sizeof(D));
 #define TRY(x)                         \
     do {                               \
@@ -309,8 +330,6 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
                 "materials");
         D.mats = mats;
     }
-    TRY(arena.upload(const_cast<float4**>(&D.isect), tIsect.data(), tIsect.size(), "triangle slots"));
-    TRY(arena.upload(const_cast<float4**>(&D.nodes), tNodes.data(), tNodes.size(), "BVH nodes"));
     TRY(arena.upload(const_cast<dk_texture_descriptor**>(&D.texdesc), sc->texture_descriptors,
                      sc->texture_descriptor_count, "texture descriptors"));
     TRY(arena.upload(const_cast<float4**>(&D.texpix), reinterpret_cast<const float4*>(sc->texture_pixels),
@@ -365,12 +384,18 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
             if (!materialBlocksShadow(sc->materials[i])) volOpaque = false;
         D.volume_all_opaque = volOpaque ? 1u : 0u;
     }
+    {
+        TraversalBuild t = pending->get();
+        if (t.rc != DK_OK) return fail(t.rc, t.err);
+        TRY(arena.upload(const_cast<float4**>(&D.isect), t.isect.data(), t.isect.size(), "triangle slots"));
+        TRY(arena.upload(const_cast<float4**>(&D.nodes), t.nodes.data(), t.nodes.size(), "BVH nodes"));
+        D.node_count = (uint32_t)(t.nodes.size() / (t.width == 8 ? 5 : 8));
+        D.wide8 = t.width == 8 ? 1u : 0u;
+        D.all_shadow_opaque = t.allOpaque ? 1u : 0u;
+    }
 #undef TRY
     D.tri_count = sc->triangle_count;
     D.mat_count = sc->material_count;
-    D.node_count = (uint32_t)(tNodes.size() / (width == 8 ? 5 : 8));
-    D.wide8 = width == 8 ? 1u : 0u;
-    D.all_shadow_opaque = allOpaque ? 1u : 0u;
     D.texdesc_count = sc->texture_descriptor_count;
     D.light_count = sc->lights ? sc->light_count : 0;
     D.env_count = sc->environment_samples ? sc->environment_sample_count : 0;
@@ -618,6 +643,15 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     if (rc != DK_OK) return rc;
     rc = dk::ensureDevice();
     if (rc != DK_OK) return rc;
+    // The host traversal build runs while this thread allocates the wave.
+    std::future<dk::TraversalBuild> traversal =
+        std::async(std::launch::async, [sc] { return dk::buildTraversal(sc); });
+    struct WaitBuild {  // the build reads `sc`: it must end before this returns
+        std::future<dk::TraversalBuild>& f;
+        ~WaitBuild() {
+            if (f.valid()) f.wait();
+        }
+    } waitBuild{traversal};
 
     Session* s = new Session();
     std::memset(&s->stats, 0, sizeof(s->stats));
@@ -635,9 +669,6 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
         freeSession(s);
         return fail(DK_ERROR_COMMAND_FAILED, "cudaStreamCreate failed");
     }
-    TRY(dk::uploadScene(s->arena, sc, s->scene, sc->material_count));
-    s->opaqueMask = dk::opaqueMask(sc->materials, sc->material_count);
-
     // Wave capacity: whole frames of the tile, up to a fixed path budget.
     const uint32_t pixels = st->width * st->height;
     uint64_t capPaths = 1ull << 24;  // 16.8 M paths (~3.5 GB of path state)
@@ -650,6 +681,8 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     }
     TRY(dk::allocAccum(s->arena, s->accum, pixels));
     TRY(s->arena.alloc(&s->staging, pixels, "readback staging"));
+    TRY(dk::uploadScene(s->arena, sc, s->scene, sc->material_count, &traversal));
+    s->opaqueMask = dk::opaqueMask(sc->materials, sc->material_count);
     TRY(dk::clearAccum(s->accum, pixels, s->stream));
     if (cudaMemsetAsync(s->accum.aov, 0, 6 * (size_t)pixels * sizeof(float4), s->stream) != cudaSuccess ||
         cudaStreamSynchronize(s->stream) != cudaSuccess) {

@@ -5,6 +5,7 @@
 #pragma once
 #include <cstdint>
 #include <functional>
+#include <future>
 #include <string>
 #include <vector>
 
@@ -59,7 +60,20 @@ int validateScene(const dk_scene* sc);
 // Uploads `sc` into `D` (traversal BVH, environment guide table, sparse-volume
 // arrays).  `materialCapacity` >= sc->material_count reserves room in D.mats
 // for per-render material tables appended later.
-int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity);
+// The traversal tree of a scene (host work, see dk_bvh.cu), built apart from
+// the upload so that it can run while the caller allocates device memory.
+struct TraversalBuild {
+    int rc = DK_OK;
+    std::string err;
+    int width = 4;
+    bool allOpaque = true;
+    std::vector<float4> nodes, isect;
+};
+TraversalBuild buildTraversal(const dk_scene* sc);
+// Uploads the scene; `pending` (may be null) is a traversal build already
+// started with std::async(buildTraversal).
+int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity,
+                std::future<TraversalBuild>* pending = nullptr);
 
 // Whether a material blocks shadow rays (shadowOccluded, PathTrace.metal:
 // 4230-4241), and the opacity bits of a table's first 32 materials.
