@@ -83,6 +83,7 @@ struct TNode {
     TNode* l = nullptr;
     TNode* r = nullptr;
     uint32_t first = 0, count = 0;  // triangle range of the subtree (in SAH order)
+    uint32_t wide = 0;              // 4-wide nodes of the collapsed subtree rooted here
 };
 
 // Nodes come from per-task chunked arenas (one heap allocation per 16K nodes,
@@ -160,6 +161,25 @@ void binRange(const Prim* p, uint32_t begin, uint32_t end, const Box& cb, const 
     for (uint32_t i = begin; i < end; ++i)
         for (int a = 0; a < 3; ++a)
             if (live[a]) nb.add(a, binOf(p[i].c[a], cb.mn[a], scale[a]), p[i]);
+}
+
+// The union of the centroids of [begin, end) (several threads for a long range).
+void centroidBounds(const Prim* p, uint32_t begin, uint32_t end, Box& out) {
+    const uint32_t n = end - begin;
+    if (n < (1u << 18)) {
+        for (uint32_t i = begin; i < end; ++i) out.grow(p[i].c, p[i].c);
+        return;
+    }
+    const uint32_t parts = std::min<uint32_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<Box> part(parts);
+    std::vector<std::thread> pool;
+    for (uint32_t t = 0; t < parts; ++t)
+        pool.emplace_back([&, t] {
+            uint32_t b0 = begin + (uint32_t)((uint64_t)n * t / parts), b1 = begin + (uint32_t)((uint64_t)n * (t + 1) / parts);
+            for (uint32_t i = b0; i < b1; ++i) part[t].grow(p[i].c, p[i].c);
+        });
+    for (auto& th : pool) th.join();
+    for (const Box& b : part) out.grow(b);
 }
 
 // Binned SAH (traversal cost kNodeCost, intersection cost 1) over the node's
@@ -248,8 +268,8 @@ TNode* build(Prim* p, uint32_t first, uint32_t n, int depth, uint32_t maxLeaf, c
                 if (!ab.cnt[b]) continue;
                 (b <= sp ? lb : rb).grow(ab.box[b]);
             }
-            for (uint32_t i = first; i < mid; ++i) lc.grow(p[i].c, p[i].c);
-            for (uint32_t i = mid; i < first + n; ++i) rc.grow(p[i].c, p[i].c);
+            centroidBounds(p, first, mid, lc);
+            centroidBounds(p, mid, first + n, rc);
             haveBoxes = true;
         } else {
             mid = first + n / 2;
@@ -316,42 +336,95 @@ void setChild4(float4* rec, int lane, const Box& b, uint32_t ref) {
     reinterpret_cast<uint32_t*>(rec + 6)[lane] = ref;
 }
 
-// Collapses the binary tree under `t` (an interior node) into 4-wide nodes:
-// a node's children are the binary subtrees reached by repeatedly opening the
-// interior child of largest surface area until there are four.
-uint32_t flatten4(const TNode* t, std::vector<float4>& nodes, uint32_t dummyLeaf, int depth, int& maxDepth) {
-    maxDepth = std::max(maxDepth, depth);
-    std::vector<const TNode*> kids = {t->l, t->r};
-    while (kids.size() < 4) {
+// The children of the 4-wide node at interior node `t`: the binary subtrees
+// reached by repeatedly opening the interior child of largest surface area
+// until there are four.
+int collapse4(const TNode* t, const TNode* kids[4]) {
+    int k = 2;
+    kids[0] = t->l;
+    kids[1] = t->r;
+    while (k < 4) {
         int best = -1;
         float area = -1.0f;
-        for (int i = 0; i < (int)kids.size(); ++i)
+        for (int i = 0; i < k; ++i)
             if (kids[i]->l && kids[i]->box.halfArea() > area) {
                 area = kids[i]->box.halfArea();
                 best = i;
             }
         if (best < 0) break;
         const TNode* open = kids[best];
+        for (int i = k; i > best + 1; --i) kids[i] = kids[i - 1];
         kids[best] = open->l;
-        kids.insert(kids.begin() + best + 1, open->r);
+        kids[best + 1] = open->r;
+        ++k;
     }
-    uint32_t idx = (uint32_t)(nodes.size() / 8);
-    nodes.resize(nodes.size() + 8);
-    uint32_t refs[4];
-    for (size_t k = 0; k < kids.size(); ++k)
-        refs[k] = kids[k]->l ? flatten4(kids[k], nodes, dummyLeaf, depth + 1, maxDepth)
-                             : (kLeaf | (kids[k]->first << 3) | (kids[k]->count - 1u));
-    float4* rec = &nodes[8 * (size_t)idx];
+    return k;
+}
+
+// Counts the 4-wide nodes of every collapsed subtree (TNode::wide) and the
+// tree depth; large subtrees on other threads.
+uint32_t count4(TNode* t, int depth, int& maxDepth) {
+    maxDepth = std::max(maxDepth, depth);
+    const TNode* kids[4];
+    const int k = collapse4(t, kids);
+    uint32_t total = 1;
+    std::vector<std::future<std::pair<uint32_t, int>>> forks;
+    for (int i = 0; i < k; ++i) {
+        if (!kids[i]->l) continue;
+        TNode* c = const_cast<TNode*>(kids[i]);
+        if (depth < 5 && c->count > 65536) {
+            forks.push_back(std::async(std::launch::async, [c, depth] {
+                int md = 0;
+                uint32_t w = count4(c, depth + 1, md);
+                return std::make_pair(w, md);
+            }));
+        } else {
+            total += count4(c, depth + 1, maxDepth);
+        }
+    }
+    for (auto& f : forks) {
+        auto r = f.get();
+        total += r.first;
+        maxDepth = std::max(maxDepth, r.second);
+    }
+    t->wide = total;
+    return total;
+}
+
+// Writes the 4-wide node of `t` at index `idx` and its subtree after it in
+// depth-first order (interior children's subtrees in child order), into the
+// pre-sized `nodes`; large subtrees on other threads.
+void emit4(const TNode* t, uint32_t idx, float4* nodes, uint32_t dummyLeaf, int depth) {
+    const TNode* kids[4];
+    const int k = collapse4(t, kids);
+    uint32_t refs[4], next = idx + 1;
+    for (int i = 0; i < k; ++i) {
+        if (kids[i]->l) {
+            refs[i] = next;
+            next += kids[i]->wide;
+        } else {
+            refs[i] = kLeaf | (kids[i]->first << 3) | (kids[i]->count - 1u);
+        }
+    }
+    float4* rec = nodes + 8 * (size_t)idx;
     Box far;
     for (int a = 0; a < 3; ++a) far.mn[a] = far.mx[a] = 1e30f;
-    for (int k = 0; k < 4; ++k) {
-        if (k < (int)kids.size())
-            setChild4(rec, k, kids[k]->box, refs[k]);
+    for (int i = 0; i < 4; ++i) {
+        if (i < k)
+            setChild4(rec, i, kids[i]->box, refs[i]);
         else
-            setChild4(rec, k, far, dummyLeaf);
+            setChild4(rec, i, far, dummyLeaf);
     }
     rec[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    return idx;
+    std::vector<std::future<void>> forks;
+    for (int i = 0; i < k; ++i) {
+        if (!kids[i]->l) continue;
+        if (depth < 5 && kids[i]->wide > 8192)
+            forks.push_back(std::async(std::launch::async, [=] { emit4(kids[i], refs[i], nodes, dummyLeaf, depth + 1); }));
+        else
+            emit4(kids[i], refs[i], nodes, dummyLeaf, depth + 1);
+    }
+    for (auto& f : forks) f.get();
 }
 
 // 8-wide node record (5 x 16 bytes):
@@ -655,7 +728,9 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
         nodes[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         return DK_OK;
     }
-    flatten4(root, nodes, dummyLeaf, 0, maxDepth);
+    const uint32_t wideNodes = count4(root, 0, maxDepth);
+    nodes.resize(8 * (size_t)wideNodes);
+    emit4(root, 0, nodes.data(), dummyLeaf, 0);
     // Each level pushes at most three siblings on the 64-entry traversal stack.
     if (3 * (maxDepth + 1) + 1 > 64) {
         err = "traversal BVH deeper than the 64-entry stack";
