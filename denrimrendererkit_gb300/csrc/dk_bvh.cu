@@ -650,20 +650,44 @@ bool referenceSlots(const dk_scene* sc, std::vector<uint32_t>& slotOfTri, std::s
 int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri,
                       const std::vector<uint8_t>& opaque, int width, std::vector<float4>& nodes,
                       std::vector<float4>& isect, std::string& err) {
-    std::vector<Prim> prims;
-    prims.reserve(sc->triangle_count);
-    for (uint32_t i = 0; i < sc->triangle_count; ++i) {
-        if (slotOfTri[i] == kNoSlot) continue;
-        const dk_triangle& t = sc->triangles[i];
-        Prim p;
-        const float* v[3] = {&t.v0.x, &t.v1.x, &t.v2.x};
-        for (int a = 0; a < 3; ++a) {
-            p.mn[a] = std::fmin(std::fmin(v[0][a], v[1][a]), v[2][a]);
-            p.mx[a] = std::fmax(std::fmax(v[0][a], v[1][a]), v[2][a]);
-            p.c[a] = 0.5f * (p.mn[a] + p.mx[a]);
-        }
-        p.tri = i;
-        prims.push_back(p);
+    // Primitives of the triangles that have a slot, in triangle order: the
+    // slotted triangles are counted per chunk, then every chunk writes its
+    // primitives at its offset (several threads).
+    const uint32_t tc = sc->triangle_count;
+    const uint32_t parts = std::min<uint32_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<uint32_t> offset(parts + 1, 0);
+    auto chunk = [&](uint32_t t, uint32_t& b0, uint32_t& b1) {
+        b0 = (uint32_t)((uint64_t)tc * t / parts);
+        b1 = (uint32_t)((uint64_t)tc * (t + 1) / parts);
+    };
+    for (uint32_t t = 0; t < parts; ++t) {
+        uint32_t b0, b1;
+        chunk(t, b0, b1);
+        uint32_t c = 0;
+        for (uint32_t i = b0; i < b1; ++i) c += slotOfTri[i] != kNoSlot;
+        offset[t + 1] = offset[t] + c;
+    }
+    std::vector<Prim> prims(offset[parts]);
+    {
+        std::vector<std::thread> pool;
+        for (uint32_t t = 0; t < parts; ++t)
+            pool.emplace_back([&, t] {
+                uint32_t b0, b1, o = offset[t];
+                chunk(t, b0, b1);
+                for (uint32_t i = b0; i < b1; ++i) {
+                    if (slotOfTri[i] == kNoSlot) continue;
+                    const dk_triangle& tr = sc->triangles[i];
+                    Prim& q = prims[o++];
+                    const float* v[3] = {&tr.v0.x, &tr.v1.x, &tr.v2.x};
+                    for (int a = 0; a < 3; ++a) {
+                        q.mn[a] = std::fmin(std::fmin(v[0][a], v[1][a]), v[2][a]);
+                        q.mx[a] = std::fmax(std::fmax(v[0][a], v[1][a]), v[2][a]);
+                        q.c[a] = 0.5f * (q.mn[a] + q.mx[a]);
+                    }
+                    q.tri = i;
+                }
+            });
+        for (auto& th : pool) th.join();
     }
     nodes.clear();
     isect.clear();
