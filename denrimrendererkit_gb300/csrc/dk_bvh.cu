@@ -729,7 +729,6 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
         }
     };
     std::vector<std::thread> fill;
-    const uint32_t parts = std::min<uint32_t>(16, std::max(1u, std::thread::hardware_concurrency()));
     for (uint32_t t = 0; t < parts; ++t)
         fill.emplace_back(fillSlots, (uint32_t)((uint64_t)n * t / parts), (uint32_t)((uint64_t)n * (t + 1) / parts));
     struct Join {
