@@ -529,6 +529,67 @@ def run_denoise(args, rank):
     mean = {k: float(np.mean(v)) for k, v in errs.items()}
     # plain sample count with the U-Net's error (noise error falls as 1/sqrt(spp))
     equal_spp = 4.0 * (mean["noisy_4spp"] / mean["unet"]) ** 2
+    # Serving with denoising against plain rendering at the same error: one
+    # held-out 256^2 variant rendered at 4 spp + U-Net, or at the plain
+    # sample count with the U-Net's error (device time per image, warm).
+    from denrimrendererkit_gb300 import compile_scene, scenes
+    wl = scenes.cornell_variant(2000, 256, 256)
+    vb = compile_scene(wl.scene)
+    plain_spp = int(np.ceil(equal_spp))
+    r = DenrimRenderer(0)
+    out = torch.empty_like(held.beauty[0])
+
+    def per_image(fn, reps=20):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    from denrimrendererkit_gb300 import RenderOutput
+    from denrimrendererkit_gb300.denoiser import GraphedDenoiser
+    graphed = GraphedDenoiser(net, 256, 256)
+    kinds = (RenderOutput.BEAUTY, RenderOutput.ALBEDO, RenderOutput.NORMAL, RenderOutput.DEPTH)
+    planes = [torch.empty(256, 256, 4, device="cuda") for _ in kinds]
+    with r.make_session(wl.scene, wl.settings, build=vb) as s4, \
+            r.make_session(wl.scene, wl.settings, build=vb) as sp:
+        # Each image: a fresh render, its AOVs handed to the denoiser on the
+        # device, the denoised image read back to the host.
+        def denoised(use_graph):
+            s4.reset_accumulation()
+            s4.render(4)
+            if use_graph:
+                for k, t in zip(kinds, graphed.inputs):
+                    s4.copy_output(k, t)
+                return graphed.replay().cpu()
+            for k, t in zip(kinds, planes):
+                s4.copy_output(k, t)
+            net.denoise(*planes, 256, 256, out)
+            return out.cpu()
+
+        def plain():
+            sp.reset_accumulation()
+            sp.render(plain_spp)
+            return sp.pixels(RenderOutput.BEAUTY)
+
+        t_denoised = per_image(lambda: denoised(False))
+        t_graphed = per_image(lambda: denoised(True))
+        t_plain = per_image(plain, reps=5)
+        check = float((denoised(True) - denoised(False)).abs().max())
+    used_graph = t_graphed <= t_denoised
+    t_ungraphed = t_denoised
+    t_denoised = min(t_denoised, t_graphed)
+    serving = {"image": "256x256 small-scene variant", "plain_spp_equal_error": plain_spp,
+               "plain_ms_per_image": t_plain * 1e3, "denoised_ms_per_image": t_denoised * 1e3,
+               "images_per_s_plain": 1.0 / t_plain, "images_per_s_denoised": 1.0 / t_denoised,
+               "images_per_s_ratio": t_plain / t_denoised, "graphed_denoiser": bool(used_graph),
+               "ungraphed_ms_per_image": t_ungraphed * 1e3, "graphed_ms_per_image": t_graphed * 1e3,
+               "graphed_vs_direct_max_abs_diff": check,
+               "note": "4 spp + U-Net vs plain rendering at the U-Net's display error; per image: reset, render, "
+                       "AOVs copied device to device into the denoiser, result read back to the host; "
+                       "sessions warm"}
     # 1080p inference timing
     B = net.buffers(1, 1088, 1920)
     for _ in range(3):
@@ -554,6 +615,7 @@ def run_denoise(args, rank):
                          "peak_source": kind, "traffic": None, "gflop_per_inference": flops / 1e9},
             "train_step_ms": train_s / steps * 1e3, "render_pairs_s": render_s,
             "display_relative_rmse_held_out": mean, "plain_spp_with_unet_error": equal_spp,
+            "serving_with_denoising": serving,
             "losses": losses}
     print(json.dumps(line), flush=True)
 

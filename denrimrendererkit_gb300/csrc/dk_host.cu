@@ -167,8 +167,21 @@ struct Session {
     dk::DevJob* jobs = nullptr;  // device copy of the wave's job table (one job)
     dk::Arena arena;
     float4* staging = nullptr;
+    // One-wave renders replayed as CUDA graphs: the wave's kernel sequence for
+    // a (tile, samples) key, captured on its first use.
+    struct WaveGraph {
+        uint32_t tx, ty, tw, th, nb, bounces;
+        int aovs;
+        cudaGraphExec_t exec;
+        size_t events;
+        std::vector<int> kinds;
+        uint64_t launches;
+    };
+    std::vector<WaveGraph> graphs;
+    bool graphsFailed = false;
     uint32_t* rgba8 = nullptr;     // display bytes (allocated on first use)
     uint32_t* encodeWs = nullptr;  // display-encoding workspace
+    cudaEvent_t copyDone = nullptr;  // orders dk_session_copy_output before the caller's stream
     cudaStream_t stream = nullptr;
     std::vector<cudaEvent_t> evPool;
     uint32_t sampleCount = 0;
@@ -180,8 +193,10 @@ struct Session {
 void freeSession(Session* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
     s->arena.release();
     for (auto& e : s->evPool) cudaEventDestroy(e);
+    if (s->copyDone) cudaEventDestroy(s->copyDone);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -765,16 +780,80 @@ static int renderSamples(Session* s, uint32_t tx, uint32_t ty, uint32_t tw, uint
     // interval between mark i and mark i+1 belongs to kind[i].
     std::vector<int> kinds;
     size_t ev = 0;
+    bool capturing = false;
     auto mark = [&](int kind) -> int {
         cudaEvent_t e;
         int rc = eventAt(s, ev++, &e);
         if (rc != DK_OK) return rc;
-        DK_CUDA(cudaEventRecord(e, q), "cudaEventRecord");
+        // Under stream capture the record must be external to become a node
+        // of the graph (recorded on every replay); the flag is refused on an
+        // ordinary record.
+        DK_CUDA(capturing ? cudaEventRecordWithFlags(e, q, cudaEventRecordExternal) : cudaEventRecord(e, q),
+                "cudaEventRecord");
         kinds.push_back(kind);
         return DK_OK;
     };
     uint64_t launches = 0;
     uint32_t done = 0;
+    // A render of one wave runs as a CUDA graph (DK_RENDER_GRAPHS=0: plain
+    // launches): the job table is uploaded on the stream as usual, then the
+    // captured kernel sequence of the wave is replayed.
+    static const bool useGraphs = [] {
+        const char* e = getenv("DK_RENDER_GRAPHS");
+        return !(e && e[0] == '0');
+    }();
+    if (useGraphs && samples <= perBatch) {
+        const uint32_t nb = samples;
+        job.P.sample_begin = sampleBegin;
+        job.P.samples_in_batch = nb;
+        job.P.path_count = nb * tileN;
+        DK_CUDA(cudaMemcpyAsync(s->jobs, &job, sizeof(job), cudaMemcpyHostToDevice, q), "job table upload");
+        Session::WaveGraph* g = nullptr;
+        for (auto& c : s->graphs)
+            if (c.tx == tx && c.ty == ty && c.tw == tw && c.th == th && c.nb == nb &&
+                c.bounces == job.P.max_bounces && c.aovs == (st.denoiser_enabled != 0))
+                g = &c;
+        if (!g && !s->graphsFailed) {
+            // Events the capture records into (created beforehand: no
+            // allocation while capturing).
+            cudaEvent_t e;
+            int rc = eventAt(s, 4 * (size_t)job.P.max_bounces + 8, &e);
+            if (rc != DK_OK) return rc;
+            dk::Wave W = s->wave;
+            W.job_count = 1;
+            W.path_count = job.P.path_count;
+            W.pixel_count = tileN;
+            uint64_t n = 0;
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            bool ok = cudaStreamBeginCapture(q, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                capturing = true;
+                rc = dk::launchWave(s->scene, W, job.P.max_bounces, st.denoiser_enabled != 0, s->grids, q, mark, n);
+                capturing = false;
+                ok = cudaStreamEndCapture(q, &graph) == cudaSuccess && rc == DK_OK && graph &&
+                     cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+            }
+            if (graph) cudaGraphDestroy(graph);
+            if (ok) {
+                s->graphs.push_back({tx, ty, tw, th, nb, job.P.max_bounces, st.denoiser_enabled != 0, exec, ev,
+                                     kinds, n});
+                g = &s->graphs.back();
+            } else {  // capture refused: plain launches for this session
+                cudaGetLastError();
+                s->graphsFailed = true;
+                ev = 0;
+                kinds.clear();
+            }
+        }
+        if (g) {
+            DK_CUDA(cudaGraphLaunch(g->exec, q), "graph launch");
+            ev = g->events;
+            kinds = g->kinds;
+            launches = g->launches;
+            done = samples;
+        }
+    }
     while (done < samples) {
         uint32_t nb = std::min(perBatch, samples - done);
         job.P.sample_begin = sampleBegin + done;
@@ -861,25 +940,6 @@ int dk_session_reset(dk_session* session) {
     return DK_OK;
 }
 
-int dk_session_read_output(dk_session* session, int output, float* rgba, size_t pixelCount) {
-    Session* s = reinterpret_cast<Session*>(session);
-    if (!s || !rgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
-    size_t pixels = (size_t)s->settings.width * s->settings.height;
-    if (pixelCount != pixels) return fail(DK_ERROR_INVALID_ARGUMENT, "pixel_count must equal width*height");
-    if (output < DK_OUTPUT_BEAUTY || output > DK_OUTPUT_MOTION_VECTOR)
-        return fail(DK_ERROR_INVALID_ARGUMENT, "unknown output kind");
-    const float4* src;
-    if (output == DK_OUTPUT_BEAUTY) {
-        DK_CUDA(dk::launchResolveBeauty(s->accum, (uint32_t)pixels, s->staging, s->grids.final, s->stream), "resolve launch");
-        src = s->staging;
-    } else {
-        src = s->accum.aov + (size_t)(output - 1) * pixels;
-    }
-    DK_CUDA(cudaMemcpyAsync(rgba, src, pixels * sizeof(float4), cudaMemcpyDeviceToHost, s->stream), "readback");
-    DK_CUDA(cudaStreamSynchronize(s->stream), "readback");
-    return DK_OK;
-}
-
 // The output plane `output` of the session on the device (the resolved
 // beauty in the staging buffer, or an AOV plane).
 static int outputPlane(Session* s, int output, const float4** src) {
@@ -892,6 +952,43 @@ static int outputPlane(Session* s, int output, const float4** src) {
     } else {
         *src = s->accum.aov + (size_t)(output - 1) * pixels;
     }
+    return DK_OK;
+}
+
+int dk_session_read_output(dk_session* session, int output, float* rgba, size_t pixelCount) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s || !rgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    size_t pixels = (size_t)s->settings.width * s->settings.height;
+    if (pixelCount != pixels) return fail(DK_ERROR_INVALID_ARGUMENT, "pixel_count must equal width*height");
+    if (output < DK_OUTPUT_BEAUTY || output > DK_OUTPUT_MOTION_VECTOR)
+        return fail(DK_ERROR_INVALID_ARGUMENT, "unknown output kind");
+    const float4* src = nullptr;
+    int rc = outputPlane(s, output, &src);
+    if (rc != DK_OK) return rc;
+    DK_CUDA(cudaMemcpyAsync(rgba, src, pixels * sizeof(float4), cudaMemcpyDeviceToHost, s->stream), "readback");
+    DK_CUDA(cudaStreamSynchronize(s->stream), "readback");
+    return DK_OK;
+}
+
+int dk_session_copy_output(dk_session* session, int output, void* deviceRgba, size_t pixelCount, void* stream) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s || !deviceRgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    const size_t pixels = (size_t)s->settings.width * s->settings.height;
+    if (pixelCount != pixels) return fail(DK_ERROR_INVALID_ARGUMENT, "pixel_count must equal width*height");
+    if (reinterpret_cast<uintptr_t>(deviceRgba) % 16u)
+        return fail(DK_ERROR_INVALID_ARGUMENT, "device_rgba must be 16-byte aligned");
+    const float4* src = nullptr;
+    int rc = outputPlane(s, output, &src);
+    if (rc != DK_OK) return rc;
+    DK_CUDA(cudaMemcpyAsync(deviceRgba, src, pixels * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream),
+            "output copy");
+    if (!stream) {
+        DK_CUDA(cudaStreamSynchronize(s->stream), "output copy");
+        return DK_OK;
+    }
+    if (!s->copyDone) DK_CUDA(cudaEventCreateWithFlags(&s->copyDone, cudaEventDisableTiming), "cudaEventCreate");
+    DK_CUDA(cudaEventRecord(s->copyDone, s->stream), "cudaEventRecord");
+    DK_CUDA(cudaStreamWaitEvent(static_cast<cudaStream_t>(stream), s->copyDone, 0), "cudaStreamWaitEvent");
     return DK_OK;
 }
 

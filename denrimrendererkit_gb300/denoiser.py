@@ -335,6 +335,51 @@ class UNet:
                                                    _ptr(out), self._st))
 
 
+class GraphedDenoiser:
+    """`UNet.denoise` of one image size as a CUDA graph: the pack, every
+    convolution / pooling / upsampling launch and the unpack are captured once
+    on a private stream and replayed per image, so a small image pays one graph
+    launch instead of ~60 kernel launches and their host calls.  Inputs are
+    copied into static device tensors before the replay; the weights are read
+    at replay time, so training between replays needs no new capture."""
+
+    def __init__(self, net: "UNet", width: int, height: int):
+        torch = _torch()
+        self.net, self.w, self.h = net, width, height
+        shape = (height, width, 4)
+        self.inputs = [torch.zeros(shape, dtype=torch.float32, device=net.device) for _ in range(4)]
+        self.out = torch.zeros(shape, dtype=torch.float32, device=net.device)
+        self.stream = torch.cuda.Stream()
+        # Pool streams do not order against the default stream: the warm-up
+        # reuses the network's activation buffers, so it waits for work
+        # already queued on the caller's stream.
+        self.stream.wait_stream(torch.cuda.current_stream())
+        saved = net.stream
+        try:
+            net.stream = self.stream.cuda_stream
+            with torch.cuda.stream(self.stream):  # warm-up: buffers, tensor-map encoders, lazy loading
+                net.denoise(*self.inputs, width, height, self.out)
+            self.stream.synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=self.stream):
+                net.denoise(*self.inputs, width, height, self.out)
+        finally:
+            net.stream = saved
+
+    def denoise(self, beauty, albedo, normal, depth, out) -> None:
+        for dst, src in zip(self.inputs, (beauty, albedo, normal, depth)):
+            dst.copy_(src)
+        self.graph.replay()
+        out.copy_(self.out)
+
+    def replay(self):
+        """Denoises what is already in `inputs` (beauty, albedo, normal,
+        depth -- e.g. filled by `RenderSession.copy_output`) into `out`, on
+        torch's current stream; returns `out`."""
+        self.graph.replay()
+        return self.out
+
+
 def spatial_denoise(beauty, depth, normal, albedo, out, width: int, height: int, radius: int = 2,
                     normal_sigma: float = 0.18, depth_sigma: float = 0.03, albedo_sigma: float = 0.25,
                     color_sigma: float = 1.0, iterations: int = 3, stream=None) -> None:

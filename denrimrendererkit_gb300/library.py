@@ -60,6 +60,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_session_reset": (i32, [P]),
             "dk_session_read_output": (i32, [P, i32, P, sz]),
             "dk_session_read_rgba8": (i32, [P, i32, P, sz]),
+            "dk_session_copy_output": (i32, [P, i32, P, sz, P]),
             "dk_session_write_png": (i32, [P, i32, C.c_char_p]),
             "dk_encode_rgba8": (i32, [P, u32, u32, i32, P, P, P]),
             "dk_write_png": (i32, [C.c_char_p, P, u32, u32]),

@@ -162,6 +162,21 @@ class RenderSession:
         library.check(self._lib.dk_session_read_output(self._handle, int(output), out.ctypes.data, w * h))
         return out
 
+    # RenderSession.texture(for:) (RenderSession.swift:1072-1094): the output
+    # copied device to device into `out`, a float32 CUDA tensor of H*W*4
+    # elements; ordered before later work on `stream` (default: torch's
+    # current stream), with no host round trip.
+    def copy_output(self, output: RenderOutput, out, stream=None):
+        import torch
+        w, h = self.settings.width, self.settings.height
+        if not (out.is_cuda and out.dtype == torch.float32 and out.is_contiguous() and out.numel() == w * h * 4):
+            raise ValueError("copy_output needs a contiguous float32 CUDA tensor of width*height*4 elements")
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        library.check(self._lib.dk_session_copy_output(self._handle, int(output), C.c_void_p(out.data_ptr()), w * h,
+                                                       C.c_void_p(stream.cuda_stream)))
+        return out
+
     def close(self) -> None:
         if self._handle:
             self._lib.dk_session_destroy(self._handle)

@@ -286,6 +286,14 @@ int dk_session_reset(dk_session* session);
  * output as RGBA32F into `rgba` (pixel_count = width*height pixels). */
 int dk_session_read_output(dk_session* session, int output, float* rgba, size_t pixel_count);
 
+/* RenderSession.texture(for:) (RenderSession.swift:1072-1094), the
+ * device-resident output the reference hands to its viewport and denoiser:
+ * copies the output as RGBA32F into caller-owned DEVICE memory `device_rgba`
+ * (pixel_count = width*height pixels, 16-byte aligned), with no host
+ * round trip.  The copy is ordered before work queued afterwards on `stream`
+ * (a cudaStream_t; NULL: the call returns when the copy is complete). */
+int dk_session_copy_output(dk_session* session, int output, void* device_rgba, size_t pixel_count, void* stream);
+
 /* PNGWriter.visualizedRGBA8Pixels (Image/PNGWriter.swift:35-53) on the device:
  * the output as the reference's PNG export shows it (beauty tonemapped, depth
  * normalised to its range, IDs hashed to colours, ...), 8-bit RGBA, row major,

@@ -169,3 +169,20 @@ def test_network_gradients_match_fp32_reference(lib):
         eb = rel_rms(l.gb.cpu(), br.grad)
         assert ew <= 6e-2, (l.name, ew)
         assert eb <= 6e-2, (l.name, eb)
+
+
+def test_graphed_denoiser_equals_direct_calls(lib):
+    # The CUDA-graph replay runs the same kernels on the same buffers.
+    from denrimrendererkit_gb300.denoiser import GraphedDenoiser
+    net = UNet(seed=5)
+    g = torch.Generator().manual_seed(2)
+    w, h = 72, 40  # padded to 80 x 48 inside
+    planes = [torch.rand(h, w, 4, generator=g).cuda() for _ in range(4)]
+    direct = torch.empty(h, w, 4, device="cuda")
+    net.denoise(*planes, w, h, direct)
+    graphed = GraphedDenoiser(net, w, h)
+    out = torch.empty_like(direct)
+    for _ in range(2):
+        graphed.denoise(*planes, out)
+    torch.cuda.synchronize()
+    assert torch.equal(out, direct)
