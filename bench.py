@@ -578,6 +578,7 @@ def run_denoise(args, rank):
         t_graphed = per_image(lambda: denoised(True))
         t_plain = per_image(plain, reps=5)
         check = float((denoised(True) - denoised(False)).abs().max())
+    batched = serve_batches_with_denoising(net, wl, vb, plain_spp)
     used_graph = t_graphed <= t_denoised
     t_ungraphed = t_denoised
     t_denoised = min(t_denoised, t_graphed)
@@ -615,9 +616,71 @@ def run_denoise(args, rank):
                          "peak_source": kind, "traffic": None, "gflop_per_inference": flops / 1e9},
             "train_step_ms": train_s / steps * 1e3, "render_pairs_s": render_s,
             "display_relative_rmse_held_out": mean, "plain_spp_with_unet_error": equal_spp,
-            "serving_with_denoising": serving,
+            "serving_with_denoising": serving, "serving_with_denoising_batched": batched,
             "losses": losses}
     print(json.dumps(line), flush=True)
+
+
+def serve_batches_with_denoising(net, wl, build, plain_spp, batch=8, batches=10):
+    """Requests served in batches through the render server: `batch` views of
+    one scene (cameras on a small orbit) rendered together in one wave at
+    4 spp, handed to the U-Net device to device, denoised as one batch by a
+    CUDA graph and read back; against the same requests rendered at the plain
+    sample count with the U-Net's error and read back."""
+    import math
+    import torch
+    from denrimrendererkit_gb300 import RenderOutput
+    from denrimrendererkit_gb300.denoiser import GraphedDenoiser
+    from denrimrendererkit_gb300.scene import Camera
+    from denrimrendererkit_gb300.serving import RenderServer
+    cam, st = wl.scene.camera, wl.settings
+    W, H = st.width, st.height
+    eye = np.subtract(cam.origin, cam.target)
+    cams = []
+    for i in range(batch):
+        a = math.radians(-6.0 + 12.0 * i / max(batch - 1, 1))
+        c, s = math.cos(a), math.sin(a)
+        e = (eye[0] * c + eye[2] * s, eye[1], -eye[0] * s + eye[2] * c)
+        cams.append(Camera(tuple(np.add(cam.target, e)), cam.target, up=cam.up,
+                           vertical_field_of_view_degrees=cam.vertical_field_of_view_degrees))
+    kinds = (RenderOutput.BEAUTY, RenderOutput.ALBEDO, RenderOutput.NORMAL, RenderOutput.DEPTH)
+    graphed = GraphedDenoiser(net, W, H, batch=batch)
+    plain_out = torch.empty((batch, H, W, 4), dtype=torch.float32, device="cuda")
+    host = torch.empty((batch, H, W, 4), dtype=torch.float32).pin_memory()
+
+    def run(server, spp, denoise):
+        ids = [server.submit(st, c, spp) for c in cams]
+        while server.step():
+            pass
+        if denoise:
+            for k, t in zip(kinds, graphed.inputs):
+                server.copy_outputs(ids, k, t)
+            host.copy_(graphed.replay())
+        else:
+            server.copy_outputs(ids, RenderOutput.BEAUTY, plain_out)
+            host.copy_(plain_out)
+        for j in ids:
+            server.release(j)
+        return host
+
+    def per_image(server, spp, denoise):
+        run(server, spp, denoise)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(batches):
+            run(server, spp, denoise)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / (batches * batch)
+
+    with RenderServer(build) as server:
+        t_den = per_image(server, 4, True)
+        t_plain = per_image(server, plain_spp, False)
+    return {"requests_per_batch": batch, "image": f"{W}x{H} views of one held-out small-scene variant",
+            "denoised_ms_per_image": t_den * 1e3, "plain_ms_per_image": t_plain * 1e3,
+            "plain_spp_equal_error": plain_spp, "images_per_s_denoised": 1.0 / t_den,
+            "images_per_s_plain": 1.0 / t_plain, "images_per_s_ratio": t_plain / t_den,
+            "note": "render server: the batch's jobs share waves; 4 spp + batched U-Net (CUDA graph) vs plain "
+                    "rendering at the U-Net's display error; outputs copied device to device, results read back"}
 
 
 def main():

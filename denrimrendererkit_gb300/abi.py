@@ -169,7 +169,7 @@ EXPORTED_SYMBOLS = (
     "dk_bake_sparse_sphere_volume",
     "dk_sparse_volume_view", "dk_sparse_volume_destroy", "dk_version",
     "dk_server_create", "dk_server_submit", "dk_server_step", "dk_server_start", "dk_server_stop",
-    "dk_server_wait", "dk_server_job_status", "dk_server_read_output", "dk_server_release",
+    "dk_server_wait", "dk_server_job_status", "dk_server_read_output", "dk_server_copy_output", "dk_server_copy_outputs", "dk_server_release",
     "dk_server_get_stats", "dk_server_destroy", "dk_denoise_spatial",
     "dk_unet_conv3x3", "dk_unet_conv3x3_wgrad", "dk_unet_relu_backward", "dk_unet_bias_grad", "dk_unet_avgpool2",
     "dk_unet_avgpool2_backward", "dk_unet_upsample2", "dk_unet_upsample2_backward", "dk_unet_copy_channels",

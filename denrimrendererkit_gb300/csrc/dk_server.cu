@@ -61,6 +61,7 @@ struct Server {
     cudaEvent_t evBegin = nullptr, evEnd = nullptr;
     float4* staging = nullptr;        // readback staging (ioStream), grown on demand
     size_t stagingPixels = 0;
+    cudaEvent_t copyDone = nullptr;   // orders dk_server_copy_output before the caller's stream
     uint32_t matCount = 0;            // M: entries of the scene's (and every job's) material table
     std::vector<dk_material> baseMaterials;
     std::vector<uint32_t> freeSlots;
@@ -101,6 +102,7 @@ void destroyServer(Server* s) {
     s->arena.release();
     if (s->evBegin) cudaEventDestroy(s->evBegin);
     if (s->evEnd) cudaEventDestroy(s->evEnd);
+    if (s->copyDone) cudaEventDestroy(s->copyDone);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->ioStream) cudaStreamDestroy(s->ioStream);
     delete s;
@@ -471,9 +473,11 @@ int dk_server_job_status(dk_server* server, uint64_t id, dk_job_status* out) {
     return DK_OK;
 }
 
-int dk_server_read_output(dk_server* server, uint64_t id, int output, float* rgba, size_t pixelCount) {
-    Server* s = asServer(server);
-    if (!s || !rgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+namespace {
+
+// A finished job's output plane on the device (the beauty resolved into the
+// staging buffer on the I/O stream, or an AOV plane).  Called with ioMu held.
+int jobPlane(Server* s, uint64_t id, int output, size_t pixelCount, const float4** src) {
     if (output < DK_OUTPUT_BEAUTY || output > DK_OUTPUT_MOTION_VECTOR)
         return fail(DK_ERROR_INVALID_ARGUMENT, "unknown output kind");
     dk::Accum A;
@@ -489,10 +493,8 @@ int dk_server_read_output(dk_server* server, uint64_t id, int output, float* rgb
     }
     if (pixelCount != pixels) return fail(DK_ERROR_INVALID_ARGUMENT, "pixel_count must equal width*height");
     // The job's last wave was synchronized before DONE was set, and no later
-    // wave touches its buffers: the readback needs no ordering with the wave
+    // wave touches its buffers: reading them needs no ordering with the wave
     // stream.
-    std::lock_guard<std::mutex> io(s->ioMu);
-    const float4* src;
     if (output == DK_OUTPUT_BEAUTY) {
         if (s->stagingPixels < pixels) {
             if (s->staging) cudaFree(s->staging);
@@ -502,12 +504,57 @@ int dk_server_read_output(dk_server* server, uint64_t id, int output, float* rgb
             s->stagingPixels = pixels;
         }
         DK_CUDA(dk::launchResolveBeauty(A, (uint32_t)pixels, s->staging, s->grids.final, s->ioStream), "resolve launch");
-        src = s->staging;
+        *src = s->staging;
     } else {
-        src = A.aov + (size_t)(output - 1) * pixels;
+        *src = A.aov + (size_t)(output - 1) * pixels;
     }
-    DK_CUDA(cudaMemcpyAsync(rgba, src, pixels * sizeof(float4), cudaMemcpyDeviceToHost, s->ioStream), "readback");
+    return DK_OK;
+}
+
+}  // namespace
+
+int dk_server_read_output(dk_server* server, uint64_t id, int output, float* rgba, size_t pixelCount) {
+    Server* s = asServer(server);
+    if (!s || !rgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> io(s->ioMu);
+    const float4* src = nullptr;
+    int rc = jobPlane(s, id, output, pixelCount, &src);
+    if (rc != DK_OK) return rc;
+    DK_CUDA(cudaMemcpyAsync(rgba, src, pixelCount * sizeof(float4), cudaMemcpyDeviceToHost, s->ioStream), "readback");
     DK_CUDA(cudaStreamSynchronize(s->ioStream), "readback");
+    return DK_OK;
+}
+
+int dk_server_copy_output(dk_server* server, uint64_t id, int output, void* deviceRgba, size_t pixelCount,
+                          void* stream) {
+    return dk_server_copy_outputs(server, &id, 1, output, deviceRgba, pixelCount, 0, stream);
+}
+
+int dk_server_copy_outputs(dk_server* server, const uint64_t* ids, size_t count, int output, void* deviceRgba,
+                           size_t pixelCount, size_t strideBytes, void* stream) {
+    Server* s = asServer(server);
+    if (!s || !ids || !deviceRgba) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    if (strideBytes == 0) strideBytes = pixelCount * sizeof(float4);
+    if (reinterpret_cast<uintptr_t>(deviceRgba) % 16u || strideBytes % 16u)
+        return fail(DK_ERROR_INVALID_ARGUMENT, "device_rgba and the stride must be 16-byte aligned");
+    if (count > 1 && strideBytes < pixelCount * sizeof(float4))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "the stride is smaller than one image");
+    std::lock_guard<std::mutex> io(s->ioMu);
+    for (size_t i = 0; i < count; ++i) {
+        const float4* src = nullptr;
+        int rc = jobPlane(s, ids[i], output, pixelCount, &src);
+        if (rc != DK_OK) return rc;
+        DK_CUDA(cudaMemcpyAsync(static_cast<char*>(deviceRgba) + i * strideBytes, src, pixelCount * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, s->ioStream),
+                "output copy");
+    }
+    if (!stream) {
+        DK_CUDA(cudaStreamSynchronize(s->ioStream), "output copy");
+        return DK_OK;
+    }
+    if (!s->copyDone) DK_CUDA(cudaEventCreateWithFlags(&s->copyDone, cudaEventDisableTiming), "cudaEventCreate");
+    DK_CUDA(cudaEventRecord(s->copyDone, s->ioStream), "cudaEventRecord");
+    DK_CUDA(cudaStreamWaitEvent(static_cast<cudaStream_t>(stream), s->copyDone, 0), "cudaStreamWaitEvent");
     return DK_OK;
 }
 

@@ -334,6 +334,20 @@ class UNet:
         self._check(self.lib.dk_unet_unpack_output(_ptr(B["pred"]), OUT_CH, h, w, _ptr(beauty), img_w, img_h, 0, 0,
                                                    _ptr(out), self._st))
 
+    def denoise_batch(self, beauty, albedo, normal, depth, img_w: int, img_h: int, out) -> None:
+        """Denoises n images of one size as one batch: every argument is a
+        device tensor (n, img_h, img_w, 4) float32.  One pass of the network
+        over the batch; each image equals its own `denoise` call."""
+        n = beauty.shape[0]
+        h = (img_h + 15) // 16 * 16
+        w = (img_w + 15) // 16 * 16
+        for i in range(n):
+            self.pack(beauty[i], albedo[i], normal[i], depth[i], img_w, img_h, 0, 0, n, h, w, i)
+        B = self.forward(n, h, w)
+        for i in range(n):
+            self._check(self.lib.dk_unet_unpack_output(_ptr(B["pred"][i]), OUT_CH, h, w, _ptr(beauty[i]), img_w,
+                                                       img_h, 0, 0, _ptr(out[i]), self._st))
+
 
 class GraphedDenoiser:
     """`UNet.denoise` of one image size as a CUDA graph: the pack, every
@@ -343,10 +357,13 @@ class GraphedDenoiser:
     copied into static device tensors before the replay; the weights are read
     at replay time, so training between replays needs no new capture."""
 
-    def __init__(self, net: "UNet", width: int, height: int):
+    def __init__(self, net: "UNet", width: int, height: int, batch: int = 0):
+        """batch 0: one image, tensors (height, width, 4); batch n >= 1: n
+        images per replay (`UNet.denoise_batch`), tensors (n, height, width, 4)."""
         torch = _torch()
-        self.net, self.w, self.h = net, width, height
-        shape = (height, width, 4)
+        self.net, self.w, self.h, self.batch = net, width, height, batch
+        shape = (batch, height, width, 4) if batch else (height, width, 4)
+        run = net.denoise_batch if batch else net.denoise
         self.inputs = [torch.zeros(shape, dtype=torch.float32, device=net.device) for _ in range(4)]
         self.out = torch.zeros(shape, dtype=torch.float32, device=net.device)
         self.stream = torch.cuda.Stream()
@@ -358,11 +375,11 @@ class GraphedDenoiser:
         try:
             net.stream = self.stream.cuda_stream
             with torch.cuda.stream(self.stream):  # warm-up: buffers, tensor-map encoders, lazy loading
-                net.denoise(*self.inputs, width, height, self.out)
+                run(*self.inputs, width, height, self.out)
             self.stream.synchronize()
             self.graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self.graph, stream=self.stream):
-                net.denoise(*self.inputs, width, height, self.out)
+                run(*self.inputs, width, height, self.out)
         finally:
             net.stream = saved
 

@@ -86,6 +86,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_server_wait": (i32, [P, C.c_uint64, u32]),
             "dk_server_job_status": (i32, [P, C.c_uint64, C.POINTER(abi.JobStatus)]),
             "dk_server_read_output": (i32, [P, C.c_uint64, i32, P, sz]),
+            "dk_server_copy_output": (i32, [P, C.c_uint64, i32, P, sz, P]),
+            "dk_server_copy_outputs": (i32, [P, P, sz, i32, P, sz, sz, P]),
             "dk_server_release": (i32, [P, C.c_uint64]),
             "dk_server_get_stats": (i32, [P, C.POINTER(abi.ServerStats)]),
             "dk_server_destroy": (i32, [P]),

@@ -81,8 +81,8 @@ def make_settings_struct(settings: RenderSettings, camera: Camera) -> abi.Settin
     s.denoiser_enabled = int(settings.denoise)
     s.collects_traversal_stats = int(settings.collects_traversal_stats)
     s.camera = camera.gpu_camera(settings.width, settings.height)
-    prev = settings.previous_camera or camera
-    s.previous_camera = prev.gpu_camera(settings.width, settings.height)
+    prev = settings.previous_camera
+    s.previous_camera = s.camera if prev is None or prev is camera else prev.gpu_camera(settings.width, settings.height)
     s.max_samples_per_launch = settings.max_samples_per_launch
     return s
 

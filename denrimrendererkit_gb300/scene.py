@@ -36,6 +36,19 @@ def _normalize_rows(v: np.ndarray) -> np.ndarray:
     return (v * inv[..., None]).astype(f32)
 
 
+def _dot3(a, b):
+    return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]
+
+
+def _normalize3(v):
+    inv = f32(1.0) / np.sqrt(_dot3(v, v))
+    return (v[0] * inv, v[1] * inv, v[2] * inv)
+
+
+def _cross3(a, b):
+    return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+
 # --------------------------------------------------------------- transform ---
 @dataclasses.dataclass
 class Transform:
@@ -315,15 +328,21 @@ class Camera:
     aperture_radius: float = 0.0
 
     def gpu_camera(self, width: int, height: int) -> abi.Camera:
-        """Camera.gpuCamera (Camera.swift:167-200) with cameraBasis (:202-218)."""
-        o = np.asarray(self.origin, f32)
-        vd = np.asarray(self.target, f32) - o
-        forward = _normalize_rows(vd[None])[0] if float((vd * vd).sum()) > 1e-8 else np.array([0, 0, -1], f32)
-        up = np.asarray(self.up, f32)
-        up = _normalize_rows(up[None])[0] if float((up * up).sum()) > 1e-8 else np.array([0, 1, 0], f32)
-        helper = up if abs(float(np.dot(forward, up))) < 0.999 else np.array([1, 0, 0], f32)
-        right = _normalize_rows(np.cross(forward, helper)[None])[0]
-        true_up = np.cross(right, forward).astype(f32)
+        """Camera.gpuCamera (Camera.swift:167-200) with cameraBasis (:202-218).
+
+        Scalar float32 arithmetic, each operation rounded to float32 in the
+        order of the reference's simd code (dot and length as ((x + y) + z),
+        cross products as a*b - c*d without fusion); a request-rate path of
+        the render server, so no per-call array allocation."""
+        o = tuple(f32(c) for c in self.origin)
+        t = tuple(f32(c) for c in self.target)
+        vd = (t[0] - o[0], t[1] - o[1], t[2] - o[2])
+        forward = _normalize3(vd) if float(_dot3(vd, vd)) > 1e-8 else (f32(0), f32(0), f32(-1))
+        u = tuple(f32(c) for c in self.up)
+        up = _normalize3(u) if float(_dot3(u, u)) > 1e-8 else (f32(0), f32(1), f32(0))
+        helper = up if abs(float(_dot3(forward, up))) < 0.999 else (f32(1), f32(0), f32(0))
+        right = _normalize3(_cross3(forward, helper))
+        true_up = _cross3(right, forward)
         aspect = f32(width) / f32(height)
         if self.orthographic_scale is None:
             theta = f32(self.vertical_field_of_view_degrees) * f32(math.pi) / f32(180)
@@ -333,15 +352,16 @@ class Camera:
             vh = f32(max(self.orthographic_scale, 0.0001))
             flag = 1.0
         vw = f32(aspect * vh)
-        horizontal = (vw * right).astype(f32)
-        vertical = (vh * true_up).astype(f32)
-        plane_center = (o + forward) if self.orthographic_scale is None else o
-        lower_left = (plane_center - horizontal * f32(0.5) - vertical * f32(0.5)).astype(f32)
+        horizontal = tuple(vw * c for c in right)
+        vertical = tuple(vh * c for c in true_up)
+        pc = tuple(o[i] + forward[i] for i in range(3)) if self.orthographic_scale is None else o
+        half = f32(0.5)
+        lower_left = tuple((pc[i] - horizontal[i] * half) - vertical[i] * half for i in range(3))
         cam = abi.Camera()
-        cam.origin = abi.Float4(*o.tolist(), flag)
-        cam.lower_left = abi.Float4(*lower_left.tolist(), 0.0)
-        cam.horizontal = abi.Float4(*horizontal.tolist(), 0.0)
-        cam.vertical = abi.Float4(*vertical.tolist(), 0.0)
+        cam.origin = abi.Float4(float(o[0]), float(o[1]), float(o[2]), flag)
+        cam.lower_left = abi.Float4(*(float(c) for c in lower_left), 0.0)
+        cam.horizontal = abi.Float4(*(float(c) for c in horizontal), 0.0)
+        cam.vertical = abi.Float4(*(float(c) for c in vertical), 0.0)
         cam.lens = abi.Float4(max(self.aperture_radius, 0.0), max(self.focus_distance, 0.0001), 0.0, 0.0)
         return cam
 

@@ -117,6 +117,41 @@ class RenderServer:
         library.check(self._lib.dk_server_read_output(self._handle, job_id, int(output), out.ctypes.data, w * h))
         return out
 
+    def copy_output(self, job_id: int, output: RenderOutput, out, stream=None):
+        """A finished job's output copied device to device into `out` (a
+        contiguous float32 CUDA tensor of H*W*4 elements), ordered before later
+        work on `stream` (default: torch's current stream)."""
+        import torch
+        w, h = self._jobs[job_id]
+        if not (out.is_cuda and out.dtype == torch.float32 and out.is_contiguous() and out.numel() == w * h * 4):
+            raise ValueError("copy_output needs a contiguous float32 CUDA tensor of width*height*4 elements")
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        library.check(self._lib.dk_server_copy_output(self._handle, job_id, int(output), C.c_void_p(out.data_ptr()),
+                                                      w * h, C.c_void_p(stream.cuda_stream)))
+        return out
+
+    def copy_outputs(self, job_ids: Sequence[int], output: RenderOutput, out, stream=None):
+        """The outputs of finished jobs of one size copied device to device
+        into `out[i]` (a contiguous float32 CUDA tensor (n, H, W, 4)) in one
+        call, ordered before later work on `stream`."""
+        import torch
+        ids = list(job_ids)
+        if not ids:
+            return out
+        w, h = self._jobs[ids[0]]
+        if any(self._jobs[j] != (w, h) for j in ids):
+            raise ValueError("copy_outputs needs jobs of one size")
+        if not (out.is_cuda and out.dtype == torch.float32 and out.is_contiguous() and out.numel() == len(ids) * w * h * 4):
+            raise ValueError("copy_outputs needs a contiguous float32 CUDA tensor of n*width*height*4 elements")
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        arr = (C.c_uint64 * len(ids))(*ids)
+        library.check(self._lib.dk_server_copy_outputs(self._handle, arr, len(ids), int(output),
+                                                       C.c_void_p(out.data_ptr()), w * h, w * h * 16,
+                                                       C.c_void_p(stream.cuda_stream)))
+        return out
+
     def release(self, job_id: int) -> None:
         library.check(self._lib.dk_server_release(self._handle, job_id))
 

@@ -583,6 +583,15 @@ int dk_server_wait(dk_server* server, uint64_t job_id, uint32_t timeout_ms);
 int dk_server_job_status(dk_server* server, uint64_t job_id, dk_job_status* out_status);
 /* Reads a finished job's output (as dk_session_read_output). */
 int dk_server_read_output(dk_server* server, uint64_t job_id, int output, float* rgba, size_t pixel_count);
+/* Copies a finished job's output into caller-owned device memory (as
+ * dk_session_copy_output): the hand-off of a batch of served images to a
+ * denoiser without a host round trip. */
+int dk_server_copy_output(dk_server* server, uint64_t job_id, int output, void* device_rgba, size_t pixel_count,
+                          void* stream);
+/* The same for `count` finished jobs of one size in one call: job i's output
+ * goes to device_rgba + i * stride_bytes (0: pixel_count * 16, packed). */
+int dk_server_copy_outputs(dk_server* server, const uint64_t* job_ids, size_t count, int output, void* device_rgba,
+                           size_t pixel_count, size_t stride_bytes, void* stream);
 /* Frees a finished job's buffers (its budget returns to admission). */
 int dk_server_release(dk_server* server, uint64_t job_id);
 int dk_server_get_stats(dk_server* server, dk_server_stats* out_stats);

@@ -94,3 +94,31 @@ def test_copy_output_equals_host_readback(dk_lib):
             assert np.array_equal(got.cpu().numpy().view(np.uint32), host.view(np.uint32)), k.name
         with pytest.raises(ValueError):
             s.copy_output(RenderOutput.BEAUTY, torch.empty(10, device="cuda"))
+
+
+def test_server_copy_output_equals_host_readback(dk_lib):
+    import torch
+    from denrimrendererkit_gb300 import RenderOutput, compile_scene, scenes
+    from denrimrendererkit_gb300.serving import RenderServer
+    wl = scenes.material_reference(32, 16)
+    with RenderServer(compile_scene(wl.scene)) as server:
+        ids = [server.submit(wl.settings, wl.scene.camera, spp) for spp in (2, 5)]
+        while server.step():
+            pass
+        for j in ids:
+            for k in RenderOutput:
+                host = server.pixels(j, k)
+                dev = torch.full((16, 32, 4), -1.0, device="cuda")
+                server.copy_output(j, k, dev)
+                assert np.array_equal(dev.cpu().numpy().view(np.uint32), host.view(np.uint32)), k.name
+        more = [server.submit(wl.settings, wl.scene.camera, spp) for spp in (1, 3, 4)]
+        while server.step():
+            pass
+        for k in RenderOutput:
+            batch = torch.full((3, 16, 32, 4), -1.0, device="cuda")
+            server.copy_outputs(more, k, batch)
+            for i, j in enumerate(more):
+                host = server.pixels(j, k)
+                assert np.array_equal(batch[i].cpu().numpy().view(np.uint32), host.view(np.uint32)), k.name
+        for j in ids + more:
+            server.release(j)

@@ -171,6 +171,28 @@ def test_network_gradients_match_fp32_reference(lib):
         assert eb <= 6e-2, (l.name, eb)
 
 
+def test_batched_denoise_equals_single_images(lib):
+    # A batch of images through one pass of the network (and its CUDA graph)
+    # gives each image's own result bit for bit.
+    from denrimrendererkit_gb300.denoiser import GraphedDenoiser
+    net = UNet(seed=6)
+    g = torch.Generator().manual_seed(3)
+    n, w, h = 3, 40, 24
+    planes = [torch.rand(n, h, w, 4, generator=g).cuda() for _ in range(4)]
+    single = torch.empty(n, h, w, 4, device="cuda")
+    for i in range(n):
+        net.denoise(*(p[i] for p in planes), w, h, single[i])
+    batched = torch.empty_like(single)
+    net.denoise_batch(*planes, w, h, batched)
+    graphed = GraphedDenoiser(net, w, h, batch=n)
+    for dst, src in zip(graphed.inputs, planes):
+        dst.copy_(src)
+    replayed = graphed.replay().clone()
+    torch.cuda.synchronize()
+    assert torch.equal(batched, single)
+    assert torch.equal(replayed, single)
+
+
 def test_graphed_denoiser_equals_direct_calls(lib):
     # The CUDA-graph replay runs the same kernels on the same buffers.
     from denrimrendererkit_gb300.denoiser import GraphedDenoiser
