@@ -578,7 +578,7 @@ def run_denoise(args, rank):
         t_graphed = per_image(lambda: denoised(True))
         t_plain = per_image(plain, reps=5)
         check = float((denoised(True) - denoised(False)).abs().max())
-    batched = serve_batches_with_denoising(net, wl, vb, plain_spp)
+    batched = {f"batch_{n}": serve_batches_with_denoising(net, wl, vb, plain_spp, batch=n) for n in (8, 16)}
     used_graph = t_graphed <= t_denoised
     t_ungraphed = t_denoised
     t_denoised = min(t_denoised, t_graphed)
@@ -591,6 +591,7 @@ def run_denoise(args, rank):
                "note": "4 spp + U-Net vs plain rendering at the U-Net's display error; per image: reset, render, "
                        "AOVs copied device to device into the denoiser, result read back to the host; "
                        "sessions warm"}
+    svgf = svgf_timing()
     # 1080p inference timing
     B = net.buffers(1, 1088, 1920)
     for _ in range(3):
@@ -616,9 +617,39 @@ def run_denoise(args, rank):
                          "peak_source": kind, "traffic": None, "gflop_per_inference": flops / 1e9},
             "train_step_ms": train_s / steps * 1e3, "render_pairs_s": render_s,
             "display_relative_rmse_held_out": mean, "plain_spp_with_unet_error": equal_spp,
-            "serving_with_denoising": serving, "serving_with_denoising_batched": batched,
+            "serving_with_denoising": serving, "serving_with_denoising_batched": batched, "svgf": svgf,
             "losses": losses}
     print(json.dumps(line), flush=True)
+
+
+def svgf_timing(width=1920, height=1080, frames=10):
+    """Device time per frame of the SVGF denoiser (DenoiseSettings.appleSVGF:
+    5 a-trous passes, radius 2) at 1920x1080 on synthetic AOV planes with a
+    full temporal history."""
+    import torch
+    from denrimrendererkit_gb300.denoiser import SvgfDenoiser
+    g = torch.Generator(device="cuda").manual_seed(5)
+    shape = (height, width, 4)
+    beauty = torch.rand(shape, generator=g, device="cuda")
+    depth = torch.rand(shape, generator=g, device="cuda") * 4 + 1
+    normal = torch.rand(shape, generator=g, device="cuda") * 0.2 + 0.4
+    normal[..., 2] = 0.9
+    normal[..., 3] = 1.0
+    motion = torch.zeros(shape, device="cuda")
+    motion[..., 3] = 1.0
+    out = torch.empty(shape, device="cuda")
+    s = SvgfDenoiser(width, height)
+    for _ in range(5):
+        s.denoise(beauty, depth, normal, motion, out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(frames):
+        s.denoise(beauty, depth, normal, motion, out)
+    e1.record()
+    torch.cuda.synchronize()
+    s.close()
+    return {"ms_per_frame_1080p": e0.elapsed_time(e1) / frames, "launches_per_frame": 9,
+            "note": "pack, temporal, variance, 5 a-trous passes, output copy; synthetic planes, history full"}
 
 
 def serve_batches_with_denoising(net, wl, build, plain_spp, batch=8, batches=10):

@@ -397,6 +397,51 @@ class GraphedDenoiser:
         return self.out
 
 
+class SvgfDenoiser:
+    """DenoiseSettings.appleSVGF (Denoiser.swift:67-76): spatiotemporal
+    variance-guided filtering with a temporal history per image size
+    (AppleSVGFDenoiser, Denoiser.swift:167-300).  `denoise` takes device
+    RGBA32F planes (beauty, depth, encoded normal and motion-vector AOVs) and
+    writes the filtered beauty into `out`; `reset` drops the history
+    (clearTemporalHistory)."""
+
+    def __init__(self, width: int, height: int):
+        self.lib = library.load()
+        self.width, self.height = width, height
+        self._h = C.c_void_p()
+        library.check(self.lib.dk_svgf_create(width, height, C.byref(self._h)))
+
+    def denoise(self, beauty, depth, normal, motion, out, radius: int = 2, normal_sigma: float = 0.18,
+                depth_sigma: float = 0.08, color_sigma: float = 4.0, iterations: int = 5, stream=None) -> None:
+        torch = _torch()
+        s = abi.SpatialDenoiseSettings(radius, normal_sigma, depth_sigma, 0.25, color_sigma, iterations)
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        library.check(self.lib.dk_svgf_denoise(self._h, _ptr(beauty), _ptr(depth), _ptr(normal), _ptr(motion),
+                                               _ptr(out), C.byref(s), C.c_void_p(st)))
+
+    def reset(self) -> None:
+        library.check(self.lib.dk_svgf_reset(self._h))
+
+    def state(self, which: int):
+        """0: history colour, 1: (luminance mean, mean square, history length, 0), 2: packed depth + normal."""
+        torch = _torch()
+        out = torch.empty(self.height, self.width, 4, dtype=torch.float32, device="cuda")
+        library.check(self.lib.dk_svgf_read_state(self._h, which, _ptr(out), self.width * self.height,
+                                                  C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            self.lib.dk_svgf_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def spatial_denoise(beauty, depth, normal, albedo, out, width: int, height: int, radius: int = 2,
                     normal_sigma: float = 0.18, depth_sigma: float = 0.03, albedo_sigma: float = 0.25,
                     color_sigma: float = 1.0, iterations: int = 3, stream=None) -> None:

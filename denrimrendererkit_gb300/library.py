@@ -92,6 +92,13 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_server_get_stats": (i32, [P, C.POINTER(abi.ServerStats)]),
             "dk_server_destroy": (i32, [P]),
             "dk_denoise_spatial": (i32, [P, P, P, P, P, P, u32, u32, C.POINTER(abi.SpatialDenoiseSettings), P]),
+            "dk_svgf_create": (i32, [u32, u32, P]),
+            "dk_svgf_reset": (i32, [P]),
+            "dk_svgf_denoise": (i32, [P, P, P, P, P, P, C.POINTER(abi.SpatialDenoiseSettings), P]),
+            "dk_svgf_read_state": (i32, [P, i32, P, sz, P]),
+            "dk_svgf_destroy": (i32, [P]),
+            "dk_svgf_pack_depth_normal": (i32, [P, P, P, u32, u32, P]),
+            "dk_svgf_copy_output": (i32, [P, P, P, u32, u32, P]),
             "dk_unet_conv3x3": (i32, [P, u32, u32, u32, u32, u32, P, P, u32, P, u32, u32, i32, i32, P]),
             "dk_unet_conv3x3_wgrad": (i32, [P, u32, P, u32, u32, u32, u32, u32, u32, P, P]),
             "dk_unet_relu_backward": (i32, [P, u32, P, u32, P, u32, u32, u32, P]),

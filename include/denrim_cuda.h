@@ -446,6 +446,35 @@ int dk_denoise_spatial(const float* beauty, const float* depth, const float* nor
                        float* out, float* scratch, uint32_t width, uint32_t height,
                        const dk_spatial_denoise_settings* settings, void* stream);
 
+/* DenoiseSettings.appleSVGF (Denoiser.swift:67-76) -- AppleSVGFDenoiser
+ * (Denoiser.swift:167-300) -- as spatiotemporal variance-guided filtering
+ * (the published SVGF algorithm; the reference's implementation is Apple's
+ * closed MPSSVGFDenoiser) with the parameters its configure(settings:) sets:
+ * a-trous iterations clamp(iterations, 1, 5), filter and variance radius
+ * clamp(radius, 1, 4), depth weight max(depth_sigma, 1e-4), normal weight
+ * clamp(24 / normal_sigma, 1, 512), luminance weight max(color_sigma, 1e-4),
+ * moving-average factor 0.2.  One object per image size holds the temporal
+ * history; dk_svgf_reset is clearTemporalHistory.  dk_svgf_denoise takes
+ * DEVICE RGBA32F planes (beauty, depth, encoded normal and motion-vector AOVs
+ * as dk_session_copy_output lays them out) and writes `out`; asynchronous on
+ * `stream`. */
+typedef struct dk_svgf dk_svgf;
+int dk_svgf_create(uint32_t width, uint32_t height, dk_svgf** out_svgf);
+int dk_svgf_reset(dk_svgf* svgf);
+int dk_svgf_denoise(dk_svgf* svgf, const float* beauty, const float* depth, const float* normal, const float* motion,
+                    float* out, const dk_spatial_denoise_settings* settings, void* stream);
+/* The filter state after the last dk_svgf_denoise, copied to device memory:
+ * 0 history colour, 1 (luminance mean, mean square, history length, 0),
+ * 2 packed (depth, signed normal). */
+int dk_svgf_read_state(dk_svgf* svgf, int which, float* device_rgba, size_t pixel_count, void* stream);
+int dk_svgf_destroy(dk_svgf* svgf);
+/* packSVGFDepthNormalKernel (Denoise.metal:117-136) and copySVGFOutputKernel
+ * (Denoise.metal:138-154) on their own, over device RGBA32F planes. */
+int dk_svgf_pack_depth_normal(const float* depth, const float* normal, float* depth_normal, uint32_t width,
+                              uint32_t height, void* stream);
+int dk_svgf_copy_output(const float* denoised, const float* original, float* out, uint32_t width, uint32_t height,
+                        void* stream);
+
 /* Learned denoiser building blocks (no counterpart in the reference, whose
  * denoisers are the spatial filter above and Apple's SVGF).  Tensors are
  * DEVICE NHWC bf16 (raw 16-bit storage) with channel counts that are

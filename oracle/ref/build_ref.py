@@ -19,7 +19,8 @@ OUT = os.path.join(ORACLE, "_ref")
 SHADERS = os.path.join("/root/reference", "Sources", "DenrimRendererKit", "Resources", "Shaders")
 # (reference shader, kernels kept, generated file)
 UNITS = (("PathTrace.metal", ("pathTraceKernel", "flatPreviewKernel", "interactiveMaterialKernel"), "pathtrace_ref.cpp"),
-         ("Denoise.metal", ("simpleSpatialDenoiseKernel",), "denoise_ref.cpp"))
+         ("Denoise.metal", ("simpleSpatialDenoiseKernel", "packSVGFDepthNormalKernel", "copySVGFOutputKernel"),
+          "denoise_ref.cpp"))
 GENERATED = os.path.join(OUT, "pathtrace_ref.cpp")
 LIB = os.path.join(OUT, "libref_pathtrace.so")
 

@@ -63,6 +63,7 @@ template <class T> struct alignas(sizeof(T) * 4) vec4 {
     constexpr vec4(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}
     explicit constexpr vec4(T s) : x(s), y(s), z(s), w(s) {}
     constexpr vec4(vec3<T> a, T d) : x(a.x), y(a.y), z(a.z), w(d) {}
+    constexpr vec4(T a, vec3<T> b) : x(a), y(b.x), z(b.y), w(b.z) {}
     constexpr vec4(vec2<T> a, vec2<T> b) : x(a.x), y(a.y), z(b.x), w(b.y) {}
     constexpr vec4(vec2<T> a, T c, T d) : x(a.x), y(a.y), z(c), w(d) {}
     template <class U> explicit constexpr vec4(vec4<U> o) : x(T(o.x)), y(T(o.y)), z(T(o.z)), w(T(o.w)) {}
@@ -197,6 +198,7 @@ MREF_MAP1(acos)
     template <class T> vec3<T> name(vec3<T> a, S<T> s) { return {name(a.x, s), name(a.y, s), name(a.z, s)}; }
 MREF_MAP2(min)
 MREF_MAP2(max)
+inline bool3 isfinite(vec3<float> v) { return {isfinite(v.x), isfinite(v.y), isfinite(v.z)}; }
 MREF_MAP2(pow)
 MREF_MAP2(fmod)
 #undef MREF_MAP2
