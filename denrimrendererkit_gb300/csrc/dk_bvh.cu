@@ -24,6 +24,9 @@
 // index), (v2 - v0, flags: bit 0 = blocks shadow rays, bits 8..15 material
 // ID).
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <deque>
 #include <mutex>
 #include <cfloat>
@@ -646,6 +649,25 @@ bool referenceSlots(const dk_scene* sc, std::vector<uint32_t>& slotOfTri, std::s
     return true;
 }
 
+namespace {
+// DK_TRACE_CREATE=1: the traversal build's phases (host wall time) on stderr.
+struct BuildTrace {
+    bool on;
+    std::chrono::steady_clock::time_point t;
+    BuildTrace() {
+        const char* e = getenv("DK_TRACE_CREATE");
+        on = e && e[0] == '1';
+        t = std::chrono::steady_clock::now();
+    }
+    void mark(const char* what) {
+        if (!on) return;
+        auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "[dk create]   %s %.1f ms\n", what, std::chrono::duration<double, std::milli>(now - t).count());
+        t = now;
+    }
+};
+}  // namespace
+
 // Binned-SAH traversal tree over every triangle that has a slot.
 int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri,
                       const std::vector<uint8_t>& opaque, int width, std::vector<float4>& nodes,
@@ -653,6 +675,7 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
     // Primitives of the triangles that have a slot, in triangle order: the
     // slotted triangles are counted per chunk, then every chunk writes its
     // primitives at its offset (several threads).
+    BuildTrace trace;
     const uint32_t tc = sc->triangle_count;
     const uint32_t parts = std::min<uint32_t>(16, std::max(1u, std::thread::hardware_concurrency()));
     std::vector<uint32_t> offset(parts + 1, 0);
@@ -689,6 +712,7 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
             });
         for (auto& th : pool) th.join();
     }
+    trace.mark("primitive records");
     nodes.clear();
     isect.clear();
     const uint32_t n = (uint32_t)prims.size();
@@ -714,6 +738,7 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
     }
     Arenas arenas;
     TNode* root = buildTree(prims, 8, arenas);
+    trace.mark("binned SAH tree");
     // The leaf slots in SAH order, filled by several threads while this
     // thread collapses the tree (the two are independent).
     isect.resize(3 * (size_t)(n + 1));
@@ -754,6 +779,7 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
     const uint32_t wideNodes = count4(root, 0, maxDepth);
     nodes.resize(8 * (size_t)wideNodes);
     emit4(root, 0, nodes.data(), dummyLeaf, 0);
+    trace.mark("4-wide collapse");
     // Each level pushes at most three siblings on the 64-entry traversal stack.
     if (3 * (maxDepth + 1) + 1 > 64) {
         err = "traversal BVH deeper than the 64-entry stack";

@@ -4,6 +4,7 @@
 // restate the reference's Swift host builders.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -291,9 +292,29 @@ static int traversalWidth() {
     return (e && e[0] == '8' && e[1] == 0) ? 8 : 4;
 }
 
+// DK_TRACE_CREATE=1: session-create phases (host wall time) on stderr.
+bool traceCreate() {
+    static const bool on = [] {
+        const char* e = getenv("DK_TRACE_CREATE");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+
+double wallMs() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 TraversalBuild buildTraversal(const dk_scene* sc) {
     // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
     // reaches, each carrying its reference DFS slot as the tie-break key.
+    const double t0 = traceCreate() ? wallMs() : 0.0;
+    struct Report {
+        double t0;
+        ~Report() {
+            if (traceCreate()) fprintf(stderr, "[dk create] traversal build %.1f ms\n", wallMs() - t0);
+        }
+    } report{t0};
     TraversalBuild t;
     t.width = traversalWidth();
     std::vector<uint32_t> slotOf;
@@ -303,6 +324,7 @@ TraversalBuild buildTraversal(const dk_scene* sc) {
         t.err = "Invalid render scene: " + err + ".";
         return t;
     }
+    if (traceCreate()) fprintf(stderr, "[dk create]   reference slots %.1f ms\n", wallMs() - t0);
     std::vector<uint8_t> opaque(sc->triangle_count);
     for (uint32_t i = 0; i < sc->triangle_count; ++i) {
         const dk_material& m = sc->materials[std::min(sc->triangles[i].material_id, sc->material_count - 1)];
@@ -658,6 +680,14 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     if (rc != DK_OK) return rc;
     rc = dk::ensureDevice();
     if (rc != DK_OK) return rc;
+    const bool trace = dk::traceCreate();
+    double tPrev = trace ? dk::wallMs() : 0.0;
+    auto phase = [&](const char* what) {
+        if (!trace) return;
+        double now = dk::wallMs();
+        fprintf(stderr, "[dk create] %s %.1f ms\n", what, now - tPrev);
+        tPrev = now;
+    };
     // The host traversal build runs while this thread allocates the wave.
     std::future<dk::TraversalBuild> traversal =
         std::async(std::launch::async, [sc] { return dk::buildTraversal(sc); });
@@ -690,13 +720,17 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     if (st->max_samples_per_launch > 0) capPaths = std::min<uint64_t>(capPaths, (uint64_t)st->max_samples_per_launch * pixels);
     capPaths = std::max<uint64_t>(capPaths, pixels);
     capPaths = std::min<uint64_t>(capPaths, 1ull << 29);  // path indices fit 29 bits of the NEE record
+    phase("stream");
     if (st->quality == DK_QUALITY_FINAL) {  // preview / interactive keep no path state
         TRY(dk::allocWave(s->arena, s->wave, capPaths, pixels, 1));
         s->jobs = const_cast<dk::DevJob*>(s->wave.jobs);
     }
+    phase("wave allocation");
     TRY(dk::allocAccum(s->arena, s->accum, pixels));
     TRY(s->arena.alloc(&s->staging, pixels, "readback staging"));
+    phase("accumulation allocation");
     TRY(dk::uploadScene(s->arena, sc, s->scene, sc->material_count, &traversal));
+    phase("scene upload (with the traversal build's tail)");
     s->opaqueMask = dk::opaqueMask(sc->materials, sc->material_count);
     TRY(dk::clearAccum(s->accum, pixels, s->stream));
     if (cudaMemsetAsync(s->accum.aov, 0, 6 * (size_t)pixels * sizeof(float4), s->stream) != cudaSuccess ||
@@ -706,6 +740,7 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     }
     s->grids = dk::kernelGrids();
     s->stats.device_bytes = s->arena.bytes;
+    phase("clears");
     *outSession = reinterpret_cast<dk_session*>(s);
     return DK_OK;
 #undef TRY

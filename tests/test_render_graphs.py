@@ -122,3 +122,39 @@ def test_server_copy_output_equals_host_readback(dk_lib):
                 assert np.array_equal(batch[i].cpu().numpy().view(np.uint32), host.view(np.uint32)), k.name
         for j in ids + more:
             server.release(j)
+
+
+def test_session_created_while_another_renders(dk_lib):
+    # Two sessions in flight, as the pipelined end-to-end loop runs them: one
+    # is created (host traversal build, uploads) on a second thread while the
+    # other renders; both images equal their one-at-a-time renders bit for bit.
+    from concurrent.futures import ThreadPoolExecutor
+    from denrimrendererkit_gb300 import RenderOutput, compile_scene, scenes
+    from denrimrendererkit_gb300.renderer import RenderSession
+    wl_a = scenes.spheres_large(width=192, height=108)
+    wl_b = scenes.material_zoo()
+    ba, bb = compile_scene(wl_a.scene), compile_scene(wl_b.scene)
+
+    def run(build, wl):
+        s = RenderSession(build, wl.settings, wl.scene.camera)
+        s.render(4)
+        img = s.pixels(RenderOutput.BEAUTY)
+        ids = s.pixels(RenderOutput.OBJECT_ID)
+        s.close()
+        return img, ids
+
+    solo_a, solo_b = run(ba, wl_a), run(bb, wl_b)
+    with ThreadPoolExecutor(1) as ex:
+        for _ in range(2):
+            sa = RenderSession(ba, wl_a.settings, wl_a.scene.camera)
+            fut = ex.submit(RenderSession, bb, wl_b.settings, wl_b.scene.camera)
+            sa.render(4)
+            got_a = (sa.pixels(RenderOutput.BEAUTY), sa.pixels(RenderOutput.OBJECT_ID))
+            sa.close()
+            sb = fut.result()
+            sb.render(4)
+            got_b = (sb.pixels(RenderOutput.BEAUTY), sb.pixels(RenderOutput.OBJECT_ID))
+            sb.close()
+            for got, want in ((got_a, solo_a), (got_b, solo_b)):
+                for g, w in zip(got, want):
+                    assert g.view(np.uint32).tobytes() == w.view(np.uint32).tobytes()
