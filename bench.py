@@ -607,7 +607,7 @@ def run_denoise(args, rank):
         t_graphed = per_image(lambda: denoised(True))
         t_plain = per_image(plain, reps=5)
         check = float((denoised(True) - denoised(False)).abs().max())
-    batched = {f"batch_{n}": serve_batches_with_denoising(net, wl, vb, plain_spp, batch=n) for n in (8, 16)}
+    batched = {f"batch_{n}": serve_batches_with_denoising(net, wl, vb, plain_spp, batch=n) for n in (8, 16, 32)}
     used_graph = t_graphed <= t_denoised
     t_ungraphed = t_denoised
     t_denoised = min(t_denoised, t_graphed)
