@@ -241,6 +241,9 @@ __global__ void __launch_bounds__(256) k_svgf_copy(const float4* __restrict__ de
 
 dim3 tiles(uint32_t w, uint32_t h) { return dim3((w + 15) / 16, (h + 15) / 16); }
 
+// The planes are read and written as float4.
+bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16u == 0u; }
+
 }  // namespace
 
 struct Svgf {
@@ -297,6 +300,9 @@ int dk_svgf_denoise(dk_svgf* svgf, const float* beauty, const float* depth, cons
     auto* s = reinterpret_cast<dk::Svgf*>(svgf);
     if (!s || !beauty || !depth || !normal || !motion || !out || !settings)
         return fail(DK_ERROR_INVALID_ARGUMENT, "dk_svgf_denoise: null argument");
+    if (!dk::aligned16(beauty) || !dk::aligned16(depth) || !dk::aligned16(normal) || !dk::aligned16(motion) ||
+        !dk::aligned16(out))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "dk_svgf_denoise: planes must be 16-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint32_t W = s->width, H = s->height;
     dim3 g = dk::tiles(W, H);
@@ -362,7 +368,9 @@ int dk_svgf_destroy(dk_svgf* svgf) {
 
 int dk_svgf_pack_depth_normal(const float* depth, const float* normal, float* depthNormal, uint32_t width,
                               uint32_t height, void* stream) {
-    if (!depth || !normal || !depthNormal) return fail(DK_ERROR_INVALID_ARGUMENT, "dk_svgf_pack_depth_normal");
+    if (!depth || !normal || !depthNormal || !dk::aligned16(depth) || !dk::aligned16(normal) ||
+        !dk::aligned16(depthNormal))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "dk_svgf_pack_depth_normal: null or misaligned plane");
     if (width == 0 || height == 0) return DK_OK;
     dk::k_svgf_pack<<<dk::tiles(width, height), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         reinterpret_cast<const float4*>(depth), reinterpret_cast<const float4*>(normal),
@@ -373,7 +381,8 @@ int dk_svgf_pack_depth_normal(const float* depth, const float* normal, float* de
 
 int dk_svgf_copy_output(const float* denoised, const float* original, float* out, uint32_t width, uint32_t height,
                         void* stream) {
-    if (!denoised || !original || !out) return fail(DK_ERROR_INVALID_ARGUMENT, "dk_svgf_copy_output");
+    if (!denoised || !original || !out || !dk::aligned16(denoised) || !dk::aligned16(original) || !dk::aligned16(out))
+        return fail(DK_ERROR_INVALID_ARGUMENT, "dk_svgf_copy_output: null or misaligned plane");
     if (width == 0 || height == 0) return DK_OK;
     dk::k_svgf_copy<<<dk::tiles(width, height), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         reinterpret_cast<const float4*>(denoised), reinterpret_cast<const float4*>(original),

@@ -151,6 +151,10 @@ def test_cuda_helpers_equal_reference_kernels(dk_lib):
     torch.cuda.synchronize()
     assert same_bits(dn.cpu().numpy(), dn_ref)
     assert same_bits(out.cpu().numpy(), out_ref)
+    # planes are float4: a misaligned pointer is refused before any launch
+    rc = dk_lib.dk_svgf_copy_output(C.c_void_p(de.data_ptr() + 4), C.c_void_p(o.data_ptr()),
+                                    C.c_void_p(out.data_ptr()), w, h, None)
+    assert rc == 6  # DK_ERROR_INVALID_ARGUMENT
 
 
 def render_frames(count, moves, width=48, height=40, spp=1):
