@@ -43,6 +43,50 @@ class RenderOutput(enum.IntEnum):
     MOTION_VECTOR = 6
 
 
+DK_ENCODE_WORKSPACE_INTS = 4  # DK_ENCODE_WORKSPACE_BYTES / 4
+
+
+class RenderDenoiser(enum.IntEnum):
+    """RenderDenoiser (Denoising/Denoiser.swift:8-18)."""
+    NONE = 0
+    SIMPLE_SPATIAL = 1
+    APPLE_SVGF = 2
+
+
+@dataclasses.dataclass(frozen=True)
+class DenoiseSettings:
+    """DenoiseSettings (Denoising/Denoiser.swift:20-77); APPLE_SVGF runs the
+    CUDA SVGF (the reference's is Apple's MPSSVGFDenoiser)."""
+    denoiser: RenderDenoiser = RenderDenoiser.NONE
+    radius: int = 2
+    normal_sigma: float = 0.18
+    depth_sigma: float = 0.03
+    albedo_sigma: float = 0.25
+    color_sigma: float = 1.0
+    iterations: int = 3
+
+
+DenoiseSettings.NONE = DenoiseSettings()
+DenoiseSettings.SIMPLE_SPATIAL = DenoiseSettings(RenderDenoiser.SIMPLE_SPATIAL)
+DenoiseSettings.APPLE_SVGF = DenoiseSettings(RenderDenoiser.APPLE_SVGF, radius=2, normal_sigma=0.18,
+                                             depth_sigma=0.08, albedo_sigma=0.25, color_sigma=4.0, iterations=5)
+
+
+def aov_ray_enabled(denoise) -> int:
+    """GPURenderConstants.denoiserEnabled (RenderSession.swift:941): 1 when a
+    denoiser is requested (or the bool knob is set)."""
+    if isinstance(denoise, DenoiseSettings):
+        return int(denoise.denoiser != RenderDenoiser.NONE)
+    return int(bool(denoise))
+
+
+def denoise_filter(denoise) -> Optional[DenoiseSettings]:
+    """The filter a settings' `denoise` requests (None: no filtered beauty)."""
+    if isinstance(denoise, DenoiseSettings) and denoise.denoiser != RenderDenoiser.NONE:
+        return denoise
+    return None
+
+
 @dataclasses.dataclass
 class RenderSettings:
     width: int = 512
@@ -53,7 +97,10 @@ class RenderSettings:
     transparent_background: bool = False
     shows_environment_background: bool = True
     background_color: Sequence[float] = (0.0, 0.0, 0.0)
-    denoise: bool = False
+    # DenoiseSettings (the reference's `denoise`, RenderSettings.swift:63): a
+    # denoiser other than NONE traces the unjittered AOV ray and makes the
+    # beauty output the filtered image; a bool enables the AOV ray alone.
+    denoise: object = False
     sample_radiance_clamp: Optional[float] = None
     collects_traversal_stats: bool = False
     frame_seed: int = 0x1234ABCD  # RenderSession.swift:917
@@ -78,7 +125,7 @@ def make_settings_struct(settings: RenderSettings, camera: Camera) -> abi.Settin
     s.sample_radiance_clamp_set = 1
     s.sample_radiance_clamp = settings.resolved_sample_radiance_clamp
     s.frame_seed = settings.frame_seed & 0xFFFFFFFF
-    s.denoiser_enabled = int(settings.denoise)
+    s.denoiser_enabled = aov_ray_enabled(settings.denoise)
     s.collects_traversal_stats = int(settings.collects_traversal_stats)
     s.camera = camera.gpu_camera(settings.width, settings.height)
     prev = settings.previous_camera
@@ -100,6 +147,44 @@ class RenderSession:
         settings_struct = make_settings_struct(settings, camera)
         library.check(self._lib.dk_session_create(C.byref(scene_struct), C.byref(settings_struct),
                                                   C.byref(self._handle)))
+        self._denoised = None  # filtered beauty (device tensor) while current
+        self._svgf = None
+
+    # RenderSession.ensureDenoisedBeautyIsCurrent (RenderSession.swift:1115-1165):
+    # the requested filter over the session's own planes on the device, once
+    # per new sample.
+    def _denoised_beauty(self):
+        f = denoise_filter(self.settings.denoise)
+        if f is None:
+            return None
+        if self._denoised is not None:
+            return self._denoised
+        import torch
+        from . import denoiser
+        w, h = self.settings.width, self.settings.height
+        planes = {k: self.copy_output(k, torch.empty(h, w, 4, device="cuda"))
+                  for k in (RenderOutput.BEAUTY, RenderOutput.DEPTH, RenderOutput.NORMAL, RenderOutput.ALBEDO,
+                            RenderOutput.MOTION_VECTOR)}
+        out = torch.empty(h, w, 4, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        if f.denoiser == RenderDenoiser.SIMPLE_SPATIAL:
+            denoiser.spatial_denoise(planes[RenderOutput.BEAUTY], planes[RenderOutput.DEPTH],
+                                     planes[RenderOutput.NORMAL], planes[RenderOutput.ALBEDO], out, w, h,
+                                     radius=f.radius, normal_sigma=f.normal_sigma, depth_sigma=f.depth_sigma,
+                                     albedo_sigma=f.albedo_sigma, color_sigma=f.color_sigma,
+                                     iterations=f.iterations, stream=st)
+        else:
+            if self._svgf is None:
+                self._svgf = denoiser.SvgfDenoiser(w, h)
+            self._svgf.denoise(planes[RenderOutput.BEAUTY], planes[RenderOutput.DEPTH], planes[RenderOutput.NORMAL],
+                               planes[RenderOutput.MOTION_VECTOR], out, radius=f.radius,
+                               normal_sigma=f.normal_sigma, depth_sigma=f.depth_sigma, color_sigma=f.color_sigma,
+                               iterations=f.iterations, stream=st)
+        self._denoised = out
+        return out
+
+    def _stale(self) -> None:
+        self._denoised = None
 
     # RenderSession.render(samples:) (RenderSession.swift:1010-1017)
     def render(self, samples: int, to: Optional[str] = None) -> None:
@@ -107,6 +192,7 @@ class RenderSession:
         with `to`, the beauty output is then written as a PNG file there."""
         if samples < 0:
             raise ValueError("Invalid render scene: Sample count must not be negative.")
+        self._stale()
         library.check(self._lib.dk_session_render(self._handle, samples))
         if to is not None:
             self.write_png(to)
@@ -114,6 +200,11 @@ class RenderSession:
     # RenderSession.writePNG(output:to:) (RenderSession.swift:1026-1034)
     def write_png(self, path: str, output: "RenderOutput" = None) -> None:
         output = RenderOutput.BEAUTY if output is None else output
+        if output == RenderOutput.BEAUTY and denoise_filter(self.settings.denoise) is not None:
+            w, h = self.settings.width, self.settings.height
+            rgba = np.ascontiguousarray(self.rgba8(output))
+            library.check(self._lib.dk_write_png(os.fsencode(path), rgba.ctypes.data, w, h))
+            return
         library.check(self._lib.dk_session_write_png(self._handle, int(output), os.fsencode(path)))
 
     def rgba8(self, output: "RenderOutput" = None) -> np.ndarray:
@@ -122,6 +213,16 @@ class RenderSession:
         output = RenderOutput.BEAUTY if output is None else output
         w, h = self.settings.width, self.settings.height
         out = np.empty((h, w, 4), np.uint8)
+        den = self._denoised_beauty() if output == RenderOutput.BEAUTY else None
+        if den is not None:
+            import torch
+            dev = torch.empty(h * w * 4, dtype=torch.uint8, device="cuda")
+            ws = torch.zeros(DK_ENCODE_WORKSPACE_INTS, dtype=torch.int32, device="cuda")
+            library.check(self._lib.dk_encode_rgba8(C.c_void_p(den.data_ptr()), w, h, int(output),
+                                                    C.c_void_p(dev.data_ptr()), C.c_void_p(ws.data_ptr()),
+                                                    C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+            out[...] = dev.cpu().numpy().reshape(h, w, 4)
+            return out
         library.check(self._lib.dk_session_read_rgba8(self._handle, int(output), out.ctypes.data, out.size))
         return out
 
@@ -130,16 +231,23 @@ class RenderSession:
 
     # RenderSession.renderNextTile(_:completesSample:) (RenderSession.swift:875-889)
     def render_next_tile(self, x: int, y: int, width: int, height: int, completes_sample: bool) -> None:
+        self._stale()
         library.check(self._lib.dk_session_render_tile(self._handle, x, y, width, height, int(completes_sample)))
 
     # RenderSession.updateCamera(_:previousCamera:) (RenderSession.swift:595-608)
     def update_camera(self, camera: Camera, previous_camera: Optional[Camera] = None) -> None:
         cur = camera.gpu_camera(self.settings.width, self.settings.height)
         prev = (previous_camera or self.camera).gpu_camera(self.settings.width, self.settings.height)
+        self._stale()
+        if self._svgf is not None:  # updateCamera resets accumulation (RenderSession.swift:594-608)
+            self._svgf.reset()
         library.check(self._lib.dk_session_update_camera(self._handle, C.byref(cur), C.byref(prev)))
         self.camera = camera
 
     def reset_accumulation(self) -> None:
+        self._stale()
+        if self._svgf is not None:  # RenderSession.resetAccumulation (RenderSession.swift:581-587)
+            self._svgf.reset()
         library.check(self._lib.dk_session_reset(self._handle))
 
     @property
@@ -159,6 +267,10 @@ class RenderSession:
         if out is None:
             out = np.empty((h, w, 4), np.float32)
         assert out.dtype == np.float32 and out.flags["C_CONTIGUOUS"] and out.size == w * h * 4
+        den = self._denoised_beauty() if output == RenderOutput.BEAUTY else None
+        if den is not None:  # texture(for: .beauty) is the denoised image (RenderSession.swift:1072-1080)
+            out[...] = den.cpu().numpy().reshape(out.shape)
+            return out
         library.check(self._lib.dk_session_read_output(self._handle, int(output), out.ctypes.data, w * h))
         return out
 
@@ -178,6 +290,10 @@ class RenderSession:
         return out
 
     def close(self) -> None:
+        if getattr(self, "_svgf", None) is not None:
+            self._svgf.close()
+            self._svgf = None
+        self._denoised = None
         if self._handle:
             self._lib.dk_session_destroy(self._handle)
             self._handle = C.c_void_p()

@@ -120,7 +120,8 @@ def make_params(settings, camera, tile=None):
         p.background_color[i] = float(settings.background_color[i])
     p.sample_radiance_clamp = settings.resolved_sample_radiance_clamp
     p.frame_seed = settings.frame_seed & 0xFFFFFFFF
-    p.denoiser_enabled = int(settings.denoise)
+    from denrimrendererkit_gb300.renderer import aov_ray_enabled
+    p.denoiser_enabled = aov_ray_enabled(settings.denoise)
     tx, ty, tw, th = tile or (0, 0, settings.width, settings.height)
     p.tile_x, p.tile_y, p.tile_w, p.tile_h = tx, ty, tw, th
     p.camera = camera.gpu_camera(settings.width, settings.height)
