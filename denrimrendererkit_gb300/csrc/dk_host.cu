@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <future>
+#include <mutex>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -305,6 +306,43 @@ double wallMs() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// The traversal working set (triangle slots + nodes) as a persisting L2
+// access-policy window of `stream`, opt-in (DK_L2_PERSIST=1): on the large
+// scene it costs a fifth of the frame rate -- the 85 MB set-aside starves the
+// shading stage's path-state and material traffic (k_shade 108 -> 162 ms)
+// and the traversal stages gain nothing.  The set-aside is a limit of this
+// process's context; the hit ratio scales the window to it.  Best effort: a
+// refusal leaves the stream as it was.
+void persistTraversal(const DevScene& D, cudaStream_t stream) {
+    static const bool on = [] {
+        const char* e = getenv("DK_L2_PERSIST");
+        return e && e[0] == '1';
+    }();
+    if (!on || !D.isect || D.traversal_bytes == 0) return;
+    int maxPersist = 0, maxWindow = 0;
+    if (cudaDeviceGetAttribute(&maxPersist, cudaDevAttrMaxPersistingL2CacheSize, g_device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxWindow, cudaDevAttrMaxAccessPolicyWindowSize, g_device) != cudaSuccess ||
+        maxPersist <= 0 || maxWindow <= 0) {
+        cudaGetLastError();
+        return;
+    }
+    static std::once_flag limitOnce;
+    std::call_once(limitOnce, [&] {
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)maxPersist) != cudaSuccess) cudaGetLastError();
+    });
+    size_t window = std::min<size_t>(D.traversal_bytes, (size_t)maxWindow);
+    cudaStreamAttrValue v{};
+    v.accessPolicyWindow.base_ptr = const_cast<float4*>(D.isect);
+    v.accessPolicyWindow.num_bytes = window;
+    v.accessPolicyWindow.hitRatio = std::min(1.0f, (float)maxPersist / (float)window);
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    if (cudaStreamSetAttribute(stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess) cudaGetLastError();
+    if (traceCreate())
+        fprintf(stderr, "[dk create] L2 window %.1f MB (set-aside %.1f MB, hit ratio %.2f)\n", window / 1e6,
+                maxPersist / 1e6, v.accessPolicyWindow.hitRatio);
+}
+
 TraversalBuild buildTraversal(const dk_scene* sc) {
     // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
     // reaches, each carrying its reference DFS slot as the tie-break key.
@@ -424,8 +462,20 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
     {
         TraversalBuild t = pending->get();
         if (t.rc != DK_OK) return fail(t.rc, t.err);
-        TRY(arena.upload(const_cast<float4**>(&D.isect), t.isect.data(), t.isect.size(), "triangle slots"));
-        TRY(arena.upload(const_cast<float4**>(&D.nodes), t.nodes.data(), t.nodes.size(), "BVH nodes"));
+        // Triangle slots and nodes in one block: the traversal working set is
+        // one address range (an L2 access-policy window covers it).
+        float4* block = nullptr;
+        TRY(arena.alloc(&block, t.isect.size() + t.nodes.size(), "triangle slots + BVH nodes"));
+        if (!t.isect.empty())
+            DK_CUDA(cudaMemcpy(block, t.isect.data(), t.isect.size() * sizeof(float4), cudaMemcpyHostToDevice),
+                    "triangle slots");
+        if (!t.nodes.empty())
+            DK_CUDA(cudaMemcpy(block + t.isect.size(), t.nodes.data(), t.nodes.size() * sizeof(float4),
+                               cudaMemcpyHostToDevice),
+                    "BVH nodes");
+        D.isect = block;
+        D.nodes = block + t.isect.size();
+        D.traversal_bytes = (t.isect.size() + t.nodes.size()) * sizeof(float4);
         D.node_count = (uint32_t)(t.nodes.size() / (t.width == 8 ? 5 : 8));
         D.wide8 = t.width == 8 ? 1u : 0u;
         D.all_shadow_opaque = t.allOpaque ? 1u : 0u;
@@ -731,6 +781,7 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     phase("accumulation allocation");
     TRY(dk::uploadScene(s->arena, sc, s->scene, sc->material_count, &traversal));
     phase("scene upload (with the traversal build's tail)");
+    dk::persistTraversal(s->scene, s->stream);
     s->opaqueMask = dk::opaqueMask(sc->materials, sc->material_count);
     TRY(dk::clearAccum(s->accum, pixels, s->stream));
     if (cudaMemsetAsync(s->accum.aov, 0, 6 * (size_t)pixels * sizeof(float4), s->stream) != cudaSuccess ||

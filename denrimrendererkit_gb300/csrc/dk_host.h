@@ -74,6 +74,8 @@ TraversalBuild buildTraversal(const dk_scene* sc);
 // started with std::async(buildTraversal).
 int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity,
                 std::future<TraversalBuild>* pending = nullptr);
+// The traversal arrays as a persisting L2 window of `stream` (best effort).
+void persistTraversal(const DevScene& D, cudaStream_t stream);
 
 // Whether a material blocks shadow rays (shadowOccluded, PathTrace.metal:
 // 4230-4241), and the opacity bits of a table's first 32 materials.

@@ -35,6 +35,7 @@ struct DevScene {
     const float2* env;
     const uint32_t* env_guide;  // G + 1 entries: first index with cdf >= b / G (G a power of two)
     uint32_t tri_count, mat_count, node_count, texdesc_count;
+    uint64_t traversal_bytes;  // triangle slots + nodes, one block starting at `isect` (host bookkeeping)
     uint32_t light_count, env_count, env_tex_plus1, all_shadow_opaque;
     float env_intensity, env_rot_y, env_max_radiance;
     uint32_t env_guide_size;
