@@ -464,18 +464,20 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
         if (t.rc != DK_OK) return fail(t.rc, t.err);
         // Triangle slots and nodes in one block: the traversal working set is
         // one address range (an L2 access-policy window covers it).
+        // Nodes start on a 128-byte line (a 4-wide node is one line).
+        const size_t nodeOfs = (t.isect.size() + 7) / 8 * 8;
         float4* block = nullptr;
-        TRY(arena.alloc(&block, t.isect.size() + t.nodes.size(), "triangle slots + BVH nodes"));
+        TRY(arena.alloc(&block, nodeOfs + t.nodes.size(), "triangle slots + BVH nodes"));
         if (!t.isect.empty())
             DK_CUDA(cudaMemcpy(block, t.isect.data(), t.isect.size() * sizeof(float4), cudaMemcpyHostToDevice),
                     "triangle slots");
         if (!t.nodes.empty())
-            DK_CUDA(cudaMemcpy(block + t.isect.size(), t.nodes.data(), t.nodes.size() * sizeof(float4),
+            DK_CUDA(cudaMemcpy(block + nodeOfs, t.nodes.data(), t.nodes.size() * sizeof(float4),
                                cudaMemcpyHostToDevice),
                     "BVH nodes");
         D.isect = block;
-        D.nodes = block + t.isect.size();
-        D.traversal_bytes = (t.isect.size() + t.nodes.size()) * sizeof(float4);
+        D.nodes = block + nodeOfs;
+        D.traversal_bytes = (nodeOfs + t.nodes.size()) * sizeof(float4);
         D.node_count = (uint32_t)(t.nodes.size() / (t.width == 8 ? 5 : 8));
         D.wide8 = t.width == 8 ? 1u : 0u;
         D.all_shadow_opaque = t.allOpaque ? 1u : 0u;
