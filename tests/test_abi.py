@@ -107,3 +107,26 @@ def test_product_fails_loudly_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(build, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         library.load()
+
+
+def test_denoise_settings_map_to_the_aov_ray_flag():
+    # GPURenderConstants.denoiserEnabled = denoise.denoiser != .none (RenderSession.swift:941);
+    # the presets are DenoiseSettings.none / .simpleSpatial / .appleSVGF (Denoiser.swift:62-76).
+    from denrimrendererkit_gb300.renderer import (DenoiseSettings, RenderDenoiser, RenderSettings, denoise_filter,
+                                                  make_settings_struct)
+    from denrimrendererkit_gb300.scene import Camera
+    cam = Camera((0, 0, 3), (0, 0, 0))
+    cases = [(False, 0, None), (True, 1, None), (DenoiseSettings.NONE, 0, None),
+             (DenoiseSettings.SIMPLE_SPATIAL, 1, RenderDenoiser.SIMPLE_SPATIAL),
+             (DenoiseSettings.APPLE_SVGF, 1, RenderDenoiser.APPLE_SVGF)]
+    for denoise, flag, filt in cases:
+        s = make_settings_struct(RenderSettings(width=8, height=8, denoise=denoise), cam)
+        assert s.denoiser_enabled == flag
+        f = denoise_filter(denoise)
+        assert (f.denoiser if f else None) == filt
+    svgf = DenoiseSettings.APPLE_SVGF
+    assert (svgf.radius, svgf.normal_sigma, svgf.depth_sigma, svgf.albedo_sigma, svgf.color_sigma,
+            svgf.iterations) == (2, 0.18, 0.08, 0.25, 4.0, 5)
+    sp = DenoiseSettings.SIMPLE_SPATIAL
+    assert (sp.radius, sp.normal_sigma, sp.depth_sigma, sp.albedo_sigma, sp.color_sigma, sp.iterations) == \
+        (2, 0.18, 0.03, 0.25, 1.0, 3)
