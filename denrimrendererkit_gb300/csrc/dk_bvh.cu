@@ -50,6 +50,10 @@ constexpr uint32_t kLeaf = 0x80000000u;
 #ifndef DK_SAH_NODE_COST
 #define DK_SAH_NODE_COST 1.0f
 #endif
+#ifndef DK_SAH_MAX_LEAF
+#define DK_SAH_MAX_LEAF 8  // <= 8: a 4-wide child reference holds count - 1 in 3 bits
+#endif
+static_assert(DK_SAH_MAX_LEAF >= 1 && DK_SAH_MAX_LEAF <= 8, "leaf size must fit the child encoding");
 constexpr int kBins = DK_SAH_BINS;
 constexpr float kNodeCost = DK_SAH_NODE_COST;  // traversal step cost in triangle tests
 
@@ -737,7 +741,7 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
         return DK_OK;
     }
     Arenas arenas;
-    TNode* root = buildTree(prims, 8, arenas);
+    TNode* root = buildTree(prims, DK_SAH_MAX_LEAF, arenas);
     trace.mark("binned SAH tree");
     // The leaf slots in SAH order, filled by several threads while this
     // thread collapses the tree (the two are independent).
