@@ -180,30 +180,37 @@ __global__ void __launch_bounds__(256) k_svgf_variance(const float4* __restrict_
     out[i] = make_float4(c.x, c.y, c.z, var);
 }
 
-// One a-trous pass over (rgb, variance) with step `p.step`.
+// One a-trous pass over (rgb, variance) with step `p.step`.  The tap weight
+// Gaussian(k) * depth * normal * luminance terms is evaluated as one
+// exp2 of the summed exponents (the normal term's power through one log2):
+// two special-function operations per tap.
 __global__ void __launch_bounds__(256) k_svgf_atrous(const float4* __restrict__ src, const float4* __restrict__ dnCur,
                                                      float4* __restrict__ dst, float4* __restrict__ history,
                                                      SvgfParams p) {
+    constexpr float kLog2e = 1.4426950408889634f;
     int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
     if (x >= (int)p.width || y >= (int)p.height) return;
     size_t i = (size_t)y * p.width + x;
     float4 cp = src[i];
     float4 dp = dnCur[i];
-    // 3x3 Gaussian prefilter of the variance
+    // 3x3 Gaussian prefilter of the variance (three distinct weights)
     float gpre = 1.0f / (2.0f * p.prefilterSigma * p.prefilterSigma);
+    const float wpre[3] = {1.0f, __expf(-gpre), __expf(-2.0f * gpre)};
     float vs = 0.0f, vw = 0.0f;
     for (int dy = -1; dy <= 1; ++dy)
         for (int dx = -1; dx <= 1; ++dx) {
             int qx = x + dx, qy = y + dy;
             if (!inside(qx, qy, p)) continue;
-            float w = __expf(-(float)(dx * dx + dy * dy) * gpre);
+            float w = wpre[dx * dx + dy * dy];
             vs += w * src[(size_t)qy * p.width + qx].w;
             vw += w;
         }
     float sigmaL = sqrtf(fmaxf(vs / vw, 0.0f));
     float lumScale = 1.0f / (p.luminanceWeight * sigmaL + 1.0e-6f);
     float lp = luminance(make_float3(cp.x, cp.y, cp.z));
-    float gb = 1.0f / (2.0f * p.bilateralSigma * p.bilateralSigma);
+    // exponents in log2 units
+    const float gb2 = kLog2e / (2.0f * p.bilateralSigma * p.bilateralSigma);
+    const float dz2 = kLog2e / p.depthWeight, dl2 = kLog2e * lumScale;
     float3 sc = make_float3(0.0f, 0.0f, 0.0f);
     float sv = 0.0f, sw = 0.0f;
     for (int ky = -p.radius; ky <= p.radius; ++ky)
@@ -212,8 +219,12 @@ __global__ void __launch_bounds__(256) k_svgf_atrous(const float4* __restrict__ 
             if (!inside(qx, qy, p)) continue;
             size_t j = (size_t)qy * p.width + qx;
             float4 cq = src[j];
+            float4 dq = dnCur[j];
             float lq = luminance(make_float3(cq.x, cq.y, cq.z));
-            float w = __expf(-(float)(kx * kx + ky * ky) * gb) * edgeWeight(dp, dnCur[j], lp, lq, lumScale, p);
+            float cosn = fmaxf(0.0f, dp.y * dq.y + dp.z * dq.z + dp.w * dq.w);
+            float e = -(float)(kx * kx + ky * ky) * gb2 - fabsf(dp.x - dq.x) * dz2 - fabsf(lp - lq) * dl2 +
+                      p.normalWeight * __log2f(cosn);
+            float w = exp2f(e);
             sc.x += w * cq.x;
             sc.y += w * cq.y;
             sc.z += w * cq.z;
