@@ -134,15 +134,6 @@ __global__ void __launch_bounds__(256) k_svgf_temporal(const float4* __restrict_
     moments[i] = outM;
 }
 
-__device__ __forceinline__ float edgeWeight(float4 dp, float4 dq, float lp, float lq, float lumScale,
-                                            const SvgfParams& p) {
-    float wz = __expf(-fabsf(dp.x - dq.x) / p.depthWeight);
-    float cosn = fmaxf(0.0f, dp.y * dq.y + dp.z * dq.z + dp.w * dq.w);
-    float wn = __powf(cosn, p.normalWeight);
-    float wl = __expf(-fabsf(lp - lq) * lumScale);
-    return wz * wn * wl;
-}
-
 // Variance: from the temporal moments once 4 frames are integrated, else a
 // bilateral estimate over the variance-estimation radius (boosted by 4 / n
 // for young histories).  Output (rgb, variance).
@@ -158,17 +149,21 @@ __global__ void __launch_bounds__(256) k_svgf_variance(const float4* __restrict_
     if (m.z >= 4.0f) {
         var = fmaxf(0.0f, m.y - m.x * m.x);
     } else {
+        constexpr float kLog2e = 1.4426950408889634f;
         float4 dp = dnCur[i];
-        float lp = m.x;
         float s1 = 0.0f, s2 = 0.0f, sw = 0.0f;
-        float g = 1.0f / (2.0f * p.varianceSigma * p.varianceSigma);
+        // Gaussian x depth x normal weights as one exp2 (as in the a-trous pass)
+        const float g2 = kLog2e / (2.0f * p.varianceSigma * p.varianceSigma), dz2 = kLog2e / p.depthWeight;
         for (int dy = -p.varianceRadius; dy <= p.varianceRadius; ++dy)
             for (int dx = -p.varianceRadius; dx <= p.varianceRadius; ++dx) {
                 int qx = x + dx, qy = y + dy;
                 if (!inside(qx, qy, p)) continue;
                 size_t j = (size_t)qy * p.width + qx;
                 float4 mq = moments[j];
-                float w = __expf(-(float)(dx * dx + dy * dy) * g) * edgeWeight(dp, dnCur[j], lp, mq.x, 0.0f, p);
+                float4 dq = dnCur[j];
+                float cosn = fmaxf(0.0f, dp.y * dq.y + dp.z * dq.z + dp.w * dq.w);
+                float w = exp2f(-(float)(dx * dx + dy * dy) * g2 - fabsf(dp.x - dq.x) * dz2 +
+                                p.normalWeight * __log2f(cosn));
                 s1 += w * mq.x;
                 s2 += w * mq.y;
                 sw += w;
