@@ -732,13 +732,47 @@ def serve_batches_with_denoising(net, wl, build, plain_spp, batch=8, batches=10)
         torch.cuda.synchronize()
         return (time.perf_counter() - t) / (batches * batch)
 
+    # Pipelined: batch b's U-Net (torch's stream) runs while batch b + 1 renders
+    # (the server's stream); two graph instances alternate their input planes
+    # (the server writes them from its own I/O stream) and pinned host buffers.
+    graphs = [graphed, GraphedDenoiser(net, W, H, batch=batch)]
+    hosts = [host, torch.empty((batch, H, W, 4), dtype=torch.float32).pin_memory()]
+    freed = [None, None]
+
+    def pipelined(server, count):
+        for b in range(count):
+            g, h = graphs[b % 2], hosts[b % 2]
+            ids = [server.submit(st, c, 4) for c in cams]
+            while server.step():
+                pass
+            if freed[b % 2] is not None:  # batch b - 2 has left this graph's inputs and host buffer
+                freed[b % 2].synchronize()
+            for k, t in zip(kinds, g.inputs):
+                server.copy_outputs(ids, k, t)
+            h.copy_(g.replay(), non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
+            freed[b % 2] = ev
+            for j in ids:
+                server.release(j)
+        torch.cuda.synchronize()
+        return hosts[(count - 1) % 2]
+
     with RenderServer(build) as server:
         t_den = per_image(server, 4, True)
         t_plain = per_image(server, plain_spp, False)
+        pipelined(server, 2)
+        t = time.perf_counter()
+        last = pipelined(server, batches).clone()
+        t_pipe = (time.perf_counter() - t) / (batches * batch)
+        same = bool(torch.equal(last, run(server, 4, True)))
     return {"requests_per_batch": batch, "image": f"{W}x{H} views of one held-out small-scene variant",
             "denoised_ms_per_image": t_den * 1e3, "plain_ms_per_image": t_plain * 1e3,
             "plain_spp_equal_error": plain_spp, "images_per_s_denoised": 1.0 / t_den,
             "images_per_s_plain": 1.0 / t_plain, "images_per_s_ratio": t_plain / t_den,
+            "pipelined": {"denoised_ms_per_image": t_pipe * 1e3, "images_per_s_denoised": 1.0 / t_pipe,
+                          "images_per_s_ratio": t_plain / t_pipe, "images_equal_sequential": same,
+                          "note": "batch b's U-Net overlaps batch b + 1's render (separate streams)"},
             "note": "render server: the batch's jobs share waves; 4 spp + batched U-Net (CUDA graph) vs plain "
                     "rendering at the U-Net's display error; outputs copied device to device, results read back"}
 
