@@ -243,3 +243,33 @@ def test_cuda_svgf_static_frames_converge(dk_lib):
     # the history's error is mostly the blur across the box's edges: it
     # still falls as frames integrate
     assert hist_errs[-1] < 0.92 * hist_errs[0], hist_errs
+
+
+def test_oracle_reprojection_follows_the_motion_convention():
+    # The motion AOV is previousScreen - currentScreen (PathTrace.metal:5569-5577): content that moved one
+    # pixel right has motion (-1, 0), and its history comes from one pixel to the left.  Stripes one pixel
+    # wide: with the right convention the blended history equals the new frame exactly; with the sign
+    # flipped it would mix the neighbouring stripes.
+    h, w = 12, 20
+    xs = np.arange(w)
+    pattern = np.zeros((h, w, 4), f32)
+    pattern[..., 0] = (xs % 2)[None, :] * 0.8 + 0.1
+    pattern[..., 1] = 0.3
+    pattern[..., 2] = ((xs // 2) % 2)[None, :] * 0.5 + 0.2
+    pattern[..., 3] = 1.0
+    depth = np.full((h, w, 4), 2.0, f32)
+    normal = np.full((h, w, 4), (0.5, 0.5, 1.0, 1.0), f32)
+    still = np.zeros((h, w, 4), f32)
+    still[..., 3] = 1.0
+    s = so.Svgf(w, h)
+    p = so.params()
+    s.denoise(pattern, depth, normal, still, p)
+    moved = np.roll(pattern, 1, axis=1)
+    motion = still.copy()
+    motion[..., 0] = -1.0
+    s.denoise(moved, depth, normal, motion, p)
+    length = s.prev[2][..., 2]
+    assert (length[:, 1:] == 2).all() and (length[:, 0] == 1).all()
+    # the integrated luminance moments of the interior equal the moved frame's (no stripe mixing)
+    lum = so.luminance(moved[..., :3])
+    assert np.allclose(s.prev[2][:, 1:, 0], lum[:, 1:], rtol=1e-6, atol=1e-7)
