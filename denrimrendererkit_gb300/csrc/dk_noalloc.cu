@@ -154,6 +154,24 @@ int dk_build_environment_samples_noalloc(const dk_float4* device_pixels, uint32_
     *out_count = 0;
     if (width == 0 || height == 0) return DK_OK;
     if (!device_pixels || !device_out) return naFail(DK_ERROR_INVALID_ARGUMENT, "device_pixels or device_out is null");
+    // The kernels read float4 texels and write float2 entries: both pointers
+    // must be aligned for those and must be device (or managed) memory, so a
+    // host or misaligned pointer is an error here, not a fault in the context.
+    if (reinterpret_cast<uintptr_t>(device_pixels) % 16u != 0 || reinterpret_cast<uintptr_t>(device_out) % 8u != 0)
+        return naFail(DK_ERROR_INVALID_ARGUMENT,
+                      "dk_build_environment_samples_noalloc: device_pixels must be 16-byte and device_out 8-byte "
+                      "aligned");
+    for (const void* ptr : {static_cast<const void*>(device_pixels), static_cast<const void*>(device_out)}) {
+        cudaPointerAttributes attr{};
+        cudaError_t pe = cudaPointerGetAttributes(&attr, ptr);
+        if (pe != cudaSuccess) {
+            cudaGetLastError();
+            return naFail(DK_ERROR_INVALID_ARGUMENT, "dk_build_environment_samples_noalloc: unknown pointer", pe);
+        }
+        if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+            return naFail(DK_ERROR_INVALID_ARGUMENT,
+                          "dk_build_environment_samples_noalloc: device_pixels and device_out must be device memory");
+    }
     uint64_t n64 = (uint64_t)width * height;
     if (n64 > kMaxTexels)
         return naFail(DK_ERROR_INVALID_ARGUMENT,
@@ -166,6 +184,17 @@ int dk_build_environment_samples_noalloc(const dk_float4* device_pixels, uint32_
     double* blockSums = scratch + kMaxTexels;
     uint32_t nb = (n + kBlock - 1u) / kBlock;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The call reads the table's total back to the host and waits for it,
+    // which a stream under capture cannot do: such a call is refused.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing(st, &capture);
+    if (ce != cudaSuccess || capture != cudaStreamCaptureStatusNone) {
+        if (ce != cudaSuccess) cudaGetLastError();
+        return naFail(DK_ERROR_INVALID_ARGUMENT,
+                      "dk_build_environment_samples_noalloc: the stream is being captured (or invalid)", ce);
+    }
+    // An error left by unrelated earlier work is not this call's failure.
+    cudaGetLastError();
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -180,6 +209,8 @@ int dk_build_environment_samples_noalloc(const dk_float4* device_pixels, uint32_
     k_na_weights<<<grid, 256, 0, st>>>(px, width, height, I, M, scratch);
     k_na_scan_block<<<nb, kBlock, 0, st>>>(scratch, n, blockSums);
     k_na_scan_totals<<<1, 32, 0, st>>>(blockSums, nb);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return naFail(DK_ERROR_COMMAND_FAILED, "environment table (no-alloc) launch failed", e);
     double total = 0.0;
     e = cudaMemcpyAsync(&total, blockSums + nb, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -1393,14 +1393,21 @@ void ORACLE_EXPORT(random_sequence)(uint32_t state, uint32_t n, double* out) {
 // 5520-5524, rounded to float per sample in the FP32 build as the RGBA32F
 // texture does) and the last-sample AOV planes (6 * W*H*4 floats, may be null).
 // `counters` (C_COUNT entries) accumulates work counts; `threads` <= 0 uses all
-// hardware threads.  Returns 0 on success.
+// hardware threads.  Returns 0 on success, 1 for a null argument, 2 for an
+// empty image, 3 for a scene without materials and 4 when a listed pixel lies
+// outside the image (nothing is written then).
 int ORACLE_EXPORT(render)(const dk_scene* scene, const oracle_params* params, uint32_t sample_begin,
                           uint32_t sample_count, const uint32_t* pixel_list, uint32_t pixel_list_count, int threads,
                           double* accum, float* aov, uint64_t* counters) {
     if (!scene || !params || !accum) return 1;
     if (scene->material_count == 0) return 3;
+    if (params->width == 0 || params->height == 0) return 2;
     std::vector<uint32_t> pixels;
     if (pixel_list) {
+        // Every listed pixel must lie in the W*H image the buffers hold.
+        const uint64_t npix = (uint64_t)params->width * params->height;
+        for (uint32_t i = 0; i < pixel_list_count; ++i)
+            if (pixel_list[i] >= npix) return 4;
         pixels.assign(pixel_list, pixel_list + pixel_list_count);
     } else {
         for (uint32_t y = params->tile_y; y < params->tile_y + params->tile_h && y < params->height; ++y)

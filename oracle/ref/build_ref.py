@@ -16,7 +16,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
-SHADERS = os.path.join("/root/reference", "Sources", "DenrimRendererKit", "Resources", "Shaders")
+# The reference checkout: DENRIM_REFERENCE, else its location in the build container.
+REFERENCE = os.environ.get("DENRIM_REFERENCE", "/root/reference")
+SHADERS = os.path.join(REFERENCE, "Sources", "DenrimRendererKit", "Resources", "Shaders")
 # (reference shader, kernels kept, generated file)
 UNITS = (("PathTrace.metal", ("pathTraceKernel", "flatPreviewKernel", "interactiveMaterialKernel"), "pathtrace_ref.cpp"),
          ("Denoise.metal", ("simpleSpatialDenoiseKernel", "packSVGFDepthNormalKernel", "copySVGFOutputKernel"),

@@ -54,7 +54,9 @@ uint32_t ref_sdf_counter_count(void) { return 13u; }
 // RGBA32F accumulation texture (W*H*4 floats), `aov` six W*H*4 float planes
 // (depth, normal, albedo, material ID, object ID, motion vector), `sdf_counters`
 // 13 counters or null (null disables sdfTraversalStatsEnabled).  `threads` <= 0
-// uses every hardware thread.  Returns 0 on success.
+// uses every hardware thread.  Returns 0 on success, 1 for a bad argument, 2
+// for an empty image and 4 when a listed pixel lies outside the image
+// (nothing is written then).
 // `quality` is RenderSettings.shaderQualityLevel: 0 preview, 1 interactive,
 // 2 final (RenderSettings.swift:96-105).
 int ref_render_quality(int quality, const dk_scene* scene, const oracle_params* p, uint32_t sample_begin,
@@ -105,8 +107,14 @@ int ref_render_quality(int quality, const dk_scene* scene, const oracle_params* 
     std::vector<atomic_uint> counters(13);
     for (auto& c : counters) c.value.store(0);
 
+    if (W == 0 || H == 0) return 2;
     std::vector<uint32_t> pixels;
     if (pixel_list) {
+        // Every listed pixel must lie in the W*H image.  (The kernels skip a
+        // pixel outside the tile or the image themselves.)
+        const uint64_t npix = (uint64_t)W * H;
+        for (uint32_t i = 0; i < pixel_list_count; ++i)
+            if (pixel_list[i] >= npix) return 4;
         pixels.assign(pixel_list, pixel_list + pixel_list_count);
     } else {
         for (uint32_t y = 0; y < p->tile_h; ++y)

@@ -81,3 +81,22 @@ def test_noalloc_rejects_maps_beyond_the_scratch(dk_lib):
     assert rc == 6  # DK_ERROR_INVALID_ARGUMENT, checked before any device work
     assert count.value == 0
     assert b"DK_ENV_NOALLOC_MAX_TEXELS" in lib.dk_last_error_message()
+
+
+def test_noalloc_rejects_host_and_misaligned_pointers(dk_lib):
+    # Both are refused on the host before any device work: a kernel never
+    # sees such a pointer.
+    torch = pytest.importorskip("torch")
+    lib = library.load()
+    library.check(lib.dk_device_open(0))
+    dev = torch.zeros(64, dtype=torch.float32, device="cuda")
+    host = np.zeros(64, np.float32)
+    count = C.c_uint32(7)
+    cases = [(dev.data_ptr() + 4, dev.data_ptr()),      # texels not 16-byte aligned
+             (dev.data_ptr(), dev.data_ptr() + 4),      # table not 8-byte aligned
+             (host.ctypes.data, dev.data_ptr()),        # texels in host memory
+             (dev.data_ptr(), host.ctypes.data)]        # table in host memory
+    for px, out in cases:
+        rc = lib.dk_build_environment_samples_noalloc(px, 2, 2, 1.0, 0.0, out, C.byref(count), None)
+        assert rc == 6 and count.value == 0
+    assert np.all(host == 0)
