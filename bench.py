@@ -64,6 +64,10 @@ def parse():
                     help="large: the headline path-tracing step (default); serving: the material-preview job "
                          "stream through the serving loop; denoise: U-Net training and 1080p inference")
     ap.add_argument("--jobs", type=int, default=1024, help="serving: jobs taken from the 4096-job stream")
+    ap.add_argument("--serving-jobs", type=int, default=256,
+                    help="jobs of the serving stream measured in the default line's `serving` object")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the default line's sdf / serving / serving_with_denoising objects")
     return ap.parse_args()
 
 
@@ -184,6 +188,17 @@ def profile_traffic(kernel: str):
         return None
     m = re.search(r"traffic_bytes_per_frame:\s*([0-9.eE+]+)", open(path).read())
     return float(m.group(1)) if m else None
+
+
+def profile_stage_figures():
+    """Per-frame L2 and DRAM bytes and issue activity of the traversal stages
+    from the committed ncu summary (profiles/traversal_stages_spheres_large.md:
+    lines `<figure>.<stage>: value`), scaled there from a small-case capture."""
+    path = os.path.join(ROOT, "profiles", "traversal_stages_spheres_large.md")
+    if not os.path.exists(path):
+        return {}
+    return {m.group(1): float(m.group(2))
+            for m in re.finditer(r"^([a-z0-9_]+\.k_[a-z_]+):\s*([0-9.eE+-]+)\s*$", open(path).read(), re.M)}
 
 
 # Algorithmic bytes per unit of the reference algorithm (reference layouts):
@@ -420,6 +435,33 @@ def run_gb300(args, rank, world, local):
                 "algorithmic_bytes_per_step": {k: float(v) for k, v in per_frame.items()},
                 "kernel_ms_per_step": kernel_ms,
                 "per_path": {k: float(v) / paths for k, v in counters.items() if k != "paths"}}
+        # Per stage: the traversal stages run from L2 (nodes + triangle slots,
+        # 109 MB, stay resident), so their roofline is L2 bytes moved against
+        # the measured L2 read bandwidth; shading's is the HBM one above.
+        figs = profile_stage_figures()
+        l2_peak = library.probe_bandwidth(64 << 20, 50)
+        hbm_probe = library.probe_bandwidth(4 << 30, 3)
+        stages = {"k_shade": {"bound": "hbm", "achieved": achieved if dom == "k_shade" else
+                              per_frame["k_shade"] / (kernel_ms["k_shade"] * 1e-3) / 1e9, "peak": peak,
+                              "unit": "GB/s", "traffic": traffic, "bytes": "algorithmic (reference layouts)"}}
+        stages["k_shade"]["frac"] = stages["k_shade"]["achieved"] / peak
+        for name, kernels in (("k_extend", ("k_extend",)), ("k_shadow", ("k_shadow_rays", "k_shadow_layers"))):
+            l2 = [figs.get(f"l2_bytes_per_frame.{k}") for k in kernels]
+            if any(v is None for v in l2):
+                stages[name] = {"bound": "l2", "achieved": None, "note": "no ncu summary of this stage"}
+                continue
+            a = sum(l2) / (kernel_ms[name] * 1e-3) / 1e9
+            stages[name] = {"bound": "l2", "achieved": a, "peak": l2_peak, "unit": "GB/s", "frac": a / l2_peak,
+                            "l2_bytes_per_frame": sum(l2),
+                            "dram_bytes_per_frame": sum(figs.get(f"dram_bytes_per_frame.{k}", 0.0) for k in kernels),
+                            "issue_active_pct": {k: figs.get(f"issue_active_pct.{k}") for k in kernels},
+                            "algorithmic_bytes_per_frame": float(per_frame[name]),
+                            "bytes": "L2 bytes moved (ncu lts__t_bytes, small case scaled to the frame)"}
+        roof["stages"] = stages
+        roof["measured_l2_read_gbs"] = l2_peak
+        roof["measured_hbm_read_gbs"] = hbm_probe
+        roof["stage_peaks"] = ("k_shade against MEASURED_PEAKS.json hbm_gbs; the traversal stages against the L2 "
+                               "read bandwidth measured live (dk_probe_bandwidth, 64 MiB buffer)")
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -427,10 +469,232 @@ def run_gb300(args, rank, world, local):
             "roofline": roof, "cpu_baseline": cpu, "wall_s_timed": wall,
             "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
             "beauty_mean": float(beauty[..., :3].mean())}
+    if not args.no_extras:
+        # The other configurations, measured after the headline's timed region.
+        line["sdf"] = sdf_measure(args, flush)
+        res, cfg = serving_measure(args.serving_jobs, modes=("packed", "one_job_per_wave", "session_per_job"))
+        line["serving"] = {**cfg, "modes": res,
+                           "images_per_s_vs_one_job_per_wave": res["packed"]["images_per_s"]
+                           / res["one_job_per_wave"]["images_per_s"],
+                           "images_per_s_vs_session_per_job": res["packed"]["images_per_s"]
+                           / res["session_per_job"]["images_per_s"]}
+        line["serving_with_denoising"] = serving_with_denoising_measure()
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+def sdf_measure(args, flush, steps=3, warmup=2):
+    """The sparse-SDF configuration (32 smooth-union spheres in a 768^3 grid of
+    8^3 bricks, ~3 % kept, FP16 distances; 1024^2 x 16 spp): device-timed
+    Mpaths/s, the volume pass's roofline against HBM (brick-sample, cell and
+    descriptor bytes of the reference algorithm, counted by the CPU oracle on
+    every 16th pixel in x and y and scaled), and the same frame with FP32
+    distances for comparison."""
+    from denrimrendererkit_gb300 import DenrimRenderer, RenderOutput, compile_scene, scenes
+    renderer = DenrimRenderer(0)
+    out = {}
+    images = {}
+    for fmt in ("fp16", "fp32"):
+        wl = scenes.sdf_spheres(fp16=(fmt == "fp16"))
+        build = compile_scene(wl.scene)
+        paths = wl.settings.width * wl.settings.height * wl.samples
+        with renderer.make_session(wl.scene, wl.settings, build=build) as s:
+            for _ in range(warmup):
+                s.render(wl.samples)
+                flush_l2(flush)
+            dev = ext = shade = shadow = 0.0
+            for _ in range(steps):
+                s.render(wl.samples)
+                st = s.stats()
+                dev += st.last_render_ms
+                ext += st.last_extend_ms
+                shade += st.last_shade_ms
+                shadow += st.last_shadow_ms
+                flush_l2(flush)
+            images[fmt] = (s.pixels(RenderOutput.BEAUTY), s.pixels(RenderOutput.DEPTH))
+            out[fmt] = {"mpaths_s": paths * steps / (dev * 1e3), "ms_per_frame": dev / steps,
+                        "extend_ms": ext / steps, "shade_ms": shade / steps, "shadow_ms": shadow / steps,
+                        "bricks": int(len(build.volume_bricks)), "samples": int(len(build.volume_brick_samples)),
+                        "distance_bytes": int(len(build.volume_brick_samples)) * (2 if fmt == "fp16" else 4)}
+        if fmt == "fp16":
+            wl16, build16 = wl, build
+    # FP16 storage against FP32: the same frame (same RNG streams).
+    b16, b32 = images["fp16"][0][..., :3].astype(np.float64), images["fp32"][0][..., :3].astype(np.float64)
+    d16, d32 = images["fp16"][1][..., 0], images["fp32"][1][..., 0]
+    out["fp16_vs_fp32"] = {"beauty_relative_rmse": float(np.sqrt(((b16 - b32) ** 2).mean()) / b32.mean()),
+                           "depth_pixels_differing": int((d16 != d32).sum()),
+                           "depth_max_relative_difference": float(np.max(np.abs(d16 - d32) / np.maximum(d32, 1e-6)))}
+    roof = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        orc.build()
+        w, h = wl16.settings.width, wl16.settings.height
+        ys, xs = np.meshgrid(np.arange(0, h, 16), np.arange(0, w, 16), indexing="ij")
+        pixels = (ys * w + xs).reshape(-1).astype(np.uint32)
+        r = orc.OracleRender(build16, wl16.settings, wl16.scene.camera)
+        r.render(wl16.samples, pixel_list=pixels, threads=os.cpu_count() or 1)
+        c = r.counter_dict()
+        sample_paths = len(pixels) * wl16.samples
+        scale = w * h * wl16.samples / sample_paths
+        vol_bytes = (16 * c["brick_samples"] + 4 * (c["grid_cells"] + c["macro_skips"]) + 128 * c["brick_tests"]) * scale
+        peak, kind = measured_peaks()
+        ext_ms = out["fp16"]["extend_ms"]
+        achieved = vol_bytes / (ext_ms * 1e-3) / 1e9
+        roof = {"kernel": "k_extend_volume (volume pass of the extend stage)", "bound": "hbm", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured" else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_frame": vol_bytes,
+                "per_path": {k: float(v) / sample_paths for k, v in c.items()
+                             if k in ("grid_cells", "macro_skips", "brick_tests", "brick_marches", "march_steps",
+                                      "brick_hits", "brick_samples")},
+                "units": "16 B per brick sample read, 4 B per grid or macro cell, 128 B per brick descriptor "
+                         "(the reference's layouts), counted by the oracle on every 16th pixel in x and y, scaled"}
+    return {"workload": "sdf-spheres 768^3, 8^3 bricks (26.8 K kept, 3 %), 1024x1024 x 16 spp, 8 bounces",
+            "value": out["fp16"]["mpaths_s"], "unit": METRIC, "fp16": out["fp16"], "fp32": out["fp32"],
+            "fp16_vs_fp32": out["fp16_vs_fp32"], "roofline": roof,
+            "note": "value: FP16 distance storage (the configuration's); fp32 is the same scene with FP32 distances"}
+
+
+def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, train_steps=2500):
+    """The benchmark spec's comparison at its stated error: requests (`views`
+    camera views of each of `n_scenes` held-out small-scene variants, all
+    resident in one render server) served until each image's estimated
+    relative RMSE (linear RGB, over the image mean) is at most `target`:
+
+    * denoised: two independent halves rendered per request, the residual
+      U-Net over A, B and F, the reference-free estimate of dF; a request over
+      the target doubles its samples (the fallback to more spp) until dF -- or
+      the plain render -- meets it (`denoiser.serve_to_error_target`);
+    * plain, batched: the same loop without the network (F returns once its
+      own estimate meets the target);
+    * plain, one session per request: the reference's way -- a RenderSession
+      per request rendering two halves progressively, doubling until the
+      estimate meets the target.
+    The true error of the returned images is measured against 16384-spp
+    renders (their own noise, from their two halves, subtracted)."""
+    import dataclasses as dc
+    import math
+    import torch
+    from denrimrendererkit_gb300 import DenrimRenderer, RenderOutput, compile_scene, scenes
+    from denrimrendererkit_gb300.denoiser import (TrainingSet, UNet, average_planes, display, display_relative_rmse,
+                                                  estimate_errors, relative_rmse, render_pairs, serve_to_error_target,
+                                                  train)
+    from denrimrendererkit_gb300.renderer import RenderSession
+    from denrimrendererkit_gb300.scene import Camera
+    from denrimrendererkit_gb300.serving import RenderServer, ServerConfig
+    r = DenrimRenderer(0)
+    t0 = time.perf_counter()
+    parts = [render_pairs(range(100 + 12 * i, 112 + 12 * i), size=size, noisy_spp=spp, target_spp=2048)
+             for i, spp in enumerate((16, 64, 256, 1024))]
+    data = TrainingSet(*[torch.cat([getattr(p, f) for p in parts])
+                         for f in ("beauty", "albedo", "normal", "depth", "target")])
+    render_s = time.perf_counter() - t0
+    net = UNet(seed=2)
+    t1 = time.perf_counter()
+    train(net, data, steps=train_steps, batch=16, crop=128, lr=1e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    del data, parts
+    # requests: views on a +-6 degree orbit of each held-out variant
+    wls = [scenes.cornell_variant(3000 + k, size, size) for k in range(n_scenes)]
+    builds = [compile_scene(wl.scene) for wl in wls]
+    requests = []
+    for si, wl in enumerate(wls):
+        cam = wl.scene.camera
+        eye = np.subtract(cam.origin, cam.target)
+        for i in range(views):
+            a = math.radians(-6.0 + 12.0 * i / max(views - 1, 1))
+            c, sn = math.cos(a), math.sin(a)
+            e = (eye[0] * c + eye[2] * sn, eye[1], -eye[0] * sn + eye[2] * c)
+            cv = Camera(tuple(np.add(cam.target, e)), cam.target, up=cam.up,
+                        vertical_field_of_view_degrees=cam.vertical_field_of_view_degrees)
+            requests.append((wl.settings, cv, None, si))
+    cfg = ServerConfig(wave_paths=1 << 24, max_jobs_per_wave=512, samples_per_wave=256)
+    with RenderServer(builds[0], cfg) as srv:
+        for b in builds[1:]:
+            srv.add_scene(b)
+        serve_to_error_target(srv, net, requests[:4], size, size, target=target)  # warm-up
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        den = serve_to_error_target(srv, net, requests, size, size, target=target, start_spp=16)
+        torch.cuda.synchronize()
+        den_s = time.perf_counter() - t
+        t = time.perf_counter()
+        plain = serve_to_error_target(srv, net, requests, size, size, target=target, start_spp=16, denoise=False)
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - t
+    # plain, one session per request (two half sessions, doubling)
+    t = time.perf_counter()
+    sess_spp = []
+    for settings, cv, _, si in requests:
+        st = [dc.replace(settings, frame_seed=(settings.frame_seed ^ k) & 0x7FFFFFFF) for k in (0x3A1, 0x3A2)]
+        ss = [RenderSession(builds[si], x, cv) for x in st]
+        n = 8
+        for s in ss:
+            s.render(n)
+        while True:
+            a, b = (torch.from_numpy(s.pixels(RenderOutput.BEAUTY)).cuda() for s in ss)
+            f = torch.empty_like(a)
+            average_planes(a, b, f)
+            e = estimate_errors(a, b, f, a, b, f, display=True)[0]
+            if e.plain <= target or 2 * n >= 8192:
+                break
+            for s in ss:
+                s.render(n)
+            n *= 2
+        sess_spp.append(2 * n)
+        for s in ss:
+            s.close()
+    torch.cuda.synchronize()
+    sess_s = time.perf_counter() - t
+    # true error of the returned images: one view per scene, against 16384-spp renders
+    true_den, true_plain, lin_den, lin_plain = [], [], [], []
+    for si in range(n_scenes):
+        k = si * views
+        settings, cv, _, _ = requests[k]
+        halves = []
+        for x in (0x7001, 0x7002):
+            with RenderSession(builds[si], dc.replace(settings, frame_seed=(settings.frame_seed ^ x) & 0x7FFFFFFF),
+                               cv) as s:
+                s.render(8192)
+                halves.append(torch.from_numpy(s.pixels(RenderOutput.BEAUTY)).cuda())
+        ref = torch.empty_like(halves[0])
+        average_planes(halves[0], halves[1], ref)
+        m = float(ref[..., :3].double().mean())
+        ref_var = float(((halves[0][..., :3] - halves[1][..., :3]).double() ** 2).mean() / 4) / (m * m)
+        md = float(display(ref).mean())
+        ref_var_d = float(((display(halves[0]) - display(halves[1])) ** 2).mean() / 4) / (md * md)
+        for res, out, lin in ((den[k], true_den, lin_den), (plain[k], true_plain, lin_plain)):
+            e = display_relative_rmse(res.image, ref)
+            out.append(math.sqrt(max(e * e - ref_var_d, 0.0)))
+            e = relative_rmse(res.image, ref)
+            lin.append(math.sqrt(max(e * e - ref_var, 0.0)))
+    n = len(requests)
+    return {"target_relative_rmse": target, "requests": n,
+            "image": f"{size}x{size} views ({views} per scene) of {n_scenes} held-out small-scene variants, "
+                     "resident together in one render server",
+            "images_per_s_denoised": n / den_s, "images_per_s_plain_batched": n / plain_s,
+            "images_per_s_plain_session_per_request": n / sess_s,
+            "ratio_vs_plain_session_per_request": sess_s / den_s, "ratio_vs_plain_batched": plain_s / den_s,
+            "denoised_returned": sum(1 for x in den if x.denoised),
+            "fallback_to_plain": sum(1 for x in den if not x.denoised),
+            "spp_denoised_mean": float(np.mean([x.spp for x in den])),
+            "spp_plain_batched_mean": float(np.mean([x.spp for x in plain])),
+            "spp_plain_session_mean": float(np.mean(sess_spp)),
+            "estimated_error_denoised_mean": float(np.mean([x.estimate.denoised if x.denoised else x.estimate.plain
+                                                            for x in den])),
+            "error_domain": "relative RMSE of the displayed image (the reference's PNG tone curve, "
+                            "PNGWriter.swift:182-188, before quantisation) over the mean displayed value",
+            "true_error_denoised": true_den, "true_error_plain_batched": true_plain,
+            "true_linear_error_denoised": lin_den, "true_linear_error_plain_batched": lin_plain,
+            "true_error_note": "one view per scene against 16384-spp renders, the reference's own noise subtracted; "
+                               "the high-spp GPU render stands in for the FP64 oracle (equal within 1e-6 relative "
+                               "RMSE on the small configuration)",
+            "train_steps": train_steps, "train_s": train_s, "training_pairs_render_s": render_s,
+            "note": "per request: two independent halves, the residual U-Net over A, B and F, the reference-free "
+                    "estimate; above the target the request doubles its samples (fallback to more spp)"}
 
 
 def percentile(values, q):
@@ -441,21 +705,22 @@ def percentile(values, q):
     return v[k]
 
 
-def run_serving(args, rank):
+def serving_measure(n_jobs, modes=("packed", "packed_fifo", "one_job_per_wave", "session_per_job")):
     """Material-preview jobs arriving as a Poisson stream (200/s) through the
     serving loop: waves packing all admitted jobs (oldest first, then fewest
-    remaining paths; and in admission order), and one job per wave (per-job
-    plain launches over the same resident scene)."""
-    if rank != 0:
-        return
-    from denrimrendererkit_gb300 import DenrimRenderer, abi, compile_scene, scenes
+    remaining paths; and in admission order), one job per wave (per-job
+    launches over the same resident scene), and one render session per job
+    (the reference's way: RenderSession per request, the scene uploaded with
+    each).  Returns (results per mode, workload description)."""
+    from denrimrendererkit_gb300 import DenrimRenderer, RenderOutput, abi, compile_scene, scenes
     from denrimrendererkit_gb300.presets import PRESETS
-    from denrimrendererkit_gb300.renderer import RenderQuality, RenderSettings
+    from denrimrendererkit_gb300.renderer import RenderQuality, RenderSettings, RenderSession
     from denrimrendererkit_gb300.serving import RenderServer, ServerConfig
+    import dataclasses
     DenrimRenderer(0)
     scene = scenes.material_preview()
     build = compile_scene(scene)
-    jobs = scenes.serving_jobs()[:args.jobs]
+    jobs = scenes.serving_jobs()[:n_jobs]
     tables = {}
     for j in jobs:
         if j.preset not in tables:
@@ -463,12 +728,42 @@ def run_serving(args, rank):
             t[1] = PRESETS[j.preset].gpu_material()
             tables[j.preset] = t
     paths = sum(j.width * j.height * j.samples for j in jobs)
+
+    def settings_of(j):
+        return RenderSettings(width=j.width, height=j.height, max_bounces=8, quality=RenderQuality.FINAL,
+                              frame_seed=1)
+
     results = {}
-    for mode, per_wave, policy in (("packed", 512, 1), ("packed_fifo", 512, 0), ("one_job_per_wave", 1, 0)):
+    for mode in modes:
+        done = {}
+        t0 = time.perf_counter()
+        if mode == "session_per_job":
+            # Jobs in arrival order, each its own session (scene upload, traversal
+            # build, render, beauty readback); latency from its arrival.
+            backlog = 0
+            for k, j in enumerate(jobs):
+                delay = j.arrival_s - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                b = dataclasses.replace(build, materials=tables[j.preset])
+                s = RenderSession(b, settings_of(j), scene.camera)
+                s.render(j.samples)
+                s.pixels(RenderOutput.BEAUTY)
+                s.close()
+                done[k] = (time.perf_counter() - t0 - j.arrival_s) * 1e3
+                backlog = max(backlog, sum(1 for x in jobs if x.arrival_s <= time.perf_counter() - t0) - len(done))
+            wall = time.perf_counter() - t0
+            lat = [done[k] for k in range(len(jobs))]
+            small = [done[k] for k in range(len(jobs)) if jobs[k].width <= 96]
+            results[mode] = {"wall_s": wall, "images_per_s": len(jobs) / wall, "mpaths_s": paths / wall / 1e6,
+                             "p50_ms": percentile(lat, 50), "p99_ms": percentile(lat, 99),
+                             "p50_ms_96px_jobs": percentile(small, 50), "p99_ms_96px_jobs": percentile(small, 99),
+                             "max_backlog_jobs": backlog}
+            continue
+        per_wave, policy = {"packed": (512, 1), "packed_fifo": (512, 0), "one_job_per_wave": (1, 0)}[mode]
         with RenderServer(build, ServerConfig(max_jobs_per_wave=per_wave, policy=policy)) as srv:
             srv.start()
             ids = []
-            done = {}
             stop = threading.Event()
 
             def collect():
@@ -488,15 +783,12 @@ def run_serving(args, rank):
 
             th = threading.Thread(target=collect)
             th.start()
-            t0 = time.perf_counter()
             backlog = 0
             for j in jobs:
                 delay = j.arrival_s - (time.perf_counter() - t0)
                 if delay > 0:
                     time.sleep(delay)
-                st = RenderSettings(width=j.width, height=j.height, max_bounces=8, quality=RenderQuality.FINAL,
-                                    frame_seed=1)
-                ids.append(srv.submit(st, scene.camera, j.samples, tables[j.preset]))
+                ids.append(srv.submit(settings_of(j), scene.camera, j.samples, tables[j.preset]))
                 backlog = max(backlog, len(ids) - len(done))
             th.join()
             wall = time.perf_counter() - t0
@@ -510,16 +802,26 @@ def run_serving(args, rank):
                          "max_backlog_jobs": backlog, "waves": stats["waves"],
                          "mean_jobs_per_wave": stats["mean_jobs_in_wave"], "busy_s": stats["busy_ms"] / 1e3,
                          "gpu_launches": stats["kernel_launches"], "budget_peak_gb": stats["budget_peak_bytes"] / 1e9}
+    workload = (f"material-preview stream: first {len(jobs)} of 4096 seeded jobs, Poisson 200/s, res "
+                "{96,256,512,1024}^2 (50/30/15/5 %), spp {16,64,256}, 7 preset families, icosphere on a plane "
+                "under the 2048x1024 HDRI")
+    return results, {"workload": workload, "paths": paths,
+                     "offered_load_gpaths_s": paths / max(jobs[-1].arrival_s, 1e-9) / 1e9}
+
+
+def run_serving(args, rank):
+    """The serving line: the material-preview job stream through the serving
+    loop (see serving_measure)."""
+    if rank != 0:
+        return
+    results, cfg = serving_measure(args.jobs)
     line = {"metric": "serving images/s", "value": results["packed"]["images_per_s"], "unit": "images/s",
             "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": f"material-preview stream: first {len(jobs)} of 4096 seeded jobs, Poisson 200/s, "
-                                   "res {96,256,512,1024}^2 (50/30/15/5 %), spp {16,64,256}, 7 preset families, "
-                                   "icosphere on a plane under the 2048x1024 HDRI",
-                       "paths": paths, "offered_load_gpaths_s": paths / max(jobs[-1].arrival_s, 1e-9) / 1e9},
-            "serving": results,
+            "data": "synthetic", "config": cfg, "serving": results,
             "images_per_s_vs_one_job_per_wave": results["packed"]["images_per_s"]
-            / results["one_job_per_wave"]["images_per_s"]}
+            / results["one_job_per_wave"]["images_per_s"],
+            "images_per_s_vs_session_per_job": results["packed"]["images_per_s"]
+            / results["session_per_job"]["images_per_s"]}
     print(json.dumps(line), flush=True)
 
 

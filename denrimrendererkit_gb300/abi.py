@@ -122,7 +122,7 @@ class Settings(C.Structure):
         ("frame_seed", C.c_uint32), ("denoiser_enabled", C.c_uint32),
         ("collects_traversal_stats", C.c_uint32),
         ("camera", Camera), ("previous_camera", Camera),
-        ("max_samples_per_launch", C.c_uint32), ("reserved", C.c_uint32),
+        ("max_samples_per_launch", C.c_uint32), ("triangle_test", C.c_uint32),
     ]
 
 
@@ -167,14 +167,15 @@ EXPORTED_SYMBOLS = (
     "dk_session_destroy", "dk_last_error_message", "dk_build_bvh", "dk_build_lights",
     "dk_build_environment_samples", "dk_build_environment_samples_noalloc", "dk_build_sparse_sphere_volume",
     "dk_bake_sparse_sphere_volume",
-    "dk_sparse_volume_view", "dk_sparse_volume_destroy", "dk_version",
-    "dk_server_create", "dk_server_submit", "dk_server_step", "dk_server_start", "dk_server_stop",
+    "dk_sparse_volume_view", "dk_sparse_volume_destroy", "dk_version", "dk_probe_bandwidth",
+    "dk_server_create", "dk_server_add_scene", "dk_server_submit", "dk_server_step", "dk_server_start", "dk_server_stop",
     "dk_server_wait", "dk_server_job_status", "dk_server_read_output", "dk_server_copy_output", "dk_server_copy_outputs", "dk_server_release",
-    "dk_server_get_stats", "dk_server_destroy", "dk_denoise_spatial", "dk_svgf_create", "dk_svgf_reset",
+    "dk_server_get_stats", "dk_server_destroy", "dk_denoise_spatial", "dk_denoise_error_terms", "dk_average_planes", "dk_svgf_create", "dk_svgf_reset",
     "dk_svgf_denoise", "dk_svgf_read_state", "dk_svgf_destroy", "dk_svgf_pack_depth_normal", "dk_svgf_copy_output",
     "dk_unet_conv3x3", "dk_unet_conv3x3_wgrad", "dk_unet_relu_backward", "dk_unet_bias_grad", "dk_unet_avgpool2",
     "dk_unet_avgpool2_backward", "dk_unet_upsample2", "dk_unet_upsample2_backward", "dk_unet_copy_channels",
-    "dk_unet_pack_input", "dk_unet_l1_loss", "dk_unet_unpack_output", "dk_unet_adam", "dk_unet_weights_to_bf16",
+    "dk_unet_pack_input", "dk_unet_l1_loss", "dk_unet_unpack_output", "dk_unet_l1_loss_residual",
+    "dk_unet_unpack_output_residual", "dk_unet_adam", "dk_unet_weights_to_bf16",
     "dk_unet_set_conv_path", "dk_unet_error",
 )
 
@@ -195,7 +196,7 @@ class ServerConfig(C.Structure):
 class JobDesc(C.Structure):
     """dk_job_desc."""
     _fields_ = [("settings", Settings), ("samples", C.c_uint32), ("material_count", C.c_uint32),
-                ("materials", C.c_void_p)]
+                ("materials", C.c_void_p), ("scene", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class JobStatus(C.Structure):
@@ -226,6 +227,6 @@ class SparseVolumeSettings(C.Structure):
     """dk_sparse_volume_settings."""
     _fields_ = [("resolution", C.c_uint32 * 3), ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
                 ("brick_size", C.c_uint32 * 3), ("narrow_band", C.c_float), ("volume_material", C.c_uint32),
-                ("object_id", C.c_uint32), ("primitive_id", C.c_uint32)]
+                ("object_id", C.c_uint32), ("primitive_id", C.c_uint32), ("fp16_distances", C.c_uint32)]
 
 assert C.sizeof(Camera) == 80

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "libdenrim_cuda.so")
-SOURCES = ("dk_kernels.cu", "dk_host.cu", "dk_bvh.cu", "dk_sdf.cu", "dk_noalloc.cu", "dk_server.cu", "dk_denoise.cu", "dk_unet.cu", "dk_image.cu", "dk_svgf.cu")
+SOURCES = ("dk_kernels.cu", "dk_host.cu", "dk_bvh.cu", "dk_sdf.cu", "dk_noalloc.cu", "dk_server.cu", "dk_denoise.cu", "dk_unet.cu", "dk_image.cu", "dk_svgf.cu", "dk_probe.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 
 

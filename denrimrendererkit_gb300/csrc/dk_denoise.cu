@@ -5,6 +5,7 @@
 // ... the way SimpleSpatialDenoiser.encode dispatches it
 // (Sources/DenrimRendererKit/Denoising/Denoiser.swift:103-160).  It is the
 // comparator of the learned denoiser.
+#include <algorithm>
 #include <cstdint>
 
 #include "dk_host.h"
@@ -90,9 +91,108 @@ __global__ void __launch_bounds__(256) k_spatial_denoise(const float4* __restric
     out[idx] = make_float4(cc.x + (d.x - cc.x) * 0.85f, cc.y + (d.y - cc.y) * 0.85f, cc.z + (d.z - cc.z) * 0.85f, cb.w);
 }
 
+// Per-image sums behind the learned denoiser's error estimate (two
+// independent half-sample renders A and B of an image, their full render F
+// and the three denoised images): over the RGB channels of every pixel,
+// (dA - dB)^2, (A - B)^2, (F - dF)^2, dF and F.  One grid row per image;
+// FP64 partial sums per block, one atomic add per block and term.
+constexpr uint32_t kErrTerms = 5;
+
+// The reference's PNG tone curve before 8-bit quantisation
+// (PNGWriter.tonemap, Sources/DenrimRendererKit/Image/PNGWriter.swift:182-188):
+// exposure 0.8, the ACES fit, clamp to [0, 1], gamma 1/2.2.
+__device__ __forceinline__ float displayValue(float v) {
+    const float x = fmaxf(v, 0.0f) * 0.8f;
+    const float m = (x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f);
+    return powf(fminf(fmaxf(m, 0.0f), 1.0f), 1.0f / 2.2f);
+}
+
+__device__ __forceinline__ float4 inDomain(float4 v, uint32_t display) {
+    if (!display) return v;
+    return make_float4(displayValue(v.x), displayValue(v.y), displayValue(v.z), v.w);
+}
+
+__global__ void __launch_bounds__(256) k_error_terms(const float4* __restrict__ a, const float4* __restrict__ b,
+                                                     const float4* __restrict__ f, const float4* __restrict__ da,
+                                                     const float4* __restrict__ db, const float4* __restrict__ df,
+                                                     uint32_t pixels, uint32_t display, double* __restrict__ terms) {
+    const size_t base = (size_t)blockIdx.y * pixels;
+    double acc[kErrTerms] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
+        const size_t k = base + i;
+        const float4 va = inDomain(a[k], display), vb = inDomain(b[k], display), vf = inDomain(f[k], display);
+        const float4 vda = inDomain(da[k], display), vdb = inDomain(db[k], display), vdf = inDomain(df[k], display);
+        const double dd[3] = {(double)vda.x - vdb.x, (double)vda.y - vdb.y, (double)vda.z - vdb.z};
+        const double nn[3] = {(double)va.x - vb.x, (double)va.y - vb.y, (double)va.z - vb.z};
+        const double fd[3] = {(double)vf.x - vdf.x, (double)vf.y - vdf.y, (double)vf.z - vdf.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            acc[0] += dd[c] * dd[c];
+            acc[1] += nn[c] * nn[c];
+            acc[2] += fd[c] * fd[c];
+        }
+        acc[3] += (double)vdf.x + vdf.y + vdf.z;
+        acc[4] += (double)vf.x + vf.y + vf.z;
+    }
+    __shared__ double part[kErrTerms][8];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (uint32_t t = 0; t < kErrTerms; ++t) {
+        double v = acc[t];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) part[t][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kErrTerms) {
+        double v = 0.0;
+        for (uint32_t w = 0; w < blockDim.x / 32u; ++w) v += part[threadIdx.x][w];
+        atomicAdd(terms + (size_t)blockIdx.y * kErrTerms + threadIdx.x, v);
+    }
+}
+
+// out = (a + b) / 2 per RGBA texel: the full render of two equal-sample
+// halves (also a doubling step of a progressive render: the previous full
+// render and a new render of as many samples).
+__global__ void __launch_bounds__(256) k_average_planes(const float4* a, const float4* b, float4* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 x = a[i], y = b[i];
+        out[i] = make_float4(0.5f * (x.x + y.x), 0.5f * (x.y + y.y), 0.5f * (x.z + y.z), 0.5f * (x.w + y.w));
+    }
+}
+
 }  // namespace
 
 }  // namespace dk
+
+extern "C" int dk_average_planes(const float* a, const float* b, float* out, size_t texels, void* stream) {
+    if (!a || !b || !out) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_average_planes: null argument");
+    if (texels == 0) return DK_OK;
+    const unsigned grid = (unsigned)std::min<size_t>((texels + 255u) / 256u, 152u * 16u);
+    dk::k_average_planes<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(b), reinterpret_cast<float4*>(out), texels);
+    DK_CUDA(cudaGetLastError(), "average planes launch");
+    return DK_OK;
+}
+
+extern "C" int dk_denoise_error_terms(const float* half_a, const float* half_b, const float* full,
+                                      const float* denoised_a, const float* denoised_b, const float* denoised_full,
+                                      uint32_t pixels, uint32_t images, uint32_t display, double* terms,
+                                      void* stream) {
+    if (!half_a || !half_b || !full || !denoised_a || !denoised_b || !denoised_full || !terms)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_denoise_error_terms: null argument");
+    if (images > 65535u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_denoise_error_terms: at most 65535 images");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DK_CUDA(cudaMemsetAsync(terms, 0, (size_t)images * dk::kErrTerms * sizeof(double), st), "error terms clear");
+    if (pixels == 0 || images == 0) return DK_OK;
+    const uint32_t blocks = std::min<uint32_t>((pixels + 255u) / 256u, 64u);
+    dk::k_error_terms<<<dim3(blocks, images), 256, 0, st>>>(
+        reinterpret_cast<const float4*>(half_a), reinterpret_cast<const float4*>(half_b),
+        reinterpret_cast<const float4*>(full), reinterpret_cast<const float4*>(denoised_a),
+        reinterpret_cast<const float4*>(denoised_b), reinterpret_cast<const float4*>(denoised_full), pixels,
+        display ? 1u : 0u, terms);
+    DK_CUDA(cudaGetLastError(), "error terms launch");
+    return DK_OK;
+}
 
 extern "C" int dk_denoise_spatial(const float* beauty, const float* depth, const float* normal, const float* albedo,
                                   float* out, float* scratch, uint32_t width, uint32_t height,

@@ -52,6 +52,32 @@ __device__ __forceinline__ bool childBox(float bx0, float bx1, float by0, float 
     return tn <= tf;
 }
 
+// The slab test of the watertight mode (after Ize, "Robust BVH Ray
+// Traversal", JCGT 2(2), 2013): a ray that lies in a slab's boundary plane
+// (0 x inf = NaN) counts as inside the slab, and the far distance is widened
+// by 1 + 2 gamma(3) so that rounding never culls a box the ray touches.  The
+// reference's test above drops such boxes, so a ray along a grid plane of a
+// tessellated surface can miss every triangle around it whatever the
+// triangle test.
+__device__ __forceinline__ float nanTo(float x, float v) { return x != x ? v : x; }
+
+__device__ __forceinline__ bool childBoxRobust(float bx0, float bx1, float by0, float by1, float bz0, float bz1,
+                                               float3 o, float3 inv, float closestT, float& tNear) {
+    const float tx0 = ex::mul(ex::sub(bx0, o.x), inv.x), tx1 = ex::mul(ex::sub(bx1, o.x), inv.x);
+    const float ty0 = ex::mul(ex::sub(by0, o.y), inv.y), ty1 = ex::mul(ex::sub(by1, o.y), inv.y);
+    const float tz0 = ex::mul(ex::sub(bz0, o.z), inv.z), tz1 = ex::mul(ex::sub(bz1, o.z), inv.z);
+    const float nx = fminf(nanTo(tx0, -INFINITY), nanTo(tx1, -INFINITY));
+    const float fx = fmaxf(nanTo(tx0, INFINITY), nanTo(tx1, INFINITY));
+    const float ny = fminf(nanTo(ty0, -INFINITY), nanTo(ty1, -INFINITY));
+    const float fy = fmaxf(nanTo(ty0, INFINITY), nanTo(ty1, INFINITY));
+    const float nz = fminf(nanTo(tz0, -INFINITY), nanTo(tz1, -INFINITY));
+    const float fz = fmaxf(nanTo(tz0, INFINITY), nanTo(tz1, INFINITY));
+    const float tn = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+    const float tf = fminf(ex::mul(fminf(fminf(fx, fy), fz), 1.0000004f), closestT);
+    tNear = tn;
+    return tn <= tf;
+}
+
 // Möller-Trumbore as intersectTriangle (PathTrace.metal:1801-1852), exact ops.
 __device__ __forceinline__ bool mtTest(float3 o, float3 d, float3 v0, float3 e1, float3 e2, float& t, float& u,
                                        float& v) {
@@ -67,6 +93,64 @@ __device__ __forceinline__ bool mtTest(float3 o, float3 d, float3 v0, float3 e1,
     if (v < 0.0f || ex::add(u, v) > 1.0f) return false;
     t = ex::mul(inv, ex::dot(e2, q));
     return t > 0.0005f;
+}
+
+// Watertight ray-triangle test (Woop, Benthin and Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013), the option beside the
+// reference's Moller-Trumbore: the ray is sheared so that it runs along +z
+// through the origin, and the 2-D edge functions of the sheared vertices
+// decide the hit.  A shared edge gives the same function (with opposite sign)
+// to both of its triangles -- every product and difference is rounded on its
+// own, never contracted -- so a ray through an edge or a vertex cannot slip
+// between neighbours; an edge function that rounds to zero is recomputed in
+// FP64.  Same outputs as mtTest: t (> 0.0005, the reference's self-hit
+// offset), u = weight of v1, v = weight of v2.
+__device__ __forceinline__ float axisOf(float3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+__device__ __forceinline__ bool wtTest(float3 o, float3 d, float3 v0, float3 v1, float3 v2, float& t, float& u,
+                                       float& v) {
+    const float adx = fabsf(d.x), ady = fabsf(d.y), adz = fabsf(d.z);
+    const int kz = adx > ady ? (adx > adz ? 0 : 2) : (ady > adz ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    const float dz = axisOf(d, kz);
+    if (dz < 0.0f) {  // keep the winding of the sheared triangle
+        const int k = kx;
+        kx = ky;
+        ky = k;
+    }
+    const float sx = ex::div(axisOf(d, kx), dz), sy = ex::div(axisOf(d, ky), dz), sz = ex::rcp(dz);
+    const float3 A = ex::sub(v0, o), B = ex::sub(v1, o), C = ex::sub(v2, o);
+    const float az = axisOf(A, kz), bz = axisOf(B, kz), cz = axisOf(C, kz);
+    const float ax = ex::sub(axisOf(A, kx), ex::mul(sx, az)), ay = ex::sub(axisOf(A, ky), ex::mul(sy, az));
+    const float bx = ex::sub(axisOf(B, kx), ex::mul(sx, bz)), by = ex::sub(axisOf(B, ky), ex::mul(sy, bz));
+    const float cx = ex::sub(axisOf(C, kx), ex::mul(sx, cz)), cy = ex::sub(axisOf(C, ky), ex::mul(sy, cz));
+    float U = ex::sub(ex::mul(cx, by), ex::mul(cy, bx));
+    float V = ex::sub(ex::mul(ax, cy), ex::mul(ay, cx));
+    float W = ex::sub(ex::mul(bx, ay), ex::mul(by, ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)__dsub_rn(__dmul_rn((double)cx, (double)by), __dmul_rn((double)cy, (double)bx));
+        V = (float)__dsub_rn(__dmul_rn((double)ax, (double)cy), __dmul_rn((double)ay, (double)cx));
+        W = (float)__dsub_rn(__dmul_rn((double)bx, (double)ay), __dmul_rn((double)by, (double)ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = ex::add(ex::add(U, V), W);
+    if (det == 0.0f) return false;
+    const float T = ex::add(ex::add(ex::mul(U, ex::mul(sz, az)), ex::mul(V, ex::mul(sz, bz))), ex::mul(W, ex::mul(sz, cz)));
+    const float inv = ex::rcp(det);
+    t = ex::mul(T, inv);
+    u = ex::mul(V, inv);
+    v = ex::mul(W, inv);
+    return t > 0.0005f;
+}
+
+// The scene's triangle test on one slot's rows (v0, slot), (e1 | v1, triangle),
+// (e2 | v2, flags): Moller-Trumbore over edges (the reference's test, the
+// default) or the watertight test over absolute vertices.
+__device__ __forceinline__ bool triTest(const DevScene& S, float3 o, float3 d, const float4& a, const float4& b,
+                                        const float4& c, float& t, float& u, float& v) {
+    if (S.watertight) return wtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v);
+    return mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v);
 }
 
 __device__ __forceinline__ float3 rcp3(float3 d) { return f3(ex::rcp(d.x), ex::rcp(d.y), ex::rcp(d.z)); }
@@ -98,13 +182,20 @@ __device__ __forceinline__ int wideVisit(const DevScene& S, uint32_t node, float
     uint4 ch = __ldg(reinterpret_cast<const uint4*>(n + 6));
     float t;
     w.c0 = ch.x;
-    w.t0 = childBox(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, o, inv, tmax, t) ? t : INFINITY;
     w.c1 = ch.y;
-    w.t1 = childBox(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, o, inv, tmax, t) ? t : INFINITY;
     w.c2 = ch.z;
-    w.t2 = childBox(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, o, inv, tmax, t) ? t : INFINITY;
     w.c3 = ch.w;
-    w.t3 = childBox(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, o, inv, tmax, t) ? t : INFINITY;
+    if (S.watertight) {
+        w.t0 = childBoxRobust(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, o, inv, tmax, t) ? t : INFINITY;
+        w.t1 = childBoxRobust(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, o, inv, tmax, t) ? t : INFINITY;
+        w.t2 = childBoxRobust(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, o, inv, tmax, t) ? t : INFINITY;
+        w.t3 = childBoxRobust(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, o, inv, tmax, t) ? t : INFINITY;
+    } else {
+        w.t0 = childBox(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, o, inv, tmax, t) ? t : INFINITY;
+        w.t1 = childBox(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, o, inv, tmax, t) ? t : INFINITY;
+        w.t2 = childBox(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, o, inv, tmax, t) ? t : INFINITY;
+        w.t3 = childBox(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, o, inv, tmax, t) ? t : INFINITY;
+    }
     int k = (w.t0 != INFINITY) + (w.t1 != INFINITY) + (w.t2 != INFINITY) + (w.t3 != INFINITY);
     if (!kSort) return k;  // lanes in child order, misses at t = +inf
     if (k > 1) {
@@ -155,7 +246,7 @@ __device__ HitRec traceClosest(const DevScene& S, float3 o, float3 d) {
                 const float4* q = S.isect + 3 * (size_t)i;
                 float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
                 float t, u, v;
-                if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v)) {
+                if (triTest(S, o, d, a, b, c, t, u, v)) {
                     uint32_t slot = __float_as_uint(a.w);
                     if (t < best.t || (t == best.t && slot < bestSlot)) {
                         best.t = t;
@@ -226,7 +317,7 @@ __device__ __forceinline__ bool closestSteps(const DevScene& S, ClosestState& st
                 const float4* q = S.isect + 3 * (size_t)i;
                 float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
                 float t, u, v;
-                if (mtTest(st.o, st.d, xyz(a), xyz(b), xyz(c), t, u, v)) {
+                if (triTest(S, st.o, st.d, a, b, c, t, u, v)) {
                     uint32_t slot = __float_as_uint(a.w);
                     if (t < st.bestT || (t == st.bestT && slot < st.bestSlot)) {
                         st.bestT = t;
@@ -329,7 +420,7 @@ __device__ __forceinline__ int anySteps(const DevScene& S, AnyState& st, int* st
                 const float4* q = S.isect + 3 * (size_t)i;
                 float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
                 float t, u, v;
-                if (mtTest(st.o, st.d, xyz(a), xyz(b), xyz(c), t, u, v) && t < st.tmax) {
+                if (triTest(S, st.o, st.d, a, b, c, t, u, v) && t < st.tmax) {
                     if (blocksShadow(__float_as_uint(c.w), st.opaqueMask)) return 2;
                     st.sawNonOpaque = true;
                     if (st.rec) {
@@ -476,7 +567,7 @@ __device__ __forceinline__ bool closestSteps(const DevScene& S, Closest8& st, ui
         const float4* q = S.isect + 3 * (size_t)i;
         const float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
         float t, u, v;
-        if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v)) {
+        if (triTest(S, o, d, a, b, c, t, u, v)) {
             const uint32_t slot = __float_as_uint(a.w);
             if (t < tmax || (t == tmax && slot < st.bestSlot)) {
                 tmax = t;
@@ -527,7 +618,7 @@ __device__ __forceinline__ int anySteps(const DevScene& S, Any8& st, uint2* stac
         const float4* q = S.isect + 3 * (size_t)i;
         const float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
         float t, u, v;
-        if (mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) && t < st.tmax) {
+        if (triTest(S, o, d, a, b, c, t, u, v) && t < st.tmax) {
             if (blocksShadow(__float_as_uint(c.w), st.opaqueMask)) return true;
             st.sawNonOpaque = true;
             if (st.rec) {

@@ -14,6 +14,8 @@
 #include <cstring>
 #include <string>
 #include <thread>
+
+#include <cuda_fp16.h>
 #include <vector>
 
 #include "dk_host.h"
@@ -343,7 +345,7 @@ void persistTraversal(const DevScene& D, cudaStream_t stream) {
                 maxPersist / 1e6, v.accessPolicyWindow.hitRatio);
 }
 
-TraversalBuild buildTraversal(const dk_scene* sc) {
+TraversalBuild buildTraversal(const dk_scene* sc, bool watertight) {
     // Traversal BVH: a binned-SAH tree over the triangles the caller's BVH
     // reaches, each carrying its reference DFS slot as the tie-break key.
     const double t0 = traceCreate() ? wallMs() : 0.0;
@@ -354,7 +356,8 @@ TraversalBuild buildTraversal(const dk_scene* sc) {
         }
     } report{t0};
     TraversalBuild t;
-    t.width = traversalWidth();
+    // The watertight mode's robust box test is the 4-wide tree's.
+    t.width = watertight ? 4 : traversalWidth();
     std::vector<uint32_t> slotOf;
     std::string err;
     if (!referenceSlots(sc, slotOf, err)) {
@@ -371,7 +374,25 @@ TraversalBuild buildTraversal(const dk_scene* sc) {
         if (!opaque[i] && slotOf[i] != kNoSlot) t.allOpaque = false;
     }
     t.rc = buildSahTraversal(sc, slotOf, opaque, t.width, t.nodes, t.isect, err);
-    if (t.rc != DK_OK) t.err = "Invalid render scene: " + err + ".";
+    if (t.rc != DK_OK) {
+        t.err = "Invalid render scene: " + err + ".";
+        return t;
+    }
+    if (watertight) {
+        // The watertight test reads the exact vertices: rows 1 and 2 of every
+        // slot become v1 and v2 (the dummy slot stays degenerate).
+        t.watertight = true;
+        const size_t slots = t.isect.size() / 3;
+        for (size_t k = 0; k < slots; ++k) {
+            uint32_t slot, tri;
+            std::memcpy(&slot, &t.isect[3 * k].w, 4);
+            std::memcpy(&tri, &t.isect[3 * k + 1].w, 4);
+            if (slot == 0xffffffffu || tri >= sc->triangle_count) continue;
+            const dk_triangle& tr = sc->triangles[tri];
+            t.isect[3 * k + 1] = make_float4(tr.v1.x, tr.v1.y, tr.v1.z, t.isect[3 * k + 1].w);
+            t.isect[3 * k + 2] = make_float4(tr.v2.x, tr.v2.y, tr.v2.z, t.isect[3 * k + 2].w);
+        }
+    }
     return t;
 }
 
@@ -442,9 +463,24 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
                          sc->volume_brick_count, "volume bricks"));
         TRY(arena.upload(const_cast<dk_volume_brick_sample**>(&D.brick_samples), sc->volume_brick_samples,
                          (size_t)sc->volume_brick_sample_count, "volume brick samples"));
-        std::vector<float> dist((size_t)sc->volume_brick_sample_count);
-        for (size_t i = 0; i < dist.size(); ++i) dist[i] = sc->volume_brick_samples[i].distance;
-        TRY(arena.upload(const_cast<float**>(&D.brick_dist), dist.data(), dist.size(), "volume brick distances"));
+        // FP16 (2 bytes a sample) when every stored distance is a half value
+        // (a build with fp16_distances), else FP32: the same floats either way.
+        const size_t ns = (size_t)sc->volume_brick_sample_count;
+        std::vector<uint16_t> half(ns);
+        bool halfExact = true;
+        for (size_t i = 0; i < ns && halfExact; ++i) {
+            const float d = sc->volume_brick_samples[i].distance;
+            const __half h = __float2half_rn(d);
+            halfExact = __half2float(h) == d && std::isfinite(d);
+            half[i] = __half_as_ushort(h);
+        }
+        if (halfExact && ns > 0) {
+            TRY(arena.upload(const_cast<uint16_t**>(&D.brick_dist16), half.data(), ns, "volume brick distances (FP16)"));
+        } else {
+            std::vector<float> dist(ns);
+            for (size_t i = 0; i < ns; ++i) dist[i] = sc->volume_brick_samples[i].distance;
+            TRY(arena.upload(const_cast<float**>(&D.brick_dist), dist.data(), dist.size(), "volume brick distances"));
+        }
         TRY(arena.upload(const_cast<dk_volume_brick_grid**>(&D.brick_grids), sc->volume_brick_grids,
                          sc->volume_brick_grid_count, "volume brick grids"));
         TRY(arena.upload(const_cast<uint32_t**>(&D.brick_grid_indices), sc->volume_brick_grid_indices,
@@ -480,6 +516,7 @@ int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t material
         D.traversal_bytes = (nodeOfs + t.nodes.size()) * sizeof(float4);
         D.node_count = (uint32_t)(t.nodes.size() / (t.width == 8 ? 5 : 8));
         D.wide8 = t.width == 8 ? 1u : 0u;
+        D.watertight = t.watertight ? 1u : 0u;
         D.all_shadow_opaque = t.allOpaque ? 1u : 0u;
     }
 #undef TRY
@@ -728,6 +765,8 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     if (st->width == 0 || st->height == 0)
         return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Render dimensions must be positive.");
     if (st->quality > DK_QUALITY_FINAL) return fail(DK_ERROR_INVALID_ARGUMENT, "unknown render quality");
+    if (st->triangle_test > DK_TRIANGLE_TEST_WATERTIGHT)
+        return fail(DK_ERROR_INVALID_ARGUMENT, "unknown triangle test");
     int rc = dk::validateScene(sc);
     if (rc != DK_OK) return rc;
     rc = dk::ensureDevice();
@@ -741,8 +780,9 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
         tPrev = now;
     };
     // The host traversal build runs while this thread allocates the wave.
+    const bool watertight = st->triangle_test == DK_TRIANGLE_TEST_WATERTIGHT;
     std::future<dk::TraversalBuild> traversal =
-        std::async(std::launch::async, [sc] { return dk::buildTraversal(sc); });
+        std::async(std::launch::async, [sc, watertight] { return dk::buildTraversal(sc, watertight); });
     struct WaitBuild {  // the build reads `sc`: it must end before this returns
         std::future<dk::TraversalBuild>& f;
         ~WaitBuild() {

@@ -67,9 +67,12 @@ struct TraversalBuild {
     std::string err;
     int width = 4;
     bool allOpaque = true;
+    bool watertight = false;  // slot rows hold v1, v2 (watertight test) instead of the edges
     std::vector<float4> nodes, isect;
 };
-TraversalBuild buildTraversal(const dk_scene* sc);
+// `watertight`: the slots carry absolute vertices for the watertight test
+// (dk_settings.triangle_test = DK_TRIANGLE_TEST_WATERTIGHT).
+TraversalBuild buildTraversal(const dk_scene* sc, bool watertight = false);
 // Uploads the scene; `pending` (may be null) is a traversal build already
 // started with std::async(buildTraversal).
 int uploadScene(Arena& arena, const dk_scene* sc, DevScene& D, uint32_t materialCapacity,

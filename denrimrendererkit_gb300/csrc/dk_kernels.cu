@@ -123,7 +123,7 @@ __device__ __forceinline__ VolumeScene volumeScene(const DevScene& S) {
     V.volumes = S.volumes;
     V.bricks = S.bricks;
     V.samples = S.brick_samples;
-    V.dist = S.brick_dist;
+    V.dist = DistSrc{S.brick_dist, S.brick_dist16};
     V.grids = S.brick_grids;
     V.gridIndices = S.brick_grid_indices;
     V.sampleCount = S.brick_sample_count;
@@ -765,6 +765,45 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
 #ifndef DK_SHADE_MIN_BLOCKS
 #define DK_SHADE_MIN_BLOCKS 4
 #endif
+__device__ __forceinline__ void prefetchL2(const void* ptr) {
+    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(ptr));
+}
+
+// The next path of this thread (shading order `i`): its hit record is loaded
+// now and consumed after the current path, when its path state and the
+// 192-byte triangle record of its hit are prefetched into L2 -- the shading
+// of one path overlaps the memory latency of the next one's dependent loads.
+struct NextPath {
+    uint32_t p;
+    float tri;
+};
+
+__device__ __forceinline__ NextPath peekNext(const Wave& W, const uint32_t* q, uint32_t i, uint32_t n) {
+    NextPath nx{0u, __uint_as_float(kNoHit)};
+    if (i < n) {
+        nx.p = __ldg(q + i);
+        nx.tri = __ldg(reinterpret_cast<const float*>(W.hit + nx.p) + 1);
+    }
+    return nx;
+}
+
+__device__ __forceinline__ void prefetchNext(const DevScene& S, const Wave& W, const NextPath& nx, uint32_t i,
+                                             uint32_t n) {
+    if (i >= n) return;
+    prefetchL2(W.ray_o + nx.p);
+    prefetchL2(W.ray_d + nx.p);
+    prefetchL2(W.tp + nx.p);
+    prefetchL2(W.rad + nx.p);
+    prefetchL2(W.rng + nx.p);
+    const uint32_t tri = __float_as_uint(nx.tri);
+    if (tri < S.tri_count) {
+        const char* rec = reinterpret_cast<const char*>(S.tris + tri);
+        prefetchL2(rec);
+        prefetchL2(rec + 64);
+        prefetchL2(rec + 128);
+    }
+}
+
 template <bool kVolumes>
 __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, Wave W, uint32_t bounce, uint32_t sel,
                                                                   uint32_t sorted) {
@@ -772,9 +811,14 @@ __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
     uint32_t* qNext = W.q[sel ^ 1u];
     const uint32_t n = W.counts[sel];
     if (globalId() == 0) W.counts[4] = 0u;  // extend cursor of the next bounce
-    for (uint32_t i = globalId(); i < n; i += gridStride()) {
-        uint32_t p = q[i];
+    const uint32_t stride = gridStride();
+    uint32_t pCur = globalId() < n ? q[globalId()] : 0u;
+    for (uint32_t i = globalId(); i < n; i += stride) {
+        const uint32_t p = pCur;
+        const NextPath nx = peekNext(W, q, i + stride, n);
         ShadeOut o = shadePath<kVolumes>(S, W, p, i, bounce);
+        prefetchNext(S, W, nx, i + stride, n);
+        pCur = nx.p;
         bool keep = o.survive && bounce + 1u < o.maxBounces;
         uint32_t slot = warpAppend(&W.counts[sel ^ 1u], keep);
         if (keep) qNext[slot] = p;
@@ -858,7 +902,7 @@ __device__ __noinline__ bool shadowLayers8(const DevScene& S, MatTable mt, uint3
         const float4* q = S.isect + 3 * (size_t)i;
         const float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
         float t, u, v;
-        if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) || !(t < tmax)) return false;
+        if (!triTest(S, o, d, a, b, c, t, u, v) || !(t < tmax)) return false;
         if (blocksShadow(__float_as_uint(c.w), opaqueMask)) return true;  // opaque blocker
         if (count == kMaxLayers - 1) return true;                        // an 8th layer: the walk ends occluded
         insertLayer(lt, ltri, lslot, lu, lv, count, t, __float_as_uint(b.w), __float_as_uint(a.w), u, v);
@@ -899,7 +943,7 @@ __device__ bool shadowLayers(const DevScene& S, MatTable mt, uint32_t opaqueMask
                 const float4* q = S.isect + 3 * (size_t)i;
                 float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
                 float t, u, v;
-                if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v) || !(t < tmax)) continue;
+                if (!triTest(S, o, d, a, b, c, t, u, v) || !(t < tmax)) continue;
                 if (blocksShadow(__float_as_uint(c.w), opaqueMask)) return true;  // opaque blocker
                 if (count == kMaxLayers - 1) return true;    // an 8th layer: the walk ends occluded
                 insertLayer(lt, ltri, lslot, lu, lv, count, t, __float_as_uint(b.w), __float_as_uint(a.w), u, v);
@@ -924,7 +968,7 @@ __device__ bool recordedLayers(const DevScene& S, MatTable mt, float3 o, float3 
         const float4* q = S.isect + 3 * (size_t)rec[k].y;
         float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2);
         float t, u, v;
-        if (!mtTest(o, d, xyz(a), xyz(b), xyz(c), t, u, v)) continue;
+        if (!triTest(S, o, d, a, b, c, t, u, v)) continue;
         insertLayer(lt, ltri, lslot, lu, lv, count, t, __float_as_uint(b.w), __float_as_uint(a.w), u, v);
     }
     return walkLayers(S, mt, o, d, lt, ltri, lu, lv, count, T);

@@ -41,11 +41,13 @@ struct DevScene {
     uint32_t env_guide_size;
     float env_rot_sin, env_rot_cos;  // sincosf(env_rot_y), evaluated once on the device
     uint32_t wide8;                  // traversal tree layout: 0 = 4-wide FP32, 1 = 8-wide quantised
+    uint32_t watertight;             // triangle test: 0 = Moller-Trumbore over edges, 1 = watertight over vertices
     // Sparse distance volumes (GPUVolumeDescriptor with metadata.w == 1).
     const dk_volume_descriptor* volumes;
     const dk_volume_brick_descriptor* bricks;
     const dk_volume_brick_sample* brick_samples;
-    const float* brick_dist;  // distance-only copy of brick_samples
+    const float* brick_dist;  // distance-only copy of brick_samples (FP32), or null
+    const uint16_t* brick_dist16;  // the same as FP16 bits when every distance is a half value, or null
     const dk_volume_brick_grid* brick_grids;
     const uint32_t* brick_grid_indices;
     uint64_t brick_sample_count, brick_grid_index_count;

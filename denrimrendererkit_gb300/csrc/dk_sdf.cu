@@ -24,6 +24,7 @@
 #include <thread>
 #include <vector>
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/denrim_cuda.h"
@@ -275,6 +276,7 @@ dk_sparse_volume* assemble(const BakeGrid& G, size_t cellCount, const std::vecto
     for (const Brick* b : perCell)
         if (b) total += (size_t)b->dims[0] * b->dims[1] * b->dims[2];
     v->samples.reserve(total);
+    const bool fp16 = st->fp16_distances != 0;
     float den[3];
     for (int a = 0; a < 3; ++a) den[a] = (float)std::max(G.dims[a] - 1, 1);
     for (size_t c = 0; c < cellCount; ++c) {
@@ -283,12 +285,14 @@ dk_sparse_volume* assemble(const BakeGrid& G, size_t cellCount, const std::vecto
         uint32_t brickIndex = (uint32_t)v->bricks.size();
         uint32_t sampleOffset = (uint32_t)v->samples.size();
         const size_t n = (size_t)b->dims[0] * b->dims[1] * b->dims[2];
-        float dmin = FLT_MAX, dmax = -FLT_MAX;
-        for (size_t k = 0; k < n; ++k) {
-            dmin = std::fmin(dmin, b->samples[k].distance);
-            dmax = std::fmax(dmax, b->samples[k].distance);
-        }
         v->samples.insert(v->samples.end(), b->samples, b->samples + n);
+        float dmin = FLT_MAX, dmax = -FLT_MAX;
+        for (size_t k = sampleOffset; k < sampleOffset + n; ++k) {
+            float& d = v->samples[k].distance;
+            if (fp16) d = __half2float(__float2half_rn(d));  // FP16 storage: the stored value is the rounded one
+            dmin = std::fmin(dmin, d);
+            dmax = std::fmax(dmax, d);
+        }
         dk_volume_brick_descriptor d;
         float cmin[3], cmax[3], smin[3], smax[3];
         for (int a = 0; a < 3; ++a) {  // brickCoreLocalBounds / brickSampleLocalBounds (:578-653)

@@ -5,9 +5,12 @@
 // 2057-2469, 2608-2807, 2862-3263).  All arithmetic uses explicitly rounded
 // IEEE operations so that hits on the distance field — and the depth, normal
 // and ID AOVs derived from them — match the reference arithmetic bit for bit.
-// The march reads the FP32 distances from a distance-only copy of the packed
-// samples (the same values as the reference's 16-byte records).
+// The march reads the distances from a distance-only copy of the packed
+// samples (the same values as the reference's 16-byte records): FP32, or FP16
+// (2 bytes per sample) when every distance is a half-precision value.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "dk_device.cuh"
 
 namespace dk {
@@ -85,12 +88,22 @@ __device__ __forceinline__ GridPos gridPos(const BrickCtx& c, float3 p) {
     return r;
 }
 
-__device__ __forceinline__ float sampleD(const float* dist, const BrickCtx& c, uint32_t x, uint32_t y, uint32_t z) {
-    return __ldg(dist + c.sampleOffset + x + y * c.strideY + z * c.strideZ);
+// The march's distance samples: FP32, or FP16 when every stored distance of
+// the scene is exactly a half-precision value (a build with FP16 distances);
+// both give the same float.
+struct DistSrc {
+    const float* f32;
+    const uint16_t* f16;
+};
+
+__device__ __forceinline__ float sampleD(const DistSrc& dist, const BrickCtx& c, uint32_t x, uint32_t y, uint32_t z) {
+    const size_t k = c.sampleOffset + x + y * c.strideY + z * c.strideZ;
+    if (dist.f16) return __half2float(__ushort_as_half(__ldg(dist.f16 + k)));
+    return __ldg(dist.f32 + k);
 }
 
 // sampleVolumeBrickDistancePrepared (:2097-2125).
-__device__ float brickDistance(const float* dist, const BrickCtx& c, float3 p) {
+__device__ float brickDistance(const DistSrc& dist, const BrickCtx& c, float3 p) {
     if (!c.valid) return INFINITY;
     GridPos g = gridPos(c, p);
     const uint32_t *b = g.base, *n = g.next;
@@ -109,7 +122,7 @@ struct DistGrad {
 };
 
 // sampleVolumeBrickDistanceGradientPrepared (:2164-2218).
-__device__ DistGrad brickDistGrad(const float* dist, const BrickCtx& c, float3 p) {
+__device__ DistGrad brickDistGrad(const DistSrc& dist, const BrickCtx& c, float3 p) {
     DistGrad r;
     r.distance = INFINITY;
     r.gradient = f3(0.0f);
@@ -151,7 +164,7 @@ __device__ __forceinline__ float catmullD(float p0, float p1, float p2, float p3
 }
 
 // sampleVolumeBrickDistanceGradientCubicPrepared (:2256-2307).
-__device__ __noinline__ DistGrad brickDistGradCubic(const float* dist, const BrickCtx& c, float3 p) {
+__device__ __noinline__ DistGrad brickDistGradCubic(const DistSrc& dist, const BrickCtx& c, float3 p) {
     if (!c.valid) {
         DistGrad r;
         r.distance = INFINITY;
@@ -197,7 +210,7 @@ __device__ __noinline__ DistGrad brickDistGradCubic(const float* dist, const Bri
 }
 
 // sampleVolumeBrickCentralGradientPrepared (:2220-2254).
-__device__ float3 brickCentralGradient(const float* dist, const BrickCtx& c, float3 p, float3 s) {
+__device__ float3 brickCentralGradient(const DistSrc& dist, const BrickCtx& c, float3 p, float3 s) {
     float3 x0 = p, x1 = p, y0 = p, y1 = p, z0 = p, z1 = p;
     x0.x = fmaxf(ex::sub(p.x, s.x), c.sampleMin.x);
     x1.x = fminf(ex::add(p.x, s.x), c.sampleMax.x);
@@ -215,7 +228,7 @@ struct VolumeScene {
     const dk_volume_descriptor* volumes;
     const dk_volume_brick_descriptor* bricks;
     const dk_volume_brick_sample* samples;
-    const float* dist;
+    DistSrc dist;
     const dk_volume_brick_grid* grids;
     const uint32_t* gridIndices;
     uint64_t sampleCount, gridIndexCount;

@@ -1,15 +1,20 @@
 // Serving loop of the C ABI (dk_server_* in include/denrim_cuda.h).
 //
-// One resident scene, many jobs.  Every wave packs the paths of the oldest
-// admitted jobs into the shared wavefront (each job contributes up to
-// `samples_per_wave` whole frames), so small previews that could never fill
-// the GPU alone run side by side with larger renders.  Per job the server
-// keeps a material table in a slot of the scene's material array and one
-// device block (from a private stream-ordered pool) with the job's Kahan
-// accumulation buffers and AOV planes; admission is first-in first-out while
-// those blocks fit the HBM budget.  Paths depend only on (pixel, sample,
-// frame seed, the job's materials and settings) and every pixel accumulates
-// its samples in order, so a job renders the same bits alone or in a mix.
+// Resident scenes, many jobs.  The scene given at create is scene 0;
+// dk_server_add_scene makes more resident (BVHs, textures, lights and the HDRI
+// table stay on the device), each with its own wavefront and stream.  Every
+// step packs, per scene, the paths of the oldest admitted jobs of that scene
+// into the scene's wavefront (each job contributes up to `samples_per_wave`
+// whole frames), so small previews that could never fill the GPU alone run
+// side by side with larger renders; the scenes' waves are issued on their own
+// streams and overlap on the device.  Per job the server keeps a material
+// table in a slot of its scene's material array and one device block (from a
+// private stream-ordered pool) with the job's Kahan accumulation buffers and
+// AOV planes; admission is first-in first-out while those blocks fit the HBM
+// budget.  Paths depend only on (pixel, sample, frame seed, the job's
+// materials and settings) and every pixel accumulates its samples in order,
+// so a job renders the same bits alone or in a mix, whatever the other
+// scenes do.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -38,10 +43,11 @@ size_t jobBlockBytes(size_t pixels) {
 
 struct Job {
     uint64_t id = 0;
+    uint32_t scene = 0;  // index into Server::scenes
     dk_settings settings;
     uint32_t samples = 0, samplesDone = 0, waves = 0, state = DK_JOB_QUEUED;
     std::vector<dk_material> materials;
-    uint32_t slot = 0;  // material slot: S.mats[(1 + slot) * M, (2 + slot) * M)
+    uint32_t slot = 0;  // material slot of its scene: S.mats[(1 + slot) * M, (2 + slot) * M)
     uint32_t opaqueMask = 0;
     dk::Accum A{};
     void* block = nullptr;
@@ -49,22 +55,28 @@ struct Job {
     double submitMs = 0, admitMs = 0, finishMs = 0;
 };
 
-struct Server {
-    dk_server_config cfg;
+// One resident scene: its device arrays (material array with one table per
+// material slot), its wavefront and the stream its waves and admissions run on.
+struct SceneSlot {
     dk::Arena arena;
     dk::DevScene scene;
     dk::Wave wave;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t evBegin = nullptr, evEnd = nullptr;
+    uint32_t matCount = 0;            // M: entries of the scene's (and its jobs') material table
+    std::vector<dk_material> baseMaterials;
+    std::vector<uint32_t> freeSlots;  // material slots (guarded by Server::mu)
+};
+
+struct Server {
+    dk_server_config cfg;
     dk::Grids grids;
-    cudaStream_t stream = nullptr;    // waves, admission uploads
+    std::vector<std::unique_ptr<SceneSlot>> scenes;  // appended under stepMu + mu; never removed
     cudaStream_t ioStream = nullptr;  // readback and release of finished jobs
     cudaMemPool_t pool = nullptr;
-    cudaEvent_t evBegin = nullptr, evEnd = nullptr;
     float4* staging = nullptr;        // readback staging (ioStream), grown on demand
     size_t stagingPixels = 0;
     cudaEvent_t copyDone = nullptr;   // orders dk_server_copy_output before the caller's stream
-    uint32_t matCount = 0;            // M: entries of the scene's (and every job's) material table
-    std::vector<dk_material> baseMaterials;
-    std::vector<uint32_t> freeSlots;
 
     std::mutex mu;                    // jobs, queues, budget, stats
     std::condition_variable cv;
@@ -92,20 +104,58 @@ Server* asServer(dk_server* s) { return reinterpret_cast<Server*>(s); }
 
 void destroyServer(Server* s) {
     if (!s) return;
-    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto& sc : s->scenes)
+        if (sc->stream) cudaStreamSynchronize(sc->stream);
     if (s->ioStream) cudaStreamSynchronize(s->ioStream);
     for (auto& kv : s->jobs)
-        if (kv.second->block) cudaFreeAsync(kv.second->block, s->stream);
-    if (s->stream) cudaStreamSynchronize(s->stream);
+        if (kv.second->block && s->ioStream) cudaFreeAsync(kv.second->block, s->ioStream);
+    if (s->ioStream) cudaStreamSynchronize(s->ioStream);
     if (s->staging) cudaFree(s->staging);
     if (s->pool) cudaMemPoolDestroy(s->pool);
-    s->arena.release();
-    if (s->evBegin) cudaEventDestroy(s->evBegin);
-    if (s->evEnd) cudaEventDestroy(s->evEnd);
+    for (auto& sc : s->scenes) {
+        sc->arena.release();
+        if (sc->evBegin) cudaEventDestroy(sc->evBegin);
+        if (sc->evEnd) cudaEventDestroy(sc->evEnd);
+        if (sc->stream) cudaStreamDestroy(sc->stream);
+    }
     if (s->copyDone) cudaEventDestroy(s->copyDone);
-    if (s->stream) cudaStreamDestroy(s->stream);
     if (s->ioStream) cudaStreamDestroy(s->ioStream);
     delete s;
+}
+
+// Uploads `sc` as a resident scene with its own wavefront and stream.
+int makeSceneSlot(Server* s, const dk_scene* sc, std::unique_ptr<SceneSlot>& out) {
+    int rc = dk::validateScene(sc);
+    if (rc != DK_OK) return rc;
+    auto slot = std::make_unique<SceneSlot>();
+    SceneSlot& S = *slot;
+    struct Cleanup {  // a failed upload releases what it made
+        std::unique_ptr<SceneSlot>& p;
+        bool keep = false;
+        ~Cleanup() {
+            if (keep || !p) return;
+            p->arena.release();
+            if (p->evBegin) cudaEventDestroy(p->evBegin);
+            if (p->evEnd) cudaEventDestroy(p->evEnd);
+            if (p->stream) cudaStreamDestroy(p->stream);
+        }
+    } cleanup{slot};
+    DK_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    DK_CUDA(cudaEventCreate(&S.evBegin), "cudaEventCreate");
+    DK_CUDA(cudaEventCreate(&S.evEnd), "cudaEventCreate");
+    S.matCount = sc->material_count;
+    S.baseMaterials.assign(sc->materials, sc->materials + sc->material_count);
+    const uint32_t slots = s->cfg.max_resident_jobs;
+    rc = dk::uploadScene(S.arena, sc, S.scene,
+                         (uint32_t)std::min<uint64_t>((uint64_t)(slots + 1) * S.matCount, 0xffffffffull));
+    if (rc != DK_OK) return rc;
+    S.scene.all_shadow_opaque = 0;  // job tables may make materials cut-out or transmissive
+    for (uint32_t k = slots; k > 0; --k) S.freeSlots.push_back(k - 1);
+    rc = dk::allocWave(S.arena, S.wave, s->cfg.wave_paths, s->cfg.wave_paths, s->cfg.max_jobs_per_wave);
+    if (rc != DK_OK) return rc;
+    cleanup.keep = true;
+    out = std::move(slot);
+    return DK_OK;
 }
 
 bool sameEmission(const dk_material& a, const dk_material& b) {
@@ -117,13 +167,14 @@ bool sameEmission(const dk_material& a, const dk_material& b) {
 int admitLocked(Server* s) {
     while (!s->pending.empty()) {
         Job& j = *s->jobs[s->pending.front()];
+        SceneSlot& S = *s->scenes[j.scene];
         size_t pixels = (size_t)j.settings.width * j.settings.height;
         size_t bytes = jobBlockBytes(pixels);
-        if (s->budgetUsed + bytes > s->cfg.hbm_budget_bytes || s->freeSlots.empty() ||
+        if (s->budgetUsed + bytes > s->cfg.hbm_budget_bytes || S.freeSlots.empty() ||
             s->running.size() >= s->cfg.max_resident_jobs)
             break;
         void* block = nullptr;
-        DK_CUDA(cudaMallocFromPoolAsync(&block, bytes, s->pool, s->stream), "job buffers");
+        DK_CUDA(cudaMallocFromPoolAsync(&block, bytes, s->pool, S.stream), "job buffers");
         char* p = static_cast<char*>(block);
         j.A.sum = reinterpret_cast<float4*>(p);
         p += alignUp(pixels * sizeof(float4));
@@ -134,13 +185,13 @@ int admitLocked(Server* s) {
         j.A.count = reinterpret_cast<uint32_t*>(p);
         p += alignUp(pixels * sizeof(uint32_t));
         j.A.aov = reinterpret_cast<float4*>(p);
-        DK_CUDA(cudaMemsetAsync(block, 0, bytes, s->stream), "job buffers");
-        j.slot = s->freeSlots.back();
-        s->freeSlots.pop_back();
-        dk_material* dst = const_cast<dk_material*>(s->scene.mats) + (size_t)(1 + j.slot) * s->matCount;
+        DK_CUDA(cudaMemsetAsync(block, 0, bytes, S.stream), "job buffers");
+        j.slot = S.freeSlots.back();
+        S.freeSlots.pop_back();
+        dk_material* dst = const_cast<dk_material*>(S.scene.mats) + (size_t)(1 + j.slot) * S.matCount;
         // Pageable source: staged before the call returns.
-        DK_CUDA(cudaMemcpyAsync(dst, j.materials.data(), s->matCount * sizeof(dk_material), cudaMemcpyHostToDevice,
-                                s->stream),
+        DK_CUDA(cudaMemcpyAsync(dst, j.materials.data(), S.matCount * sizeof(dk_material), cudaMemcpyHostToDevice,
+                                S.stream),
                 "job materials");
         j.block = block;
         j.bytes = bytes;
@@ -160,108 +211,140 @@ bool hasWorkLocked(Server* s) {
     if (s->pending.empty()) return false;
     const Job& j = *s->jobs.at(s->pending.front());
     size_t bytes = jobBlockBytes((size_t)j.settings.width * j.settings.height);
-    return s->budgetUsed + bytes <= s->cfg.hbm_budget_bytes && !s->freeSlots.empty() &&
+    return s->budgetUsed + bytes <= s->cfg.hbm_budget_bytes && !s->scenes[j.scene]->freeSlots.empty() &&
            s->running.size() < s->cfg.max_resident_jobs;
 }
 
-// Admission, one packed wave, completion.
+// Admission, one packed wave per scene with work (the scenes' waves overlap
+// on their streams), completion.
 int stepServer(Server* s, uint32_t* outJobs) {
     std::lock_guard<std::mutex> stepLock(s->stepMu);
     if (outJobs) *outJobs = 0;
-    std::vector<dk::DevJob> table;
-    std::vector<Job*> members;
-    std::vector<uint32_t> counts;
-    uint32_t maxBounces = 1;
-    bool anyDenoiser = false;
+    struct Plan {
+        std::vector<dk::DevJob> table;
+        std::vector<Job*> members;
+        std::vector<uint32_t> counts;
+        uint32_t maxBounces = 1;
+        bool anyDenoiser = false;
+    };
+    std::vector<Plan> plans;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         int rc = admitLocked(s);
         if (rc != DK_OK) return rc;
-        uint64_t used = 0, pix = 0;
-        const uint64_t cap = s->wave.cap;
-        // Wave order: the oldest running job first (it always progresses), then
-        // the others by remaining paths, fewest first (policy 1), or in
-        // admission order (policy 0).
-        std::vector<uint64_t> order;
-        for (uint64_t id : s->running)
-            if (s->jobs[id]->state == DK_JOB_RUNNING) order.push_back(id);
-        if (s->cfg.policy == 1 && order.size() > 2) {
-            auto remaining = [&](uint64_t id) {
-                const Job& j = *s->jobs[id];
-                return (uint64_t)(j.samples - j.samplesDone) * j.settings.width * j.settings.height;
-            };
-            std::stable_sort(order.begin() + 1, order.end(),
-                             [&](uint64_t x, uint64_t y) { return remaining(x) < remaining(y); });
+        plans.resize(s->scenes.size());
+        // Wave order per scene: its oldest running job first (it always
+        // progresses), then the others by remaining paths, fewest first
+        // (policy 1), or in admission order (policy 0).
+        std::vector<std::vector<uint64_t>> order(s->scenes.size());
+        for (uint64_t id : s->running) {
+            const Job& j = *s->jobs[id];
+            if (j.state == DK_JOB_RUNNING) order[j.scene].push_back(id);
         }
-        for (uint64_t id : order) {
-            Job& j = *s->jobs[id];
-            if (table.size() >= s->cfg.max_jobs_per_wave) break;
-            uint64_t pixels = (uint64_t)j.settings.width * j.settings.height;
-            uint64_t room = (cap - used) / pixels;
-            uint32_t nb = (uint32_t)std::min<uint64_t>({(uint64_t)(j.samples - j.samplesDone),
-                                                         (uint64_t)s->cfg.samples_per_wave, room});
-            if (nb == 0) continue;  // no room for a frame of this job; a smaller one may still fit
-            dk::DevJob dj;
-            std::memset(&dj, 0, sizeof(dj));
-            dk::fillParams(dj.P, j.settings);
-            dj.P.sample_begin = j.samplesDone;
-            dj.P.samples_in_batch = nb;
-            dj.P.path_count = (uint32_t)(nb * pixels);
-            dj.A = j.A;
-            dj.path_begin = (uint32_t)used;
-            dj.pixel_begin = (uint32_t)pix;
-            dj.mat_base = (1 + j.slot) * s->matCount;
-            dj.mat_count = s->matCount;
-            dj.opaque_mask = j.opaqueMask;
-            table.push_back(dj);
-            members.push_back(&j);
-            counts.push_back(nb);
-            used += nb * pixels;
-            pix += pixels;
-            maxBounces = std::max(maxBounces, dj.P.max_bounces);
-            anyDenoiser = anyDenoiser || dj.P.denoiser != 0;
+        for (size_t si = 0; si < s->scenes.size(); ++si) {
+            std::vector<uint64_t>& ord = order[si];
+            if (s->cfg.policy == 1 && ord.size() > 2) {
+                auto remaining = [&](uint64_t id) {
+                    const Job& j = *s->jobs[id];
+                    return (uint64_t)(j.samples - j.samplesDone) * j.settings.width * j.settings.height;
+                };
+                std::stable_sort(ord.begin() + 1, ord.end(),
+                                 [&](uint64_t x, uint64_t y) { return remaining(x) < remaining(y); });
+            }
+            const SceneSlot& S = *s->scenes[si];
+            Plan& pl = plans[si];
+            uint64_t used = 0, pix = 0;
+            const uint64_t cap = S.wave.cap;
+            for (uint64_t id : ord) {
+                Job& j = *s->jobs[id];
+                if (pl.table.size() >= s->cfg.max_jobs_per_wave) break;
+                uint64_t pixels = (uint64_t)j.settings.width * j.settings.height;
+                uint64_t room = (cap - used) / pixels;
+                uint32_t nb = (uint32_t)std::min<uint64_t>({(uint64_t)(j.samples - j.samplesDone),
+                                                             (uint64_t)s->cfg.samples_per_wave, room});
+                if (nb == 0) continue;  // no room for a frame of this job; a smaller one may still fit
+                dk::DevJob dj;
+                std::memset(&dj, 0, sizeof(dj));
+                dk::fillParams(dj.P, j.settings);
+                dj.P.sample_begin = j.samplesDone;
+                dj.P.samples_in_batch = nb;
+                dj.P.path_count = (uint32_t)(nb * pixels);
+                dj.A = j.A;
+                dj.path_begin = (uint32_t)used;
+                dj.pixel_begin = (uint32_t)pix;
+                dj.mat_base = (1 + j.slot) * S.matCount;
+                dj.mat_count = S.matCount;
+                dj.opaque_mask = j.opaqueMask;
+                pl.table.push_back(dj);
+                pl.members.push_back(&j);
+                pl.counts.push_back(nb);
+                used += nb * pixels;
+                pix += pixels;
+                pl.maxBounces = std::max(pl.maxBounces, dj.P.max_bounces);
+                pl.anyDenoiser = pl.anyDenoiser || dj.P.denoiser != 0;
+            }
         }
     }
-    if (table.empty()) return DK_OK;
-    cudaStream_t q = s->stream;
-    DK_CUDA(cudaMemcpyAsync(const_cast<dk::DevJob*>(s->wave.jobs), table.data(), table.size() * sizeof(dk::DevJob),
-                            cudaMemcpyHostToDevice, q),
-            "job table upload");
-    dk::Wave W = s->wave;
-    W.job_count = (uint32_t)table.size();
-    W.path_count = table.back().path_begin + table.back().P.path_count;
-    W.pixel_count = table.back().pixel_begin + table.back().P.tile_w * table.back().P.tile_h;
-    DK_CUDA(cudaEventRecord(s->evBegin, q), "cudaEventRecord");
-    uint64_t launches = 0;
-    auto mark = [](int) { return (int)DK_OK; };
-    int rc = dk::launchWave(s->scene, W, maxBounces, anyDenoiser, s->grids, q, mark, launches);
-    if (rc != DK_OK) return rc;
-    DK_CUDA(cudaEventRecord(s->evEnd, q), "cudaEventRecord");
-    DK_CUDA(cudaEventSynchronize(s->evEnd), "wave");
+    uint64_t launches = 0, paths = 0;
+    uint32_t jobsInStep = 0, wavesInStep = 0;
+    int first = -1;
+    for (size_t si = 0; si < plans.size(); ++si) {
+        Plan& pl = plans[si];
+        if (pl.table.empty()) continue;
+        SceneSlot& S = *s->scenes[si];
+        cudaStream_t q = S.stream;
+        DK_CUDA(cudaMemcpyAsync(const_cast<dk::DevJob*>(S.wave.jobs), pl.table.data(),
+                                pl.table.size() * sizeof(dk::DevJob), cudaMemcpyHostToDevice, q),
+                "job table upload");
+        dk::Wave W = S.wave;
+        W.job_count = (uint32_t)pl.table.size();
+        W.path_count = pl.table.back().path_begin + pl.table.back().P.path_count;
+        W.pixel_count = pl.table.back().pixel_begin + pl.table.back().P.tile_w * pl.table.back().P.tile_h;
+        DK_CUDA(cudaEventRecord(S.evBegin, q), "cudaEventRecord");
+        auto mark = [](int) { return (int)DK_OK; };
+        uint64_t l = 0;
+        int rc = dk::launchWave(S.scene, W, pl.maxBounces, pl.anyDenoiser, s->grids, q, mark, l);
+        if (rc != DK_OK) return rc;
+        DK_CUDA(cudaEventRecord(S.evEnd, q), "cudaEventRecord");
+        launches += l;
+        paths += W.path_count;
+        jobsInStep += W.job_count;
+        wavesInStep += 1;
+        if (first < 0) first = (int)si;
+    }
+    if (first < 0) return DK_OK;
+    // Busy time of the step: from the first wave's start to the last end.
     float ms = 0;
-    DK_CUDA(cudaEventElapsedTime(&ms, s->evBegin, s->evEnd), "cudaEventElapsedTime");
+    for (size_t si = 0; si < plans.size(); ++si) {
+        if (plans[si].table.empty()) continue;
+        DK_CUDA(cudaEventSynchronize(s->scenes[si]->evEnd), "wave");
+        float e = 0;
+        DK_CUDA(cudaEventElapsedTime(&e, s->scenes[first]->evBegin, s->scenes[si]->evEnd), "cudaEventElapsedTime");
+        ms = std::max(ms, e);
+    }
     {
         std::lock_guard<std::mutex> lk(s->mu);
         double now = s->nowMs();
-        for (size_t k = 0; k < members.size(); ++k) {
-            Job& j = *members[k];
-            j.samplesDone += counts[k];
-            j.waves += 1;
-            if (j.samplesDone >= j.samples) {
-                j.state = DK_JOB_DONE;
-                j.finishMs = now;
-                s->done += 1;
+        for (const Plan& pl : plans)
+            for (size_t k = 0; k < pl.members.size(); ++k) {
+                Job& j = *pl.members[k];
+                j.samplesDone += pl.counts[k];
+                j.waves += 1;
+                if (j.samplesDone >= j.samples) {
+                    j.state = DK_JOB_DONE;
+                    j.finishMs = now;
+                    s->done += 1;
+                }
             }
-        }
-        s->waves += 1;
-        s->paths += W.path_count;
+        s->waves += wavesInStep;
+        s->paths += paths;
         s->launches += launches;
         s->busyMs += ms;
-        s->jobsInWaveSum += (double)table.size();
-        s->jobsInWaveMax = std::max(s->jobsInWaveMax, (double)table.size());
+        s->jobsInWaveSum += (double)jobsInStep;
+        s->jobsInWaveMax = std::max(s->jobsInWaveMax, (double)jobsInStep / wavesInStep);
     }
     s->cv.notify_all();
-    if (outJobs) *outJobs = (uint32_t)table.size();
+    if (outJobs) *outJobs = jobsInStep;
     return DK_OK;
 }
 
@@ -284,7 +367,15 @@ void workerLoop(Server* s) {
     }
 }
 
+// The scene a job names, or null (under mu: the list only grows).
+const SceneSlot* jobScene(Server* s, uint32_t index) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    return index < s->scenes.size() ? s->scenes[index].get() : nullptr;
+}
+
 int validateJob(Server* s, const dk_job_desc* jd) {
+    const SceneSlot* S = jobScene(s, jd->scene);
+    if (!S) return fail(DK_ERROR_INVALID_ARGUMENT, "a job names a scene the server does not hold");
     const dk_settings& st = jd->settings;
     if (st.width == 0 || st.height == 0)
         return fail(DK_ERROR_INVALID_SCENE, "Invalid render scene: Render dimensions must be positive.");
@@ -292,21 +383,21 @@ int validateJob(Server* s, const dk_job_desc* jd) {
         return fail(DK_ERROR_INVALID_ARGUMENT, "only RenderQuality.final (the path tracer) is implemented");
     if (jd->samples == 0) return fail(DK_ERROR_INVALID_ARGUMENT, "a job must render at least one sample");
     uint64_t pixels = (uint64_t)st.width * st.height;
-    if (pixels > s->wave.cap) return fail(DK_ERROR_INVALID_ARGUMENT, "one frame of the job exceeds the wave capacity");
+    if (pixels > S->wave.cap) return fail(DK_ERROR_INVALID_ARGUMENT, "one frame of the job exceeds the wave capacity");
     if (jobBlockBytes(pixels) > s->cfg.hbm_budget_bytes)
         return fail(DK_ERROR_OUT_OF_MEMORY, "the job's buffers exceed the server's HBM budget");
-    if (jd->material_count != s->matCount || !jd->materials)
+    if (jd->material_count != S->matCount || !jd->materials)
         return fail(DK_ERROR_INVALID_ARGUMENT, "a job's material table must have the scene's material count");
-    for (uint32_t i = 0; i < s->matCount; ++i) {
+    for (uint32_t i = 0; i < S->matCount; ++i) {
         const dk_material& m = jd->materials[i];
-        const dk_material& b = s->baseMaterials[i];
+        const dk_material& b = S->baseMaterials[i];
         if (!sameEmission(m, b))
             return fail(DK_ERROR_INVALID_ARGUMENT, "a job may not change a material's emission (the light list is shared)");
         if (i >= 32 && dk::materialBlocksShadow(m) != dk::materialBlocksShadow(b))
             return fail(DK_ERROR_INVALID_ARGUMENT,
                         "a job may not change whether material IDs from 32 up block shadow rays");
         float texB = m.parameters.z, texN = m.parameters.w;
-        if (texB < 0.0f || texN < 0.0f || texB > (float)s->scene.texdesc_count || texN > (float)s->scene.texdesc_count)
+        if (texB < 0.0f || texN < 0.0f || texB > (float)S->scene.texdesc_count || texN > (float)S->scene.texdesc_count)
             return fail(DK_ERROR_INVALID_ARGUMENT, "a job material references a texture the scene does not have");
     }
     return DK_OK;
@@ -336,14 +427,6 @@ int dk_server_create(const dk_scene* sc, const dk_server_config* config, dk_serv
         return fail(DK_ERROR_INVALID_ARGUMENT, "dk_server_config.policy must be 0 or 1");
     }
     s->cfg.wave_paths = std::min<uint32_t>(s->cfg.wave_paths, 1u << 29);  // path indices fit 29 bits
-#define TRY(x)                  \
-    do {                        \
-        int _rc = (x);          \
-        if (_rc != DK_OK) {     \
-            destroyServer(s);   \
-            return _rc;         \
-        }                       \
-    } while (0)
 #define TRY_CUDA(x, what)                                                                          \
     do {                                                                                           \
         cudaError_t _e = (x);                                                                      \
@@ -352,10 +435,7 @@ int dk_server_create(const dk_scene* sc, const dk_server_config* config, dk_serv
             return fail(DK_ERROR_COMMAND_FAILED, std::string(what) + ": " + cudaGetErrorString(_e)); \
         }                                                                                          \
     } while (0)
-    TRY_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     TRY_CUDA(cudaStreamCreateWithFlags(&s->ioStream, cudaStreamNonBlocking), "cudaStreamCreate");
-    TRY_CUDA(cudaEventCreate(&s->evBegin), "cudaEventCreate");
-    TRY_CUDA(cudaEventCreate(&s->evEnd), "cudaEventCreate");
     int device = 0;
     TRY_CUDA(cudaGetDevice(&device), "cudaGetDevice");
     cudaMemPoolProps props;
@@ -366,19 +446,29 @@ int dk_server_create(const dk_scene* sc, const dk_server_config* config, dk_serv
     TRY_CUDA(cudaMemPoolCreate(&s->pool, &props), "cudaMemPoolCreate");
     uint64_t keep = ~0ull;  // keep freed job blocks in the pool for the next admissions
     TRY_CUDA(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
-
-    s->matCount = sc->material_count;
-    s->baseMaterials.assign(sc->materials, sc->materials + sc->material_count);
-    const uint32_t slots = s->cfg.max_resident_jobs;
-    TRY(dk::uploadScene(s->arena, sc, s->scene, (uint32_t)std::min<uint64_t>((uint64_t)(slots + 1) * s->matCount,
-                                                                             0xffffffffull)));
-    s->scene.all_shadow_opaque = 0;  // job tables may make materials cut-out or transmissive
-    for (uint32_t k = slots; k > 0; --k) s->freeSlots.push_back(k - 1);
-    TRY(dk::allocWave(s->arena, s->wave, s->cfg.wave_paths, s->cfg.wave_paths, s->cfg.max_jobs_per_wave));
-    s->grids = dk::kernelGrids();
-#undef TRY
 #undef TRY_CUDA
+    std::unique_ptr<SceneSlot> first;
+    rc = makeSceneSlot(s, sc, first);
+    if (rc != DK_OK) {
+        destroyServer(s);
+        return rc;
+    }
+    s->scenes.push_back(std::move(first));
+    s->grids = dk::kernelGrids();
     *out = reinterpret_cast<dk_server*>(s);
+    return DK_OK;
+}
+
+int dk_server_add_scene(dk_server* server, const dk_scene* sc, uint32_t* outScene) {
+    Server* s = asServer(server);
+    if (!s || !sc || !outScene) return fail(DK_ERROR_INVALID_ARGUMENT, "dk_server_add_scene: null argument");
+    std::unique_ptr<SceneSlot> slot;
+    int rc = makeSceneSlot(s, sc, slot);
+    if (rc != DK_OK) return rc;
+    std::lock_guard<std::mutex> stepLock(s->stepMu);  // no wave reads the list meanwhile
+    std::lock_guard<std::mutex> lk(s->mu);
+    *outScene = (uint32_t)s->scenes.size();
+    s->scenes.push_back(std::move(slot));
     return DK_OK;
 }
 
@@ -388,11 +478,12 @@ int dk_server_submit(dk_server* server, const dk_job_desc* jd, uint64_t* outId) 
     int rc = validateJob(s, jd);
     if (rc != DK_OK) return rc;
     auto j = std::make_unique<Job>();
+    j->scene = jd->scene;
     j->settings = jd->settings;
     if (j->settings.max_bounces < 1) j->settings.max_bounces = 1;
     j->samples = jd->samples;
-    j->materials.assign(jd->materials, jd->materials + s->matCount);
-    j->opaqueMask = dk::opaqueMask(j->materials.data(), s->matCount);
+    j->materials.assign(jd->materials, jd->materials + jd->material_count);
+    j->opaqueMask = dk::opaqueMask(j->materials.data(), jd->material_count);
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->workerError != DK_OK) return fail(s->workerError, "server stopped: " + s->workerMessage);
@@ -572,7 +663,7 @@ int dk_server_release(dk_server* server, uint64_t id) {
         DK_CUDA(cudaFreeAsync(j.block, s->ioStream), "release job buffers");
         j.block = nullptr;
         s->budgetUsed -= j.bytes;
-        s->freeSlots.push_back(j.slot);
+        s->scenes[j.scene]->freeSlots.push_back(j.slot);
         s->running.erase(std::find(s->running.begin(), s->running.end(), j.id));
         j.state = DK_JOB_RELEASED;
         j.materials.clear();
@@ -599,7 +690,9 @@ int dk_server_get_stats(dk_server* server, dk_server_stats* out) {
     out->kernel_launches = s->launches;
     out->budget_used_bytes = s->budgetUsed;
     out->budget_peak_bytes = s->budgetPeak;
-    out->device_bytes = s->arena.bytes + s->budgetUsed;
+    uint64_t sceneBytes = 0;
+    for (const auto& sc : s->scenes) sceneBytes += sc->arena.bytes;
+    out->device_bytes = sceneBytes + s->budgetUsed;
     out->busy_ms = s->busyMs;
     out->max_jobs_in_wave = s->jobsInWaveMax;
     out->mean_jobs_in_wave = s->waves ? s->jobsInWaveSum / (double)s->waves : 0.0;

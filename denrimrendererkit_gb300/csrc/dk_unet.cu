@@ -599,6 +599,235 @@ __global__ void __launch_bounds__(192, 1)
 
 size_t tmaSmemBytes(uint32_t cout) { return (size_t)kTmaStages * (128u * 128u + cout * 128u) + 1024u + 128u; }
 
+// -------------------------------------- tcgen05 + TMA, halo-row ring ----
+// The convolution for wide, shallow layers (the full- and half-resolution
+// levels of the U-Net, where the per-tap kernel above re-reads every input
+// pixel nine times from L2 and waits on it).  An output tile is 128
+// consecutive pixels of one image row; a persistent CTA walks a column of
+// such tiles down `rowBlock` rows and keeps the input rows it needs in a ring
+// of halo rows: one TMA box {64 channels, 130 pixels} per 64-channel chunk
+// and input row, loaded once (zero filled outside the image).  For tap
+// (dy, dx) the MMA's A operand is the 128 rows of halo row y - 1 + dy that
+// start at pixel dx: a contiguous run of 128-byte rows inside the slot, so all
+// nine taps read the same shared-memory rows and each input row crosses L2
+// once per tile column.  The weights of the layer (9 x chunks boxes of
+// {64 channels, Cout}) stay resident in shared memory for the whole launch.
+//   warp 0     TMA producer: the weights once, then the halo rows in order;
+//   warp 1     MMA issuer: per output row 9 taps x chunks x K-steps of
+//              tcgen05.mma M = 128, N = Cout, K = 16 into one of two TMEM
+//              accumulators; releases a halo row once its last reader is done;
+//   warps 2-5  epilogue as in k_conv3x3_tma.
+// Waits are bounded as there.
+constexpr uint32_t kHaloRing = 4;           // halo-row slots
+constexpr uint32_t kHaloPix = 130;          // 128 output pixels and one on each side
+constexpr uint32_t kHaloSlotBytes = 17408;  // 130 rows of 128 B, padded to 17 x 1024 B
+
+struct HaloConvArgs {
+    const float* bias;
+    __nv_bfloat16* out;
+    uint32_t n, h, w, cin, cout, ldo, coOff;
+    uint32_t tilesX, rowBlock, rowBlocks, numItems, chunks, cols;
+    int act, accumulate;
+};
+
+__global__ void __launch_bounds__(192, 1)
+    k_conv3x3_halo(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW,
+                   HaloConvArgs a) {
+    extern __shared__ unsigned char dsm[];
+    const uint32_t raw = smemAddr(dsm);
+    unsigned char* sm = dsm + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t N = a.cout, C = a.chunks;
+    const uint32_t slotBytes = C * kHaloSlotBytes;
+    const uint32_t wBoxBytes = N * 128u, wBytes = 9u * C * wBoxBytes;
+    unsigned char* sRing = sm;
+    unsigned char* sW = sm + kHaloRing * slotBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sW + wBytes);
+    // bars: full[R], empty[R], weights, accFull[2], accEmpty[2]
+    const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kHaloRing;
+    const uint32_t wBar = emptyBar + 8u * kHaloRing, accFullBar = wBar + 8u, accEmptyBar = accFullBar + 16u;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kHaloRing + 5);
+    int* abortFlag = reinterpret_cast<int*>(tslot + 1);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(tslot)),
+                     "r"(2u * a.cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (uint32_t s = 0; s < kHaloRing; ++s) {
+            mbarInit(fullBar + 8u * s, 1);
+            mbarInit(emptyBar + 8u * s, 1);
+        }
+        mbarInit(wBar, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbarInit(accFullBar + 8u * b, 1);
+            mbarInit(accEmptyBar + 8u * b, 128);
+        }
+        *abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(&mapIn) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(&mapW) : "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *tslot;
+    volatile int* abortV = abortFlag;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            mbarExpectTx(wBar, wBytes);
+            for (uint32_t tap = 0; tap < 9u; ++tap)
+                for (uint32_t c = 0; c < C; ++c)
+                    tmaLoad3(smemAddr(sW + (tap * C + c) * wBoxBytes), &mapW, (int)(c * 64u), (int)tap, 0, wBar);
+            uint32_t g = 0;
+            for (uint32_t item = blockIdx.x; item < a.numItems && !*abortV; item += gridDim.x) {
+                const uint32_t tx = item % a.tilesX, rest = item / a.tilesX;
+                const uint32_t rb = rest % a.rowBlocks, img = rest / a.rowBlocks;
+                const int x0 = (int)(tx * 128u), y0 = (int)(rb * a.rowBlock);
+                const int y1 = min((int)a.h, y0 + (int)a.rowBlock);
+                bool ok = true;
+                for (int hy = y0 - 1; hy <= y1; ++hy, ++g) {
+                    const uint32_t s = g % kHaloRing, u = g / kHaloRing;
+                    if (u > 0 && !mbarWait(emptyBar + 8u * s, (u - 1u) & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    mbarExpectTx(fullBar + 8u * s, C * kHaloPix * 128u);
+                    for (uint32_t c = 0; c < C; ++c)
+                        tmaLoad4(smemAddr(sRing + s * slotBytes + c * kHaloSlotBytes), &mapIn, (int)(c * 64u), x0 - 1,
+                                 hy, (int)img, fullBar + 8u * s);
+                }
+                if (!ok) {
+                    *abortV = 1;
+                    break;
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
+            const uint32_t ringBase = smemAddr(sRing), wBase = smemAddr(sW);
+            bool ok = mbarWait(wBar, 0u);
+            uint32_t g = 0, t = 0;
+            for (uint32_t item = blockIdx.x; ok && item < a.numItems && !*abortV; item += gridDim.x) {
+                const uint32_t rest = item / a.tilesX;
+                const uint32_t rb = rest % a.rowBlocks;
+                const uint32_t y0 = rb * a.rowBlock, y1 = min(a.h, y0 + a.rowBlock);
+                const uint32_t rows = y1 - y0;
+                for (uint32_t k = 0; ok && k < rows; ++k, ++t) {
+                    // halo rows g + k .. g + k + 2 feed output row y0 + k
+                    for (uint32_t j = (k == 0 ? 0u : 2u); j < 3u; ++j) {
+                        const uint32_t idx = g + k + j;
+                        if (!mbarWait(fullBar + 8u * (idx % kHaloRing), (idx / kHaloRing) & 1u)) ok = false;
+                    }
+                    const uint32_t b = t & 1u, v = t >> 1;
+                    if (ok && v > 0 && !mbarWait(accEmptyBar + 8u * b, (v - 1u) & 1u)) ok = false;
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t dAddr = taddr + b * a.cols;
+                    uint32_t acc = 0;
+                    for (uint32_t tap = 0; tap < 9u; ++tap) {
+                        const uint32_t dy = tap / 3u, dx = tap - dy * 3u;
+                        const uint32_t slot = (g + k + dy) % kHaloRing;
+                        for (uint32_t c = 0; c < C; ++c) {
+                            const uint32_t aBase = ringBase + slot * slotBytes + c * kHaloSlotBytes + dx * 128u;
+                            const uint32_t bBase = wBase + (tap * C + c) * wBoxBytes;
+                            for (uint32_t ks = 0; ks < 4u; ++ks) {
+                                if (c * 64u + ks * 16u >= a.cin) break;
+                                // A run that starts inside the 1024-byte swizzle pattern
+                                // (pixel dx) takes the plain descriptor: the tensor core
+                                // applies the 128-byte swizzle to absolute shared-memory
+                                // address bits, as the copy engine wrote it (measured:
+                                // a base offset of (start >> 7) & 7 gives wrong sums).
+                                const uint64_t ad = umaDesc(aBase + ks * 32u);
+                                const uint64_t bd = umaDesc(bBase + ks * 32u);
+                                asm volatile(
+                                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dAddr),
+                                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                                acc = 1u;
+                            }
+                        }
+                    }
+                    umaCommit(accFullBar + 8u * b);                      // output row complete
+                    umaCommit(emptyBar + 8u * ((g + k) % kHaloRing));    // its top halo row has no reader left
+                }
+                if (!ok) break;
+                umaCommit(emptyBar + 8u * ((g + rows) % kHaloRing));     // the item's last two halo rows
+                umaCommit(emptyBar + 8u * ((g + rows + 1u) % kHaloRing));
+                g += rows + 2u;
+            }
+            if (!ok) *abortV = 1;
+        }
+    } else {
+        // Epilogue warps 2..5: TMEM lane quarter (warp % 4), one output pixel per thread.
+        const uint32_t q = warp & 3u;
+        const uint32_t r = q * 32u + lane;
+        uint32_t t = 0;
+        bool ok = true;
+        for (uint32_t item = blockIdx.x; ok && item < a.numItems; item += gridDim.x) {
+            const uint32_t tx = item % a.tilesX, rest = item / a.tilesX;
+            const uint32_t rb = rest % a.rowBlocks, img = rest / a.rowBlocks;
+            const uint32_t y0 = rb * a.rowBlock, y1 = min(a.h, y0 + a.rowBlock);
+            const uint32_t px = tx * 128u + r;
+            for (uint32_t py = y0; py < y1; ++py, ++t) {
+                const uint32_t b = t & 1u, v = t >> 1;
+                if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
+                    *abortV = 1;
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const bool valid = px < a.w;
+                __nv_bfloat16* orow = a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff;
+                const uint32_t src = taddr + ((q * 32u) << 16) + b * a.cols;
+                for (uint32_t c0 = 0; c0 < N; c0 += 16u) {
+                    uint32_t rr[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];\n"
+                        : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]),
+                          "=r"(rr[7]), "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]),
+                          "=r"(rr[13]), "=r"(rr[14]), "=r"(rr[15])
+                        : "r"(src + c0));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    if (!valid) continue;
+                    float v2[16];
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        float x = __uint_as_float(rr[k]);
+                        if (a.bias) x += a.bias[c0 + k];
+                        if (a.act == 1) x = fmaxf(x, 0.0f);
+                        v2[k] = x;
+                    }
+                    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(orow + c0);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        float x0v = v2[2 * k], x1v = v2[2 * k + 1];
+                        if (a.accumulate) {
+                            float2 o = __bfloat1622float2(dst[k]);
+                            x0v += o.x;
+                            x1v += o.y;
+                        }
+                        dst[k] = __floats2bfloat162_rn(x0v, x1v);
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                mbarArrive(accEmptyBar + 8u * b);
+            }
+        }
+    }
+    __syncthreads();
+    if (*abortV && tid == 0) atomicExch(&g_unetError, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(2u * a.cols));
+}
+
+size_t haloSmemBytes(uint32_t cout, uint32_t chunks) {
+    return 1024u + (size_t)kHaloRing * chunks * kHaloSlotBytes + 9u * (size_t)chunks * cout * 128u + 128u;
+}
+
 // -------------------------------------------------------------- wgrad ----
 struct WgradArgs {
     const __nv_bfloat16* in;    // [M][ldi], channels [0, cin)
@@ -873,9 +1102,11 @@ __global__ void k_pack_input(const float4* beauty, const float4* albedo, const f
 }
 
 // L1 loss in log space against a target image (RGBA32F) and its gradient
-// (scaled by 1 / (3 * pixels)) into the prediction's first 3 channels.
-__global__ void k_l1_loss(const __nv_bfloat16* pred, uint32_t ldp, const float4* target, uint32_t M,
-                          __nv_bfloat16* grad, uint32_t ldg, float* loss) {
+// (scaled by 1 / (3 * pixels)) into the prediction's first 3 channels.  With
+// `base` (the network input, whose first 3 channels are log(1 + noisy)), the
+// prediction is a residual: the output is base + pred.
+__global__ void k_l1_loss(const __nv_bfloat16* pred, uint32_t ldp, const __nv_bfloat16* base, uint32_t ldb,
+                          const float4* target, uint32_t M, __nv_bfloat16* grad, uint32_t ldg, float* loss) {
     __shared__ float red[256];
     float s = 0.0f;
     const float scale = 1.0f / (3.0f * (float)M);
@@ -885,7 +1116,9 @@ __global__ void k_l1_loss(const __nv_bfloat16* pred, uint32_t ldp, const float4*
         float g[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            float d = __bfloat162float(pred[(size_t)p * ldp + k]) - tl[k];
+            float y = __bfloat162float(pred[(size_t)p * ldp + k]);
+            if (base) y += __bfloat162float(base[(size_t)p * ldb + k]);
+            float d = y - tl[k];
             s += fabsf(d);
             g[k] = (d > 0.0f ? scale : (d < 0.0f ? -scale : 0.0f));
         }
@@ -904,16 +1137,26 @@ __global__ void k_l1_loss(const __nv_bfloat16* pred, uint32_t ldp, const float4*
     if (threadIdx.x == 0) atomicAdd(loss, red[0] * scale);
 }
 
-// Network output (log space, first 3 channels) to an RGBA32F image; alpha from `alphaSrc`.
-__global__ void k_unpack_output(const __nv_bfloat16* pred, uint32_t ldp, uint32_t h, uint32_t w, const float4* alphaSrc,
-                                uint32_t imgW, uint32_t imgH, uint32_t x0, uint32_t y0, float4* out) {
+// Network output (log space, first 3 channels) to an RGBA32F image; alpha from
+// `alphaSrc`.  With `base`: the output is base + pred (a residual over the
+// network input's log(1 + noisy) channels), summed in FP32.
+__global__ void k_unpack_output(const __nv_bfloat16* pred, uint32_t ldp, const __nv_bfloat16* base, uint32_t ldb,
+                                uint32_t h, uint32_t w, const float4* alphaSrc, uint32_t imgW, uint32_t imgH,
+                                uint32_t x0, uint32_t y0, float4* out) {
     for (uint32_t i = gid(); i < h * w; i += gstride()) {
         uint32_t ix = x0 + i % w, iy = y0 + i / w;
         if (ix >= imgW || iy >= imgH) continue;
         size_t s = (size_t)iy * imgW + ix;
         const __nv_bfloat16* p = pred + (size_t)i * ldp;
-        out[s] = make_float4(fmaxf(expm1f(__bfloat162float(p[0])), 0.0f), fmaxf(expm1f(__bfloat162float(p[1])), 0.0f),
-                             fmaxf(expm1f(__bfloat162float(p[2])), 0.0f), alphaSrc[s].w);
+        float y[3] = {__bfloat162float(p[0]), __bfloat162float(p[1]), __bfloat162float(p[2])};
+        if (base) {
+            const __nv_bfloat16* b = base + (size_t)i * ldb;
+            y[0] += __bfloat162float(b[0]);
+            y[1] += __bfloat162float(b[1]);
+            y[2] += __bfloat162float(b[2]);
+        }
+        out[s] = make_float4(fmaxf(expm1f(y[0]), 0.0f), fmaxf(expm1f(y[1]), 0.0f), fmaxf(expm1f(y[2]), 0.0f),
+                             alphaSrc[s].w);
     }
 }
 
@@ -959,9 +1202,10 @@ inline int gridFor(uint64_t work, int block = 256) {
 
 inline bool aligned16(uint32_t v) { return v % 16u == 0u; }
 
-// 2: persistent TMA + tcgen05 convolution (default), 1: the cp.async +
-// tcgen05 one, 0: the mma.sync one.
-int g_convPath = 2;
+// 3: halo-row TMA + tcgen05 convolution where the layer fits it, else the
+// per-tap one (default); 2: the per-tap persistent TMA + tcgen05 convolution;
+// 1: the cp.async + tcgen05 one; 0: the mma.sync one.
+int g_convPath = 3;
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // dependency on libcuda).
@@ -980,6 +1224,67 @@ EncodeTiledFn encodeTiled() {
             fn = reinterpret_cast<EncodeTiledFn>(p);
     }
     return fn;
+}
+
+// The halo-row kernel's launch, or kHaloUnfit (nothing launched) when the
+// layer does not fit it: narrow images, or weights and halo ring beyond the
+// shared memory of one CTA.
+constexpr int kHaloUnfit = -1;
+int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
+    const uint32_t chunks = (c.cin + 63u) / 64u;
+    const size_t smem = haloSmemBytes(c.cout, chunks);
+    if (c.w_ < 128u || c.cout > 256u || smem > (size_t)deviceProp().sharedMemPerBlockOptin) return kHaloUnfit;
+    EncodeTiledFn enc = encodeTiled();
+    if (!enc) return fail(DK_ERROR_COMMAND_FAILED, "cuTensorMapEncodeTiled is not available");
+    HaloConvArgs a;
+    a.bias = c.bias;
+    a.out = c.out;
+    a.n = c.n;
+    a.h = c.h;
+    a.w = c.w_;
+    a.cin = c.cin;
+    a.cout = c.cout;
+    a.ldo = c.ldo;
+    a.coOff = c.coOff;
+    a.act = c.act;
+    a.accumulate = c.accumulate;
+    a.chunks = chunks;
+    a.cols = 32u;
+    while (a.cols < c.cout) a.cols <<= 1;
+    a.tilesX = (c.w_ + 127u) / 128u;
+    const uint32_t sms = (uint32_t)deviceProp().multiProcessorCount;
+    // About four items per CTA: enough to balance, few halo rows re-read.
+    const uint64_t rowsTotal = (uint64_t)c.n * a.tilesX * c.h;
+    uint64_t rb = (rowsTotal + 4u * sms - 1u) / (4u * sms);
+    a.rowBlock = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(rb, 2u), c.h);
+    a.rowBlocks = (c.h + a.rowBlock - 1u) / a.rowBlock;
+    a.numItems = c.n * a.tilesX * a.rowBlocks;
+    alignas(64) CUtensorMap mapIn, mapW;
+    cuuint64_t dimIn[4] = {c.cin, c.w_, c.h, c.n};
+    cuuint64_t strideIn[3] = {(cuuint64_t)c.ldi * 2u, (cuuint64_t)c.w_ * c.ldi * 2u, (cuuint64_t)c.h * c.w_ * c.ldi * 2u};
+    cuuint32_t boxIn[4] = {64u, kHaloPix, 1u, 1u};
+    cuuint32_t unit[4] = {1u, 1u, 1u, 1u};
+    CUresult r = enc(&mapIn, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(c.in), dimIn, strideIn,
+                     boxIn, unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "activation tensor map rejected");
+    cuuint64_t dimW[3] = {c.cin, 9u, c.cout};
+    cuuint64_t strideW[2] = {(cuuint64_t)c.cin * 2u, (cuuint64_t)9u * c.cin * 2u};
+    cuuint32_t boxW[3] = {64u, 1u, c.cout};
+    r = enc(&mapW, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(c.w), dimW, strideW, boxW, unit,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "weight tensor map rejected");
+    static size_t configured = 0;
+    if (smem > configured) {
+        DK_CUDA(cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                "conv3x3 (halo) shared memory");
+        configured = smem;
+    }
+    uint32_t grid = std::min(sms, a.numItems);
+    k_conv3x3_halo<<<grid, 192, smem, st>>>(mapIn, mapW, a);
+    DK_CUDA(cudaGetLastError(), "conv3x3 (halo rows, TMA + tcgen05) launch");
+    return DK_OK;
 }
 
 int launchConvTma(const ConvArgs& c, cudaStream_t st) {
@@ -1058,7 +1363,11 @@ int dk_unet_conv3x3(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t
     dk::ConvArgs a{static_cast<const bf16*>(in), static_cast<const bf16*>(weight), bias, static_cast<bf16*>(out),
                    n, h, w, cin, ldi, cout, ldo, coOff, (uint32_t)M, act, accumulate};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (dk::g_convPath == 2 && cout <= 256u) {
+    if (dk::g_convPath == 3 && cout <= 256u) {
+        int rc = dk::launchConvHalo(a, st);
+        if (rc != dk::kHaloUnfit) return rc;
+    }
+    if (dk::g_convPath >= 2 && cout <= 256u) {
         int rc = dk::launchConvTma(a, st);
         if (rc != DK_OK) return rc;
         return DK_OK;
@@ -1201,8 +1510,19 @@ int dk_unet_l1_loss(const void* pred, uint32_t ldp, const float* target, uint32_
     if (!pred || !target || !grad || !loss || ldp < 3u || ldg < 3u)
         return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_l1_loss");
     dk::k_l1_loss<<<dk::gridFor(pixels), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const bf16*>(pred), ldp, reinterpret_cast<const float4*>(target), pixels, static_cast<bf16*>(grad),
-        ldg, loss);
+        static_cast<const bf16*>(pred), ldp, nullptr, 0u, reinterpret_cast<const float4*>(target), pixels,
+        static_cast<bf16*>(grad), ldg, loss);
+    DK_CUDA(cudaGetLastError(), "loss launch");
+    return DK_OK;
+}
+
+int dk_unet_l1_loss_residual(const void* pred, uint32_t ldp, const void* base, uint32_t ldb, const float* target,
+                             uint32_t pixels, void* grad, uint32_t ldg, float* loss, void* stream) {
+    if (!pred || !base || !target || !grad || !loss || ldp < 3u || ldb < 3u || ldg < 3u)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_l1_loss_residual");
+    dk::k_l1_loss<<<dk::gridFor(pixels), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(pred), ldp, static_cast<const bf16*>(base), ldb,
+        reinterpret_cast<const float4*>(target), pixels, static_cast<bf16*>(grad), ldg, loss);
     DK_CUDA(cudaGetLastError(), "loss launch");
     return DK_OK;
 }
@@ -1211,8 +1531,20 @@ int dk_unet_unpack_output(const void* pred, uint32_t ldp, uint32_t h, uint32_t w
                           uint32_t imgH, uint32_t x0, uint32_t y0, float* out, void* stream) {
     if (!pred || !alphaSrc || !out) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_unpack_output");
     dk::k_unpack_output<<<dk::gridFor((uint64_t)h * w), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const bf16*>(pred), ldp, h, w, reinterpret_cast<const float4*>(alphaSrc), imgW, imgH, x0, y0,
-        reinterpret_cast<float4*>(out));
+        static_cast<const bf16*>(pred), ldp, nullptr, 0u, h, w, reinterpret_cast<const float4*>(alphaSrc), imgW, imgH,
+        x0, y0, reinterpret_cast<float4*>(out));
+    DK_CUDA(cudaGetLastError(), "unpack output launch");
+    return DK_OK;
+}
+
+int dk_unet_unpack_output_residual(const void* pred, uint32_t ldp, const void* base, uint32_t ldb, uint32_t h,
+                                   uint32_t w, const float* alphaSrc, uint32_t imgW, uint32_t imgH, uint32_t x0,
+                                   uint32_t y0, float* out, void* stream) {
+    if (!pred || !base || !alphaSrc || !out || ldb < 3u)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_unpack_output_residual");
+    dk::k_unpack_output<<<dk::gridFor((uint64_t)h * w), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(pred), ldp, static_cast<const bf16*>(base), ldb, h, w,
+        reinterpret_cast<const float4*>(alphaSrc), imgW, imgH, x0, y0, reinterpret_cast<float4*>(out));
     DK_CUDA(cudaGetLastError(), "unpack output launch");
     return DK_OK;
 }
@@ -1230,7 +1562,7 @@ int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t
 }
 
 int dk_unet_set_conv_path(int path) {
-    if (path < 0 || path > 2) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_set_conv_path: 0, 1 or 2");
+    if (path < 0 || path > 3) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_set_conv_path: 0, 1, 2 or 3");
     dk::g_convPath = path;
     return DK_OK;
 }

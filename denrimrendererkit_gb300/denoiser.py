@@ -11,6 +11,8 @@ nearest upsampling, skip concatenation.  Activations are NHWC bf16, weights
 FP32 masters with bf16 copies, FP32 accumulation; every convolution, its
 input and weight gradients, the pooling/upsampling and their gradients, the
 loss and Adam run in the library.  PyTorch only owns the device buffers.
+The network predicts a residual over the input's log(1 + noisy) channels,
+composed in FP32 when the image is written (`UNet.residual`).
 """
 from __future__ import annotations
 
@@ -93,10 +95,15 @@ def flops_per_pixel() -> float:
 class UNet:
     """The network, its optimiser state and its activation buffers."""
 
-    def __init__(self, seed: int = 0, device: str = "cuda", stream=None):
+    def __init__(self, seed: int = 0, device: str = "cuda", stream=None, residual: bool = True):
         torch = _torch()
         self.lib = library.load()
         self.device = device
+        # The output is a residual over the input's log(1 + noisy) channels
+        # (summed in FP32 when the image is written), so converged pixels --
+        # visible lights -- keep their value instead of the bf16 activations'
+        # 3 significant digits; False predicts log(1 + radiance) directly.
+        self.residual = residual
         self.layers = layer_plan()
         self.by_name = {l.name: l for l in self.layers}
         g = torch.Generator().manual_seed(seed)
@@ -305,6 +312,11 @@ class UNet:
         """L1 in log space against `target` (N*H*W RGBA32F, device); the mean
         is added to grad_buffers()['loss']."""
         B = self.grad_buffers(n, h, w)
+        if self.residual:
+            self._check(self.lib.dk_unet_l1_loss_residual(_ptr(B["pred"]), OUT_CH, _ptr(B["x"]), IN_CH, _ptr(target),
+                                                          n * h * w, _ptr(B["g_pred"]), OUT_CH, _ptr(B["loss"]),
+                                                          self._st))
+            return
         self._check(self.lib.dk_unet_l1_loss(_ptr(B["pred"]), OUT_CH, _ptr(target), n * h * w, _ptr(B["g_pred"]),
                                              OUT_CH, _ptr(B["loss"]), self._st))
 
@@ -331,8 +343,15 @@ class UNet:
         w = (img_w + 15) // 16 * 16
         self.pack(beauty, albedo, normal, depth, img_w, img_h, 0, 0, 1, h, w, 0)
         B = self.forward(1, h, w)
-        self._check(self.lib.dk_unet_unpack_output(_ptr(B["pred"]), OUT_CH, h, w, _ptr(beauty), img_w, img_h, 0, 0,
-                                                   _ptr(out), self._st))
+        self._unpack(B["pred"], B["x"], h, w, beauty, img_w, img_h, out)
+
+    def _unpack(self, pred, x, h, w, beauty, img_w, img_h, out) -> None:
+        if self.residual:
+            self._check(self.lib.dk_unet_unpack_output_residual(_ptr(pred), OUT_CH, _ptr(x), IN_CH, h, w, _ptr(beauty),
+                                                                img_w, img_h, 0, 0, _ptr(out), self._st))
+        else:
+            self._check(self.lib.dk_unet_unpack_output(_ptr(pred), OUT_CH, h, w, _ptr(beauty), img_w, img_h, 0, 0,
+                                                       _ptr(out), self._st))
 
     def denoise_batch(self, beauty, albedo, normal, depth, img_w: int, img_h: int, out) -> None:
         """Denoises n images of one size as one batch: every argument is a
@@ -345,8 +364,7 @@ class UNet:
             self.pack(beauty[i], albedo[i], normal[i], depth[i], img_w, img_h, 0, 0, n, h, w, i)
         B = self.forward(n, h, w)
         for i in range(n):
-            self._check(self.lib.dk_unet_unpack_output(_ptr(B["pred"][i]), OUT_CH, h, w, _ptr(beauty[i]), img_w,
-                                                       img_h, 0, 0, _ptr(out[i]), self._st))
+            self._unpack(B["pred"][i], B["x"][i], h, w, beauty[i], img_w, img_h, out[i])
 
 
 class GraphedDenoiser:
@@ -556,3 +574,165 @@ def display_relative_rmse(image, reference) -> float:
     torch = _torch()
     a, b = display(image), display(reference)
     return float(torch.sqrt(((a - b) ** 2).mean()) / b.mean())
+
+
+# ------------------------------------------------------ error estimate ---
+@dataclasses.dataclass
+class ErrorEstimate:
+    """Estimated relative RMSE (linear RGB, over the image's mean) of one
+    image's denoised full render dF and of its plain full render F."""
+    denoised: float
+    noise: float     # the variance part of `denoised`
+    bias: float      # the bias part of `denoised`
+    plain: float
+
+
+def estimate_errors(half_a, half_b, full, den_a, den_b, den_full, stream=None,
+                    display: bool = False) -> List[ErrorEstimate]:
+    """Per-image error estimates from two independent half-sample renders A and
+    B, their full render F = (A + B) / 2 and the three denoised images (device
+    tensors (n, H, W, 4) or (H, W, 4) float32), with no reference image:
+
+    * noise: the denoised output's variance, Var(dF) ~ E|dA - dB|^2 / 4 (A and
+      B carry half the samples each, so each has twice F's variance);
+    * bias: what the denoiser changes beyond F's own noise, E|F - dF|^2 -
+      Var(F), with Var(F) ~ E|A - B|^2 / 4 (clamped at zero);
+    * plain: F's own error, sqrt(Var(F)) -- unbiased, the progressive
+      renderer's estimate.
+    `display`: the same on the displayed images (the reference's PNG tone
+    curve, as `display_relative_rmse` measures).  The sums run on the device
+    (dk_denoise_error_terms)."""
+    torch = _torch()
+    lib = library.load()
+    t = [x if x.dim() == 4 else x.unsqueeze(0) for x in (half_a, half_b, full, den_a, den_b, den_full)]
+    n, h, w = t[0].shape[0], t[0].shape[1], t[0].shape[2]
+    for x in t:
+        if not (x.is_cuda and x.dtype == torch.float32 and x.is_contiguous() and tuple(x.shape) == (n, h, w, 4)):
+            raise ValueError("estimate_errors needs contiguous float32 CUDA tensors of one shape (n, H, W, 4)")
+    terms = torch.empty(n, 5, dtype=torch.float64, device=t[0].device)
+    library.check(lib.dk_denoise_error_terms(*(_ptr(x) for x in t), h * w, n, 1 if display else 0, _ptr(terms),
+                                             None if stream is None else C.c_void_p(stream)))
+    out = []
+    m = 3.0 * h * w
+    for dd, nn, fd, sd, sf in terms.cpu().numpy().tolist():
+        var_dn = dd / (4.0 * m)
+        var_f = nn / (4.0 * m)
+        bias2 = max(0.0, fd / m - var_f)
+        mean_d = max(sd / m, 1e-12)
+        mean_f = max(sf / m, 1e-12)
+        out.append(ErrorEstimate(denoised=math.sqrt(var_dn + bias2) / mean_d, noise=math.sqrt(var_dn) / mean_d,
+                                 bias=math.sqrt(bias2) / mean_d, plain=math.sqrt(var_f) / mean_f))
+    return out
+
+
+def average_planes(a, b, out, stream=None) -> None:
+    """out = (a + b) / 2 on the device (dk_average_planes); tensors of one size."""
+    library.check(library.load().dk_average_planes(_ptr(a), _ptr(b), _ptr(out), a.numel() // 4,
+                                                   None if stream is None else C.c_void_p(stream)))
+
+
+@dataclasses.dataclass
+class ServedImage:
+    """One request of `serve_to_error_target`: the image returned, the samples
+    it took, its last estimate, and whether it is the denoised image or the
+    plain render (the fallback)."""
+    image: object
+    spp: int
+    estimate: ErrorEstimate
+    denoised: bool
+    rounds: int
+
+
+def serve_to_error_target(server, net: "UNet", requests, width: int, height: int, target: float = 0.02,
+                          start_spp: int = 16, max_spp: int = 8192, denoise: bool = True,
+                          seed_base: int = 0x51ED, display: bool = True) -> List[ServedImage]:
+    """Renders each request (settings, camera, materials or None, scene index)
+    through the render server until its estimated relative RMSE is at most
+    `target`, and returns the images.
+
+    Round 0 renders two independent halves A and B of `start_spp` samples per
+    request (two jobs with different frame seeds, packed into the same waves
+    as every other request's); F = (A + B) / 2.  With `denoise`, the U-Net
+    denoises A, B and F of every open request as one batch and
+    `estimate_errors` judges dF without a reference: a request whose
+    estimate is within the target returns dF.  Otherwise -- and always without
+    `denoise` -- F returns once its own (unbiased) estimate is within the
+    target.  A request that meets neither doubles its samples: F becomes the
+    next A, a new render of as many samples the next B.  At `max_spp` the
+    plain render returns (the fallback) whatever its estimate.  `display`:
+    the error is that of the displayed images (the reference's PNG tone
+    curve), else of the linear radiance."""
+    torch = _torch()
+    import dataclasses as dc
+    from .renderer import RenderOutput
+    n = len(requests)
+    shape = (height, width, 4)
+    st0 = [r[0] for r in requests]
+    open_ = list(range(n))
+    full = [None] * n          # F of each request (device tensor)
+    spp = [0] * n
+    aov = [None] * n           # albedo, normal, depth of each request
+    result: List[Optional[ServedImage]] = [None] * n
+    rounds = 0
+    seed = [seed_base + 7919 * k for k in range(n)]
+
+    def submit(k, samples, s):
+        settings, camera, materials, scene = requests[k]
+        st = dc.replace(settings, frame_seed=s & 0x7FFFFFFF)
+        return server.submit(st, camera, samples, materials, scene=scene)
+
+    while open_:
+        # jobs of this round: round 0 two halves per request, later one
+        jobs = {}
+        for k in open_:
+            if spp[k] == 0:
+                jobs[k] = (submit(k, start_spp // 2, seed[k]), submit(k, start_spp // 2, seed[k] + 1))
+                seed[k] += 2
+            else:
+                jobs[k] = (None, submit(k, spp[k], seed[k]))
+                seed[k] += 1
+        while server.step():
+            pass
+        m = len(open_)
+        A = torch.empty((m,) + shape, device="cuda")
+        B = torch.empty_like(A)
+        F = torch.empty_like(A)
+        for i, k in enumerate(open_):
+            ja, jb = jobs[k]
+            if ja is None:
+                A[i].copy_(full[k])
+            else:
+                server.copy_output(ja, RenderOutput.BEAUTY, A[i])
+                aov[k] = [server.copy_output(ja, kind, torch.empty(shape, device="cuda"))
+                          for kind in (RenderOutput.ALBEDO, RenderOutput.NORMAL, RenderOutput.DEPTH)]
+                server.release(ja)
+            server.copy_output(jb, RenderOutput.BEAUTY, B[i])
+            server.release(jb)
+        average_planes(A, B, F)
+        for i, k in enumerate(open_):
+            spp[k] = start_spp if spp[k] == 0 else 2 * spp[k]
+        if denoise:
+            al = torch.stack([aov[k][0] for k in open_]).repeat(3, 1, 1, 1).contiguous()
+            no = torch.stack([aov[k][1] for k in open_]).repeat(3, 1, 1, 1).contiguous()
+            de = torch.stack([aov[k][2] for k in open_]).repeat(3, 1, 1, 1).contiguous()
+            noisy = torch.cat([A, B, F]).contiguous()
+            den = torch.empty_like(noisy)
+            net.denoise_batch(noisy, al, no, de, width, height, den)
+            dA, dB, dF = den[:m], den[m:2 * m], den[2 * m:]
+        else:
+            dA, dB, dF = A, B, F
+        est = estimate_errors(A.contiguous(), B.contiguous(), F, dA.contiguous(), dB.contiguous(), dF.contiguous(),
+                              display=display)
+        rounds += 1
+        still = []
+        for i, k in enumerate(open_):
+            e = est[i]
+            if denoise and e.denoised <= target:
+                result[k] = ServedImage(dF[i].clone(), spp[k], e, True, rounds)
+            elif e.plain <= target or spp[k] >= max_spp:
+                result[k] = ServedImage(F[i].clone(), spp[k], e, False, rounds)
+            else:
+                full[k] = F[i].clone()
+                still.append(k)
+        open_ = still
+    return result

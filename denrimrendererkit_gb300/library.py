@@ -78,7 +78,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_sparse_volume_view": (i32, [P, C.POINTER(abi.Scene)]),
             "dk_sparse_volume_destroy": (i32, [P]),
             "dk_version": (C.c_char_p, []),
+            "dk_probe_bandwidth": (i32, [C.c_uint64, u32, C.POINTER(C.c_double), P]),
             "dk_server_create": (i32, [C.POINTER(abi.Scene), C.POINTER(abi.ServerConfig), C.POINTER(P)]),
+            "dk_server_add_scene": (i32, [P, C.POINTER(abi.Scene), C.POINTER(u32)]),
             "dk_server_submit": (i32, [P, C.POINTER(abi.JobDesc), C.POINTER(C.c_uint64)]),
             "dk_server_step": (i32, [P, C.POINTER(u32)]),
             "dk_server_start": (i32, [P]),
@@ -92,6 +94,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_server_get_stats": (i32, [P, C.POINTER(abi.ServerStats)]),
             "dk_server_destroy": (i32, [P]),
             "dk_denoise_spatial": (i32, [P, P, P, P, P, P, u32, u32, C.POINTER(abi.SpatialDenoiseSettings), P]),
+            "dk_denoise_error_terms": (i32, [P, P, P, P, P, P, u32, u32, u32, P, P]),
+            "dk_average_planes": (i32, [P, P, P, sz, P]),
             "dk_svgf_create": (i32, [u32, u32, P]),
             "dk_svgf_reset": (i32, [P]),
             "dk_svgf_denoise": (i32, [P, P, P, P, P, P, C.POINTER(abi.SpatialDenoiseSettings), P]),
@@ -111,6 +115,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_unet_pack_input": (i32, [P, P, P, P, u32, u32, u32, u32, P, u32, u32, u32, P]),
             "dk_unet_l1_loss": (i32, [P, u32, P, u32, P, u32, P, P]),
             "dk_unet_unpack_output": (i32, [P, u32, u32, u32, P, u32, u32, u32, u32, P, P]),
+            "dk_unet_l1_loss_residual": (i32, [P, u32, P, u32, P, u32, P, u32, P, P]),
+            "dk_unet_unpack_output_residual": (i32, [P, u32, P, u32, u32, u32, P, u32, u32, u32, u32, P, P]),
             "dk_unet_adam": (i32, [P, P, P, P, u32, C.c_float, C.c_float, C.c_float, C.c_float, u32, P, P, u32, u32,
                                    P]),
             "dk_unet_weights_to_bf16": (i32, [P, u32, P, P, u32, u32, P]),
@@ -174,14 +180,31 @@ def build_environment_samples(texture, intensity: float, max_radiance: float) ->
     return out[: count.value].copy()
 
 
+class _VolumeHandle:
+    """Owns a dk_sparse_volume; destroyed when the last array viewing it goes."""
+
+    def __init__(self, handle: C.c_void_p):
+        self.handle = handle
+
+    def __del__(self):
+        try:
+            if self.handle:
+                load().dk_sparse_volume_destroy(self.handle)
+                self.handle = C.c_void_p()
+        except Exception:
+            pass
+
+
 class SparseVolume:
     """A sparse distance volume built by dk_bake_sparse_sphere_volume on the GPU
     (`on_device` None: when a CUDA device is present) or by the host build
     dk_build_sparse_sphere_volume (the two are bit-identical); the arrays are
-    numpy views of the library-owned buffers (valid while this object lives)."""
+    numpy views of the library-owned buffers, each of which keeps them alive.
+    `fp16_distances` stores every sample distance rounded to half precision
+    (the renderer then marches over 2-byte samples)."""
 
     def __init__(self, spheres, resolution, bounds_min, bounds_max, brick_size, narrow_band, volume_material=0,
-                 object_id=0, primitive_id=0, on_device=None):
+                 object_id=0, primitive_id=0, on_device=None, fp16_distances=False):
         lib = load()
         if on_device is None:
             n = C.c_int(0)
@@ -200,16 +223,22 @@ class SparseVolume:
         st.narrow_band = narrow_band
         st.volume_material = volume_material
         st.object_id, st.primitive_id = object_id, primitive_id
-        self._h = C.c_void_p()
+        st.fp16_distances = 1 if fp16_distances else 0
         build = lib.dk_bake_sparse_sphere_volume if on_device else lib.dk_build_sparse_sphere_volume
-        check(build(arr, len(spheres), C.byref(st), C.byref(self._h)))
+        handle = C.c_void_p()
+        check(build(arr, len(spheres), C.byref(st), C.byref(handle)))
+        self._owner = _VolumeHandle(handle)
         view = abi.Scene()
-        check(lib.dk_sparse_volume_view(self._h, C.byref(view)))
+        check(lib.dk_sparse_volume_view(handle, C.byref(view)))
+        owner = self._owner
 
         def arr_of(ptr, count, dtype):
             if not count:
                 return np.zeros(0, dtype)
             buf = (C.c_uint8 * (count * dtype.itemsize)).from_address(ptr)
+            # Every view holds the library handle: the buffers stay alive
+            # while any array over them does, even after this object is gone.
+            buf._owner = owner
             return np.frombuffer(buf, dtype=dtype, count=count)
 
         self.volumes = arr_of(view.volumes, view.volume_count, abi.VOLUME_DTYPE)
@@ -218,9 +247,9 @@ class SparseVolume:
         self.grids = arr_of(view.volume_brick_grids, view.volume_brick_grid_count, abi.BRICK_GRID_DTYPE)
         self.grid_indices = arr_of(view.volume_brick_grid_indices, view.volume_brick_grid_index_count, np.dtype(np.uint32))
 
-    def __del__(self):
-        try:
-            if self._h:
-                load().dk_sparse_volume_destroy(self._h)
-        except Exception:
-            pass
+
+def probe_bandwidth(nbytes: int, passes: int = 20) -> float:
+    """dk_probe_bandwidth: measured read GB/s over an `nbytes` buffer (L2-sized or HBM-sized)."""
+    out = C.c_double(0.0)
+    check(load().dk_probe_bandwidth(int(nbytes), int(passes), C.byref(out), None))
+    return out.value

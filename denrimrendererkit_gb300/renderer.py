@@ -105,6 +105,10 @@ class RenderSettings:
     collects_traversal_stats: bool = False
     frame_seed: int = 0x1234ABCD  # RenderSession.swift:917
     max_samples_per_launch: int = 0
+    # Ray-triangle test: False is the reference's Moller-Trumbore (bit-exact
+    # parity); True the watertight test (Woop, Benthin and Wald 2013), which no
+    # ray slips through at a shared edge or vertex.
+    watertight: bool = False
 
     @property
     def resolved_sample_radiance_clamp(self) -> float:
@@ -131,6 +135,7 @@ def make_settings_struct(settings: RenderSettings, camera: Camera) -> abi.Settin
     prev = settings.previous_camera
     s.previous_camera = s.camera if prev is None or prev is camera else prev.gpu_camera(settings.width, settings.height)
     s.max_samples_per_launch = settings.max_samples_per_launch
+    s.triangle_test = 1 if settings.watertight else 0
     return s
 
 

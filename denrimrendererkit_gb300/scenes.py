@@ -187,13 +187,14 @@ def spheres_large(width: int = 1920, height: int = 1080, samples: int = 64, seed
 
 
 def sdf_spheres(width: int = 1024, height: int = 1024, samples: int = 16, resolution: int = 768, seed: int = 5,
-                narrow_band: float = 0.012) -> Workload:
+                narrow_band: float = 0.012, fp16: bool = True) -> Workload:
     """The sparse-SDF configuration: 32 seeded spheres (radii U[0.03, 0.15],
     centres in [-0.85, 0.85]^3) joined by a polynomial smooth union (k = 0.05),
     baked into a `resolution`^3 virtual grid over [-1, 1]^3 with 8^3-sample
     bricks; a narrow band of 0.012 keeps 3.0% of the 96^3 bricks at 768^3.
-    Spheres alternate a diffuse and a GGX metal material; lit by the default
-    sky.  1024x1024, 16 spp."""
+    Distances stored as FP16 (`fp16`; False keeps FP32).  Spheres alternate a
+    diffuse and a GGX metal material; lit by the default sky.  1024x1024,
+    16 spp."""
     from .library import SparseVolume
     rng = np.random.default_rng(seed)
     scene = RenderScene(camera=Camera((0.0, 0.9, 3.1), (0.0, 0.0, 0.0), vertical_field_of_view_degrees=40.0))
@@ -202,10 +203,11 @@ def sdf_spheres(width: int = 1024, height: int = 1024, samples: int = 16, resolu
     spheres = [dict(center=rng.uniform(-0.85, 0.85, 3), radius=float(rng.uniform(0.03, 0.15)),
                     material=(diffuse if i % 2 == 0 else metal), smooth_union_radius=0.05) for i in range(32)]
     vol = SparseVolume(spheres, (resolution,) * 3, (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0), (8, 8, 8), narrow_band,
-                       volume_material=diffuse, object_id=0, primitive_id=0)
+                       volume_material=diffuse, object_id=0, primitive_id=0, fp16_distances=fp16)
     scene.sparse_volumes.append(vol)
     settings = RenderSettings(width=width, height=height, max_bounces=8, quality=RenderQuality.FINAL, frame_seed=1)
-    return Workload(f"sdf-spheres-{resolution}^3-{width}x{height}-{samples}spp", scene, settings, samples)
+    return Workload(f"sdf-spheres-{resolution}^3-{width}x{height}-{samples}spp-{'fp16' if fp16 else 'fp32'}", scene,
+                    settings, samples)
 
 
 def _checker(width: int, height: int, a, b, cells: int = 8) -> Texture2D:

@@ -1,4 +1,4 @@
-"""Serving: a persistent request loop over one resident scene (dk_server_*).
+"""Serving: a persistent request loop over resident scenes (dk_server_*).
 
 The reference renders one scene per `RenderSession`
 (Sources/DenrimRendererKit/Renderer/RenderSession.swift); its CLI renders one
@@ -7,6 +7,8 @@ Sources/DenrimCLI/main.swift:133-163).  `RenderServer` keeps a preview scene
 resident and renders many such jobs at once: each job brings its own
 settings, camera, sample count and material table over the shared geometry,
 and the server packs every admitted job's paths into one wavefront per wave.
+More scenes can be made resident (`add_scene`); jobs name theirs, and each
+step runs one packed wave per scene with work, overlapping on the device.
 """
 from __future__ import annotations
 
@@ -65,7 +67,7 @@ def material_table(materials: Sequence[Material]) -> np.ndarray:
 
 
 class RenderServer:
-    """A compiled scene resident on the GPU serving render jobs."""
+    """Compiled scenes resident on the GPU serving render jobs."""
 
     def __init__(self, build: AccelerationBuild, config: Optional[ServerConfig] = None):
         self._lib = library.load()
@@ -75,17 +77,29 @@ class RenderServer:
         scene_struct = build.as_struct()
         cfg = self.config.as_struct()
         library.check(self._lib.dk_server_create(C.byref(scene_struct), C.byref(cfg), C.byref(self._handle)))
+        self._builds = [build]
         self._jobs = {}
 
+    def add_scene(self, build: AccelerationBuild) -> int:
+        """Makes another compiled scene resident; returns the index jobs name it by."""
+        scene_struct = build.as_struct()
+        idx = C.c_uint32(0)
+        library.check(self._lib.dk_server_add_scene(self._handle, C.byref(scene_struct), C.byref(idx)))
+        self._builds.append(build)
+        return idx.value
+
     def submit(self, settings: RenderSettings, camera: Camera, samples: int,
-               materials: Optional[np.ndarray] = None) -> int:
-        table = np.ascontiguousarray(self._build.materials if materials is None else materials)
+               materials: Optional[np.ndarray] = None, scene: int = 0) -> int:
+        if not 0 <= scene < len(self._builds):
+            raise ValueError("unknown scene index")
+        table = np.ascontiguousarray(self._builds[scene].materials if materials is None else materials)
         assert table.dtype == abi.MATERIAL_DTYPE
         jd = abi.JobDesc()
         jd.settings = make_settings_struct(settings, camera)
         jd.samples = int(samples)
         jd.material_count = len(table)
         jd.materials = table.ctypes.data
+        jd.scene = int(scene)
         jid = C.c_uint64(0)
         library.check(self._lib.dk_server_submit(self._handle, C.byref(jd), C.byref(jid)))
         self._jobs[jid.value] = (settings.width, settings.height)

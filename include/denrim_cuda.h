@@ -212,8 +212,16 @@ typedef struct dk_settings {
     dk_camera camera;
     dk_camera previous_camera;
     uint32_t max_samples_per_launch;      /* 0: the library picks; caps one wavefront batch */
-    uint32_t reserved;
+    uint32_t triangle_test;               /* DK_TRIANGLE_TEST_*; 0 (the reference's test) by default */
 } dk_settings;
+
+/* Ray-triangle test of a session.  MOLLER_TRUMBORE is the reference's
+ * intersectTriangle (PathTrace.metal:1801-1852) and the only mode with
+ * bit-exact parity against it.  WATERTIGHT is the shear-and-edge-function test
+ * of Woop, Benthin and Wald (JCGT 2013): no ray slips through a shared edge or
+ * vertex; hits near edges may differ from the reference's in the last bits. */
+#define DK_TRIANGLE_TEST_MOLLER_TRUMBORE 0u
+#define DK_TRIANGLE_TEST_WATERTIGHT 1u
 
 /* RenderOutput (Renderer/RenderOutput.swift:4-25). */
 typedef enum dk_output {
@@ -379,6 +387,9 @@ typedef struct dk_sparse_volume_settings {
     uint32_t volume_material; /* the volume's fallback material               */
     uint32_t object_id;
     uint32_t primitive_id;
+    uint32_t fp16_distances;  /* 1: store every sample distance rounded to half precision (the
+                               * packed records keep the rounded value as FP32; the march then
+                               * reads 2 bytes a sample).  No counterpart in the reference. */
 } dk_sparse_volume_settings;
 
 typedef struct dk_sparse_volume dk_sparse_volume;
@@ -403,14 +414,18 @@ int dk_sparse_volume_destroy(dk_sparse_volume* volume);
  * call cudaMalloc: applications that give the renderer only device memory from
  * their own arena or pool, and real-time frame loops that must not allocate.
  * The caller passes DEVICE pointers: `device_pixels` (width*height float4
- * texels) and `device_out` (width*height entries).  The FP64 prefix-sum scratch
+ * texels, 16-byte aligned) and `device_out` (width*height entries, 8-byte
+ * aligned); host or misaligned pointers fail with DK_ERROR_INVALID_ARGUMENT.
+ * The FP64 prefix-sum scratch
  * is one static __device__ array sized for DK_ENV_NOALLOC_MAX_TEXELS texels
  * (2048 x 1024, 16 MiB), held by every GPU that loads this library until the
  * process exits; larger maps fail with DK_ERROR_INVALID_ARGUMENT.  The first
  * call on a device looks up the array's device address (make that first call
  * before any stream capture).  All calls share the one array: calls that
  * overlap on the GPU (other threads, other streams) race.  Works on `stream`
- * (NULL: the default stream) and returns after the table is complete;
+ * (NULL: the default stream) and returns after the table is complete (it
+ * reads the table's total back to the host, so a call on a stream that is
+ * being captured fails with DK_ERROR_INVALID_ARGUMENT);
  * *out_count is width*height, or 0 for a map without energy.  Allocates
  * nothing: no cudaMalloc, no cudaFree, no allocating library routine. */
 #define DK_ENV_NOALLOC_MAX_TEXELS (2048u * 1024u)
@@ -420,6 +435,14 @@ int dk_build_environment_samples_noalloc(const dk_float4* device_pixels, uint32_
 
 /* Library version string. */
 const char* dk_version(void);
+
+/* Measured read bandwidth of the current device in GB/s: `passes` sweeps of
+ * 16-byte loads over a `bytes` buffer (>= 1 MiB) after one warm-up sweep,
+ * timed with CUDA events on `stream`.  A buffer well inside L2 (e.g. 64 MiB of
+ * the 129 MB) measures L2, one far larger HBM.  Allocates and frees the
+ * buffer; blocks until done.  Measurement only (the traversal stages'
+ * rooflines are stated against it); no counterpart in the reference. */
+int dk_probe_bandwidth(uint64_t bytes, uint32_t passes, double* out_gbs, void* stream);
 
 /* ------------------------------------------------------------------------- */
 /* Denoising.                                                                 */
@@ -445,6 +468,25 @@ typedef struct dk_spatial_denoise_settings {
 int dk_denoise_spatial(const float* beauty, const float* depth, const float* normal, const float* albedo,
                        float* out, float* scratch, uint32_t width, uint32_t height,
                        const dk_spatial_denoise_settings* settings, void* stream);
+
+/* The sums behind the learned denoiser's per-image error estimate, for
+ * `images` images of `pixels` RGBA32F pixels each (DEVICE pointers, images
+ * back to back): two independent half-sample renders A and B, the full render
+ * F of the same samples, and the three denoised images.  `terms` (DEVICE,
+ * images x 5 doubles, overwritten) receives per image the sums over pixels and
+ * RGB of (dA - dB)^2, (A - B)^2, (F - dF)^2, dF and F -- of the linear values
+ * (`display` 0) or of the displayed ones (`display` 1: the reference's PNG
+ * tone curve, PNGWriter.swift:182-188, before quantisation).  Asynchronous on
+ * `stream`.  No counterpart in the reference (its denoisers carry no error
+ * estimate); it drives the fallback to more samples of the serving loop. */
+int dk_denoise_error_terms(const float* half_a, const float* half_b, const float* full, const float* denoised_a,
+                           const float* denoised_b, const float* denoised_full, uint32_t pixels, uint32_t images,
+                           uint32_t display, double* terms, void* stream);
+
+/* out = (a + b) / 2 over `texels` RGBA32F texels (DEVICE pointers; `out` may
+ * alias `a` or `b`): the full render of two independent renders of equal
+ * sample counts.  Asynchronous on `stream`. */
+int dk_average_planes(const float* a, const float* b, float* out, size_t texels, void* stream);
 
 /* DenoiseSettings.appleSVGF (Denoiser.swift:67-76) -- AppleSVGFDenoiser
  * (Denoiser.swift:167-300) -- as spatiotemporal variance-guided filtering
@@ -524,6 +566,15 @@ int dk_unet_l1_loss(const void* pred, uint32_t ldp, const float* target, uint32_
 int dk_unet_unpack_output(const void* pred, uint32_t ldp, uint32_t h, uint32_t w, const float* alpha_src,
                           uint32_t image_width, uint32_t image_height, uint32_t x0, uint32_t y0, float* out,
                           void* stream);
+/* The same two with the prediction a residual over the network input `base`
+ * (whose first 3 channels are log(1 + noisy beauty)): output = base + pred in
+ * log space, summed in FP32, so a converged pixel (a visible light) keeps its
+ * value to the residual's precision instead of the activations'. */
+int dk_unet_l1_loss_residual(const void* pred, uint32_t ldp, const void* base, uint32_t ldb, const float* target,
+                             uint32_t pixels, void* grad, uint32_t ldg, float* loss, void* stream);
+int dk_unet_unpack_output_residual(const void* pred, uint32_t ldp, const void* base, uint32_t ldb, uint32_t h,
+                                   uint32_t w, const float* alpha_src, uint32_t image_width, uint32_t image_height,
+                                   uint32_t x0, uint32_t y0, float* out, void* stream);
 /* Adam step on FP32 master weights; refreshes the bf16 copy and (3x3 layers,
  * wflip non-null) the tap-flipped transposed copy [cin][9][cout]. */
 int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t count, float lr, float beta1,
@@ -531,12 +582,15 @@ int dk_unet_adam(float* weights, const float* grad, float* m, float* v, uint32_t
                  void* stream);
 int dk_unet_weights_to_bf16(const float* weights, uint32_t count, void* wbf16, void* wflip, uint32_t cout,
                             uint32_t cin, void* stream);
-/* Selects the convolution kernel (Cout <= 256 for the tcgen05 ones): 2
- * (default) persistent TMA + tcgen05 with warp roles, 1 cp.async + tcgen05,
+/* Selects the convolution kernel (Cout <= 256 for the tcgen05 ones): 3
+ * (default) the halo-row TMA + tcgen05 kernel for images at least 128 pixels
+ * wide whose weights and input rows fit one CTA's shared memory, else 2;
+ * 2 persistent per-tap TMA + tcgen05 with warp roles, 1 cp.async + tcgen05,
  * 0 mma.sync; the alternatives are kept for comparison. */
 int dk_unet_set_conv_path(int path);
-/* Reads and clears the denoiser kernels' error flag (1: a bounded wait for the
- * tensor cores timed out and the affected tiles were not written). */
+/* Reads and clears the denoiser kernels' error flag (non-zero: a bounded wait
+ * for the tensor cores or a copy timed out and the affected tiles were not
+ * written; 1, 2, 3 name the cp.async, per-tap TMA and halo-row kernels). */
 int dk_unet_error(int* out_error);
 
 /* ------------------------------------------------------------------------- */
@@ -574,6 +628,8 @@ typedef struct dk_job_desc {
     uint32_t samples;
     uint32_t material_count;
     const dk_material* materials;
+    uint32_t scene;                /* resident scene: 0 the create-time one, else dk_server_add_scene's */
+    uint32_t reserved;
 } dk_job_desc;
 
 enum { DK_JOB_QUEUED = 0, DK_JOB_RUNNING = 1, DK_JOB_DONE = 2, DK_JOB_RELEASED = 3 };
@@ -599,6 +655,12 @@ typedef struct dk_server_stats {
 
 /* Uploads `scene` once and prepares the shared wave. */
 int dk_server_create(const dk_scene* scene, const dk_server_config* config, dk_server** out_server);
+/* Makes another scene resident in the server (its BVH, textures, lights and
+ * HDRI table uploaded once, with its own wavefront of `wave_paths` paths and
+ * stream); jobs name it by the returned index.  Every step runs one packed
+ * wave per scene with work, the scenes' waves overlapping on the device.  No
+ * counterpart in the reference, whose RenderSession holds one scene. */
+int dk_server_add_scene(dk_server* server, const dk_scene* scene, uint32_t* out_scene);
 /* Queues a job; validation errors are returned here (DK_ERROR_INVALID_*). */
 int dk_server_submit(dk_server* server, const dk_job_desc* job, uint64_t* out_job_id);
 /* Admits queued jobs and runs one wave on the calling thread; `out_jobs` (may

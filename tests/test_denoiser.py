@@ -79,3 +79,33 @@ def test_unet_trained_on_rendered_pairs_beats_input_and_spatial_filter(renderer)
     print(f"display relative RMSE on held-out variants: 4 spp {n:.4f}, spatial filter {s:.4f}, U-Net {l:.4f}; "
           f"linear: {np.mean(lin, axis=0)}; losses {losses}")
     assert l < 0.5 * n and l < s
+
+
+def test_error_terms_match_a_float64_reduction(renderer):
+    # dk_denoise_error_terms against the same sums in FP64 on the host, for a
+    # batch of images of a size that is not a multiple of the block.
+    from denrimrendererkit_gb300.denoiser import estimate_errors
+    import ctypes as C
+    from denrimrendererkit_gb300 import library
+    g = torch.Generator(device="cuda").manual_seed(3)
+    n, h, w = 3, 37, 53
+    planes = [torch.rand(n, h, w, 4, generator=g, device="cuda") + 0.1 * k for k in range(6)]
+    terms = torch.empty(n, 5, dtype=torch.float64, device="cuda")
+    library.check(library.load().dk_denoise_error_terms(*(C.c_void_p(p.data_ptr()) for p in planes), h * w, n, 0,
+                                                        C.c_void_p(terms.data_ptr()), None))
+    torch.cuda.synchronize()
+    a, b, f, da, db, df = (p[..., :3].double().cpu() for p in planes)
+    want = torch.stack([((da - db) ** 2).sum((1, 2, 3)), ((a - b) ** 2).sum((1, 2, 3)), ((f - df) ** 2).sum((1, 2, 3)),
+                        df.sum((1, 2, 3)), f.sum((1, 2, 3))], 1)
+    assert torch.allclose(terms.cpu(), want, rtol=1e-9, atol=0)
+    est = estimate_errors(*planes)
+    assert len(est) == n and all(e.denoised >= e.noise >= 0 and e.plain > 0 for e in est)
+    # the displayed-image sums: the reference's tone curve applied to every plane first
+    from denrimrendererkit_gb300.denoiser import display
+    library.check(library.load().dk_denoise_error_terms(*(C.c_void_p(p.data_ptr()) for p in planes), h * w, n, 1,
+                                                        C.c_void_p(terms.data_ptr()), None))
+    torch.cuda.synchronize()
+    a, b, f, da, db, df = (display(p).cpu() for p in planes)
+    want = torch.stack([((da - db) ** 2).sum((1, 2, 3)), ((a - b) ** 2).sum((1, 2, 3)), ((f - df) ** 2).sum((1, 2, 3)),
+                        df.sum((1, 2, 3)), f.sum((1, 2, 3))], 1)
+    assert torch.allclose(terms.cpu(), want, rtol=1e-5, atol=1e-6)

@@ -154,3 +154,37 @@ def test_invalid_jobs_are_refused(preview):
         srv.release(jid)
         with pytest.raises(library.DenrimError):
             srv.pixels(jid)
+
+
+def test_jobs_across_resident_scenes_equal_their_solo_renders(preview):
+    # Two resident scenes in one server: the preview scene and the small
+    # Cornell box (another BVH, light list and environment).  Jobs of both
+    # scenes share every step -- one packed wave per scene, the two waves on
+    # their own streams -- and each renders what it renders alone.
+    scene, build = preview
+    box = scenes.cornell_small(width=64, height=48)
+    box_build = compile_scene(box.scene)
+    with RenderServer(build, ServerConfig(wave_paths=1 << 18, samples_per_wave=6)) as srv:
+        b_idx = srv.add_scene(box_build)
+        assert b_idx == 1
+        jobs = [(0, 96, 96, 12, PRESETS["metal.gold"]), (1, 64, 48, 10, None), (0, 128, 64, 9,
+                PRESETS["fabric.velvet-purple"]), (1, 80, 60, 7, None)]
+        ids = []
+        for sc, w, h, spp, m in jobs:
+            if sc == 0:
+                ids.append(srv.submit(_settings(w, h), scene.camera, spp, _table(build, m)))
+            else:
+                ids.append(srv.submit(_settings(w, h), box.scene.camera, spp, scene=1))
+        while any(srv.status(i).state != abi.JOB_DONE for i in ids):
+            assert srv.step() > 0
+        stats = srv.stats()
+        assert stats["waves"] > 2
+        for jid, (sc, w, h, spp, m) in zip(ids, jobs):
+            got = {o: srv.pixels(jid, o) for o in OUTPUTS}
+            if sc == 0:
+                want = _solo(scene, build, w, h, spp, _table(build, m), None)
+            else:
+                want = _solo(box.scene, box_build, w, h, spp, box_build.materials, None)
+            _assert_same(got, want, f"scene {sc} job {jid}")
+        with pytest.raises(ValueError):
+            srv.submit(_settings(32, 32), scene.camera, 1, scene=2)  # no such scene

@@ -28,10 +28,13 @@ def to_torch_weight(w):  # [co][9][ci] -> [co][ci][3][3]
     return w.reshape(co, 3, 3, ci).permute(0, 3, 1, 2).contiguous()
 
 
-@pytest.fixture(scope="module", params=[2, 1, 0], ids=["tma_tcgen05", "cpasync_tcgen05", "mma_sync"])
+@pytest.fixture(scope="module", params=[3, 2, 1, 0], ids=["halo_tcgen05", "tma_tcgen05", "cpasync_tcgen05",
+                                                          "mma_sync"])
 def lib(dk_lib, request):
-    """Runs every test with each convolution kernel: persistent TMA + tcgen05
-    (the default), cp.async + tcgen05, and mma.sync."""
+    """Runs every test with each convolution kernel: the halo-row TMA + tcgen05
+    kernel where a layer fits it, else the per-tap one (the default), the
+    per-tap persistent TMA + tcgen05 kernel alone, cp.async + tcgen05, and
+    mma.sync."""
     import ctypes as C
     from denrimrendererkit_gb300 import DenrimRenderer
     DenrimRenderer(0)
@@ -40,7 +43,7 @@ def lib(dk_lib, request):
     yield lib
     err = C.c_int(0)
     library.check(lib.dk_unet_error(C.byref(err)))
-    library.check(lib.dk_unet_set_conv_path(2))
+    library.check(lib.dk_unet_set_conv_path(3))
     assert err.value == 0, "a tensor-core wait timed out"
 
 
@@ -69,6 +72,37 @@ def test_conv3x3_forward(lib, cin, cout, act, ldi_extra, ldo_extra, co_off):
         if accumulate:
             ref = ref + prior[..., co_off:co_off + cout].float()
         assert rel_rms(got[..., co_off:co_off + cout], ref) <= 1e-2
+        untouched = torch.cat([got[..., :co_off], got[..., co_off + cout:]], -1)
+        expect = torch.cat([prior[..., :co_off], prior[..., co_off + cout:]], -1).float()
+        assert torch.equal(untouched, expect)
+
+
+@pytest.mark.parametrize("cin,cout,act,ldi_extra,ldo_extra,co_off", [
+    (16, 32, 1, 0, 0, 0), (32, 32, 1, 32, 0, 0), (96, 32, 1, 0, 64, 64), (32, 16, 0, 0, 0, 0), (64, 64, 1, 0, 0, 0),
+    (64, 96, 1, 0, 0, 0), (128, 32, 1, 0, 0, 0)])
+def test_conv3x3_forward_wide(lib, cin, cout, act, ldi_extra, ldo_extra, co_off):
+    # Images at least 128 pixels wide (the halo-row kernel's layers), with a
+    # partial last tile column and rows that do not fill the row blocks.
+    g = torch.Generator().manual_seed(cin * 11 + cout)
+    n, h, w = 2, 9, 200
+    ldi, ldo = cin + ldi_extra, cout + ldo_extra + co_off
+    x = torch.randn(n, h, w, ldi, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) / (3 * cin ** 0.5)).to(torch.bfloat16)
+    b = torch.randn(cout, generator=g) * 0.1
+    prior = torch.randn(n, h, w, ldo, generator=g).to(torch.bfloat16)
+    ref = torch.nn.functional.conv2d(x[..., :cin].float().permute(0, 3, 1, 2), to_torch_weight(wt.float()), b,
+                                     padding=1).permute(0, 2, 3, 1)
+    if act:
+        ref = torch.relu(ref)
+    xd, wd, bd = x.cuda(), wt.cuda(), b.cuda()  # held: the kernel reads them after this statement
+    for accumulate in (0, 1):
+        out = prior.clone().cuda()
+        library.check(lib.dk_unet_conv3x3(_ptr(xd), n, h, w, cin, ldi, _ptr(wd), _ptr(bd), cout, _ptr(out), ldo,
+                                          co_off, act, accumulate, None))
+        torch.cuda.synchronize()
+        got = out.cpu().float()
+        want = ref + prior[..., co_off:co_off + cout].float() if accumulate else ref
+        assert rel_rms(got[..., co_off:co_off + cout], want) <= 1e-2
         untouched = torch.cat([got[..., :co_off], got[..., co_off + cout:]], -1)
         expect = torch.cat([prior[..., :co_off], prior[..., co_off + cout:]], -1).float()
         assert torch.equal(untouched, expect)
@@ -140,8 +174,13 @@ def test_network_gradients_match_fp32_reference(lib):
         wv, _ = net.state()[l.name]
         state[l.name] = (wv, (torch.randn(l.cout, generator=g) * 0.05).numpy())
     net.load_state(state)
-    x = torch.randn(n, h, w, IN_CH, generator=g).to(torch.bfloat16)
-    target = torch.rand(n * h * w, 4, generator=g) * 2.0
+    x = torch.randn(n, h, w, IN_CH, generator=g)
+    x[..., :3] = x[..., :3].abs()  # log(1 + noisy) channels are non-negative
+    x = x.to(torch.bfloat16)
+    # Targets 0.5..1.5 above the residual's base in log space: the L1 loss's
+    # sign stays away from zero, where bf16 rounding would flip gradient terms.
+    tl0 = x[..., :3].float() + 0.5 + torch.rand(n, h, w, 3, generator=g)
+    target = torch.cat([torch.expm1(tl0), torch.ones(n, h, w, 1)], -1).reshape(n * h * w, 4)
     B = net.grad_buffers(n, h, w)
     B["x"].copy_(x.cuda())
     net.zero_grad()
@@ -158,7 +197,8 @@ def test_network_gradients_match_fp32_reference(lib):
         wts[l.name] = (wr, br)
     pred = torch_unet(x.float().permute(0, 3, 1, 2), wts)
     tl = torch.log1p(target[:, :3].reshape(n, h, w, 3).permute(0, 3, 1, 2))
-    loss = (pred[:, :3] - tl).abs().mean()
+    # the network's output is a residual over the input's first 3 channels
+    loss = (pred[:, :3] + x.float().permute(0, 3, 1, 2)[:, :3] - tl).abs().mean()
     loss.backward()
     assert abs(B["loss"].item() - loss.item()) <= 2e-2 * loss.item()
     got_pred = B["pred"].cpu().float()[..., :3].permute(0, 3, 1, 2)
