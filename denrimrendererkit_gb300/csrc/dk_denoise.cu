@@ -150,13 +150,15 @@ __global__ void __launch_bounds__(256) k_error_terms(const float4* __restrict__ 
     }
 }
 
-// out = (a + b) / 2 per RGBA texel: the full render of two equal-sample
-// halves (also a doubling step of a progressive render: the previous full
-// render and a new render of as many samples).
-__global__ void __launch_bounds__(256) k_average_planes(const float4* a, const float4* b, float4* out, size_t n) {
+// out = (1 - t) a + t b per RGBA texel: the full render of two independent
+// renders of n_a and n_b samples with t = n_b / (n_a + n_b) (0.5 for two
+// halves; the previous full render and a render of more samples when a
+// progressive render grows).
+__global__ void __launch_bounds__(256) k_average_planes(const float4* a, const float4* b, float4* out, size_t n, float t) {
+    const float s = 1.0f - t;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const float4 x = a[i], y = b[i];
-        out[i] = make_float4(0.5f * (x.x + y.x), 0.5f * (x.y + y.y), 0.5f * (x.z + y.z), 0.5f * (x.w + y.w));
+        out[i] = make_float4(s * x.x + t * y.x, s * x.y + t * y.y, s * x.z + t * y.z, s * x.w + t * y.w);
     }
 }
 
@@ -164,12 +166,14 @@ __global__ void __launch_bounds__(256) k_average_planes(const float4* a, const f
 
 }  // namespace dk
 
-extern "C" int dk_average_planes(const float* a, const float* b, float* out, size_t texels, void* stream) {
+extern "C" int dk_average_planes(const float* a, const float* b, float* out, size_t texels, float t, void* stream) {
     if (!a || !b || !out) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_average_planes: null argument");
+    if (!(t >= 0.0f && t <= 1.0f)) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_average_planes: t outside [0, 1]");
     if (texels == 0) return DK_OK;
     const unsigned grid = (unsigned)std::min<size_t>((texels + 255u) / 256u, 152u * 16u);
     dk::k_average_planes<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(b), reinterpret_cast<float4*>(out), texels);
+        reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(b), reinterpret_cast<float4*>(out), texels,
+        t);
     DK_CUDA(cudaGetLastError(), "average planes launch");
     return DK_OK;
 }

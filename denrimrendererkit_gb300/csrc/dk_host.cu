@@ -571,6 +571,8 @@ int allocWave(Arena& arena, Wave& W, uint64_t capPaths, uint32_t pixelCap, uint3
     TRY(arena.alloc(&W.aov, 4 * (size_t)pixelCap, "AOV records"));
     TRY(arena.alloc(&W.layer_hits, 3 * cap * kRecLayers, "recorded shadow layers"));
     TRY(arena.alloc(&W.layer_count, 3 * cap, "recorded shadow layer counts"));
+    TRY(arena.alloc(&W.live, cap, "survivor flags"));
+    TRY(arena.alloc(&W.scan, (cap + kLiveBlock - 1) / kLiveBlock + 1, "survivor block offsets"));
     TRY(arena.alloc(&W.qsorted, cap, "material-ordered queue"));
     TRY(arena.alloc(&W.keys, cap, "material keys"));
     TRY(arena.alloc(&W.bins, kSortBins + 1, "material bins"));

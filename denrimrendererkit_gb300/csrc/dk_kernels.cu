@@ -520,33 +520,141 @@ __global__ void __launch_bounds__(kSortBins) k_sort_scan(Wave W) {
     W.bins[t] = v[t] - x;
 }
 
-// Block b places queue entries [b * 2048, b * 2048 + 2048): ranks within the
-// block from shared-memory counters, one global reservation per (block, key).
+// Block b places queue entries [b * 2048, b * 2048 + 2048) stably: an entry's
+// rank among the block's entries of its key follows queue order (in-warp
+// ranks from __match_any_sync, warp offsets per key scanned in shared memory,
+// eight rounds of 256 entries in order), and one global reservation per
+// (block, key) places the block's run.  The queue is in path order, so every
+// run of a key holds increasing path indices -- neighbouring lanes of the
+// shading kernel read neighbouring path state.
 constexpr uint32_t kSortItems = 8;
 __global__ void __launch_bounds__(256) k_sort_scatter(Wave W, uint32_t sel) {
     __shared__ uint32_t cnt[kSortBins];
     __shared__ uint32_t base[kSortBins];
+    __shared__ uint32_t warpCnt[8][kSortBins];
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
     const uint32_t start = blockIdx.x * 256u * kSortItems;
     if (start >= n) return;  // uniform over the block
-    for (uint32_t b = threadIdx.x; b < kSortBins; b += blockDim.x) cnt[b] = 0u;
-    __syncthreads();
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t lanesBelow = (1u << lane) - 1u;
+    cnt[tid] = 0u;  // kSortBins == blockDim.x
     uint32_t key[kSortItems], rank[kSortItems];
 #pragma unroll
     for (uint32_t k = 0; k < kSortItems; ++k) {
-        uint32_t i = start + k * 256u + threadIdx.x;
-        key[k] = i < n ? W.keys[i] : 0u;
-        rank[k] = i < n ? atomicAdd(&cnt[key[k]], 1u) : 0u;
+#pragma unroll
+        for (uint32_t w = 0; w < 8u; ++w) warpCnt[w][tid] = 0u;
+        __syncthreads();
+        const uint32_t i = start + k * 256u + tid;
+        const bool valid = i < n;
+        key[k] = valid ? W.keys[i] : kSortBins - 1u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? key[k] : 0xffffffffu);
+        const uint32_t inWarp = __popc(peers & lanesBelow);
+        if (valid && inWarp == 0u) warpCnt[warp][key[k]] = __popc(peers);
+        __syncthreads();
+        {  // thread `tid` scans key `tid` over the warps, after the earlier rounds
+            uint32_t run = cnt[tid];
+#pragma unroll
+            for (uint32_t w = 0; w < 8u; ++w) {
+                const uint32_t c = warpCnt[w][tid];
+                warpCnt[w][tid] = run;
+                run += c;
+            }
+            cnt[tid] = run;
+        }
+        __syncthreads();
+        rank[k] = valid ? warpCnt[warp][key[k]] + inWarp : 0u;
+        __syncthreads();
     }
-    __syncthreads();
-    for (uint32_t b = threadIdx.x; b < kSortBins; b += blockDim.x)
-        if (cnt[b]) base[b] = atomicAdd(&W.bins[b], cnt[b]);
+    if (cnt[tid]) base[tid] = atomicAdd(&W.bins[tid], cnt[tid]);
     __syncthreads();
 #pragma unroll
     for (uint32_t k = 0; k < kSortItems; ++k) {
-        uint32_t i = start + k * 256u + threadIdx.x;
+        uint32_t i = start + k * 256u + tid;
         if (i < n) W.qsorted[base[key[k]] + rank[k]] = q[i];
+    }
+}
+
+// ------------------------------------------ survivors in path order ----
+// Shading writes a flag per path; the next bounce's queue is the flagged
+// paths in increasing path order: a count per block of kLiveBlock paths, one
+// block's scan of the counts, and a scatter of each block's paths at its
+// offset.  Path order keeps the extension stage's and (through the stable
+// material sort) the shading stage's path-state accesses coalesced.
+__device__ __forceinline__ uint32_t liveCount16(const Wave& W, uint32_t first, uint32_t n, uint32_t& bits) {
+    bits = 0u;
+    if (first + 16u <= n) {
+        const uint4 v = *reinterpret_cast<const uint4*>(W.live + first);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (uint32_t j = 0; j < 4u; ++j)
+#pragma unroll
+            for (uint32_t b = 0; b < 4u; ++b) bits |= (((w[j] >> (8u * b)) & 0xffu) ? 1u : 0u) << (4u * j + b);
+    } else {
+        for (uint32_t j = 0; j < 16u && first + j < n; ++j) bits |= (W.live[first + j] ? 1u : 0u) << j;
+    }
+    return __popc(bits);
+}
+
+__device__ __forceinline__ uint32_t blockExclusiveScan256(uint32_t v, uint32_t& total) {
+    __shared__ uint32_t warpSums[8];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (uint32_t o = 1; o < 32u; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31u) warpSums[warp] = x;
+    __syncthreads();
+    uint32_t before = 0u;
+    total = 0u;
+#pragma unroll
+    for (uint32_t w = 0; w < 8u; ++w) {
+        const uint32_t c = warpSums[w];
+        if (w < warp) before += c;
+        total += c;
+    }
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(256) k_live_count(Wave W) {
+    const uint32_t n = W.path_count;
+    const uint32_t first = blockIdx.x * kLiveBlock + threadIdx.x * 16u;
+    uint32_t bits, total;
+    const uint32_t c = first < n ? liveCount16(W, first, n, bits) : 0u;
+    blockExclusiveScan256(c, total);
+    if (threadIdx.x == 0) W.scan[blockIdx.x] = total;
+}
+
+// Exclusive scan of the block counts (one block); the total is the next queue's length.
+__global__ void __launch_bounds__(256) k_live_scan(Wave W, uint32_t sel, uint32_t blocks) {
+    const uint32_t per = (blocks + 255u) / 256u;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t sum = 0u;
+    for (uint32_t b = b0; b < b0 + per && b < blocks; ++b) sum += W.scan[b];
+    uint32_t total;
+    uint32_t run = blockExclusiveScan256(sum, total);
+    for (uint32_t b = b0; b < b0 + per && b < blocks; ++b) {
+        const uint32_t c = W.scan[b];
+        W.scan[b] = run;
+        run += c;
+    }
+    if (threadIdx.x == 0) W.counts[sel ^ 1u] = total;
+}
+
+__global__ void __launch_bounds__(256) k_live_scatter(Wave W, uint32_t sel) {
+    const uint32_t n = W.path_count;
+    const uint32_t first = blockIdx.x * kLiveBlock + threadIdx.x * 16u;
+    uint32_t bits = 0u, total;
+    const uint32_t c = first < n ? liveCount16(W, first, n, bits) : 0u;
+    uint32_t slot = W.scan[blockIdx.x] + blockExclusiveScan256(c, total);
+    uint32_t* qNext = W.q[sel ^ 1u];
+    while (bits) {
+        const uint32_t j = __ffs(bits) - 1u;
+        bits &= bits - 1u;
+        qNext[slot++] = first + j;
     }
 }
 
@@ -765,63 +873,17 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
 #ifndef DK_SHADE_MIN_BLOCKS
 #define DK_SHADE_MIN_BLOCKS 4
 #endif
-__device__ __forceinline__ void prefetchL2(const void* ptr) {
-    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(ptr));
-}
-
-// The next path of this thread (shading order `i`): its hit record is loaded
-// now and consumed after the current path, when its path state and the
-// 192-byte triangle record of its hit are prefetched into L2 -- the shading
-// of one path overlaps the memory latency of the next one's dependent loads.
-struct NextPath {
-    uint32_t p;
-    float tri;
-};
-
-__device__ __forceinline__ NextPath peekNext(const Wave& W, const uint32_t* q, uint32_t i, uint32_t n) {
-    NextPath nx{0u, __uint_as_float(kNoHit)};
-    if (i < n) {
-        nx.p = __ldg(q + i);
-        nx.tri = __ldg(reinterpret_cast<const float*>(W.hit + nx.p) + 1);
-    }
-    return nx;
-}
-
-__device__ __forceinline__ void prefetchNext(const DevScene& S, const Wave& W, const NextPath& nx, uint32_t i,
-                                             uint32_t n) {
-    if (i >= n) return;
-    prefetchL2(W.ray_o + nx.p);
-    prefetchL2(W.ray_d + nx.p);
-    prefetchL2(W.tp + nx.p);
-    prefetchL2(W.rad + nx.p);
-    prefetchL2(W.rng + nx.p);
-    const uint32_t tri = __float_as_uint(nx.tri);
-    if (tri < S.tri_count) {
-        const char* rec = reinterpret_cast<const char*>(S.tris + tri);
-        prefetchL2(rec);
-        prefetchL2(rec + 64);
-        prefetchL2(rec + 128);
-    }
-}
-
 template <bool kVolumes>
 __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, Wave W, uint32_t bounce, uint32_t sel,
                                                                   uint32_t sorted) {
     const uint32_t* q = sorted ? W.qsorted : W.q[sel];
-    uint32_t* qNext = W.q[sel ^ 1u];
     const uint32_t n = W.counts[sel];
     if (globalId() == 0) W.counts[4] = 0u;  // extend cursor of the next bounce
-    const uint32_t stride = gridStride();
-    uint32_t pCur = globalId() < n ? q[globalId()] : 0u;
-    for (uint32_t i = globalId(); i < n; i += stride) {
-        const uint32_t p = pCur;
-        const NextPath nx = peekNext(W, q, i + stride, n);
+    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+        uint32_t p = q[i];
         ShadeOut o = shadePath<kVolumes>(S, W, p, i, bounce);
-        prefetchNext(S, W, nx, i + stride, n);
-        pCur = nx.p;
         bool keep = o.survive && bounce + 1u < o.maxBounces;
-        uint32_t slot = warpAppend(&W.counts[sel ^ 1u], keep);
-        if (keep) qNext[slot] = p;
+        W.live[p] = keep ? 1u : 0u;  // the next queue is built from these flags in path order
         bool sh = o.neeMask != 0u;
         uint32_t sslot = warpAppend(&W.counts[2], sh);
         if (sh) W.qs[sslot] = i;
@@ -1614,7 +1676,7 @@ uint32_t bounceLaunches(const DevScene& S) {
         g_sortMaterials = (e && e[0] == '0') ? 0 : 1;
     }
     uint32_t n = 1u + (S.volume_count ? 1u : 0u);                  // extend
-    n += 1u + (g_sortMaterials ? 3u : 0u);                           // shade
+    n += 1u + (g_sortMaterials ? 3u : 0u) + 3u;                      // shade, survivor queue
     n += 1u + ((!S.all_shadow_opaque || S.volume_count) ? 1u : 0u);  // shadow
     return n + 1u;                                                   // resolve
 }
@@ -1637,6 +1699,15 @@ cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint3
         k_shade<true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
     else
         k_shade<false><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
+    // The survivors, in path order, are the next bounce's queue.
+    const uint32_t blocks = (W.path_count + kLiveBlock - 1u) / kLiveBlock;
+    if (blocks) {
+        k_live_count<<<blocks, 256, 0, st>>>(W);
+        k_live_scan<<<1, 256, 0, st>>>(W, sel, blocks);
+        k_live_scatter<<<blocks, 256, 0, st>>>(W, sel);
+    } else {
+        k_live_scan<<<1, 256, 0, st>>>(W, sel, 0u);
+    }
     return cudaGetLastError();
 }
 cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st) {

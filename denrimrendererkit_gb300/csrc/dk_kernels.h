@@ -13,6 +13,7 @@ namespace dk {
 
 constexpr uint32_t kNoSlot = 0xffffffffu;
 constexpr uint32_t kSortBins = 256;      // shading-order keys: 0 miss, 1 + material ID (< 254), 255 other
+constexpr uint32_t kLiveBlock = 4096;    // paths per block of the survivor compaction (256 threads x 16)
 constexpr uint32_t kRecLayers = 4;       // non-opaque layers the any-hit pass records per shadow ray
 constexpr uint32_t kTraversalStack = 32; // groups on the 8-wide traversal stack (bounds the tree depth)
 
@@ -122,6 +123,8 @@ struct Wave {
     float4* aov;       // 4 planes of aov_stride tile pixels: primary-hit record of each job's last sample
     uint2* layer_hits;      // kRecLayers per shadow-ray slot: (t bits, triangle slot) of crossed non-opaque triangles
     uint32_t* layer_count;  // per shadow-ray slot: recorded layers, bit 31 = more than kRecLayers
+    uint8_t* live;     // per path: 1 when it goes on to the next bounce (written by shading)
+    uint32_t* scan;    // per block of kLiveBlock paths: live count, then its queue offset
     uint32_t* qsorted; // the active queue reordered by material (the shading order)
     uint32_t* keys;    // material key of each active-queue entry
     uint32_t* bins;    // kSortBins + 1 counters: key histogram, then bucket cursors

@@ -96,14 +96,25 @@ struct DistSrc {
     const uint16_t* f16;
 };
 
-__device__ __forceinline__ float sampleD(const DistSrc& dist, const BrickCtx& c, uint32_t x, uint32_t y, uint32_t z) {
-    const size_t k = c.sampleOffset + x + y * c.strideY + z * c.strideZ;
-    if (dist.f16) return __half2float(__ushort_as_half(__ldg(dist.f16 + k)));
-    return __ldg(dist.f32 + k);
+// The two sample formats as template arguments of the march, so that the
+// format is decided once per brick and not per sample.
+struct DistF32 {
+    const float* p;
+    __device__ __forceinline__ float at(size_t k) const { return __ldg(p + k); }
+};
+struct DistF16 {
+    const uint16_t* p;
+    __device__ __forceinline__ float at(size_t k) const { return __half2float(__ushort_as_half(__ldg(p + k))); }
+};
+
+template <class D>
+__device__ __forceinline__ float sampleD(const D& dist, const BrickCtx& c, uint32_t x, uint32_t y, uint32_t z) {
+    return dist.at(c.sampleOffset + x + y * c.strideY + z * c.strideZ);
 }
 
 // sampleVolumeBrickDistancePrepared (:2097-2125).
-__device__ float brickDistance(const DistSrc& dist, const BrickCtx& c, float3 p) {
+template <class D>
+__device__ float brickDistance(const D& dist, const BrickCtx& c, float3 p) {
     if (!c.valid) return INFINITY;
     GridPos g = gridPos(c, p);
     const uint32_t *b = g.base, *n = g.next;
@@ -122,7 +133,8 @@ struct DistGrad {
 };
 
 // sampleVolumeBrickDistanceGradientPrepared (:2164-2218).
-__device__ DistGrad brickDistGrad(const DistSrc& dist, const BrickCtx& c, float3 p) {
+template <class D>
+__device__ DistGrad brickDistGrad(const D& dist, const BrickCtx& c, float3 p) {
     DistGrad r;
     r.distance = INFINITY;
     r.gradient = f3(0.0f);
@@ -164,7 +176,8 @@ __device__ __forceinline__ float catmullD(float p0, float p1, float p2, float p3
 }
 
 // sampleVolumeBrickDistanceGradientCubicPrepared (:2256-2307).
-__device__ __noinline__ DistGrad brickDistGradCubic(const DistSrc& dist, const BrickCtx& c, float3 p) {
+template <class D>
+__device__ __noinline__ DistGrad brickDistGradCubic(const D& dist, const BrickCtx& c, float3 p) {
     if (!c.valid) {
         DistGrad r;
         r.distance = INFINITY;
@@ -210,7 +223,8 @@ __device__ __noinline__ DistGrad brickDistGradCubic(const DistSrc& dist, const B
 }
 
 // sampleVolumeBrickCentralGradientPrepared (:2220-2254).
-__device__ float3 brickCentralGradient(const DistSrc& dist, const BrickCtx& c, float3 p, float3 s) {
+template <class D>
+__device__ float3 brickCentralGradient(const D& dist, const BrickCtx& c, float3 p, float3 s) {
     float3 x0 = p, x1 = p, y0 = p, y1 = p, z0 = p, z1 = p;
     x0.x = fmaxf(ex::sub(p.x, s.x), c.sampleMin.x);
     x1.x = fminf(ex::add(p.x, s.x), c.sampleMax.x);
@@ -243,15 +257,16 @@ __device__ __forceinline__ float cellSizeOf(const dk_volume_descriptor& vol) {
 }
 
 // volumeBrickNormal (:2420-2469).
-__device__ __noinline__ float3 brickNormal(const VolumeScene& V, const dk_volume_descriptor& vol, const BrickCtx& c, float3 p,
-                              bool cubic, bool coarse) {
+template <class D>
+__device__ __noinline__ float3 brickNormalT(const D& dist, const dk_volume_descriptor& vol, const BrickCtx& c, float3 p,
+                                           bool cubic, bool coarse) {
     if (!c.valid) return f3(0, 1, 0);
-    float3 n = cubic ? brickDistGradCubic(V.dist, c, p).gradient : brickDistGrad(V.dist, c, p).gradient;
+    float3 n = cubic ? brickDistGradCubic(dist, c, p).gradient : brickDistGrad(dist, c, p).gradient;
     if (coarse) {
         float3 ext = mx(ex::sub(ld3f(vol.local_bounds_max), ld3f(vol.local_bounds_min)), f3(1e-6f));
         float3 den = mx(ex::sub(f3((float)vol.dimensions.x, (float)vol.dimensions.y, (float)vol.dimensions.z), f3(1.0f)), f3(1.0f));
         float3 spacing = exDiv(ext, den);
-        float3 central = brickCentralGradient(V.dist, c, p, ex::mul(spacing, 1.5f));
+        float3 central = brickCentralGradient(dist, c, p, ex::mul(spacing, 1.5f));
         if (ex::dot(central, central) > 1e-10f) {
             float3 a = ex::normalize(n), b = ex::normalize(central);
             n = ex::normalize(f3(exMix(a.x, b.x, 0.35f), exMix(a.y, b.y, 0.35f), exMix(a.z, b.z, 0.35f)));
@@ -261,6 +276,12 @@ __device__ __noinline__ float3 brickNormal(const VolumeScene& V, const dk_volume
     return ex::normalize(mulColumns(vol.normal_transform, ex::normalize(n), 0.0f));
 }
 
+__device__ __forceinline__ float3 brickNormal(const VolumeScene& V, const dk_volume_descriptor& vol, const BrickCtx& c,
+                                              float3 p, bool cubic, bool coarse) {
+    if (V.dist.f16) return brickNormalT(DistF16{V.dist.f16}, vol, c, p, cubic, coarse);
+    return brickNormalT(DistF32{V.dist.f32}, vol, c, p, cubic, coarse);
+}
+
 struct VolumeHitRec {
     float t;
     uint32_t brick;
@@ -268,8 +289,9 @@ struct VolumeHitRec {
 
 // intersectVolumeBrickPrepared (:2608-2807) up to the refined distance (the
 // hit attributes are rebuilt from (t, brick) by makeVolumeHit).
-__device__ __noinline__ bool intersectBrick(const VolumeScene& V, uint32_t brickIndex, float closestT, float3 lo, float3 ld,
-                               float upw, float cellSize, float& outT) {
+template <class D>
+__device__ __noinline__ bool intersectBrickT(const D& dist, const VolumeScene& V, uint32_t brickIndex, float closestT,
+                                            float3 lo, float3 ld, float upw, float cellSize, float& outT) {
     const dk_volume_brick_descriptor& brick = V.bricks[brickIndex];
     float tNear, tFar;
     if (!intersectAABB(lo, ld, ld3f(brick.local_bounds_min), ld3f(brick.local_bounds_max), closestT, tNear, tFar))
@@ -280,7 +302,7 @@ __device__ __noinline__ bool intersectBrick(const VolumeScene& V, uint32_t brick
     float minimumStep = fmaxf(ex::div(ex::mul(cellSize, 0.10f), upw), 0.0005f);
     float prevT = tNear;
     float3 prevP = ex::add(lo, ex::mul(ld, prevT));
-    float prevD = brickDistance(V.dist, c, prevP);
+    float prevD = brickDistance(dist, c, prevP);
     if (!isfinite(prevD)) return false;
     float originalEntryT = prevT;
     if (prevD <= 0.0f) {
@@ -289,7 +311,7 @@ __device__ __noinline__ bool intersectBrick(const VolumeScene& V, uint32_t brick
         for (uint32_t bt = 0u; bt < 12u; ++bt) {
             searchT = fmaxf(ex::sub(searchT, backStep), 0.0005f);
             float3 sp = ex::add(lo, ex::mul(ld, searchT));
-            float sd = brickDistance(V.dist, c, sp);
+            float sd = brickDistance(dist, c, sp);
             if (!isfinite(sd)) break;
             if (sd > 0.0f) {
                 prevT = searchT;
@@ -303,14 +325,14 @@ __device__ __noinline__ bool intersectBrick(const VolumeScene& V, uint32_t brick
     float t = fmaxf(originalEntryT, ex::add(prevT, fmaxf(ex::mul(ex::div(fabsf(prevD), upw), 0.9f), minimumStep)));
     for (uint32_t step = 0u; step < 192u && t <= tFar && t < closestT; ++step) {
         float3 p = ex::add(lo, ex::mul(ld, t));
-        float d = brickDistance(V.dist, c, p);
+        float d = brickDistance(dist, c, p);
         if (!isfinite(d)) return false;
         bool crossed = (prevD > 0.0f && d <= 0.0f) || (prevD < 0.0f && d >= 0.0f);
         if (crossed) {
             float lowT = prevT, highT = t, lowD = prevD, refinedT = t;
             for (uint32_t r = 0u; r < 8u; ++r) {
                 float midT = ex::mul(0.5f, ex::add(lowT, highT));
-                float md = brickDistance(V.dist, c, ex::add(lo, ex::mul(ld, midT)));
+                float md = brickDistance(dist, c, ex::add(lo, ex::mul(ld, midT)));
                 if ((lowD > 0.0f && md > 0.0f) || (lowD < 0.0f && md < 0.0f)) {
                     lowT = midT;
                     lowD = md;
@@ -322,7 +344,7 @@ __device__ __noinline__ bool intersectBrick(const VolumeScene& V, uint32_t brick
             if (cellSize <= 0.03f) {  // cubic polish, renderQuality 2: two Newton steps
                 float3 rp = ex::add(lo, ex::mul(ld, refinedT));
                 for (uint32_t pol = 0u; pol < 2u; ++pol) {
-                    DistGrad pg = brickDistGradCubic(V.dist, c, rp);
+                    DistGrad pg = brickDistGradCubic(dist, c, rp);
                     float slope = ex::dot(pg.gradient, ld);
                     if (!isfinite(pg.distance) || fabsf(slope) <= 1e-6f) break;
                     float projected = ex::sub(refinedT, ex::div(pg.distance, slope));
@@ -339,6 +361,12 @@ __device__ __noinline__ bool intersectBrick(const VolumeScene& V, uint32_t brick
         t = ex::add(t, fmaxf(ex::mul(ex::div(fabsf(d), upw), 0.8f), minimumStep));
     }
     return false;
+}
+
+__device__ __forceinline__ bool intersectBrick(const VolumeScene& V, uint32_t brickIndex, float closestT, float3 lo,
+                                               float3 ld, float upw, float cellSize, float& outT) {
+    if (V.dist.f16) return intersectBrickT(DistF16{V.dist.f16}, V, brickIndex, closestT, lo, ld, upw, cellSize, outT);
+    return intersectBrickT(DistF32{V.dist.f32}, V, brickIndex, closestT, lo, ld, upw, cellSize, outT);
 }
 
 struct VolumeRay {

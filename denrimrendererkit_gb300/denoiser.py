@@ -587,20 +587,25 @@ class ErrorEstimate:
     plain: float
 
 
-def estimate_errors(half_a, half_b, full, den_a, den_b, den_full, stream=None,
-                    display: bool = False) -> List[ErrorEstimate]:
+def estimate_errors(half_a, half_b, full, den_a, den_b, den_full, stream=None, display: bool = False,
+                    samples=None) -> List[ErrorEstimate]:
     """Per-image error estimates from two independent half-sample renders A and
     B, their full render F = (A + B) / 2 and the three denoised images (device
     tensors (n, H, W, 4) or (H, W, 4) float32), with no reference image:
 
     * noise: the denoised output's variance, Var(dF) ~ E|dA - dB|^2 / 4 (A and
       B carry half the samples each, so each has twice F's variance);
-    * bias: what the denoiser changes beyond F's own noise, E|F - dF|^2 -
-      Var(F), with Var(F) ~ E|A - B|^2 / 4 (clamped at zero);
+    * bias: what the denoiser changes beyond F's own noise.  With dF keeping
+      a fraction g of F's noise (g^2 ~ E|dA - dB|^2 / E|A - B|^2),
+      E|F - dF|^2 ~ (1 - g)^2 Var(F) + bias^2, Var(F) ~ E|A - B|^2 / 4, so
+      bias^2 ~ E|F - dF|^2 - (1 - g)^2 Var(F) (clamped at zero);
     * plain: F's own error, sqrt(Var(F)) -- unbiased, the progressive
       renderer's estimate.
     `display`: the same on the displayed images (the reference's PNG tone
-    curve, as `display_relative_rmse` measures).  The sums run on the device
+    curve, as `display_relative_rmse` measures).  `samples` (per image, or one
+    pair for all): the sample counts (n_a, n_b) of A and B when they differ;
+    then Var(F) ~ E|A - B|^2 n_a n_b / (n_a + n_b)^2 (1/4 for halves), and
+    the same factor for dF.  The sums run on the device
     (dk_denoise_error_terms)."""
     torch = _torch()
     lib = library.load()
@@ -614,10 +619,16 @@ def estimate_errors(half_a, half_b, full, den_a, den_b, den_full, stream=None,
                                              None if stream is None else C.c_void_p(stream)))
     out = []
     m = 3.0 * h * w
-    for dd, nn, fd, sd, sf in terms.cpu().numpy().tolist():
-        var_dn = dd / (4.0 * m)
-        var_f = nn / (4.0 * m)
-        bias2 = max(0.0, fd / m - var_f)
+    if samples is None:
+        weights = [0.25] * n
+    else:
+        pairs = [samples] * n if isinstance(samples[0], (int, float)) else list(samples)
+        weights = [na * nb / float(na + nb) ** 2 for na, nb in pairs]
+    for (dd, nn, fd, sd, sf), wgt in zip(terms.cpu().numpy().tolist(), weights):
+        var_dn = dd * wgt / m
+        var_f = nn * wgt / m
+        g = min(1.0, math.sqrt(dd / nn)) if nn > 0.0 else 0.0
+        bias2 = max(0.0, fd / m - var_f * (1.0 - g) ** 2)
         mean_d = max(sd / m, 1e-12)
         mean_f = max(sf / m, 1e-12)
         out.append(ErrorEstimate(denoised=math.sqrt(var_dn + bias2) / mean_d, noise=math.sqrt(var_dn) / mean_d,
@@ -625,9 +636,11 @@ def estimate_errors(half_a, half_b, full, den_a, den_b, den_full, stream=None,
     return out
 
 
-def average_planes(a, b, out, stream=None) -> None:
-    """out = (a + b) / 2 on the device (dk_average_planes); tensors of one size."""
-    library.check(library.load().dk_average_planes(_ptr(a), _ptr(b), _ptr(out), a.numel() // 4,
+def average_planes(a, b, out, t: float = 0.5, stream=None) -> None:
+    """out = (1 - t) a + t b on the device (dk_average_planes): the full render
+    of two independent renders of n_a and n_b samples with t = n_b / (n_a +
+    n_b); tensors of one size."""
+    library.check(library.load().dk_average_planes(_ptr(a), _ptr(b), _ptr(out), a.numel() // 4, float(t),
                                                    None if stream is None else C.c_void_p(stream)))
 
 
@@ -643,6 +656,16 @@ class ServedImage:
     rounds: int
 
 
+def next_sample_count(spp: int, estimate: float, target: float, step: int = 8) -> int:
+    """The sample count a progressive render grows to when its error estimate
+    is `estimate` at `spp` samples: error ~ 1 / sqrt(spp) predicts
+    spp (estimate / target)^2; 10 % more, at least 1.25x and at most 4x the
+    current count, rounded up to a multiple of `step`."""
+    want = spp * 1.1 * (estimate / target) ** 2 if target > 0 else 4.0 * spp
+    want = min(max(want, 1.25 * spp), 4.0 * spp)
+    return int(math.ceil(want / step) * step)
+
+
 def serve_to_error_target(server, net: "UNet", requests, width: int, height: int, target: float = 0.02,
                           start_spp: int = 16, max_spp: int = 8192, denoise: bool = True,
                           seed_base: int = 0x51ED, display: bool = True) -> List[ServedImage]:
@@ -652,25 +675,26 @@ def serve_to_error_target(server, net: "UNet", requests, width: int, height: int
 
     Round 0 renders two independent halves A and B of `start_spp` samples per
     request (two jobs with different frame seeds, packed into the same waves
-    as every other request's); F = (A + B) / 2.  With `denoise`, the U-Net
+    as every other request's); F is their average.  With `denoise`, the U-Net
     denoises A, B and F of every open request as one batch and
     `estimate_errors` judges dF without a reference: a request whose
     estimate is within the target returns dF.  Otherwise -- and always without
     `denoise` -- F returns once its own (unbiased) estimate is within the
-    target.  A request that meets neither doubles its samples: F becomes the
-    next A, a new render of as many samples the next B.  At `max_spp` the
-    plain render returns (the fallback) whatever its estimate.  `display`:
-    the error is that of the displayed images (the reference's PNG tone
-    curve), else of the linear radiance."""
+    target.  A request that meets neither grows: its F becomes the next A, a
+    new render of as many more samples as `next_sample_count` predicts the
+    next B, and F their sample-weighted average.  At `max_spp` the plain
+    render returns (the fallback) whatever its estimate.  `display`: the
+    error is that of the displayed images (the reference's PNG tone curve),
+    else of the linear radiance."""
     torch = _torch()
     import dataclasses as dc
     from .renderer import RenderOutput
     n = len(requests)
     shape = (height, width, 4)
-    st0 = [r[0] for r in requests]
     open_ = list(range(n))
     full = [None] * n          # F of each request (device tensor)
-    spp = [0] * n
+    spp = [0] * n              # samples in F
+    grow = [0] * n             # samples of the next render
     aov = [None] * n           # albedo, normal, depth of each request
     result: List[Optional[ServedImage]] = [None] * n
     rounds = 0
@@ -682,14 +706,13 @@ def serve_to_error_target(server, net: "UNet", requests, width: int, height: int
         return server.submit(st, camera, samples, materials, scene=scene)
 
     while open_:
-        # jobs of this round: round 0 two halves per request, later one
         jobs = {}
         for k in open_:
             if spp[k] == 0:
-                jobs[k] = (submit(k, start_spp // 2, seed[k]), submit(k, start_spp // 2, seed[k] + 1))
+                jobs[k] = (submit(k, start_spp // 2, seed[k]), submit(k, start_spp - start_spp // 2, seed[k] + 1))
                 seed[k] += 2
             else:
-                jobs[k] = (None, submit(k, spp[k], seed[k]))
+                jobs[k] = (None, submit(k, grow[k], seed[k]))
                 seed[k] += 1
         while server.step():
             pass
@@ -697,20 +720,23 @@ def serve_to_error_target(server, net: "UNet", requests, width: int, height: int
         A = torch.empty((m,) + shape, device="cuda")
         B = torch.empty_like(A)
         F = torch.empty_like(A)
+        pairs = []
         for i, k in enumerate(open_):
             ja, jb = jobs[k]
             if ja is None:
                 A[i].copy_(full[k])
+                na, nb = spp[k], grow[k]
             else:
                 server.copy_output(ja, RenderOutput.BEAUTY, A[i])
                 aov[k] = [server.copy_output(ja, kind, torch.empty(shape, device="cuda"))
                           for kind in (RenderOutput.ALBEDO, RenderOutput.NORMAL, RenderOutput.DEPTH)]
                 server.release(ja)
+                na, nb = start_spp // 2, start_spp - start_spp // 2
             server.copy_output(jb, RenderOutput.BEAUTY, B[i])
             server.release(jb)
-        average_planes(A, B, F)
-        for i, k in enumerate(open_):
-            spp[k] = start_spp if spp[k] == 0 else 2 * spp[k]
+            average_planes(A[i], B[i], F[i], nb / float(na + nb))
+            spp[k] = na + nb
+            pairs.append((na, nb))
         if denoise:
             al = torch.stack([aov[k][0] for k in open_]).repeat(3, 1, 1, 1).contiguous()
             no = torch.stack([aov[k][1] for k in open_]).repeat(3, 1, 1, 1).contiguous()
@@ -718,11 +744,10 @@ def serve_to_error_target(server, net: "UNet", requests, width: int, height: int
             noisy = torch.cat([A, B, F]).contiguous()
             den = torch.empty_like(noisy)
             net.denoise_batch(noisy, al, no, de, width, height, den)
-            dA, dB, dF = den[:m], den[m:2 * m], den[2 * m:]
+            dA, dB, dF = den[:m].contiguous(), den[m:2 * m].contiguous(), den[2 * m:].contiguous()
         else:
             dA, dB, dF = A, B, F
-        est = estimate_errors(A.contiguous(), B.contiguous(), F, dA.contiguous(), dB.contiguous(), dF.contiguous(),
-                              display=display)
+        est = estimate_errors(A, B, F, dA, dB, dF, display=display, samples=pairs)
         rounds += 1
         still = []
         for i, k in enumerate(open_):
@@ -733,6 +758,8 @@ def serve_to_error_target(server, net: "UNet", requests, width: int, height: int
                 result[k] = ServedImage(F[i].clone(), spp[k], e, False, rounds)
             else:
                 full[k] = F[i].clone()
+                need = min(e.denoised, e.plain) if denoise else e.plain
+                grow[k] = min(next_sample_count(spp[k], need, target), max_spp) - spp[k]
                 still.append(k)
         open_ = still
     return result

@@ -95,7 +95,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_server_destroy": (i32, [P]),
             "dk_denoise_spatial": (i32, [P, P, P, P, P, P, u32, u32, C.POINTER(abi.SpatialDenoiseSettings), P]),
             "dk_denoise_error_terms": (i32, [P, P, P, P, P, P, u32, u32, u32, P, P]),
-            "dk_average_planes": (i32, [P, P, P, sz, P]),
+            "dk_average_planes": (i32, [P, P, P, sz, C.c_float, P]),
             "dk_svgf_create": (i32, [u32, u32, P]),
             "dk_svgf_reset": (i32, [P]),
             "dk_svgf_denoise": (i32, [P, P, P, P, P, P, C.POINTER(abi.SpatialDenoiseSettings), P]),

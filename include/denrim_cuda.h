@@ -483,10 +483,10 @@ int dk_denoise_error_terms(const float* half_a, const float* half_b, const float
                            const float* denoised_b, const float* denoised_full, uint32_t pixels, uint32_t images,
                            uint32_t display, double* terms, void* stream);
 
-/* out = (a + b) / 2 over `texels` RGBA32F texels (DEVICE pointers; `out` may
- * alias `a` or `b`): the full render of two independent renders of equal
- * sample counts.  Asynchronous on `stream`. */
-int dk_average_planes(const float* a, const float* b, float* out, size_t texels, void* stream);
+/* out = (1 - t) a + t b over `texels` RGBA32F texels (DEVICE pointers; `out`
+ * may alias `a` or `b`): the full render of two independent renders of n_a and
+ * n_b samples with t = n_b / (n_a + n_b).  Asynchronous on `stream`. */
+int dk_average_planes(const float* a, const float* b, float* out, size_t texels, float t, void* stream);
 
 /* DenoiseSettings.appleSVGF (Denoiser.swift:67-76) -- AppleSVGFDenoiser
  * (Denoiser.swift:167-300) -- as spatiotemporal variance-guided filtering

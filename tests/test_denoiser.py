@@ -109,3 +109,26 @@ def test_error_terms_match_a_float64_reduction(renderer):
     want = torch.stack([((da - db) ** 2).sum((1, 2, 3)), ((a - b) ** 2).sum((1, 2, 3)), ((f - df) ** 2).sum((1, 2, 3)),
                         df.sum((1, 2, 3)), f.sum((1, 2, 3))], 1)
     assert torch.allclose(terms.cpu(), want, rtol=1e-5, atol=1e-6)
+
+
+def test_serving_to_an_error_target_falls_back_to_more_samples(renderer):
+    # denoiser.serve_to_error_target through the render server: a target every
+    # estimate meets returns the denoised images after the first round; one no
+    # estimate can meet grows the samples round after round up to max_spp and
+    # returns the plain renders (the fallback).
+    from denrimrendererkit_gb300.denoiser import UNet, serve_to_error_target
+    from denrimrendererkit_gb300.serving import RenderServer, ServerConfig
+    wl = scenes.cornell_variant(7, 64, 64)
+    b = compile_scene(wl.scene)
+    net = UNet(seed=1)
+    reqs = [(wl.settings, wl.scene.camera, None, 0), (wl.settings, wl.scene.camera, None, 0)]
+    with RenderServer(b, ServerConfig(wave_paths=1 << 20)) as srv:
+        loose = serve_to_error_target(srv, net, reqs, 64, 64, target=10.0, start_spp=8)
+        assert all(x.denoised and x.spp == 8 and x.rounds == 1 for x in loose)
+        tight = serve_to_error_target(srv, net, reqs, 64, 64, target=1e-6, start_spp=8, max_spp=64)
+        assert all(not x.denoised and x.spp == 64 and x.rounds == 3 for x in tight)  # 8 -> 32 -> 64
+        for x in tight:
+            img = x.image.cpu().numpy()
+            assert np.isfinite(img).all() and img[..., :3].mean() > 0
+            assert x.estimate.plain > 1e-6
+        assert srv.stats()["jobs_submitted"] == 2 * 2 + 2 * (2 + 1 + 1)
