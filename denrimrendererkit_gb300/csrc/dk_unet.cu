@@ -15,6 +15,8 @@
 // Shared-memory tiles are filled with cp.async (zero fill for the padding)
 // through an XOR swizzle that keeps ldmatrix conflict-free.
 #include <cstdint>
+#include <cstdlib>
+#include <initializer_list>
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -212,19 +214,50 @@ __device__ __forceinline__ uint64_t umaDesc(uint32_t saddr) {
            | ((uint64_t)2 << 61);               // 128-byte swizzle
 }
 
+// tcgen05.mma kind::f16 with both shared-memory descriptors given as their
+// low words (start address >> 4 in bits 0-13, leading byte offset) and the
+// high word they share (stride byte offset, version, 128-byte swizzle): an
+// operand's position inside a tile is then one 32-bit add, and the single
+// issuing thread spends a few instructions per MMA.
+__device__ __forceinline__ uint32_t descLo(uint32_t saddr) { return (uint32_t)umaDesc(saddr); }
+__device__ __forceinline__ uint32_t descHi() { return (uint32_t)(umaDesc(0u) >> 32); }
+__device__ __forceinline__ void mmaF16(uint32_t d, uint32_t aLo, uint32_t bLo, uint32_t hi, uint32_t idesc,
+                                       uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\n.reg .b64 da, db;\nsetp.ne.b32 p, %5, 0;\nmov.b64 da, {%1, %3};\nmov.b64 db, {%2, %3};\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %4, p;\n}\n" ::"r"(d),
+        "r"(aLo), "r"(bLo), "r"(hi), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0u;
+}
 __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
+    if (mbarTryWait(bar, parity)) return true;
     const long long start = clock64();
     for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
+        if (mbarTryWait(bar, parity)) return true;
         if (clock64() - start > 4000000000ll) return false;  // about 2 s
     }
 }
+
+// A slot of an n-slot ring and the parity of its current use, advanced one
+// use at a time (no division on the issuing threads' path).
+struct RingPos {
+    uint32_t slot, phase;
+    __device__ __forceinline__ void advance(uint32_t n) {
+        if (++slot == n) {
+            slot = 0u;
+            phase ^= 1u;
+        }
+    }
+};
 
 __global__ void __launch_bounds__(128, 1) k_conv3x3_tc(ConvArgs a, uint32_t tmemCols) {
     extern __shared__ unsigned char dsm[];
@@ -394,13 +427,17 @@ size_t tcSmemBytes(uint32_t cout) { return (size_t)kTcStages * (kTcRows * 128u +
 // Every mbarrier wait is bounded (about 2 s); a role that times out records
 // the error and stops, the others then time out in turn, and the CTA frees
 // its tensor memory before returning.
-constexpr int kTmaStages = 4;
+constexpr uint32_t kTmaStagesMin = 4;   // (tap, chunk) stages in flight: at least 4,
+constexpr uint32_t kTmaStagesMax = 8;   // more where shared memory holds them
+constexpr uint32_t kTmaBarBytes = 192;  // full[8] empty[8] accFull[2] accEmpty[2], TMEM slot, flag
 
 struct TmaConvArgs {
     const float* bias;
     __nv_bfloat16* out;
     uint32_t n, h, w, cin, cout, ldo, coOff, tw, th, tilesX, tilesY, numTiles, chunks, cols;
+    uint32_t stages;  // kTmaStagesMin..kTmaStagesMax
     int act, accumulate;
+    int staged;  // epilogue rows through shared memory (see epilogueRow)
 };
 
 __device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
@@ -434,6 +471,83 @@ __device__ __forceinline__ void umaCommit(uint32_t bar) {
                  : "memory");
 }
 
+// Shared memory one epilogue warp uses to transpose an output row: 32 pixels
+// of N bf16 channels at a pitch of 2N + 16 bytes (an odd number of 16-byte
+// units, so eight lanes' 16-byte writes fall on distinct banks), then the 32
+// pixels' global row pointers.
+__host__ __device__ constexpr uint32_t epiPitch(uint32_t n) { return 2u * n + 16u; }
+__host__ __device__ constexpr uint32_t epiWarpBytes(uint32_t n) { return 32u * epiPitch(n) + 32u * 8u; }
+
+// One accumulator (this warp's 32 TMEM lanes: 32 output pixels x N channels)
+// to global memory: bias, ReLU, bf16, optionally added to the destination.
+// `dst` is this lane's pixel (its channel 0), nullptr outside the image.
+// With `stage` the warp writes the row into shared memory and then stores
+// every pixel's channels as 16-byte pieces by consecutive lanes (one 32-byte
+// sector per two lanes instead of one per lane and 4-byte store), and hands
+// the accumulator back as soon as it is read; `stage` is null when the
+// destination is accumulated into (its bf16 sum is formed from the FP32
+// value, as on the direct path) or not 16-byte aligned.
+__device__ __forceinline__ void epilogueRow(uint32_t src, uint32_t N, const float* bias, int act, int accumulate,
+                                            __nv_bfloat16* dst, unsigned char* stage, uint32_t accEmptyBar) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t c0 = 0; c0 < N; c0 += 16u) {
+        uint32_t rr[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+            "%12, %13, %14, %15}, [%16];\n"
+            : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
+              "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]),
+              "=r"(rr[15])
+            : "r"(src + c0));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        float v2[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            float x = __uint_as_float(rr[k]);
+            if (bias) x += __ldg(bias + c0 + k);
+            if (act == 1) x = fmaxf(x, 0.0f);
+            v2[k] = x;
+        }
+        if (stage) {
+            uint32_t packed[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                __nv_bfloat162 h2 = __floats2bfloat162_rn(v2[2 * k], v2[2 * k + 1]);
+                packed[k] = *reinterpret_cast<uint32_t*>(&h2);
+            }
+            uint4* s = reinterpret_cast<uint4*>(stage + lane * epiPitch(N) + c0 * 2u);
+            s[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+            s[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+            continue;
+        }
+        if (!dst) continue;
+        __nv_bfloat162* d2 = reinterpret_cast<__nv_bfloat162*>(dst + c0);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            float x0v = v2[2 * k], x1v = v2[2 * k + 1];
+            if (accumulate) {
+                float2 o = __bfloat1622float2(d2[k]);
+                x0v += o.x;
+                x1v += o.y;
+            }
+            d2[k] = __floats2bfloat162_rn(x0v, x1v);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    mbarArrive(accEmptyBar);
+    if (!stage) return;
+    __nv_bfloat16** rows = reinterpret_cast<__nv_bfloat16**>(stage + 32u * epiPitch(N));
+    rows[lane] = dst;
+    __syncwarp();
+    const uint32_t per = N / 8u;  // 16-byte pieces per pixel
+    for (uint32_t j = lane; j < 32u * per; j += 32u) {
+        const uint32_t pix = j / per, part = j - pix * per;
+        __nv_bfloat16* d = rows[pix];
+        if (d) *reinterpret_cast<uint4*>(d + part * 8u) = *reinterpret_cast<const uint4*>(stage + pix * epiPitch(N) + part * 16u);
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(192, 1)
     k_conv3x3_tma(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW, TmaConvArgs a) {
     extern __shared__ unsigned char dsm[];
@@ -442,12 +556,13 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t N = a.cout;
     const uint32_t aBytes = 128u * 128u, bBytes = N * 128u;
     unsigned char* sA = sm;
-    unsigned char* sB = sm + kTmaStages * aBytes;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kTmaStages * bBytes);
+    const uint32_t S = a.stages;
+    unsigned char* sB = sm + S * aBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sB + S * bBytes);
     // bars: full[S], empty[S], accFull[2], accEmpty[2]
-    const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kTmaStages;
-    const uint32_t accFullBar = emptyBar + 8u * kTmaStages, accEmptyBar = accFullBar + 16u;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kTmaStages + 4);
+    const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kTmaStagesMax;
+    const uint32_t accFullBar = emptyBar + 8u * kTmaStagesMax, accEmptyBar = accFullBar + 16u;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kTmaStagesMax + 4);
     int* abortFlag = reinterpret_cast<int*>(tslot + 1);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 
@@ -457,7 +572,7 @@ __global__ void __launch_bounds__(192, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
     if (tid == 0) {
-        for (int s = 0; s < kTmaStages; ++s) {
+        for (uint32_t s = 0; s < S; ++s) {
             mbarInit(fullBar + 8u * s, 1);
             mbarInit(emptyBar + 8u * s, 1);
         }
@@ -473,35 +588,42 @@ __global__ void __launch_bounds__(192, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t taddr = *tslot;
-    const uint32_t kIters = 9u * a.chunks;
     const uint32_t txBytes = aBytes + bBytes;
     volatile int* abortV = abortFlag;
 
     if (warp == 0) {
         if (lane == 0) {
             uint32_t g = 0;
-            for (uint32_t tile = blockIdx.x; tile < a.numTiles && !*abortV; tile += gridDim.x) {
+            RingPos pos{0u, 0u};
+            bool ok = true;
+            for (uint32_t tile = blockIdx.x; ok && tile < a.numTiles && !*abortV; tile += gridDim.x) {
                 uint32_t tx = tile % a.tilesX, rest = tile / a.tilesX;
                 uint32_t ty = rest % a.tilesY, img = rest / a.tilesY;
                 int x0 = (int)(tx * a.tw), y0 = (int)(ty * a.th);
-                for (uint32_t it = 0; it < kIters; ++it, ++g) {
-                    uint32_t s = g % kTmaStages, u = g / kTmaStages;
-                    if (u > 0 && !mbarWait(emptyBar + 8u * s, (u - 1u) & 1u)) {
-                        *abortV = 1;
-                        break;
+                for (uint32_t tap = 0; ok && tap < 9u; ++tap) {
+                    const int dy = (int)(tap / 3u), dx = (int)tap - 3 * dy;
+                    for (uint32_t c = 0; c < a.chunks; ++c, ++g, pos.advance(S)) {
+                        if (g >= S && !mbarWait(emptyBar + 8u * pos.slot, pos.phase ^ 1u)) {
+                            ok = false;
+                            break;
+                        }
+                        const uint32_t full = fullBar + 8u * pos.slot;
+                        mbarExpectTx(full, txBytes);
+                        tmaLoad4(smemAddr(sA + pos.slot * aBytes), &mapIn, (int)(c * 64u), x0 + dx - 1, y0 + dy - 1,
+                                 (int)img, full);
+                        tmaLoad3(smemAddr(sB + pos.slot * bBytes), &mapW, (int)(c * 64u), (int)tap, 0, full);
                     }
-                    uint32_t tap = it / a.chunks, c0 = (it - tap * a.chunks) * 64u;
-                    mbarExpectTx(fullBar + 8u * s, txBytes);
-                    tmaLoad4(smemAddr(sA + s * aBytes), &mapIn, (int)c0, x0 + (int)(tap % 3u) - 1,
-                             y0 + (int)(tap / 3u) - 1, (int)img, fullBar + 8u * s);
-                    tmaLoad3(smemAddr(sB + s * bBytes), &mapW, (int)c0, (int)tap, 0, fullBar + 8u * s);
                 }
             }
+            if (!ok) *abortV = 1;
         }
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
-            uint32_t g = 0, t = 0;
+            const uint32_t hi = descHi(), aLo0 = descLo(smemAddr(sA)), bLo0 = descLo(smemAddr(sB));
+            const uint32_t lastSteps = (a.cin - (a.chunks - 1u) * 64u + 15u) / 16u;
+            RingPos pos{0u, 0u};
+            uint32_t t = 0;
             for (uint32_t tile = blockIdx.x; tile < a.numTiles && !*abortV; tile += gridDim.x, ++t) {
                 uint32_t b = t & 1u, v = t >> 1;
                 if (v > 0 && !mbarWait(accEmptyBar + 8u * b, (v - 1u) & 1u)) {
@@ -511,25 +633,24 @@ __global__ void __launch_bounds__(192, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint32_t dAddr = taddr + b * a.cols;
                 bool ok = true;
-                for (uint32_t it = 0; it < kIters; ++it, ++g) {
-                    uint32_t s = g % kTmaStages, u = g / kTmaStages;
-                    if (!mbarWait(fullBar + 8u * s, u & 1u)) {
-                        ok = false;
-                        break;
+                uint32_t acc = 0u;
+                for (uint32_t it = 0; ok && it < 9u; ++it) {
+                    for (uint32_t c = 0; c < a.chunks; ++c, pos.advance(S)) {
+                        if (!mbarWait(fullBar + 8u * pos.slot, pos.phase)) {
+                            ok = false;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                        // K steps of 16 channels in this (tap, chunk): 4, fewer in a partial last chunk
+                        const uint32_t steps = c + 1u < a.chunks ? 4u : lastSteps;
+                        const uint32_t aLo = aLo0 + pos.slot * (aBytes >> 4), bLo = bLo0 + pos.slot * (bBytes >> 4);
+                        mmaF16(dAddr, aLo, bLo, hi, idesc, acc);
+                        acc = 1u;
+                        if (steps > 1u) mmaF16(dAddr, aLo + 2u, bLo + 2u, hi, idesc, 1u);
+                        if (steps > 2u) mmaF16(dAddr, aLo + 4u, bLo + 4u, hi, idesc, 1u);
+                        if (steps > 3u) mmaF16(dAddr, aLo + 6u, bLo + 6u, hi, idesc, 1u);
+                        umaCommit(emptyBar + 8u * pos.slot);  // the stage is free once these MMAs are done
                     }
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    const uint32_t c0 = (it % a.chunks) * 64u;
-                    const uint32_t aBase = smemAddr(sA + s * aBytes), bBase = smemAddr(sB + s * bBytes);
-                    for (uint32_t ks = 0; ks < 4; ++ks) {
-                        if (c0 + ks * 16u >= a.cin) break;
-                        uint64_t ad = umaDesc(aBase + ks * 32u), bd = umaDesc(bBase + ks * 32u);
-                        uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
-                        asm volatile(
-                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dAddr),
-                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-                    }
-                    umaCommit(emptyBar + 8u * s);  // the stage is free once these MMAs are done
                 }
                 if (!ok) {
                     *abortV = 1;
@@ -542,6 +663,8 @@ __global__ void __launch_bounds__(192, 1)
         // Epilogue warps 2..5: TMEM lane quarter (warp % 4).
         const uint32_t q = warp & 3u;
         const uint32_t r = q * 32u + lane;
+        unsigned char* stage =
+            a.staged ? reinterpret_cast<unsigned char*>(bars) + kTmaBarBytes + q * epiWarpBytes(N) : nullptr;
         uint32_t t = 0;
         for (uint32_t tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++t) {
             uint32_t b = t & 1u, v = t >> 1;
@@ -554,41 +677,9 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t ty = rest % a.tilesY, img = rest / a.tilesY;
             uint32_t px = tx * a.tw + r % a.tw, py = ty * a.th + r / a.tw;
             bool valid = px < a.w && py < a.h;
-            __nv_bfloat16* orow = a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff;
-            const uint32_t src = taddr + ((q * 32u) << 16) + b * a.cols;
-            for (uint32_t c0 = 0; c0 < N; c0 += 16u) {
-                uint32_t rr[16];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-                    "%13, %14, %15}, [%16];\n"
-                    : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]),
-                      "=r"(rr[7]), "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]),
-                      "=r"(rr[14]), "=r"(rr[15])
-                    : "r"(src + c0));
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (!valid) continue;
-                float v2[16];
-#pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                    float x = __uint_as_float(rr[k]);
-                    if (a.bias) x += a.bias[c0 + k];
-                    if (a.act == 1) x = fmaxf(x, 0.0f);
-                    v2[k] = x;
-                }
-                __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(orow + c0);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    float x0v = v2[2 * k], x1v = v2[2 * k + 1];
-                    if (a.accumulate) {
-                        float2 o = __bfloat1622float2(dst[k]);
-                        x0v += o.x;
-                        x1v += o.y;
-                    }
-                    dst[k] = __floats2bfloat162_rn(x0v, x1v);
-                }
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            mbarArrive(accEmptyBar + 8u * b);
+            __nv_bfloat16* orow = valid ? a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff : nullptr;
+            epilogueRow(taddr + ((q * 32u) << 16) + b * a.cols, N, a.bias, a.act, a.accumulate, orow, stage,
+                        accEmptyBar + 8u * b);
         }
     }
     __syncthreads();
@@ -597,7 +688,9 @@ __global__ void __launch_bounds__(192, 1)
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(2u * a.cols));
 }
 
-size_t tmaSmemBytes(uint32_t cout) { return (size_t)kTmaStages * (128u * 128u + cout * 128u) + 1024u + 128u; }
+size_t tmaSmemBytes(uint32_t cout, bool staged, uint32_t stages) {
+    return (size_t)stages * (128u * 128u + cout * 128u) + 1024u + kTmaBarBytes + (staged ? 4u * epiWarpBytes(cout) : 0u);
+}
 
 // -------------------------------------- tcgen05 + TMA, halo-row ring ----
 // The convolution for wide, shallow layers (the full- and half-resolution
@@ -618,7 +711,9 @@ size_t tmaSmemBytes(uint32_t cout) { return (size_t)kTmaStages * (128u * 128u + 
 //              accumulators; releases a halo row once its last reader is done;
 //   warps 2-5  epilogue as in k_conv3x3_tma.
 // Waits are bounded as there.
-constexpr uint32_t kHaloRing = 4;           // halo-row slots
+constexpr uint32_t kHaloRingMin = 4;        // halo-row slots: three rows in use and one loading at least,
+constexpr uint32_t kHaloRingMax = 16;       // and as many more loading as shared memory holds
+constexpr uint32_t kHaloBarBytes = 384;     // full[16] empty[16] weights accFull[2] accEmpty[2], TMEM slot, flag
 constexpr uint32_t kHaloPix = 130;          // 128 output pixels and one on each side
 constexpr uint32_t kHaloSlotBytes = 17408;  // 130 rows of 128 B, padded to 17 x 1024 B
 
@@ -627,7 +722,9 @@ struct HaloConvArgs {
     __nv_bfloat16* out;
     uint32_t n, h, w, cin, cout, ldo, coOff;
     uint32_t tilesX, rowBlock, rowBlocks, numItems, chunks, cols;
+    uint32_t ring;  // halo-row slots, kHaloRingMin..kHaloRingMax
     int act, accumulate;
+    int staged;  // epilogue rows through shared memory (see epilogueRow)
 };
 
 __global__ void __launch_bounds__(192, 1)
@@ -640,12 +737,13 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t slotBytes = C * kHaloSlotBytes;
     const uint32_t wBoxBytes = N * 128u, wBytes = 9u * C * wBoxBytes;
     unsigned char* sRing = sm;
-    unsigned char* sW = sm + kHaloRing * slotBytes;
+    const uint32_t R = a.ring;
+    unsigned char* sW = sm + R * slotBytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sW + wBytes);
     // bars: full[R], empty[R], weights, accFull[2], accEmpty[2]
-    const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kHaloRing;
-    const uint32_t wBar = emptyBar + 8u * kHaloRing, accFullBar = wBar + 8u, accEmptyBar = accFullBar + 16u;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kHaloRing + 5);
+    const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kHaloRingMax;
+    const uint32_t wBar = emptyBar + 8u * kHaloRingMax, accFullBar = wBar + 8u, accEmptyBar = accFullBar + 16u;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kHaloRingMax + 5);
     int* abortFlag = reinterpret_cast<int*>(tslot + 1);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 
@@ -655,7 +753,7 @@ __global__ void __launch_bounds__(192, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
     if (tid == 0) {
-        for (uint32_t s = 0; s < kHaloRing; ++s) {
+        for (uint32_t s = 0; s < R; ++s) {
             mbarInit(fullBar + 8u * s, 1);
             mbarInit(emptyBar + 8u * s, 1);
         }
@@ -681,22 +779,23 @@ __global__ void __launch_bounds__(192, 1)
                 for (uint32_t c = 0; c < C; ++c)
                     tmaLoad3(smemAddr(sW + (tap * C + c) * wBoxBytes), &mapW, (int)(c * 64u), (int)tap, 0, wBar);
             uint32_t g = 0;
+            RingPos pos{0u, 0u};
             for (uint32_t item = blockIdx.x; item < a.numItems && !*abortV; item += gridDim.x) {
                 const uint32_t tx = item % a.tilesX, rest = item / a.tilesX;
                 const uint32_t rb = rest % a.rowBlocks, img = rest / a.rowBlocks;
                 const int x0 = (int)(tx * 128u), y0 = (int)(rb * a.rowBlock);
                 const int y1 = min((int)a.h, y0 + (int)a.rowBlock);
                 bool ok = true;
-                for (int hy = y0 - 1; hy <= y1; ++hy, ++g) {
-                    const uint32_t s = g % kHaloRing, u = g / kHaloRing;
-                    if (u > 0 && !mbarWait(emptyBar + 8u * s, (u - 1u) & 1u)) {
+                for (int hy = y0 - 1; hy <= y1; ++hy, ++g, pos.advance(R)) {
+                    if (g >= R && !mbarWait(emptyBar + 8u * pos.slot, pos.phase ^ 1u)) {
                         ok = false;
                         break;
                     }
-                    mbarExpectTx(fullBar + 8u * s, C * kHaloPix * 128u);
+                    const uint32_t full = fullBar + 8u * pos.slot;
+                    mbarExpectTx(full, C * kHaloPix * 128u);
                     for (uint32_t c = 0; c < C; ++c)
-                        tmaLoad4(smemAddr(sRing + s * slotBytes + c * kHaloSlotBytes), &mapIn, (int)(c * 64u), x0 - 1,
-                                 hy, (int)img, fullBar + 8u * s);
+                        tmaLoad4(smemAddr(sRing + pos.slot * slotBytes + c * kHaloSlotBytes), &mapIn, (int)(c * 64u),
+                                 x0 - 1, hy, (int)img, full);
                 }
                 if (!ok) {
                     *abortV = 1;
@@ -707,56 +806,62 @@ __global__ void __launch_bounds__(192, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
-            const uint32_t ringBase = smemAddr(sRing), wBase = smemAddr(sW);
+            const uint32_t hi = descHi(), aLo0 = descLo(smemAddr(sRing)), bLo0 = descLo(smemAddr(sW));
+            const uint32_t lastSteps = (a.cin - (C - 1u) * 64u + 15u) / 16u;  // K steps of the last chunk
             bool ok = mbarWait(wBar, 0u);
-            uint32_t g = 0, t = 0;
+            uint32_t t = 0;
+            RingPos top{0u, 0u};  // the item's first halo row
             for (uint32_t item = blockIdx.x; ok && item < a.numItems && !*abortV; item += gridDim.x) {
                 const uint32_t rest = item / a.tilesX;
                 const uint32_t rb = rest % a.rowBlocks;
                 const uint32_t y0 = rb * a.rowBlock, y1 = min(a.h, y0 + a.rowBlock);
                 const uint32_t rows = y1 - y0;
+                // halo rows w0, w1, w2 feed the current output row
+                RingPos w0 = top, w1 = top, w2;
+                w1.advance(R);
+                w2 = w1;
+                w2.advance(R);
+                if (!mbarWait(fullBar + 8u * w0.slot, w0.phase) || !mbarWait(fullBar + 8u * w1.slot, w1.phase))
+                    ok = false;
                 for (uint32_t k = 0; ok && k < rows; ++k, ++t) {
-                    // halo rows g + k .. g + k + 2 feed output row y0 + k
-                    for (uint32_t j = (k == 0 ? 0u : 2u); j < 3u; ++j) {
-                        const uint32_t idx = g + k + j;
-                        if (!mbarWait(fullBar + 8u * (idx % kHaloRing), (idx / kHaloRing) & 1u)) ok = false;
-                    }
+                    if (!mbarWait(fullBar + 8u * w2.slot, w2.phase)) ok = false;
                     const uint32_t b = t & 1u, v = t >> 1;
                     if (ok && v > 0 && !mbarWait(accEmptyBar + 8u * b, (v - 1u) & 1u)) ok = false;
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                     const uint32_t dAddr = taddr + b * a.cols;
-                    uint32_t acc = 0;
+                    // A run that starts inside the 1024-byte swizzle pattern (pixel dx)
+                    // takes the plain descriptor: the tensor core applies the 128-byte
+                    // swizzle to absolute shared-memory address bits, as the copy engine
+                    // wrote it (measured: a base offset of (start >> 7) & 7 gives wrong sums).
+                    const uint32_t rowLo[3] = {aLo0 + w0.slot * (slotBytes >> 4), aLo0 + w1.slot * (slotBytes >> 4),
+                                               aLo0 + w2.slot * (slotBytes >> 4)};
+                    uint32_t acc = 0u;
+#pragma unroll
                     for (uint32_t tap = 0; tap < 9u; ++tap) {
                         const uint32_t dy = tap / 3u, dx = tap - dy * 3u;
-                        const uint32_t slot = (g + k + dy) % kHaloRing;
+                        const uint32_t aT = rowLo[dy] + dx * 8u;  // pixel dx: 128 bytes further
+                        const uint32_t bT = bLo0 + tap * C * (wBoxBytes >> 4);
                         for (uint32_t c = 0; c < C; ++c) {
-                            const uint32_t aBase = ringBase + slot * slotBytes + c * kHaloSlotBytes + dx * 128u;
-                            const uint32_t bBase = wBase + (tap * C + c) * wBoxBytes;
-                            for (uint32_t ks = 0; ks < 4u; ++ks) {
-                                if (c * 64u + ks * 16u >= a.cin) break;
-                                // A run that starts inside the 1024-byte swizzle pattern
-                                // (pixel dx) takes the plain descriptor: the tensor core
-                                // applies the 128-byte swizzle to absolute shared-memory
-                                // address bits, as the copy engine wrote it (measured:
-                                // a base offset of (start >> 7) & 7 gives wrong sums).
-                                const uint64_t ad = umaDesc(aBase + ks * 32u);
-                                const uint64_t bd = umaDesc(bBase + ks * 32u);
-                                asm volatile(
-                                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dAddr),
-                                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-                                acc = 1u;
-                            }
+                            const uint32_t steps = c + 1u < C ? 4u : lastSteps;
+                            const uint32_t aC = aT + c * (kHaloSlotBytes >> 4), bC = bT + c * (wBoxBytes >> 4);
+                            mmaF16(dAddr, aC, bC, hi, idesc, acc);
+                            acc = 1u;
+                            if (steps > 1u) mmaF16(dAddr, aC + 2u, bC + 2u, hi, idesc, 1u);
+                            if (steps > 2u) mmaF16(dAddr, aC + 4u, bC + 4u, hi, idesc, 1u);
+                            if (steps > 3u) mmaF16(dAddr, aC + 6u, bC + 6u, hi, idesc, 1u);
                         }
                     }
-                    umaCommit(accFullBar + 8u * b);                      // output row complete
-                    umaCommit(emptyBar + 8u * ((g + k) % kHaloRing));    // its top halo row has no reader left
+                    umaCommit(accFullBar + 8u * b);          // output row complete
+                    umaCommit(emptyBar + 8u * w0.slot);      // its top halo row has no reader left
+                    w0 = w1;
+                    w1 = w2;
+                    w2.advance(R);
                 }
                 if (!ok) break;
-                umaCommit(emptyBar + 8u * ((g + rows) % kHaloRing));     // the item's last two halo rows
-                umaCommit(emptyBar + 8u * ((g + rows + 1u) % kHaloRing));
-                g += rows + 2u;
+                umaCommit(emptyBar + 8u * w0.slot);  // the item's last two halo rows
+                umaCommit(emptyBar + 8u * w1.slot);
+                top = w2;
             }
             if (!ok) *abortV = 1;
         }
@@ -764,6 +869,8 @@ __global__ void __launch_bounds__(192, 1)
         // Epilogue warps 2..5: TMEM lane quarter (warp % 4), one output pixel per thread.
         const uint32_t q = warp & 3u;
         const uint32_t r = q * 32u + lane;
+        unsigned char* stage =
+            a.staged ? reinterpret_cast<unsigned char*>(bars) + kHaloBarBytes + q * epiWarpBytes(N) : nullptr;
         uint32_t t = 0;
         bool ok = true;
         for (uint32_t item = blockIdx.x; ok && item < a.numItems; item += gridDim.x) {
@@ -779,42 +886,10 @@ __global__ void __launch_bounds__(192, 1)
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                const bool valid = px < a.w;
-                __nv_bfloat16* orow = a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff;
-                const uint32_t src = taddr + ((q * 32u) << 16) + b * a.cols;
-                for (uint32_t c0 = 0; c0 < N; c0 += 16u) {
-                    uint32_t rr[16];
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                        "%12, %13, %14, %15}, [%16];\n"
-                        : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]),
-                          "=r"(rr[7]), "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]),
-                          "=r"(rr[13]), "=r"(rr[14]), "=r"(rr[15])
-                        : "r"(src + c0));
-                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                    if (!valid) continue;
-                    float v2[16];
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        float x = __uint_as_float(rr[k]);
-                        if (a.bias) x += a.bias[c0 + k];
-                        if (a.act == 1) x = fmaxf(x, 0.0f);
-                        v2[k] = x;
-                    }
-                    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(orow + c0);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        float x0v = v2[2 * k], x1v = v2[2 * k + 1];
-                        if (a.accumulate) {
-                            float2 o = __bfloat1622float2(dst[k]);
-                            x0v += o.x;
-                            x1v += o.y;
-                        }
-                        dst[k] = __floats2bfloat162_rn(x0v, x1v);
-                    }
-                }
-                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-                mbarArrive(accEmptyBar + 8u * b);
+                __nv_bfloat16* orow =
+                    px < a.w ? a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff : nullptr;
+                epilogueRow(taddr + ((q * 32u) << 16) + b * a.cols, N, a.bias, a.act, a.accumulate, orow, stage,
+                            accEmptyBar + 8u * b);
             }
         }
     }
@@ -824,8 +899,9 @@ __global__ void __launch_bounds__(192, 1)
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(2u * a.cols));
 }
 
-size_t haloSmemBytes(uint32_t cout, uint32_t chunks) {
-    return 1024u + (size_t)kHaloRing * chunks * kHaloSlotBytes + 9u * (size_t)chunks * cout * 128u + 128u;
+size_t haloSmemBytes(uint32_t cout, uint32_t chunks, bool staged, uint32_t ring) {
+    return 1024u + (size_t)ring * chunks * kHaloSlotBytes + 9u * (size_t)chunks * cout * 128u + kHaloBarBytes +
+           (staged ? 4u * epiWarpBytes(cout) : 0u);
 }
 
 // -------------------------------------------------------------- wgrad ----
@@ -1066,6 +1142,142 @@ __global__ void k_copy_channels(const __nv_bfloat16* src, uint32_t lds, uint32_t
     }
 }
 
+// The same element-wise layers over groups of 8 channels (one 16-byte load or
+// store per group) with 32-bit indices: used when every channel count, leading
+// dimension and offset is a multiple of 8, the pointers are 16-byte aligned
+// and the element count fits 32 bits (the host checks); the arithmetic per
+// channel is the one of the kernels above.
+__device__ __forceinline__ void ld8(const __nv_bfloat16* p, float (&f)[8]) {
+    const uint4 u = *reinterpret_cast<const uint4*>(p);
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[k]));
+        f[2 * k] = t.x;
+        f[2 * k + 1] = t.y;
+    }
+}
+__device__ __forceinline__ void st8(__nv_bfloat16* p, const float (&f)[8]) {
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        __nv_bfloat162 h2 = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+        w[k] = *reinterpret_cast<uint32_t*>(&h2);
+    }
+    *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void k_relu_backward8(const __nv_bfloat16* out, uint32_t ldo, const __nv_bfloat16* dout, uint32_t ldd,
+                                 __nv_bfloat16* dpre, uint32_t ldp, uint32_t groups, uint32_t total) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
+        const uint32_t p = i / groups, k = (i - p * groups) * 8u;
+        float o[8], d[8];
+        ld8(out + (size_t)p * ldo + k, o);
+        ld8(dout + (size_t)p * ldd + k, d);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) d[j] = o[j] > 0.0f ? d[j] : 0.0f;
+        st8(dpre + (size_t)p * ldp + k, d);
+    }
+}
+
+__global__ void k_avgpool2_8(const __nv_bfloat16* in, uint32_t ldi, __nv_bfloat16* out, uint32_t ldo, uint32_t coOff,
+                             uint32_t groups, uint32_t h, uint32_t w, uint32_t total) {
+    const uint32_t wo = w / 2u, ho = h / 2u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
+        const uint32_t q = i / groups, k = (i - q * groups) * 8u;
+        const uint32_t x = q % wo, r = q / wo, y = r % ho, b = r / ho;
+        const size_t base = ((size_t)(b * h + 2u * y) * w + 2u * x) * ldi + k;
+        float s[8], t[8], u[8], v[8];
+        ld8(in + base, s);
+        ld8(in + base + ldi, t);
+        ld8(in + base + (size_t)w * ldi, u);
+        ld8(in + base + (size_t)w * ldi + ldi, v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s[j] = 0.25f * (s[j] + t[j] + u[j] + v[j]);
+        st8(out + (size_t)q * ldo + coOff + k, s);
+    }
+}
+
+__global__ void k_avgpool2_backward8(const __nv_bfloat16* dout, uint32_t ldd, __nv_bfloat16* din, uint32_t ldi,
+                                     uint32_t groups, uint32_t h, uint32_t w, int accumulate, uint32_t total) {
+    // one thread per pooled pixel and group: its gradient goes to the 4 inputs
+    const uint32_t wo = w / 2u, ho = h / 2u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
+        const uint32_t q = i / groups, k = (i - q * groups) * 8u;
+        const uint32_t x = q % wo, r = q / wo, y = r % ho, b = r / ho;
+        float d[8];
+        ld8(dout + (size_t)q * ldd + k, d);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) d[j] *= 0.25f;
+        const size_t base = ((size_t)(b * h + 2u * y) * w + 2u * x) * ldi + k;
+        const size_t offs[4] = {0, ldi, (size_t)w * ldi, (size_t)w * ldi + ldi};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[j] = d[j];
+            if (accumulate) {
+                float o[8];
+                ld8(din + base + offs[c], o);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) v[j] += o[j];
+            }
+            st8(din + base + offs[c], v);
+        }
+    }
+}
+
+__global__ void k_upsample2_8(const __nv_bfloat16* in, uint32_t ldi, __nv_bfloat16* out, uint32_t ldo, uint32_t coOff,
+                              uint32_t groups, uint32_t h, uint32_t w, uint32_t total) {
+    // one thread per input pixel and group, written to its 2x2 outputs
+    const uint32_t W = 2u * w;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
+        const uint32_t q = i / groups, k = (i - q * groups) * 8u;
+        const uint32_t x = q % w, r = q / w, y = r % h, b = r / h;
+        const uint4 v = *reinterpret_cast<const uint4*>(in + (size_t)q * ldi + k);
+        const size_t o = ((size_t)(b * 2u * h + 2u * y) * W + 2u * x) * ldo + coOff + k;
+        *reinterpret_cast<uint4*>(out + o) = v;
+        *reinterpret_cast<uint4*>(out + o + ldo) = v;
+        *reinterpret_cast<uint4*>(out + o + (size_t)W * ldo) = v;
+        *reinterpret_cast<uint4*>(out + o + (size_t)W * ldo + ldo) = v;
+    }
+}
+
+__global__ void k_upsample2_backward8(const __nv_bfloat16* dout, uint32_t ldd, uint32_t ciOff, __nv_bfloat16* din,
+                                      uint32_t ldi, uint32_t groups, uint32_t h, uint32_t w, uint32_t total) {
+    const uint32_t W = 2u * w;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
+        const uint32_t q = i / groups, k = (i - q * groups) * 8u;
+        const uint32_t x = q % w, r = q / w, y = r % h, b = r / h;
+        const size_t base = ((size_t)(b * 2u * h + 2u * y) * W + 2u * x) * ldd + ciOff + k;
+        float s[8], t[8], u[8], v[8];
+        ld8(dout + base, s);
+        ld8(dout + base + ldd, t);
+        ld8(dout + base + (size_t)W * ldd, u);
+        ld8(dout + base + (size_t)W * ldd + ldd, v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s[j] = s[j] + t[j] + u[j] + v[j];
+        st8(din + (size_t)q * ldi + k, s);
+    }
+}
+
+__global__ void k_copy_channels8(const __nv_bfloat16* src, uint32_t lds, uint32_t sOff, __nv_bfloat16* dst,
+                                 uint32_t ldd, uint32_t dOff, uint32_t groups, int accumulate, uint32_t total) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
+        const uint32_t p = i / groups, k = (i - p * groups) * 8u;
+        float v[8];
+        ld8(src + (size_t)p * lds + sOff + k, v);
+        __nv_bfloat16* d = dst + (size_t)p * ldd + dOff + k;
+        if (accumulate) {
+            float o[8];
+            ld8(d, o);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[j] += o[j];
+        }
+        st8(d, v);
+    }
+}
+
 // Network input: 16 channels per pixel from the AOV planes (RGBA32F, image
 // rows y0.., columns x0.. of a W_img-wide image; pixels outside the image are
 // zero): log(1 + beauty) (3), albedo (3), normal in [-1, 1] (3), depth / (1 +
@@ -1202,6 +1414,17 @@ inline int gridFor(uint64_t work, int block = 256) {
 
 inline bool aligned16(uint32_t v) { return v % 16u == 0u; }
 
+// The 8-channel element-wise kernels apply: channel counts, leading
+// dimensions and offsets multiples of 8, pointers 16-byte aligned, and the
+// element count within 32 bits.
+inline bool vec8(std::initializer_list<uint32_t> counts, std::initializer_list<const void*> ptrs, uint64_t total) {
+    for (uint32_t v : counts)
+        if (v % 8u) return false;
+    for (const void* q : ptrs)
+        if (reinterpret_cast<uintptr_t>(q) % 16u) return false;
+    return total > 0 && total < (1ull << 31);
+}
+
 // 3: halo-row TMA + tcgen05 convolution where the layer fits it, else the
 // per-tap one (default); 2: the per-tap persistent TMA + tcgen05 convolution;
 // 1: the cp.async + tcgen05 one; 0: the mma.sync one.
@@ -1226,14 +1449,37 @@ EncodeTiledFn encodeTiled() {
     return fn;
 }
 
+// Pipeline depth limit from the environment (a tuning knob, read at each
+// launch), clamped to [lo, hi]; hi when unset.
+uint32_t depthCap(const char* name, uint32_t lo, uint32_t hi) {
+    const char* e = getenv(name);
+    if (!e || !*e) return hi;
+    const long v = strtol(e, nullptr, 10);
+    return v < (long)lo ? lo : (v > (long)hi ? hi : (uint32_t)v);
+}
+
+// Output rows go through the epilogue's shared-memory transpose when the
+// destination is overwritten and every pixel's channel run starts on a
+// 16-byte boundary.
+bool stagedStores(const ConvArgs& c) {
+    return !c.accumulate && c.cout % 8u == 0u && c.ldo % 8u == 0u && c.coOff % 8u == 0u &&
+           reinterpret_cast<uintptr_t>(c.out) % 16u == 0u;
+}
+
 // The halo-row kernel's launch, or kHaloUnfit (nothing launched) when the
 // layer does not fit it: narrow images, or weights and halo ring beyond the
 // shared memory of one CTA.
 constexpr int kHaloUnfit = -1;
 int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     const uint32_t chunks = (c.cin + 63u) / 64u;
-    const size_t smem = haloSmemBytes(c.cout, chunks);
-    if (c.w_ < 128u || c.cout > 256u || smem > (size_t)deviceProp().sharedMemPerBlockOptin) return kHaloUnfit;
+    const size_t optin = (size_t)deviceProp().sharedMemPerBlockOptin;
+    if (c.w_ < 128u || c.cout > 256u || haloSmemBytes(c.cout, chunks, false, kHaloRingMin) > optin) return kHaloUnfit;
+    const bool staged = stagedStores(c) && haloSmemBytes(c.cout, chunks, true, kHaloRingMin) <= optin;
+    // The deepest ring that fits: every slot beyond three is a row in flight.
+    uint32_t ring = kHaloRingMin;
+    const uint32_t ringCap = depthCap("DK_CONV_HALO_RING", kHaloRingMin, kHaloRingMax);
+    while (ring < ringCap && haloSmemBytes(c.cout, chunks, staged, ring + 1u) <= optin) ++ring;
+    const size_t smem = haloSmemBytes(c.cout, chunks, staged, ring);
     EncodeTiledFn enc = encodeTiled();
     if (!enc) return fail(DK_ERROR_COMMAND_FAILED, "cuTensorMapEncodeTiled is not available");
     HaloConvArgs a;
@@ -1248,6 +1494,8 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     a.coOff = c.coOff;
     a.act = c.act;
     a.accumulate = c.accumulate;
+    a.staged = staged ? 1 : 0;
+    a.ring = ring;
     a.chunks = chunks;
     a.cols = 32u;
     while (a.cols < c.cout) a.cols <<= 1;
@@ -1328,7 +1576,14 @@ int launchConvTma(const ConvArgs& c, cudaStream_t st) {
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "weight tensor map rejected");
-    size_t smem = tmaSmemBytes(c.cout);
+    const size_t optin = (size_t)deviceProp().sharedMemPerBlockOptin;
+    const bool staged = stagedStores(c) && tmaSmemBytes(c.cout, true, kTmaStagesMin) <= optin;
+    uint32_t stages = kTmaStagesMin;
+    const uint32_t stageCap = depthCap("DK_CONV_STAGES", kTmaStagesMin, kTmaStagesMax);
+    while (stages < stageCap && tmaSmemBytes(c.cout, staged, stages + 1u) <= optin) ++stages;
+    a.staged = staged ? 1 : 0;
+    a.stages = stages;
+    size_t smem = tmaSmemBytes(c.cout, staged, stages);
     static size_t configured = 0;
     if (smem > configured) {
         DK_CUDA(cudaFuncSetAttribute(k_conv3x3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -1428,6 +1683,14 @@ int dk_unet_conv3x3_wgrad(const void* in, uint32_t ldi, const void* dout, uint32
 int dk_unet_relu_backward(const void* out, uint32_t ldo, const void* dout, uint32_t ldd, void* dpre, uint32_t ldp,
                           uint32_t c, uint32_t pixels, void* stream) {
     if (!out || !dout || !dpre || c % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_relu_backward");
+    const uint64_t total8 = (uint64_t)pixels * (c / 8u);
+    if (dk::vec8({c, ldo, ldd, ldp}, {out, dout, dpre}, total8)) {
+        dk::k_relu_backward8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const bf16*>(out), ldo, static_cast<const bf16*>(dout), ldd, static_cast<bf16*>(dpre), ldp,
+            c / 8u, (uint32_t)total8);
+        DK_CUDA(cudaGetLastError(), "relu backward launch");
+        return DK_OK;
+    }
     dk::k_relu_backward<<<dk::gridFor((uint64_t)pixels * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const bf16*>(out), ldo, static_cast<const bf16*>(dout), ldd, static_cast<bf16*>(dpre), ldp, c,
         pixels);
@@ -1449,6 +1712,13 @@ int dk_unet_bias_grad(const void* dpre, uint32_t ld, uint32_t c, uint32_t pixels
 int dk_unet_avgpool2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint32_t coOff, uint32_t c, uint32_t n,
                      uint32_t h, uint32_t w, void* stream) {
     if (!in || !out || c % 2u || h % 2u || w % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_avgpool2");
+    const uint64_t total8 = (uint64_t)n * (h / 2u) * (w / 2u) * (c / 8u);
+    if (dk::vec8({c, ldi, ldo, coOff}, {in, out}, total8)) {
+        dk::k_avgpool2_8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c / 8u, h, w, (uint32_t)total8);
+        DK_CUDA(cudaGetLastError(), "avgpool launch");
+        return DK_OK;
+    }
     dk::k_avgpool2<<<dk::gridFor((uint64_t)n * h * w / 4 * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c, n, h, w);
     DK_CUDA(cudaGetLastError(), "avgpool launch");
@@ -1459,6 +1729,14 @@ int dk_unet_avgpool2_backward(const void* dout, uint32_t ldd, void* din, uint32_
                               uint32_t h, uint32_t w, int accumulate, void* stream) {
     if (!dout || !din || c % 2u || h % 2u || w % 2u)
         return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_avgpool2_backward");
+    const uint64_t total8 = (uint64_t)n * (h / 2u) * (w / 2u) * (c / 8u);
+    if (dk::vec8({c, ldd, ldi}, {dout, din}, total8)) {
+        dk::k_avgpool2_backward8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const bf16*>(dout), ldd, static_cast<bf16*>(din), ldi, c / 8u, h, w, accumulate,
+            (uint32_t)total8);
+        DK_CUDA(cudaGetLastError(), "avgpool backward launch");
+        return DK_OK;
+    }
     dk::k_avgpool2_backward<<<dk::gridFor((uint64_t)n * h * w * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const bf16*>(dout), ldd, static_cast<bf16*>(din), ldi, c, n, h, w, accumulate);
     DK_CUDA(cudaGetLastError(), "avgpool backward launch");
@@ -1468,6 +1746,13 @@ int dk_unet_avgpool2_backward(const void* dout, uint32_t ldd, void* din, uint32_
 int dk_unet_upsample2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint32_t coOff, uint32_t c, uint32_t n,
                       uint32_t h, uint32_t w, void* stream) {
     if (!in || !out || c % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_upsample2");
+    const uint64_t total8 = (uint64_t)n * h * w * (c / 8u);
+    if (dk::vec8({c, ldi, ldo, coOff}, {in, out}, total8)) {
+        dk::k_upsample2_8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c / 8u, h, w, (uint32_t)total8);
+        DK_CUDA(cudaGetLastError(), "upsample launch");
+        return DK_OK;
+    }
     dk::k_upsample2<<<dk::gridFor((uint64_t)n * h * w * 4 * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c, n, h, w);
     DK_CUDA(cudaGetLastError(), "upsample launch");
@@ -1477,6 +1762,13 @@ int dk_unet_upsample2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uin
 int dk_unet_upsample2_backward(const void* dout, uint32_t ldd, uint32_t ciOff, void* din, uint32_t ldi, uint32_t c,
                                uint32_t n, uint32_t h, uint32_t w, void* stream) {
     if (!dout || !din || c % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_upsample2_backward");
+    const uint64_t total8 = (uint64_t)n * h * w * (c / 8u);
+    if (dk::vec8({c, ldd, ciOff, ldi}, {dout, din}, total8)) {
+        dk::k_upsample2_backward8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const bf16*>(dout), ldd, ciOff, static_cast<bf16*>(din), ldi, c / 8u, h, w, (uint32_t)total8);
+        DK_CUDA(cudaGetLastError(), "upsample backward launch");
+        return DK_OK;
+    }
     dk::k_upsample2_backward<<<dk::gridFor((uint64_t)n * h * w * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const bf16*>(dout), ldd, ciOff, static_cast<bf16*>(din), ldi, c, n, h, w);
     DK_CUDA(cudaGetLastError(), "upsample backward launch");
@@ -1487,6 +1779,14 @@ int dk_unet_copy_channels(const void* src, uint32_t lds, uint32_t sOff, void* ds
                           uint32_t c, uint32_t pixels, int accumulate, void* stream) {
     if (!src || !dst || c % 2u || sOff % 2u || dOff % 2u)
         return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_copy_channels");
+    const uint64_t total8 = (uint64_t)pixels * (c / 8u);
+    if (dk::vec8({c, lds, sOff, ldd, dOff}, {src, dst}, total8)) {
+        dk::k_copy_channels8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const bf16*>(src), lds, sOff, static_cast<bf16*>(dst), ldd, dOff, c / 8u, accumulate,
+            (uint32_t)total8);
+        DK_CUDA(cudaGetLastError(), "copy channels launch");
+        return DK_OK;
+    }
     dk::k_copy_channels<<<dk::gridFor((uint64_t)pixels * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const bf16*>(src), lds, sOff, static_cast<bf16*>(dst), ldd, dOff, c, pixels, accumulate);
     DK_CUDA(cudaGetLastError(), "copy channels launch");

@@ -108,6 +108,25 @@ def test_conv3x3_forward_wide(lib, cin, cout, act, ldi_extra, ldo_extra, co_off)
         assert torch.equal(untouched, expect)
 
 
+@pytest.mark.parametrize("cin,cout", [(32, 32), (96, 32)])
+def test_conv3x3_forward_tall(lib, cin, cout):
+    # Enough rows per persistent CTA that the halo-row ring (up to 16 slots)
+    # wraps several times: every slot is reused under its barrier phases.
+    g = torch.Generator().manual_seed(cin + 7 * cout)
+    n, h, w = 1, 720, 256
+    x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) / (3 * cin ** 0.5)).to(torch.bfloat16)
+    b = torch.randn(cout, generator=g) * 0.1
+    ref = torch.relu(torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), to_torch_weight(wt.float()), b,
+                                                padding=1)).permute(0, 2, 3, 1)
+    xd, wd, bd = x.cuda(), wt.cuda(), b.cuda()
+    out = torch.zeros(n, h, w, cout, dtype=torch.bfloat16, device="cuda")
+    library.check(lib.dk_unet_conv3x3(_ptr(xd), n, h, w, cin, cin, _ptr(wd), _ptr(bd), cout, _ptr(out), cout, 0, 1, 0,
+                                      None))
+    torch.cuda.synchronize()
+    assert rel_rms(out.cpu().float(), ref) <= 1e-2
+
+
 @pytest.mark.parametrize("cin,cout", [(16, 32), (64, 96), (160, 128), (96, 16)])
 def test_conv3x3_input_and_weight_gradients(lib, cin, cout):
     g = torch.Generator().manual_seed(cin + 3 * cout)
