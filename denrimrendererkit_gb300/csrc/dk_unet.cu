@@ -419,17 +419,18 @@ size_t tcSmemBytes(uint32_t cout) { return (size_t)kTcStages * (kTcRows * 128u +
 //              by the copy engine) and one 3-D box of the weights
 //              {64 ch, 1 tap, Cout}, both into 128-byte-swizzled K-major tiles;
 //   warp 1     MMA issuer: tcgen05.mma M = 128, N = Cout, K = 16 into one of
-//              two tensor-memory accumulators, stage release and
+//              the tensor-memory accumulators, stage release and
 //              accumulator hand-off through tcgen05.commit;
-//   warps 2-5  epilogue: tcgen05.ld of their TMEM lane quarter, bias, ReLU,
-//              optional accumulate, bf16 stores; the next tile's MMAs run
-//              into the other accumulator meanwhile.
+//   warps 2-9  epilogue: tcgen05.ld of their TMEM lane quarter (two warps
+//              per quarter, each half of the channels), bias, ReLU, optional
+//              accumulate, bf16 stores; the next tiles' MMAs run into the
+//              other accumulators (up to four) meanwhile.
 // Every mbarrier wait is bounded (about 2 s); a role that times out records
 // the error and stops, the others then time out in turn, and the CTA frees
 // its tensor memory before returning.
 constexpr uint32_t kTmaStagesMin = 4;   // (tap, chunk) stages in flight: at least 4,
 constexpr uint32_t kTmaStagesMax = 8;   // more where shared memory holds them
-constexpr uint32_t kTmaBarBytes = 192;  // full[8] empty[8] accFull[2] accEmpty[2], TMEM slot, flag
+constexpr uint32_t kTmaBarBytes = 256;  // full[8] empty[8] accFull[4] accEmpty[4], TMEM slot, flag
 
 struct TmaConvArgs {
     const float* bias;
@@ -471,26 +472,50 @@ __device__ __forceinline__ void umaCommit(uint32_t bar) {
                  : "memory");
 }
 
-// Shared memory one epilogue warp uses to transpose an output row: 32 pixels
-// of N bf16 channels at a pitch of 2N + 16 bytes (an odd number of 16-byte
-// units, so eight lanes' 16-byte writes fall on distinct banks), then the 32
-// pixels' global row pointers.
-__host__ __device__ constexpr uint32_t epiPitch(uint32_t n) { return 2u * n + 16u; }
-__host__ __device__ constexpr uint32_t epiWarpBytes(uint32_t n) { return 32u * epiPitch(n) + 32u * 8u; }
+// The epilogue: eight warps, two per tensor-memory lane quarter (32 output
+// pixels each).  When Cout is a multiple of 32 the two warps of a quarter
+// split every accumulator's channels in halves; otherwise the first takes all
+// of them and the second has nothing to do.  Up to four accumulators (as many
+// as tensor memory holds, at least two) let the MMA warp run ahead of them.
+constexpr uint32_t kEpiWarps = 8;
+__host__ __device__ constexpr bool epiSplit(uint32_t n) { return n % 32u == 0u; }
+__host__ __device__ constexpr uint32_t epiCols(uint32_t n) { return epiSplit(n) ? n / 2u : n; }
+// Shared memory one epilogue warp uses to transpose its part of an output
+// row: 32 pixels of its channels at a pitch of 2 x channels + 16 bytes (an odd
+// number of 16-byte units, so eight lanes' 16-byte writes fall on distinct
+// banks), then the 32 pixels' global row pointers.
+__host__ __device__ constexpr uint32_t epiPitch(uint32_t cols) { return 2u * cols + 16u; }
+__host__ __device__ constexpr uint32_t epiWarpBytes(uint32_t n) { return 32u * epiPitch(epiCols(n)) + 32u * 8u; }
+__host__ __device__ constexpr uint32_t accBuffers(uint32_t cols) { return 4u * cols <= 512u ? 4u : 2u; }
 
-// One accumulator (this warp's 32 TMEM lanes: 32 output pixels x N channels)
-// to global memory: bias, ReLU, bf16, optionally added to the destination.
-// `dst` is this lane's pixel (its channel 0), nullptr outside the image.
-// With `stage` the warp writes the row into shared memory and then stores
-// every pixel's channels as 16-byte pieces by consecutive lanes (one 32-byte
-// sector per two lanes instead of one per lane and 4-byte store), and hands
-// the accumulator back as soon as it is read; `stage` is null when the
+// This warp's channels [c0, c1) of one accumulator (its 32 TMEM lanes: 32
+// output pixels) to global memory: bias, ReLU, bf16, optionally added to the
+// destination.  `src` is the accumulator's TMEM address for the warp's lane
+// quarter, `dst` this lane's pixel (its channel 0), nullptr outside the image.
+// With `stage` the warp writes its part of the row into shared memory and then
+// stores every pixel's channels as 16-byte pieces by consecutive lanes, and
+// hands the accumulator back as soon as it is read; `stage` is null when the
 // destination is accumulated into (its bf16 sum is formed from the FP32
-// value, as on the direct path) or not 16-byte aligned.
-__device__ __forceinline__ void epilogueRow(uint32_t src, uint32_t N, const float* bias, int act, int accumulate,
-                                            __nv_bfloat16* dst, unsigned char* stage, uint32_t accEmptyBar) {
+// value, as on the direct path) or not 16-byte aligned.  With `zero` the
+// warp clears the columns it read before handing the accumulator back.
+__device__ __forceinline__ void zeroColumns(uint32_t src, uint32_t c0, uint32_t c1) {
+    const uint32_t z = 0u;
+    for (uint32_t c = c0; c < c1; c += 16u)
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+            "%1, %1};\n" ::"r"(src + c),
+            "r"(z)
+            : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void epilogueRow(uint32_t src, uint32_t c0, uint32_t c1, const float* bias, int act,
+                                            int accumulate, __nv_bfloat16* dst, unsigned char* stage,
+                                            uint32_t accEmptyBar, bool zero = false) {
     const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t c0 = 0; c0 < N; c0 += 16u) {
+    const uint32_t pitch = epiPitch(c1 - c0);
+    const bool biasVec = bias && (reinterpret_cast<uintptr_t>(bias) & 15u) == 0u;
+    for (uint32_t c = c0; c < c1; c += 16u) {
         uint32_t rr[16];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
@@ -498,13 +523,27 @@ __device__ __forceinline__ void epilogueRow(uint32_t src, uint32_t N, const floa
             : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
               "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]),
               "=r"(rr[15])
-            : "r"(src + c0));
+            : "r"(src + c));
+        float bv[16];
+        if (biasVec) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float4 b4 = __ldg(reinterpret_cast<const float4*>(bias + c) + k);
+                bv[4 * k] = b4.x;
+                bv[4 * k + 1] = b4.y;
+                bv[4 * k + 2] = b4.z;
+                bv[4 * k + 3] = b4.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) bv[k] = bias ? __ldg(bias + c + k) : 0.0f;
+        }
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
         float v2[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
             float x = __uint_as_float(rr[k]);
-            if (bias) x += __ldg(bias + c0 + k);
+            if (bias) x += bv[k];
             if (act == 1) x = fmaxf(x, 0.0f);
             v2[k] = x;
         }
@@ -515,13 +554,13 @@ __device__ __forceinline__ void epilogueRow(uint32_t src, uint32_t N, const floa
                 __nv_bfloat162 h2 = __floats2bfloat162_rn(v2[2 * k], v2[2 * k + 1]);
                 packed[k] = *reinterpret_cast<uint32_t*>(&h2);
             }
-            uint4* s = reinterpret_cast<uint4*>(stage + lane * epiPitch(N) + c0 * 2u);
-            s[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-            s[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+            uint4* sp = reinterpret_cast<uint4*>(stage + lane * pitch + (c - c0) * 2u);
+            sp[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+            sp[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
             continue;
         }
         if (!dst) continue;
-        __nv_bfloat162* d2 = reinterpret_cast<__nv_bfloat162*>(dst + c0);
+        __nv_bfloat162* d2 = reinterpret_cast<__nv_bfloat162*>(dst + c);
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             float x0v = v2[2 * k], x1v = v2[2 * k + 1];
@@ -533,22 +572,33 @@ __device__ __forceinline__ void epilogueRow(uint32_t src, uint32_t N, const floa
             d2[k] = __floats2bfloat162_rn(x0v, x1v);
         }
     }
+    if (zero) zeroColumns(src, c0, c1);  // the next row in this accumulator slot starts from zero
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     mbarArrive(accEmptyBar);
     if (!stage) return;
-    __nv_bfloat16** rows = reinterpret_cast<__nv_bfloat16**>(stage + 32u * epiPitch(N));
-    rows[lane] = dst;
+    __nv_bfloat16** rows = reinterpret_cast<__nv_bfloat16**>(stage + 32u * pitch);
+    rows[lane] = dst ? dst + c0 : nullptr;
     __syncwarp();
-    const uint32_t per = N / 8u;  // 16-byte pieces per pixel
-    for (uint32_t j = lane; j < 32u * per; j += 32u) {
-        const uint32_t pix = j / per, part = j - pix * per;
+    // 16-byte pieces: `per` per pixel; lane j takes pieces j, j + 32, ...
+    const uint32_t per = (c1 - c0) / 8u;
+    const bool pow2 = (per & (per - 1u)) == 0u;
+    const uint32_t sh = 31u - __clz(per);
+    uint32_t pix = pow2 ? lane >> sh : lane / per;
+    uint32_t part = lane - pix * per;
+    const uint32_t dq = pow2 ? 32u >> sh : 32u / per, dr = 32u - dq * per;
+    for (; pix < 32u; pix += dq) {
         __nv_bfloat16* d = rows[pix];
-        if (d) *reinterpret_cast<uint4*>(d + part * 8u) = *reinterpret_cast<const uint4*>(stage + pix * epiPitch(N) + part * 16u);
+        if (d) *reinterpret_cast<uint4*>(d + part * 8u) = *reinterpret_cast<const uint4*>(stage + pix * pitch + part * 16u);
+        part += dr;
+        if (part >= per) {
+            part -= per;
+            ++pix;
+        }
     }
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(320, 1)
     k_conv3x3_tma(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW, TmaConvArgs a) {
     extern __shared__ unsigned char dsm[];
     const uint32_t raw = smemAddr(dsm);
@@ -559,16 +609,17 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t S = a.stages;
     unsigned char* sB = sm + S * aBytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sB + S * bBytes);
-    // bars: full[S], empty[S], accFull[2], accEmpty[2]
+    // bars: full[S], empty[S], accFull[4], accEmpty[4]
     const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kTmaStagesMax;
-    const uint32_t accFullBar = emptyBar + 8u * kTmaStagesMax, accEmptyBar = accFullBar + 16u;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kTmaStagesMax + 4);
+    const uint32_t accFullBar = emptyBar + 8u * kTmaStagesMax, accEmptyBar = accFullBar + 32u;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kTmaStagesMax + 8);
+    const uint32_t nbuf = accBuffers(a.cols), bufShift = nbuf == 4u ? 2u : 1u;
     int* abortFlag = reinterpret_cast<int*>(tslot + 1);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(tslot)),
-                     "r"(2u * a.cols));
+                     "r"(nbuf * a.cols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
     if (tid == 0) {
@@ -576,9 +627,9 @@ __global__ void __launch_bounds__(192, 1)
             mbarInit(fullBar + 8u * s, 1);
             mbarInit(emptyBar + 8u * s, 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (uint32_t b = 0; b < nbuf; ++b) {
             mbarInit(accFullBar + 8u * b, 1);
-            mbarInit(accEmptyBar + 8u * b, 128);
+            mbarInit(accEmptyBar + 8u * b, epiSplit(N) ? 256u : 128u);
         }
         *abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -625,7 +676,7 @@ __global__ void __launch_bounds__(192, 1)
             RingPos pos{0u, 0u};
             uint32_t t = 0;
             for (uint32_t tile = blockIdx.x; tile < a.numTiles && !*abortV; tile += gridDim.x, ++t) {
-                uint32_t b = t & 1u, v = t >> 1;
+                uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
                 if (v > 0 && !mbarWait(accEmptyBar + 8u * b, (v - 1u) & 1u)) {
                     *abortV = 1;
                     break;
@@ -660,14 +711,15 @@ __global__ void __launch_bounds__(192, 1)
             }
         }
     } else {
-        // Epilogue warps 2..5: TMEM lane quarter (warp % 4).
-        const uint32_t q = warp & 3u;
+        // Epilogue warps 2..9: TMEM lane quarter warp % 4, channel half (warp - 2) / 4.
+        const uint32_t q = warp & 3u, half = (warp - 2u) >> 2;
         const uint32_t r = q * 32u + lane;
+        const uint32_t cw = epiCols(N), c0 = half * cw, c1 = epiSplit(N) ? c0 + cw : (half ? 0u : N);
         unsigned char* stage =
-            a.staged ? reinterpret_cast<unsigned char*>(bars) + kTmaBarBytes + q * epiWarpBytes(N) : nullptr;
+            a.staged ? reinterpret_cast<unsigned char*>(bars) + kTmaBarBytes + (warp - 2u) * epiWarpBytes(N) : nullptr;
         uint32_t t = 0;
-        for (uint32_t tile = blockIdx.x; tile < a.numTiles; tile += gridDim.x, ++t) {
-            uint32_t b = t & 1u, v = t >> 1;
+        for (uint32_t tile = blockIdx.x; c1 > c0 && tile < a.numTiles; tile += gridDim.x, ++t) {
+            uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
             if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
                 *abortV = 1;
                 break;
@@ -678,26 +730,29 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t px = tx * a.tw + r % a.tw, py = ty * a.th + r / a.tw;
             bool valid = px < a.w && py < a.h;
             __nv_bfloat16* orow = valid ? a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff : nullptr;
-            epilogueRow(taddr + ((q * 32u) << 16) + b * a.cols, N, a.bias, a.act, a.accumulate, orow, stage,
+            epilogueRow(taddr + ((q * 32u) << 16) + b * a.cols, c0, c1, a.bias, a.act, a.accumulate, orow, stage,
                         accEmptyBar + 8u * b);
         }
     }
     __syncthreads();
     if (*abortV && tid == 0) atomicExch(&g_unetError, 2);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(2u * a.cols));
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(nbuf * a.cols));
 }
 
 size_t tmaSmemBytes(uint32_t cout, bool staged, uint32_t stages) {
-    return (size_t)stages * (128u * 128u + cout * 128u) + 1024u + kTmaBarBytes + (staged ? 4u * epiWarpBytes(cout) : 0u);
+    return (size_t)stages * (128u * 128u + cout * 128u) + 1024u + kTmaBarBytes +
+           (staged ? kEpiWarps * epiWarpBytes(cout) : 0u);
 }
 
 // -------------------------------------- tcgen05 + TMA, halo-row ring ----
 // The convolution for wide, shallow layers (the full- and half-resolution
 // levels of the U-Net, where the per-tap kernel above re-reads every input
 // pixel nine times from L2 and waits on it).  An output tile is 128
-// consecutive pixels of one image row; a persistent CTA walks a column of
-// such tiles down `rowBlock` rows and keeps the input rows it needs in a ring
+// consecutive pixels of one image row; a persistent CTA walks its share of
+// the output rows (an equal, contiguous range of the rows numbered image by
+// image, tile column by tile column, top to bottom), down one tile column at
+// a time, and keeps the input rows it needs in a ring
 // of halo rows: one TMA box {64 channels, 130 pixels} per 64-channel chunk
 // and input row, loaded once (zero filled outside the image).  For tap
 // (dy, dx) the MMA's A operand is the 128 rows of halo row y - 1 + dy that
@@ -707,13 +762,14 @@ size_t tmaSmemBytes(uint32_t cout, bool staged, uint32_t stages) {
 // {64 channels, Cout}) stay resident in shared memory for the whole launch.
 //   warp 0     TMA producer: the weights once, then the halo rows in order;
 //   warp 1     MMA issuer: per output row 9 taps x chunks x K-steps of
-//              tcgen05.mma M = 128, N = Cout, K = 16 into one of two TMEM
+//              tcgen05.mma M = 128, N = Cout, K = 16 into one of the TMEM
 //              accumulators; releases a halo row once its last reader is done;
-//   warps 2-5  epilogue as in k_conv3x3_tma.
+//   warps 2-9  epilogue as in k_conv3x3_tma.
 // Waits are bounded as there.
 constexpr uint32_t kHaloRingMin = 4;        // halo-row slots: three rows in use and one loading at least,
 constexpr uint32_t kHaloRingMax = 16;       // and as many more loading as shared memory holds
-constexpr uint32_t kHaloBarBytes = 384;     // full[16] empty[16] weights accFull[2] accEmpty[2], TMEM slot, flag
+constexpr uint32_t kHaloBarBytes = 1024;    // full[16] empty[16] weights accFull[32] accEmpty[32], TMEM slot, flag
+constexpr uint32_t kHaloAccMax = 32;
 constexpr uint32_t kHaloPix = 130;          // 128 output pixels and one on each side
 constexpr uint32_t kHaloSlotBytes = 17408;  // 130 rows of 128 B, padded to 17 x 1024 B
 
@@ -721,13 +777,35 @@ struct HaloConvArgs {
     const float* bias;
     __nv_bfloat16* out;
     uint32_t n, h, w, cin, cout, ldo, coOff;
-    uint32_t tilesX, rowBlock, rowBlocks, numItems, chunks, cols;
+    uint32_t tilesX, totalRows, chunks, cols;  // totalRows = n x tilesX x h output rows of 128 pixels
     uint32_t ring;  // halo-row slots, kHaloRingMin..kHaloRingMax
+    uint32_t slots, logSlots;  // stacked variant: accumulator slots of Cout columns (a power of two)
     int act, accumulate;
     int staged;  // epilogue rows through shared memory (see epilogueRow)
 };
 
-__global__ void __launch_bounds__(192, 1)
+// A run of output rows y0..y1-1 of tile column tx of image img.
+struct RowSegment {
+    uint32_t img, tx, y0, y1;
+};
+// The next segment of this CTA's rows [cur, end): the rest of the current
+// tile column at most; false when the range is done.
+__device__ __forceinline__ bool nextSegment(const HaloConvArgs& a, uint32_t& cur, uint32_t end, RowSegment& sg) {
+    if (cur >= end) return false;
+    const uint32_t col = cur / a.h;
+    sg.y0 = cur - col * a.h;
+    sg.y1 = min(a.h, sg.y0 + (end - cur));
+    sg.tx = col % a.tilesX;
+    sg.img = col / a.tilesX;
+    cur += sg.y1 - sg.y0;
+    return true;
+}
+__device__ __forceinline__ uint32_t rangeBegin(const HaloConvArgs& a, uint32_t cta) {
+    return (uint32_t)((uint64_t)cta * a.totalRows / gridDim.x);
+}
+
+template <bool kStack>
+__global__ void __launch_bounds__(320, 1)
     k_conv3x3_halo(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW,
                    HaloConvArgs a) {
     extern __shared__ unsigned char dsm[];
@@ -740,16 +818,22 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t R = a.ring;
     unsigned char* sW = sm + R * slotBytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sW + wBytes);
-    // bars: full[R], empty[R], weights, accFull[2], accEmpty[2]
+    // bars: full[R], empty[R], weights, accFull[Q], accEmpty[Q]
     const uint32_t fullBar = smemAddr(bars), emptyBar = fullBar + 8u * kHaloRingMax;
-    const uint32_t wBar = emptyBar + 8u * kHaloRingMax, accFullBar = wBar + 8u, accEmptyBar = accFullBar + 16u;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kHaloRingMax + 5);
+    const uint32_t wBar = emptyBar + 8u * kHaloRingMax, accFullBar = wBar + 8u;
+    const uint32_t accEmptyBar = accFullBar + 8u * kHaloAccMax;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * kHaloRingMax + 1 + 2 * kHaloAccMax);
+    // Accumulators: Q slots of Cout columns for the stacked variant (a rolling
+    // window over the output rows), else nbuf buffers of `cols` columns.
+    const uint32_t nbuf = kStack ? a.slots : accBuffers(a.cols);
+    const uint32_t bufShift = kStack ? a.logSlots : (nbuf == 4u ? 2u : 1u);
+    const uint32_t tmemCols = kStack ? 512u : nbuf * a.cols;
     int* abortFlag = reinterpret_cast<int*>(tslot + 1);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(tslot)),
-                     "r"(2u * a.cols));
+                     "r"(tmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
     if (tid == 0) {
@@ -758,9 +842,9 @@ __global__ void __launch_bounds__(192, 1)
             mbarInit(emptyBar + 8u * s, 1);
         }
         mbarInit(wBar, 1);
-        for (int b = 0; b < 2; ++b) {
+        for (uint32_t b = 0; b < nbuf; ++b) {
             mbarInit(accFullBar + 8u * b, 1);
-            mbarInit(accEmptyBar + 8u * b, 128);
+            mbarInit(accEmptyBar + 8u * b, epiSplit(N) ? 256u : 128u);
         }
         *abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -775,16 +859,23 @@ __global__ void __launch_bounds__(192, 1)
     if (warp == 0) {
         if (lane == 0) {
             mbarExpectTx(wBar, wBytes);
+            // Stacked: per (dx, chunk) one tile of 3 x Cout weight rows, the taps
+            // dy = 2, 1, 0 in that order (an MMA with N = 3 Cout then yields the
+            // contributions of one halo row to output rows y - 2, y - 1, y).
             for (uint32_t tap = 0; tap < 9u; ++tap)
-                for (uint32_t c = 0; c < C; ++c)
-                    tmaLoad3(smemAddr(sW + (tap * C + c) * wBoxBytes), &mapW, (int)(c * 64u), (int)tap, 0, wBar);
+                for (uint32_t c = 0; c < C; ++c) {
+                    const uint32_t dy = tap / 3u, dx = tap - 3u * dy;
+                    const uint32_t box = kStack ? (dx * C + c) * 3u + (2u - dy) : tap * C + c;
+                    tmaLoad3(smemAddr(sW + box * wBoxBytes), &mapW, (int)(c * 64u), (int)tap, 0, wBar);
+                }
             uint32_t g = 0;
             RingPos pos{0u, 0u};
-            for (uint32_t item = blockIdx.x; item < a.numItems && !*abortV; item += gridDim.x) {
-                const uint32_t tx = item % a.tilesX, rest = item / a.tilesX;
-                const uint32_t rb = rest % a.rowBlocks, img = rest / a.rowBlocks;
-                const int x0 = (int)(tx * 128u), y0 = (int)(rb * a.rowBlock);
-                const int y1 = min((int)a.h, y0 + (int)a.rowBlock);
+            uint32_t cur = rangeBegin(a, blockIdx.x);
+            const uint32_t end = rangeBegin(a, blockIdx.x + 1u);
+            RowSegment sg;
+            while (!*abortV && nextSegment(a, cur, end, sg)) {
+                const int x0 = (int)(sg.tx * 128u), y0 = (int)sg.y0, y1 = (int)sg.y1;
+                const uint32_t img = sg.img;
                 bool ok = true;
                 for (int hy = y0 - 1; hy <= y1; ++hy, ++g, pos.advance(R)) {
                     if (g >= R && !mbarWait(emptyBar + 8u * pos.slot, pos.phase ^ 1u)) {
@@ -803,6 +894,68 @@ __global__ void __launch_bounds__(192, 1)
                 }
             }
         }
+    } else if (warp == 1 && kStack) {
+        if (lane == 0) {
+            // Per halo row k of a segment of `rows` output rows: the row's
+            // contributions to output rows k - 2, k - 1, k (taps dy = 2, 1, 0).
+            // Between the segment's edges, and when the three rows' slots are
+            // adjacent, that is one MMA per (dx, chunk, K step) with N = 3 Cout
+            // into the three slots; otherwise one MMA with N = Cout per valid
+            // row.  Slots start zeroed (the epilogue clears a slot when it has
+            // read it), so every MMA accumulates.
+            const uint32_t idesc1 = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
+            const uint32_t idesc3 = (1u << 4) | (1u << 7) | (1u << 10) | (((3u * N) >> 3) << 17) | ((128u >> 4) << 24);
+            const uint32_t hi = descHi(), aLo0 = descLo(smemAddr(sRing)), bLo0 = descLo(smemAddr(sW));
+            const uint32_t lastSteps = (a.cin - (C - 1u) * 64u + 15u) / 16u;  // K steps of the last chunk
+            const uint32_t tileU = (3u * wBoxBytes) >> 4, dyU = wBoxBytes >> 4;  // in 16-byte units
+            const uint32_t Q = nbuf;
+            bool ok = mbarWait(wBar, 0u);
+            uint32_t t0 = 0;      // output rows of the earlier segments
+            RingPos hp{0u, 0u};   // the current halo row's ring slot
+            uint32_t cur = rangeBegin(a, blockIdx.x);
+            const uint32_t end = rangeBegin(a, blockIdx.x + 1u);
+            RowSegment sg;
+            while (ok && !*abortV && nextSegment(a, cur, end, sg)) {
+                const uint32_t rows = sg.y1 - sg.y0;
+                for (uint32_t k = 0; k < rows + 2u; ++k, hp.advance(R)) {
+                    if (k < rows) {  // output row k enters: its slot must have been read and cleared
+                        const uint32_t t = t0 + k;
+                        if (!mbarWait(accEmptyBar + 8u * (t & (Q - 1u)), (t >> bufShift) & 1u)) ok = false;
+                    }
+                    if (ok && !mbarWait(fullBar + 8u * hp.slot, hp.phase)) ok = false;
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t aRow = aLo0 + hp.slot * (slotBytes >> 4);
+                    const uint32_t jLo = k >= 2u ? k - 2u : 0u, jHi = min(k, rows - 1u);
+                    const uint32_t sLo = (t0 + jLo) & (Q - 1u);
+                    const bool stacked = k >= 2u && k < rows && sLo + 2u < Q;
+                    for (uint32_t dx = 0; dx < 3u; ++dx) {
+                        for (uint32_t c = 0; c < C; ++c) {
+                            const uint32_t steps = c + 1u < C ? 4u : lastSteps;
+                            const uint32_t aC = aRow + dx * 8u + c * (kHaloSlotBytes >> 4);  // pixel dx: 128 B on
+                            const uint32_t bT = bLo0 + (dx * C + c) * tileU;
+                            if (stacked) {
+                                const uint32_t d = taddr + sLo * N;
+                                for (uint32_t ks = 0; ks < steps; ++ks)
+                                    mmaF16(d, aC + 2u * ks, bT + 2u * ks, hi, idesc3, 1u);
+                            } else {
+                                for (uint32_t j = jLo; j <= jHi; ++j) {
+                                    const uint32_t dy = k - j;
+                                    const uint32_t d = taddr + ((t0 + j) & (Q - 1u)) * N;
+                                    const uint32_t bD = bT + (2u - dy) * dyU;
+                                    for (uint32_t ks = 0; ks < steps; ++ks)
+                                        mmaF16(d, aC + 2u * ks, bD + 2u * ks, hi, idesc1, 1u);
+                                }
+                            }
+                        }
+                    }
+                    umaCommit(emptyBar + 8u * hp.slot);  // halo row k has no reader left
+                    if (k >= 2u) umaCommit(accFullBar + 8u * ((t0 + k - 2u) & (Q - 1u)));  // row k - 2 is complete
+                }
+                t0 += rows;
+            }
+            if (!ok) *abortV = 1;
+        }
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
@@ -811,11 +964,11 @@ __global__ void __launch_bounds__(192, 1)
             bool ok = mbarWait(wBar, 0u);
             uint32_t t = 0;
             RingPos top{0u, 0u};  // the item's first halo row
-            for (uint32_t item = blockIdx.x; ok && item < a.numItems && !*abortV; item += gridDim.x) {
-                const uint32_t rest = item / a.tilesX;
-                const uint32_t rb = rest % a.rowBlocks;
-                const uint32_t y0 = rb * a.rowBlock, y1 = min(a.h, y0 + a.rowBlock);
-                const uint32_t rows = y1 - y0;
+            uint32_t cur = rangeBegin(a, blockIdx.x);
+            const uint32_t end = rangeBegin(a, blockIdx.x + 1u);
+            RowSegment sg;
+            while (ok && !*abortV && nextSegment(a, cur, end, sg)) {
+                const uint32_t rows = sg.y1 - sg.y0;
                 // halo rows w0, w1, w2 feed the current output row
                 RingPos w0 = top, w1 = top, w2;
                 w1.advance(R);
@@ -825,7 +978,7 @@ __global__ void __launch_bounds__(192, 1)
                     ok = false;
                 for (uint32_t k = 0; ok && k < rows; ++k, ++t) {
                     if (!mbarWait(fullBar + 8u * w2.slot, w2.phase)) ok = false;
-                    const uint32_t b = t & 1u, v = t >> 1;
+                    const uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
                     if (ok && v > 0 && !mbarWait(accEmptyBar + 8u * b, (v - 1u) & 1u)) ok = false;
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -866,20 +1019,30 @@ __global__ void __launch_bounds__(192, 1)
             if (!ok) *abortV = 1;
         }
     } else {
-        // Epilogue warps 2..5: TMEM lane quarter (warp % 4), one output pixel per thread.
-        const uint32_t q = warp & 3u;
+        // Epilogue warps 2..9: TMEM lane quarter warp % 4 (one output pixel per
+        // thread), channel half (warp - 2) / 4.
+        const uint32_t q = warp & 3u, half = (warp - 2u) >> 2;
         const uint32_t r = q * 32u + lane;
+        const uint32_t cw = epiCols(N), c0 = half * cw, c1 = epiSplit(N) ? c0 + cw : (half ? 0u : N);
         unsigned char* stage =
-            a.staged ? reinterpret_cast<unsigned char*>(bars) + kHaloBarBytes + q * epiWarpBytes(N) : nullptr;
+            a.staged ? reinterpret_cast<unsigned char*>(bars) + kHaloBarBytes + (warp - 2u) * epiWarpBytes(N) : nullptr;
         uint32_t t = 0;
-        bool ok = true;
-        for (uint32_t item = blockIdx.x; ok && item < a.numItems; item += gridDim.x) {
-            const uint32_t tx = item % a.tilesX, rest = item / a.tilesX;
-            const uint32_t rb = rest % a.rowBlocks, img = rest / a.rowBlocks;
-            const uint32_t y0 = rb * a.rowBlock, y1 = min(a.h, y0 + a.rowBlock);
-            const uint32_t px = tx * 128u + r;
-            for (uint32_t py = y0; py < y1; ++py, ++t) {
-                const uint32_t b = t & 1u, v = t >> 1;
+        bool ok = c1 > c0;
+        const uint32_t quarter = taddr + ((q * 32u) << 16);
+        const uint32_t slotCols = kStack ? N : a.cols;
+        if (kStack && ok) {
+            // Every slot starts zeroed; its first release lets the MMA warp in.
+            for (uint32_t b = 0; b < nbuf; ++b) zeroColumns(quarter + b * slotCols, c0, c1);
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            for (uint32_t b = 0; b < nbuf; ++b) mbarArrive(accEmptyBar + 8u * b);
+        }
+        uint32_t cur = rangeBegin(a, blockIdx.x);
+        const uint32_t end = rangeBegin(a, blockIdx.x + 1u);
+        RowSegment sg;
+        while (ok && nextSegment(a, cur, end, sg)) {
+            const uint32_t img = sg.img, px = sg.tx * 128u + r;
+            for (uint32_t py = sg.y0; py < sg.y1; ++py, ++t) {
+                const uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
                 if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
                     *abortV = 1;
                     ok = false;
@@ -888,20 +1051,20 @@ __global__ void __launch_bounds__(192, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 __nv_bfloat16* orow =
                     px < a.w ? a.out + ((size_t)(img * a.h + py) * a.w + px) * a.ldo + a.coOff : nullptr;
-                epilogueRow(taddr + ((q * 32u) << 16) + b * a.cols, N, a.bias, a.act, a.accumulate, orow, stage,
-                            accEmptyBar + 8u * b);
+                epilogueRow(quarter + b * slotCols, c0, c1, a.bias, a.act, a.accumulate, orow, stage,
+                            accEmptyBar + 8u * b, kStack);
             }
         }
     }
     __syncthreads();
     if (*abortV && tid == 0) atomicExch(&g_unetError, 3);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(2u * a.cols));
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(tmemCols));
 }
 
 size_t haloSmemBytes(uint32_t cout, uint32_t chunks, bool staged, uint32_t ring) {
     return 1024u + (size_t)ring * chunks * kHaloSlotBytes + 9u * (size_t)chunks * cout * 128u + kHaloBarBytes +
-           (staged ? 4u * epiWarpBytes(cout) : 0u);
+           (staged ? kEpiWarps * epiWarpBytes(cout) : 0u);
 }
 
 // -------------------------------------------------------------- wgrad ----
@@ -1496,17 +1659,25 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     a.accumulate = c.accumulate;
     a.staged = staged ? 1 : 0;
     a.ring = ring;
+    // Vertical taps stacked into one MMA (N = 3 Cout <= 256) with a rolling
+    // window of accumulator slots; DK_CONV_STACK=0 keeps one MMA per tap.
+    const char* stackEnv = getenv("DK_CONV_STACK");
+    const bool stack = c.cout * 3u <= 256u && !(stackEnv && stackEnv[0] == '0');
+    a.slots = 0u;
+    a.logSlots = 0u;
+    if (stack) {
+        a.slots = 1u;
+        while (a.slots * 2u * c.cout <= 512u && a.slots * 2u <= kHaloAccMax) a.slots *= 2u;
+        while ((1u << a.logSlots) < a.slots) ++a.logSlots;
+    }
     a.chunks = chunks;
     a.cols = 32u;
     while (a.cols < c.cout) a.cols <<= 1;
     a.tilesX = (c.w_ + 127u) / 128u;
     const uint32_t sms = (uint32_t)deviceProp().multiProcessorCount;
-    // About four items per CTA: enough to balance, few halo rows re-read.
     const uint64_t rowsTotal = (uint64_t)c.n * a.tilesX * c.h;
-    uint64_t rb = (rowsTotal + 4u * sms - 1u) / (4u * sms);
-    a.rowBlock = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(rb, 2u), c.h);
-    a.rowBlocks = (c.h + a.rowBlock - 1u) / a.rowBlock;
-    a.numItems = c.n * a.tilesX * a.rowBlocks;
+    if (rowsTotal >= (1ull << 32)) return kHaloUnfit;
+    a.totalRows = (uint32_t)rowsTotal;
     alignas(64) CUtensorMap mapIn, mapW;
     cuuint64_t dimIn[4] = {c.cin, c.w_, c.h, c.n};
     cuuint64_t strideIn[3] = {(cuuint64_t)c.ldi * 2u, (cuuint64_t)c.w_ * c.ldi * 2u, (cuuint64_t)c.h * c.w_ * c.ldi * 2u};
@@ -1523,14 +1694,18 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "weight tensor map rejected");
-    static size_t configured = 0;
-    if (smem > configured) {
-        DK_CUDA(cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    static size_t configured[2] = {0, 0};
+    if (smem > configured[stack]) {
+        DK_CUDA(cudaFuncSetAttribute(stack ? k_conv3x3_halo<true> : k_conv3x3_halo<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                 "conv3x3 (halo) shared memory");
-        configured = smem;
+        configured[stack] = smem;
     }
-    uint32_t grid = std::min(sms, a.numItems);
-    k_conv3x3_halo<<<grid, 192, smem, st>>>(mapIn, mapW, a);
+    uint32_t grid = std::min(sms, a.totalRows);
+    if (stack)
+        k_conv3x3_halo<true><<<grid, 320, smem, st>>>(mapIn, mapW, a);
+    else
+        k_conv3x3_halo<false><<<grid, 320, smem, st>>>(mapIn, mapW, a);
     DK_CUDA(cudaGetLastError(), "conv3x3 (halo rows, TMA + tcgen05) launch");
     return DK_OK;
 }
@@ -1592,7 +1767,7 @@ int launchConvTma(const ConvArgs& c, cudaStream_t st) {
     }
     uint32_t grid = (uint32_t)deviceProp().multiProcessorCount;
     if (grid > a.numTiles) grid = a.numTiles;
-    k_conv3x3_tma<<<grid, 192, smem, st>>>(mapIn, mapW, a);
+    k_conv3x3_tma<<<grid, 320, smem, st>>>(mapIn, mapW, a);
     DK_CUDA(cudaGetLastError(), "conv3x3 (TMA + tcgen05) launch");
     return DK_OK;
 }

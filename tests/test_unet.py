@@ -108,12 +108,14 @@ def test_conv3x3_forward_wide(lib, cin, cout, act, ldi_extra, ldo_extra, co_off)
         assert torch.equal(untouched, expect)
 
 
-@pytest.mark.parametrize("cin,cout", [(32, 32), (96, 32)])
+@pytest.mark.parametrize("cin,cout", [(32, 32), (96, 32), (64, 64), (32, 16)])
 def test_conv3x3_forward_tall(lib, cin, cout):
-    # Enough rows per persistent CTA that the halo-row ring (up to 16 slots)
-    # wraps several times: every slot is reused under its barrier phases.
+    # About 40 output rows per persistent CTA, crossing tile columns and
+    # images: the halo-row ring (up to 16 slots) and the stacked-tap
+    # accumulator window (8 to 32 slots) wrap, and the MMAs at a segment's
+    # first and last rows and at the window's wrap take the per-tap form.
     g = torch.Generator().manual_seed(cin + 7 * cout)
-    n, h, w = 1, 720, 256
+    n, h, w = 3, 1000, 136
     x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
     wt = (torch.randn(cout, 9, cin, generator=g) / (3 * cin ** 0.5)).to(torch.bfloat16)
     b = torch.randn(cout, generator=g) * 0.1
