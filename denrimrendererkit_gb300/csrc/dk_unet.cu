@@ -804,7 +804,12 @@ __device__ __forceinline__ uint32_t rangeBegin(const HaloConvArgs& a, uint32_t c
     return (uint32_t)((uint64_t)cta * a.totalRows / gridDim.x);
 }
 
-template <bool kStack>
+// kC: 64-channel chunks of the input (Cin / 64 rounded up), kLast: K steps of
+// 16 channels in the last chunk.  Both are compile-time so that each output
+// row's MMAs are straight-line code: a branch between two tcgen05.mma costs
+// the issuing thread a few hundred cycles (measured), about the time of a
+// 128 x 32 x 16 MMA twenty times over.
+template <bool kStack, uint32_t kC, uint32_t kLast>
 __global__ void __launch_bounds__(320, 1)
     k_conv3x3_halo(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW,
                    HaloConvArgs a) {
@@ -906,7 +911,6 @@ __global__ void __launch_bounds__(320, 1)
             const uint32_t idesc1 = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
             const uint32_t idesc3 = (1u << 4) | (1u << 7) | (1u << 10) | (((3u * N) >> 3) << 17) | ((128u >> 4) << 24);
             const uint32_t hi = descHi(), aLo0 = descLo(smemAddr(sRing)), bLo0 = descLo(smemAddr(sW));
-            const uint32_t lastSteps = (a.cin - (C - 1u) * 64u + 15u) / 16u;  // K steps of the last chunk
             const uint32_t tileU = (3u * wBoxBytes) >> 4, dyU = wBoxBytes >> 4;  // in 16-byte units
             const uint32_t Q = nbuf;
             bool ok = mbarWait(wBar, 0u);
@@ -929,24 +933,29 @@ __global__ void __launch_bounds__(320, 1)
                     const uint32_t jLo = k >= 2u ? k - 2u : 0u, jHi = min(k, rows - 1u);
                     const uint32_t sLo = (t0 + jLo) & (Q - 1u);
                     const bool stacked = k >= 2u && k < rows && sLo + 2u < Q;
-                    for (uint32_t dx = 0; dx < 3u; ++dx) {
-                        for (uint32_t c = 0; c < C; ++c) {
-                            const uint32_t steps = c + 1u < C ? 4u : lastSteps;
-                            const uint32_t aC = aRow + dx * 8u + c * (kHaloSlotBytes >> 4);  // pixel dx: 128 B on
-                            const uint32_t bT = bLo0 + (dx * C + c) * tileU;
-                            if (stacked) {
-                                const uint32_t d = taddr + sLo * N;
-                                for (uint32_t ks = 0; ks < steps; ++ks)
-                                    mmaF16(d, aC + 2u * ks, bT + 2u * ks, hi, idesc3, 1u);
-                            } else {
-                                for (uint32_t j = jLo; j <= jHi; ++j) {
-                                    const uint32_t dy = k - j;
-                                    const uint32_t d = taddr + ((t0 + j) & (Q - 1u)) * N;
-                                    const uint32_t bD = bT + (2u - dy) * dyU;
-                                    for (uint32_t ks = 0; ks < steps; ++ks)
-                                        mmaF16(d, aC + 2u * ks, bD + 2u * ks, hi, idesc1, 1u);
-                                }
-                            }
+                    if (stacked) {
+                        const uint32_t d = taddr + sLo * N;
+#pragma unroll
+                        for (uint32_t dx = 0; dx < 3u; ++dx)
+#pragma unroll
+                            for (uint32_t c = 0; c < kC; ++c)
+#pragma unroll
+                                for (uint32_t ks = 0; ks < (c + 1u < kC ? 4u : kLast); ++ks)
+                                    mmaF16(d, aRow + dx * 8u + c * (kHaloSlotBytes >> 4) + 2u * ks,  // pixel dx: 128 B on
+                                           bLo0 + (dx * kC + c) * tileU + 2u * ks, hi, idesc3, 1u);
+                    } else {
+                        for (uint32_t j = jLo; j <= jHi; ++j) {
+                            const uint32_t dy = k - j;
+                            const uint32_t d = taddr + ((t0 + j) & (Q - 1u)) * N;
+#pragma unroll
+                            for (uint32_t dx = 0; dx < 3u; ++dx)
+#pragma unroll
+                                for (uint32_t c = 0; c < kC; ++c)
+#pragma unroll
+                                    for (uint32_t ks = 0; ks < (c + 1u < kC ? 4u : kLast); ++ks)
+                                        mmaF16(d, aRow + dx * 8u + c * (kHaloSlotBytes >> 4) + 2u * ks,
+                                               bLo0 + (dx * kC + c) * tileU + (2u - dy) * dyU + 2u * ks, hi, idesc1,
+                                               1u);
                         }
                     }
                     umaCommit(emptyBar + 8u * hp.slot);  // halo row k has no reader left
@@ -960,7 +969,6 @@ __global__ void __launch_bounds__(320, 1)
         if (lane == 0) {
             const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((128u >> 4) << 24);
             const uint32_t hi = descHi(), aLo0 = descLo(smemAddr(sRing)), bLo0 = descLo(smemAddr(sW));
-            const uint32_t lastSteps = (a.cin - (C - 1u) * 64u + 15u) / 16u;  // K steps of the last chunk
             bool ok = mbarWait(wBar, 0u);
             uint32_t t = 0;
             RingPos top{0u, 0u};  // the item's first halo row
@@ -989,21 +997,17 @@ __global__ void __launch_bounds__(320, 1)
                     // wrote it (measured: a base offset of (start >> 7) & 7 gives wrong sums).
                     const uint32_t rowLo[3] = {aLo0 + w0.slot * (slotBytes >> 4), aLo0 + w1.slot * (slotBytes >> 4),
                                                aLo0 + w2.slot * (slotBytes >> 4)};
-                    uint32_t acc = 0u;
 #pragma unroll
                     for (uint32_t tap = 0; tap < 9u; ++tap) {
                         const uint32_t dy = tap / 3u, dx = tap - dy * 3u;
                         const uint32_t aT = rowLo[dy] + dx * 8u;  // pixel dx: 128 bytes further
-                        const uint32_t bT = bLo0 + tap * C * (wBoxBytes >> 4);
-                        for (uint32_t c = 0; c < C; ++c) {
-                            const uint32_t steps = c + 1u < C ? 4u : lastSteps;
-                            const uint32_t aC = aT + c * (kHaloSlotBytes >> 4), bC = bT + c * (wBoxBytes >> 4);
-                            mmaF16(dAddr, aC, bC, hi, idesc, acc);
-                            acc = 1u;
-                            if (steps > 1u) mmaF16(dAddr, aC + 2u, bC + 2u, hi, idesc, 1u);
-                            if (steps > 2u) mmaF16(dAddr, aC + 4u, bC + 4u, hi, idesc, 1u);
-                            if (steps > 3u) mmaF16(dAddr, aC + 6u, bC + 6u, hi, idesc, 1u);
-                        }
+                        const uint32_t bT = bLo0 + tap * kC * (wBoxBytes >> 4);
+#pragma unroll
+                        for (uint32_t c = 0; c < kC; ++c)
+#pragma unroll
+                            for (uint32_t ks = 0; ks < (c + 1u < kC ? 4u : kLast); ++ks)
+                                mmaF16(dAddr, aT + c * (kHaloSlotBytes >> 4) + 2u * ks, bT + c * (wBoxBytes >> 4) + 2u * ks,
+                                       hi, idesc, (tap | c | ks) ? 1u : 0u);
                     }
                     umaCommit(accFullBar + 8u * b);          // output row complete
                     umaCommit(emptyBar + 8u * w0.slot);      // its top halo row has no reader left
@@ -1636,7 +1640,8 @@ constexpr int kHaloUnfit = -1;
 int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     const uint32_t chunks = (c.cin + 63u) / 64u;
     const size_t optin = (size_t)deviceProp().sharedMemPerBlockOptin;
-    if (c.w_ < 128u || c.cout > 256u || haloSmemBytes(c.cout, chunks, false, kHaloRingMin) > optin) return kHaloUnfit;
+    if (c.w_ < 128u || c.cout > 256u || chunks > 2u || haloSmemBytes(c.cout, chunks, false, kHaloRingMin) > optin)
+        return kHaloUnfit;
     const bool staged = stagedStores(c) && haloSmemBytes(c.cout, chunks, true, kHaloRingMin) <= optin;
     // The deepest ring that fits: every slot beyond three is a row in flight.
     uint32_t ring = kHaloRingMin;
@@ -1694,18 +1699,26 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "weight tensor map rejected");
-    static size_t configured[2] = {0, 0};
-    if (smem > configured[stack]) {
-        DK_CUDA(cudaFuncSetAttribute(stack ? k_conv3x3_halo<true> : k_conv3x3_halo<false>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    using HaloKernel = void (*)(const CUtensorMap, const CUtensorMap, HaloConvArgs);
+    const uint32_t last = (c.cin - (chunks - 1u) * 64u + 15u) / 16u;
+    HaloKernel kernels[2][2][4] = {
+        {{k_conv3x3_halo<false, 1, 1>, k_conv3x3_halo<false, 1, 2>, k_conv3x3_halo<false, 1, 3>,
+          k_conv3x3_halo<false, 1, 4>},
+         {k_conv3x3_halo<false, 2, 1>, k_conv3x3_halo<false, 2, 2>, k_conv3x3_halo<false, 2, 3>,
+          k_conv3x3_halo<false, 2, 4>}},
+        {{k_conv3x3_halo<true, 1, 1>, k_conv3x3_halo<true, 1, 2>, k_conv3x3_halo<true, 1, 3>,
+          k_conv3x3_halo<true, 1, 4>},
+         {k_conv3x3_halo<true, 2, 1>, k_conv3x3_halo<true, 2, 2>, k_conv3x3_halo<true, 2, 3>,
+          k_conv3x3_halo<true, 2, 4>}}};
+    HaloKernel kernel = kernels[stack][chunks - 1u][last - 1u];
+    static size_t configured[2][2][4] = {};
+    if (smem > configured[stack][chunks - 1u][last - 1u]) {
+        DK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                 "conv3x3 (halo) shared memory");
-        configured[stack] = smem;
+        configured[stack][chunks - 1u][last - 1u] = smem;
     }
     uint32_t grid = std::min(sms, a.totalRows);
-    if (stack)
-        k_conv3x3_halo<true><<<grid, 320, smem, st>>>(mapIn, mapW, a);
-    else
-        k_conv3x3_halo<false><<<grid, 320, smem, st>>>(mapIn, mapW, a);
+    kernel<<<grid, 320, smem, st>>>(mapIn, mapW, a);
     DK_CUDA(cudaGetLastError(), "conv3x3 (halo rows, TMA + tcgen05) launch");
     return DK_OK;
 }

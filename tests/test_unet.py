@@ -79,7 +79,7 @@ def test_conv3x3_forward(lib, cin, cout, act, ldi_extra, ldo_extra, co_off):
 
 @pytest.mark.parametrize("cin,cout,act,ldi_extra,ldo_extra,co_off", [
     (16, 32, 1, 0, 0, 0), (32, 32, 1, 32, 0, 0), (96, 32, 1, 0, 64, 64), (32, 16, 0, 0, 0, 0), (64, 64, 1, 0, 0, 0),
-    (64, 96, 1, 0, 0, 0), (128, 32, 1, 0, 0, 0)])
+    (64, 96, 1, 0, 0, 0), (128, 32, 1, 0, 0, 0), (48, 32, 1, 0, 0, 0), (80, 16, 1, 0, 0, 0), (112, 64, 1, 0, 0, 0)])
 def test_conv3x3_forward_wide(lib, cin, cout, act, ldi_extra, ldo_extra, co_off):
     # Images at least 128 pixels wide (the halo-row kernel's layers), with a
     # partial last tile column and rows that do not fill the row blocks.
@@ -108,7 +108,7 @@ def test_conv3x3_forward_wide(lib, cin, cout, act, ldi_extra, ldo_extra, co_off)
         assert torch.equal(untouched, expect)
 
 
-@pytest.mark.parametrize("cin,cout", [(32, 32), (96, 32), (64, 64), (32, 16)])
+@pytest.mark.parametrize("cin,cout", [(32, 32), (96, 32), (64, 64), (32, 16), (48, 32), (80, 16)])
 def test_conv3x3_forward_tall(lib, cin, cout):
     # About 40 output rows per persistent CTA, crossing tile columns and
     # images: the halo-row ring (up to 16 slots) and the stacked-tap
