@@ -428,6 +428,8 @@ size_t tcSmemBytes(uint32_t cout) { return (size_t)kTcStages * (kTcRows * 128u +
 // Every mbarrier wait is bounded (about 2 s); a role that times out records
 // the error and stops, the others then time out in turn, and the CTA frees
 // its tensor memory before returning.
+constexpr uint32_t kHaloPix = 130;          // 128 output pixels and one on each side
+constexpr uint32_t kHaloSlotBytes = 17408;  // 130 rows of 128 B, padded to 17 x 1024 B
 constexpr uint32_t kTmaStagesMin = 4;   // (tap, chunk) stages in flight: at least 4,
 constexpr uint32_t kTmaStagesMax = 8;   // more where shared memory holds them
 constexpr uint32_t kTmaBarBytes = 256;  // full[8] empty[8] accFull[4] accEmpty[4], TMEM slot, flag
@@ -598,13 +600,32 @@ __device__ __forceinline__ void epilogueRow(uint32_t src, uint32_t c0, uint32_t 
     __syncwarp();
 }
 
+// The K steps of one row-tap stage: for dx = 0, 1, 2 the A operand is the
+// stage's input row from pixel dx on (128 bytes further per pixel) and the B
+// operand the weights of tap (dy, dx); straight-line code (see the halo
+// kernel on branches between MMAs).
+template <uint32_t kSteps>
+__device__ __forceinline__ void rowTapMmas(uint32_t d, uint32_t aLo, uint32_t bLo, uint32_t bTapU, uint32_t hi,
+                                           uint32_t idesc, uint32_t acc) {
+#pragma unroll
+    for (uint32_t dx = 0; dx < 3u; ++dx)
+#pragma unroll
+        for (uint32_t ks = 0; ks < kSteps; ++ks)
+            mmaF16(d, aLo + dx * 8u + 2u * ks, bLo + dx * bTapU + 2u * ks, hi, idesc, (dx | ks) ? 1u : acc);
+}
+
+// kRowTap (images at least 128 pixels wide): an output tile is 128 pixels of
+// one row and a pipeline stage is (dy, 64-channel chunk): one box of the input
+// row y + dy - 1, 130 pixels wide, and the weights of the three taps (dy, 0..2),
+// so a tile takes 3 x chunks stages and waits instead of 9 x chunks.
+template <bool kRowTap>
 __global__ void __launch_bounds__(320, 1)
     k_conv3x3_tma(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW, TmaConvArgs a) {
     extern __shared__ unsigned char dsm[];
     const uint32_t raw = smemAddr(dsm);
     unsigned char* sm = dsm + (((raw + 1023u) & ~1023u) - raw);
     const uint32_t N = a.cout;
-    const uint32_t aBytes = 128u * 128u, bBytes = N * 128u;
+    const uint32_t aBytes = kRowTap ? kHaloSlotBytes : 128u * 128u, bBytes = (kRowTap ? 3u : 1u) * N * 128u;
     unsigned char* sA = sm;
     const uint32_t S = a.stages;
     unsigned char* sB = sm + S * aBytes;
@@ -639,10 +660,37 @@ __global__ void __launch_bounds__(320, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t taddr = *tslot;
-    const uint32_t txBytes = aBytes + bBytes;
+    const uint32_t txBytes = (kRowTap ? kHaloPix * 128u : aBytes) + bBytes;
     volatile int* abortV = abortFlag;
 
-    if (warp == 0) {
+    if (warp == 0 && kRowTap) {
+        if (lane == 0) {
+            uint32_t g = 0;
+            RingPos pos{0u, 0u};
+            bool ok = true;
+            for (uint32_t tile = blockIdx.x; ok && tile < a.numTiles && !*abortV; tile += gridDim.x) {
+                uint32_t tx = tile % a.tilesX, rest = tile / a.tilesX;
+                uint32_t ty = rest % a.tilesY, img = rest / a.tilesY;
+                int x0 = (int)(tx * 128u), y0 = (int)ty;
+                for (uint32_t dy = 0; ok && dy < 3u; ++dy) {
+                    for (uint32_t c = 0; c < a.chunks; ++c, ++g, pos.advance(S)) {
+                        if (g >= S && !mbarWait(emptyBar + 8u * pos.slot, pos.phase ^ 1u)) {
+                            ok = false;
+                            break;
+                        }
+                        const uint32_t full = fullBar + 8u * pos.slot;
+                        mbarExpectTx(full, txBytes);
+                        tmaLoad4(smemAddr(sA + pos.slot * aBytes), &mapIn, (int)(c * 64u), x0 - 1, y0 + (int)dy - 1,
+                                 (int)img, full);
+                        for (uint32_t dx = 0; dx < 3u; ++dx)
+                            tmaLoad3(smemAddr(sB + pos.slot * bBytes + dx * N * 128u), &mapW, (int)(c * 64u),
+                                     (int)(dy * 3u + dx), 0, full);
+                    }
+                }
+            }
+            if (!ok) *abortV = 1;
+        }
+    } else if (warp == 0) {
         if (lane == 0) {
             uint32_t g = 0;
             RingPos pos{0u, 0u};
@@ -685,7 +733,7 @@ __global__ void __launch_bounds__(320, 1)
                 const uint32_t dAddr = taddr + b * a.cols;
                 bool ok = true;
                 uint32_t acc = 0u;
-                for (uint32_t it = 0; ok && it < 9u; ++it) {
+                for (uint32_t it = 0; ok && it < (kRowTap ? 3u : 9u); ++it) {
                     for (uint32_t c = 0; c < a.chunks; ++c, pos.advance(S)) {
                         if (!mbarWait(fullBar + 8u * pos.slot, pos.phase)) {
                             ok = false;
@@ -695,6 +743,16 @@ __global__ void __launch_bounds__(320, 1)
                         // K steps of 16 channels in this (tap, chunk): 4, fewer in a partial last chunk
                         const uint32_t steps = c + 1u < a.chunks ? 4u : lastSteps;
                         const uint32_t aLo = aLo0 + pos.slot * (aBytes >> 4), bLo = bLo0 + pos.slot * (bBytes >> 4);
+                        if (kRowTap) {
+                            const uint32_t bTapU = (N * 128u) >> 4;
+                            if (steps == 4u) rowTapMmas<4>(dAddr, aLo, bLo, bTapU, hi, idesc, acc);
+                            else if (steps == 3u) rowTapMmas<3>(dAddr, aLo, bLo, bTapU, hi, idesc, acc);
+                            else if (steps == 2u) rowTapMmas<2>(dAddr, aLo, bLo, bTapU, hi, idesc, acc);
+                            else rowTapMmas<1>(dAddr, aLo, bLo, bTapU, hi, idesc, acc);
+                            acc = 1u;
+                            umaCommit(emptyBar + 8u * pos.slot);
+                            continue;
+                        }
                         mmaF16(dAddr, aLo, bLo, hi, idesc, acc);
                         acc = 1u;
                         if (steps > 1u) mmaF16(dAddr, aLo + 2u, bLo + 2u, hi, idesc, 1u);
@@ -740,9 +798,9 @@ __global__ void __launch_bounds__(320, 1)
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(nbuf * a.cols));
 }
 
-size_t tmaSmemBytes(uint32_t cout, bool staged, uint32_t stages) {
-    return (size_t)stages * (128u * 128u + cout * 128u) + 1024u + kTmaBarBytes +
-           (staged ? kEpiWarps * epiWarpBytes(cout) : 0u);
+size_t tmaSmemBytes(uint32_t cout, bool staged, uint32_t stages, bool rowTap) {
+    const size_t stage = rowTap ? kHaloSlotBytes + 3u * cout * 128u : 128u * 128u + cout * 128u;
+    return (size_t)stages * stage + 1024u + kTmaBarBytes + (staged ? kEpiWarps * epiWarpBytes(cout) : 0u);
 }
 
 // -------------------------------------- tcgen05 + TMA, halo-row ring ----
@@ -770,8 +828,6 @@ constexpr uint32_t kHaloRingMin = 4;        // halo-row slots: three rows in use
 constexpr uint32_t kHaloRingMax = 16;       // and as many more loading as shared memory holds
 constexpr uint32_t kHaloBarBytes = 1024;    // full[16] empty[16] weights accFull[32] accEmpty[32], TMEM slot, flag
 constexpr uint32_t kHaloAccMax = 32;
-constexpr uint32_t kHaloPix = 130;          // 128 output pixels and one on each side
-constexpr uint32_t kHaloSlotBytes = 17408;  // 130 rows of 128 B, padded to 17 x 1024 B
 
 struct HaloConvArgs {
     const float* bias;
@@ -1723,7 +1779,10 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     return DK_OK;
 }
 
-int launchConvTma(const ConvArgs& c, cudaStream_t st) {
+// rowTap: the row-tap mode (images at least 128 pixels wide); else one stage
+// per (tap, chunk) over 2-D tiles.
+int launchConvTma(const ConvArgs& c, cudaStream_t st, bool rowTap) {
+    rowTap = rowTap && c.w_ >= 128u;
     EncodeTiledFn enc = encodeTiled();
     if (!enc) return fail(DK_ERROR_COMMAND_FAILED, "cuTensorMapEncodeTiled is not available");
     TmaConvArgs a;
@@ -1740,6 +1799,7 @@ int launchConvTma(const ConvArgs& c, cudaStream_t st) {
     a.accumulate = c.accumulate;
     uint32_t tw = 1;
     while (tw * 2u <= c.w_ && tw < 128u) tw *= 2u;
+    if (rowTap) tw = 128u;
     a.tw = tw;
     a.th = 128u / tw;
     a.tilesX = (c.w_ + a.tw - 1) / a.tw;
@@ -1751,7 +1811,7 @@ int launchConvTma(const ConvArgs& c, cudaStream_t st) {
     alignas(64) CUtensorMap mapIn, mapW;
     cuuint64_t dimIn[4] = {c.cin, c.w_, c.h, c.n};
     cuuint64_t strideIn[3] = {(cuuint64_t)c.ldi * 2u, (cuuint64_t)c.w_ * c.ldi * 2u, (cuuint64_t)c.h * c.w_ * c.ldi * 2u};
-    cuuint32_t boxIn[4] = {64u, a.tw, a.th, 1u};
+    cuuint32_t boxIn[4] = {64u, rowTap ? kHaloPix : a.tw, a.th, 1u};
     cuuint32_t unit[4] = {1u, 1u, 1u, 1u};
     CUresult r = enc(&mapIn, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(c.in), dimIn, strideIn,
                      boxIn, unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -1765,22 +1825,31 @@ int launchConvTma(const ConvArgs& c, cudaStream_t st) {
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "weight tensor map rejected");
     const size_t optin = (size_t)deviceProp().sharedMemPerBlockOptin;
-    const bool staged = stagedStores(c) && tmaSmemBytes(c.cout, true, kTmaStagesMin) <= optin;
-    uint32_t stages = kTmaStagesMin;
-    const uint32_t stageCap = depthCap("DK_CONV_STAGES", kTmaStagesMin, kTmaStagesMax);
-    while (stages < stageCap && tmaSmemBytes(c.cout, staged, stages + 1u) <= optin) ++stages;
+    const uint32_t minStages = rowTap ? 2u : kTmaStagesMin;
+    if (tmaSmemBytes(c.cout, false, minStages, rowTap) > optin) {
+        if (rowTap) return launchConvTma(c, st, false);
+        return fail(DK_ERROR_INVALID_ARGUMENT, "conv3x3: the layer does not fit shared memory");
+    }
+    const bool staged = stagedStores(c) && tmaSmemBytes(c.cout, true, minStages, rowTap) <= optin;
+    uint32_t stages = minStages;
+    const uint32_t stageCap = depthCap("DK_CONV_STAGES", minStages, kTmaStagesMax);
+    while (stages < stageCap && tmaSmemBytes(c.cout, staged, stages + 1u, rowTap) <= optin) ++stages;
     a.staged = staged ? 1 : 0;
     a.stages = stages;
-    size_t smem = tmaSmemBytes(c.cout, staged, stages);
-    static size_t configured = 0;
-    if (smem > configured) {
-        DK_CUDA(cudaFuncSetAttribute(k_conv3x3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    size_t smem = tmaSmemBytes(c.cout, staged, stages, rowTap);
+    static size_t configured[2] = {0, 0};
+    if (smem > configured[rowTap]) {
+        DK_CUDA(cudaFuncSetAttribute(rowTap ? k_conv3x3_tma<true> : k_conv3x3_tma<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                 "conv3x3 shared memory");
-        configured = smem;
+        configured[rowTap] = smem;
     }
     uint32_t grid = (uint32_t)deviceProp().multiProcessorCount;
     if (grid > a.numTiles) grid = a.numTiles;
-    k_conv3x3_tma<<<grid, 320, smem, st>>>(mapIn, mapW, a);
+    if (rowTap)
+        k_conv3x3_tma<true><<<grid, 320, smem, st>>>(mapIn, mapW, a);
+    else
+        k_conv3x3_tma<false><<<grid, 320, smem, st>>>(mapIn, mapW, a);
     DK_CUDA(cudaGetLastError(), "conv3x3 (TMA + tcgen05) launch");
     return DK_OK;
 }
@@ -1811,7 +1880,7 @@ int dk_unet_conv3x3(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t
         if (rc != dk::kHaloUnfit) return rc;
     }
     if (dk::g_convPath >= 2 && cout <= 256u) {
-        int rc = dk::launchConvTma(a, st);
+        int rc = dk::launchConvTma(a, st, dk::g_convPath == 3);
         if (rc != DK_OK) return rc;
         return DK_OK;
     }

@@ -79,10 +79,13 @@ def test_conv3x3_forward(lib, cin, cout, act, ldi_extra, ldo_extra, co_off):
 
 @pytest.mark.parametrize("cin,cout,act,ldi_extra,ldo_extra,co_off", [
     (16, 32, 1, 0, 0, 0), (32, 32, 1, 32, 0, 0), (96, 32, 1, 0, 64, 64), (32, 16, 0, 0, 0, 0), (64, 64, 1, 0, 0, 0),
-    (64, 96, 1, 0, 0, 0), (128, 32, 1, 0, 0, 0), (48, 32, 1, 0, 0, 0), (80, 16, 1, 0, 0, 0), (112, 64, 1, 0, 0, 0)])
+    (64, 96, 1, 0, 0, 0), (128, 32, 1, 0, 0, 0), (48, 32, 1, 0, 0, 0), (80, 16, 1, 0, 0, 0), (112, 64, 1, 0, 0, 0),
+    (160, 64, 1, 32, 0, 0), (224, 96, 1, 0, 32, 32), (288, 128, 1, 0, 0, 0), (96, 96, 1, 0, 0, 0),
+    (176, 160, 0, 16, 0, 0)])
 def test_conv3x3_forward_wide(lib, cin, cout, act, ldi_extra, ldo_extra, co_off):
-    # Images at least 128 pixels wide (the halo-row kernel's layers), with a
-    # partial last tile column and rows that do not fill the row blocks.
+    # Images at least 128 pixels wide (the halo-row kernel's layers, and the
+    # row-tap mode of the per-tap kernel for the layers whose weights do not
+    # fit the halo kernel), with a partial last tile column.
     g = torch.Generator().manual_seed(cin * 11 + cout)
     n, h, w = 2, 9, 200
     ldi, ldo = cin + ldi_extra, cout + ldo_extra + co_off
