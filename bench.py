@@ -705,7 +705,8 @@ def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, t
 def unet_inference_measure(reps=10):
     """The U-Net's forward pass at 1920x1088 (the network's padding of 1080p):
     CUDA-event time, TFLOP/s against the dense bf16 peak, per convolution path
-    (3: halo-row kernel where a layer fits, else per-tap; 2: per-tap only)."""
+    (3: the halo-row kernel where a layer fits, else the per-tap kernel in its
+    row-tap mode; 2: the per-tap kernel alone, one stage per tap and chunk)."""
     import torch
     from denrimrendererkit_gb300 import DenrimRenderer, library
     from denrimrendererkit_gb300.denoiser import UNet, flops_per_pixel
@@ -734,7 +735,8 @@ def unet_inference_measure(reps=10):
     best = out["path3"]
     return {"workload": "5-level U-Net 32-64-96-128-160, one 1920x1088 image, forward", "ms": best["ms"],
             "gflop": flops / 1e9,
-            "roofline": {"kernel": "k_conv3x3_halo / k_conv3x3_tma (whole forward pass)", "bound": "tensor",
+            "roofline": {"kernel": "k_conv3x3_halo (stacked taps) / k_conv3x3_tma (row-tap) / avgpool / upsample "
+                                   "(whole forward pass)", "bound": "tensor",
                          "achieved": best["tflops"], "peak": peak, "unit": "TFLOP/s", "frac": best["tflops"] / peak,
                          "peak_source": f"{kind} (MEASURED_PEAKS.json bf16_tflops)"},
             "per_path": out, "tensor_wait_errors": int(err.value)}
