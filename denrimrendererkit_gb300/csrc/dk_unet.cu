@@ -488,6 +488,8 @@ __host__ __device__ constexpr uint32_t epiCols(uint32_t n) { return epiSplit(n) 
 // banks), then the 32 pixels' global row pointers.
 __host__ __device__ constexpr uint32_t epiPitch(uint32_t cols) { return 2u * cols + 16u; }
 __host__ __device__ constexpr uint32_t epiWarpBytes(uint32_t n) { return 32u * epiPitch(epiCols(n)) + 32u * 8u; }
+// The same for a warp that takes all N channels of its rows.
+__host__ __device__ constexpr uint32_t epiWarpBytesAll(uint32_t n) { return 32u * epiPitch(n) + 32u * 8u; }
 __host__ __device__ constexpr uint32_t accBuffers(uint32_t cols) { return 4u * cols <= 512u ? 4u : 2u; }
 
 // This warp's channels [c0, c1) of one accumulator (its 32 TMEM lanes: 32
@@ -905,7 +907,7 @@ __global__ void __launch_bounds__(320, 1)
         mbarInit(wBar, 1);
         for (uint32_t b = 0; b < nbuf; ++b) {
             mbarInit(accFullBar + 8u * b, 1);
-            mbarInit(accEmptyBar + 8u * b, epiSplit(N) ? 256u : 128u);
+            mbarInit(accEmptyBar + 8u * b, (kStack || !epiSplit(N)) ? 128u : 256u);
         }
         *abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -969,6 +971,17 @@ __global__ void __launch_bounds__(320, 1)
             const uint32_t hi = descHi(), aLo0 = descLo(smemAddr(sRing)), bLo0 = descLo(smemAddr(sW));
             const uint32_t tileU = (3u * wBoxBytes) >> 4, dyU = wBoxBytes >> 4;  // in 16-byte units
             const uint32_t Q = nbuf;
+            // One halo row's stacked MMAs (N = 3 Cout) into the slots from `d` on.
+            auto stackedRow = [&](uint32_t aRow, uint32_t d) {
+#pragma unroll
+                for (uint32_t dx = 0; dx < 3u; ++dx)
+#pragma unroll
+                    for (uint32_t c = 0; c < kC; ++c)
+#pragma unroll
+                        for (uint32_t ks = 0; ks < (c + 1u < kC ? 4u : kLast); ++ks)
+                            mmaF16(d, aRow + dx * 8u + c * (kHaloSlotBytes >> 4) + 2u * ks,  // pixel dx: 128 B on
+                                   bLo0 + (dx * kC + c) * tileU + 2u * ks, hi, idesc3, 1u);
+            };
             bool ok = mbarWait(wBar, 0u);
             uint32_t t0 = 0;      // output rows of the earlier segments
             RingPos hp{0u, 0u};   // the current halo row's ring slot
@@ -977,7 +990,32 @@ __global__ void __launch_bounds__(320, 1)
             RowSegment sg;
             while (ok && !*abortV && nextSegment(a, cur, end, sg)) {
                 const uint32_t rows = sg.y1 - sg.y0;
-                for (uint32_t k = 0; k < rows + 2u; ++k, hp.advance(R)) {
+                for (uint32_t k = 0; k < rows + 2u;) {
+                    // Two interior halo rows at once when both stack into adjacent
+                    // slots: their waits first, then both rows' MMAs and commits as
+                    // one straight-line run (one branch per two rows).
+                    if (k >= 2u && k + 1u < rows && ((t0 + k - 2u) & (Q - 1u)) + 3u < Q) {
+                        RingPos hp1 = hp;
+                        hp1.advance(R);
+                        const uint32_t t = t0 + k, sLo = (t0 + k - 2u) & (Q - 1u);
+                        if (!mbarWait(accEmptyBar + 8u * (t & (Q - 1u)), (t >> bufShift) & 1u) ||
+                            !mbarWait(accEmptyBar + 8u * ((t + 1u) & (Q - 1u)), ((t + 1u) >> bufShift) & 1u) ||
+                            !mbarWait(fullBar + 8u * hp.slot, hp.phase) || !mbarWait(fullBar + 8u * hp1.slot, hp1.phase)) {
+                            ok = false;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                        stackedRow(aLo0 + hp.slot * (slotBytes >> 4), taddr + sLo * N);
+                        umaCommit(emptyBar + 8u * hp.slot);
+                        umaCommit(accFullBar + 8u * sLo);
+                        stackedRow(aLo0 + hp1.slot * (slotBytes >> 4), taddr + (sLo + 1u) * N);
+                        umaCommit(emptyBar + 8u * hp1.slot);
+                        umaCommit(accFullBar + 8u * (sLo + 1u));
+                        k += 2u;
+                        hp = hp1;
+                        hp.advance(R);
+                        continue;
+                    }
                     if (k < rows) {  // output row k enters: its slot must have been read and cleared
                         const uint32_t t = t0 + k;
                         if (!mbarWait(accEmptyBar + 8u * (t & (Q - 1u)), (t >> bufShift) & 1u)) ok = false;
@@ -990,15 +1028,7 @@ __global__ void __launch_bounds__(320, 1)
                     const uint32_t sLo = (t0 + jLo) & (Q - 1u);
                     const bool stacked = k >= 2u && k < rows && sLo + 2u < Q;
                     if (stacked) {
-                        const uint32_t d = taddr + sLo * N;
-#pragma unroll
-                        for (uint32_t dx = 0; dx < 3u; ++dx)
-#pragma unroll
-                            for (uint32_t c = 0; c < kC; ++c)
-#pragma unroll
-                                for (uint32_t ks = 0; ks < (c + 1u < kC ? 4u : kLast); ++ks)
-                                    mmaF16(d, aRow + dx * 8u + c * (kHaloSlotBytes >> 4) + 2u * ks,  // pixel dx: 128 B on
-                                           bLo0 + (dx * kC + c) * tileU + 2u * ks, hi, idesc3, 1u);
+                        stackedRow(aRow, taddr + sLo * N);
                     } else {
                         for (uint32_t j = jLo; j <= jHi; ++j) {
                             const uint32_t dy = k - j;
@@ -1016,6 +1046,8 @@ __global__ void __launch_bounds__(320, 1)
                     }
                     umaCommit(emptyBar + 8u * hp.slot);  // halo row k has no reader left
                     if (k >= 2u) umaCommit(accFullBar + 8u * ((t0 + k - 2u) & (Q - 1u)));  // row k - 2 is complete
+                    ++k;
+                    hp.advance(R);
                 }
                 t0 += rows;
             }
@@ -1080,21 +1112,26 @@ __global__ void __launch_bounds__(320, 1)
         }
     } else {
         // Epilogue warps 2..9: TMEM lane quarter warp % 4 (one output pixel per
-        // thread), channel half (warp - 2) / 4.
-        const uint32_t q = warp & 3u, half = (warp - 2u) >> 2;
+        // thread); set (warp - 2) / 4.  Stacked: set s takes every channel of
+        // the rows of parity s (and owns the accumulator slots of that parity:
+        // the slot count is even), two rows in flight; otherwise both sets take
+        // every row, each half of the channels.
+        const uint32_t q = warp & 3u, set = (warp - 2u) >> 2;
         const uint32_t r = q * 32u + lane;
-        const uint32_t cw = epiCols(N), c0 = half * cw, c1 = epiSplit(N) ? c0 + cw : (half ? 0u : N);
-        unsigned char* stage =
-            a.staged ? reinterpret_cast<unsigned char*>(bars) + kHaloBarBytes + (warp - 2u) * epiWarpBytes(N) : nullptr;
+        const uint32_t cw = epiCols(N);
+        const uint32_t c0 = kStack ? 0u : set * cw, c1 = kStack ? N : (epiSplit(N) ? c0 + cw : (set ? 0u : N));
+        unsigned char* stage = a.staged ? reinterpret_cast<unsigned char*>(bars) + kHaloBarBytes +
+                                              (warp - 2u) * (kStack ? epiWarpBytesAll(N) : epiWarpBytes(N))
+                                        : nullptr;
         uint32_t t = 0;
         bool ok = c1 > c0;
         const uint32_t quarter = taddr + ((q * 32u) << 16);
         const uint32_t slotCols = kStack ? N : a.cols;
-        if (kStack && ok) {
+        if (kStack) {
             // Every slot starts zeroed; its first release lets the MMA warp in.
-            for (uint32_t b = 0; b < nbuf; ++b) zeroColumns(quarter + b * slotCols, c0, c1);
+            for (uint32_t b = set; b < nbuf; b += 2u) zeroColumns(quarter + b * slotCols, c0, c1);
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            for (uint32_t b = 0; b < nbuf; ++b) mbarArrive(accEmptyBar + 8u * b);
+            for (uint32_t b = set; b < nbuf; b += 2u) mbarArrive(accEmptyBar + 8u * b);
         }
         uint32_t cur = rangeBegin(a, blockIdx.x);
         const uint32_t end = rangeBegin(a, blockIdx.x + 1u);
@@ -1102,6 +1139,7 @@ __global__ void __launch_bounds__(320, 1)
         while (ok && nextSegment(a, cur, end, sg)) {
             const uint32_t img = sg.img, px = sg.tx * 128u + r;
             for (uint32_t py = sg.y0; py < sg.y1; ++py, ++t) {
+                if (kStack && (t & 1u) != set) continue;  // the other set's row
                 const uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
                 if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
                     *abortV = 1;
@@ -1122,9 +1160,9 @@ __global__ void __launch_bounds__(320, 1)
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(tmemCols));
 }
 
-size_t haloSmemBytes(uint32_t cout, uint32_t chunks, bool staged, uint32_t ring) {
+size_t haloSmemBytes(uint32_t cout, uint32_t chunks, bool staged, uint32_t ring, bool stack) {
     return 1024u + (size_t)ring * chunks * kHaloSlotBytes + 9u * (size_t)chunks * cout * 128u + kHaloBarBytes +
-           (staged ? kEpiWarps * epiWarpBytes(cout) : 0u);
+           (staged ? kEpiWarps * (stack ? epiWarpBytesAll(cout) : epiWarpBytes(cout)) : 0u);
 }
 
 // -------------------------------------------------------------- wgrad ----
@@ -1696,14 +1734,21 @@ constexpr int kHaloUnfit = -1;
 int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     const uint32_t chunks = (c.cin + 63u) / 64u;
     const size_t optin = (size_t)deviceProp().sharedMemPerBlockOptin;
-    if (c.w_ < 128u || c.cout > 256u || chunks > 2u || haloSmemBytes(c.cout, chunks, false, kHaloRingMin) > optin)
+    // Vertical taps stacked into one MMA (N = 3 Cout <= 256) with a rolling
+    // window of accumulator slots; DK_CONV_STACK=0 keeps one MMA per tap.
+    const char* stackEnv = getenv("DK_CONV_STACK");
+    const bool stack = c.cout * 3u <= 256u && !(stackEnv && stackEnv[0] == '0');
+    // Stacked, a halo row is read only in its own step: two slots suffice
+    // (one in use, one loading); else three rows are in use at a time.
+    const uint32_t minRing = stack ? 2u : kHaloRingMin;
+    if (c.w_ < 128u || c.cout > 256u || chunks > 2u || haloSmemBytes(c.cout, chunks, false, minRing, stack) > optin)
         return kHaloUnfit;
-    const bool staged = stagedStores(c) && haloSmemBytes(c.cout, chunks, true, kHaloRingMin) <= optin;
-    // The deepest ring that fits: every slot beyond three is a row in flight.
-    uint32_t ring = kHaloRingMin;
-    const uint32_t ringCap = depthCap("DK_CONV_HALO_RING", kHaloRingMin, kHaloRingMax);
-    while (ring < ringCap && haloSmemBytes(c.cout, chunks, staged, ring + 1u) <= optin) ++ring;
-    const size_t smem = haloSmemBytes(c.cout, chunks, staged, ring);
+    const bool staged = stagedStores(c) && haloSmemBytes(c.cout, chunks, true, minRing, stack) <= optin;
+    // The deepest ring that fits: every further slot is a row in flight.
+    uint32_t ring = minRing;
+    const uint32_t ringCap = depthCap("DK_CONV_HALO_RING", minRing, kHaloRingMax);
+    while (ring < ringCap && haloSmemBytes(c.cout, chunks, staged, ring + 1u, stack) <= optin) ++ring;
+    const size_t smem = haloSmemBytes(c.cout, chunks, staged, ring, stack);
     EncodeTiledFn enc = encodeTiled();
     if (!enc) return fail(DK_ERROR_COMMAND_FAILED, "cuTensorMapEncodeTiled is not available");
     HaloConvArgs a;
@@ -1720,10 +1765,6 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     a.accumulate = c.accumulate;
     a.staged = staged ? 1 : 0;
     a.ring = ring;
-    // Vertical taps stacked into one MMA (N = 3 Cout <= 256) with a rolling
-    // window of accumulator slots; DK_CONV_STACK=0 keeps one MMA per tap.
-    const char* stackEnv = getenv("DK_CONV_STACK");
-    const bool stack = c.cout * 3u <= 256u && !(stackEnv && stackEnv[0] == '0');
     a.slots = 0u;
     a.logSlots = 0u;
     if (stack) {
