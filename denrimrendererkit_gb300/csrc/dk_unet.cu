@@ -30,6 +30,16 @@ __device__ __forceinline__ uint32_t smemAddr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// Programmatic dependent launch: the forward pass's kernels are launched so
+// that each may start (and set up shared memory, barriers and tensor memory)
+// while the previous one drains.  pdlWait() blocks until the previous kernel
+// in the stream has completed and its writes are visible; every thread calls
+// it before its first global memory access.  pdlRelease() lets the next
+// kernel be scheduled.  Both are no-ops for a kernel launched without the
+// attribute.
+__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdlRelease() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // 16-byte async copy; `bytes` 0 fills the destination with zeros.
 __device__ __forceinline__ void cpAsync16(void* dst, const void* src, uint32_t bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smemAddr(dst)), "l"(src), "r"(bytes));
@@ -661,6 +671,8 @@ __global__ void __launch_bounds__(320, 1)
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    pdlRelease();
+    pdlWait();
     const uint32_t taddr = *tslot;
     const uint32_t txBytes = (kRowTap ? kHaloPix * 128u : aBytes) + bBytes;
     volatile int* abortV = abortFlag;
@@ -916,6 +928,8 @@ __global__ void __launch_bounds__(320, 1)
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    pdlRelease();
+    pdlWait();
     const uint32_t taddr = *tslot;
     volatile int* abortV = abortFlag;
 
@@ -1443,6 +1457,8 @@ __global__ void k_relu_backward8(const __nv_bfloat16* out, uint32_t ldo, const _
 
 __global__ void k_avgpool2_8(const __nv_bfloat16* in, uint32_t ldi, __nv_bfloat16* out, uint32_t ldo, uint32_t coOff,
                              uint32_t groups, uint32_t h, uint32_t w, uint32_t total) {
+    pdlRelease();
+    pdlWait();
     const uint32_t wo = w / 2u, ho = h / 2u;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
         const uint32_t q = i / groups, k = (i - q * groups) * 8u;
@@ -1491,6 +1507,8 @@ __global__ void k_avgpool2_backward8(const __nv_bfloat16* dout, uint32_t ldd, __
 __global__ void k_upsample2_8(const __nv_bfloat16* in, uint32_t ldi, __nv_bfloat16* out, uint32_t ldo, uint32_t coOff,
                               uint32_t groups, uint32_t h, uint32_t w, uint32_t total) {
     // one thread per input pixel and group, written to its 2x2 outputs
+    pdlRelease();
+    pdlWait();
     const uint32_t W = 2u * w;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gstride()) {
         const uint32_t q = i / groups, k = (i - q * groups) * 8u;
@@ -1691,6 +1709,29 @@ inline bool vec8(std::initializer_list<uint32_t> counts, std::initializer_list<c
 // 1: the cp.async + tcgen05 one; 0: the mma.sync one.
 int g_convPath = 3;
 
+// Launch with programmatic stream serialization (see pdlWait); DK_PDL=0 launches
+// plainly.
+template <typename... KArgs, typename... Args>
+cudaError_t launchPdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                      Args... args) {
+    static int enabled = -1;
+    if (enabled < 0) {
+        const char* e = getenv("DK_PDL");
+        enabled = (e && e[0] == '0') ? 0 : 1;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = enabled ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // dependency on libcuda).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -1815,7 +1856,7 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
         configured[stack][chunks - 1u][last - 1u] = smem;
     }
     uint32_t grid = std::min(sms, a.totalRows);
-    kernel<<<grid, 320, smem, st>>>(mapIn, mapW, a);
+    DK_CUDA(launchPdl(kernel, dim3(grid), dim3(320), smem, st, mapIn, mapW, a), "conv3x3 (halo) launch");
     DK_CUDA(cudaGetLastError(), "conv3x3 (halo rows, TMA + tcgen05) launch");
     return DK_OK;
 }
@@ -1888,9 +1929,9 @@ int launchConvTma(const ConvArgs& c, cudaStream_t st, bool rowTap) {
     uint32_t grid = (uint32_t)deviceProp().multiProcessorCount;
     if (grid > a.numTiles) grid = a.numTiles;
     if (rowTap)
-        k_conv3x3_tma<true><<<grid, 320, smem, st>>>(mapIn, mapW, a);
+        DK_CUDA(launchPdl(k_conv3x3_tma<true>, dim3(grid), dim3(320), smem, st, mapIn, mapW, a), "conv3x3 launch");
     else
-        k_conv3x3_tma<false><<<grid, 320, smem, st>>>(mapIn, mapW, a);
+        DK_CUDA(launchPdl(k_conv3x3_tma<false>, dim3(grid), dim3(320), smem, st, mapIn, mapW, a), "conv3x3 launch");
     DK_CUDA(cudaGetLastError(), "conv3x3 (TMA + tcgen05) launch");
     return DK_OK;
 }
@@ -2012,9 +2053,10 @@ int dk_unet_avgpool2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint
     if (!in || !out || c % 2u || h % 2u || w % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_avgpool2");
     const uint64_t total8 = (uint64_t)n * (h / 2u) * (w / 2u) * (c / 8u);
     if (dk::vec8({c, ldi, ldo, coOff}, {in, out}, total8)) {
-        dk::k_avgpool2_8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-            static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c / 8u, h, w, (uint32_t)total8);
-        DK_CUDA(cudaGetLastError(), "avgpool launch");
+        DK_CUDA(dk::launchPdl(dk::k_avgpool2_8, dim3(dk::gridFor(total8)), dim3(256), 0,
+                              static_cast<cudaStream_t>(stream), static_cast<const bf16*>(in), ldi,
+                              static_cast<bf16*>(out), ldo, coOff, c / 8u, h, w, (uint32_t)total8),
+                "avgpool launch");
         return DK_OK;
     }
     dk::k_avgpool2<<<dk::gridFor((uint64_t)n * h * w / 4 * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
@@ -2046,9 +2088,10 @@ int dk_unet_upsample2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uin
     if (!in || !out || c % 2u) return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_upsample2");
     const uint64_t total8 = (uint64_t)n * h * w * (c / 8u);
     if (dk::vec8({c, ldi, ldo, coOff}, {in, out}, total8)) {
-        dk::k_upsample2_8<<<dk::gridFor(total8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-            static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c / 8u, h, w, (uint32_t)total8);
-        DK_CUDA(cudaGetLastError(), "upsample launch");
+        DK_CUDA(dk::launchPdl(dk::k_upsample2_8, dim3(dk::gridFor(total8)), dim3(256), 0,
+                              static_cast<cudaStream_t>(stream), static_cast<const bf16*>(in), ldi,
+                              static_cast<bf16*>(out), ldo, coOff, c / 8u, h, w, (uint32_t)total8),
+                "upsample launch");
         return DK_OK;
     }
     dk::k_upsample2<<<dk::gridFor((uint64_t)n * h * w * 4 * c / 2), 256, 0, static_cast<cudaStream_t>(stream)>>>(
