@@ -281,7 +281,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(args, wl, {"implementation": impl}),
+            "config": config(args, wl), "implementation": impl,
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": kind, "sample": desc},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -988,7 +988,8 @@ def run_denoise(args, rank):
             "config": {"workload": "5-level U-Net 32-64-96-128-160 over beauty+albedo+normal+depth, "
                                    "1920x1088 inference; training 16 x 128^2 crops of 64 rendered 256^2 "
                                    "small-scene variants (4 spp -> 1024 spp)", "train_steps": steps},
-            "roofline": {"kernel": "k_conv3x3_tma (whole forward pass)", "bound": "tensor", "achieved": achieved,
+            "roofline": {"kernel": "U-Net convolutions, pooling, upsampling (whole forward pass)", "bound": "tensor",
+                         "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                          "peak_source": kind, "traffic": None, "gflop_per_inference": flops / 1e9},
             "train_step_ms": train_s / steps * 1e3, "render_pairs_s": render_s,
