@@ -481,11 +481,24 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
 // branches and read the same material record.  The order of paths does not
 // change any result: every path carries its own RNG state and pixel samples
 // are accumulated in sample order.
+// Keys: 0 a miss, 1 + material ID (at most kSortBins - 3), kSortBins - 2 a
+// material with a subsurface weight (shaded by the kernel that carries the
+// subsurface random walk), kSortBins - 1 a distance-volume hit.
+constexpr uint32_t kSubsurfaceKey = kSortBins - 2u;
 __device__ __forceinline__ uint32_t shadeKey(const DevScene& S, const Wave& W, uint32_t p) {
     uint32_t tri = __float_as_uint(W.hit[p].y);
     if (tri == kNoHit) return 0u;
     if (tri >= S.tri_count) return kSortBins - 1u;  // distance-volume hits
-    return 1u + min(__ldg(&S.tris[tri].material_id), kSortBins - 3u);
+    const uint32_t id = __ldg(&S.tris[tri].material_id);
+    // the material the shading kernel loads, and materialSubsurface's own test
+    const MatTable mt = matTable(W.jobs[W.rng[p].y >> 8]);
+    const float4* q = reinterpret_cast<const float4*>(S.mats + mt.base + min(id, mt.count - 1u));
+    Material m;
+    m.emission = __ldg(q + 1);
+    m.parameters = __ldg(q + 2);
+    m.subsurfaceColor = __ldg(q + 12);
+    if (materialSubsurface(m) > 0.0f) return kSubsurfaceKey;
+    return 1u + min(id, kSortBins - 3u);
 }
 
 __global__ void __launch_bounds__(256) k_sort_count(DevScene S, Wave W, uint32_t sel) {
@@ -518,6 +531,7 @@ __global__ void __launch_bounds__(kSortBins) k_sort_scan(Wave W) {
         __syncthreads();
     }
     W.bins[t] = v[t] - x;
+    if (t == kSubsurfaceKey) W.counts[7] = v[t] - x;  // shading-order index of the first subsurface path
 }
 
 // Block b places queue entries [b * 2048, b * 2048 + 2048) stably: an entry's
@@ -662,7 +676,11 @@ struct ShadeOut { bool survive; uint32_t neeMask; uint32_t maxBounces; };
 
 // The body of the reference bounce loop (PathTrace.metal:5252-5518) for one
 // path whose closest hit is already in W.hit.
-template <bool kVolumes>
+// kSss: the subsurface random walk is compiled in (the kernel for materials
+// with a subsurface weight, and for unsorted queues); without it the walk's
+// test is false at compile time, which leaves every other material's path
+// as it was (the walk is entered only for a positive weight).
+template <bool kVolumes, bool kSss>
 __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint32_t i, uint32_t bounce) {
     float4 ro = W.ray_o[p], rd = W.ray_d[p], tpw = W.tp[p], radw = W.rad[p], hr = W.hit[p];
     uint2 rs = W.rng[p];
@@ -724,7 +742,7 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
         continued = true;
     } else {
         float subsurface = materialSubsurface(m);
-        if (subsurface > 0.0f && randomFloat(state) < subsurface &&
+        if (kSss && subsurface > 0.0f && randomFloat(state) < subsurface &&
             continueSubsurfaceRandomWalk<kVolumes>(S, h, m, ray, tp, prevPdf, state)) {
             continued = true;
         } else if (continueTransmissiveSurface(h, m, ray, tp, prevPdf, state)) {
@@ -873,15 +891,18 @@ __device__ ShadeOut shadePath(const DevScene& S, const Wave& W, uint32_t p, uint
 #ifndef DK_SHADE_MIN_BLOCKS
 #define DK_SHADE_MIN_BLOCKS 4
 #endif
-template <bool kVolumes>
+// range 0: the whole queue; 1: the sorted queue before the subsurface bucket;
+// 2: from it on.
+template <bool kVolumes, bool kSss>
 __global__ void __launch_bounds__(128, DK_SHADE_MIN_BLOCKS) k_shade(DevScene S, Wave W, uint32_t bounce, uint32_t sel,
-                                                                  uint32_t sorted) {
+                                                                  uint32_t sorted, uint32_t range) {
     const uint32_t* q = sorted ? W.qsorted : W.q[sel];
     const uint32_t n = W.counts[sel];
+    const uint32_t begin = range == 2u ? W.counts[7] : 0u, end = range == 1u ? W.counts[7] : n;
     if (globalId() == 0) W.counts[4] = 0u;  // extend cursor of the next bounce
-    for (uint32_t i = globalId(); i < n; i += gridStride()) {
+    for (uint32_t i = begin + globalId(); i < end; i += gridStride()) {
         uint32_t p = q[i];
-        ShadeOut o = shadePath<kVolumes>(S, W, p, i, bounce);
+        ShadeOut o = shadePath<kVolumes, kSss>(S, W, p, i, bounce);
         bool keep = o.survive && bounce + 1u < o.maxBounces;
         W.live[p] = keep ? 1u : 0u;  // the next queue is built from these flags in path order
         bool sh = o.neeMask != 0u;
@@ -1632,7 +1653,7 @@ int kernelGrid(int which, int smCount) {
     switch (which) {
         case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_generate, 256, 0); break;
         case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend<false>, 128, 0); break;
-        case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade<false>, 128, 0); break;
+        case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shade<false, false>, 128, 0); break;
         case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<false>, 128, 0); break;
         case 5: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend<true>, 128, 0); break;
         case 6: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<true>, 128, 0); break;
@@ -1676,7 +1697,7 @@ uint32_t bounceLaunches(const DevScene& S) {
         g_sortMaterials = (e && e[0] == '0') ? 0 : 1;
     }
     uint32_t n = 1u + (S.volume_count ? 1u : 0u);                  // extend
-    n += 1u + (g_sortMaterials ? 3u : 0u) + 3u;                      // shade, survivor queue
+    n += 1u + (g_sortMaterials ? (S.volume_count || S.wide8 ? 3u : 4u) : 0u) + 3u;  // sort, shade, survivor queue
     n += 1u + ((!S.all_shadow_opaque || S.volume_count) ? 1u : 0u);  // shadow
     return n + 1u;                                                   // resolve
 }
@@ -1695,10 +1716,15 @@ cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint3
     // The general shading kernel (volume hits, random walks through
     // traceScene) also serves the 8-wide tree, keeping the layout switch out
     // of the triangle-only kernel.
-    if (S.volume_count || S.wide8)
-        k_shade<true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
-    else
-        k_shade<false><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted);
+    if (S.volume_count || S.wide8) {
+        k_shade<true, true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted, 0u);
+    } else if (sorted) {
+        // materials without a subsurface weight, then those with one
+        k_shade<false, false><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted, 1u);
+        k_shade<false, true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted, 2u);
+    } else {
+        k_shade<false, true><<<grid, 128, 0, st>>>(S, W, bounce, sel, sorted, 0u);
+    }
     // The survivors, in path order, are the next bounce's queue.
     const uint32_t blocks = (W.path_count + kLiveBlock - 1u) / kLiveBlock;
     if (blocks) {
