@@ -17,10 +17,13 @@ Printed JSON fields:
               next step's session is created on a second host thread while the
               current step renders (the host build overlaps the GPU's work);
               `sequential` in the same object is the one-at-a-time figure.
-  roofline    the dominant kernel's algorithmic bytes (the reference algorithm's
-              BVH-node / triangle / material / light / environment bytes, counted
-              by the CPU oracle on a 1/64 pixel subsample and scaled) over its
-              event-timed duration, against the measured HBM copy bandwidth.
+  roofline    the HBM-bound stage's (shading's) algorithmic bytes (the reference
+              algorithm's material / light / environment / path-state bytes,
+              counted by the CPU oracle on a 1/64 pixel subsample and scaled)
+              over its event-timed duration, against the measured HBM copy
+              bandwidth; `roofline.stages` adds the traversal stages (extension,
+              shadow), which run from L2: the L2 bytes they move against the L2
+              read bandwidth measured in the same process.
   cpu_baseline  the reference's own kernel (PathTrace.metal compiled for the
               host from oracle/_ref; the FP32 oracle port where that is not
               built) on all host cores, on a 1/64 pixel subsample of the frame.
@@ -423,7 +426,9 @@ def run_gb300(args, rank, world, local):
         cpu = {"value": rpaths / rdt / 1e6, "unit": METRIC, "cores": threads, "kind": rkind, "sample": rdesc,
                "oracle_port_mpaths_s": paths / dt / 1e6}
         kernel_ms = {k: stage[k] / args.steps for k in ("k_extend", "k_shade", "k_shadow")}
-        dom = max(kernel_ms, key=kernel_ms.get)
+        # The memory roofline belongs to the HBM-bound stage, shading; the
+        # traversal stages run from L2 and get the L2 roofline in `stages`.
+        dom = "k_shade"
         peak, kind = measured_peaks()
         achieved = per_frame[dom] / (kernel_ms[dom] * 1e-3) / 1e9
         traffic = profile_traffic(dom)
@@ -433,7 +438,7 @@ def run_gb300(args, rank, world, local):
                 "units": "achieved and traffic are per step (one frame, all launches of the stage); traffic = "
                          "DRAM read+write bytes scaled from a small-case ncu capture (profiles/<stage>_spheres_large.md)",
                 "algorithmic_bytes_per_step": {k: float(v) for k, v in per_frame.items()},
-                "kernel_ms_per_step": kernel_ms,
+                "kernel_ms_per_step": kernel_ms, "slowest_stage": max(kernel_ms, key=kernel_ms.get),
                 "per_path": {k: float(v) / paths for k, v in counters.items() if k != "paths"}}
         # Per stage: the traversal stages run from L2 (nodes + triangle slots,
         # 109 MB, stay resident), so their roofline is L2 bytes moved against

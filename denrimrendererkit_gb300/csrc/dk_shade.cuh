@@ -378,7 +378,7 @@ __device__ __forceinline__ float bsdfPDF(const ShadePoint& sp, float3 l) {  // :
     return sp.dP * (nDotL * 0.31830988618f) + sp.sP * specPDF + sp.cP * ccPDF;
 }
 
-__device__ __noinline__ float3 diffuseBounceWeight(const Material& m, const ShadePoint& sp, float3 l) {  // :1492-1518
+__device__ __forceinline__ float3 diffuseBounceWeight(const Material& m, const ShadePoint& sp, float3 l) {  // :1492-1518
     float3 hd = sp.v + l;
     if (dot(hd, hd) <= 1e-8f) return f3(0.0f);
     float3 h = normalize(hd);
@@ -392,7 +392,7 @@ __device__ __noinline__ float3 diffuseBounceWeight(const Material& m, const Shad
 }
 
 // sampleGGXVisibleNormal (:1620-1660) with the shading point's frame.
-__device__ __noinline__ float3 sampleVNDF(const ShadePoint& sp, float ux, float uy, float2 a) {
+__device__ __forceinline__ float3 sampleVNDF(const ShadePoint& sp, float ux, float uy, float2 a) {
     float3 lv = normalize(f3(dot(sp.v, sp.fr.tangent), dot(sp.v, sp.fr.bitangent), fmaxf(dot(sp.v, sp.n), 1e-5f)));
     float3 sv = normalize(f3(a.x * lv.x, a.y * lv.y, lv.z));
     float lensq = sv.x * sv.x + sv.y * sv.y;
@@ -525,7 +525,7 @@ __device__ __forceinline__ float environmentPDF(const DevScene& S, float3 d) {  
     return fmaxf(__ldg(&S.env[index].y), 0.0f);
 }
 // sampleEnvironmentDirection (:3937-3987) with selectEnvironmentSampleIndex (:3916-3935).
-__device__ __noinline__ float3 sampleEnvironmentDirection(const DevScene& S, float px, float py, float cdfSample, float& pdf) {
+__device__ __forceinline__ float3 sampleEnvironmentDirection(const DevScene& S, float px, float py, float cdfSample, float& pdf) {
     pdf = 0.0f;
     if (S.env_tex_plus1 == 0u || S.env_count == 0u || S.env == nullptr) return f3(0, 1, 0);
     uint4 md = __ldg(reinterpret_cast<const uint4*>(&S.texdesc[S.env_tex_plus1 - 1u]));
