@@ -563,12 +563,14 @@ def sdf_measure(args, flush, steps=3, warmup=2):
             "note": "value: FP16 distance storage (the configuration's); fp32 is the same scene with FP32 distances"}
 
 
-def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, train_steps=2500):
+def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, train_steps=2500, margin=0.9):
     """The benchmark spec's comparison at its stated error (relative RMSE of the
-    displayed image): requests (`views`
-    camera views of each of `n_scenes` held-out small-scene variants, all
-    resident in one render server) served until each image's estimated
-    relative RMSE (linear RGB, over the image mean) is at most `target`:
+    displayed image): requests (`views` camera views of each of `n_scenes`
+    held-out small-scene variants, all resident in one render server) served
+    until each image's estimated relative RMSE (of the displayed image, over
+    its mean) is at most `target` x `margin` (the estimate is statistical; the
+    returned images must meet `target` itself, which the true errors below
+    check):
 
     * denoised: two independent halves rendered per request, the residual
       U-Net over A, B and F, the reference-free estimate of dF; a request over
@@ -620,17 +622,20 @@ def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, t
                         vertical_field_of_view_degrees=cam.vertical_field_of_view_degrees)
             requests.append((wl.settings, cv, None, si))
     cfg = ServerConfig(wave_paths=1 << 24, max_jobs_per_wave=512, samples_per_wave=256)
+    # Requests are served to an estimate 10 % under the target: the estimate is
+    # statistical, and the images returned must meet the target itself.
+    serve_at = target * margin
     with RenderServer(builds[0], cfg) as srv:
         for b in builds[1:]:
             srv.add_scene(b)
-        serve_to_error_target(srv, net, requests[:4], size, size, target=target)  # warm-up
+        serve_to_error_target(srv, net, requests[:4], size, size, target=serve_at)  # warm-up
         torch.cuda.synchronize()
         t = time.perf_counter()
-        den = serve_to_error_target(srv, net, requests, size, size, target=target, start_spp=16)
+        den = serve_to_error_target(srv, net, requests, size, size, target=serve_at, start_spp=16)
         torch.cuda.synchronize()
         den_s = time.perf_counter() - t
         t = time.perf_counter()
-        plain = serve_to_error_target(srv, net, requests, size, size, target=target, start_spp=16, denoise=False)
+        plain = serve_to_error_target(srv, net, requests, size, size, target=serve_at, start_spp=16, denoise=False)
         torch.cuda.synchronize()
         plain_s = time.perf_counter() - t
     # plain, one session per request (two half sessions, doubling)
@@ -647,9 +652,9 @@ def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, t
             f = torch.empty_like(a)
             average_planes(a, b, f)
             e = estimate_errors(a, b, f, a, b, f, display=True)[0]
-            if e.plain <= target or 2 * n >= 8192:
+            if e.plain <= serve_at or 2 * n >= 8192:
                 break
-            add = min(next_sample_count(2 * n, e.plain, target, step=16), 8192) // 2 - n
+            add = min(next_sample_count(2 * n, e.plain, serve_at, step=16), 8192) // 2 - n
             for s in ss:
                 s.render(add)
             n += add
@@ -681,7 +686,7 @@ def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, t
             e = relative_rmse(res.image, ref)
             lin.append(math.sqrt(max(e * e - ref_var, 0.0)))
     n = len(requests)
-    return {"target_relative_rmse": target, "requests": n,
+    return {"target_relative_rmse": target, "served_to_estimate": serve_at, "requests": n,
             "image": f"{size}x{size} views ({views} per scene) of {n_scenes} held-out small-scene variants, "
                      "resident together in one render server",
             "images_per_s_denoised": n / den_s, "images_per_s_plain_batched": n / plain_s,
