@@ -740,6 +740,19 @@ def unet_inference_measure(reps=10):
         ms = e0.elapsed_time(e1) / reps
         out[f"path{path}"] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12}
     library.check(lib.dk_unet_set_conv_path(3))
+    # the convolutions alone: each layer of the pass timed by itself (CUDA events, 20 launches after 3)
+    conv_ms = 0.0
+    for (l, src, so, ldi, dst, do, ldo, hh, ww) in net.conv_plan(1, 1088, 1920):
+        for _ in range(3):
+            net._conv(l, src, so, ldi, dst, do, ldo, 1, hh, ww)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(20):
+            net._conv(l, src, so, ldi, dst, do, ldo, 1, hh, ww)
+        e1.record()
+        torch.cuda.synchronize()
+        conv_ms += e0.elapsed_time(e1) / 20
+    conv_tflops = flops / (conv_ms * 1e-3) / 1e12
     err = C.c_int(0)
     library.check(lib.dk_unet_error(C.byref(err)))
     best = out["path3"]
@@ -749,6 +762,9 @@ def unet_inference_measure(reps=10):
                                    "(whole forward pass)", "bound": "tensor",
                          "achieved": best["tflops"], "peak": peak, "unit": "TFLOP/s", "frac": best["tflops"] / peak,
                          "peak_source": f"{kind} (MEASURED_PEAKS.json bf16_tflops)"},
+            "convolutions": {"ms": conv_ms, "tflops": conv_tflops, "frac": conv_tflops / peak,
+                             "note": "the 19 convolutions of the pass, each layer timed by itself (the pass "
+                                     "minus its pooling and upsampling and the gaps between launches)"},
             "per_path": out, "tensor_wait_errors": int(err.value)}
 
 

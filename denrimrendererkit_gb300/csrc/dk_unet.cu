@@ -850,9 +850,88 @@ struct HaloConvArgs {
     uint32_t tilesX, totalRows, chunks, cols;  // totalRows = n x tilesX x h output rows of 128 pixels
     uint32_t ring;  // halo-row slots, kHaloRingMin..kHaloRingMax
     uint32_t slots, logSlots;  // stacked variant: accumulator slots of Cout columns (a power of two)
+    uint32_t tmaStore;         // stacked variant: output rows leave by TMA tensor stores (Cout 16, 32 or 64)
     int act, accumulate;
     int staged;  // epilogue rows through shared memory (see epilogueRow)
 };
+
+// One accumulator slot of the stacked halo kernel to global memory through a
+// TMA tensor store: this warp's 32 pixels (TMEM lanes) x all N channels are
+// staged as a box {N channels, 32 pixels} in shared memory, laid out with the
+// store map's swizzle (16-byte chunk j of pixel row r at r * 2N + 16 (j ^ f(r)),
+// f(r) the row's address bits 7.. -- XOR-swizzle over 2N-byte rows, which also
+// keeps the eight lanes of a 16-byte store on distinct banks), then one lane
+// issues the store of the box at (channel offset, pixel, row, image); pixels
+// beyond the image width are clipped by the copy engine.  `buf` alternates
+// between two boxes per warp: before writing one, the warp waits until the
+// store issued from it two rows earlier has read it.
+__device__ __forceinline__ void tmaStoreRow(uint32_t src, uint32_t N, const float* bias, int act,
+                                            unsigned char* buf, uint32_t accEmptyBar, const CUtensorMap* mapOut,
+                                            int cx, int px0, int py, int img) {
+    const uint32_t lane = threadIdx.x & 31u;
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
+    __syncwarp();
+    const uint32_t rowBytes = 2u * N;
+    const uint32_t swzMask = (rowBytes >> 4) - 1u;                          // 16-byte chunks per row - 1
+    const uint32_t f = ((lane * rowBytes) >> 7) & swzMask;                  // address bits 7.. of the row
+    const bool biasVec = bias && (reinterpret_cast<uintptr_t>(bias) & 15u) == 0u;
+    for (uint32_t c = 0; c < N; c += 16u) {
+        uint32_t rr[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+            "%12, %13, %14, %15}, [%16];\n"
+            : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
+              "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]),
+              "=r"(rr[15])
+            : "r"(src + c));
+        float bv[16];
+        if (biasVec) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float4 b4 = __ldg(reinterpret_cast<const float4*>(bias + c) + k);
+                bv[4 * k] = b4.x;
+                bv[4 * k + 1] = b4.y;
+                bv[4 * k + 2] = b4.z;
+                bv[4 * k + 3] = b4.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) bv[k] = bias ? __ldg(bias + c + k) : 0.0f;
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        uint32_t packed[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            float x0 = __uint_as_float(rr[2 * k]), x1 = __uint_as_float(rr[2 * k + 1]);
+            if (bias) {
+                x0 += bv[2 * k];
+                x1 += bv[2 * k + 1];
+            }
+            if (act == 1) {
+                x0 = fmaxf(x0, 0.0f);
+                x1 = fmaxf(x1, 0.0f);
+            }
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
+            packed[k] = *reinterpret_cast<uint32_t*>(&h2);
+        }
+        const uint32_t j = c >> 3;  // first 16-byte chunk of these 16 channels
+        unsigned char* row = buf + lane * rowBytes;
+        *reinterpret_cast<uint4*>(row + (((j) ^ f) << 4)) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        *reinterpret_cast<uint4*>(row + (((j + 1u) ^ f) << 4)) = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    }
+    zeroColumns(src, 0u, N);  // the next row in this accumulator slot starts from zero
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    mbarArrive(accEmptyBar);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the box is visible to the copy engine
+    __syncwarp();
+    if (lane == 0) {
+        asm volatile(
+            "cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];\n" ::"l"(mapOut),
+            "r"(cx), "r"(px0), "r"(py), "r"(img), "r"(smemAddr(buf))
+            : "memory");
+        asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+    }
+}
 
 // A run of output rows y0..y1-1 of tile column tx of image img.
 struct RowSegment {
@@ -882,7 +961,7 @@ __device__ __forceinline__ uint32_t rangeBegin(const HaloConvArgs& a, uint32_t c
 template <bool kStack, uint32_t kC, uint32_t kLast>
 __global__ void __launch_bounds__(320, 1)
     k_conv3x3_halo(const __grid_constant__ CUtensorMap mapIn, const __grid_constant__ CUtensorMap mapW,
-                   HaloConvArgs a) {
+                   const __grid_constant__ CUtensorMap mapOut, HaloConvArgs a) {
     extern __shared__ unsigned char dsm[];
     const uint32_t raw = smemAddr(dsm);
     unsigned char* sm = dsm + (((raw + 1023u) & ~1023u) - raw);
@@ -1150,10 +1229,27 @@ __global__ void __launch_bounds__(320, 1)
         uint32_t cur = rangeBegin(a, blockIdx.x);
         const uint32_t end = rangeBegin(a, blockIdx.x + 1u);
         RowSegment sg;
+        // Stacked with TMA stores: two boxes of 32 pixels x N channels per warp.
+        unsigned char* boxes = reinterpret_cast<unsigned char*>(bars) + kHaloBarBytes + (warp - 2u) * 128u * N;
+        uint32_t stored = 0;
         while (ok && nextSegment(a, cur, end, sg)) {
             const uint32_t img = sg.img, px = sg.tx * 128u + r;
             for (uint32_t py = sg.y0; py < sg.y1; ++py, ++t) {
                 if (kStack && (t & 1u) != set) continue;  // the other set's row
+                if (kStack && a.tmaStore) {
+                    const uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
+                    if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
+                        *abortV = 1;
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    tmaStoreRow(quarter + b * slotCols, N, a.bias, a.act, boxes + (stored & 1u) * 64u * N,
+                                accEmptyBar + 8u * b, &mapOut, (int)a.coOff, (int)(sg.tx * 128u + q * 32u), (int)py,
+                                (int)img);
+                    ++stored;
+                    continue;
+                }
                 const uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
                 if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
                     *abortV = 1;
@@ -1167,6 +1263,7 @@ __global__ void __launch_bounds__(320, 1)
                             accEmptyBar + 8u * b, kStack);
             }
         }
+        if (kStack && a.tmaStore && lane == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
     }
     __syncthreads();
     if (*abortV && tid == 0) atomicExch(&g_unetError, 3);
@@ -1174,9 +1271,10 @@ __global__ void __launch_bounds__(320, 1)
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(tmemCols));
 }
 
-size_t haloSmemBytes(uint32_t cout, uint32_t chunks, bool staged, uint32_t ring, bool stack) {
-    return 1024u + (size_t)ring * chunks * kHaloSlotBytes + 9u * (size_t)chunks * cout * 128u + kHaloBarBytes +
-           (staged ? kEpiWarps * (stack ? epiWarpBytesAll(cout) : epiWarpBytes(cout)) : 0u);
+size_t haloSmemBytes(uint32_t cout, uint32_t chunks, bool staged, uint32_t ring, bool stack, bool tmaStore = false) {
+    const size_t epi = tmaStore ? kEpiWarps * 128u * cout  // two boxes of 32 pixels x Cout per warp
+                                : (staged ? kEpiWarps * (stack ? epiWarpBytesAll(cout) : epiWarpBytes(cout)) : 0u);
+    return 1024u + (size_t)ring * chunks * kHaloSlotBytes + 9u * (size_t)chunks * cout * 128u + kHaloBarBytes + epi;
 }
 
 // -------------------------------------------------------------- wgrad ----
@@ -1785,11 +1883,17 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     if (c.w_ < 128u || c.cout > 256u || chunks > 2u || haloSmemBytes(c.cout, chunks, false, minRing, stack) > optin)
         return kHaloUnfit;
     const bool staged = stagedStores(c) && haloSmemBytes(c.cout, chunks, true, minRing, stack) <= optin;
+    // Stacked layers of 16, 32 or 64 output channels write their rows with
+    // TMA tensor stores (DK_CONV_TMA_STORE=0: through the lanes).
+    const char* storeEnv = getenv("DK_CONV_TMA_STORE");
+    const bool tmaStore = stack && staged && (c.cout == 16u || c.cout == 32u || c.cout == 64u) &&
+                          !(storeEnv && storeEnv[0] == '0') &&
+                          haloSmemBytes(c.cout, chunks, true, minRing, stack, true) <= optin;
     // The deepest ring that fits: every further slot is a row in flight.
     uint32_t ring = minRing;
     const uint32_t ringCap = depthCap("DK_CONV_HALO_RING", minRing, kHaloRingMax);
-    while (ring < ringCap && haloSmemBytes(c.cout, chunks, staged, ring + 1u, stack) <= optin) ++ring;
-    const size_t smem = haloSmemBytes(c.cout, chunks, staged, ring, stack);
+    while (ring < ringCap && haloSmemBytes(c.cout, chunks, staged, ring + 1u, stack, tmaStore) <= optin) ++ring;
+    const size_t smem = haloSmemBytes(c.cout, chunks, staged, ring, stack, tmaStore);
     EncodeTiledFn enc = encodeTiled();
     if (!enc) return fail(DK_ERROR_COMMAND_FAILED, "cuTensorMapEncodeTiled is not available");
     HaloConvArgs a;
@@ -1806,6 +1910,7 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     a.accumulate = c.accumulate;
     a.staged = staged ? 1 : 0;
     a.ring = ring;
+    a.tmaStore = tmaStore ? 1u : 0u;
     a.slots = 0u;
     a.logSlots = 0u;
     if (stack) {
@@ -1837,7 +1942,22 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "weight tensor map rejected");
-    using HaloKernel = void (*)(const CUtensorMap, const CUtensorMap, HaloConvArgs);
+    // Output rows as boxes {Cout channels, 32 pixels} of the 4-D output (channels, x, y, image) at the
+    // slice's channel offset; 2 Cout bytes per pixel row, swizzled like the staging boxes.
+    alignas(64) CUtensorMap mapOut = mapIn;
+    if (tmaStore) {
+        cuuint64_t dimOut[4] = {c.ldo, c.w_, c.h, c.n};
+        cuuint64_t strideOut[3] = {(cuuint64_t)c.ldo * 2u, (cuuint64_t)c.w_ * c.ldo * 2u,
+                                   (cuuint64_t)c.h * c.w_ * c.ldo * 2u};
+        cuuint32_t boxOut[4] = {c.cout, 32u, 1u, 1u};
+        const CUtensorMapSwizzle swz = c.cout == 16u   ? CU_TENSOR_MAP_SWIZZLE_32B
+                                       : c.cout == 32u ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                       : CU_TENSOR_MAP_SWIZZLE_128B;
+        r = enc(&mapOut, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, c.out, dimOut, strideOut, boxOut, unit,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(DK_ERROR_INVALID_ARGUMENT, "output tensor map rejected");
+    }
+    using HaloKernel = void (*)(const CUtensorMap, const CUtensorMap, const CUtensorMap, HaloConvArgs);
     const uint32_t last = (c.cin - (chunks - 1u) * 64u + 15u) / 16u;
     HaloKernel kernels[2][2][4] = {
         {{k_conv3x3_halo<false, 1, 1>, k_conv3x3_halo<false, 1, 2>, k_conv3x3_halo<false, 1, 3>,
@@ -1856,7 +1976,7 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
         configured[stack][chunks - 1u][last - 1u] = smem;
     }
     uint32_t grid = std::min(sms, a.totalRows);
-    DK_CUDA(launchPdl(kernel, dim3(grid), dim3(320), smem, st, mapIn, mapW, a), "conv3x3 (halo) launch");
+    DK_CUDA(launchPdl(kernel, dim3(grid), dim3(320), smem, st, mapIn, mapW, mapOut, a), "conv3x3 (halo) launch");
     DK_CUDA(cudaGetLastError(), "conv3x3 (halo rows, TMA + tcgen05) launch");
     return DK_OK;
 }

@@ -187,6 +187,34 @@ class UNet:
         return B
 
     # ---------------------------------------------------------- forward --
+    def conv_plan(self, n: int, h: int, w: int):
+        """The forward pass's convolutions in order, as (layer, source, source
+        channel offset, source leading dimension, destination, destination
+        offset, destination leading dimension, height, width) over buffers(n, h,
+        w): what `forward` runs between its pooling and upsampling steps, for
+        timing the convolutions alone."""
+        B = self.buffers(n, h, w)
+        c = LEVELS
+        L = self.by_name
+        cat = [B["cat0"], B["cat1"], B["cat2"], B["cat3"]]
+        catc = [c[1] + c[0], c[2] + c[1], c[3] + c[2], c[4] + c[3]]
+        upc = [c[1], c[2], c[3], c[4]]
+        firsts = [B["e0a"], B["e1a"], B["e2a"], B["e3a"]]
+        srcs = [(B["x"], IN_CH), (B["p1"], c[0]), (B["p2"], c[1]), (B["p3"], c[2])]
+        plan = []
+        for k in range(4):
+            hk, wk = h >> k, w >> k
+            plan.append((L[f"enc{k}a"], srcs[k][0], 0, srcs[k][1], firsts[k], 0, c[k], hk, wk))
+            plan.append((L[f"enc{k}b"], firsts[k], 0, c[k], cat[k], upc[k], catc[k], hk, wk))
+        plan.append((L["bota"], B["p4"], 0, c[3], B["ba"], 0, c[4], h >> 4, w >> 4))
+        plan.append((L["botb"], B["ba"], 0, c[4], B["bb"], 0, c[4], h >> 4, w >> 4))
+        for k in (3, 2, 1, 0):
+            hk, wk = h >> k, w >> k
+            plan.append((L[f"dec{k}a"], cat[k], 0, catc[k], B[f"d{k}a"], 0, c[k], hk, wk))
+            plan.append((L[f"dec{k}b"], B[f"d{k}a"], 0, c[k], B[f"d{k}b"], 0, c[k], hk, wk))
+        plan.append((L["out"], B["d0b"], 0, c[0], B["pred"], 0, OUT_CH, h, w))
+        return plan
+
     def _conv(self, l: Conv, src, src_off, ldi, dst, dst_off, ldo, n, h, w, accumulate=0):
         self._check(self.lib.dk_unet_conv3x3(_ptr(src, src_off), n, h, w, l.cin, ldi, _ptr(l.wbf), _ptr(l.b), l.cout,
                                              _ptr(dst), ldo, dst_off, l.act, accumulate, self._st))

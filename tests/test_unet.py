@@ -272,3 +272,24 @@ def test_graphed_denoiser_equals_direct_calls(lib):
         graphed.denoise(*planes, out)
     torch.cuda.synchronize()
     assert torch.equal(out, direct)
+
+
+def test_conv_plan_replays_the_forward_convolutions(lib):
+    # conv_plan lists forward's convolutions with its buffers: replayed over the
+    # buffers forward left (pooled and upsampled inputs in place), every
+    # convolution's output -- and so the prediction -- is unchanged.
+    net = UNet(seed=4)
+    n, h, w = 1, 32, 48
+    B = net.buffers(n, h, w)
+    g = torch.Generator().manual_seed(8)
+    B["x"].copy_(torch.randn(n, h, w, IN_CH, generator=g).to(torch.bfloat16).cuda())
+    net.forward(n, h, w)
+    torch.cuda.synchronize()
+    pred = B["pred"].clone()
+    plan = net.conv_plan(n, h, w)
+    assert len(plan) == len(net.layers)
+    B["pred"].zero_()
+    for (l, src, so, ldi, dst, do, ldo, hh, ww) in plan:
+        net._conv(l, src, so, ldi, dst, do, ldo, n, hh, ww)
+    torch.cuda.synchronize()
+    assert torch.equal(B["pred"], pred)
