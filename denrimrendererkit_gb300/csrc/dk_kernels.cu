@@ -1159,6 +1159,11 @@ __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
 #ifndef DK_LAYERS_MIN_BLOCKS
 #define DK_LAYERS_MIN_BLOCKS 4
 #endif
+// kVolumes: scenes with sparse volumes walk every shadow ray the reference's
+// way (shadowWalk); the others take the recorded layers, or the collecting
+// traversal when more were crossed -- two kernels, so that neither carries the
+// other's code.
+template <bool kVolumes>
 __global__ void __launch_bounds__(128, DK_LAYERS_MIN_BLOCKS) k_shadow_layers(DevScene S, Wave W) {
     const uint32_t n = W.counts[6];
     const size_t cap = W.cap;
@@ -1170,7 +1175,7 @@ __global__ void __launch_bounds__(128, DK_LAYERS_MIN_BLOCKS) k_shadow_layers(Dev
         const DevJob& J = W.jobs[__float_as_uint(d.w)];
         const MatTable mt = matTable(J);
         bool occluded;
-        if (S.volume_count) {
+        if (kVolumes) {
             occluded = shadowWalk(S, mt, xyz(o), xyz(d), o.w, T);
         } else {
             uint32_t lc = W.layer_count[slot];
@@ -1741,7 +1746,10 @@ cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_
         k_shadow_rays<true><<<grid, 128, 0, st>>>(S, W);
     else
         k_shadow_rays<false><<<grid, 128, 0, st>>>(S, W);
-    if (!S.all_shadow_opaque || S.volume_count) k_shadow_layers<<<grid, 128, 0, st>>>(S, W);
+    if (S.volume_count)
+        k_shadow_layers<true><<<grid, 128, 0, st>>>(S, W);
+    else if (!S.all_shadow_opaque)
+        k_shadow_layers<false><<<grid, 128, 0, st>>>(S, W);
     return cudaGetLastError();
 }
 cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st) {
