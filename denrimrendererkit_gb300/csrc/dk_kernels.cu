@@ -1090,7 +1090,7 @@ __device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, f
 // Distance-volume closest hit for every ray of the queue, bounded by the
 // triangle hit k_extend found (the volume half of intersectScene).
 #ifndef DK_VOLUME_MIN_BLOCKS
-#define DK_VOLUME_MIN_BLOCKS 3
+#define DK_VOLUME_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(DevScene S, Wave W, uint32_t sel) {
     const uint32_t* q = W.q[sel];
