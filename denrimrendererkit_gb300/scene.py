@@ -109,8 +109,12 @@ class Mesh:
                     texcoords=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], dtype=f32))
 
     @staticmethod
-    def box(minimum, maximum) -> "Mesh":
-        """Mesh.box(minimum:maximum:) (Mesh.swift:61-86)."""
+    def box(minimum=None, maximum=None, *, size=None) -> "Mesh":
+        """Mesh.box(minimum:maximum:) (Mesh.swift:61-86); with `size` instead,
+        Mesh.box(size:) (:52-58), the box of that size centred on the origin."""
+        if size is not None:
+            half = np.asarray(size, f32) * f32(0.5)
+            minimum, maximum = -half, half
         lo, hi = np.asarray(minimum, f32), np.asarray(maximum, f32)
         v = np.array([[lo[0], lo[1], lo[2]], [hi[0], lo[1], lo[2]], [hi[0], hi[1], lo[2]], [lo[0], hi[1], lo[2]],
                       [lo[0], lo[1], hi[2]], [hi[0], lo[1], hi[2]], [hi[0], hi[1], hi[2]], [lo[0], hi[1], hi[2]]], f32)
@@ -364,6 +368,22 @@ class Camera:
         cam.vertical = abi.Float4(*(float(c) for c in vertical), 0.0)
         cam.lens = abi.Float4(max(self.aperture_radius, 0.0), max(self.focus_distance, 0.0001), 0.0, 0.0)
         return cam
+
+    def view_direction(self) -> tuple:
+        """Camera.viewDirection (Camera.swift:80-87): the normalised origin -> target
+        vector, (0, 0, -1) when the two points coincide."""
+        o = tuple(f32(c) for c in self.origin)
+        vd = tuple(f32(c) - o[i] for i, c in enumerate(self.target))
+        return _normalize3(vd) if float(_dot3(vd, vd)) > 1e-8 else (f32(0), f32(0), f32(-1))
+
+    def focused(self, point: Sequence[float], aperture_radius: float) -> "Camera":
+        """Camera.focused(on:apertureRadius:) (Camera.swift:89-101): a copy whose focal
+        plane passes through `point` (its distance along the view direction, at
+        least 0.0001) with the given aperture radius (at least 0)."""
+        o = tuple(f32(c) for c in self.origin)
+        rel = tuple(f32(c) - o[i] for i, c in enumerate(point))
+        distance = max(float(_dot3(rel, self.view_direction())), 0.0001)
+        return dataclasses.replace(self, focus_distance=distance, aperture_radius=max(float(aperture_radius), 0.0))
 
 
 # ------------------------------------------------------------ render scene ---

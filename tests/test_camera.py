@@ -2,10 +2,11 @@
 `Camera.gpu_camera` against a vectorised numpy float32 restatement of the same
 operations, bit for bit, over seeded random cameras (perspective and
 orthographic, up vectors parallel to the view direction, degenerate up and
-view vectors)."""
+view vectors), and the reference's own camera known answers (APITests.swift:23-76)."""
 import math
 
 import numpy as np
+import pytest
 
 from denrimrendererkit_gb300.scene import Camera
 
@@ -67,3 +68,39 @@ def test_scalar_camera_basis_equals_vectorised_restatement():
         o, ll, hz, vt = reference_basis(c, w, h)
         for a, b in ((got.origin, o), (got.lower_left, ll), (got.horizontal, hz), (got.vertical, vt)):
             assert as_array(a).view(np.uint32).tolist() == b.view(np.uint32).tolist(), c
+
+
+def _length(v):
+    return math.sqrt(v.x * v.x + v.y * v.y + v.z * v.z)
+
+
+def test_perspective_camera_known_answer():
+    # APITests.testPerspectiveCameraGeneratesPerspectiveGPUCamera (APITests.swift:23-37)
+    gpu = Camera((0, 0, 3), (0, 0, 0), vertical_field_of_view_degrees=90).gpu_camera(200, 100)
+    assert abs(gpu.origin.w - 0) < 1e-4 and abs(gpu.origin.z - 3) < 1e-4
+    assert abs(gpu.lower_left.z - 2) < 1e-4
+    assert abs(_length(gpu.horizontal) - 4) < 1e-4 and abs(_length(gpu.vertical) - 2) < 1e-4
+
+
+def test_orthographic_camera_known_answer():
+    # APITests.testOrthographicCameraGeneratesOrthographicGPUCamera (APITests.swift:39-55)
+    gpu = Camera((0, 0, 3), (0, 0, 2), orthographic_scale=6).gpu_camera(200, 100)
+    assert abs(gpu.origin.w - 1) < 1e-4 and abs(gpu.origin.z - 3) < 1e-4
+    assert abs(gpu.lower_left.x + 6) < 1e-4 and abs(gpu.lower_left.y + 3) < 1e-4 and abs(gpu.lower_left.z - 3) < 1e-4
+    assert abs(_length(gpu.horizontal) - 12) < 1e-4 and abs(_length(gpu.vertical) - 6) < 1e-4
+
+
+def test_camera_lens_known_answer():
+    # APITests.testCameraLensReachesGPUCamera (APITests.swift:57-67)
+    gpu = Camera((0, 0, 3), (0, 0, 0), focus_distance=4.5, aperture_radius=0.08).gpu_camera(200, 100)
+    assert abs(gpu.lens.x - 0.08) < 1e-4 and abs(gpu.lens.y - 4.5) < 1e-4
+
+
+def test_camera_focused_on_point_known_answer():
+    # APITests.testCameraFocusedOnPointSetsFocusDistance (APITests.swift:69-76)
+    cam = Camera((0, 0, 5), (0, 0, 0)).focused((0, 0, 1), aperture_radius=0.12)
+    assert abs(cam.focus_distance - 4) < 1e-4 and abs(cam.aperture_radius - 0.12) < 1e-4
+    # behind the camera: the focal distance clamps at 0.0001; a coincident target looks down -z
+    assert Camera((0, 0, 5), (0, 0, 0)).focused((0, 0, 9), 0.1).focus_distance == 0.0001
+    assert Camera((1, 2, 3), (1, 2, 3)).focused((1, 2, 1), -1.0).focus_distance == pytest.approx(2.0)
+    assert Camera((1, 2, 3), (1, 2, 3)).focused((1, 2, 1), -1.0).aperture_radius == 0.0
