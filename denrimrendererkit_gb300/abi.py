@@ -172,7 +172,8 @@ EXPORTED_SYMBOLS = (
     "dk_server_wait", "dk_server_job_status", "dk_server_read_output", "dk_server_copy_output", "dk_server_copy_outputs", "dk_server_release",
     "dk_server_get_stats", "dk_server_destroy", "dk_denoise_spatial", "dk_denoise_error_terms", "dk_average_planes", "dk_svgf_create", "dk_svgf_reset",
     "dk_svgf_denoise", "dk_svgf_read_state", "dk_svgf_destroy", "dk_svgf_pack_depth_normal", "dk_svgf_copy_output",
-    "dk_unet_conv3x3", "dk_unet_conv3x3_wgrad", "dk_unet_relu_backward", "dk_unet_bias_grad", "dk_unet_avgpool2",
+    "dk_unet_conv3x3", "dk_unet_conv3x3_avgpool2", "dk_unet_conv3x3_wgrad", "dk_unet_relu_backward", "dk_unet_bias_grad",
+    "dk_unet_avgpool2",
     "dk_unet_avgpool2_backward", "dk_unet_upsample2", "dk_unet_upsample2_backward", "dk_unet_copy_channels",
     "dk_unet_pack_input", "dk_unet_l1_loss", "dk_unet_unpack_output", "dk_unet_l1_loss_residual",
     "dk_unet_unpack_output_residual", "dk_unet_adam", "dk_unet_weights_to_bf16",

@@ -853,6 +853,10 @@ struct HaloConvArgs {
     uint32_t tmaStore;         // stacked variant: output rows leave by TMA tensor stores (Cout 16, 32 or 64)
     int act, accumulate;
     int staged;  // epilogue rows through shared memory (see epilogueRow)
+    // With tensor-store rows: the 2x2 average of the output (h, w even) is also
+    // written here, [n][h / 2][w / 2][poolLd] (channels 0 .. Cout), or null.
+    __nv_bfloat16* pool;
+    uint32_t poolLd;
 };
 
 // One accumulator slot of the stacked halo kernel to global memory through a
@@ -933,6 +937,45 @@ __device__ __forceinline__ void tmaStoreRow(uint32_t src, uint32_t N, const floa
     }
 }
 
+// The 2x2 average of the two rows a warp has just staged for tensor stores
+// (`top`: row 2i, `bottom`: row 2i + 1; 32 pixels x N channels each, laid out
+// as in tmaStoreRow): lane l takes pooled pixel l / 2 and half of its
+// channels and writes them to `dst` (that pooled pixel's first channel, or
+// null past the image's right edge).  The staged values are the output's
+// bf16 bits, and the sum ((top-left + top-right) + bottom-left) +
+// bottom-right, times 0.25, is the pooling kernel's own, so the result is the
+// one a separate pooling pass over the stored output gives.  The boxes were
+// written before the warp's last __syncwarp in tmaStoreRow; they are next
+// overwritten after the next one.
+__device__ __forceinline__ void poolPairRow(const unsigned char* top, const unsigned char* bottom, uint32_t N,
+                                            __nv_bfloat16* dst) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t rowBytes = 2u * N, swzMask = (rowBytes >> 4) - 1u;
+    const uint32_t left = lane & ~1u, right = left + 1u;
+    const uint32_t fl = ((left * rowBytes) >> 7) & swzMask, fr = ((right * rowBytes) >> 7) & swzMask;
+    const uint32_t per = N >> 4;  // 16-byte chunks (8 channels) per lane
+    const uint32_t j0 = (lane & 1u) * per;
+    for (uint32_t j = j0; j < j0 + per; ++j) {
+        const uint4 tl = *reinterpret_cast<const uint4*>(top + left * rowBytes + ((j ^ fl) << 4));
+        const uint4 tr = *reinterpret_cast<const uint4*>(top + right * rowBytes + ((j ^ fr) << 4));
+        const uint4 bl = *reinterpret_cast<const uint4*>(bottom + left * rowBytes + ((j ^ fl) << 4));
+        const uint4 br = *reinterpret_cast<const uint4*>(bottom + right * rowBytes + ((j ^ fr) << 4));
+        const uint32_t a[4] = {tl.x, tl.y, tl.z, tl.w}, b[4] = {tr.x, tr.y, tr.z, tr.w};
+        const uint32_t c[4] = {bl.x, bl.y, bl.z, bl.w}, d[4] = {br.x, br.y, br.z, br.w};
+        uint32_t o[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float2 s = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&a[k]));
+            const float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&b[k]));
+            const float2 u = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&c[k]));
+            const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&d[k]));
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(0.25f * (s.x + t.x + u.x + v.x), 0.25f * (s.y + t.y + u.y + v.y));
+            o[k] = *reinterpret_cast<uint32_t*>(&h2);
+        }
+        if (dst) *reinterpret_cast<uint4*>(dst + 8u * j) = make_uint4(o[0], o[1], o[2], o[3]);
+    }
+}
+
 // A run of output rows y0..y1-1 of tile column tx of image img.
 struct RowSegment {
     uint32_t img, tx, y0, y1;
@@ -949,7 +992,10 @@ __device__ __forceinline__ bool nextSegment(const HaloConvArgs& a, uint32_t& cur
     cur += sg.y1 - sg.y0;
     return true;
 }
+// With pooling (h even), ranges hold whole row pairs, so that rows 2i and
+// 2i + 1 of a tile column reach the same epilogue set one after the other.
 __device__ __forceinline__ uint32_t rangeBegin(const HaloConvArgs& a, uint32_t cta) {
+    if (a.pool) return 2u * (uint32_t)((uint64_t)cta * (a.totalRows >> 1) / gridDim.x);
     return (uint32_t)((uint64_t)cta * a.totalRows / gridDim.x);
 }
 
@@ -1207,8 +1253,9 @@ __global__ void __launch_bounds__(320, 1)
         // Epilogue warps 2..9: TMEM lane quarter warp % 4 (one output pixel per
         // thread); set (warp - 2) / 4.  Stacked: set s takes every channel of
         // the rows of parity s (and owns the accumulator slots of that parity:
-        // the slot count is even), two rows in flight; otherwise both sets take
-        // every row, each half of the channels.
+        // the slot count is even), two rows in flight -- with pooling, of the
+        // row pairs of parity s (slot count a multiple of 4); otherwise both
+        // sets take every row, each half of the channels.
         const uint32_t q = warp & 3u, set = (warp - 2u) >> 2;
         const uint32_t r = q * 32u + lane;
         const uint32_t cw = epiCols(N);
@@ -1220,11 +1267,14 @@ __global__ void __launch_bounds__(320, 1)
         bool ok = c1 > c0;
         const uint32_t quarter = taddr + ((q * 32u) << 16);
         const uint32_t slotCols = kStack ? N : a.cols;
+        const uint32_t pairShift = a.pool ? 1u : 0u;  // rows (or row pairs) alternate between the sets
         if (kStack) {
             // Every slot starts zeroed; its first release lets the MMA warp in.
-            for (uint32_t b = set; b < nbuf; b += 2u) zeroColumns(quarter + b * slotCols, c0, c1);
+            for (uint32_t b = 0; b < nbuf; ++b)
+                if (((b >> pairShift) & 1u) == set) zeroColumns(quarter + b * slotCols, c0, c1);
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            for (uint32_t b = set; b < nbuf; b += 2u) mbarArrive(accEmptyBar + 8u * b);
+            for (uint32_t b = 0; b < nbuf; ++b)
+                if (((b >> pairShift) & 1u) == set) mbarArrive(accEmptyBar + 8u * b);
         }
         uint32_t cur = rangeBegin(a, blockIdx.x);
         const uint32_t end = rangeBegin(a, blockIdx.x + 1u);
@@ -1235,7 +1285,7 @@ __global__ void __launch_bounds__(320, 1)
         while (ok && nextSegment(a, cur, end, sg)) {
             const uint32_t img = sg.img, px = sg.tx * 128u + r;
             for (uint32_t py = sg.y0; py < sg.y1; ++py, ++t) {
-                if (kStack && (t & 1u) != set) continue;  // the other set's row
+                if (kStack && ((t >> pairShift) & 1u) != set) continue;  // the other set's row
                 if (kStack && a.tmaStore) {
                     const uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
                     if (!mbarWait(accFullBar + 8u * b, v & 1u)) {
@@ -1244,10 +1294,18 @@ __global__ void __launch_bounds__(320, 1)
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    tmaStoreRow(quarter + b * slotCols, N, a.bias, a.act, boxes + (stored & 1u) * 64u * N,
-                                accEmptyBar + 8u * b, &mapOut, (int)a.coOff, (int)(sg.tx * 128u + q * 32u), (int)py,
-                                (int)img);
+                    const uint32_t box = stored & 1u;
+                    tmaStoreRow(quarter + b * slotCols, N, a.bias, a.act, boxes + box * 64u * N, accEmptyBar + 8u * b,
+                                &mapOut, (int)a.coOff, (int)(sg.tx * 128u + q * 32u), (int)py, (int)img);
                     ++stored;
+                    if (a.pool && (py & 1u)) {  // rows py - 1 and py are in this warp's two boxes
+                        const uint32_t left = sg.tx * 128u + q * 32u + (lane & ~1u);
+                        __nv_bfloat16* dst =
+                            left < a.w ? a.pool + ((size_t)(img * (a.h >> 1) + (py >> 1)) * (a.w >> 1) + (left >> 1)) *
+                                                      a.poolLd
+                                       : nullptr;
+                        poolPairRow(boxes + (box ^ 1u) * 64u * N, boxes + box * 64u * N, N, dst);
+                    }
                     continue;
                 }
                 const uint32_t b = t & (nbuf - 1u), v = t >> bufShift;
@@ -1870,7 +1928,12 @@ bool stagedStores(const ConvArgs& c) {
 // layer does not fit it: narrow images, or weights and halo ring beyond the
 // shared memory of one CTA.
 constexpr int kHaloUnfit = -1;
-int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
+// `pool` (optional): where the 2x2 average of the output goes ([n][h / 2][w / 2]
+// [poolLd]); *pooled says whether this launch writes it (tensor-store rows
+// only), else the caller pools separately.
+int launchConvHalo(const ConvArgs& c, cudaStream_t st, __nv_bfloat16* pool = nullptr, uint32_t poolLd = 0,
+                   bool* pooled = nullptr) {
+    if (pooled) *pooled = false;
     const uint32_t chunks = (c.cin + 63u) / 64u;
     const size_t optin = (size_t)deviceProp().sharedMemPerBlockOptin;
     // Vertical taps stacked into one MMA (N = 3 Cout <= 256) with a rolling
@@ -1918,6 +1981,14 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
         while (a.slots * 2u * c.cout <= 512u && a.slots * 2u <= kHaloAccMax) a.slots *= 2u;
         while ((1u << a.logSlots) < a.slots) ++a.logSlots;
     }
+    // The pooled epilogue (DK_CONV_POOL=0: a separate pass): tensor-store rows,
+    // slots in pairs of pairs, whole 2x2 windows, 16-byte pooled stores.
+    const char* poolEnv = getenv("DK_CONV_POOL");
+    const bool fusePool = pool && tmaStore && a.slots >= 4u && c.h % 2u == 0u && c.w_ % 2u == 0u && !c.accumulate &&
+                          poolLd >= c.cout && poolLd % 8u == 0u && (reinterpret_cast<uintptr_t>(pool) & 15u) == 0u &&
+                          !(poolEnv && poolEnv[0] == '0');
+    a.pool = fusePool ? pool : nullptr;
+    a.poolLd = fusePool ? poolLd : 0u;
     a.chunks = chunks;
     a.cols = 32u;
     while (a.cols < c.cout) a.cols <<= 1;
@@ -1978,6 +2049,7 @@ int launchConvHalo(const ConvArgs& c, cudaStream_t st) {
     uint32_t grid = std::min(sms, a.totalRows);
     DK_CUDA(launchPdl(kernel, dim3(grid), dim3(320), smem, st, mapIn, mapW, mapOut, a), "conv3x3 (halo) launch");
     DK_CUDA(cudaGetLastError(), "conv3x3 (halo rows, TMA + tcgen05) launch");
+    if (pooled) *pooled = fusePool;
     return DK_OK;
 }
 
@@ -2183,6 +2255,28 @@ int dk_unet_avgpool2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint
         static_cast<const bf16*>(in), ldi, static_cast<bf16*>(out), ldo, coOff, c, n, h, w);
     DK_CUDA(cudaGetLastError(), "avgpool launch");
     return DK_OK;
+}
+
+int dk_unet_conv3x3_avgpool2(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, uint32_t ldi,
+                             const void* weight, const float* bias, uint32_t cout, void* out, uint32_t ldo,
+                             uint32_t coOff, int act, void* pool, uint32_t poolLd, void* stream) {
+    if (!pool || h % 2u || w % 2u || poolLd < cout)
+        return dk::fail(DK_ERROR_INVALID_ARGUMENT, "dk_unet_conv3x3_avgpool2: pool target or odd extent");
+    if (dk::g_convPath == 3 && cout <= 256u && in && weight && out && dk::aligned16(cin) && dk::aligned16(cout) &&
+        ldi >= cin && ldo >= coOff + cout && ldi % 8u == 0u && ldo % 2u == 0u && coOff % 2u == 0u &&
+        (uint64_t)n * h * w > 0 && (uint64_t)n * h * w < (1ull << 31)) {
+        dk::ConvArgs a{static_cast<const bf16*>(in), static_cast<const bf16*>(weight), bias, static_cast<bf16*>(out),
+                       n, h, w, cin, ldi, cout, ldo, coOff, (uint32_t)((uint64_t)n * h * w), act, 0};
+        bool pooled = false;
+        int rc = dk::launchConvHalo(a, static_cast<cudaStream_t>(stream), static_cast<bf16*>(pool), poolLd, &pooled);
+        if (rc != dk::kHaloUnfit) {
+            if (rc != DK_OK || pooled) return rc;
+            return dk_unet_avgpool2(static_cast<const bf16*>(out) + coOff, ldo, pool, poolLd, 0u, cout, n, h, w, stream);
+        }
+    }
+    int rc = dk_unet_conv3x3(in, n, h, w, cin, ldi, weight, bias, cout, out, ldo, coOff, act, 0, stream);
+    if (rc != DK_OK) return rc;
+    return dk_unet_avgpool2(static_cast<const bf16*>(out) + coOff, ldo, pool, poolLd, 0u, cout, n, h, w, stream);
 }
 
 int dk_unet_avgpool2_backward(const void* dout, uint32_t ldd, void* din, uint32_t ldi, uint32_t c, uint32_t n,

@@ -237,9 +237,10 @@ class UNet:
         for k in range(4):
             la, lb = L[f"enc{k}a"], L[f"enc{k}b"]
             self._conv(la, src, 0, src_ld, firsts[k], 0, c[k], n, hs[k], ws[k])
-            self._conv(lb, firsts[k], 0, c[k], cat[k], upc[k], catc[k], n, hs[k], ws[k])
-            self._check(lib.dk_unet_avgpool2(_ptr(cat[k], upc[k]), catc[k], _ptr(pools[k + 1]), c[k], 0, c[k], n,
-                                             hs[k], ws[k], st))
+            # the second convolution and the 2x2 average of its output (fused where its rows leave by TMA stores)
+            self._check(lib.dk_unet_conv3x3_avgpool2(_ptr(firsts[k]), n, hs[k], ws[k], lb.cin, c[k], _ptr(lb.wbf),
+                                                     _ptr(lb.b), lb.cout, _ptr(cat[k]), catc[k], upc[k], lb.act,
+                                                     _ptr(pools[k + 1]), c[k], st))
             src, src_ld = pools[k + 1], c[k]
         # bottleneck
         self._conv(L["bota"], B["p4"], 0, c[3], B["ba"], 0, c[4], n, hs[4], ws[4])

@@ -104,6 +104,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_svgf_pack_depth_normal": (i32, [P, P, P, u32, u32, P]),
             "dk_svgf_copy_output": (i32, [P, P, P, u32, u32, P]),
             "dk_unet_conv3x3": (i32, [P, u32, u32, u32, u32, u32, P, P, u32, P, u32, u32, i32, i32, P]),
+            "dk_unet_conv3x3_avgpool2": (i32, [P, u32, u32, u32, u32, u32, P, P, u32, P, u32, u32, i32, P, u32, P]),
             "dk_unet_conv3x3_wgrad": (i32, [P, u32, P, u32, u32, u32, u32, u32, u32, P, P]),
             "dk_unet_relu_backward": (i32, [P, u32, P, u32, P, u32, u32, u32, P]),
             "dk_unet_bias_grad": (i32, [P, u32, u32, u32, P, P]),

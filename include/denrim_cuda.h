@@ -540,6 +540,15 @@ int dk_unet_relu_backward(const void* out, uint32_t ldo, const void* dout, uint3
                           uint32_t c, uint32_t pixels, void* stream);
 /* dbias[c] += sum_p dpre[p][c] (c <= 256). */
 int dk_unet_bias_grad(const void* dpre, uint32_t ld, uint32_t c, uint32_t pixels, float* dbias, void* stream);
+/* dk_unet_conv3x3 (no accumulation) followed by dk_unet_avgpool2 of the
+ * channels it wrote: pool[q][c] (channel stride pool_ld, offset 0) = the 2x2
+ * average of out's channels co_off .. co_off + cout; h and w even.  The same
+ * bits as the two calls; where the convolution's rows leave by tensor stores
+ * (16, 32 or 64 output channels, at most 128 input channels, w >= 128) its
+ * epilogue averages the row pairs it has staged, so the output is not read back. */
+int dk_unet_conv3x3_avgpool2(const void* in, uint32_t n, uint32_t h, uint32_t w, uint32_t cin, uint32_t ldi,
+                             const void* weight, const float* bias, uint32_t cout, void* out, uint32_t ldo,
+                             uint32_t co_off, int act, void* pool, uint32_t pool_ld, void* stream);
 /* 2x2 average pooling of an (h, w) tensor, and its gradient. */
 int dk_unet_avgpool2(const void* in, uint32_t ldi, void* out, uint32_t ldo, uint32_t co_off, uint32_t c, uint32_t n,
                      uint32_t h, uint32_t w, void* stream);

@@ -132,6 +132,53 @@ def test_conv3x3_forward_tall(lib, cin, cout):
     assert rel_rms(out.cpu().float(), ref) <= 1e-2
 
 
+@pytest.mark.parametrize("cin,cout,ldo_extra,co_off,n,h,w", [
+    (32, 32, 64, 64, 3, 200, 136),   # the first level's second convolution: 32 of 96 channels at offset 64
+    (32, 32, 0, 0, 3, 1000, 136),    # ~40 rows per CTA: rings and accumulator windows wrap
+    (64, 64, 96, 96, 2, 34, 130),    # the second level's, ragged right tile, row pairs across images
+    (16, 32, 0, 0, 1, 16, 128),      # fewer row pairs than CTAs: CTAs with empty ranges
+    (48, 16, 16, 0, 2, 64, 256),
+    (96, 96, 0, 0, 1, 32, 160),      # not a tensor-store layer: convolution and pooling run separately
+    (32, 32, 0, 0, 2, 8, 48),        # narrower than one 128-pixel tile: the per-tap kernel
+])
+def test_conv3x3_avgpool2_equals_its_two_steps(lib, cin, cout, ldo_extra, co_off, n, h, w):
+    # The fused call writes the convolution's output and the 2x2 average of it;
+    # the average must be the pooling kernel's over that output bit for bit,
+    # channels outside the slices stay untouched, and the output matches the
+    # plain convolution call and FP32.
+    g = torch.Generator().manual_seed(cin + 5 * cout + h)
+    x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) / (3 * cin ** 0.5)).to(torch.bfloat16)
+    b = torch.randn(cout, generator=g) * 0.1
+    ref = torch.relu(torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), to_torch_weight(wt.float()), b,
+                                                padding=1)).permute(0, 2, 3, 1)
+    xd, wd, bd = x.cuda(), wt.cuda(), b.cuda()
+    ldo, pld = cout + ldo_extra, cout + 16
+    out = torch.full((n, h, w, ldo), 3.0, dtype=torch.bfloat16, device="cuda")
+    pool = torch.full((n, h // 2, w // 2, pld), 7.0, dtype=torch.bfloat16, device="cuda")
+    library.check(lib.dk_unet_conv3x3_avgpool2(_ptr(xd), n, h, w, cin, cin, _ptr(wd), _ptr(bd), cout, _ptr(out), ldo,
+                                               co_off, 1, _ptr(pool), pld, None))
+    plain = torch.zeros(n, h, w, cout, dtype=torch.bfloat16, device="cuda")
+    library.check(lib.dk_unet_conv3x3(_ptr(xd), n, h, w, cin, cin, _ptr(wd), _ptr(bd), cout, _ptr(plain), cout, 0, 1,
+                                      0, None))
+    check = torch.zeros(n, h // 2, w // 2, cout, dtype=torch.bfloat16, device="cuda")
+    library.check(lib.dk_unet_avgpool2(_ptr(out, co_off), ldo, _ptr(check), cout, 0, cout, n, h, w, None))
+    torch.cuda.synchronize()
+    got = out[..., co_off:co_off + cout].cpu()
+    assert torch.equal(pool[..., :cout].cpu(), check.cpu())
+    assert bool((pool[..., cout:] == 7.0).all()) and bool((out[..., :co_off] == 3.0).all())
+    assert bool((out[..., co_off + cout:] == 3.0).all())
+    assert rel_rms(got.float(), plain.cpu().float()) <= 1e-3
+    assert rel_rms(got.float(), ref) <= 1e-2
+
+
+def test_conv3x3_avgpool2_rejects_odd_extents(lib):
+    t = torch.zeros(64, dtype=torch.bfloat16, device="cuda")
+    with pytest.raises(RuntimeError):
+        library.check(lib.dk_unet_conv3x3_avgpool2(_ptr(t), 1, 3, 4, 16, 16, _ptr(t), None, 16, _ptr(t), 16, 0, 1,
+                                                   _ptr(t), 16, None))
+
+
 @pytest.mark.parametrize("cin,cout", [(16, 32), (64, 96), (160, 128), (96, 16)])
 def test_conv3x3_input_and_weight_gradients(lib, cin, cout):
     g = torch.Generator().manual_seed(cin + 3 * cout)
