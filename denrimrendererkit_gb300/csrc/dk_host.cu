@@ -236,7 +236,7 @@ int kernelGrid(int which, int smCount);
 Grids kernelGrids() {
     int sm = g_prop.multiProcessorCount;
     return Grids{kernelGrid(0, sm), kernelGrid(1, sm), kernelGrid(2, sm), kernelGrid(3, sm), kernelGrid(4, sm),
-                 kernelGrid(5, sm), kernelGrid(6, sm)};
+                 kernelGrid(5, sm), kernelGrid(6, sm), kernelGrid(7, sm)};
 }
 
 bool materialBlocksShadow(const dk_material& m) {
@@ -567,7 +567,7 @@ int allocWave(Arena& arena, Wave& W, uint64_t capPaths, uint32_t pixelCap, uint3
     TRY(arena.alloc(&W.qs, cap, "shadow queue"));
     TRY(arena.alloc(&W.qr, 3 * cap, "shadow ray queue"));
     TRY(arena.alloc(&W.qr2, 3 * cap, "layer-walk queue"));
-    TRY(arena.alloc(&W.counts, 8, "queue counters"));
+    TRY(arena.alloc(&W.counts, 16, "queue counters"));
     TRY(arena.alloc(&W.aov, 4 * (size_t)pixelCap, "AOV records"));
     TRY(arena.alloc(&W.layer_hits, 3 * cap * kRecLayers, "recorded shadow layers"));
     TRY(arena.alloc(&W.layer_count, 3 * cap, "recorded shadow layer counts"));
@@ -635,7 +635,7 @@ int launchWave(const DevScene& S, const Wave& W, uint32_t maxBounces, bool anyDe
     for (uint32_t b = 0; b < maxBounces; ++b) {
         uint32_t sel = b & 1u;
         MARK(1);
-        DK_CUDA(launchExtend(S, W, sel, S.wide8 ? g.extend8 : g.extend, q), "extend launch");
+        DK_CUDA(launchExtend(S, W, sel, S.wide8 ? g.extend8 : g.extend, g.volume, q), "extend launch");
         MARK(2);
         DK_CUDA(launchShade(S, W, b, sel, g.shade, q), "shade launch");
         MARK(3);

@@ -96,6 +96,7 @@ void fillParams(DevParams& P, const dk_settings& st);
 struct Grids {
     int gen, extend, shade, shadow, final;
     int extend8, shadow8;  // the traversal kernels over the 8-wide tree
+    int volume;            // the distance-volume pass (persistent: its resident blocks)
 };
 Grids kernelGrids();
 

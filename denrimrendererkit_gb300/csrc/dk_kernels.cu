@@ -440,6 +440,7 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel
         W.counts[5] = 0u;
         W.counts[6] = 0u;
         W.counts[7] = 0u;
+        W.counts[8] = 0u;
     }
     // The stacks stay separate objects from the scalar state, so that only
     // they live in local memory.
@@ -1092,17 +1093,53 @@ __device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, f
 #ifndef DK_VOLUME_MIN_BLOCKS
 #define DK_VOLUME_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(DevScene S, Wave W, uint32_t sel) {
+// Scenes with one sparse volume (the common case) run it as persistent threads
+// with per-lane refill: the volume's grid constants are read once per thread,
+// each lane advances its ray `budget` grid cells at a time and takes the next
+// ray of the queue when its walk is over.  W.counts[8] is the work cursor
+// (zeroed by k_extend).  Measured on the sparse-SDF configuration: budgets of
+// 2 / 8 / 32 cells 417 / 570 / 672 Mpaths/s, 64 to 1024 cells 697-698 (a step
+// then almost always ends the walk: the per-step ballots cost more than the
+// shorter waits for a warp's longest walk save), one ray per thread over the
+// general path 493.  Scenes with several volumes, or budget 0
+// (DK_VOLUME_REFILL=0), take one ray per thread and walk the volumes in turn.
+__global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(DevScene S, Wave W, uint32_t sel,
+                                                                           uint32_t budget) {
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
     VolumeScene V = volumeScene(S);
-    for (uint32_t i = globalId(); i < n; i += gridStride()) {
-        uint32_t p = q[i];
-        float4 o = W.ray_o[p], d = W.ray_d[p];
-        float4 h = W.hit[p];
-        VolumeHitRec vh;
-        if (closestVolumeHit(V, xyz(o), xyz(d), h.x, vh))
-            W.hit[p] = make_float4(vh.t, __uint_as_float(kVolumeHit), __uint_as_float(vh.brick), 0.0f);
+    DDAGrid g;
+    const bool single = budget && V.volumeCount == 1u && V.gridCount != 0u && V.gridIndexCount != 0u &&
+                        V.volumes[0].metadata.w == 1u && ddaGrid(V, 0u, g);
+    if (!single) {
+        for (uint32_t i = globalId(); i < n; i += gridStride()) {
+            uint32_t p = q[i];
+            float4 o = W.ray_o[p], d = W.ray_d[p];
+            float4 h = W.hit[p];
+            VolumeHitRec vh;
+            if (closestVolumeHit(V, xyz(o), xyz(d), h.x, vh))
+                W.hit[p] = make_float4(vh.t, __uint_as_float(kVolumeHit), __uint_as_float(vh.brick), 0.0f);
+        }
+        return;
+    }
+    DDAState st;
+    float closestT = 0.0f;
+    uint32_t p = kNoWork;
+    bool exhausted = false;
+    for (;;) {
+        uint32_t idx = warpFetch(&W.counts[8], n, p == kNoWork && !exhausted, exhausted);
+        if (idx != kNoWork) {
+            p = q[idx];
+            float4 o = W.ray_o[p], d = W.ray_d[p];
+            closestT = W.hit[p].x;
+            if (!ddaBegin(g, xyz(o), xyz(d), closestT, st)) p = kNoWork;  // misses the volume's bounds
+        }
+        if (__all_sync(0xffffffffu, p == kNoWork && exhausted)) break;
+        if (p != kNoWork && ddaSteps(V, g, st, (int)budget)) {
+            if (st.found && st.out.t < closestT)
+                W.hit[p] = make_float4(st.out.t, __uint_as_float(kVolumeHit), __uint_as_float(st.out.brick), 0.0f);
+            p = kNoWork;
+        }
     }
 }
 
@@ -1662,6 +1699,7 @@ int kernelGrid(int which, int smCount) {
         case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<false>, 128, 0); break;
         case 5: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend<true>, 128, 0); break;
         case 6: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<true>, 128, 0); break;
+        case 7: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend_volume, 128, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_finalize, 256, 0); break;
     }
     return (perSM < 1 ? 1 : perSM) * smCount;
@@ -1671,12 +1709,20 @@ cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStrea
     k_generate<<<grid, 256, 0, st>>>(S, W);
     return cudaGetLastError();
 }
-cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st) {
+cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, int volumeGrid, cudaStream_t st) {
     if (S.wide8)
         k_extend<true><<<grid, 128, 0, st>>>(S, W, sel);
     else
         k_extend<false><<<grid, 128, 0, st>>>(S, W, sel);
-    if (S.volume_count) k_extend_volume<<<grid, 128, 0, st>>>(S, W, sel);
+    if (S.volume_count) {
+        // grid cells per refill step (DK_VOLUME_BUDGET, default 256); DK_VOLUME_REFILL=0: one ray per thread
+        const char* refill = getenv("DK_VOLUME_REFILL");
+        const char* env = getenv("DK_VOLUME_BUDGET");
+        uint32_t budget = env ? (uint32_t)strtoul(env, nullptr, 10) : 256u;
+        budget = budget < 1u ? 1u : (budget > 1024u ? 1024u : budget);
+        if (refill && refill[0] == '0') budget = 0u;
+        k_extend_volume<<<volumeGrid, 128, 0, st>>>(S, W, sel, budget);
+    }
     return cudaGetLastError();
 }
 // The environment rotation's sine and cosine with the device's sincosf, the

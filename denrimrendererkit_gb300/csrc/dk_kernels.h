@@ -148,7 +148,7 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
                       int width, std::vector<float4>& nodes, std::vector<float4>& isect, std::string& err);
 
 cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
-cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, cudaStream_t st);
+cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, int volumeGrid, cudaStream_t st);
 cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint32_t sel, int grid, cudaStream_t st);
 cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st);

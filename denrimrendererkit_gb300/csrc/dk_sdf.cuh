@@ -383,8 +383,31 @@ __device__ __forceinline__ VolumeRay volumeRay(const dk_volume_descriptor& vol, 
     return r;
 }
 
-// closestSparseVolumeBrickDDAHit (:2881-3088) for volume `vi`.
-__device__ bool sparseDDAHit(const VolumeScene& V, uint32_t vi, float3 o, float3 d, float closestT, VolumeHitRec& out) {
+// closestSparseVolumeBrickDDAHit (:2881-3088) in three parts, so that a
+// persistent kernel can advance each lane's ray a few cells at a time and
+// refill lanes whose ray is done (the operations and their order are those of
+// the reference's single loop; sparseDDAHit below runs them back to back).
+// The grid of volume `vi` (uniform over a launch):
+struct DDAGrid {
+    const dk_volume_descriptor* vol;
+    uint32_t gd[3], gridOffset, bsz[3];
+    uint32_t md[3], macroOffset, msz[3];
+    bool hasMacro;
+    uint32_t maxSteps;
+};
+// One ray's walk through it:
+struct DDAState {
+    VolumeRay vr;
+    float bpa[3], va[3], tMax[3], tDelta[3];
+    int cell[3], stepDir[3];
+    float t, tNear, tFar, closest;
+    uint32_t step;
+    bool found;
+    VolumeHitRec out;
+};
+
+// The brick grid of volume `vi`; false when it has none.
+__device__ __forceinline__ bool ddaGrid(const VolumeScene& V, uint32_t vi, DDAGrid& g) {
     const dk_volume_brick_grid* grid = nullptr;
     for (uint32_t i = 0; i < V.gridCount; ++i)
         if (V.grids[i].brick_size_and_volume.w == vi) {
@@ -392,112 +415,148 @@ __device__ bool sparseDDAHit(const VolumeScene& V, uint32_t vi, float3 o, float3
             break;
         }
     if (!grid || !V.gridIndices) return false;
-    const dk_volume_descriptor& vol = V.volumes[vi];
-    uint32_t gd[3] = {grid->dimensions_and_index_offset.x, grid->dimensions_and_index_offset.y, grid->dimensions_and_index_offset.z};
-    uint32_t gridOffset = grid->dimensions_and_index_offset.w;
-    uint32_t bsz[3] = {max(grid->brick_size_and_volume.x, 1u), max(grid->brick_size_and_volume.y, 1u),
-                       max(grid->brick_size_and_volume.z, 1u)};
-    if (gd[0] == 0u || gd[1] == 0u || gd[2] == 0u) return false;
-    float tNear, tFar;
-    if (!intersectAABB(o, d, ld3f(vol.world_bounds_min), ld3f(vol.world_bounds_max), closestT, tNear, tFar)) return false;
-    VolumeRay vr = volumeRay(vol, o, d);
+    g.vol = &V.volumes[vi];
+    g.gd[0] = grid->dimensions_and_index_offset.x;
+    g.gd[1] = grid->dimensions_and_index_offset.y;
+    g.gd[2] = grid->dimensions_and_index_offset.z;
+    g.gridOffset = grid->dimensions_and_index_offset.w;
+    g.bsz[0] = max(grid->brick_size_and_volume.x, 1u);
+    g.bsz[1] = max(grid->brick_size_and_volume.y, 1u);
+    g.bsz[2] = max(grid->brick_size_and_volume.z, 1u);
+    if (g.gd[0] == 0u || g.gd[1] == 0u || g.gd[2] == 0u) return false;
+    g.md[0] = grid->macro_dimensions_and_index_offset.x;
+    g.md[1] = grid->macro_dimensions_and_index_offset.y;
+    g.md[2] = grid->macro_dimensions_and_index_offset.z;
+    g.macroOffset = grid->macro_dimensions_and_index_offset.w;
+    g.msz[0] = max(grid->macro_size_and_reserved.x, 1u);
+    g.msz[1] = max(grid->macro_size_and_reserved.y, 1u);
+    g.msz[2] = max(grid->macro_size_and_reserved.z, 1u);
+    g.hasMacro = g.md[0] > 0u && g.md[1] > 0u && g.md[2] > 0u && g.macroOffset < V.gridIndexCount;
+    g.maxSteps = min(g.gd[0] + g.gd[1] + g.gd[2] + 8u, 1024u);
+    return true;
+}
+
+// The ray's entry into the volume's bounds and its first cell; false when it
+// misses the bounds before closestT (no hit).
+__device__ __forceinline__ bool ddaBegin(const DDAGrid& g, float3 o, float3 d, float closestT, DDAState& s) {
+    const dk_volume_descriptor& vol = *g.vol;
+    if (!intersectAABB(o, d, ld3f(vol.world_bounds_min), ld3f(vol.world_bounds_max), closestT, s.tNear, s.tFar))
+        return false;
+    s.vr = volumeRay(vol, o, d);
     float3 extent = mx(ex::sub(ld3f(vol.local_bounds_max), ld3f(vol.local_bounds_min)), f3(1e-6f));
     float3 sampleDen = mx(ex::sub(f3((float)vol.dimensions.x, (float)vol.dimensions.y, (float)vol.dimensions.z), f3(1.0f)), f3(1.0f));
-    float3 bsf = mx(f3((float)bsz[0], (float)bsz[1], (float)bsz[2]), f3(1.0f));
-    float t = tNear;
-    float3 lp = ex::add(vr.lo, ex::mul(vr.ld, t));
+    float3 bsf = mx(f3((float)g.bsz[0], (float)g.bsz[1], (float)g.bsz[2]), f3(1.0f));
+    s.t = s.tNear;
+    float3 lp = ex::add(s.vr.lo, ex::mul(s.vr.ld, s.t));
     float3 sp = exDiv(ex::sub(lp, ld3f(vol.local_bounds_min)), extent);
     sp = f3(ex::mul(sp.x, sampleDen.x), ex::mul(sp.y, sampleDen.y), ex::mul(sp.z, sampleDen.z));
     float3 bp = exDiv(ex::add(sp, f3(0.5f)), bsf);
-    float bpa[3] = {bp.x, bp.y, bp.z};
-    float3 vel3 = exDiv(exDiv(vr.ld, extent), f3(1.0f));
+    s.bpa[0] = bp.x;
+    s.bpa[1] = bp.y;
+    s.bpa[2] = bp.z;
+    float3 vel3 = exDiv(exDiv(s.vr.ld, extent), f3(1.0f));
     vel3 = f3(ex::mul(vel3.x, sampleDen.x), ex::mul(vel3.y, sampleDen.y), ex::mul(vel3.z, sampleDen.z));
     vel3 = exDiv(vel3, bsf);
-    float va[3] = {vel3.x, vel3.y, vel3.z};
-    int cell[3], stepDir[3];
-    float tMax[3], tDelta[3];
+    s.va[0] = vel3.x;
+    s.va[1] = vel3.y;
+    s.va[2] = vel3.z;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        cell[a] = (int)clampf(floorf(bpa[a]), 0.0f, ex::sub((float)gd[a], 1.0f));
-        stepDir[a] = va[a] > 0.0f ? 1 : (va[a] < 0.0f ? -1 : 0);
-        float nb = stepDir[a] > 0 ? ex::add((float)cell[a], 1.0f) : (float)cell[a];
-        tMax[a] = stepDir[a] == 0 ? INFINITY : ex::add(t, ex::div(ex::sub(nb, bpa[a]), va[a]));
-        tDelta[a] = stepDir[a] == 0 ? INFINITY : fabsf(ex::div(1.0f, va[a]));
+        s.cell[a] = (int)clampf(floorf(s.bpa[a]), 0.0f, ex::sub((float)g.gd[a], 1.0f));
+        s.stepDir[a] = s.va[a] > 0.0f ? 1 : (s.va[a] < 0.0f ? -1 : 0);
+        float nb = s.stepDir[a] > 0 ? ex::add((float)s.cell[a], 1.0f) : (float)s.cell[a];
+        s.tMax[a] = s.stepDir[a] == 0 ? INFINITY : ex::add(s.t, ex::div(ex::sub(nb, s.bpa[a]), s.va[a]));
+        s.tDelta[a] = s.stepDir[a] == 0 ? INFINITY : fabsf(ex::div(1.0f, s.va[a]));
     }
-    uint32_t md[3] = {grid->macro_dimensions_and_index_offset.x, grid->macro_dimensions_and_index_offset.y,
-                      grid->macro_dimensions_and_index_offset.z};
-    uint32_t macroOffset = grid->macro_dimensions_and_index_offset.w;
-    uint32_t msz[3] = {max(grid->macro_size_and_reserved.x, 1u), max(grid->macro_size_and_reserved.y, 1u),
-                       max(grid->macro_size_and_reserved.z, 1u)};
-    bool hasMacro = md[0] > 0u && md[1] > 0u && md[2] > 0u && macroOffset < V.gridIndexCount;
-    uint32_t maxSteps = min(gd[0] + gd[1] + gd[2] + 8u, 1024u);
-    bool found = false;
-    float closest = closestT;
-    for (uint32_t step = 0u; step < maxSteps && t <= tFar && t < closest; ++step) {
-        if (cell[0] < 0 || cell[1] < 0 || cell[2] < 0 || cell[0] >= (int)gd[0] || cell[1] >= (int)gd[1] ||
-            cell[2] >= (int)gd[2])
-            break;
-        if (hasMacro) {
+    s.step = 0u;
+    s.found = false;
+    s.closest = closestT;
+    return true;
+}
+
+// Up to `budget` iterations of the walk (one brick-grid cell or one skipped
+// macro cell each); true when the walk is over, with the nearest brick hit in
+// s.out when s.found.
+__device__ __forceinline__ bool ddaSteps(const VolumeScene& V, const DDAGrid& g, DDAState& s, int budget) {
+    for (int it = 0; it < budget; ++it, ++s.step) {
+        if (!(s.step < g.maxSteps && s.t <= s.tFar && s.t < s.closest)) return true;
+        if (s.cell[0] < 0 || s.cell[1] < 0 || s.cell[2] < 0 || s.cell[0] >= (int)g.gd[0] ||
+            s.cell[1] >= (int)g.gd[1] || s.cell[2] >= (int)g.gd[2])
+            return true;
+        if (g.hasMacro) {
             uint32_t mc[3];
 #pragma unroll
-            for (int a = 0; a < 3; ++a) mc[a] = min((uint32_t)cell[a] / msz[a], md[a] - 1u);
-            uint64_t macroSlot = (uint64_t)macroOffset + mc[0] + mc[1] * md[0] + mc[2] * md[0] * md[1];
+            for (int a = 0; a < 3; ++a) mc[a] = min((uint32_t)s.cell[a] / g.msz[a], g.md[a] - 1u);
+            uint64_t macroSlot = (uint64_t)g.macroOffset + mc[0] + mc[1] * g.md[0] + mc[2] * g.md[0] * g.md[1];
             if (macroSlot < V.gridIndexCount && __ldg(V.gridIndices + macroSlot) == 0u) {
-                float dt = ex::sub(t, tNear);
-                float cb[3] = {ex::add(bpa[0], ex::mul(va[0], dt)), ex::add(bpa[1], ex::mul(va[1], dt)),
-                               ex::add(bpa[2], ex::mul(va[2], dt))};
+                float dt = ex::sub(s.t, s.tNear);
+                float cb[3] = {ex::add(s.bpa[0], ex::mul(s.va[0], dt)), ex::add(s.bpa[1], ex::mul(s.va[1], dt)),
+                               ex::add(s.bpa[2], ex::mul(s.va[2], dt))};
                 float mt[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    float mb = stepDir[a] > 0 ? (float)min((mc[a] + 1u) * msz[a], gd[a]) : (float)(mc[a] * msz[a]);
-                    mt[a] = stepDir[a] == 0 ? INFINITY : ex::add(t, ex::div(ex::sub(mb, cb[a]), va[a]));
+                    float mb = s.stepDir[a] > 0 ? (float)min((mc[a] + 1u) * g.msz[a], g.gd[a]) : (float)(mc[a] * g.msz[a]);
+                    mt[a] = s.stepDir[a] == 0 ? INFINITY : ex::add(s.t, ex::div(ex::sub(mb, cb[a]), s.va[a]));
                 }
                 float macroNextT = fminf(mt[0], fminf(mt[1], mt[2]));
-                if (macroNextT > ex::add(t, 1e-6f)) {
-                    if (macroNextT > tFar || macroNextT >= closest) break;
-                    t = ex::add(macroNextT, 1e-5f);
-                    float dt2 = ex::sub(t, tNear);
+                if (macroNextT > ex::add(s.t, 1e-6f)) {
+                    if (macroNextT > s.tFar || macroNextT >= s.closest) return true;
+                    s.t = ex::add(macroNextT, 1e-5f);
+                    float dt2 = ex::sub(s.t, s.tNear);
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
-                        float c2 = ex::add(bpa[a], ex::mul(va[a], dt2));
-                        cell[a] = (int)clampf(floorf(c2), 0.0f, ex::sub((float)gd[a], 1.0f));
-                        float nb = stepDir[a] > 0 ? ex::add((float)cell[a], 1.0f) : (float)cell[a];
-                        tMax[a] = stepDir[a] == 0 ? INFINITY : ex::add(t, ex::div(ex::sub(nb, c2), va[a]));
+                        float c2 = ex::add(s.bpa[a], ex::mul(s.va[a], dt2));
+                        s.cell[a] = (int)clampf(floorf(c2), 0.0f, ex::sub((float)g.gd[a], 1.0f));
+                        float nb = s.stepDir[a] > 0 ? ex::add((float)s.cell[a], 1.0f) : (float)s.cell[a];
+                        s.tMax[a] = s.stepDir[a] == 0 ? INFINITY : ex::add(s.t, ex::div(ex::sub(nb, c2), s.va[a]));
                     }
                     continue;
                 }
             }
         }
-        uint64_t slot = (uint64_t)gridOffset + (uint32_t)cell[0] + (uint32_t)cell[1] * gd[0] + (uint32_t)cell[2] * gd[0] * gd[1];
+        uint64_t slot = (uint64_t)g.gridOffset + (uint32_t)s.cell[0] + (uint32_t)s.cell[1] * g.gd[0] +
+                        (uint32_t)s.cell[2] * g.gd[0] * g.gd[1];
         if (slot < V.gridIndexCount) {
             uint32_t bi = __ldg(V.gridIndices + slot);
             float bt;
             if (bi != 0xffffffffu && bi < V.brickCount &&
-                intersectBrick(V, bi, closest, vr.lo, vr.ld, vr.upw, vr.cellSize, bt) && bt < closest) {
-                closest = bt;
-                out.t = bt;
-                out.brick = bi;
-                found = true;
+                intersectBrick(V, bi, s.closest, s.vr.lo, s.vr.ld, s.vr.upw, s.vr.cellSize, bt) && bt < s.closest) {
+                s.closest = bt;
+                s.out.t = bt;
+                s.out.brick = bi;
+                s.found = true;
             }
         }
-        float nextT = fminf(tMax[0], fminf(tMax[1], tMax[2]));
-        if (found && closest <= ex::add(nextT, 0.0005f)) return true;
-        if (nextT > tFar || nextT >= closest) break;
-        if (tMax[0] <= tMax[1] && tMax[0] <= tMax[2]) {
-            cell[0] += stepDir[0];
-            t = tMax[0];
-            tMax[0] = ex::add(tMax[0], tDelta[0]);
-        } else if (tMax[1] <= tMax[2]) {
-            cell[1] += stepDir[1];
-            t = tMax[1];
-            tMax[1] = ex::add(tMax[1], tDelta[1]);
+        float nextT = fminf(s.tMax[0], fminf(s.tMax[1], s.tMax[2]));
+        if (s.found && s.closest <= ex::add(nextT, 0.0005f)) return true;
+        if (nextT > s.tFar || nextT >= s.closest) return true;
+        if (s.tMax[0] <= s.tMax[1] && s.tMax[0] <= s.tMax[2]) {
+            s.cell[0] += s.stepDir[0];
+            s.t = s.tMax[0];
+            s.tMax[0] = ex::add(s.tMax[0], s.tDelta[0]);
+        } else if (s.tMax[1] <= s.tMax[2]) {
+            s.cell[1] += s.stepDir[1];
+            s.t = s.tMax[1];
+            s.tMax[1] = ex::add(s.tMax[1], s.tDelta[1]);
         } else {
-            cell[2] += stepDir[2];
-            t = tMax[2];
-            tMax[2] = ex::add(tMax[2], tDelta[2]);
+            s.cell[2] += s.stepDir[2];
+            s.t = s.tMax[2];
+            s.tMax[2] = ex::add(s.tMax[2], s.tDelta[2]);
         }
     }
-    return found;
+    return false;
+}
+
+// closestSparseVolumeBrickDDAHit (:2881-3088) for volume `vi`.
+__device__ bool sparseDDAHit(const VolumeScene& V, uint32_t vi, float3 o, float3 d, float closestT, VolumeHitRec& out) {
+    DDAGrid g;
+    if (!ddaGrid(V, vi, g)) return false;
+    DDAState s;
+    if (!ddaBegin(g, o, d, closestT, s)) return false;
+    while (!ddaSteps(V, g, s, 1 << 20)) {
+    }
+    if (s.found) out = s.out;
+    return s.found;
 }
 
 // closestVolumeHit (:3090-3157), sparse-brick volumes only.
