@@ -111,12 +111,14 @@ def test_conv3x3_forward_wide(lib, cin, cout, act, ldi_extra, ldo_extra, co_off)
         assert torch.equal(untouched, expect)
 
 
-@pytest.mark.parametrize("cin,cout", [(32, 32), (96, 32), (64, 64), (32, 16), (48, 32), (80, 16)])
+@pytest.mark.parametrize("cin,cout", [(32, 32), (96, 32), (64, 64), (32, 16), (48, 32), (80, 16), (144, 32),
+                                       (160, 64)])
 def test_conv3x3_forward_tall(lib, cin, cout):
     # About 40 output rows per persistent CTA, crossing tile columns and
     # images: the halo-row ring (up to 16 slots) and the stacked-tap
     # accumulator window (8 to 32 slots) wrap, and the MMAs at a segment's
     # first and last rows and at the window's wrap take the per-tap form.
+    # Three input chunks (144, 160): the per-tap kernel's row-tap mode.
     g = torch.Generator().manual_seed(cin + 7 * cout)
     n, h, w = 3, 1000, 136
     x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
