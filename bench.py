@@ -564,8 +564,8 @@ def sdf_measure(args, flush, steps=3, warmup=2):
 
 
 def serving_with_denoising_measure(target=0.02, n_scenes=4, views=8, size=256, train_steps=2500, margin=0.9):
-    """The benchmark spec's comparison at its stated error (relative RMSE of the
-    displayed image): requests (`views` camera views of each of `n_scenes`
+    """Serving with denoising against plain rendering at a stated error target
+    (relative RMSE of the displayed image): requests (`views` camera views of each of `n_scenes`
     held-out small-scene variants, all resident in one render server) served
     until each image's estimated relative RMSE (of the displayed image, over
     its mean) is at most `target` x `margin` (the estimate is statistical; the
