@@ -415,6 +415,31 @@ class RenderScene:
     def add(self, mesh: Mesh, material: int, transform: Optional[Transform] = None) -> None:
         self.mesh_instances.append(MeshInstance(mesh, material, transform or Transform.identity()))
 
+    def add_quad_light(self, light: "QuadLight") -> int:
+        """RenderScene.addQuadLight (RenderScene.swift:307-321): the light's
+        emissive material and its quad; returns the material index.  Scenes
+        get no lights by default."""
+        material = self.add_material(light.material())
+        self.add(Mesh.quad(light.a, light.b, light.c, light.d), material)
+        return material
+
+
+@dataclasses.dataclass
+class QuadLight:
+    """QuadLight (Scene/QuadLight.swift:5-50): a rectangular area light from
+    four corners, emitting `color` x `intensity`."""
+    a: Sequence[float]
+    b: Sequence[float]
+    c: Sequence[float]
+    d: Sequence[float]
+    color: Sequence[float] = (1.0, 1.0, 1.0)
+    intensity: float = 1.0
+
+    def material(self) -> Material:
+        """The light's material (QuadLight.swift:41-50)."""
+        return Material(base_color=tuple(self.color), emission=tuple(self.color), emission_strength=self.intensity,
+                        roughness=0.4, metallic=0.0, specular=0.0)
+
 
 @dataclasses.dataclass
 class AccelerationBuild:
