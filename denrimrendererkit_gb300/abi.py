@@ -163,7 +163,7 @@ EXPORTED_SYMBOLS = (
     "dk_device_open", "dk_device_count", "dk_session_create", "dk_session_render",
     "dk_session_render_tile", "dk_session_update_camera", "dk_session_reset",
     "dk_session_read_output", "dk_session_copy_output", "dk_session_read_rgba8", "dk_session_write_png", "dk_encode_rgba8", "dk_write_png",
-    "dk_session_sample_count", "dk_session_stats",
+    "dk_session_sample_count", "dk_session_stats", "dk_session_reset_sdf_stats",
     "dk_session_destroy", "dk_last_error_message", "dk_build_bvh", "dk_build_lights",
     "dk_build_environment_samples", "dk_build_environment_samples_noalloc", "dk_build_sparse_sphere_volume",
     "dk_bake_sparse_sphere_volume",

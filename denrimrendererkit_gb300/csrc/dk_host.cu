@@ -192,6 +192,7 @@ struct Session {
     dk_stats stats;
     dk::Grids grids;
     uint32_t opaqueMask = 0;
+    unsigned long long* sdfCounters = nullptr;  // settings.collects_traversal_stats: the 13 SDF counters
 };
 
 void freeSession(Session* s) {
@@ -635,7 +636,7 @@ int launchWave(const DevScene& S, const Wave& W, uint32_t maxBounces, bool anyDe
     for (uint32_t b = 0; b < maxBounces; ++b) {
         uint32_t sel = b & 1u;
         MARK(1);
-        DK_CUDA(launchExtend(S, W, sel, S.wide8 ? g.extend8 : g.extend, g.volume, q), "extend launch");
+        DK_CUDA(launchExtend(S, W, sel, b, S.wide8 ? g.extend8 : g.extend, g.volume, q), "extend launch");
         MARK(2);
         DK_CUDA(launchShade(S, W, b, sel, g.shade, q), "shade launch");
         MARK(3);
@@ -825,6 +826,15 @@ int dk_session_create(const dk_scene* sc, const dk_settings* st, dk_session** ou
     phase("accumulation allocation");
     TRY(dk::uploadScene(s->arena, sc, s->scene, sc->material_count, &traversal));
     phase("scene upload (with the traversal build's tail)");
+    if (st->collects_traversal_stats) {  // RenderSettings.collectsSDFTraversalStats (RenderSettings.swift:73)
+        TRY(s->arena.alloc(&s->sdfCounters, dk::kSdfCounterSlots, "SDF traversal counters"));
+        s->scene.sdf_counters = s->sdfCounters;
+        if (cudaMemsetAsync(s->sdfCounters, 0, dk::kSdfCounterSlots * sizeof(unsigned long long), s->stream) !=
+            cudaSuccess) {
+            freeSession(s);
+            return fail(DK_ERROR_COMMAND_FAILED, "clearing the SDF traversal counters failed");
+        }
+    }
     dk::persistTraversal(s->scene, s->stream);
     s->opaqueMask = dk::opaqueMask(sc->materials, sc->material_count);
     TRY(dk::clearAccum(s->accum, pixels, s->stream));
@@ -1162,6 +1172,23 @@ int dk_session_stats(const dk_session* session, dk_stats* out) {
     const Session* s = reinterpret_cast<const Session*>(session);
     if (!s || !out) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
     *out = s->stats;
+    if (s->sdfCounters) {  // sdfTraversalStats (RenderSession.swift:808-831)
+        unsigned long long c[dk::kSdfCounterSlots];
+        if (cudaStreamSynchronize(s->stream) != cudaSuccess ||
+            cudaMemcpy(c, s->sdfCounters, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return fail(DK_ERROR_COMMAND_FAILED, "reading the SDF traversal counters failed");
+        for (uint32_t k = 0; k < dk::kSdfCounterSlots; ++k) out->sdf_counters[k] = c[k];
+    }
+    return DK_OK;
+}
+
+int dk_session_reset_sdf_stats(dk_session* session) {
+    Session* s = reinterpret_cast<Session*>(session);
+    if (!s) return fail(DK_ERROR_INVALID_ARGUMENT, "null argument");
+    if (!s->sdfCounters) return DK_OK;
+    if (cudaMemsetAsync(s->sdfCounters, 0, dk::kSdfCounterSlots * sizeof(unsigned long long), s->stream) != cudaSuccess ||
+        cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return fail(DK_ERROR_COMMAND_FAILED, "clearing the SDF traversal counters failed");
     return DK_OK;
 }
 

@@ -181,7 +181,7 @@ __device__ __noinline__ HitRec traceScene(const DevScene& S, float3 o, float3 d)
     HitRec r = S.wide8 ? traceClosest8(S, o, d) : traceClosest(S, o, d);
     if (S.volume_count) {
         VolumeHitRec vh;
-        if (closestVolumeHit(volumeScene(S), o, d, r.t, vh)) {
+        if (closestVolumeHitAny(volumeScene(S), o, d, r.t, vh, S.sdf_counters)) {
             r.t = vh.t;
             r.tri = kVolumeHit;
             r.u = __uint_as_float(vh.brick);
@@ -220,6 +220,7 @@ __device__ bool continueSubsurfaceRandomWalk(const DevScene& S, const Hit& entry
     float3 albedo = clamp3(xyz(m.subsurfaceColor), f3(0.0f), f3(0.999f));
     float anisotropy = clampf(m.subsurfaceParameters.x, -0.95f, 0.95f);
     for (uint32_t step = 0u; step < 8u; ++step) {
+        sdfCount(S.sdf_counters, kSdfBounceSceneQueries);
         HitRec r = kVolumes ? traceScene(S, medium.origin, medium.direction) : traceClosest(S, medium.origin, medium.direction);
         if (r.tri == kNoHit) return false;
         float f0 = randomFloat(state);
@@ -428,12 +429,16 @@ __device__ __forceinline__ uint32_t warpFetch(uint32_t* counter, uint32_t n, boo
 // threads with per-lane refill.  W.counts[4] is the work cursor (zeroed by the
 // kernel that runs before).
 template <bool kWide8>
-__global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel) {
+__global__ void __launch_bounds__(128) k_extend(DevScene S, Wave W, uint32_t sel, uint32_t bounce) {
     const uint32_t* q = W.q[sel];
     const uint32_t n = W.counts[sel];
     if (blockIdx.x == 0)
         for (uint32_t b = threadIdx.x; b <= kSortBins; b += blockDim.x) W.bins[b] = 0u;
     if (globalId() == 0) {
+        // one scene query per active path and bounce (PathTrace.metal:5252-5256)
+        if (S.sdf_counters && n)
+            atomicAdd(S.sdf_counters + (bounce == 0u ? kSdfPrimarySceneQueries : kSdfBounceSceneQueries),
+                      (unsigned long long)n);
         W.counts[sel ^ 1u] = 0u;
         W.counts[2] = 0u;
         W.counts[3] = 0u;
@@ -1064,6 +1069,7 @@ __device__ bool recordedLayers(const DevScene& S, MatTable mt, float3 o, float3 
 __device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, float maxDistance, float3& T) {
     float traveled = 0.0f;
     for (uint32_t step = 0; step < 8u; ++step) {
+        sdfCount(S.sdf_counters, kSdfShadowSceneQueries);
         HitRec r = traceScene(S, o, d);
         if (r.tri == kNoHit || traveled + r.t >= maxDistance) return false;
         Ray ray{o, d};
@@ -1103,6 +1109,7 @@ __device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, f
 // shorter waits for a warp's longest walk save), one ray per thread over the
 // general path 493.  Scenes with several volumes, or budget 0
 // (DK_VOLUME_REFILL=0), take one ray per thread and walk the volumes in turn.
+template <bool kStats>
 __global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(DevScene S, Wave W, uint32_t sel,
                                                                            uint32_t budget) {
     const uint32_t* q = W.q[sel];
@@ -1117,7 +1124,8 @@ __global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(Dev
             float4 o = W.ray_o[p], d = W.ray_d[p];
             float4 h = W.hit[p];
             VolumeHitRec vh;
-            if (closestVolumeHit(V, xyz(o), xyz(d), h.x, vh))
+            if (kStats ? closestVolumeHitCounted(V, xyz(o), xyz(d), h.x, vh, S.sdf_counters)
+                       : closestVolumeHit(V, xyz(o), xyz(d), h.x, vh))
                 W.hit[p] = make_float4(vh.t, __uint_as_float(kVolumeHit), __uint_as_float(vh.brick), 0.0f);
         }
         return;
@@ -1135,7 +1143,8 @@ __global__ void __launch_bounds__(128, DK_VOLUME_MIN_BLOCKS) k_extend_volume(Dev
             if (!ddaBegin(g, xyz(o), xyz(d), closestT, st)) p = kNoWork;  // misses the volume's bounds
         }
         if (__all_sync(0xffffffffu, p == kNoWork && exhausted)) break;
-        if (p != kNoWork && ddaSteps(V, g, st, (int)budget)) {
+        if (p != kNoWork && (kStats ? ddaStepsCounted(V, g, st, (int)budget, S.sdf_counters)
+                                    : ddaSteps(V, g, st, (int)budget))) {
             if (st.found && st.out.t < closestT)
                 W.hit[p] = make_float4(st.out.t, __uint_as_float(kVolumeHit), __uint_as_float(st.out.brick), 0.0f);
             p = kNoWork;
@@ -1152,6 +1161,10 @@ template <bool kWide8>
 __global__ void __launch_bounds__(128) k_shadow_rays(DevScene S, Wave W) {
     const uint32_t n = W.counts[3];
     const size_t cap = W.cap;
+    // Triangle-only scenes: one scene query per shadow ray (the reference steps through
+    // transmissive layers one closest hit at a time; scenes with volumes count the walk's steps).
+    if (S.sdf_counters && S.volume_count == 0u && globalId() == 0 && n)
+        atomicAdd(S.sdf_counters + kSdfShadowSceneQueries, (unsigned long long)n);
     int stackNode[kWide8 ? 1 : kStackSize];
     uint2 stack8[kWide8 ? kTraversalStack : 1];
     std::conditional_t<kWide8, Any8, AnyState> st;
@@ -1257,6 +1270,7 @@ __global__ void __launch_bounds__(128) k_aov_primary(DevScene S, Wave W) {
         Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, 0.5f, 0.5f, 0.0f, 0.0f);
         writeAovMiss(W.aov, i, W.aov_stride);
         for (uint32_t pass = 0; pass < 32u; ++pass) {
+            sdfCount(S.sdf_counters, kSdfPrimarySceneQueries);
             HitRec r = traceScene(S, ray.origin, ray.direction);
             if (r.tri == kNoHit) break;
             Hit h = makeHitAny(S, ray, r);
@@ -1368,6 +1382,7 @@ __device__ float interactiveContactAO(const DevScene& S, MatTable mt, const Hit&
         float3 l = normalize(local[k]);
         float3 dir = normalize(l.x * frame.tangent + l.y * frame.bitangent + l.z * n);
         Ray ray{h.position + n * 0.003f, dir};
+        sdfCount(S.sdf_counters, kSdfShadowSceneQueries);
         HitRec r = traceScene(S, ray.origin, ray.direction);
         if (r.tri == kNoHit || !(r.t < kRadius)) continue;
         Hit oh = makeHitAny(S, ray, r);
@@ -1387,6 +1402,7 @@ __global__ void __launch_bounds__(128) k_preview(DevScene S, DevParams P, Accum 
         const uint32_t px = P.tile_x + i % P.tile_w, py = P.tile_y + i / P.tile_w;
         const size_t pix = (size_t)py * P.width + px;
         Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, 0.5f, 0.5f, 0.0f, 0.0f);
+        sdfCount(S.sdf_counters, kSdfPrimarySceneQueries);
         HitRec rec = traceScene(S, ray.origin, ray.direction);
         float4 beauty;
         if (rec.tri == kNoHit) {
@@ -1450,6 +1466,7 @@ __global__ void __launch_bounds__(128) k_preview(DevScene S, DevParams P, Accum 
                     if (cosS <= 0.0f || cosL <= 0.0f) continue;
                     float3 T = f3(1.0f);
                     float3 so = h.position + n * 0.001f;
+                    if (!S.volume_count) sdfCount(S.sdf_counters, kSdfShadowSceneQueries);
                     bool occluded = S.volume_count ? shadowWalk(S, mt, so, ld, dist - 0.002f, T)
                                                    : shadowLayers(S, mt, opaqueMask, so, ld, dist - 0.002f, T);
                     if (occluded) continue;
@@ -1699,7 +1716,7 @@ int kernelGrid(int which, int smCount) {
         case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<false>, 128, 0); break;
         case 5: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend<true>, 128, 0); break;
         case 6: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_shadow_rays<true>, 128, 0); break;
-        case 7: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend_volume, 128, 0); break;
+        case 7: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_extend_volume<false>, 128, 0); break;
         default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_finalize, 256, 0); break;
     }
     return (perSM < 1 ? 1 : perSM) * smCount;
@@ -1709,11 +1726,12 @@ cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStrea
     k_generate<<<grid, 256, 0, st>>>(S, W);
     return cudaGetLastError();
 }
-cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, int volumeGrid, cudaStream_t st) {
+cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, uint32_t bounce, int grid, int volumeGrid,
+                         cudaStream_t st) {
     if (S.wide8)
-        k_extend<true><<<grid, 128, 0, st>>>(S, W, sel);
+        k_extend<true><<<grid, 128, 0, st>>>(S, W, sel, bounce);
     else
-        k_extend<false><<<grid, 128, 0, st>>>(S, W, sel);
+        k_extend<false><<<grid, 128, 0, st>>>(S, W, sel, bounce);
     if (S.volume_count) {
         // grid cells per refill step (DK_VOLUME_BUDGET, default 256); DK_VOLUME_REFILL=0: one ray per thread
         const char* refill = getenv("DK_VOLUME_REFILL");
@@ -1721,7 +1739,10 @@ cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int gri
         uint32_t budget = env ? (uint32_t)strtoul(env, nullptr, 10) : 256u;
         budget = budget < 1u ? 1u : (budget > 1024u ? 1024u : budget);
         if (refill && refill[0] == '0') budget = 0u;
-        k_extend_volume<<<volumeGrid, 128, 0, st>>>(S, W, sel, budget);
+        if (S.sdf_counters)  // the counting instantiation only when the session collects them
+            k_extend_volume<true><<<volumeGrid, 128, 0, st>>>(S, W, sel, budget);
+        else
+            k_extend_volume<false><<<volumeGrid, 128, 0, st>>>(S, W, sel, budget);
     }
     return cudaGetLastError();
 }

@@ -53,7 +53,10 @@ struct DevScene {
     const uint32_t* brick_grid_indices;
     uint64_t brick_sample_count, brick_grid_index_count;
     uint32_t volume_count, brick_count, brick_grid_count, volume_all_opaque;
+    // The reference's 13 SDF traversal counters (RenderSettings.collectsSDFTraversalStats), or null.
+    unsigned long long* sdf_counters;
 };
+constexpr uint32_t kSdfCounterSlots = 13;
 
 // GPURenderConstants (PathTrace.metal:143-182) for one batch of samples of
 // one render.
@@ -148,7 +151,8 @@ int buildSahTraversal(const dk_scene* sc, const std::vector<uint32_t>& slotOfTri
                       int width, std::vector<float4>& nodes, std::vector<float4>& isect, std::string& err);
 
 cudaError_t launchGenerate(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
-cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, int grid, int volumeGrid, cudaStream_t st);
+cudaError_t launchExtend(const DevScene& S, const Wave& W, uint32_t sel, uint32_t bounce, int grid, int volumeGrid,
+                         cudaStream_t st);
 cudaError_t launchShade(const DevScene& S, const Wave& W, uint32_t bounce, uint32_t sel, int grid, cudaStream_t st);
 cudaError_t launchShadow(const DevScene& S, const Wave& W, int grid, cudaStream_t st);
 cudaError_t launchResolve(const Wave& W, int grid, cudaStream_t st);

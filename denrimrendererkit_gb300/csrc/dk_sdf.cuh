@@ -249,6 +249,23 @@ struct VolumeScene {
     uint32_t volumeCount, brickCount, gridCount;
 };
 
+// The reference's SDF traversal counter slots (PathTrace.metal:191-203).
+enum : uint32_t {
+    kSdfDenseVolumeTests = 0, kSdfDenseMarchSteps = 1, kSdfGridCellsVisited = 2, kSdfGridMacroSkips = 3,
+    kSdfBrickTests = 4, kSdfBrickInvalid = 5, kSdfBrickRangeCulls = 6, kSdfBrickMarches = 7,
+    kSdfBrickMarchSteps = 8, kSdfBrickHits = 9, kSdfPrimarySceneQueries = 10, kSdfBounceSceneQueries = 11,
+    kSdfShadowSceneQueries = 12, kSdfCounterCount = 13
+};
+
+// addSDFTraversalCounter (PathTrace.metal:205-214): one event per calling
+// lane, aggregated over the lanes that arrive together (one atomic per warp);
+// nothing when collection is off (null).
+__device__ __forceinline__ void sdfCount(unsigned long long* counters, uint32_t k) {
+    if (!counters) return;
+    const unsigned m = __activemask();
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(counters + k, (unsigned long long)__popc(m));
+}
+
 __device__ __forceinline__ float cellSizeOf(const dk_volume_descriptor& vol) {
     float3 ext = mx(ex::sub(ld3f(vol.local_bounds_max), ld3f(vol.local_bounds_min)), f3(1e-6f));
     float3 den = mx(ex::sub(f3((float)vol.dimensions.x, (float)vol.dimensions.y, (float)vol.dimensions.z), f3(1.0f)), f3(1.0f));
@@ -286,88 +303,6 @@ struct VolumeHitRec {
     float t;
     uint32_t brick;
 };
-
-// intersectVolumeBrickPrepared (:2608-2807) up to the refined distance (the
-// hit attributes are rebuilt from (t, brick) by makeVolumeHit).
-template <class D>
-__device__ __noinline__ bool intersectBrickT(const D& dist, const VolumeScene& V, uint32_t brickIndex, float closestT,
-                                            float3 lo, float3 ld, float upw, float cellSize, float& outT) {
-    const dk_volume_brick_descriptor& brick = V.bricks[brickIndex];
-    float tNear, tFar;
-    if (!intersectAABB(lo, ld, ld3f(brick.local_bounds_min), ld3f(brick.local_bounds_max), closestT, tNear, tFar))
-        return false;
-    BrickCtx c = makeBrickCtx(brick, V.sampleCount);
-    if (!c.valid) return false;
-    if (__ldg(&brick.sample_bounds_min.w) > 0.0f || __ldg(&brick.sample_bounds_max.w) < 0.0f) return false;
-    float minimumStep = fmaxf(ex::div(ex::mul(cellSize, 0.10f), upw), 0.0005f);
-    float prevT = tNear;
-    float3 prevP = ex::add(lo, ex::mul(ld, prevT));
-    float prevD = brickDistance(dist, c, prevP);
-    if (!isfinite(prevD)) return false;
-    float originalEntryT = prevT;
-    if (prevD <= 0.0f) {
-        float backStep = fmaxf(ex::mul(ex::div(cellSize, upw), 0.5f), minimumStep);
-        float searchT = prevT;
-        for (uint32_t bt = 0u; bt < 12u; ++bt) {
-            searchT = fmaxf(ex::sub(searchT, backStep), 0.0005f);
-            float3 sp = ex::add(lo, ex::mul(ld, searchT));
-            float sd = brickDistance(dist, c, sp);
-            if (!isfinite(sd)) break;
-            if (sd > 0.0f) {
-                prevT = searchT;
-                prevP = sp;
-                prevD = sd;
-                break;
-            }
-            if (searchT <= 0.0005f) break;
-        }
-    }
-    float t = fmaxf(originalEntryT, ex::add(prevT, fmaxf(ex::mul(ex::div(fabsf(prevD), upw), 0.9f), minimumStep)));
-    for (uint32_t step = 0u; step < 192u && t <= tFar && t < closestT; ++step) {
-        float3 p = ex::add(lo, ex::mul(ld, t));
-        float d = brickDistance(dist, c, p);
-        if (!isfinite(d)) return false;
-        bool crossed = (prevD > 0.0f && d <= 0.0f) || (prevD < 0.0f && d >= 0.0f);
-        if (crossed) {
-            float lowT = prevT, highT = t, lowD = prevD, refinedT = t;
-            for (uint32_t r = 0u; r < 8u; ++r) {
-                float midT = ex::mul(0.5f, ex::add(lowT, highT));
-                float md = brickDistance(dist, c, ex::add(lo, ex::mul(ld, midT)));
-                if ((lowD > 0.0f && md > 0.0f) || (lowD < 0.0f && md < 0.0f)) {
-                    lowT = midT;
-                    lowD = md;
-                } else {
-                    highT = midT;
-                }
-                refinedT = ex::mul(0.5f, ex::add(lowT, highT));
-            }
-            if (cellSize <= 0.03f) {  // cubic polish, renderQuality 2: two Newton steps
-                float3 rp = ex::add(lo, ex::mul(ld, refinedT));
-                for (uint32_t pol = 0u; pol < 2u; ++pol) {
-                    DistGrad pg = brickDistGradCubic(dist, c, rp);
-                    float slope = ex::dot(pg.gradient, ld);
-                    if (!isfinite(pg.distance) || fabsf(slope) <= 1e-6f) break;
-                    float projected = ex::sub(refinedT, ex::div(pg.distance, slope));
-                    if (projected <= lowT || projected >= highT) break;
-                    refinedT = projected;
-                    rp = ex::add(lo, ex::mul(ld, refinedT));
-                }
-            }
-            outT = refinedT;
-            return true;
-        }
-        prevT = t;
-        prevD = d;
-        t = ex::add(t, fmaxf(ex::mul(ex::div(fabsf(d), upw), 0.8f), minimumStep));
-    }
-    return false;
-}
-
-__device__ __forceinline__ bool intersectBrick(const VolumeScene& V, uint32_t brickIndex, float closestT, float3 lo,
-                                               float3 ld, float upw, float cellSize, float& outT) {
-    if (V.dist.f16) return intersectBrickT(DistF16{V.dist.f16}, V, brickIndex, closestT, lo, ld, upw, cellSize, outT);
-    return intersectBrickT(DistF32{V.dist.f32}, V, brickIndex, closestT, lo, ld, upw, cellSize, outT);
-}
 
 struct VolumeRay {
     float3 lo, ld;
@@ -474,80 +409,32 @@ __device__ __forceinline__ bool ddaBegin(const DDAGrid& g, float3 o, float3 d, f
     return true;
 }
 
-// Up to `budget` iterations of the walk (one brick-grid cell or one skipped
-// macro cell each); true when the walk is over, with the nearest brick hit in
-// s.out when s.found.
-__device__ __forceinline__ bool ddaSteps(const VolumeScene& V, const DDAGrid& g, DDAState& s, int budget) {
-    for (int it = 0; it < budget; ++it, ++s.step) {
-        if (!(s.step < g.maxSteps && s.t <= s.tFar && s.t < s.closest)) return true;
-        if (s.cell[0] < 0 || s.cell[1] < 0 || s.cell[2] < 0 || s.cell[0] >= (int)g.gd[0] ||
-            s.cell[1] >= (int)g.gd[1] || s.cell[2] >= (int)g.gd[2])
-            return true;
-        if (g.hasMacro) {
-            uint32_t mc[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) mc[a] = min((uint32_t)s.cell[a] / g.msz[a], g.md[a] - 1u);
-            uint64_t macroSlot = (uint64_t)g.macroOffset + mc[0] + mc[1] * g.md[0] + mc[2] * g.md[0] * g.md[1];
-            if (macroSlot < V.gridIndexCount && __ldg(V.gridIndices + macroSlot) == 0u) {
-                float dt = ex::sub(s.t, s.tNear);
-                float cb[3] = {ex::add(s.bpa[0], ex::mul(s.va[0], dt)), ex::add(s.bpa[1], ex::mul(s.va[1], dt)),
-                               ex::add(s.bpa[2], ex::mul(s.va[2], dt))};
-                float mt[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    float mb = s.stepDir[a] > 0 ? (float)min((mc[a] + 1u) * g.msz[a], g.gd[a]) : (float)(mc[a] * g.msz[a]);
-                    mt[a] = s.stepDir[a] == 0 ? INFINITY : ex::add(s.t, ex::div(ex::sub(mb, cb[a]), s.va[a]));
-                }
-                float macroNextT = fminf(mt[0], fminf(mt[1], mt[2]));
-                if (macroNextT > ex::add(s.t, 1e-6f)) {
-                    if (macroNextT > s.tFar || macroNextT >= s.closest) return true;
-                    s.t = ex::add(macroNextT, 1e-5f);
-                    float dt2 = ex::sub(s.t, s.tNear);
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        float c2 = ex::add(s.bpa[a], ex::mul(s.va[a], dt2));
-                        s.cell[a] = (int)clampf(floorf(c2), 0.0f, ex::sub((float)g.gd[a], 1.0f));
-                        float nb = s.stepDir[a] > 0 ? ex::add((float)s.cell[a], 1.0f) : (float)s.cell[a];
-                        s.tMax[a] = s.stepDir[a] == 0 ? INFINITY : ex::add(s.t, ex::div(ex::sub(nb, c2), s.va[a]));
-                    }
-                    continue;
-                }
-            }
-        }
-        uint64_t slot = (uint64_t)g.gridOffset + (uint32_t)s.cell[0] + (uint32_t)s.cell[1] * g.gd[0] +
-                        (uint32_t)s.cell[2] * g.gd[0] * g.gd[1];
-        if (slot < V.gridIndexCount) {
-            uint32_t bi = __ldg(V.gridIndices + slot);
-            float bt;
-            if (bi != 0xffffffffu && bi < V.brickCount &&
-                intersectBrick(V, bi, s.closest, s.vr.lo, s.vr.ld, s.vr.upw, s.vr.cellSize, bt) && bt < s.closest) {
-                s.closest = bt;
-                s.out.t = bt;
-                s.out.brick = bi;
-                s.found = true;
-            }
-        }
-        float nextT = fminf(s.tMax[0], fminf(s.tMax[1], s.tMax[2]));
-        if (s.found && s.closest <= ex::add(nextT, 0.0005f)) return true;
-        if (nextT > s.tFar || nextT >= s.closest) return true;
-        if (s.tMax[0] <= s.tMax[1] && s.tMax[0] <= s.tMax[2]) {
-            s.cell[0] += s.stepDir[0];
-            s.t = s.tMax[0];
-            s.tMax[0] = ex::add(s.tMax[0], s.tDelta[0]);
-        } else if (s.tMax[1] <= s.tMax[2]) {
-            s.cell[1] += s.stepDir[1];
-            s.t = s.tMax[1];
-            s.tMax[1] = ex::add(s.tMax[1], s.tDelta[1]);
-        } else {
-            s.cell[2] += s.stepDir[2];
-            s.t = s.tMax[2];
-            s.tMax[2] = ex::add(s.tMax[2], s.tDelta[2]);
-        }
-    }
-    return false;
-}
+// The walk without counters, then with them (dk_sdf_walk.inc).
+#define DK_WALK(name) name
+#define DK_WALK_PARAMS
+#define DK_WALK_ARGS
+#define DK_WALK_COUNT(k)
+#define DK_WALK_COUNT_TRUE(k) true
+#include "dk_sdf_walk.inc"
+#undef DK_WALK
+#undef DK_WALK_PARAMS
+#undef DK_WALK_ARGS
+#undef DK_WALK_COUNT
+#undef DK_WALK_COUNT_TRUE
+#define DK_WALK(name) name##Counted
+#define DK_WALK_PARAMS , unsigned long long* counters
+#define DK_WALK_ARGS , counters
+#define DK_WALK_COUNT(k) sdfCount(counters, k)
+#define DK_WALK_COUNT_TRUE(k) (sdfCount(counters, k), true)
+#include "dk_sdf_walk.inc"
+#undef DK_WALK
+#undef DK_WALK_PARAMS
+#undef DK_WALK_ARGS
+#undef DK_WALK_COUNT
+#undef DK_WALK_COUNT_TRUE
 
-// closestSparseVolumeBrickDDAHit (:2881-3088) for volume `vi`.
+// closestSparseVolumeBrickDDAHit (:2881-3088) for volume `vi`; the Counted
+// form counts into `counters`.
 __device__ bool sparseDDAHit(const VolumeScene& V, uint32_t vi, float3 o, float3 d, float closestT, VolumeHitRec& out) {
     DDAGrid g;
     if (!ddaGrid(V, vi, g)) return false;
@@ -558,8 +445,20 @@ __device__ bool sparseDDAHit(const VolumeScene& V, uint32_t vi, float3 o, float3
     if (s.found) out = s.out;
     return s.found;
 }
+__device__ bool sparseDDAHitCounted(const VolumeScene& V, uint32_t vi, float3 o, float3 d, float closestT,
+                                    VolumeHitRec& out, unsigned long long* counters) {
+    DDAGrid g;
+    if (!ddaGrid(V, vi, g)) return false;
+    DDAState s;
+    if (!ddaBegin(g, o, d, closestT, s)) return false;
+    while (!ddaStepsCounted(V, g, s, 1 << 20, counters)) {
+    }
+    if (s.found) out = s.out;
+    return s.found;
+}
 
-// closestVolumeHit (:3090-3157), sparse-brick volumes only.
+// closestVolumeHit (:3090-3157), sparse-brick volumes only; the Counted form
+// counts into `counters`.
 __device__ __noinline__ bool closestVolumeHit(const VolumeScene& V, float3 o, float3 d, float closestT, VolumeHitRec& out) {
     if (V.volumeCount == 0 || V.gridCount == 0 || V.gridIndexCount == 0) return false;
     bool found = false;
@@ -574,6 +473,28 @@ __device__ __noinline__ bool closestVolumeHit(const VolumeScene& V, float3 o, fl
         }
     }
     return found;
+}
+__device__ __noinline__ bool closestVolumeHitCounted(const VolumeScene& V, float3 o, float3 d, float closestT,
+                                                    VolumeHitRec& out, unsigned long long* counters) {
+    if (V.volumeCount == 0 || V.gridCount == 0 || V.gridIndexCount == 0) return false;
+    bool found = false;
+    float closest = closestT;
+    for (uint32_t i = 0; i < V.volumeCount; ++i) {
+        if (V.volumes[i].metadata.w != 1u) continue;
+        VolumeHitRec r;
+        if (sparseDDAHitCounted(V, i, o, d, closest, r, counters) && r.t < closest) {
+            closest = r.t;
+            out = r;
+            found = true;
+        }
+    }
+    return found;
+}
+// One call site for the scene query: the counting form when `counters` is set.
+__device__ __noinline__ bool closestVolumeHitAny(const VolumeScene& V, float3 o, float3 d, float closestT,
+                                                VolumeHitRec& out, unsigned long long* counters) {
+    return counters ? closestVolumeHitCounted(V, o, d, closestT, out, counters)
+                    : closestVolumeHit(V, o, d, closestT, out);
 }
 
 }  // namespace dk

@@ -66,6 +66,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
             "dk_write_png": (i32, [C.c_char_p, P, u32, u32]),
             "dk_session_sample_count": (i32, [P, C.POINTER(u32)]),
             "dk_session_stats": (i32, [P, C.POINTER(abi.Stats)]),
+            "dk_session_reset_sdf_stats": (i32, [P]),
             "dk_session_destroy": (i32, [P]),
             "dk_last_error_message": (C.c_char_p, []),
             "dk_build_bvh": (i32, [P, u32, u32, P, C.POINTER(u32), P]),

@@ -266,6 +266,26 @@ class RenderSession:
         library.check(self._lib.dk_session_stats(self._handle, C.byref(st)))
         return st
 
+    # RenderSession.sdfTraversalStats() / resetSDFTraversalStats() (RenderSession.swift:808-840):
+    # the SDF traversal counters of a session made with `collects_traversal_stats`, by the
+    # reference's names (all zero otherwise).
+    SDF_COUNTER_NAMES = ("dense_volume_tests", "dense_march_steps", "sparse_grid_cells_visited",
+                         "sparse_grid_macro_skips", "sparse_brick_tests", "sparse_brick_invalid",
+                         "sparse_brick_range_culls", "sparse_brick_marches", "sparse_brick_march_steps",
+                         "sparse_brick_hits", "primary_scene_queries", "bounce_scene_queries",
+                         "shadow_scene_queries")
+
+    def sdf_traversal_stats(self) -> dict:
+        st = self.stats()
+        d = {k: int(st.sdf_counters[i]) for i, k in enumerate(self.SDF_COUNTER_NAMES)}
+        # derived as RenderSession.swift:819 does: cells visited without a brick test
+        d["sparse_grid_empty_cells"] = d["sparse_grid_cells_visited"] - min(d["sparse_grid_cells_visited"],
+                                                                            d["sparse_brick_tests"])
+        return d
+
+    def reset_sdf_traversal_stats(self) -> None:
+        library.check(self._lib.dk_session_reset_sdf_stats(self._handle))
+
     # RenderSession.pixels(for:) (RenderSession.swift:1037-1039): (H, W, 4) float32
     def pixels(self, output: RenderOutput = RenderOutput.BEAUTY, out: Optional[np.ndarray] = None) -> np.ndarray:
         w, h = self.settings.width, self.settings.height

@@ -327,8 +327,12 @@ int dk_write_png(const char* path, const uint8_t* rgba, uint32_t width, uint32_t
 /* RenderSession.sampleCount. */
 int dk_session_sample_count(const dk_session* session, uint32_t* out_count);
 
-/* RenderSession.sdfTraversalStats() (RenderSession.swift:808-831) plus timing. */
+/* RenderSession.sdfTraversalStats() (RenderSession.swift:808-831) plus timing.
+ * `sdf_counters` holds the reference's 13 counter slots (PathTrace.metal:191-203)
+ * when the session was created with `collects_traversal_stats`, else zeros. */
 int dk_session_stats(const dk_session* session, dk_stats* out_stats);
+/* RenderSession.resetSDFTraversalStats(): zeroes the SDF traversal counters. */
+int dk_session_reset_sdf_stats(dk_session* session);
 
 /* Releases every device buffer of the session. */
 int dk_session_destroy(dk_session* session);
