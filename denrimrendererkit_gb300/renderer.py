@@ -266,7 +266,7 @@ class RenderSession:
         library.check(self._lib.dk_session_stats(self._handle, C.byref(st)))
         return st
 
-    # RenderSession.sdfTraversalStats() / resetSDFTraversalStats() (RenderSession.swift:808-840):
+    # RenderSession.sdfTraversalStats() / resetSDFTraversalStats() (RenderSession.swift:808-831, :611-614):
     # the SDF traversal counters of a session made with `collects_traversal_stats`, by the
     # reference's names (all zero otherwise).
     SDF_COUNTER_NAMES = ("dense_volume_tests", "dense_march_steps", "sparse_grid_cells_visited",

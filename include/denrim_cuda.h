@@ -331,7 +331,7 @@ int dk_session_sample_count(const dk_session* session, uint32_t* out_count);
  * `sdf_counters` holds the reference's 13 counter slots (PathTrace.metal:191-203)
  * when the session was created with `collects_traversal_stats`, else zeros. */
 int dk_session_stats(const dk_session* session, dk_stats* out_stats);
-/* RenderSession.resetSDFTraversalStats(): zeroes the SDF traversal counters. */
+/* RenderSession.resetSDFTraversalStats() (RenderSession.swift:611-614): zeroes the SDF traversal counters. */
 int dk_session_reset_sdf_stats(dk_session* session);
 
 /* Releases every device buffer of the session. */
