@@ -176,8 +176,24 @@ __device__ __forceinline__ Hit makeHitAny(const DevScene& S, const Ray& ray, con
 }
 
 // intersectScene (:3294-3421): triangles, then the sparse volumes with the
-// triangle distance as the bound.
+// triangle distance as the bound.  traceSceneCounting also counts the volume
+// walk's events into the session's SDF traversal counters when it has them;
+// the subsurface walk inside the shading kernel takes the plain form, which
+// keeps that kernel's registers (its walk steps still count as scene queries).
 __device__ __noinline__ HitRec traceScene(const DevScene& S, float3 o, float3 d) {
+    HitRec r = S.wide8 ? traceClosest8(S, o, d) : traceClosest(S, o, d);
+    if (S.volume_count) {
+        VolumeHitRec vh;
+        if (closestVolumeHit(volumeScene(S), o, d, r.t, vh)) {
+            r.t = vh.t;
+            r.tri = kVolumeHit;
+            r.u = __uint_as_float(vh.brick);
+            r.v = 0.0f;
+        }
+    }
+    return r;
+}
+__device__ __noinline__ HitRec traceSceneCounting(const DevScene& S, float3 o, float3 d) {
     HitRec r = S.wide8 ? traceClosest8(S, o, d) : traceClosest(S, o, d);
     if (S.volume_count) {
         VolumeHitRec vh;
@@ -1070,7 +1086,7 @@ __device__ bool shadowWalk(const DevScene& S, MatTable mt, float3 o, float3 d, f
     float traveled = 0.0f;
     for (uint32_t step = 0; step < 8u; ++step) {
         sdfCount(S.sdf_counters, kSdfShadowSceneQueries);
-        HitRec r = traceScene(S, o, d);
+        HitRec r = traceSceneCounting(S, o, d);
         if (r.tri == kNoHit || traveled + r.t >= maxDistance) return false;
         Ray ray{o, d};
         Hit h = makeHitAny(S, ray, r);
@@ -1271,7 +1287,7 @@ __global__ void __launch_bounds__(128) k_aov_primary(DevScene S, Wave W) {
         writeAovMiss(W.aov, i, W.aov_stride);
         for (uint32_t pass = 0; pass < 32u; ++pass) {
             sdfCount(S.sdf_counters, kSdfPrimarySceneQueries);
-            HitRec r = traceScene(S, ray.origin, ray.direction);
+            HitRec r = traceSceneCounting(S, ray.origin, ray.direction);
             if (r.tri == kNoHit) break;
             Hit h = makeHitAny(S, ray, r);
             Material m = materialForHit(S, mt, h);
@@ -1383,7 +1399,7 @@ __device__ float interactiveContactAO(const DevScene& S, MatTable mt, const Hit&
         float3 dir = normalize(l.x * frame.tangent + l.y * frame.bitangent + l.z * n);
         Ray ray{h.position + n * 0.003f, dir};
         sdfCount(S.sdf_counters, kSdfShadowSceneQueries);
-        HitRec r = traceScene(S, ray.origin, ray.direction);
+        HitRec r = traceSceneCounting(S, ray.origin, ray.direction);
         if (r.tri == kNoHit || !(r.t < kRadius)) continue;
         Hit oh = makeHitAny(S, ray, r);
         Material om = materialForHit(S, mt, oh);
@@ -1403,7 +1419,7 @@ __global__ void __launch_bounds__(128) k_preview(DevScene S, DevParams P, Accum 
         const size_t pix = (size_t)py * P.width + px;
         Ray ray = makeCameraRay(P.cam, P.width, P.height, px, py, 0.5f, 0.5f, 0.0f, 0.0f);
         sdfCount(S.sdf_counters, kSdfPrimarySceneQueries);
-        HitRec rec = traceScene(S, ray.origin, ray.direction);
+        HitRec rec = traceSceneCounting(S, ray.origin, ray.direction);
         float4 beauty;
         if (rec.tri == kNoHit) {
             float alpha = P.transparent_background ? 0.0f : 1.0f;
