@@ -646,14 +646,22 @@ def estimate_errors(half_a, half_b, full, den_a, den_b, den_full, stream=None, d
     terms = torch.empty(n, 5, dtype=torch.float64, device=t[0].device)
     library.check(lib.dk_denoise_error_terms(*(_ptr(x) for x in t), h * w, n, 1 if display else 0, _ptr(terms),
                                              None if stream is None else C.c_void_p(stream)))
+    return estimates_from_terms(terms.cpu().numpy().tolist(), h * w, samples)
+
+
+def estimates_from_terms(terms, pixels: int, samples=None) -> List[ErrorEstimate]:
+    """The estimates of `estimate_errors` from its per-image sums over the
+    RGB channels of `pixels` pixels: (sum |dA - dB|^2, sum |A - B|^2,
+    sum |F - dF|^2, sum dF, sum F) per image."""
     out = []
-    m = 3.0 * h * w
+    m = 3.0 * pixels
+    n = len(terms)
     if samples is None:
         weights = [0.25] * n
     else:
         pairs = [samples] * n if isinstance(samples[0], (int, float)) else list(samples)
         weights = [na * nb / float(na + nb) ** 2 for na, nb in pairs]
-    for (dd, nn, fd, sd, sf), wgt in zip(terms.cpu().numpy().tolist(), weights):
+    for (dd, nn, fd, sd, sf), wgt in zip(terms, weights):
         var_dn = dd * wgt / m
         var_f = nn * wgt / m
         g = min(1.0, math.sqrt(dd / nn)) if nn > 0.0 else 0.0
