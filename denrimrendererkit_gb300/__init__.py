@@ -7,11 +7,11 @@ reference's Swift API (scene description, scene compile, render session).
 from .library import DenrimError, device_count, load  # noqa: F401
 from .renderer import DenrimRenderer, RenderOutput, RenderQuality, RenderSession, RenderSettings  # noqa: F401
 from .scene import (AccelerationBuild, Camera, Environment, Material, Mesh, QuadLight, RenderScene,  # noqa: F401
-                    Texture2D, Transform, compile_scene, icosphere)
+                    SceneBounds, Texture2D, Transform, compile_scene, icosphere)
 
 __all__ = [
     "DenrimError", "DenrimRenderer", "RenderOutput", "RenderQuality", "RenderSession", "RenderSettings",
-    "AccelerationBuild", "Camera", "Environment", "Material", "Mesh", "QuadLight", "RenderScene", "Texture2D",
-    "Transform",
+    "AccelerationBuild", "Camera", "Environment", "Material", "Mesh", "QuadLight", "RenderScene", "SceneBounds",
+    "Texture2D", "Transform",
     "compile_scene", "icosphere", "device_count", "load",
 ]

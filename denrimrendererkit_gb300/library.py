@@ -221,6 +221,7 @@ class SparseVolume:
         st.resolution[:] = list(resolution)
         st.bounds_min[:] = list(bounds_min)
         st.bounds_max[:] = list(bounds_max)
+        self.bounds_min, self.bounds_max = tuple(bounds_min), tuple(bounds_max)  # world space
         st.brick_size[:] = list(brick_size)
         st.narrow_band = narrow_band
         st.volume_material = volume_material

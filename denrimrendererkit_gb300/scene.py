@@ -319,6 +319,60 @@ class Environment:
     max_radiance: float = 16.0
 
 
+# ------------------------------------------------------------------ bounds ---
+@dataclasses.dataclass
+class SceneBounds:
+    """SceneBounds (Scene/SceneBounds.swift:5-111): an axis-aligned box, empty
+    while any minimum exceeds its maximum."""
+    minimum: tuple = (math.inf, math.inf, math.inf)
+    maximum: tuple = (-math.inf, -math.inf, -math.inf)
+
+    @staticmethod
+    def of(a, b) -> "SceneBounds":
+        """SceneBounds(minimum:maximum:): the box of two corners in any order."""
+        return SceneBounds(tuple(min(float(x), float(y)) for x, y in zip(a, b)),
+                           tuple(max(float(x), float(y)) for x, y in zip(a, b)))
+
+    def is_empty(self) -> bool:
+        return any(lo > hi for lo, hi in zip(self.minimum, self.maximum))
+
+    def center(self) -> tuple:
+        if self.is_empty():
+            return (0.0, 0.0, 0.0)
+        return tuple((lo + hi) * 0.5 for lo, hi in zip(self.minimum, self.maximum))
+
+    def extent(self) -> tuple:
+        if self.is_empty():
+            return (0.0, 0.0, 0.0)
+        return tuple(hi - lo for lo, hi in zip(self.minimum, self.maximum))
+
+    def corners(self) -> list:
+        """The eight corners, x fastest (SceneBounds.swift:69-83)."""
+        if self.is_empty():
+            return []
+        (x0, y0, z0), (x1, y1, z1) = self.minimum, self.maximum
+        return [(x, y, z) for z in (z0, z1) for y in (y0, y1) for x in (x0, x1)]
+
+    def including(self, other) -> "SceneBounds":
+        """include(_:) for a point (3 numbers) or a non-empty SceneBounds."""
+        if isinstance(other, SceneBounds):
+            if other.is_empty():
+                return self
+            return self.including(other.minimum).including(other.maximum)
+        return SceneBounds(tuple(min(lo, float(v)) for lo, v in zip(self.minimum, other)),
+                           tuple(max(hi, float(v)) for hi, v in zip(self.maximum, other)))
+
+    def transformed(self, transform: "Transform") -> "SceneBounds":
+        """transformed(by:) (SceneBounds.swift:100-110): the box of the transformed corners."""
+        if self.is_empty():
+            return SceneBounds()
+        pts = transform.transform_points(np.asarray(self.corners(), f32))
+        out = SceneBounds()
+        for p in pts:
+            out = out.including(tuple(float(v) for v in p))
+        return out
+
+
 # ------------------------------------------------------------------ camera ---
 @dataclasses.dataclass
 class Camera:
@@ -385,6 +439,65 @@ class Camera:
         distance = max(float(_dot3(rel, self.view_direction())), 0.0001)
         return dataclasses.replace(self, focus_distance=distance, aperture_radius=max(float(aperture_radius), 0.0))
 
+    @staticmethod
+    def framing(bounds: SceneBounds, aspect_ratio: float, view_direction=(0.0, -0.25, -1.0), up=(0.0, 1.0, 0.0),
+                padding: float = 1.15, center_offset=(0.0, 0.0), target_offset=(0.0, 0.0, 0.0),
+                orthographic: bool = False, vertical_field_of_view_degrees: float = 45.0,
+                aperture_radius: float = 0.0) -> "Camera":
+        """Camera.framing (Camera.swift:103-165): a camera looking along
+        `view_direction` that fits the padded corners of `bounds`, perspective
+        (the field of view clamped to 1-175 degrees) or orthographic (vertical
+        scale from the fitted extents).  `center_offset` moves the bounds'
+        centre on the image in fitted-frame units (+x right, +y up)."""
+        def basis(view, upv):
+            v = tuple(float(c) for c in view)
+            fwd = _normalize3(v) if _dot3(v, v) > 1e-8 else (0.0, 0.0, -1.0)
+            u = tuple(float(c) for c in upv)
+            u = _normalize3(u) if _dot3(u, u) > 1e-8 else (0.0, 1.0, 0.0)
+            helper = u if abs(_dot3(fwd, u)) < 0.999 else (1.0, 0.0, 0.0)
+            right = _normalize3(_cross3(fwd, helper))
+            return fwd, right, _cross3(right, fwd)
+
+        def extents(corners, center, b):
+            fwd, right, tup = b
+            hw = hh = 0.0
+            zs = []
+            for c in corners:
+                rel = tuple(c[i] - center[i] for i in range(3))
+                hw = max(hw, abs(_dot3(rel, right)))
+                hh = max(hh, abs(_dot3(rel, tup)))
+                zs.append(_dot3(rel, fwd))
+            return max(hw, 0.0001), max(hh, 0.0001), max(max(zs) - min(zs), 0.0001)
+
+        fwd, right, tup = b = basis(view_direction, up)
+        bc = bounds.center()
+        center = tuple(bc[i] + float(target_offset[i]) for i in range(3))
+        pad = max(float(padding), 0.0001)
+        corners = [tuple(center[i] + (c[i] - bc[i]) * pad for i in range(3)) for c in bounds.corners()]
+        aspect = max(float(aspect_ratio), 0.0001)
+        hw, hh, _ = extents(corners, center, b)
+        shift = tuple(right[i] * (hw * float(center_offset[0])) + tup[i] * (hh * float(center_offset[1]))
+                      for i in range(3))
+        target = tuple(center[i] - shift[i] for i in range(3))
+        if not orthographic:
+            fov = min(max(float(vertical_field_of_view_degrees), 1.0), 175.0)
+            tan_y = math.tan(fov * math.pi / 360.0)
+            tan_x = tan_y * aspect
+            distance = 0.0001
+            for c in corners:
+                rel = tuple(c[i] - target[i] for i in range(3))
+                x, y, z = _dot3(rel, right), _dot3(rel, tup), _dot3(rel, fwd)
+                distance = max(distance, abs(x) / max(tan_x, 0.0001) - z, abs(y) / max(tan_y, 0.0001) - z)
+            origin = tuple(target[i] - fwd[i] * distance for i in range(3))
+            return Camera(origin, target, up=tup, vertical_field_of_view_degrees=fov, focus_distance=distance,
+                          aperture_radius=max(float(aperture_radius), 0.0))
+        thw, thh, depth = extents(corners, target, b)
+        scale = max(thh, thw / aspect) * 2.0
+        distance = max(depth * 0.5 + max(thw, thh), 0.0001)
+        origin = tuple(target[i] - fwd[i] * distance for i in range(3))
+        return Camera(origin, target, up=tup, orthographic_scale=max(scale, 0.0001), focus_distance=distance,
+                      aperture_radius=max(float(aperture_radius), 0.0))
+
 
 # ------------------------------------------------------------ render scene ---
 @dataclasses.dataclass
@@ -414,6 +527,23 @@ class RenderScene:
 
     def add(self, mesh: Mesh, material: int, transform: Optional[Transform] = None) -> None:
         self.mesh_instances.append(MeshInstance(mesh, material, transform or Transform.identity()))
+
+    def world_bounds(self) -> Optional[SceneBounds]:
+        """RenderScene.worldBounds (SceneBounds.swift:136-170): the mesh
+        instances' transformed vertex bounds and the sparse volumes' bounds;
+        None for an empty scene."""
+        out = SceneBounds()
+        for inst in self.mesh_instances:
+            v = np.asarray(inst.mesh.vertices, f32)
+            if len(v) == 0:
+                continue
+            local = SceneBounds.of(v.min(axis=0), v.max(axis=0))
+            out = out.including(local.transformed(inst.transform))
+        for vol in self.sparse_volumes:
+            lo, hi = getattr(vol, "bounds_min", None), getattr(vol, "bounds_max", None)
+            if lo is not None and hi is not None:
+                out = out.including(SceneBounds.of(lo, hi))
+        return None if out.is_empty() else out
 
     def add_quad_light(self, light: "QuadLight") -> int:
         """RenderScene.addQuadLight (RenderScene.swift:307-321): the light's

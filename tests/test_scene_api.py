@@ -60,3 +60,34 @@ def test_settings_override_or_disable_the_sample_radiance_clamp():
     assert RenderSettings(quality=RenderQuality.FINAL).resolved_sample_radiance_clamp == 64
     assert RenderSettings(sample_radiance_clamp=0).resolved_sample_radiance_clamp == 0
     assert RenderSettings(sample_radiance_clamp=18).resolved_sample_radiance_clamp == 18
+
+
+def test_scene_world_bounds_include_transformed_meshes():
+    # APITests.testSceneWorldBoundsIncludeTransformedMeshesAndVolumes (a box at +2; the reference's second
+    # object, a dense volume, is a box of the same extent at -2 here: dense volumes are not part of this path)
+    from denrimrendererkit_gb300 import Mesh, Transform
+    scene = RenderScene()
+    m = scene.add_material(Material(base_color=(0.8, 0.8, 0.8)))
+    assert scene.world_bounds() is None
+    scene.add(Mesh.box(size=(2, 2, 2)), m, Transform.translation((2, 0, 0)))
+    scene.add(Mesh.box(size=(1, 1, 1)), m, Transform.translation((-2.5, 0, 0)))
+    b = scene.world_bounds()
+    assert np.allclose(b.minimum, (-3, -1, -1), atol=1e-4) and np.allclose(b.maximum, (3, 1, 1), atol=1e-4)
+
+
+def test_camera_frames_perspective_bounds_with_offset():
+    # APITests.testCameraFramesPerspectiveBoundsWithOffset
+    from denrimrendererkit_gb300.scene import Camera, SceneBounds
+    cam = Camera.framing(SceneBounds.of((-1, -1, -1), (1, 1, 1)), aspect_ratio=1, view_direction=(0, 0, -1),
+                         padding=1, center_offset=(0.5, 0), vertical_field_of_view_degrees=90)
+    assert abs(cam.origin[0] + 0.5) < 1e-4 and abs(cam.origin[2] - 2.5) < 1e-4
+    assert abs(cam.target[0] + 0.5) < 1e-4 and abs(cam.focus_distance - 2.5) < 1e-4
+
+
+def test_camera_frames_orthographic_bounds():
+    # APITests.testCameraFramesOrthographicBounds
+    from denrimrendererkit_gb300.scene import Camera, SceneBounds
+    cam = Camera.framing(SceneBounds.of((-1, -1, -1), (1, 1, 1)), aspect_ratio=1, view_direction=(0, 0, -1),
+                         padding=1, orthographic=True)
+    assert cam.orthographic_scale is not None and abs(cam.orthographic_scale - 2) < 1e-4
+    assert abs(cam.origin[2] - 2) < 1e-4 and abs(cam.target[2]) < 1e-4
