@@ -556,7 +556,10 @@ def sdf_measure(args, flush, steps=3, warmup=2):
                              if k in ("grid_cells", "macro_skips", "brick_tests", "brick_marches", "march_steps",
                                       "brick_hits", "brick_samples")},
                 "units": "16 B per brick sample read, 4 B per grid or macro cell, 128 B per brick descriptor "
-                         "(the reference's layouts), counted by the oracle on every 16th pixel in x and y, scaled"}
+                         "(the reference's layouts), counted by the oracle on every 16th pixel in x and y, scaled",
+                "note": "a lower bound of the memory side only: the 92 MB of FP16 samples stay in L2 and the pass "
+                        "is bound by instruction issue and dependent-load latency (ncu, small case: 0.49 TB/s "
+                        "of L2, 41 % issue-active at bounce 0; profiles/k_extend_volume_sdf_spheres.md)"}
     return {"workload": "sdf-spheres 768^3, 8^3 bricks (26.8 K kept, 3 %), 1024x1024 x 16 spp, 8 bounces",
             "value": out["fp16"]["mpaths_s"], "unit": METRIC, "fp16": out["fp16"], "fp32": out["fp32"],
             "fp16_vs_fp32": out["fp16_vs_fp32"], "roofline": roof,
